@@ -1,0 +1,334 @@
+"""Benchmark of the GB300 mLW step: zone-updates/s on the 2-D Orszag-Tang
+vortex, 512 x 512 cells, 2.5-D MHD (mlw_m3, 9 FP64 arrays), periodic box.
+
+One benchmark step = `--mlw-steps` (default 100) iterations of the reference
+time loop (cfl -> t += dt -> mlw_m3 -> bnd) kept on the device and replayed
+as a CUDA graph.  L2 is flushed (256 MiB write) between benchmark steps; the
+state itself (2 x 19 MB) fits in L2 and stays there across the iterations of
+one step, as it does in a production run of this size.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU restatement of the reference Fortran (the
+oracle, with every host thread) on the same workload.  Under torchrun every
+rank runs an independent replica ("replicas only": the mLW path has no
+exchange on one GPU per run); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "mLW MHD zone-updates/s"
+UNIT = "zone-updates/s"
+N_CELLS = 512
+B_PER_ZONE = 144  # mlw_m3: 9 arrays read once and written once, 8 B each
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--mlw-steps", type=int, default=100)
+    p.add_argument("--n", type=int, default=N_CELLS)
+    p.add_argument("--exact", action="store_true", help="exact arithmetic policy")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("CANS_BENCH_GLOO") is None else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            lines = Path(self.f.name).read_text().strip().splitlines()
+        except OSError:
+            lines = []
+        rows = [[c.strip() for c in ln.split(",")] for ln in lines if ln.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[5 + k].lower().startswith("active")})
+        loaded = [v for v in sm if smax and v >= 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_summary():
+    """Per-launch DRAM bytes and FP64 operation counts of the step kernel from
+    the committed ncu summary (profiles/), if present."""
+    out = {}
+    p = ROOT / "profiles" / "ncu_mlw2d_step_ot512.txt"
+    if p.exists():
+        for ln in p.read_text().splitlines():
+            if ":" in ln and ln.split(":", 1)[0].strip() in (
+                    "dram_bytes_per_launch", "fp64_flops_per_zone"):
+                k, v = ln.split(":", 1)
+                try:
+                    out[k.strip()] = float(v.split()[0])
+                except (ValueError, IndexError):
+                    pass
+    return out
+
+
+def cpu_baseline(n, seconds_target=15.0):
+    """The oracle (C restatement of the reference) on the host cores."""
+    import oracle
+    from utrip_gb300 import setups
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    s = setups.orszag_tang(n)
+    st = setups.copy_state(s)
+    oracle.run_2d(s, st, 1)  # warm the arena
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds_target or steps < 2:
+        oracle.run_2d(s, st, 1)
+        steps += 1
+    el = time.perf_counter() - t0
+    zones = n * n * steps
+    return {"value": zones / el, "unit": UNIT, "cores": oracle.get_threads(), "kind": "port",
+            "sample": f"{steps} loop iterations (cfl_m3+mlw_m3+bnd) of Orszag-Tang {n}x{n} "
+                      f"in {el:.1f} s"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import oracle
+    from utrip_gb300 import setups
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    n = args.n
+    s = setups.orszag_tang(n)
+    st = setups.copy_state(s)
+    t0 = time.perf_counter()
+    oracle.run_2d(s, st, 1)
+    per_iter = time.perf_counter() - t0
+    iters = max(1, int(3.0 / max(per_iter, 1e-6)))  # about 3 s per benchmark step
+    for _ in range(args.warmup):
+        oracle.run_2d(s, st, iters)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.run_2d(s, st, iters)
+    el = time.perf_counter() - t0
+    value = n * n * iters * args.steps / el
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"orszag_tang_{n}x{n}_mlw_m3", "solver": "mlw_m3",
+                       "mlw_steps_per_bench_step": iters, "parallelism": "openmp"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.get_threads(),
+                             "kind": "port",
+                             "sample": f"{args.steps} x {iters} loop iterations of "
+                                       f"Orszag-Tang {n}x{n}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    from utrip_gb300 import capi, drivers, setups
+    torch.cuda.set_device(local)
+    capi.load()
+    if not capi.device_ok():
+        raise SystemExit("no usable sm_103 device")
+    n = args.n
+    s = setups.orszag_tang(n)
+    stream = torch.cuda.current_stream()
+    run = drivers.make_run(s, exact=args.exact, stream=stream.cuda_stream)
+    run.push(setups.copy_state(s))
+    tile = run.autotune(5)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    m = args.mlw_steps
+    total_iters = (args.warmup + args.steps) * m
+    run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        run.advance(m)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    c0 = capi.launch_count()
+    with Clocks(local) as clk:
+        w0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(1.0)
+            ev[k][0].record(stream)
+            run.advance(m)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    barrier(ws)
+    launches = capi.launch_count() - c0
+    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+    st = run.query()
+    assert st.nexec == total_iters and st.merr == 0, (st.nexec, total_iters, st.merr)
+    dev_ms = max_over_ranks(dev_ms, ws)
+    zones = n * n * m * args.steps
+    value = zones * ws / (dev_ms * 1e-3)
+
+    # dominant kernel: the fused step, timed alone inside un-graphed iterations
+    prof_iters = 200
+    step_ms, iter_ms = run.profile(prof_iters)
+    step_avg = step_ms / prof_iters
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = B_PER_ZONE * n * n / (step_avg * 1e-3) / 1e9
+    ncu = ncu_summary()
+    traffic = ncu.get("dram_bytes_per_launch")
+    fp64_peak = capi.measure_fp64_tflops()
+    flops_zone = ncu.get("fp64_flops_per_zone")
+    fp64 = None
+    if flops_zone:
+        ach = flops_zone * n * n / (step_avg * 1e-3) / 1e12
+        fp64 = {"achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "flops_per_zone": flops_zone, "peak_kind": "measured live (FP64 FMA chains)"}
+
+    # end to end through the public API with pinned host buffers
+    host = [torch.empty((n + 2, n + 2), dtype=torch.float64, pin_memory=True).numpy().T
+            for _ in range(run.nvar)]
+    for h, a in zip(host, s["state"]):
+        h[...] = a
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        run.push(host)
+        run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+        run.advance(m)
+        run.pull(host)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), ws)
+    e2e_val = n * n * m * e2e_steps * ws / (e2e_ms * 1e-3)
+    nbytes = run.nvar * (n + 2) * (n + 2) * 8
+    run.close()
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"orszag_tang_{n}x{n}_mlw_m3", "solver": "mlw_m3",
+                   "grid": [n + 2, n + 2], "mlw_steps_per_bench_step": m,
+                   "policy": "exact" if args.exact else "fast", "tile": tile,
+                   "l2": "flushed between benchmark steps (256 MiB write)",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "peak_kind": peak_kind, "bytes_per_zone": B_PER_ZONE,
+                     "step_kernel_ms": step_avg, "iteration_ms": iter_ms / prof_iters},
+        "roofline_fp64": fp64,
+        "fp64_peak_tflops_measured": fp64_peak,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": int(launches),
+        "wall_s": wall,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(n)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

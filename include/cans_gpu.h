@@ -1,0 +1,215 @@
+/*
+ * cans_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the CANS
+ * ideal-MHD modified Lax-Wendroff step.
+ *
+ * Three layers, all plain C (pointers and sizes only):
+ *
+ *  1. Drop-in entry points with the argument lists of the reference Fortran
+ *     routines.  Every argument is passed by reference, as a Fortran-77 caller
+ *     passes it, so a bind(C) interface maps each call one to one.  The same
+ *     routine name exists in the reference's 1-D, 2-D and 3-D libraries with
+ *     different arguments (libcans1d.a / libcans2d.a / libcans3d.a), so each C
+ *     symbol carries a _1d/_2d/_3d suffix.  Arrays are column-major with their
+ *     ghost cells, exactly as the caller holds them.
+ *       - If the arrays were registered with cans_gpu_register(), the call
+ *         works on their device-resident mirrors and moves no field data
+ *         (cfl_m returns only dt and merr to the host).
+ *       - Otherwise the call copies its arrays to the device, runs there and
+ *         copies the results back before returning.
+ *     There is no CPU fallback: without a usable GPU every call returns
+ *     CANS_ERR_CUDA.
+ *
+ *  2. Residency registry (cans_gpu_register / pull / push / release), the
+ *     only calls a reference driver adds: register the state after the model
+ *     set-up and pull it before each output write.
+ *
+ *  3. A device-resident run handle (cans_run_*) that keeps the whole
+ *     reference time loop -- cfl, step, boundary fill, t += dt, the
+ *     tend/nstop/dtmin tests -- on the GPU, replayed as a CUDA graph.
+ *
+ * Status codes: every entry point returns 0 on success or one of CANS_ERR_*.
+ * Where the reference sets merr, the entry point sets it too.
+ */
+#ifndef CANS_GPU_H
+#define CANS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CANS_OK 0
+#define CANS_ERR_DTMIN 9001    /* dt < dtmin, as the reference merr=9001 */
+#define CANS_ERR_NONFINITE 9100
+#define CANS_ERR_CUDA 9200     /* CUDA failure; see cans_last_error()     */
+#define CANS_ERR_TIMEOUT 9300  /* a bounded device wait gave up           */
+#define CANS_ERR_ARG 9400      /* invalid argument                        */
+
+/* ------------------------------------------------------------------------ */
+/* Library settings                                                          */
+/* ------------------------------------------------------------------------ */
+/* Arithmetic policy of the drop-in entry points: 0 = fast (FMA contraction,
+ * one reciprocal per cell), 1 = exact (reference operation order, no
+ * contraction; bit-identical to the reference arithmetic).  The initial value
+ * comes from the environment variable CANS_GPU_EXACT (default 0). */
+int cans_set_exact(int exact);
+int cans_get_exact(void);
+/* CUDA stream (cudaStream_t) used by the drop-in entry points; NULL selects
+ * the library's own stream. */
+int cans_set_stream(void *stream);
+/* Text of the last CUDA error seen by the library (thread-compatible). */
+const char *cans_last_error(void);
+/* Number of kernel launches issued by this library so far (graph replays
+ * count every kernel node). */
+unsigned long long cans_launch_count(void);
+/* 1 if a CUDA device of compute capability 10.3 is usable, else 0. */
+int cans_device_ok(void);
+
+/* ------------------------------------------------------------------------ */
+/* 1. Drop-in entry points: 2-D                                              */
+/* ------------------------------------------------------------------------ */
+/* replaces subroutine mlw_m3  (cans2d/hdmlw/mlw_m3.f:2-3) */
+int cans_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                   double *bx, double *by, double *bz, double *az,
+                   const double *dt, const double *qav, const double *gm,
+                   const double *dx, const double *dxm, const int *ix,
+                   const double *dy, const double *dym, const int *jx);
+/* replaces subroutine mlw_m   (cans2d/hdmlw/mlw_m.f:2-3) */
+int cans_mlw_m_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
+                  double *by, double *az, const double *dt, const double *qav,
+                  const double *gm, const double *dx, const double *dxm,
+                  const int *ix, const double *dy, const double *dym,
+                  const int *jx);
+/* replaces subroutine cfl_m3  (cans2d/common/cfl_m3.f:2-3) */
+int cans_cfl_m3_2d(double *dt, const double *safety, const double *dtmin,
+                   int *merr, const double *gm, const double *ro,
+                   const double *pr, const double *vx, const double *vy,
+                   const double *vz, const double *bx, const double *by,
+                   const double *bz, const double *dx, const int *ix,
+                   const double *dy, const int *jx);
+/* replaces subroutine cfl_m   (cans2d/common/cfl_m.f:2-3) */
+int cans_cfl_m_2d(double *dt, const double *safety, const double *dtmin,
+                  int *merr, const double *gm, const double *ro,
+                  const double *pr, const double *vx, const double *vy,
+                  const double *bx, const double *by, const double *dx,
+                  const int *ix, const double *dy, const int *jx);
+
+/* Ghost-cell fill, 2-D (cans2d/bc/bd*.f:2).  bdper* take (margin0, margin1);
+ * the others take (mbnd, margin) with mbnd 0 = lower face, 1 = upper face. */
+int cans_bdperx_2d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx); /* bdperx.f:2 */
+int cans_bdpery_2d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx); /* bdpery.f:2 */
+int cans_bdsppx_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdsppx.f:2 */
+int cans_bdsppy_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdsppy.f:2 */
+int cans_bdspnx_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdspnx.f:2 */
+int cans_bdspny_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdspny.f:2 */
+int cans_bdsmpx_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdsmpx.f:2 */
+int cans_bdsmpy_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdsmpy.f:2 */
+int cans_bdsmnx_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdsmnx.f:2 */
+int cans_bdsmny_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdsmny.f:2 */
+int cans_bdfrex_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdfrex.f:2 */
+int cans_bdfrey_2d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx);    /* bdfrey.f:2 */
+int cans_bdcnsx_2d(const int *mbnd, const int *margin, double *qq, const double *q0, const int *ix, const int *jx); /* bdcnsx.f:2 */
+int cans_bdcnsy_2d(const int *mbnd, const int *margin, double *qq, const double *q0, const int *ix, const int *jx); /* bdcnsy.f:2 */
+int cans_bdfrdx_2d(const int *mbnd, const int *margin, double *qq, const double *dxm, const int *ix, const int *jx); /* bdfrdx.f:2 */
+int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq, const double *dym, const int *ix, const int *jx); /* bdfrdy.f:2 */
+
+/* ------------------------------------------------------------------------ */
+/* 2. Residency registry                                                     */
+/* ------------------------------------------------------------------------ */
+/* Register `narr` host arrays of ix*jx*kx doubles each (jx = kx = 1 for
+ * fewer dimensions) as one device-resident set and copy them to the device.
+ * Later drop-in calls that pass these host pointers run on the mirrors.  A
+ * step call must pass the arrays of one set in the set's order, which must
+ * be the step's argument order (e.g. ro,pr,vx,vy,vz,bx,by,bz,az for mlw_m3). */
+int cans_gpu_register(double *const *arrays, const int *narr, const int *ix,
+                      const int *jx, const int *kx);
+/* Copy the whole set containing `any` between device and host. */
+int cans_gpu_pull(const double *any);
+int cans_gpu_push(const double *any);
+/* Forget the set containing `any` and free its device memory. */
+int cans_gpu_release(const double *any);
+
+/* ------------------------------------------------------------------------ */
+/* 3. Device-resident run handle                                             */
+/* ------------------------------------------------------------------------ */
+#define CANS_SOLVER_MLW_M_2D 0   /* mlw_m  2-D: ro,pr,vx,vy,bx,by,az         */
+#define CANS_SOLVER_MLW_M3_2D 1  /* mlw_m3 2-D: ro,pr,vx,vy,vz,bx,by,bz,az   */
+
+/* Boundary kinds, one per reference bd* family. */
+#define CANS_BD_NONE (-1)
+#define CANS_BD_PER 0  /* bdper*  periodic                               */
+#define CANS_BD_SPP 1  /* bdspp*  symmetric about the face, even         */
+#define CANS_BD_SPN 2  /* bdspn*  symmetric about the face, odd          */
+#define CANS_BD_SMP 3  /* bdsmp*  symmetric about the boundary cell, even */
+#define CANS_BD_SMN 4  /* bdsmn*  ... odd, boundary cell set to zero      */
+#define CANS_BD_FRE 5  /* bdfre*  zero gradient                          */
+#define CANS_BD_CNS 6  /* bdcns*  constant value q0                      */
+#define CANS_BD_FRD 7  /* bdfrd*  constant gradient                      */
+
+typedef struct cans_run cans_run;
+
+typedef struct {
+  int solver;                 /* CANS_SOLVER_*                              */
+  int ix, jx, kx;             /* extents including ghost cells (kx=1 in 2-D) */
+  int margin;                 /* ghost layers filled by the boundary program */
+  double gm, qav;             /* gamma and the artificial-viscosity factor  */
+  const double *dx, *dxm;     /* host metric arrays (grdrdy output)         */
+  const double *dy, *dym;
+  const double *dz, *dzm;
+  int exact;                  /* 1 = exact arithmetic policy                */
+  int tile;                   /* tile configuration, -1 = library default   */
+  void *stream;               /* cudaStream_t or NULL (library stream)      */
+} cans_run_desc;
+
+typedef struct {
+  double t, dt;               /* time after the last step; its dt           */
+  long long ns;               /* loop counter of the reference driver       */
+  long long nexec;            /* steps executed since cans_run_start        */
+  int merr;                   /* 0 or 9001                                  */
+  int done;                   /* 1 when tend/nstop/merr ended the loop      */
+  int pause;                  /* 1 when an output time was crossed          */
+} cans_run_state;
+
+int cans_run_create(cans_run **h, const cans_run_desc *d);
+int cans_run_destroy(cans_run *h);
+/* Boundary program entry: variable index in solver order, face 0..5
+ * (x-lo, x-hi, y-lo, y-hi, z-lo, z-hi), CANS_BD_* kind and constant q0. */
+int cans_run_set_bc(cans_run *h, int var, int face, int kind, double q0);
+/* Copy the state between host arrays (solver order) and the device. */
+int cans_run_push(cans_run *h, double *const *host);
+int cans_run_pull(cans_run *h, double *const *host);
+/* Start the reference loop: t=t0, ns=0, first CFL and t+=dt on the device.
+ * pause_on_output=1 stops the loop whenever int(tp/dtout) < int(t/dtout). */
+int cans_run_start(cans_run *h, double t0, double tend, long long nstop,
+                   double safety, double dtmin, double dtout,
+                   int pause_on_output);
+/* Enqueue up to `iters` further loop iterations (asynchronous). */
+int cans_run_advance(cans_run *h, int iters);
+/* Wait for the stream and read the loop state. */
+int cans_run_query(cans_run *h, cans_run_state *st);
+/* Clear a pause after the host has read the output state. */
+int cans_run_resume(cans_run *h);
+/* One step with a given dt, optionally followed by the boundary program
+ * (no CFL, no loop bookkeeping); asynchronous. */
+int cans_run_step(cans_run *h, const double *dt, int apply_bc);
+/* Full-grid CFL of the current state (cfl_m3 / cfl_m); synchronous. */
+int cans_run_cfl(cans_run *h, double safety, double *dt);
+/* Time each tile configuration on `trial_steps` steps of the current state
+ * and keep the fastest; returns its index in *tile. */
+int cans_run_autotune(cans_run *h, int trial_steps, int *tile);
+/* Device pointers of the current state arrays (solver order). */
+int cans_run_device_state(cans_run *h, double **dev);
+/* Run `iters` loop iterations without a graph, timing each with CUDA events
+ * on the run's stream: *step_ms = summed duration of the step kernels,
+ * *iter_ms = summed duration of whole iterations.  Synchronous. */
+int cans_run_profile(cans_run *h, int iters, double *step_ms, double *iter_ms);
+
+/* ------------------------------------------------------------------------ */
+/* Measurement                                                               */
+/* ------------------------------------------------------------------------ */
+/* FP64 fused multiply-add throughput of the current device, TFLOP/s. */
+int cans_measure_fp64_tflops(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CANS_GPU_H */

@@ -1,0 +1,171 @@
+"""CPU oracle of the CANS mLW step -- TEST INFRASTRUCTURE ONLY.
+
+ctypes binding of the C restatement in this directory (libcansoracle.so) with
+the same Python signatures as utrip_gb300.capi, plus a restatement of the
+model-package time loop (cans2d/md_mhdkh/hdmlw/main.f:160-219).  Only the
+tests, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use it.
+
+Parity status: parity unpinned against the Fortran itself (no Fortran
+compiler is available and the reference ships no golden vectors for this
+path); the restatement is pinned by invariants and frozen fixtures in
+tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libcansoracle.so"
+_lib = None
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(8)
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = C.CDLL(str(LIB))
+        d, i = C.c_double, C.c_int
+        lib.oracle_mlw_m3_2d.argtypes = [_dp] * 9 + [d, d, d, _dp, _dp, i, _dp, _dp, i]
+        lib.oracle_mlw_m_2d.argtypes = [_dp] * 7 + [d, d, d, _dp, _dp, i, _dp, _dp, i]
+        lib.oracle_cfl_m3_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i]
+        lib.oracle_cfl_m_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 6 + [_dp, i, _dp, i]
+        lib.oracle_bd_2d.argtypes = [i, i, i, i, _dp, d, _dp, i, i]
+        lib.oracle_bd_1d.argtypes = [i, i, i, _dp, d, _dp, i]
+        lib.oracle_bd_3d.argtypes = [i, i, i, i, _dp, d, _dp, i, i, i]
+        lib.oracle_bbtoaa_2d.argtypes = [_dp, _dp, _dp, _dp, _dp, i, i, i]
+        lib.oracle_grdrdy.argtypes = [_dp, _dp, _dp, _dp, i]
+        lib.oracle_mlw_m_1d.argtypes = [_dp] * 7 + [d, d, d, _dp, _dp, i]
+        lib.oracle_cfl_m_1d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 6 + [_dp, i]
+        lib.oracle_mlw_m_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, _dp, i, _dp, _dp, i, _dp, _dp, i]
+        lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
+        lib.oracle_set_threads.argtypes = [i]
+        lib.oracle_get_threads.restype = i
+        _lib = lib
+    return _lib
+
+
+def P(a):
+    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1)
+    return a.ctypes.data_as(_dp)
+
+
+def set_threads(n: int) -> None:
+    load().oracle_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(load().oracle_get_threads())
+
+
+def mlw_m3(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, dx, dxm, dy, dym):
+    ix, jx = ro.shape
+    load().oracle_mlw_m3_2d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)],
+                            dt, qav, gm, P(dx), P(dxm), ix, P(dy), P(dym), jx)
+
+
+def mlw_m(ro, pr, vx, vy, bx, by, az, dt, qav, gm, dx, dxm, dy, dym):
+    ix, jx = ro.shape
+    load().oracle_mlw_m_2d(*[P(a) for a in (ro, pr, vx, vy, bx, by, az)],
+                           dt, qav, gm, P(dx), P(dxm), ix, P(dy), P(dym), jx)
+
+
+def cfl_m3(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy):
+    ix, jx = ro.shape
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m3_2d(C.byref(dt), safety, dtmin, C.byref(merr), gm,
+                            *[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
+                            P(dx), ix, P(dy), jx)
+    return dt.value, merr.value
+
+
+def cfl_m(safety, dtmin, gm, ro, pr, vx, vy, bx, by, dx, dy):
+    ix, jx = ro.shape
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m_2d(C.byref(dt), safety, dtmin, C.byref(merr), gm,
+                           *[P(a) for a in (ro, pr, vx, vy, bx, by)], P(dx), ix, P(dy), jx)
+    return dt.value, merr.value
+
+
+def bd(kind, axis, mbnd, margin, qq, q0=0.0, dxm=None):
+    """One bd* call on a 2-D array; BD_PER does both faces like bdper?."""
+    ix, jx = qq.shape
+    lib = load()
+    dp = P(dxm) if dxm is not None else None
+    if kind == BD_PER:
+        lib.oracle_bd_2d(kind, axis, 0, margin, P(qq), q0, dp, ix, jx)
+        lib.oracle_bd_2d(kind, axis, 1, margin, P(qq), q0, dp, ix, jx)
+    else:
+        lib.oracle_bd_2d(kind, axis, mbnd, margin, P(qq), q0, dp, ix, jx)
+
+
+def bbtoaa(bx, by, dxm, dym, margin):
+    ix, jx = bx.shape
+    az = np.zeros((ix, jx), order="F")
+    load().oracle_bbtoaa_2d(P(az), P(bx), P(by), P(dxm), P(dym), margin, ix, jx)
+    return az
+
+
+def apply_bc_program(state, program, margin, grid=None):
+    """Apply a boundary program axis by axis (all x faces, then all y faces),
+    as cans2d/md_mhdkh/hdmlw/bnd.f:11-39 orders its bd* calls."""
+    for axis in (0, 1):
+        for var, face, kind, q0 in program:
+            if face // 2 != axis or kind < 0:
+                continue
+            dxm = None
+            if grid is not None:
+                dxm = grid["dxm"] if axis == 0 else grid["dym"]
+            if kind == BD_PER:
+                load().oracle_bd_2d(kind, axis, face % 2, margin, P(state[var]), q0,
+                                    P(dxm) if dxm is not None else None, *state[var].shape)
+            else:
+                bd(kind, axis, face % 2, margin, state[var], q0, dxm)
+
+
+def step_2d(setup, state, dt):
+    args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
+    if setup["solver"] == "mlw_m3":
+        mlw_m3(*state, dt, *args)
+    else:
+        mlw_m(*state, dt, *args)
+
+
+def cfl_2d(setup, state, safety):
+    if setup["solver"] == "mlw_m3":
+        return cfl_m3(safety, setup["dtmin"], setup["gm"], *state[:8], setup["dx"], setup["dy"])
+    return cfl_m(safety, setup["dtmin"], setup["gm"], *state[:6], setup["dx"], setup["dy"])
+
+
+def run_2d(setup, state, nstop, tend=None, safety=None, t0=0.0):
+    """Restatement of the model-package loop (md_mhdkh/hdmlw/main.f:160-219):
+    ns+=1; cfl; merr test; t+=dt; step; bnd; loop while ns<nstop and t<tend.
+    Returns (t, ns, merr, dts)."""
+    tend = setup.get("tend", 1e30) if tend is None else tend
+    safety = setup["safety"] if safety is None else safety
+    t, ns, dts = t0, 0, []
+    while True:
+        ns += 1
+        dt, merr = cfl_2d(setup, state, safety)
+        if merr:
+            return t, ns, merr, dts
+        t = t + dt
+        dts.append(dt)
+        step_2d(setup, state, dt)
+        apply_bc_program(state, setup["bc"], setup["margin"], setup)
+        if not (ns < nstop and t < tend):
+            return t, ns, 0, dts

@@ -1,0 +1,745 @@
+/*
+ * 2-D mLW step, CFL and vector-potential set-up: line-faithful C restatement
+ * of the CANS Fortran (TEST INFRASTRUCTURE ONLY; see oracle.h).
+ *
+ *   mlwhalf   cans2d/hdmlw/mlwhalf.f:36-52
+ *   mlwsrch   cans2d/hdmlw/mlwsrch.f:87-102
+ *   mlwfull   cans2d/hdmlw/mlwfull.f:136-146
+ *   mlwsrcf   cans2d/hdmlw/mlwsrcf.f:182-189
+ *   mlwartv   cans2d/hdmlw/mlwartv.f:225-233
+ *   mlw_m3    cans2d/hdmlw/mlw_m3.f:64-374   (8 conserved variables + az)
+ *   mlw_m     cans2d/hdmlw/mlw_m.f           (6 conserved variables + az)
+ *   cfl_m3    cans2d/common/cfl_m3.f:38-65
+ *   cfl_m     cans2d/common/cfl_m.f:38-77
+ *   bbtoaa    cans2d/common/bbtoaa.f:28-49
+ */
+#include "oracle.h"
+#include "oracle_common.h"
+
+static oracle_arena arena2d;
+
+/* cans2d/hdmlw/mlwhalf.f:36-52 */
+static void mlwhalf2(const double *u, double *un, double *du, double dt,
+                     const double *fx, const double *dxi, const double *dxim,
+                     int ix, const double *fy, const double *dyi,
+                     const double *dyim, int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++)
+      du[I2(i, j)] =
+          du[I2(i, j)] -
+          0.5 * dt * (0.5 * dxi[I1(i)] * (fx[I2(i + 1, j)] - fx[I2(i - 1, j)])) -
+          0.5 * dt * (0.5 * dyi[I1(j)] * (fy[I2(i, j + 1)] - fy[I2(i, j - 1)]));
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      double uh = 0.25 * (u[I2(i + 1, j)] + u[I2(i, j)] + u[I2(i + 1, j + 1)] +
+                          u[I2(i, j + 1)]);
+      double dfdx = dxim[I1(i)] *
+                    (fx[I2(i + 1, j)] - fx[I2(i, j)] + fx[I2(i + 1, j + 1)] -
+                     fx[I2(i, j + 1)]) /
+                    2;
+      double dfdy = dyim[I1(j)] *
+                    (fy[I2(i, j + 1)] - fy[I2(i, j)] + fy[I2(i + 1, j + 1)] -
+                     fy[I2(i + 1, j)]) /
+                    2;
+      un[I2(i, j)] = uh - dt * dfdx - dt * dfdy;
+    }
+}
+
+/* cans2d/hdmlw/mlwsrch.f:87-102 */
+static void mlwsrch2(double *un, double *du, double dt, const double *s, int ix,
+                     int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++)
+      du[I2(i, j)] = du[I2(i, j)] + 0.5 * dt * s[I2(i, j)];
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      double sh = (s[I2(i + 1, j)] + s[I2(i, j)] + s[I2(i + 1, j + 1)] +
+                   s[I2(i, j + 1)]) /
+                  4.0;
+      un[I2(i, j)] = un[I2(i, j)] + dt * sh;
+    }
+}
+
+/* cans2d/hdmlw/mlwfull.f:136-146 */
+static void mlwfull2(double *du, double dt, const double *fx, const double *dxi,
+                     const double *ux0, const double *ux1, int ix,
+                     const double *fy, const double *dyi, const double *uy0,
+                     const double *uy1, int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++) {
+      double dfdx =
+          dxi[I1(i)] *
+          (uy0[I1(j)] * (fx[I2(i, j - 1)] - fx[I2(i - 1, j - 1)]) +
+           uy1[I1(j)] * (fx[I2(i, j)] - fx[I2(i - 1, j)]));
+      double dfdy =
+          dyi[I1(j)] *
+          (ux0[I1(i)] * (fy[I2(i - 1, j)] - fy[I2(i - 1, j - 1)]) +
+           ux1[I1(i)] * (fy[I2(i, j)] - fy[I2(i, j - 1)]));
+      du[I2(i, j)] = du[I2(i, j)] - 0.5 * dt * dfdx - 0.5 * dt * dfdy;
+    }
+}
+
+/* cans2d/hdmlw/mlwsrcf.f:182-189 */
+static void mlwsrcf2(double *du, double dt, const double *s, const double *ux0,
+                     const double *ux1, int ix, const double *uy0,
+                     const double *uy1, int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++) {
+      double sh = uy0[I1(j)] * (ux0[I1(i)] * s[I2(i - 1, j - 1)] +
+                                ux1[I1(i)] * s[I2(i, j - 1)]) +
+                  uy1[I1(j)] * (ux0[I1(i)] * s[I2(i - 1, j)] +
+                                ux1[I1(i)] * s[I2(i, j)]);
+      du[I2(i, j)] = du[I2(i, j)] + 0.5 * dt * sh;
+    }
+}
+
+/* cans2d/hdmlw/mlwartv.f:225-233 */
+static void mlwartv2(const double *u, double *du, double dt, const double *qx,
+                     const double *dxi, const double *dxim, int ix,
+                     const double *qy, const double *dyi, const double *dyim,
+                     int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++)
+      du[I2(i, j)] =
+          du[I2(i, j)] +
+          dt * (dxi[I1(i)] *
+                (qx[I2(i, j)] * dxim[I1(i)] * (u[I2(i + 1, j)] - u[I2(i, j)]) -
+                 qx[I2(i - 1, j)] * dxim[I1(i - 1)] *
+                     (u[I2(i, j)] - u[I2(i - 1, j)]))) +
+          dt * (dyi[I1(j)] *
+                (qy[I2(i, j)] * dyim[I1(j)] * (u[I2(i, j + 1)] - u[I2(i, j)]) -
+                 qy[I2(i, j - 1)] * dyim[I1(j - 1)] *
+                     (u[I2(i, j)] - u[I2(i, j - 1)])));
+}
+
+/* Metric set-up shared by mlw_m and mlw_m3 (mlw_m3.f:70-86). */
+static void metrics2(const double *dx, const double *dxm, int ix,
+                     const double *dy, const double *dym, int jx, double *dxi,
+                     double *dxim, double *ux0, double *ux1, double *dyi,
+                     double *dyim, double *uy0, double *uy1) {
+  for (int i = 1; i <= ix; i++) {
+    dxi[I1(i)] = 1.0 / dx[I1(i)];
+    dxim[I1(i)] = 1.0 / dxm[I1(i)];
+  }
+  for (int i = 2; i <= ix - 1; i++) {
+    ux1[I1(i)] = 0.5 * dxm[I1(i - 1)] / dx[I1(i)];
+    ux0[I1(i)] = 0.5 * dxm[I1(i)] / dx[I1(i)];
+  }
+  for (int j = 1; j <= jx; j++) {
+    dyi[I1(j)] = 1.0 / dy[I1(j)];
+    dyim[I1(j)] = 1.0 / dym[I1(j)];
+  }
+  for (int j = 2; j <= jx - 1; j++) {
+    uy1[I1(j)] = 0.5 * dym[I1(j - 1)] / dy[I1(j)];
+    uy0[I1(j)] = 0.5 * dym[I1(j)] / dy[I1(j)];
+  }
+}
+
+/* cans2d/hdmlw/mlw_m3.f:2-377 */
+void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
+                      double *vz, double *bx, double *by, double *bz,
+                      double *az, double dt, double qav, double gm,
+                      const double *dx, const double *dxm, int ix,
+                      const double *dy, const double *dym, int jx) {
+  const size_t n = (size_t)ix * (size_t)jx;
+  const size_t nm = (size_t)(ix > jx ? ix : jx);
+  enum { NT = 37 };
+  double *w = arena_get(&arena2d, NT * n + 8 * nm);
+  double *t[NT];
+  for (int a = 0; a < NT; a++) t[a] = w + a * n;
+  double *ee = t[0], *rx = t[1], *ry = t[2], *rz = t[3];
+  double *ex = t[4], *ey = t[5], *ez = t[6];
+  double *roh = t[7], *eeh = t[8], *rxh = t[9], *ryh = t[10], *rzh = t[11];
+  double *bxh = t[12], *byh = t[13], *bzh = t[14];
+  double *prh = t[15], *vxh = t[16], *vyh = t[17], *vzh = t[18];
+  double *exh = t[19], *eyh = t[20], *ezh = t[21], *azh = t[22];
+  double *dro = t[23], *dee = t[24], *drx = t[25], *dry = t[26], *drz = t[27];
+  double *dbx = t[28], *dby = t[29], *dbz = t[30], *daz = t[31];
+  double *fx = t[32], *qx = t[33], *fy = t[34], *qy = t[35], *ss = t[36];
+  double *m = w + NT * n;
+  double *dxi = m, *dxim = m + nm, *ux0 = m + 2 * nm, *ux1 = m + 3 * nm;
+  double *dyi = m + 4 * nm, *dyim = m + 5 * nm, *uy0 = m + 6 * nm,
+         *uy1 = m + 7 * nm;
+
+  const double pi = acos(-1.0);
+  const double pi8i = 1. / pi / 8.;
+  const double pi4i = 1. / pi / 4.;
+  metrics2(dx, dxm, ix, dy, dym, jx, dxi, dxim, ux0, ux1, dyi, dyim, uy0, uy1);
+
+  /* initialize dro etc. (:91-103) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      dro[c] = 0.0; dee[c] = 0.0; drx[c] = 0.0; dry[c] = 0.0; drz[c] = 0.0;
+      dbx[c] = 0.0; dby[c] = 0.0; dbz[c] = 0.0; daz[c] = 0.0;
+    }
+  /* energy from pressure (:107-116) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double vv = vx[c] * vx[c] + vy[c] * vy[c] + vz[c] * vz[c];
+      double bb = bx[c] * bx[c] + by[c] * by[c] + bz[c] * bz[c];
+      ee[c] = pr[c] / (gm - 1) + 0.5 * ro[c] * vv + pi8i * bb;
+      rx[c] = ro[c] * vx[c];
+      ry[c] = ro[c] * vy[c];
+      rz[c] = ro[c] * vz[c];
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      ex[c] = -vy[c] * bz[c] + vz[c] * by[c];
+      ey[c] = -vz[c] * bx[c] + vx[c] * bz[c];
+      ez[c] = -vx[c] * by[c] + vy[c] * bx[c];
+    }
+
+  /* density (:129-135) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * vx[c];
+      fy[c] = ro[c] * vy[c];
+    }
+  mlwhalf2(ro, roh, dro, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* energy (:138-146) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double vv = vx[c] * vx[c] + vy[c] * vy[c] + vz[c] * vz[c];
+      double ep = pr[c] * gm / (gm - 1.) + 0.5 * ro[c] * vv;
+      fx[c] = ep * vx[c] + (bz[c] * ey[c] - by[c] * ez[c]) * pi4i;
+      fy[c] = ep * vy[c] + (bx[c] * ez[c] - bz[c] * ex[c]) * pi4i;
+    }
+  mlwhalf2(ee, eeh, dee, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* x-momentum (:149-156) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * (vx[c] * vx[c]) + pr[c] +
+              pi8i * (by[c] * by[c] + bz[c] * bz[c] - bx[c] * bx[c]);
+      fy[c] = ro[c] * vx[c] * vy[c] - pi4i * bx[c] * by[c];
+    }
+  mlwhalf2(rx, rxh, drx, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* y-momentum (:159-166) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * vy[c] * vx[c] - pi4i * by[c] * bx[c];
+      fy[c] = ro[c] * (vy[c] * vy[c]) + pr[c] +
+              pi8i * (bx[c] * bx[c] + bz[c] * bz[c] - by[c] * by[c]);
+    }
+  mlwhalf2(ry, ryh, dry, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* z-momentum (:169-175) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * vz[c] * vx[c] - pi4i * bz[c] * bx[c];
+      fy[c] = ro[c] * vz[c] * vy[c] - pi4i * bz[c] * by[c];
+    }
+  mlwhalf2(rz, rzh, drz, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* x-magnetic (:178-184) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = 0.;
+      fy[c] = ez[c];
+    }
+  mlwhalf2(bx, bxh, dbx, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* y-magnetic (:187-193) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = -ez[c];
+      fy[c] = 0.;
+    }
+  mlwhalf2(by, byh, dby, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* z-magnetic (:196-202) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ey[c];
+      fy[c] = -ex[c];
+    }
+  mlwhalf2(bz, bzh, dbz, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  /* z-magnetic potential (:205-210) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) ss[I2(i, j)] = -ez[I2(i, j)];
+  mlwsrch2(azh, daz, dt, ss, ix, jx);
+
+  /* half-step primitives (:214-230) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      vxh[c] = rxh[c] / roh[c];
+      vyh[c] = ryh[c] / roh[c];
+      vzh[c] = rzh[c] / roh[c];
+      double vv = vxh[c] * vxh[c] + vyh[c] * vyh[c] + vzh[c] * vzh[c];
+      double bb = bxh[c] * bxh[c] + byh[c] * byh[c] + bzh[c] * bzh[c];
+      prh[c] = (gm - 1) * (eeh[c] - 0.5 * roh[c] * vv - pi8i * bb);
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      exh[c] = -vyh[c] * bzh[c] + vzh[c] * byh[c];
+      eyh[c] = -vzh[c] * bxh[c] + vxh[c] * bzh[c];
+      ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c];
+    }
+
+  /* full step: density (:235-241) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * vxh[c];
+      fy[c] = roh[c] * vyh[c];
+    }
+  mlwfull2(dro, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* energy (:244-254) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      double vv = vxh[c] * vxh[c] + vyh[c] * vyh[c] + vzh[c] * vzh[c];
+      double ep = prh[c] * gm / (gm - 1.) + 0.5 * roh[c] * vv;
+      fx[c] = ep * vxh[c] + (bzh[c] * eyh[c] - byh[c] * ezh[c]) * pi4i;
+      fy[c] = ep * vyh[c] + (bxh[c] * ezh[c] - bzh[c] * exh[c]) * pi4i;
+    }
+  mlwfull2(dee, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* x-momentum (:257-264) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * (vxh[c] * vxh[c]) + prh[c] +
+              pi8i * (byh[c] * byh[c] + bzh[c] * bzh[c] - bxh[c] * bxh[c]);
+      fy[c] = roh[c] * vxh[c] * vyh[c] - pi4i * bxh[c] * byh[c];
+    }
+  mlwfull2(drx, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* y-momentum (:267-274) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * vyh[c] * vxh[c] - pi4i * byh[c] * bxh[c];
+      fy[c] = roh[c] * (vyh[c] * vyh[c]) + prh[c] +
+              pi8i * (bxh[c] * bxh[c] + bzh[c] * bzh[c] - byh[c] * byh[c]);
+    }
+  mlwfull2(dry, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* z-momentum (:277-283); the reference sweeps the whole array here, the
+   * extra edge entries are never read by mlwfull. */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * vzh[c] * vxh[c] - pi4i * bzh[c] * bxh[c];
+      fy[c] = roh[c] * vzh[c] * vyh[c] - pi4i * bzh[c] * byh[c];
+    }
+  mlwfull2(drz, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* x-magnetic (:286-292) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = 0.;
+      fy[c] = ezh[c];
+    }
+  mlwfull2(dbx, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* y-magnetic (:294-301) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = -ezh[c];
+      fy[c] = 0.;
+    }
+  mlwfull2(dby, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* z-magnetic (:303-310) */
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = eyh[c];
+      fy[c] = -exh[c];
+    }
+  mlwfull2(dbz, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  /* z-magnetic potential (:313-318) */
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) ss[I2(i, j)] = -ezh[I2(i, j)];
+  mlwsrcf2(daz, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+
+  /* artificial-viscosity coefficients (:324-334) */
+  const double zero = 0.0;
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++)
+      qx[I2(i, j)] =
+          qav * dxm[I1(i)] *
+          fmax2(zero, fabs(vx[I2(i + 1, j)] - vx[I2(i, j)]) - R4_1EM4);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix; i++)
+      qy[I2(i, j)] =
+          qav * dym[I1(j)] *
+          fmax2(zero, fabs(vy[I2(i, j + 1)] - vy[I2(i, j)]) - R4_1EM4);
+  /* apply artificial viscosity (:338-345) */
+  mlwartv2(ro, dro, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(ee, dee, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(rx, drx, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(ry, dry, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(rz, drz, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(bx, dbx, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(by, dby, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(bz, dbz, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+
+  /* update internal points (:349-361) */
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      ro[c] = ro[c] + dro[c];
+      ee[c] = ee[c] + dee[c];
+      rx[c] = rx[c] + drx[c];
+      ry[c] = ry[c] + dry[c];
+      rz[c] = rz[c] + drz[c];
+      bx[c] = bx[c] + dbx[c];
+      by[c] = by[c] + dby[c];
+      bz[c] = bz[c] + dbz[c];
+      az[c] = az[c] + daz[c];
+    }
+  /* total energy to pressure (:365-374) */
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      vx[c] = rx[c] / ro[c];
+      vy[c] = ry[c] / ro[c];
+      vz[c] = rz[c] / ro[c];
+      double vv = vx[c] * vx[c] + vy[c] * vy[c] + vz[c] * vz[c];
+      double bb = bx[c] * bx[c] + by[c] * by[c] + bz[c] * bz[c];
+      pr[c] = (gm - 1) * (ee[c] - 0.5 * ro[c] * vv - pi8i * bb);
+    }
+}
+
+/* cans2d/hdmlw/mlw_m.f:2-324 (ro,pr,vx,vy,bx,by + az; no z components) */
+void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
+                     double *bx, double *by, double *az, double dt, double qav,
+                     double gm, const double *dx, const double *dxm, int ix,
+                     const double *dy, const double *dym, int jx) {
+  const size_t n = (size_t)ix * (size_t)jx;
+  const size_t nm = (size_t)(ix > jx ? ix : jx);
+  enum { NT = 27 };
+  double *w = arena_get(&arena2d, NT * n + 8 * nm);
+  double *t[NT];
+  for (int a = 0; a < NT; a++) t[a] = w + a * n;
+  double *ee = t[0], *rx = t[1], *ry = t[2], *ez = t[3];
+  double *roh = t[4], *eeh = t[5], *rxh = t[6], *ryh = t[7];
+  double *bxh = t[8], *byh = t[9];
+  double *prh = t[10], *vxh = t[11], *vyh = t[12], *ezh = t[13], *azh = t[14];
+  double *dro = t[15], *dee = t[16], *drx = t[17], *dry = t[18];
+  double *dbx = t[19], *dby = t[20], *daz = t[21];
+  double *fx = t[22], *qx = t[23], *fy = t[24], *qy = t[25], *ss = t[26];
+  double *m = w + NT * n;
+  double *dxi = m, *dxim = m + nm, *ux0 = m + 2 * nm, *ux1 = m + 3 * nm;
+  double *dyi = m + 4 * nm, *dyim = m + 5 * nm, *uy0 = m + 6 * nm,
+         *uy1 = m + 7 * nm;
+
+  const double pi = acos(-1.0);
+  const double pi8i = 1. / pi / 8.;
+  const double pi4i = 1. / pi / 4.;
+  metrics2(dx, dxm, ix, dy, dym, jx, dxi, dxim, ux0, ux1, dyi, dyim, uy0, uy1);
+
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      dro[c] = 0.0; dee[c] = 0.0; drx[c] = 0.0; dry[c] = 0.0;
+      dbx[c] = 0.0; dby[c] = 0.0; daz[c] = 0.0;
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double vv = vx[c] * vx[c] + vy[c] * vy[c];
+      double bb = bx[c] * bx[c] + by[c] * by[c];
+      ee[c] = pr[c] / (gm - 1) + 0.5 * ro[c] * vv + pi8i * bb;
+      rx[c] = ro[c] * vx[c];
+      ry[c] = ro[c] * vy[c];
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      ez[c] = -vx[c] * by[c] + vy[c] * bx[c];
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * vx[c];
+      fy[c] = ro[c] * vy[c];
+    }
+  mlwhalf2(ro, roh, dro, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double vv = vx[c] * vx[c] + vy[c] * vy[c];
+      double ep = pr[c] * gm / (gm - 1.) + 0.5 * ro[c] * vv;
+      fx[c] = ep * vx[c] - by[c] * ez[c] * pi4i;
+      fy[c] = ep * vy[c] + bx[c] * ez[c] * pi4i;
+    }
+  mlwhalf2(ee, eeh, dee, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * (vx[c] * vx[c]) + pr[c] +
+              pi8i * (by[c] * by[c] - bx[c] * bx[c]);
+      fy[c] = ro[c] * vx[c] * vy[c] - pi4i * bx[c] * by[c];
+    }
+  mlwhalf2(rx, rxh, drx, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = ro[c] * vy[c] * vx[c] - pi4i * by[c] * bx[c];
+      fy[c] = ro[c] * (vy[c] * vy[c]) + pr[c] +
+              pi8i * (bx[c] * bx[c] - by[c] * by[c]);
+    }
+  mlwhalf2(ry, ryh, dry, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = 0.;
+      fy[c] = ez[c];
+    }
+  mlwhalf2(bx, bxh, dbx, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      fx[c] = -ez[c];
+      fy[c] = 0.;
+    }
+  mlwhalf2(by, byh, dby, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) ss[I2(i, j)] = -ez[I2(i, j)];
+  mlwsrch2(azh, daz, dt, ss, ix, jx);
+
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      vxh[c] = rxh[c] / roh[c];
+      vyh[c] = ryh[c] / roh[c];
+      double vv = vxh[c] * vxh[c] + vyh[c] * vyh[c];
+      double bb = bxh[c] * bxh[c] + byh[c] * byh[c];
+      prh[c] = (gm - 1) * (eeh[c] - 0.5 * roh[c] * vv - pi8i * bb);
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c];
+    }
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * vxh[c];
+      fy[c] = roh[c] * vyh[c];
+    }
+  mlwfull2(dro, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      double vv = vxh[c] * vxh[c] + vyh[c] * vyh[c];
+      double ep = prh[c] * gm / (gm - 1.) + 0.5 * roh[c] * vv;
+      fx[c] = ep * vxh[c] - byh[c] * ezh[c] * pi4i;
+      fy[c] = ep * vyh[c] + bxh[c] * ezh[c] * pi4i;
+    }
+  mlwfull2(dee, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * (vxh[c] * vxh[c]) + prh[c] +
+              pi8i * (byh[c] * byh[c] - bxh[c] * bxh[c]);
+      fy[c] = roh[c] * vxh[c] * vyh[c] - pi4i * bxh[c] * byh[c];
+    }
+  mlwfull2(drx, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = roh[c] * vyh[c] * vxh[c] - pi4i * byh[c] * bxh[c];
+      fy[c] = roh[c] * (vyh[c] * vyh[c]) + prh[c] +
+              pi8i * (bxh[c] * bxh[c] - byh[c] * byh[c]);
+    }
+  mlwfull2(dry, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = 0.;
+      fy[c] = ezh[c];
+    }
+  mlwfull2(dbx, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      fx[c] = -ezh[c];
+      fy[c] = 0.;
+    }
+  mlwfull2(dby, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  OMP_FOR
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) ss[I2(i, j)] = -ezh[I2(i, j)];
+  mlwsrcf2(daz, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+
+  const double zero = 0.0;
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix - 1; i++)
+      qx[I2(i, j)] =
+          qav * dxm[I1(i)] *
+          fmax2(zero, fabs(vx[I2(i + 1, j)] - vx[I2(i, j)]) - R4_1EM4);
+  OMP_FOR
+  for (int j = 1; j <= jx - 1; j++)
+    for (int i = 1; i <= ix; i++)
+      qy[I2(i, j)] =
+          qav * dym[I1(j)] *
+          fmax2(zero, fabs(vy[I2(i, j + 1)] - vy[I2(i, j)]) - R4_1EM4);
+  mlwartv2(ro, dro, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(ee, dee, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(rx, drx, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(ry, dry, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(bx, dbx, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  mlwartv2(by, dby, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      ro[c] = ro[c] + dro[c];
+      ee[c] = ee[c] + dee[c];
+      rx[c] = rx[c] + drx[c];
+      ry[c] = ry[c] + dry[c];
+      bx[c] = bx[c] + dbx[c];
+      by[c] = by[c] + dby[c];
+      az[c] = az[c] + daz[c];
+    }
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++) {
+      size_t c = I2(i, j);
+      vx[c] = rx[c] / ro[c];
+      vy[c] = ry[c] / ro[c];
+      double vv = vx[c] * vx[c] + vy[c] * vy[c];
+      double bb = bx[c] * bx[c] + by[c] * by[c];
+      pr[c] = (gm - 1) * (ee[c] - 0.5 * ro[c] * vv - pi8i * bb);
+    }
+}
+
+/* cans2d/common/cfl_m3.f:38-65.  The per-cell dtq array and the serial
+ * first-minimum scan give the same value as a min-reduction: min is exact. */
+void oracle_cfl_m3_2d(double *dt, double safety, double dtmin, int *merr,
+                      double gm, const double *ro, const double *pr,
+                      const double *vx, const double *vy, const double *vz,
+                      const double *bx, const double *by, const double *bz,
+                      const double *dx, int ix, const double *dy, int jx) {
+  const double pi = acos(-1.0);
+  const double pi4i = 1. / pi / 4.;
+  double dmin = R4_1E20;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(min : dmin) schedule(static)
+#endif
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double b2 = bx[c] * bx[c] + by[c] * by[c] + bz[c] * bz[c];
+      double ca2 = b2 * pi4i / ro[c];
+      double cs2 = gm * pr[c] / ro[c];
+      double v2 = vx[c] * vx[c] + vy[c] * vy[c] + vz[c] * vz[c];
+      double dtcfl = fmin2(dx[I1(i)], dy[I1(j)]) / sqrt(v2 + cs2 + ca2);
+      double dtq = safety * dtcfl;
+      if (dtq < dmin) dmin = dtq;
+    }
+  *dt = dmin;
+  *merr = 0;
+  if (*dt < dtmin) *merr = 9001;
+}
+
+/* cans2d/common/cfl_m.f:38-77 */
+void oracle_cfl_m_2d(double *dt, double safety, double dtmin, int *merr,
+                     double gm, const double *ro, const double *pr,
+                     const double *vx, const double *vy, const double *bx,
+                     const double *by, const double *dx, int ix,
+                     const double *dy, int jx) {
+  const double pi = acos(-1.0);
+  const double pi4i = 1. / pi / 4.;
+  double dmin = R4_1E20;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(min : dmin) schedule(static)
+#endif
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double b2 = bx[c] * bx[c] + by[c] * by[c];
+      double ca2 = b2 * pi4i / ro[c];
+      double cs2 = gm * pr[c] / ro[c];
+      double v2 = vx[c] * vx[c] + vy[c] * vy[c];
+      double dtcfl = fmin2(dx[I1(i)], dy[I1(j)]) / sqrt(v2 + cs2 + ca2);
+      double dtq = safety * dtcfl;
+      if (dtq < dmin) dmin = dtq;
+    }
+  *dt = dmin;
+  *merr = 0;
+  if (*dt < dtmin) *merr = 9001;
+}
+
+/* cans2d/common/bbtoaa.f:28-49 */
+void oracle_bbtoaa_2d(double *az, const double *bx, const double *by,
+                      const double *dxm, const double *dym, int margin, int ix,
+                      int jx) {
+  az[I2(margin + 1, margin + 1)] = 0.0;
+  int i = margin + 1;
+  for (int j = margin + 2; j <= jx; j++)
+    az[I2(i, j)] = az[I2(i, j - 1)] +
+                   0.5 * (bx[I2(i, j - 1)] + bx[I2(i, j)]) * dym[I1(j - 1)];
+  for (int j = margin; j >= 1; j--)
+    az[I2(i, j)] =
+        az[I2(i, j + 1)] - 0.5 * (bx[I2(i, j)] + bx[I2(i, j + 1)]) * dym[I1(j)];
+  for (int j = 1; j <= jx; j++) {
+    for (int ii = margin + 2; ii <= ix; ii++)
+      az[I2(ii, j)] = az[I2(ii - 1, j)] -
+                      0.5 * (by[I2(ii - 1, j)] + by[I2(ii, j)]) * dxm[I1(ii - 1)];
+    for (int ii = margin; ii >= 1; ii--)
+      az[I2(ii, j)] =
+          az[I2(ii + 1, j)] + 0.5 * (by[I2(ii, j)] + by[I2(ii + 1, j)]) * dxm[I1(ii)];
+  }
+}

@@ -1,0 +1,113 @@
+/*
+ * CPU oracle for the CANS modified Lax-Wendroff (mLW) MHD step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a line-faithful C restatement of the
+ * reference Fortran-77 routines (CANS, cans{1,2,3}d/hdmlw, common, bc).  It is
+ * used by the test-suite as the checker, by __graft_entry__.smoke() and by the
+ * CPU-baseline leg of bench.py.  No product code path links or calls it.
+ *
+ * Parity status: parity unpinned against the Fortran itself.  No Fortran
+ * compiler exists in the build or GPU environment and the reference ships no
+ * golden vectors for mlw_m / mlw_m3 / cfl_m, so the restatement is pinned by
+ * hand-checkable invariants instead (uniform-state invariance, mirror
+ * symmetry, exact periodic conservation, linear-wave phase speed) and by the
+ * committed fixtures in tests/golden/ that freeze its own outputs.
+ *
+ * Fidelity rules followed throughout:
+ *   - same loop bounds and the same left-to-right operation order as the
+ *     Fortran source (C and Fortran share associativity for + - * /);
+ *   - x**2 is x*x, as gfortran expands it;
+ *   - real*4 literals are kept in single precision where the value is not
+ *     exactly representable (1.0e-4 in the artificial viscosity, 1.e20 as the
+ *     initial CFL minimum, acos(-1.0) in the 3-D CFL);
+ *   - build with -O2 -ffp-contract=off -fno-fast-math (no FMA contraction);
+ *   - the Fortran automatic arrays become one cached, zero-initialised heap
+ *     arena, reused between calls of the same size.
+ *
+ * Arrays are column-major with 1-based Fortran indices mapped by the I1/I2/I3
+ * macros below; ghost cells are included exactly as in the reference.
+ */
+#ifndef CANS_ORACLE_H
+#define CANS_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- threading (OpenMP when compiled with -fopenmp) ---------------------- */
+void oracle_set_threads(int n);
+int oracle_get_threads(void);
+
+/* ---- 1-D  (cans1d) ------------------------------------------------------- */
+void oracle_grdrdy(double *dx, double *xm, double *dxm, const double *x, int ix);
+void oracle_mlw_m_1d(double *ro, double *pr, double *vx, double *vy, double *by,
+                     const double *bx, const double *bxm, double dt, double qav,
+                     double gm, const double *dx, const double *dxm, int ix);
+void oracle_cfl_m_1d(double *dt, double safety, double dtmin, int *merr,
+                     double gm, const double *bx, const double *ro,
+                     const double *pr, const double *vx, const double *vy,
+                     const double *by, const double *dx, int ix);
+void oracle_bd_1d(int kind, int mbnd, int margin, double *qq, double q0,
+                  const double *dxm, int ix);
+
+/* ---- 2-D  (cans2d) ------------------------------------------------------- */
+void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
+                      double *vz, double *bx, double *by, double *bz,
+                      double *az, double dt, double qav, double gm,
+                      const double *dx, const double *dxm, int ix,
+                      const double *dy, const double *dym, int jx);
+void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
+                     double *bx, double *by, double *az, double dt, double qav,
+                     double gm, const double *dx, const double *dxm, int ix,
+                     const double *dy, const double *dym, int jx);
+void oracle_cfl_m3_2d(double *dt, double safety, double dtmin, int *merr,
+                      double gm, const double *ro, const double *pr,
+                      const double *vx, const double *vy, const double *vz,
+                      const double *bx, const double *by, const double *bz,
+                      const double *dx, int ix, const double *dy, int jx);
+void oracle_cfl_m_2d(double *dt, double safety, double dtmin, int *merr,
+                     double gm, const double *ro, const double *pr,
+                     const double *vx, const double *vy, const double *bx,
+                     const double *by, const double *dx, int ix,
+                     const double *dy, int jx);
+void oracle_bbtoaa_2d(double *az, const double *bx, const double *by,
+                      const double *dxm, const double *dym, int margin, int ix,
+                      int jx);
+/* kind: see BD_* below; axis 0 = x, 1 = y; mbnd 0 = lower, 1 = upper face.
+ * q0 is the constant for BD_CNS; dxm the spacing for BD_FRD. */
+void oracle_bd_2d(int kind, int axis, int mbnd, int margin, double *qq,
+                  double q0, const double *dxm, int ix, int jx);
+
+/* ---- 3-D  (cans3d) ------------------------------------------------------- */
+void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                     double *bx, double *by, double *bz, double dt, double qav,
+                     double gm, const double *dx, const double *dxm, int ix,
+                     const double *dy, const double *dym, int jx,
+                     const double *dz, const double *dzm, int kx);
+void oracle_cfl_m_3d(double *dt, double safety, double dtmin, int *merr,
+                     double gm, const double *ro, const double *pr,
+                     const double *vx, const double *vy, const double *vz,
+                     const double *bx, const double *by, const double *bz,
+                     const double *dx, int ix, const double *dy, int jx,
+                     const double *dz, int kx);
+void oracle_bd_3d(int kind, int axis, int mbnd, int margin, double *qq,
+                  double q0, const double *dxm, int ix, int jx, int kx);
+
+/* Boundary kinds (reference routine family in parentheses). */
+enum {
+  BD_PER = 0, /* periodic            (bdperx/bdpery/bdperz)          */
+  BD_SPP = 1, /* symmetric, even     (bdsppx/...) ghost(i)=q(bnd-1+i) */
+  BD_SPN = 2, /* symmetric, odd      (bdspnx/...) ghost=-q(bnd-1+i)   */
+  BD_SMP = 3, /* symmetric about cell, even (bdsmpx/...)              */
+  BD_SMN = 4, /* symmetric about cell, odd, boundary cell zeroed (bdsmnx) */
+  BD_FRE = 5, /* free, zero gradient (bdfrex/...)                     */
+  BD_CNS = 6, /* constant value      (bdcnsx/...)                     */
+  BD_FRD = 7  /* free, constant gradient (bdfrdx/...)                 */
+};
+
+#ifdef __cplusplus
+}
+#endif
+#endif

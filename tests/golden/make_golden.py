@@ -1,0 +1,62 @@
+"""Generate the frozen oracle fixtures in this directory.
+
+Run from the repository root:  python tests/golden/make_golden.py
+The fixtures freeze the CPU oracle's outputs on small seeded inputs so that a
+change to the oracle (and through it the exact-mode GPU parity) is caught.
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import oracle  # noqa: E402
+from utrip_gb300 import setups  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def case_2d(solver, ix, jx, seed, nsteps):
+    s = setups.random_state(ix, jx, seed=seed, solver=solver)
+    # inputs are stored too: the NumPy transcendental functions that build
+    # them may differ in the last bit between machines
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dxm", "dy", "dym"):
+        out["grid_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt0, _ = oracle.cfl_2d(s, st, 0.4)
+    one = setups.copy_state(s)
+    oracle.step_2d(s, one, dt0)
+    t, ns, merr, dts = oracle.run_2d(s, st, nsteps)
+    out.update({"dt0": np.array(dt0), "t": np.array(t), "ns": np.array(ns),
+                "dts": np.array(dts)})
+    for k, a in zip(s["names"], one):
+        out["step1_" + k] = a
+    for k, a in zip(s["names"], st):
+        out["loop_" + k] = a
+    return out
+
+
+def main():
+    oracle.build()
+    np.savez_compressed(OUT / "mlw_m3_2d_18x14.npz", **case_2d("mlw_m3", 18, 14, 11, 10))
+    np.savez_compressed(OUT / "mlw_m_2d_16x20.npz", **case_2d("mlw_m", 16, 20, 12, 10))
+    rng = np.random.default_rng(13)
+    q = np.asfortranarray(rng.standard_normal((9, 7)))
+    dxm = np.linspace(0.1, 0.2, 9)
+    dym = np.linspace(0.1, 0.3, 7)
+    bc = {}
+    for kind in range(8):
+        for axis in (0, 1):
+            for mbnd in (0, 1):
+                a = q.copy(order="F")
+                oracle.bd(kind, axis, mbnd, 2, a, q0=0.75, dxm=dxm if axis == 0 else dym)
+                bc[f"k{kind}_a{axis}_m{mbnd}"] = a
+    np.savez_compressed(OUT / "bd_2d_9x7.npz", q=q, dxm=dxm, dym=dym, **bc)
+    print("wrote fixtures to", OUT)
+
+
+if __name__ == "__main__":
+    main()

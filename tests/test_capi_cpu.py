@@ -1,0 +1,51 @@
+"""CPU-side checks of the C ABI: the library builds, loads, exports every
+symbol include/cans_gpu.h declares, and rejects bad arguments before it
+touches a device.  No compute call is made here (there is no GPU)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from utrip_gb300 import build, capi
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return capi.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = capi.exported_symbols()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_header_declares_the_drop_in_routines():
+    names = set(capi.exported_symbols())
+    for n in ("cans_mlw_m3_2d", "cans_mlw_m_2d", "cans_cfl_m3_2d", "cans_cfl_m_2d",
+              "cans_bdperx_2d", "cans_bdsppy_2d", "cans_bdsmnx_2d", "cans_gpu_register",
+              "cans_gpu_pull", "cans_run_create", "cans_run_advance"):
+        assert n in names, n
+
+
+def test_bad_sizes_are_rejected_without_a_device(lib):
+    a = np.zeros((2, 5), order="F")
+    z = C.c_double(0.1)
+    with pytest.raises(capi.CansError) as e:
+        capi.mlw_m3(*([a] * 9), 0.1, 3.0, 5 / 3, np.ones(2), np.ones(2), np.ones(5), np.ones(5))
+    assert e.value.code == capi.CANS_ERR_ARG
+    # bd with a margin larger than the axis
+    q = np.zeros((3, 3), order="F")
+    with pytest.raises(capi.CansError) as e:
+        capi.bd(capi.BD_SPP, 0, 0, 4, q)
+    assert e.value.code == capi.CANS_ERR_ARG
+    del z
+
+
+def test_run_desc_layout_matches_header():
+    # the ctypes mirror of cans_run_desc must keep the C field order
+    fields = [f[0] for f in capi._Desc._fields_]
+    assert fields == ["solver", "ix", "jx", "kx", "margin", "gm", "qav", "dx", "dxm", "dy",
+                      "dym", "dz", "dzm", "exact", "tile", "stream"]

@@ -1,0 +1,324 @@
+"""ctypes binding of libcansgpu.so (the C ABI declared in include/cans_gpu.h).
+
+The Python functions keep the reference routine names and argument meaning
+(cans2d/hdmlw/mlw_m3.f:2, cans2d/common/cfl_m3.f:2, cans2d/bc/bd*.f:2, ...):
+arrays are NumPy float64 arrays in Fortran (column-major) order with their
+ghost cells, updated in place; scalars are plain Python numbers.  Every call
+goes to the GPU library; there is no CPU path, and a missing or unusable
+library raises CansError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIBDIR / _build.LIBNAME
+
+CANS_OK = 0
+CANS_ERR_DTMIN = 9001
+CANS_ERR_CUDA = 9200
+CANS_ERR_ARG = 9400
+
+SOLVER_MLW_M_2D = 0
+SOLVER_MLW_M3_2D = 1
+
+BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lib = None
+
+
+class CansError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        super().__init__(f"{where} returned {code}" + (f": {detail}" if detail else ""))
+        self.code = code
+
+
+def load() -> C.CDLL:
+    """Load libcansgpu.so (built by __graft_entry__.build()); raise if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise CansError(CANS_ERR_CUDA, "load",
+                        f"{LIB_PATH} is missing; build it with __graft_entry__.build()")
+    lib = C.CDLL(str(LIB_PATH))
+    i, d, vp = C.c_int, C.c_double, C.c_void_p
+    sig = {
+        "cans_set_exact": (i, [i]), "cans_get_exact": (i, []),
+        "cans_set_stream": (i, [vp]), "cans_last_error": (C.c_char_p, []),
+        "cans_launch_count": (C.c_ulonglong, []), "cans_device_ok": (i, []),
+        "cans_mlw_m3_2d": (i, [_dp] * 9 + [_dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip]),
+        "cans_mlw_m_2d": (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip]),
+        "cans_cfl_m3_2d": (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 + [_dp, _ip, _dp, _ip]),
+        "cans_cfl_m_2d": (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 6 + [_dp, _ip, _dp, _ip]),
+        "cans_gpu_register": (i, [C.POINTER(_dp), _ip, _ip, _ip, _ip]),
+        "cans_gpu_pull": (i, [_dp]), "cans_gpu_push": (i, [_dp]),
+        "cans_gpu_release": (i, [_dp]),
+        "cans_run_create": (i, [C.POINTER(vp), vp]), "cans_run_destroy": (i, [vp]),
+        "cans_run_set_bc": (i, [vp, i, i, i, d]),
+        "cans_run_push": (i, [vp, C.POINTER(_dp)]), "cans_run_pull": (i, [vp, C.POINTER(_dp)]),
+        "cans_run_start": (i, [vp, d, d, C.c_longlong, d, d, d, i]),
+        "cans_run_advance": (i, [vp, i]), "cans_run_query": (i, [vp, vp]),
+        "cans_run_resume": (i, [vp]), "cans_run_step": (i, [vp, _dp, i]),
+        "cans_run_cfl": (i, [vp, d, _dp]), "cans_run_autotune": (i, [vp, i, _ip]),
+        "cans_run_device_state": (i, [vp, C.POINTER(_dp)]),
+        "cans_run_profile": (i, [vp, i, _dp, _dp]),
+        "cans_measure_fp64_tflops": (i, [_dp]),
+    }
+    for name in ("bdperx", "bdpery"):
+        sig[f"cans_{name}_2d"] = (i, [_ip, _ip, _dp, _ip, _ip])
+    for fam in ("spp", "spn", "smp", "smn", "fre"):
+        for ax in "xy":
+            sig[f"cans_bd{fam}{ax}_2d"] = (i, [_ip, _ip, _dp, _ip, _ip])
+    for ax in "xy":
+        sig[f"cans_bdcns{ax}_2d"] = (i, [_ip, _ip, _dp, _dp, _ip, _ip])
+        sig[f"cans_bdfrd{ax}_2d"] = (i, [_ip, _ip, _dp, _dp, _ip, _ip])
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    """Names declared in include/cans_gpu.h (for the export check)."""
+    import re
+    hdr = (_build.ROOT / "include" / "cans_gpu.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*|unsigned long long)\s*\*?\s*(cans_\w+)\s*\(",
+                                 hdr, flags=re.M)))
+
+
+def _check(rc: int, where: str) -> int:
+    if rc not in (CANS_OK,):
+        detail = load().cans_last_error().decode() if rc == CANS_ERR_CUDA else ""
+        raise CansError(rc, where, detail)
+    return rc
+
+
+def _ptr(a: np.ndarray):
+    if a.dtype != np.float64 or not (a.flags.f_contiguous or a.ndim == 1):
+        raise CansError(CANS_ERR_ARG, "array", "float64 Fortran-ordered arrays are required")
+    return a.ctypes.data_as(_dp)
+
+
+def _dref(x: float):
+    return C.byref(C.c_double(float(x)))
+
+
+def _iref(x: int):
+    return C.byref(C.c_int(int(x)))
+
+
+def set_exact(flag: bool) -> None:
+    load().cans_set_exact(1 if flag else 0)
+
+
+def launch_count() -> int:
+    return int(load().cans_launch_count())
+
+
+def device_ok() -> bool:
+    return bool(load().cans_device_ok())
+
+
+# ---- drop-in routines (2-D) ------------------------------------------------
+
+def mlw_m3(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m3.f:2 -- one mLW step of the 2.5-D state, in place."""
+    ix, jx = ro.shape
+    lib = load()
+    return _check(lib.cans_mlw_m3_2d(*[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)],
+                                     _dref(dt), _dref(qav), _dref(gm), _ptr(dx), _ptr(dxm),
+                                     _iref(ix), _ptr(dy), _ptr(dym), _iref(jx)), "mlw_m3")
+
+
+def mlw_m(ro, pr, vx, vy, bx, by, az, dt, qav, gm, dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m.f:2 -- one mLW step of the 2-D state, in place."""
+    ix, jx = ro.shape
+    lib = load()
+    return _check(lib.cans_mlw_m_2d(*[_ptr(a) for a in (ro, pr, vx, vy, bx, by, az)],
+                                    _dref(dt), _dref(qav), _dref(gm), _ptr(dx), _ptr(dxm),
+                                    _iref(ix), _ptr(dy), _ptr(dym), _iref(jx)), "mlw_m")
+
+
+def cfl_m3(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy):
+    """cans2d/common/cfl_m3.f:2 -- returns (dt, merr)."""
+    ix, jx = ro.shape
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m3_2d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                 _dref(gm), *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
+                                 _ptr(dx), _iref(ix), _ptr(dy), _iref(jx)), "cfl_m3")
+    return dt.value, merr.value
+
+
+def cfl_m(safety, dtmin, gm, ro, pr, vx, vy, bx, by, dx, dy):
+    """cans2d/common/cfl_m.f:2 -- returns (dt, merr)."""
+    ix, jx = ro.shape
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m_2d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                _dref(gm), *[_ptr(a) for a in (ro, pr, vx, vy, bx, by)],
+                                _ptr(dx), _iref(ix), _ptr(dy), _iref(jx)), "cfl_m")
+    return dt.value, merr.value
+
+
+_BD_NAMES = {BD_SPP: "spp", BD_SPN: "spn", BD_SMP: "smp", BD_SMN: "smn",
+             BD_FRE: "fre", BD_CNS: "cns", BD_FRD: "frd"}
+
+
+def bd(kind: int, axis: int, mbnd: int, margin: int, qq: np.ndarray,
+       q0: float = 0.0, dxm: np.ndarray | None = None) -> int:
+    """One reference bd* call on a 2-D array (cans2d/bc/bd*.f).
+
+    For BD_PER, mbnd is ignored and the call is bdper?(margin, margin, ...)."""
+    lib = load()
+    ix, jx = qq.shape
+    a = "xy"[axis]
+    if kind == BD_PER:
+        f = getattr(lib, f"cans_bdper{a}_2d")
+        return _check(f(_iref(margin), _iref(margin), _ptr(qq), _iref(ix), _iref(jx)), f"bdper{a}")
+    name = f"cans_bd{_BD_NAMES[kind]}{a}_2d"
+    f = getattr(lib, name)
+    if kind == BD_CNS:
+        return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _dref(q0), _iref(ix), _iref(jx)), name)
+    if kind == BD_FRD:
+        return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _ptr(dxm), _iref(ix), _iref(jx)), name)
+    return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _iref(ix), _iref(jx)), name)
+
+
+# ---- residency registry ----------------------------------------------------
+
+def register(arrays) -> None:
+    arr = (_dp * len(arrays))(*[_ptr(a) for a in arrays])
+    shp = arrays[0].shape + (1,) * (3 - arrays[0].ndim)
+    _check(load().cans_gpu_register(arr, _iref(len(arrays)), _iref(shp[0]), _iref(shp[1]),
+                                    _iref(shp[2])), "cans_gpu_register")
+
+
+def pull(any_array) -> None:
+    _check(load().cans_gpu_pull(_ptr(any_array)), "cans_gpu_pull")
+
+
+def push(any_array) -> None:
+    _check(load().cans_gpu_push(_ptr(any_array)), "cans_gpu_push")
+
+
+def release(any_array) -> None:
+    _check(load().cans_gpu_release(_ptr(any_array)), "cans_gpu_release")
+
+
+# ---- device-resident run handle --------------------------------------------
+
+class _Desc(C.Structure):
+    _fields_ = [("solver", C.c_int), ("ix", C.c_int), ("jx", C.c_int), ("kx", C.c_int),
+                ("margin", C.c_int), ("gm", C.c_double), ("qav", C.c_double),
+                ("dx", _dp), ("dxm", _dp), ("dy", _dp), ("dym", _dp), ("dz", _dp), ("dzm", _dp),
+                ("exact", C.c_int), ("tile", C.c_int), ("stream", C.c_void_p)]
+
+
+class RunState(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("ns", C.c_longlong),
+                ("nexec", C.c_longlong), ("merr", C.c_int), ("done", C.c_int),
+                ("pause", C.c_int)]
+
+
+class Run:
+    """Device-resident run of the reference time loop (cans_run_* API)."""
+
+    def __init__(self, solver: int, grid: dict, gm: float, qav: float, margin: int = 1,
+                 exact: bool = False, tile: int = -1, stream: int | None = None):
+        self.lib = load()
+        self.solver = solver
+        self.nvar = 9 if solver == SOLVER_MLW_M3_2D else 7
+        self._keep = [np.ascontiguousarray(grid[k], dtype=np.float64)
+                      for k in ("dx", "dxm", "dy", "dym")]
+        dx, dxm, dy, dym = self._keep
+        d = _Desc(solver, dx.size, dy.size, 1, margin, gm, qav,
+                  dx.ctypes.data_as(_dp), dxm.ctypes.data_as(_dp),
+                  dy.ctypes.data_as(_dp), dym.ctypes.data_as(_dp), None, None,
+                  1 if exact else 0, tile, C.c_void_p(stream) if stream else None)
+        self.shape = (dx.size, dy.size)
+        h = C.c_void_p()
+        _check(self.lib.cans_run_create(C.byref(h), C.byref(d)), "cans_run_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.cans_run_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_bc(self, var: int, face: int, kind: int, q0: float = 0.0):
+        _check(self.lib.cans_run_set_bc(self.h, var, face, kind, q0), "cans_run_set_bc")
+
+    def set_bc_program(self, program):
+        """program: iterable of (var, face, kind, q0)."""
+        for var, face, kind, q0 in program:
+            self.set_bc(var, face, kind, q0)
+
+    def push(self, arrays):
+        arr = (_dp * self.nvar)(*[_ptr(a) for a in arrays])
+        _check(self.lib.cans_run_push(self.h, arr), "cans_run_push")
+
+    def pull(self, arrays=None):
+        if arrays is None:
+            arrays = [np.zeros(self.shape, order="F") for _ in range(self.nvar)]
+        arr = (_dp * self.nvar)(*[_ptr(a) for a in arrays])
+        _check(self.lib.cans_run_pull(self.h, arr), "cans_run_pull")
+        return arrays
+
+    def start(self, t0=0.0, tend=1e30, nstop=10 ** 12, safety=0.4, dtmin=1e-10,
+              dtout=0.0, pause_on_output=False):
+        _check(self.lib.cans_run_start(self.h, t0, tend, nstop, safety, dtmin, dtout,
+                                       1 if pause_on_output else 0), "cans_run_start")
+
+    def advance(self, iters: int):
+        _check(self.lib.cans_run_advance(self.h, iters), "cans_run_advance")
+
+    def query(self) -> RunState:
+        st = RunState()
+        rc = self.lib.cans_run_query(self.h, C.byref(st))
+        if rc not in (CANS_OK, CANS_ERR_DTMIN):
+            _check(rc, "cans_run_query")
+        return st
+
+    def resume(self):
+        _check(self.lib.cans_run_resume(self.h), "cans_run_resume")
+
+    def step(self, dt: float, apply_bc: bool = True):
+        _check(self.lib.cans_run_step(self.h, _dref(dt), 1 if apply_bc else 0), "cans_run_step")
+
+    def cfl(self, safety: float) -> float:
+        dt = C.c_double(0.0)
+        _check(self.lib.cans_run_cfl(self.h, safety, C.byref(dt)), "cans_run_cfl")
+        return dt.value
+
+    def autotune(self, trial_steps: int = 5) -> int:
+        t = C.c_int(0)
+        _check(self.lib.cans_run_autotune(self.h, trial_steps, C.byref(t)), "cans_run_autotune")
+        return t.value
+
+    def profile(self, iters: int):
+        """(summed step-kernel ms, summed iteration ms) over `iters` un-graphed
+        iterations timed with CUDA events on the run's stream."""
+        a, b = C.c_double(0.0), C.c_double(0.0)
+        _check(self.lib.cans_run_profile(self.h, iters, C.byref(a), C.byref(b)),
+               "cans_run_profile")
+        return a.value, b.value
+
+
+def measure_fp64_tflops() -> float:
+    x = C.c_double(0.0)
+    _check(load().cans_measure_fp64_tflops(C.byref(x)), "cans_measure_fp64_tflops")
+    return x.value

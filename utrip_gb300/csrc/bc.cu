@@ -1,0 +1,189 @@
+// On-device ghost-cell fill (the reference bd* routines) and the run-start
+// kernel of the device time loop.
+//
+// Every bd* routine applies one rule to each grid line that runs along its
+// axis (cans2d/bc/bdperx.f:33-46, bdsppx.f:31-47, bdsmnx.f:31-55, bdfrex.f,
+// bdcnsx.f, bdfrdx.f and their y/z and 1-D/3-D twins), so one device function
+// serves every family and dimension.  A boundary program (BcTable) applies
+// the rules of all variables axis by axis, x first, as the model packages'
+// bnd routines do (cans2d/md_mhdkh/hdmlw/bnd.f:11-39).
+#include <cuda_runtime.h>
+
+#include "cans_common.cuh"
+#include "cans_internal.h"
+
+namespace cans {
+
+// One rule on one line: q(l), l = 1..n, at stride `stride`.
+__device__ __forceinline__ void bd_line(int kind, int mbnd, int m0, int m1,
+                                        double *q, int n, size_t stride,
+                                        double q0, const double *dxm) {
+#define QL(l) q[(size_t)((l)-1) * stride]
+  if (kind == BD_PER) {  // bdperx(margin0, margin1)
+    const int b0 = 1 + m0, b1 = n - m1;
+    if (mbnd == 0)
+      for (int i = 1; i <= m0; i++) QL(b0 - i) = QL(b1 + 1 - i);
+    else
+      for (int i = 1; i <= m1; i++) QL(b1 + i) = QL(b0 - 1 + i);
+    return;
+  }
+  const int m = (mbnd == 0) ? m0 : m1;
+  if (mbnd == 0) {
+    const int b = 1 + m;
+    switch (kind) {
+      case BD_SPP: for (int i = 1; i <= m; i++) QL(b - i) = QL(b - 1 + i); break;
+      case BD_SPN: for (int i = 1; i <= m; i++) QL(b - i) = -QL(b - 1 + i); break;
+      case BD_SMP: for (int i = 1; i <= m; i++) QL(b - i) = QL(b + i); break;
+      case BD_SMN:
+        for (int i = 1; i <= m; i++) QL(b - i) = -QL(b + i);
+        QL(b) = 0.;
+        break;
+      case BD_FRE: for (int i = 1; i <= m; i++) QL(b - i) = QL(b); break;
+      case BD_CNS: for (int i = 1; i <= m; i++) QL(b - i) = q0; break;
+      case BD_FRD:
+        for (int i = 1; i <= m; i++) {
+          const double dqq = __ddiv_rn(__dsub_rn(QL(b + 1), QL(b)), dxm[b - 1]);
+          QL(b - i) = __dsub_rn(QL(b - i + 1), __dmul_rn(dqq, dxm[b - i - 1]));
+        }
+        break;
+      default: break;
+    }
+  } else {
+    const int b = n - m;
+    switch (kind) {
+      case BD_SPP: for (int i = 1; i <= m; i++) QL(b + i) = QL(b + 1 - i); break;
+      case BD_SPN: for (int i = 1; i <= m; i++) QL(b + i) = -QL(b + 1 - i); break;
+      case BD_SMP: for (int i = 1; i <= m; i++) QL(b + i) = QL(b - i); break;
+      case BD_SMN:
+        for (int i = 1; i <= m; i++) QL(b + i) = -QL(b - i);
+        QL(b) = 0.;
+        break;
+      case BD_FRE: for (int i = 1; i <= m; i++) QL(b + i) = QL(b); break;
+      case BD_CNS: for (int i = 1; i <= m; i++) QL(b + i) = q0; break;
+      case BD_FRD:
+        for (int i = 1; i <= m; i++) {
+          const double dqq = __ddiv_rn(__dsub_rn(QL(b), QL(b - 1)), dxm[b - 2]);
+          QL(b + i) = __dadd_rn(QL(b + i - 1), __dmul_rn(dqq, dxm[b + i - 2]));
+        }
+        break;
+      default: break;
+    }
+  }
+#undef QL
+}
+
+// Lines along `axis` of an (n0, n1, n2) array: line index -> base offset.
+__device__ __forceinline__ size_t line_base(int axis, long long line, int n0,
+                                            int n1) {
+  if (axis == 0) return (size_t)line * n0;                 // (j,k) -> j*n0 + k*n0*n1
+  if (axis == 1) {
+    const long long i = line % n0, k = line / n0;
+    return (size_t)i + (size_t)k * n0 * n1;
+  }
+  return (size_t)line;                                     // (i,j) plane index
+}
+
+// Boundary program of one axis over all variables: thread per (var, line).
+__global__ void k_bc_axis(int nvar, double *S, int n0, int n1, int n2,
+                          int axis, BcTable bc, const double *dxm,
+                          const Ctl *ctl) {
+  if (ctl != nullptr) {
+    if (ctl->done | ctl->pause) return;
+    S = ctl->buf[ctl->cur ^ 1];  // the state the step just wrote
+  }
+  const int dims[3] = {n0, n1, n2};
+  const int n = dims[axis];
+  const size_t stride = axis == 0 ? 1 : (axis == 1 ? (size_t)n0 : (size_t)n0 * n1);
+  const long long nlines = (long long)n0 * n1 * n2 / n;
+  const size_t nall = (size_t)n0 * n1 * n2;
+  const long long total = nlines * nvar;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(t / nlines);
+    const long long line = t % nlines;
+    double *q = S + (size_t)v * nall + line_base(axis, line, n0, n1);
+    const int klo = bc.kind[v][2 * axis], khi = bc.kind[v][2 * axis + 1];
+    if (klo >= 0)
+      bd_line(klo, 0, bc.margin, bc.margin, q, n, stride, bc.q0[v][2 * axis], dxm);
+    if (khi >= 0)
+      bd_line(khi, 1, bc.margin, bc.margin, q, n, stride, bc.q0[v][2 * axis + 1], dxm);
+  }
+}
+
+static cudaError_t bc_axis(int nvar, double *S, int n0, int n1, int n2,
+                           int axis, const BcTable &bc, const double *dxm,
+                           const Ctl *ctl, cudaStream_t s) {
+  const int dims[3] = {n0, n1, n2};
+  const long long total = (long long)n0 * n1 * n2 / dims[axis] * nvar;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  k_bc_axis<<<blocks, 256, 0, s>>>(nvar, S, n0, n1, n2, axis, bc, dxm, ctl);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc2d(int nvar, double *S, int ix, int jx, const Axis &ax,
+                        const Axis &ay, const BcTable &bc, const Ctl *ctl,
+                        cudaStream_t s) {
+  cudaError_t e = bc_axis(nvar, S, ix, jx, 1, 0, bc, ax.dm, ctl, s);
+  if (e != cudaSuccess) return e;
+  return bc_axis(nvar, S, ix, jx, 1, 1, bc, ay.dm, ctl, s);
+}
+
+// A single reference bd* call on one array: thread per line.
+__global__ void k_bd_one(int kind, int axis, int mbnd, int m0, int m1,
+                         double *q, double q0, const double *dxm, int n0,
+                         int n1, int n2) {
+  const int dims[3] = {n0, n1, n2};
+  const int n = dims[axis];
+  const size_t stride = axis == 0 ? 1 : (axis == 1 ? (size_t)n0 : (size_t)n0 * n1);
+  const long long nlines = (long long)n0 * n1 * n2 / n;
+  for (long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       line < nlines; line += (long long)gridDim.x * blockDim.x) {
+    bd_line(kind, mbnd, m0, m1, q + line_base(axis, line, n0, n1), n, stride,
+            q0, dxm);
+  }
+}
+
+cudaError_t launch_bd_one(int kind, int axis, int mbnd, int margin0,
+                          int margin1, double *q, double q0, const double *dxm,
+                          int n0, int n1, int n2, cudaStream_t s) {
+  const int dims[3] = {n0, n1, n2};
+  const long long nlines = (long long)n0 * n1 * n2 / dims[axis];
+  int blocks = (int)((nlines + 255) / 256);
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  k_bd_one<<<blocks, 256, 0, s>>>(kind, axis, mbnd, margin0, margin1, q, q0,
+                                  dxm, n0, n1, n2);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Start of the first loop iteration (main.f:161-173): ns+=1, dt from the CFL
+// minimum already reduced into ctl->cfl_bits, the dtmin test, tp=t, t+=dt.
+__global__ void k_prepare(Ctl *ctl) {
+  // The reference loop tests its condition at the end of the body, so the
+  // first iteration always starts.
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (ctl->done) return;
+  ctl->ns += 1;
+  const double dt = __longlong_as_double((long long)ctl->cfl_bits);
+  ctl->dt = dt;
+  ctl->cfl_bits = 0x7ff0000000000000ull;
+  if (dt < ctl->dtmin) {
+    ctl->merr = 9001;
+    ctl->done = 1;
+    return;
+  }
+  ctl->tp = ctl->t;
+  ctl->t = ctl->t + dt;
+}
+
+cudaError_t launch_prepare(Ctl *ctl, cudaStream_t s) {
+  k_prepare<<<1, 32, 0, s>>>(ctl);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace cans

@@ -1,0 +1,126 @@
+// Shared device-side definitions for the CANS mLW GPU library (sm_103a).
+//
+// Two arithmetic policies are compiled from one source:
+//   exact (E=true)  every + - * / and sqrt is an explicitly rounded intrinsic
+//                   (__dadd_rn, __dmul_rn, ...), so nothing is contracted into
+//                   an FMA and the order written is the order executed.  With
+//                   the expressions written as in the reference Fortran this
+//                   reproduces a -ffp-contract=off CPU build bit for bit.
+//   fast  (E=false) plain double operators: the compiler contracts into FMA,
+//                   and the kernels replace divisions by one reciprocal per
+//                   cell where the reference divides several times.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cans {
+
+template <bool E> struct F {
+  double v;
+  __device__ __forceinline__ F() {}
+  __device__ __forceinline__ F(double x) : v(x) {}
+};
+
+#define CANS_BINOP(OP, RN)                                                     \
+  template <bool E> __device__ __forceinline__ F<E> operator OP(F<E> a, F<E> b) { \
+    if constexpr (E) return F<E>(RN(a.v, b.v));                                \
+    else return F<E>(a.v OP b.v);                                              \
+  }                                                                            \
+  template <bool E> __device__ __forceinline__ F<E> operator OP(double a, F<E> b) { \
+    return F<E>(a) OP b;                                                       \
+  }                                                                            \
+  template <bool E> __device__ __forceinline__ F<E> operator OP(F<E> a, double b) { \
+    return a OP F<E>(b);                                                       \
+  }
+CANS_BINOP(+, __dadd_rn)
+CANS_BINOP(-, __dsub_rn)
+CANS_BINOP(*, __dmul_rn)
+CANS_BINOP(/, __ddiv_rn)
+#undef CANS_BINOP
+
+template <bool E> __device__ __forceinline__ F<E> operator-(F<E> a) {
+  return F<E>(-a.v);
+}
+template <bool E> __device__ __forceinline__ F<E> fsqrt(F<E> a) {
+  if constexpr (E) return F<E>(__dsqrt_rn(a.v));
+  else return F<E>(sqrt(a.v));
+}
+template <bool E> __device__ __forceinline__ F<E> fabs_(F<E> a) {
+  return F<E>(fabs(a.v));
+}
+// Fortran max(zero, a) on finite values
+template <bool E> __device__ __forceinline__ F<E> max0(F<E> a) {
+  return F<E>(a.v > 0.0 ? a.v : 0.0);
+}
+template <bool E> __device__ __forceinline__ F<E> fmin_(F<E> a, F<E> b) {
+  return F<E>(a.v < b.v ? a.v : b.v);
+}
+
+// 1.0e-4 as the single-precision literal of the reference artificial
+// viscosity threshold, widened to double.
+#define CANS_AV_EPS ((double)1.0e-4f)
+
+// Device control block of a resident run: the time-loop state of the
+// reference driver (ns, t, dt, merr) lives here so that no per-step host
+// round trip is needed.
+struct Ctl {
+  double dt;        // time step used by the next step kernel
+  double t;         // current time (after the step that dt belongs to)
+  double tp;        // time before that step
+  double tend;      // loop ends when t >= tend
+  double dtmin;     // merr=9001 when dt < dtmin
+  double safety;    // CFL safety factor
+  double dtout;     // pause for output when int(tp/dtout) < int(t/dtout)
+  unsigned long long cfl_bits;  // running CFL minimum (bit pattern, >= 0)
+  long long ns;     // steps taken
+  long long nstop;  // loop ends when ns >= nstop
+  int merr;         // 0, or 9001 (dt < dtmin)
+  int done;         // 1: loop finished (tend/nstop/merr); kernels are no-ops
+  int pause;        // 1: an output time was crossed; host clears it
+  int pause_on_output;
+  unsigned int frame_blocks_done;  // last-block detection in the frame kernel
+  int nonfinite;    // count of non-finite / non-positive pressures seen
+  // Double-buffered state: a step reads buf[cur] and writes buf[cur^1]; the
+  // frame kernel flips cur once the boundary fill and CFL are done, so the
+  // same captured graph serves every iteration.
+  double *buf[2];
+  int cur;
+  long long nexec;  // steps executed since the run started
+};
+
+// Positive doubles order like their unsigned bit patterns.
+__device__ __forceinline__ void atomic_min_pos(unsigned long long *addr,
+                                               double v) {
+  // NaN never compares below the running minimum, as in the reference
+  // `if (dtq .lt. dt)`.
+  if (!(v >= 0.0)) return;
+  atomicMin(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w < v || v != v) ? w : v;   // a NaN never survives a finite value
+  }
+  return v;
+}
+
+// Block-wide minimum reduced into one atomicMin.  All threads of the block
+// must call it; tid is the linear thread index, nthreads the block size.
+__device__ __forceinline__ void block_min_to(unsigned long long *addr,
+                                             double v, double *red, int tid,
+                                             int nthreads) {
+  v = warp_min(v);
+  const int lane = tid & 31, w = tid >> 5;
+  const int nw = (nthreads + 31) >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double x = (lane < nw) ? red[lane] : __longlong_as_double(0x7ff0000000000000LL);
+    x = warp_min(x);
+    if (lane == 0) atomic_min_pos(addr, x);
+  }
+}
+
+}  // namespace cans

@@ -1,0 +1,87 @@
+// Internal host-side declarations shared by the kernel translation units and
+// the C-ABI layer.  Not part of the public interface (include/cans_gpu.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cans_common.cuh"
+
+namespace cans {
+
+// Device copies of the per-axis metric arrays of the reference step
+// (cans2d/hdmlw/mlw_m3.f:70-86): spacing d/dm, their inverses di/dim and
+// the corner weights u0/u1, plus the host copies they were computed from.
+struct Axis {
+  int n = 0;
+  double *d = nullptr, *dm = nullptr, *di = nullptr, *dim = nullptr,
+         *u0 = nullptr, *u1 = nullptr;
+};
+
+// Physical constants of one run, computed on the host exactly as the
+// reference computes them.
+struct Phys {
+  double gm, gm1, gm1i, ggm1, pi8i, pi4i, qav;
+  double pi4i_cfl;  // 3-D cfl_m uses a single-precision pi
+};
+
+// Boundary program: per variable and face (x-lo, x-hi, y-lo, y-hi, z-lo,
+// z-hi) a bd* kind and its constant; applied axis by axis (x, then y, then z)
+// after each step, as the reference model packages do.
+constexpr int kMaxVar = 9;
+struct BcTable {
+  int margin;
+  int kind[kMaxVar][6];
+  double q0[kMaxVar][6];
+};
+
+enum BdKind { BD_NONE = -1, BD_PER = 0, BD_SPP = 1, BD_SPN = 2, BD_SMP = 3,
+              BD_SMN = 4, BD_FRE = 5, BD_CNS = 6, BD_FRD = 7 };
+
+// Region whose CFL the step kernel reduces (0-based inclusive box).  Cells
+// outside it are reduced after the boundary fill by the frame kernel.
+struct Box3 { int lo[3], hi[3]; };
+
+// ---- 2-D ------------------------------------------------------------------
+// solver: 0 = mlw_m (7 arrays), 1 = mlw_m3 (9 arrays).  A and B hold nvar
+// contiguous arrays of ix*jx doubles.  If ctl is non-null the kernel takes dt
+// from it, skips when the run is done or paused, and reduces the CFL of the
+// cells inside `box` into ctl->cfl_bits.
+cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
+                         double *B, int ix, int jx, const Axis &ax,
+                         const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
+                         Box3 box, cudaStream_t s);
+int mlw2d_tile_count();
+cudaError_t launch_cfl2d_full(int solver, bool exact, const double *S, int ix,
+                              int jx, const Axis &ax, const Axis &ay,
+                              const Phys &ph, double safety,
+                              unsigned long long *out_bits, cudaStream_t s);
+cudaError_t launch_bc2d(int nvar, double *S, int ix, int jx, const Axis &ax,
+                        const Axis &ay, const BcTable &bc, const Ctl *ctl,
+                        cudaStream_t s);
+cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
+                           int jx, const Axis &ax, const Axis &ay,
+                           const Phys &ph, int margin, Ctl *ctl,
+                           cudaStream_t s);
+
+// ---- single bd* operation on one array (literal entry points) -------------
+// kind/axis/mbnd follow the reference routine; dims = (n0, n1, n2).
+cudaError_t launch_bd_one(int kind, int axis, int mbnd, int margin0,
+                          int margin1, double *q, double q0, const double *dxm,
+                          int n0, int n1, int n2, cudaStream_t s);
+
+// ---- control block helpers --------------------------------------------------
+// Start of the reference loop body: ns+=1, dt from the CFL minimum, the dtmin
+// test, tp=t, t+=dt.  Runs on one thread.
+cudaError_t launch_prepare(Ctl *ctl, cudaStream_t s);
+
+// Host-side metric construction with the reference expressions.
+void build_axis_host(int n, const double *d, const double *dm, double *di,
+                     double *dim, double *u0, double *u1);
+Phys make_phys(double gm, double qav);
+
+// Kernel-launch counter (all launches issued by this library).
+void count_launch(int n = 1);
+unsigned long long launch_count();
+
+}  // namespace cans

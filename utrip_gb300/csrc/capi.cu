@@ -1,0 +1,927 @@
+// C-ABI layer: drop-in entry points with the reference argument lists, the
+// residency registry, and the device-resident run handle.
+//
+// Host-side bookkeeping mirrors the reference drivers (for example
+// cans2d/md_mhdkh/hdmlw/main.f:160-219): cfl -> t += dt -> step -> bnd ->
+// output test -> loop test.  The run handle keeps that loop on the device
+// and replays it as a CUDA graph; the drop-in entry points serve a Fortran
+// driver that still calls cfl_m3 / mlw_m3 / bd* once per step.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "cans_gpu.h"
+#include "cans_internal.h"
+
+namespace cans {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(int n) { g_launches += (unsigned long long)n; }
+unsigned long long launch_count() { return g_launches.load(); }
+
+// Reference metric set-up (cans2d/hdmlw/mlw_m3.f:70-86).  Index 0 and n-1 of
+// u0/u1 are never read by the step.
+void build_axis_host(int n, const double *d, const double *dm, double *di,
+                     double *dim, double *u0, double *u1) {
+  for (int i = 0; i < n; i++) {
+    di[i] = 1.0 / d[i];
+    dim[i] = 1.0 / dm[i];
+    u0[i] = 0.0;
+    u1[i] = 0.0;
+  }
+  for (int i = 1; i < n - 1; i++) {
+    u1[i] = 0.5 * dm[i - 1] / d[i];
+    u0[i] = 0.5 * dm[i] / d[i];
+  }
+}
+
+Phys make_phys(double gm, double qav) {
+  Phys p;
+  const double pi = std::acos(-1.0);
+  p.gm = gm;
+  p.gm1 = gm - 1;
+  p.gm1i = 1.0 / p.gm1;
+  p.ggm1 = gm / p.gm1;
+  p.pi8i = 1. / pi / 8.;
+  p.pi4i = 1. / pi / 4.;
+  p.qav = qav;
+  p.pi4i_cfl = 0.25 / (double)std::acos(-1.0f);  // cans3d/common/cfl_m.f:39-40
+  return p;
+}
+
+}  // namespace cans
+
+using namespace cans;
+
+// ---------------------------------------------------------------------------
+// Library state
+namespace {
+
+thread_local std::string g_last_error;
+std::mutex g_mu;
+int g_exact = -1;            // -1: read CANS_GPU_EXACT on first use
+cudaStream_t g_stream = nullptr;
+bool g_stream_user = false;
+
+int fail_cuda(cudaError_t e, const char *where) {
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return CANS_ERR_CUDA;
+}
+#define CK(call)                                             \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return fail_cuda(_e, #call);      \
+  } while (0)
+
+int exact_mode() {
+  if (g_exact < 0) {
+    const char *s = std::getenv("CANS_GPU_EXACT");
+    g_exact = (s && s[0] == '1') ? 1 : 0;
+  }
+  return g_exact;
+}
+
+int lib_stream(cudaStream_t *s) {
+  if (!g_stream && !g_stream_user) {
+    CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+  }
+  *s = g_stream;
+  return CANS_OK;
+}
+
+// Device metric arrays of one axis (six arrays in one allocation).
+struct DevAxis {
+  Axis a;
+  double *mem = nullptr;
+  int cap = 0;
+  std::vector<double> h;  // host staging: d, dm, di, dim, u0, u1
+  int ensure(int n) {
+    if (cap < n) {
+      if (mem) cudaFree(mem);
+      mem = nullptr;
+      cap = 0;
+      CK(cudaMalloc(&mem, sizeof(double) * 6 * (size_t)n));
+      cap = n;
+    }
+    a.n = n;
+    a.d = mem;
+    a.dm = mem + n;
+    a.di = mem + 2 * n;
+    a.dim = mem + 3 * n;
+    a.u0 = mem + 4 * n;
+    a.u1 = mem + 5 * n;
+    return CANS_OK;
+  }
+  // Upload d and dm, plus the derived arrays computed on the host with the
+  // reference expressions.
+  int upload(int n, const double *d, const double *dm, cudaStream_t s) {
+    int rc = ensure(n);
+    if (rc) return rc;
+    h.assign(6 * (size_t)n, 0.0);
+    std::memcpy(h.data(), d, sizeof(double) * n);
+    std::memcpy(h.data() + n, dm, sizeof(double) * n);
+    build_axis_host(n, d, dm, h.data() + 2 * n, h.data() + 3 * n,
+                    h.data() + 4 * n, h.data() + 5 * n);
+    CK(cudaMemcpyAsync(mem, h.data(), sizeof(double) * 6 * (size_t)n,
+                       cudaMemcpyHostToDevice, s));
+    return CANS_OK;
+  }
+  void release() {
+    if (mem) cudaFree(mem);
+    mem = nullptr;
+    cap = 0;
+  }
+};
+
+// Scratch of the non-resident drop-in calls: state buffers and metrics,
+// reused while the sizes stay the same.
+struct Scratch {
+  double *A = nullptr, *B = nullptr;
+  size_t cap = 0;  // doubles per buffer
+  DevAxis ax, ay, az;
+  unsigned long long *bits = nullptr;
+  int ensure(size_t ndoubles) {
+    if (cap < ndoubles) {
+      if (A) cudaFree(A);
+      if (B) cudaFree(B);
+      A = B = nullptr;
+      cap = 0;
+      CK(cudaMalloc(&A, sizeof(double) * ndoubles));
+      CK(cudaMalloc(&B, sizeof(double) * ndoubles));
+      cap = ndoubles;
+    }
+    if (!bits) CK(cudaMalloc(&bits, sizeof(unsigned long long) * 2));
+    return CANS_OK;
+  }
+};
+Scratch g_scratch;
+
+// Registered host-array sets and their device mirrors.
+struct MirrorSet {
+  int n0 = 1, n1 = 1, n2 = 1, narr = 0;
+  size_t n = 0;
+  std::vector<double *> host;
+  double *buf[2] = {nullptr, nullptr};
+  int cur = 0;
+  DevAxis ax, ay, az;
+  unsigned long long *bits = nullptr;
+  double *arr(int v) { return buf[cur] + (size_t)v * n; }
+};
+std::unordered_map<const double *, std::pair<MirrorSet *, int>> g_registry;
+
+MirrorSet *find_set(const double *p, int *var) {
+  auto it = g_registry.find(p);
+  if (it == g_registry.end()) return nullptr;
+  if (var) *var = it->second.second;
+  return it->second.first;
+}
+
+// The step's arrays are resident if they are the first nvar arrays of one
+// set, in order.
+MirrorSet *resident_step_set(double *const *arrs, int nvar) {
+  int v0 = -1;
+  MirrorSet *m = find_set(arrs[0], &v0);
+  if (!m || v0 != 0 || m->narr < nvar) return nullptr;
+  for (int v = 1; v < nvar; v++) {
+    int vv = -1;
+    if (find_set(arrs[v], &vv) != m || vv != v) return nullptr;
+  }
+  return m;
+}
+
+double bits_to_double(unsigned long long b) {
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+// ---- generic 2-D step (drop-in) -------------------------------------------
+int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
+           double gm, const double *dx, const double *dxm, int ix,
+           const double *dy, const double *dym, int jx) {
+  if (ix < 3 || jx < 3) return CANS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(gm, qav);
+  const size_t n = (size_t)ix * jx;
+  Box3 box{};
+  MirrorSet *m = resident_step_set(arrs, nvar);
+  if (m) {
+    if ((rc = m->ax.upload(ix, dx, dxm, s))) return rc;
+    if ((rc = m->ay.upload(jx, dy, dym, s))) return rc;
+    CK(launch_mlw2d(solver, exact_mode(), 0, m->buf[m->cur], m->buf[m->cur ^ 1],
+                    ix, jx, m->ax.a, m->ay.a, ph, dt, nullptr, box, s));
+    m->cur ^= 1;
+    return CANS_OK;
+  }
+  if ((rc = g_scratch.ensure((size_t)nvar * n))) return rc;
+  for (int v = 0; v < nvar; v++)
+    CK(cudaMemcpyAsync(g_scratch.A + v * n, arrs[v], sizeof(double) * n,
+                       cudaMemcpyHostToDevice, s));
+  if ((rc = g_scratch.ax.upload(ix, dx, dxm, s))) return rc;
+  if ((rc = g_scratch.ay.upload(jx, dy, dym, s))) return rc;
+  CK(launch_mlw2d(solver, exact_mode(), 0, g_scratch.A, g_scratch.B, ix, jx,
+                  g_scratch.ax.a, g_scratch.ay.a, ph, dt, nullptr, box, s));
+  for (int v = 0; v < nvar; v++)
+    CK(cudaMemcpyAsync(arrs[v], g_scratch.B + v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+int cfl2d(int solver, double *dt, double safety, double dtmin, int *merr,
+          double gm, const double *const *arrs, int nvar, const double *dx,
+          int ix, const double *dy, int jx) {
+  if (ix < 1 || jx < 1) return CANS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(gm, 0.0);
+  const size_t n = (size_t)ix * jx;
+  // cfl reads only d (dx, dy); dm is passed as the same array for the
+  // derived metrics, which the CFL never reads.
+  const double *base = nullptr;
+  Axis ax, ay;
+  unsigned long long *bits = nullptr;
+  MirrorSet *m = resident_step_set(const_cast<double *const *>(arrs), nvar);
+  if (m) {
+    if ((rc = m->ax.upload(ix, dx, dx, s))) return rc;
+    if ((rc = m->ay.upload(jx, dy, dy, s))) return rc;
+    if (!m->bits) CK(cudaMalloc(&m->bits, sizeof(unsigned long long)));
+    base = m->buf[m->cur];
+    ax = m->ax.a;
+    ay = m->ay.a;
+    bits = m->bits;
+  } else {
+    if ((rc = g_scratch.ensure((size_t)nvar * n))) return rc;
+    for (int v = 0; v < nvar; v++)
+      CK(cudaMemcpyAsync(g_scratch.A + v * n, arrs[v], sizeof(double) * n,
+                         cudaMemcpyHostToDevice, s));
+    if ((rc = g_scratch.ax.upload(ix, dx, dx, s))) return rc;
+    if ((rc = g_scratch.ay.upload(jx, dy, dy, s))) return rc;
+    base = g_scratch.A;
+    ax = g_scratch.ax.a;
+    ay = g_scratch.ay.a;
+    bits = g_scratch.bits;
+  }
+  // dt = 1.e20 (real*4) is the starting minimum of the reference scan
+  const unsigned long long init = [] {
+    double d = (double)1.e20f;
+    unsigned long long b;
+    std::memcpy(&b, &d, sizeof b);
+    return b;
+  }();
+  CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, s));
+  CK(launch_cfl2d_full(solver, exact_mode(), base, ix, jx, ax, ay, ph, safety,
+                       bits, s));
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *dt = bits_to_double(out);
+  *merr = (*dt < dtmin) ? 9001 : 0;
+  return CANS_OK;
+}
+
+// One reference bd* call.  dims = (n0, n1, n2).
+int bd_call(int kind, int axis, int mbnd, int m0, int m1, double *qq,
+            double q0, const double *dxm, int n0, int n1, int n2) {
+  if (n0 < 1 || n1 < 1 || n2 < 1) return CANS_ERR_ARG;
+  const int dims[3] = {n0, n1, n2};
+  if (m0 < 0 || m1 < 0 || m0 + m1 > dims[axis]) return CANS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const size_t n = (size_t)n0 * n1 * n2;
+  const double *ddxm = nullptr;
+  int var = -1;
+  MirrorSet *m = find_set(qq, &var);
+  DevAxis *dax = nullptr;
+  if (m) dax = axis == 0 ? &m->ax : (axis == 1 ? &m->ay : &m->az);
+  else dax = axis == 0 ? &g_scratch.ax : (axis == 1 ? &g_scratch.ay : &g_scratch.az);
+  if (kind == BD_FRD) {
+    if ((rc = dax->upload(dims[axis], dxm, dxm, s))) return rc;
+    ddxm = dax->a.dm;
+  }
+  if (m) {
+    CK(launch_bd_one(kind, axis, mbnd, m0, m1, m->arr(var), q0, ddxm, n0, n1,
+                     n2, s));
+    return CANS_OK;
+  }
+  if ((rc = g_scratch.ensure(n))) return rc;
+  CK(cudaMemcpyAsync(g_scratch.A, qq, sizeof(double) * n,
+                     cudaMemcpyHostToDevice, s));
+  CK(launch_bd_one(kind, axis, mbnd, m0, m1, g_scratch.A, q0, ddxm, n0, n1, n2,
+                   s));
+  CK(cudaMemcpyAsync(qq, g_scratch.A, sizeof(double) * n,
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Settings
+extern "C" int cans_set_exact(int exact) {
+  g_exact = exact ? 1 : 0;
+  return CANS_OK;
+}
+extern "C" int cans_get_exact(void) { return exact_mode(); }
+extern "C" int cans_set_stream(void *stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_stream = (cudaStream_t)stream;
+  g_stream_user = (stream != nullptr);
+  return CANS_OK;
+}
+extern "C" const char *cans_last_error(void) { return g_last_error.c_str(); }
+extern "C" unsigned long long cans_launch_count(void) { return launch_count(); }
+extern "C" int cans_device_ok(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return 0;
+  return (p.major == 10 && p.minor == 3) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// 2-D drop-in entry points
+extern "C" int cans_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
+                              double *vz, double *bx, double *by, double *bz,
+                              double *az, const double *dt, const double *qav,
+                              const double *gm, const double *dx,
+                              const double *dxm, const int *ix,
+                              const double *dy, const double *dym,
+                              const int *jx) {
+  double *arrs[9] = {ro, pr, vx, vy, vz, bx, by, bz, az};
+  return step2d(1, arrs, 9, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx);
+}
+
+extern "C" int cans_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
+                             double *bx, double *by, double *az,
+                             const double *dt, const double *qav,
+                             const double *gm, const double *dx,
+                             const double *dxm, const int *ix,
+                             const double *dy, const double *dym,
+                             const int *jx) {
+  double *arrs[7] = {ro, pr, vx, vy, bx, by, az};
+  return step2d(0, arrs, 7, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx);
+}
+
+extern "C" int cans_cfl_m3_2d(double *dt, const double *safety,
+                              const double *dtmin, int *merr,
+                              const double *gm, const double *ro,
+                              const double *pr, const double *vx,
+                              const double *vy, const double *vz,
+                              const double *bx, const double *by,
+                              const double *bz, const double *dx,
+                              const int *ix, const double *dy,
+                              const int *jx) {
+  const double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  return cfl2d(1, dt, *safety, *dtmin, merr, *gm, arrs, 8, dx, *ix, dy, *jx);
+}
+
+extern "C" int cans_cfl_m_2d(double *dt, const double *safety,
+                             const double *dtmin, int *merr, const double *gm,
+                             const double *ro, const double *pr,
+                             const double *vx, const double *vy,
+                             const double *bx, const double *by,
+                             const double *dx, const int *ix,
+                             const double *dy, const int *jx) {
+  const double *arrs[6] = {ro, pr, vx, vy, bx, by};
+  return cfl2d(0, dt, *safety, *dtmin, merr, *gm, arrs, 6, dx, *ix, dy, *jx);
+}
+
+#define CANS_BD2(NAME, KIND, AXIS)                                              \
+  extern "C" int NAME(const int *mbnd, const int *margin, double *qq,           \
+                      const int *ix, const int *jx) {                           \
+    return bd_call(KIND, AXIS, *mbnd, *margin, *margin, qq, 0.0, nullptr, *ix,  \
+                   *jx, 1);                                                      \
+  }
+CANS_BD2(cans_bdsppx_2d, BD_SPP, 0)
+CANS_BD2(cans_bdsppy_2d, BD_SPP, 1)
+CANS_BD2(cans_bdspnx_2d, BD_SPN, 0)
+CANS_BD2(cans_bdspny_2d, BD_SPN, 1)
+CANS_BD2(cans_bdsmpx_2d, BD_SMP, 0)
+CANS_BD2(cans_bdsmpy_2d, BD_SMP, 1)
+CANS_BD2(cans_bdsmnx_2d, BD_SMN, 0)
+CANS_BD2(cans_bdsmny_2d, BD_SMN, 1)
+CANS_BD2(cans_bdfrex_2d, BD_FRE, 0)
+CANS_BD2(cans_bdfrey_2d, BD_FRE, 1)
+#undef CANS_BD2
+
+extern "C" int cans_bdperx_2d(const int *margin0, const int *margin1,
+                              double *qq, const int *ix, const int *jx) {
+  int rc = bd_call(BD_PER, 0, 0, *margin0, *margin1, qq, 0.0, nullptr, *ix, *jx, 1);
+  if (rc) return rc;
+  return bd_call(BD_PER, 0, 1, *margin0, *margin1, qq, 0.0, nullptr, *ix, *jx, 1);
+}
+extern "C" int cans_bdpery_2d(const int *margin0, const int *margin1,
+                              double *qq, const int *ix, const int *jx) {
+  int rc = bd_call(BD_PER, 1, 0, *margin0, *margin1, qq, 0.0, nullptr, *ix, *jx, 1);
+  if (rc) return rc;
+  return bd_call(BD_PER, 1, 1, *margin0, *margin1, qq, 0.0, nullptr, *ix, *jx, 1);
+}
+extern "C" int cans_bdcnsx_2d(const int *mbnd, const int *margin, double *qq,
+                              const double *q0, const int *ix, const int *jx) {
+  return bd_call(BD_CNS, 0, *mbnd, *margin, *margin, qq, *q0, nullptr, *ix, *jx, 1);
+}
+extern "C" int cans_bdcnsy_2d(const int *mbnd, const int *margin, double *qq,
+                              const double *q0, const int *ix, const int *jx) {
+  return bd_call(BD_CNS, 1, *mbnd, *margin, *margin, qq, *q0, nullptr, *ix, *jx, 1);
+}
+extern "C" int cans_bdfrdx_2d(const int *mbnd, const int *margin, double *qq,
+                              const double *dxm, const int *ix, const int *jx) {
+  return bd_call(BD_FRD, 0, *mbnd, *margin, *margin, qq, 0.0, dxm, *ix, *jx, 1);
+}
+extern "C" int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq,
+                              const double *dym, const int *ix, const int *jx) {
+  return bd_call(BD_FRD, 1, *mbnd, *margin, *margin, qq, 0.0, dym, *ix, *jx, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Residency registry
+extern "C" int cans_gpu_register(double *const *arrays, const int *narr,
+                                 const int *ix, const int *jx, const int *kx) {
+  if (!arrays || *narr < 1 || *ix < 1 || *jx < 1 || *kx < 1) return CANS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (int v = 0; v < *narr; v++)
+    if (!arrays[v] || g_registry.count(arrays[v])) return CANS_ERR_ARG;
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  auto *m = new MirrorSet();
+  m->n0 = *ix;
+  m->n1 = *jx;
+  m->n2 = *kx;
+  m->narr = *narr;
+  m->n = (size_t)*ix * *jx * *kx;
+  m->host.assign(arrays, arrays + *narr);
+  for (int b = 0; b < 2; b++) {
+    cudaError_t e = cudaMalloc(&m->buf[b], sizeof(double) * m->n * m->narr);
+    if (e != cudaSuccess) {
+      if (m->buf[0]) cudaFree(m->buf[0]);
+      delete m;
+      return fail_cuda(e, "cudaMalloc(mirror)");
+    }
+  }
+  for (int v = 0; v < m->narr; v++) {
+    CK(cudaMemcpyAsync(m->buf[0] + v * m->n, arrays[v], sizeof(double) * m->n,
+                       cudaMemcpyHostToDevice, s));
+    g_registry[arrays[v]] = {m, v};
+  }
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+static int mirror_copy(const double *any, bool to_host) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  MirrorSet *m = find_set(any, nullptr);
+  if (!m) return CANS_ERR_ARG;
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  for (int v = 0; v < m->narr; v++) {
+    if (to_host)
+      CK(cudaMemcpyAsync(m->host[v], m->arr(v), sizeof(double) * m->n,
+                         cudaMemcpyDeviceToHost, s));
+    else
+      CK(cudaMemcpyAsync(m->arr(v), m->host[v], sizeof(double) * m->n,
+                         cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+extern "C" int cans_gpu_pull(const double *any) { return mirror_copy(any, true); }
+extern "C" int cans_gpu_push(const double *any) { return mirror_copy(any, false); }
+
+extern "C" int cans_gpu_release(const double *any) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  MirrorSet *m = find_set(any, nullptr);
+  if (!m) return CANS_ERR_ARG;
+  if (g_stream) cudaStreamSynchronize(g_stream);
+  for (double *h : m->host) g_registry.erase(h);
+  cudaFree(m->buf[0]);
+  cudaFree(m->buf[1]);
+  if (m->bits) cudaFree(m->bits);
+  m->ax.release();
+  m->ay.release();
+  m->az.release();
+  delete m;
+  return CANS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident run handle
+struct cans_run {
+  cans_run_desc d{};
+  int nvar = 0;
+  size_t n = 0;
+  Phys ph{};
+  BcTable bc{};
+  DevAxis ax, ay, az;
+  double *buf[2] = {nullptr, nullptr};
+  Ctl *ctl = nullptr;          // device control block
+  Ctl host_ctl{};              // last copy read back
+  cudaStream_t s = nullptr;
+  bool own_stream = false;
+  int tile = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_iters = 0;
+  int graph_nodes = 0;
+};
+
+namespace {
+
+int solver_nvar(int solver) {
+  switch (solver) {
+    case CANS_SOLVER_MLW_M_2D: return 7;
+    case CANS_SOLVER_MLW_M3_2D: return 9;
+    default: return 0;
+  }
+}
+
+// Kernels of one loop iteration on the device: step, boundary program,
+// frame CFL (+ start of the next iteration).
+int enqueue_iteration(cans_run *h) {
+  const int ix = h->d.ix, jx = h->d.jx;
+  const int w = h->bc.margin + 1;
+  Box3 box{};
+  box.lo[0] = w;
+  box.hi[0] = ix - 1 - w;
+  box.lo[1] = w;
+  box.hi[1] = jx - 1 - w;
+  box.lo[2] = 0;
+  box.hi[2] = 0;
+  CK(launch_mlw2d(h->d.solver, h->d.exact != 0, h->tile, nullptr, nullptr, ix,
+                  jx, h->ax.a, h->ay.a, h->ph, 0.0, h->ctl, box, h->s));
+  CK(launch_bc2d(h->nvar, nullptr, ix, jx, h->ax.a, h->ay.a, h->bc, h->ctl,
+                 h->s));
+  CK(launch_frame2d(h->d.solver, h->d.exact != 0, nullptr, ix, jx, h->ax.a,
+                    h->ay.a, h->ph, h->bc.margin, h->ctl, h->s));
+  return CANS_OK;
+}
+
+void drop_graph(cans_run *h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  h->graph = nullptr;
+  h->graph_iters = 0;
+}
+
+int build_graph(cans_run *h, int iters) {
+  drop_graph(h);
+  cudaGraph_t g = nullptr;
+  const unsigned long long before = launch_count();
+  CK(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+  int rc = CANS_OK;
+  for (int k = 0; k < iters && rc == CANS_OK; k++) rc = enqueue_iteration(h);
+  cudaError_t e = cudaStreamEndCapture(h->s, &g);
+  // captured launches are counted when the graph is replayed
+  g_launches -= (launch_count() - before);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail_cuda(e, "cudaStreamEndCapture");
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail_cuda(e, "cudaGraphInstantiate");
+  h->graph_iters = iters;
+  h->graph_nodes = (int)nn;
+  return CANS_OK;
+}
+
+int read_ctl(cans_run *h) {
+  CK(cudaMemcpyAsync(&h->host_ctl, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost,
+                     h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+}  // namespace
+
+extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
+  if (!out || !d) return CANS_ERR_ARG;
+  const int nvar = solver_nvar(d->solver);
+  if (nvar == 0 || d->ix < 3 || d->jx < 3 || d->kx != 1 || d->margin < 1)
+    return CANS_ERR_ARG;
+  if (!d->dx || !d->dxm || !d->dy || !d->dym) return CANS_ERR_ARG;
+  auto *h = new cans_run();
+  h->d = *d;
+  h->nvar = nvar;
+  h->n = (size_t)d->ix * d->jx;
+  h->ph = make_phys(d->gm, d->qav);
+  h->tile = d->tile >= 0 && d->tile < mlw2d_tile_count() ? d->tile : 0;
+  h->bc.margin = d->margin;
+  for (int v = 0; v < kMaxVar; v++)
+    for (int f = 0; f < 6; f++) {
+      h->bc.kind[v][f] = BD_NONE;
+      h->bc.q0[v][f] = 0.0;
+    }
+  int rc = CANS_OK;
+  auto bail = [&](int code) {
+    cans_run_destroy(h);
+    return code;
+  };
+  if (d->stream) {
+    h->s = (cudaStream_t)d->stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaStreamCreate"));
+    h->own_stream = true;
+  }
+  for (int b = 0; b < 2; b++) {
+    cudaError_t e = cudaMalloc(&h->buf[b], sizeof(double) * h->n * nvar);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(state)"));
+    e = cudaMemsetAsync(h->buf[b], 0, sizeof(double) * h->n * nvar, h->s);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemset(state)"));
+  }
+  cudaError_t e = cudaMalloc(&h->ctl, sizeof(Ctl));
+  if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(ctl)"));
+  if ((rc = h->ax.upload(d->ix, d->dx, d->dxm, h->s))) return bail(rc);
+  if ((rc = h->ay.upload(d->jx, d->dy, d->dym, h->s))) return bail(rc);
+  std::memset(&h->host_ctl, 0, sizeof(Ctl));
+  h->host_ctl.done = 1;
+  h->host_ctl.buf[0] = h->buf[0];
+  h->host_ctl.buf[1] = h->buf[1];
+  e = cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s);
+  if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy(ctl)"));
+  e = cudaStreamSynchronize(h->s);
+  if (e != cudaSuccess) return bail(fail_cuda(e, "cudaStreamSynchronize"));
+  *out = h;
+  return CANS_OK;
+}
+
+extern "C" int cans_run_destroy(cans_run *h) {
+  if (!h) return CANS_ERR_ARG;
+  if (h->s) cudaStreamSynchronize(h->s);
+  drop_graph(h);
+  for (int b = 0; b < 2; b++)
+    if (h->buf[b]) cudaFree(h->buf[b]);
+  if (h->ctl) cudaFree(h->ctl);
+  h->ax.release();
+  h->ay.release();
+  h->az.release();
+  if (h->own_stream && h->s) cudaStreamDestroy(h->s);
+  delete h;
+  return CANS_OK;
+}
+
+extern "C" int cans_run_set_bc(cans_run *h, int var, int face, int kind,
+                               double q0) {
+  if (!h || var < 0 || var >= h->nvar || face < 0 || face >= 4 ||
+      kind < CANS_BD_NONE || kind > CANS_BD_FRD)
+    return CANS_ERR_ARG;
+  h->bc.kind[var][face] = kind;
+  h->bc.q0[var][face] = q0;
+  drop_graph(h);
+  return CANS_OK;
+}
+
+extern "C" int cans_run_push(cans_run *h, double *const *host) {
+  if (!h || !host) return CANS_ERR_ARG;
+  int rc = read_ctl(h);  // learn which buffer is current
+  if (rc) return rc;
+  const int cur = h->host_ctl.cur;
+  for (int v = 0; v < h->nvar; v++)
+    CK(cudaMemcpyAsync(h->buf[cur] + v * h->n, host[v], sizeof(double) * h->n,
+                       cudaMemcpyHostToDevice, h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_pull(cans_run *h, double *const *host) {
+  if (!h || !host) return CANS_ERR_ARG;
+  int rc = read_ctl(h);  // learn which buffer is current
+  if (rc) return rc;
+  const int cur = h->host_ctl.cur;
+  for (int v = 0; v < h->nvar; v++)
+    CK(cudaMemcpyAsync(host[v], h->buf[cur] + v * h->n, sizeof(double) * h->n,
+                       cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_device_state(cans_run *h, double **dev) {
+  if (!h || !dev) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  for (int v = 0; v < h->nvar; v++)
+    dev[v] = h->buf[h->host_ctl.cur] + v * h->n;
+  return CANS_OK;
+}
+
+extern "C" int cans_run_start(cans_run *h, double t0, double tend,
+                              long long nstop, double safety, double dtmin,
+                              double dtout, int pause_on_output) {
+  if (!h) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  Ctl c = h->host_ctl;
+  c.t = t0;
+  c.tp = t0;
+  c.tend = tend;
+  c.nstop = nstop;
+  c.safety = safety;
+  c.dtmin = dtmin;
+  c.dtout = dtout;
+  c.pause_on_output = pause_on_output;
+  c.ns = 0;
+  c.nexec = 0;
+  c.merr = 0;
+  c.done = 0;
+  c.pause = 0;
+  c.frame_blocks_done = 0;
+  c.nonfinite = 0;
+  {
+    double d = (double)1.e20f;  // the reference's starting minimum
+    std::memcpy(&c.cfl_bits, &d, sizeof d);
+  }
+  h->host_ctl = c;
+  CK(cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice,
+                     h->s));
+  CK(launch_cfl2d_full(h->d.solver, h->d.exact != 0, h->buf[c.cur], h->d.ix,
+                       h->d.jx, h->ax.a, h->ay.a, h->ph, safety,
+                       &h->ctl->cfl_bits, h->s));
+  CK(launch_prepare(h->ctl, h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_advance(cans_run *h, int iters) {
+  if (!h || iters < 0) return CANS_ERR_ARG;
+  if (iters == 0) return CANS_OK;
+  const int chunk = iters < 32 ? iters : 32;
+  if (!h->graph || h->graph_iters != chunk) {
+    int rc = build_graph(h, chunk);
+    if (rc) return rc;
+  }
+  int done = 0;
+  while (done + chunk <= iters) {
+    CK(cudaGraphLaunch(h->graph, h->s));
+    count_launch(h->graph_nodes);
+    done += chunk;
+  }
+  for (; done < iters; done++) {
+    int rc = enqueue_iteration(h);
+    if (rc) return rc;
+  }
+  return CANS_OK;
+}
+
+extern "C" int cans_run_query(cans_run *h, cans_run_state *st) {
+  if (!h || !st) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  const Ctl &c = h->host_ctl;
+  st->t = c.t;
+  st->dt = c.dt;
+  st->ns = c.ns;
+  st->nexec = c.nexec;
+  st->merr = c.merr;
+  st->done = c.done;
+  st->pause = c.pause;
+  return c.merr ? c.merr : CANS_OK;
+}
+
+extern "C" int cans_run_resume(cans_run *h) {
+  if (!h) return CANS_ERR_ARG;
+  int zero = 0;
+  CK(cudaMemcpyAsync(&h->ctl->pause, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                     h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_step(cans_run *h, const double *dt, int apply_bc) {
+  if (!h || !dt) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  const int cur = h->host_ctl.cur;
+  Box3 box{};
+  CK(launch_mlw2d(h->d.solver, h->d.exact != 0, h->tile, h->buf[cur],
+                  h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph,
+                  *dt, nullptr, box, h->s));
+  if (apply_bc)
+    CK(launch_bc2d(h->nvar, h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a,
+                   h->ay.a, h->bc, nullptr, h->s));
+  // flip the current buffer on the device copy of the control block
+  const int nc = cur ^ 1;
+  CK(cudaMemcpyAsync(&h->ctl->cur, &nc, sizeof nc, cudaMemcpyHostToDevice,
+                     h->s));
+  h->host_ctl.cur = nc;
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_cfl(cans_run *h, double safety, double *dt) {
+  if (!h || !dt) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  unsigned long long *bits = &h->ctl->cfl_bits;
+  unsigned long long save = h->host_ctl.cfl_bits;
+  double d0 = (double)1.e20f;
+  unsigned long long init;
+  std::memcpy(&init, &d0, sizeof init);
+  CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, h->s));
+  CK(launch_cfl2d_full(h->d.solver, h->d.exact != 0, h->buf[h->host_ctl.cur],
+                       h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph, safety, bits,
+                       h->s));
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, h->s));
+  CK(cudaMemcpyAsync(bits, &save, sizeof save, cudaMemcpyHostToDevice, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  *dt = bits_to_double(out);
+  return CANS_OK;
+}
+
+extern "C" int cans_run_profile(cans_run *h, int iters, double *step_ms,
+                                double *iter_ms) {
+  if (!h || iters < 1 || !step_ms || !iter_ms) return CANS_ERR_ARG;
+  std::vector<cudaEvent_t> ev(3 * (size_t)iters);
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  const int ix = h->d.ix, jx = h->d.jx;
+  const int w = h->bc.margin + 1;
+  Box3 box{};
+  box.lo[0] = w;
+  box.hi[0] = ix - 1 - w;
+  box.lo[1] = w;
+  box.hi[1] = jx - 1 - w;
+  for (int k = 0; k < iters; k++) {
+    CK(cudaEventRecord(ev[3 * k], h->s));
+    CK(launch_mlw2d(h->d.solver, h->d.exact != 0, h->tile, nullptr, nullptr, ix,
+                    jx, h->ax.a, h->ay.a, h->ph, 0.0, h->ctl, box, h->s));
+    CK(cudaEventRecord(ev[3 * k + 1], h->s));
+    CK(launch_bc2d(h->nvar, nullptr, ix, jx, h->ax.a, h->ay.a, h->bc, h->ctl,
+                   h->s));
+    CK(launch_frame2d(h->d.solver, h->d.exact != 0, nullptr, ix, jx, h->ax.a,
+                      h->ay.a, h->ph, h->bc.margin, h->ctl, h->s));
+    CK(cudaEventRecord(ev[3 * k + 2], h->s));
+  }
+  CK(cudaStreamSynchronize(h->s));
+  double s1 = 0.0, s2 = 0.0;
+  for (int k = 0; k < iters; k++) {
+    float a = 0.f, b = 0.f;
+    CK(cudaEventElapsedTime(&a, ev[3 * k], ev[3 * k + 1]));
+    CK(cudaEventElapsedTime(&b, ev[3 * k], ev[3 * k + 2]));
+    s1 += a;
+    s2 += b;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  *step_ms = s1;
+  *iter_ms = s2;
+  return CANS_OK;
+}
+
+extern "C" int cans_run_autotune(cans_run *h, int trial_steps, int *tile) {
+  if (!h || trial_steps < 1) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  const int cur = h->host_ctl.cur;
+  double dt = 0.0;  // a zero step leaves the state unchanged; only timing
+  if ((rc = cans_run_cfl(h, 0.4, &dt))) return rc;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_tile = h->tile;
+  Box3 box{};
+  for (int t = 0; t < mlw2d_tile_count(); t++) {
+    // warm-up launch, then timed launches
+    CK(launch_mlw2d(h->d.solver, h->d.exact != 0, t, h->buf[cur],
+                    h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph,
+                    dt, nullptr, box, h->s));
+    CK(cudaEventRecord(e0, h->s));
+    for (int k = 0; k < trial_steps; k++)
+      CK(launch_mlw2d(h->d.solver, h->d.exact != 0, t, h->buf[cur],
+                      h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a, h->ay.a,
+                      h->ph, dt, nullptr, box, h->s));
+    CK(cudaEventRecord(e1, h->s));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      best_tile = t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best_tile != h->tile) {
+    h->tile = best_tile;
+    drop_graph(h);
+  }
+  if (tile) *tile = best_tile;
+  return CANS_OK;
+}

@@ -1,0 +1,684 @@
+// Fused 2-D modified Lax-Wendroff step (sm_103a, FP64).
+//
+// One kernel replaces the whole body of the reference routines
+//   mlw_m3  cans2d/hdmlw/mlw_m3.f:64-374  (ro,pr,vx,vy,vz,bx,by,bz + az)
+//   mlw_m   cans2d/hdmlw/mlw_m.f          (ro,pr,vx,vy,bx,by + az)
+// with their primitives mlwhalf (cans2d/hdmlw/mlwhalf.f:36-52), mlwsrch
+// (mlwsrch.f:87-102), mlwfull (mlwfull.f:136-146), mlwsrcf (mlwsrcf.f:182-189)
+// and mlwartv (mlwartv.f:225-233).  The reference makes ~30 sweeps over ~37
+// full-grid temporaries; here each thread block stages a TX x TY tile plus a
+// one-cell halo in shared memory and makes three passes over it:
+//   phase 1  cells (TX+2)(TY+2): conserved variables, cell fluxes, E = -v x B
+//   phase 2  corners (TX+1)(TY+1): half-step predictor (mlwhalf part 2,
+//            mlwsrch), half-step primitives and corner fluxes; and the
+//            artificial-viscosity face coefficients q*dxim
+//   phase 3  cells TX x TY: du = central-difference half-step term
+//            (mlwhalf part 1) + corrector (mlwfull, mlwsrcf) + artificial
+//            viscosity (mlwartv); u += du; back to primitives; write out.
+// The state crosses HBM once in and once out (9 arrays for mlw_m3).
+//
+// In the exact policy every operation is the reference's, in its order, so
+// the result equals a -ffp-contract=off CPU build of the Fortran bit for bit.
+// Terms whose flux is identically zero (fx of bx, fy of by) are skipped: the
+// reference adds dt*(+0) to them, which leaves every value unchanged.
+#include <cuda_runtime.h>
+
+#include "cans_common.cuh"
+#include "cans_internal.h"
+
+namespace cans {
+
+namespace {
+
+// Cell-array slots in shared memory (per cell of the halo tile).
+template <bool M3> struct CellSlots;
+template <> struct CellSlots<true> {
+  // conserved: ro ee rx ry rz bx by bz
+  static constexpr int RO = 0, EE = 1, RX = 2, RY = 3, RZ = 4, BX = 5, BY = 6,
+                       BZ = 7;
+  static constexpr int FXE = 8, FXRX = 9, FXRY = 10, FXRZ = 11;
+  static constexpr int FYE = 12, FYRX = 13, FYRY = 14, FYRZ = 15;
+  static constexpr int EX = 16, EY = 17, EZ = 18, VX = 19, VY = 20;
+  static constexpr int N = 21, NU = 8;
+};
+template <> struct CellSlots<false> {
+  static constexpr int RO = 0, EE = 1, RX = 2, RY = 3, BX = 4, BY = 5;
+  static constexpr int FXE = 6, FXRX = 7, FXRY = 8;
+  static constexpr int FYE = 9, FYRX = 10, FYRY = 11;
+  static constexpr int EZ = 12, VX = 13, VY = 14;
+  static constexpr int N = 15, NU = 6;
+  // unused in 2-D, kept so generic code compiles
+  static constexpr int RZ = -1, BZ = -1, FXRZ = -1, FYRZ = -1, EX = -1, EY = -1;
+};
+// Corner-array slots (half-step fluxes at the cell corners).
+template <bool M3> struct CornerSlots;
+template <> struct CornerSlots<true> {
+  static constexpr int XRO = 0, XEE = 1, XRX = 2, XRY = 3, XRZ = 4;
+  static constexpr int YRO = 5, YEE = 6, YRX = 7, YRY = 8, YRZ = 9;
+  static constexpr int EX = 10, EY = 11, EZ = 12, N = 13;
+};
+template <> struct CornerSlots<false> {
+  static constexpr int XRO = 0, XEE = 1, XRX = 2, XRY = 3;
+  static constexpr int YRO = 4, YEE = 5, YRX = 6, YRY = 7;
+  static constexpr int EZ = 8, N = 9;
+  static constexpr int XRZ = -1, YRZ = -1, EX = -1, EY = -1;
+};
+// Primitive-array order in global memory.
+template <bool M3> struct Prim;
+template <> struct Prim<true> {
+  static constexpr int RO = 0, PR = 1, VX = 2, VY = 3, VZ = 4, BX = 5, BY = 6,
+                       BZ = 7, AZ = 8, N = 9;
+};
+template <> struct Prim<false> {
+  static constexpr int RO = 0, PR = 1, VX = 2, VY = 3, BX = 4, BY = 5, AZ = 6,
+                       N = 7;
+  static constexpr int VZ = -1, BZ = -1;
+};
+
+template <int TX, int TY, bool M3> struct Tile {
+  static constexpr int CX = TX + 2, CY = TY + 2, NC = CX * CY;
+  static constexpr int KX = TX + 1, KY = TY + 1, NK = KX * KY;
+  static constexpr int NQX = (TX + 1) * TY, NQY = TX * (TY + 1);
+  static constexpr int NT = TX * TY / 2;
+  static constexpr size_t smem_doubles =
+      (size_t)CellSlots<M3>::N * NC + (size_t)CornerSlots<M3>::N * NK + NQX +
+      NQY + 32;
+  static constexpr size_t smem_bytes = smem_doubles * sizeof(double);
+};
+
+// Zero-flux marker for the corrector / central-difference helpers.
+constexpr int NOFLUX = -1;
+
+}  // namespace
+
+template <bool E, bool M3, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY / 2, 1)
+    k_mlw2d(const double *__restrict__ A, double *__restrict__ B, int ix,
+            int jx, Axis ax, Axis ay, Phys ph, double dt_arg,
+            Ctl *__restrict__ ctl, Box3 box) {
+  using T = Tile<TX, TY, M3>;
+  using C = CellSlots<M3>;
+  using K = CornerSlots<M3>;
+  using P = Prim<M3>;
+  using FT = F<E>;
+  extern __shared__ double smem[];
+  double *sc = smem;                            // cells   [C::N][NC]
+  double *sk = sc + (size_t)C::N * T::NC;       // corners [K::N][NK]
+  double *sqx = sk + (size_t)K::N * T::NK;      // q*dxim  [TY][TX+1]
+  double *sqy = sqx + T::NQX;                   // q*dyim  [TY+1][TX]
+  double *sred = sqy + T::NQY;                  // reduction scratch (32)
+
+  if (ctl != nullptr) {
+    if (ctl->done | ctl->pause) return;
+    A = ctl->buf[ctl->cur];
+    B = ctl->buf[ctl->cur ^ 1];
+  }
+  const double dtv = (ctl != nullptr) ? ctl->dt : dt_arg;
+  const FT dt(dtv);
+  const size_t n = (size_t)ix * (size_t)jx;
+  const int i0 = 1 + blockIdx.x * TX;  // first interior cell of the tile
+  const int j0 = 1 + blockIdx.y * TY;
+  const int tid = threadIdx.x + threadIdx.y * TX;
+  const FT gm(ph.gm), gm1(ph.gm1), pi8i(ph.pi8i), pi4i(ph.pi4i);
+
+#define SC(slot, c) sc[(size_t)(slot) * T::NC + (c)]
+#define SK(slot, c) sk[(size_t)(slot) * T::NK + (c)]
+
+  // ---------------- phase 1: cells of the halo tile ------------------------
+  for (int c = tid; c < T::NC; c += T::NT) {
+    const int lx = c % T::CX, ly = c / T::CX;
+    const int gi = i0 - 1 + lx, gj = j0 - 1 + ly;
+    if (gi < ix && gj < jx) {
+      const size_t g = (size_t)gi + (size_t)gj * ix;
+      const FT ro(A[P::RO * n + g]), pr(A[P::PR * n + g]);
+      const FT vx(A[P::VX * n + g]), vy(A[P::VY * n + g]);
+      const FT bx(A[P::BX * n + g]), by(A[P::BY * n + g]);
+      FT vz(0.0), bz(0.0);
+      if constexpr (M3) { vz = FT(A[P::VZ * n + g]); bz = FT(A[P::BZ * n + g]); }
+      FT vv, bb;
+      if constexpr (M3) {
+        vv = vx * vx + vy * vy + vz * vz;
+        bb = bx * bx + by * by + bz * bz;
+      } else {
+        vv = vx * vx + vy * vy;
+        bb = bx * bx + by * by;
+      }
+      FT ee, ep;
+      if constexpr (E) {
+        ee = pr / gm1 + 0.5 * ro * vv + pi8i * bb;     // mlw_m3.f:111
+        ep = pr * gm / gm1 + 0.5 * ro * vv;            // mlw_m3.f:141
+      } else {
+        ee = pr * ph.gm1i + 0.5 * ro * vv + pi8i * bb;
+        ep = pr * ph.ggm1 + 0.5 * ro * vv;
+      }
+      const FT rx = ro * vx, ry = ro * vy;
+      SC(C::RO, c) = ro.v; SC(C::EE, c) = ee.v;
+      SC(C::RX, c) = rx.v; SC(C::RY, c) = ry.v;
+      SC(C::BX, c) = bx.v; SC(C::BY, c) = by.v;
+      SC(C::VX, c) = vx.v; SC(C::VY, c) = vy.v;
+      if constexpr (M3) {
+        const FT rz = ro * vz;
+        const FT ex = -vy * bz + vz * by;              // mlw_m3.f:119-121
+        const FT ey = -vz * bx + vx * bz;
+        const FT ez = -vx * by + vy * bx;
+        SC(C::RZ, c) = rz.v; SC(C::BZ, c) = bz.v;
+        SC(C::EX, c) = ex.v; SC(C::EY, c) = ey.v; SC(C::EZ, c) = ez.v;
+        // energy flux (:141-143)
+        SC(C::FXE, c) = (ep * vx + (bz * ey - by * ez) * pi4i).v;
+        SC(C::FYE, c) = (ep * vy + (bx * ez - bz * ex) * pi4i).v;
+        // momentum fluxes (:151-153, :161-163, :171-172)
+        SC(C::FXRX, c) = (ro * (vx * vx) + pr + pi8i * (by * by + bz * bz - bx * bx)).v;
+        SC(C::FYRX, c) = (ro * vx * vy - pi4i * bx * by).v;
+        SC(C::FXRY, c) = (ro * vy * vx - pi4i * by * bx).v;
+        SC(C::FYRY, c) = (ro * (vy * vy) + pr + pi8i * (bx * bx + bz * bz - by * by)).v;
+        SC(C::FXRZ, c) = (ro * vz * vx - pi4i * bz * bx).v;
+        SC(C::FYRZ, c) = (ro * vz * vy - pi4i * bz * by).v;
+      } else {
+        const FT ez = -vx * by + vy * bx;              // mlw_m.f:70
+        SC(C::EZ, c) = ez.v;
+        SC(C::FXE, c) = (ep * vx - by * ez * pi4i).v;  // mlw_m.f:85-86
+        SC(C::FYE, c) = (ep * vy + bx * ez * pi4i).v;
+        SC(C::FXRX, c) = (ro * (vx * vx) + pr + pi8i * (by * by - bx * bx)).v;
+        SC(C::FYRX, c) = (ro * vx * vy - pi4i * bx * by).v;
+        SC(C::FXRY, c) = (ro * vy * vx - pi4i * by * bx).v;
+        SC(C::FYRY, c) = (ro * (vy * vy) + pr + pi8i * (bx * bx - by * by)).v;
+      }
+    } else {
+#pragma unroll 1
+      for (int s = 0; s < C::N; s++) SC(s, c) = 0.0;
+    }
+  }
+  __syncthreads();
+
+  // ---------------- phase 2: corners and viscosity faces -------------------
+  for (int c = tid; c < T::NK; c += T::NT) {
+    const int kx = c % T::KX, ky = c / T::KX;
+    const int gi = i0 - 1 + kx, gj = j0 - 1 + ky;  // lower-left cell of corner
+    if (gi <= ix - 2 && gj <= jx - 2) {
+      const int a = kx + ky * T::CX;      // (i  ,j  )
+      const int b = a + 1;                // (i+1,j  )
+      const int cc = a + 1 + T::CX;       // (i+1,j+1)
+      const int d = a + T::CX;            // (i  ,j+1)
+      const FT dxim(ax.dim[gi]), dyim(ay.dim[gj]);
+      // mlwhalf part 2: un = avg4(u) - dt*dfdx - dt*dfdy   (mlwhalf.f:45-52)
+      auto pred = [&](int su, int sfx, int sfy, bool negx, bool negy) -> FT {
+        const FT uh = 0.25 * (FT(SC(su, b)) + FT(SC(su, a)) + FT(SC(su, cc)) +
+                              FT(SC(su, d)));
+        FT un = uh;
+        if (sfx != NOFLUX) {
+          FT fb(SC(sfx, b)), fa(SC(sfx, a)), fc(SC(sfx, cc)), fd(SC(sfx, d));
+          if (negx) { fb = -fb; fa = -fa; fc = -fc; fd = -fd; }
+          const FT dfdx = dxim * (fb - fa + fc - fd) * 0.5;
+          un = un - dt * dfdx;
+        }
+        if (sfy != NOFLUX) {
+          FT fd(SC(sfy, d)), fa(SC(sfy, a)), fc(SC(sfy, cc)), fb(SC(sfy, b));
+          if (negy) { fd = -fd; fa = -fa; fc = -fc; fb = -fb; }
+          const FT dfdy = dyim * (fd - fa + fc - fb) * 0.5;
+          un = un - dt * dfdy;
+        }
+        return un;
+      };
+      const FT roh = pred(C::RO, C::RX, C::RY, false, false);
+      const FT eeh = pred(C::EE, C::FXE, C::FYE, false, false);
+      const FT rxh = pred(C::RX, C::FXRX, C::FYRX, false, false);
+      const FT ryh = pred(C::RY, C::FXRY, C::FYRY, false, false);
+      const FT bxh = pred(C::BX, NOFLUX, C::EZ, false, false);
+      const FT byh = pred(C::BY, C::EZ, NOFLUX, true, false);
+      FT rzh(0.0), bzh(0.0);
+      if constexpr (M3) {
+        rzh = pred(C::RZ, C::FXRZ, C::FYRZ, false, false);
+        bzh = pred(C::BZ, C::EY, C::EX, false, true);
+      }
+      // half-step primitives (mlw_m3.f:214-230)
+      FT vxh, vyh, vzh(0.0);
+      if constexpr (E) {
+        vxh = rxh / roh;
+        vyh = ryh / roh;
+        if constexpr (M3) vzh = rzh / roh;
+      } else {
+        const FT rinv(1.0 / roh.v);
+        vxh = rxh * rinv;
+        vyh = ryh * rinv;
+        if constexpr (M3) vzh = rzh * rinv;
+      }
+      FT vv, bb;
+      if constexpr (M3) {
+        vv = vxh * vxh + vyh * vyh + vzh * vzh;
+        bb = bxh * bxh + byh * byh + bzh * bzh;
+      } else {
+        vv = vxh * vxh + vyh * vyh;
+        bb = bxh * bxh + byh * byh;
+      }
+      const FT prh = gm1 * (eeh - 0.5 * roh * vv - pi8i * bb);
+      FT ep;
+      if constexpr (E) ep = prh * gm / gm1 + 0.5 * roh * vv;
+      else ep = prh * ph.ggm1 + 0.5 * roh * vv;
+      SK(K::XRO, c) = (roh * vxh).v;
+      SK(K::YRO, c) = (roh * vyh).v;
+      if constexpr (M3) {
+        const FT exh = -vyh * bzh + vzh * byh;
+        const FT eyh = -vzh * bxh + vxh * bzh;
+        const FT ezh = -vxh * byh + vyh * bxh;
+        SK(K::EX, c) = exh.v; SK(K::EY, c) = eyh.v; SK(K::EZ, c) = ezh.v;
+        SK(K::XEE, c) = (ep * vxh + (bzh * eyh - byh * ezh) * pi4i).v;
+        SK(K::YEE, c) = (ep * vyh + (bxh * ezh - bzh * exh) * pi4i).v;
+        SK(K::XRX, c) = (roh * (vxh * vxh) + prh + pi8i * (byh * byh + bzh * bzh - bxh * bxh)).v;
+        SK(K::YRX, c) = (roh * vxh * vyh - pi4i * bxh * byh).v;
+        SK(K::XRY, c) = (roh * vyh * vxh - pi4i * byh * bxh).v;
+        SK(K::YRY, c) = (roh * (vyh * vyh) + prh + pi8i * (bxh * bxh + bzh * bzh - byh * byh)).v;
+        SK(K::XRZ, c) = (roh * vzh * vxh - pi4i * bzh * bxh).v;
+        SK(K::YRZ, c) = (roh * vzh * vyh - pi4i * bzh * byh).v;
+      } else {
+        const FT ezh = -vxh * byh + vyh * bxh;
+        SK(K::EZ, c) = ezh.v;
+        SK(K::XEE, c) = (ep * vxh - byh * ezh * pi4i).v;
+        SK(K::YEE, c) = (ep * vyh + bxh * ezh * pi4i).v;
+        SK(K::XRX, c) = (roh * (vxh * vxh) + prh + pi8i * (byh * byh - bxh * bxh)).v;
+        SK(K::YRX, c) = (roh * vxh * vyh - pi4i * bxh * byh).v;
+        SK(K::XRY, c) = (roh * vyh * vxh - pi4i * byh * bxh).v;
+        SK(K::YRY, c) = (roh * (vyh * vyh) + prh + pi8i * (bxh * bxh - byh * byh)).v;
+      }
+    } else {
+#pragma unroll 1
+      for (int s = 0; s < K::N; s++) SK(s, c) = 0.0;
+    }
+  }
+  // artificial-viscosity face coefficients q*dxim (mlw_m3.f:325-334; the
+  // product qx(i,j)*dxim(i) is the first operation mlwartv applies)
+  const FT qav(ph.qav);
+  for (int f = tid; f < T::NQX; f += T::NT) {
+    const int fx = f % (TX + 1), r = f / (TX + 1);
+    const int gi = i0 - 1 + fx, gj = j0 + r;
+    double v = 0.0;
+    if (gi + 1 < ix && gj < jx) {
+      const int cl = fx + (r + 1) * T::CX;
+      const FT q = qav * FT(ax.dm[gi]) *
+                   max0(fabs_(FT(SC(C::VX, cl + 1)) - FT(SC(C::VX, cl))) - CANS_AV_EPS);
+      v = (q * FT(ax.dim[gi])).v;
+    }
+    sqx[f] = v;
+  }
+  for (int f = tid; f < T::NQY; f += T::NT) {
+    const int fx = f % TX, r = f / TX;
+    const int gi = i0 + fx, gj = j0 - 1 + r;
+    double v = 0.0;
+    if (gi < ix && gj + 1 < jx) {
+      const int cl = (fx + 1) + r * T::CX;
+      const FT q = qav * FT(ay.dm[gj]) *
+                   max0(fabs_(FT(SC(C::VY, cl + T::CX)) - FT(SC(C::VY, cl))) - CANS_AV_EPS);
+      v = (q * FT(ay.dim[gj])).v;
+    }
+    sqy[f] = v;
+  }
+  __syncthreads();
+
+  // ---------------- phase 3: full step on the tile's own cells -------------
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+  const int lx = threadIdx.x + 1;
+#pragma unroll 1
+  for (int rr = 0; rr < 2; rr++) {
+    const int ly = threadIdx.y + 1 + rr * (TY / 2);
+    const int gi = i0 - 1 + lx, gj = j0 - 1 + ly;
+    if (gi > ix - 2 || gj > jx - 2) continue;
+    const int c = lx + ly * T::CX;
+    const int cE = c + 1, cW = c - 1, cN = c + T::CX, cS = c - T::CX;
+    // corners around the cell: (i-1,j-1) (i,j-1) (i-1,j) (i,j)
+    const int kSW = (lx - 1) + (ly - 1) * T::KX, kSE = kSW + 1;
+    const int kNW = kSW + T::KX, kNE = kNW + 1;
+    const FT hdt = 0.5 * dt;
+    const FT hdx = 0.5 * FT(ax.di[gi]), hdy = 0.5 * FT(ay.di[gj]);
+    const FT dxi(ax.di[gi]), dyi(ay.di[gj]);
+    const FT ux0(ax.u0[gi]), ux1(ax.u1[gi]), uy0(ay.u0[gj]), uy1(ay.u1[gj]);
+    const FT qxe(sqx[lx + (ly - 1) * (TX + 1)]), qxw(sqx[lx - 1 + (ly - 1) * (TX + 1)]);
+    const FT qyn(sqy[(lx - 1) + ly * TX]), qys(sqy[(lx - 1) + (ly - 1) * TX]);
+
+    // du for one conserved variable: half-step central difference,
+    // corrector and artificial viscosity, in the reference order.
+    auto dstep = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx,
+                     bool nkx, int kfy, bool nky) -> FT {
+      FT du(0.0);
+      // mlwhalf part 1 (mlwhalf.f:36-41)
+      if (sfx != NOFLUX) {
+        FT fe(SC(sfx, cE)), fw(SC(sfx, cW));
+        if (negx) { fe = -fe; fw = -fw; }
+        du = du - hdt * (hdx * (fe - fw));
+      }
+      if (sfy != NOFLUX) {
+        FT fn(SC(sfy, cN)), fs(SC(sfy, cS));
+        if (negy) { fn = -fn; fs = -fs; }
+        du = du - hdt * (hdy * (fn - fs));
+      }
+      // mlwfull (mlwfull.f:136-146)
+      if (kfx != NOFLUX) {
+        FT sw(SK(kfx, kSW)), se(SK(kfx, kSE)), nw(SK(kfx, kNW)), ne(SK(kfx, kNE));
+        if (nkx) { sw = -sw; se = -se; nw = -nw; ne = -ne; }
+        const FT dfdx = dxi * (uy0 * (se - sw) + uy1 * (ne - nw));
+        du = du - hdt * dfdx;
+      }
+      if (kfy != NOFLUX) {
+        FT sw(SK(kfy, kSW)), se(SK(kfy, kSE)), nw(SK(kfy, kNW)), ne(SK(kfy, kNE));
+        if (nky) { sw = -sw; se = -se; nw = -nw; ne = -ne; }
+        const FT dfdy = dyi * (ux0 * (nw - sw) + ux1 * (ne - se));
+        du = du - hdt * dfdy;
+      }
+      // mlwartv (mlwartv.f:225-233)
+      const FT u(SC(su, c));
+      du = du + dt * (dxi * (qxe * (FT(SC(su, cE)) - u) - qxw * (u - FT(SC(su, cW))))) +
+           dt * (dyi * (qyn * (FT(SC(su, cN)) - u) - qys * (u - FT(SC(su, cS)))));
+      return u + du;
+    };
+
+    const FT ro = dstep(C::RO, C::RX, false, C::RY, false, K::XRO, false, K::YRO, false);
+    const FT ee = dstep(C::EE, C::FXE, false, C::FYE, false, K::XEE, false, K::YEE, false);
+    const FT rx = dstep(C::RX, C::FXRX, false, C::FYRX, false, K::XRX, false, K::YRX, false);
+    const FT ry = dstep(C::RY, C::FXRY, false, C::FYRY, false, K::XRY, false, K::YRY, false);
+    const FT bx = dstep(C::BX, NOFLUX, false, C::EZ, false, NOFLUX, false, K::EZ, false);
+    const FT by = dstep(C::BY, C::EZ, true, NOFLUX, false, K::EZ, true, NOFLUX, false);
+    FT rz(0.0), bz(0.0);
+    if constexpr (M3) {
+      rz = dstep(C::RZ, C::FXRZ, false, C::FYRZ, false, K::XRZ, false, K::YRZ, false);
+      bz = dstep(C::BZ, C::EY, false, C::EX, true, K::EY, false, K::EX, true);
+    }
+    // vector potential: mlwsrch part 1 + mlwsrcf with s = -ez, -ezh
+    const size_t g = (size_t)gi + (size_t)gj * ix;
+    FT daz(0.0);
+    daz = daz + hdt * (-FT(SC(C::EZ, c)));
+    {
+      const FT ssw = -FT(SK(K::EZ, kSW)), sse = -FT(SK(K::EZ, kSE));
+      const FT snw = -FT(SK(K::EZ, kNW)), sne = -FT(SK(K::EZ, kNE));
+      const FT sh = uy0 * (ux0 * ssw + ux1 * sse) + uy1 * (ux0 * snw + ux1 * sne);
+      daz = daz + hdt * sh;
+    }
+    const FT az = FT(A[P::AZ * n + g]) + daz;
+
+    // back to primitives (mlw_m3.f:365-374)
+    FT vx, vy, vz(0.0);
+    if constexpr (E) {
+      vx = rx / ro;
+      vy = ry / ro;
+      if constexpr (M3) vz = rz / ro;
+    } else {
+      const FT rinv(1.0 / ro.v);
+      vx = rx * rinv;
+      vy = ry * rinv;
+      if constexpr (M3) vz = rz * rinv;
+    }
+    FT vv, bb;
+    if constexpr (M3) {
+      vv = vx * vx + vy * vy + vz * vz;
+      bb = bx * bx + by * by + bz * bz;
+    } else {
+      vv = vx * vx + vy * vy;
+      bb = bx * bx + by * by;
+    }
+    const FT pr = gm1 * (ee - 0.5 * ro * vv - pi8i * bb);
+    B[P::RO * n + g] = ro.v;
+    B[P::PR * n + g] = pr.v;
+    B[P::VX * n + g] = vx.v;
+    B[P::VY * n + g] = vy.v;
+    B[P::BX * n + g] = bx.v;
+    B[P::BY * n + g] = by.v;
+    B[P::AZ * n + g] = az.v;
+    if constexpr (M3) {
+      B[P::VZ * n + g] = vz.v;
+      B[P::BZ * n + g] = bz.v;
+    }
+    // CFL of the new state (cfl_m3.f:46-55 / cfl_m.f:46-55)
+    if (ctl != nullptr && gi >= box.lo[0] && gi <= box.hi[0] &&
+        gj >= box.lo[1] && gj <= box.hi[1]) {
+      FT b2, v2;
+      if constexpr (M3) {
+        b2 = bx * bx + by * by + bz * bz;
+        v2 = vx * vx + vy * vy + vz * vz;
+      } else {
+        b2 = bx * bx + by * by;
+        v2 = vx * vx + vy * vy;
+      }
+      const FT ca2 = b2 * pi4i / ro;
+      const FT cs2 = gm * pr / ro;
+      const FT dtcfl = fmin_(FT(ax.d[gi]), FT(ay.d[gj])) / fsqrt(v2 + cs2 + ca2);
+      const double dtq = (FT(ctl->safety) * dtcfl).v;
+      if (dtq < dmin) dmin = dtq;
+    }
+  }
+
+  // ghost cells of the output keep their input values, as in the reference;
+  // each ghost cell is copied by the tile that owns its nearest interior cell
+  if (blockIdx.x == 0 || blockIdx.y == 0 || blockIdx.x == gridDim.x - 1 ||
+      blockIdx.y == gridDim.y - 1) {
+    for (int c = tid; c < T::NC; c += T::NT) {
+      const int hx = c % T::CX, hy = c / T::CX;
+      const int gi = i0 - 1 + hx, gj = j0 - 1 + hy;
+      if (gi >= ix || gj >= jx) continue;
+      if (gi != 0 && gi != ix - 1 && gj != 0 && gj != jx - 1) continue;
+      const int ci = min(max(gi, 1), ix - 2), cj = min(max(gj, 1), jx - 2);
+      if (ci < i0 || ci >= i0 + TX || cj < j0 || cj >= j0 + TY) continue;
+      const size_t g = (size_t)gi + (size_t)gj * ix;
+#pragma unroll
+      for (int v = 0; v < P::N; v++) B[v * n + g] = A[v * n + g];
+    }
+  }
+  if (ctl != nullptr) block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
+#undef SC
+#undef SK
+}
+
+// ---------------------------------------------------------------------------
+// Tile configurations offered to the autotuner: (TX, TY).
+namespace {
+template <bool E, bool M3, int TX, int TY>
+cudaError_t launch_tile(const double *A, double *B, int ix, int jx,
+                        const Axis &ax, const Axis &ay, const Phys &ph,
+                        double dt, Ctl *ctl, Box3 box, cudaStream_t s) {
+  using T = Tile<TX, TY, M3>;
+  static bool attr_set = false;  // per template instance
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(
+        k_mlw2d<E, M3, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)T::smem_bytes);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  dim3 grid((ix - 2 + TX - 1) / TX, (jx - 2 + TY - 1) / TY);
+  dim3 block(TX, TY / 2);
+  k_mlw2d<E, M3, TX, TY><<<grid, block, T::smem_bytes, s>>>(A, B, ix, jx, ax,
+                                                           ay, ph, dt, ctl, box);
+  count_launch();
+  return cudaGetLastError();
+}
+
+template <bool E, bool M3>
+cudaError_t launch_sel(int tile, const double *A, double *B, int ix, int jx,
+                       const Axis &ax, const Axis &ay, const Phys &ph,
+                       double dt, Ctl *ctl, Box3 box, cudaStream_t s) {
+  switch (tile) {
+    case 1: return launch_tile<E, M3, 32, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 2: return launch_tile<E, M3, 16, 16>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 3: return launch_tile<E, M3, 64, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    default: return launch_tile<E, M3, 32, 16>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+  }
+}
+}  // namespace
+
+int mlw2d_tile_count() { return 4; }
+
+cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
+                         double *B, int ix, int jx, const Axis &ax,
+                         const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
+                         Box3 box, cudaStream_t s) {
+  if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
+  if (solver == 1) {
+    return exact ? launch_sel<true, true>(tile, A, B, ix, jx, ax, ay, ph, dt, ctl, box, s)
+                 : launch_sel<false, true>(tile, A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+  }
+  return exact ? launch_sel<true, false>(tile, A, B, ix, jx, ax, ay, ph, dt, ctl, box, s)
+               : launch_sel<false, false>(tile, A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+}
+
+// ---------------------------------------------------------------------------
+// Standalone CFL over all cells (cfl_m3.f:46-65, cfl_m.f:46-65).
+template <bool E, bool M3>
+__global__ void k_cfl2d_full(const double *__restrict__ S, int ix, int jx,
+                             Axis ax, Axis ay, Phys ph, double safety,
+                             unsigned long long *out) {
+  using FT = F<E>;
+  using P = Prim<M3>;
+  __shared__ double red[32];
+  const size_t n = (size_t)ix * jx;
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  const FT gm(ph.gm), pi4i(ph.pi4i);
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n;
+       g += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(g % ix), j = (int)(g / ix);
+    const FT ro(S[P::RO * n + g]), pr(S[P::PR * n + g]);
+    const FT vx(S[P::VX * n + g]), vy(S[P::VY * n + g]);
+    const FT bx(S[P::BX * n + g]), by(S[P::BY * n + g]);
+    FT b2, v2;
+    if constexpr (M3) {
+      const FT vz(S[P::VZ * n + g]), bz(S[P::BZ * n + g]);
+      b2 = bx * bx + by * by + bz * bz;
+      v2 = vx * vx + vy * vy + vz * vz;
+    } else {
+      b2 = bx * bx + by * by;
+      v2 = vx * vx + vy * vy;
+    }
+    const FT ca2 = b2 * pi4i / ro;
+    const FT cs2 = gm * pr / ro;
+    const FT dtcfl = fmin_(FT(ax.d[i]), FT(ay.d[j])) / fsqrt(v2 + cs2 + ca2);
+    const double dtq = (FT(safety) * dtcfl).v;
+    if (dtq < dmin) dmin = dtq;
+  }
+  block_min_to(out, dmin, red, threadIdx.x, blockDim.x);
+}
+
+cudaError_t launch_cfl2d_full(int solver, bool exact, const double *S, int ix,
+                              int jx, const Axis &ax, const Axis &ay,
+                              const Phys &ph, double safety,
+                              unsigned long long *out_bits, cudaStream_t s) {
+  const size_t n = (size_t)ix * jx;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (solver == 1) {
+    if (exact) k_cfl2d_full<true, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, safety, out_bits);
+    else k_cfl2d_full<false, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, safety, out_bits);
+  } else {
+    if (exact) k_cfl2d_full<true, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, safety, out_bits);
+    else k_cfl2d_full<false, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, safety, out_bits);
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// CFL over the frame of cells the boundary fill may have rewritten (ghost
+// layers plus the first interior layer), then the start of the next loop
+// iteration by the last block to finish.
+template <bool E, bool M3>
+__global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
+                          Axis ax, Axis ay, Phys ph, int w, Ctl *ctl) {
+  using FT = F<E>;
+  using P = Prim<M3>;
+  __shared__ double red[32];
+  if (ctl->done | ctl->pause) return;
+  S = ctl->buf[ctl->cur ^ 1];  // the state the step just wrote
+  const size_t n = (size_t)ix * jx;
+  // frame = rows j < w or j >= jx-w (all i), plus columns i < w or
+  // i >= ix-w of the remaining rows
+  const long long nrow = 2LL * w * ix;
+  const long long inner_rows = jx - 2LL * w;
+  const long long total = nrow + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  const FT gm(ph.gm), pi4i(ph.pi4i);
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       f < total; f += (long long)gridDim.x * blockDim.x) {
+    int i, j;
+    if (f < nrow) {
+      const long long r = f / ix;
+      i = (int)(f % ix);
+      j = (r < w) ? (int)r : (int)(jx - 2 * w + r);
+    } else {
+      const long long q = f - nrow;
+      const long long r = q / (2 * w);
+      const int cidx = (int)(q % (2 * w));
+      j = (int)(w + r);
+      i = (cidx < w) ? cidx : (ix - 2 * w + cidx);
+    }
+    const size_t g = (size_t)i + (size_t)j * ix;
+    const FT ro(S[P::RO * n + g]), pr(S[P::PR * n + g]);
+    const FT vx(S[P::VX * n + g]), vy(S[P::VY * n + g]);
+    const FT bx(S[P::BX * n + g]), by(S[P::BY * n + g]);
+    FT b2, v2;
+    if constexpr (M3) {
+      const FT vz(S[P::VZ * n + g]), bz(S[P::BZ * n + g]);
+      b2 = bx * bx + by * by + bz * bz;
+      v2 = vx * vx + vy * vy + vz * vz;
+    } else {
+      b2 = bx * bx + by * by;
+      v2 = vx * vx + vy * vy;
+    }
+    const FT ca2 = b2 * pi4i / ro;
+    const FT cs2 = gm * pr / ro;
+    const FT dtcfl = fmin_(FT(ax.d[i]), FT(ay.d[j])) / fsqrt(v2 + cs2 + ca2);
+    const double dtq = (FT(ctl->safety) * dtcfl).v;
+    if (dtq < dmin) dmin = dtq;
+  }
+  block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&ctl->frame_blocks_done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      ctl->frame_blocks_done = 0;
+      ctl->cur ^= 1;
+      ctl->nexec += 1;
+      // end of the reference loop body: output test, loop test, then the
+      // start of the next iteration (ns+=1, dt=cfl, dtmin test, t+=dt)
+      if (ctl->pause_on_output && ctl->dtout > 0.0) {
+        const long long nt1 = (long long)(ctl->tp / ctl->dtout);
+        const long long nt2 = (long long)(ctl->t / ctl->dtout);
+        if (nt1 < nt2) ctl->pause = 1;
+      }
+      if (!(ctl->ns < ctl->nstop && ctl->t < ctl->tend)) {
+        ctl->done = 1;
+        return;
+      }
+      ctl->ns += 1;
+      const unsigned long long bits =
+          atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
+      const double dt = __longlong_as_double((long long)bits);
+      ctl->dt = dt;
+      ctl->cfl_bits = 0x7ff0000000000000ull;
+      if (dt < ctl->dtmin) {
+        ctl->merr = 9001;
+        ctl->done = 1;
+        return;
+      }
+      ctl->tp = ctl->t;
+      ctl->t = ctl->t + dt;
+    }
+  }
+}
+
+cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
+                           int jx, const Axis &ax, const Axis &ay,
+                           const Phys &ph, int margin, Ctl *ctl,
+                           cudaStream_t s) {
+  const int w = margin + 1;
+  const long long total = 2LL * w * ix + 2LL * w * (jx - 2LL * w);
+  int blocks = (int)((total + 255) / 256);
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152) blocks = 152;
+  if (solver == 1) {
+    if (exact) k_frame2d<true, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
+    else k_frame2d<false, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
+  } else {
+    if (exact) k_frame2d<true, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
+    else k_frame2d<false, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace cans

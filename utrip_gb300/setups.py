@@ -1,0 +1,189 @@
+"""Model set-ups: grids, initial states and boundary programs.
+
+These play the part of the reference model packages (md_*/hdmlw/model.f,
+bnd.f and the grdrdy / bbtoaa calls of main.f) for the benchmark
+configurations.  Everything is computed once on the host in NumPy and shared
+by the GPU path and the CPU oracle, so transcendental functions in the
+initial conditions never differ between them.
+
+Field values are in CANS units: magnetic pressure is B^2/8pi, so a field
+given in Heaviside-Lorentz form (B^2/2) is multiplied by sqrt(4 pi), as the
+reference shock-tube set-up does (cans1d/md_mhdshktb/hdmlw/model.f:45-54).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .capi import BD_PER, BD_SPP, BD_SMN, SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D
+
+SQ4PI = math.sqrt(4.0 * math.pi)
+
+# variable order of each solver (the order of the reference arguments)
+VARS = {
+    "mlw_m3": ["ro", "pr", "vx", "vy", "vz", "bx", "by", "bz", "az"],
+    "mlw_m": ["ro", "pr", "vx", "vy", "bx", "by", "az"],
+}
+SOLVER_ID = {"mlw_m": SOLVER_MLW_M_2D, "mlw_m3": SOLVER_MLW_M3_2D}
+
+
+def grdrdy(x: np.ndarray):
+    """cans2d/common/grdrdy.f:28-42: dx, xm, dxm from the cell positions."""
+    ix = x.size
+    dxm = np.empty(ix)
+    dxm[: ix - 1] = x[1:] - x[:-1]
+    dxm[ix - 1] = dxm[ix - 2]
+    dx = np.empty(ix)
+    dx[1: ix - 1] = (dxm[: ix - 2] + dxm[1: ix - 1]) / 2.0
+    dx[0] = dx[1]
+    dx[ix - 1] = dx[ix - 2]
+    xm = np.empty(ix)
+    xm[: ix - 1] = (x[: ix - 1] + x[1:]) / 2.0
+    xm[ix - 1] = xm[ix - 2] + dx[ix - 2]
+    return dx, xm, dxm
+
+
+def uniform_axis(n: int, length: float, margin: int = 1, origin: float = 0.0):
+    """Cell positions built the way the model packages build them
+    (cans2d/md_mhdkh/hdmlw/model.f:64-76): constant dxm, the first interior
+    cell centred half a cell from `origin`, positions accumulated outward."""
+    ix = n + 2 * margin
+    d0 = length / n
+    x = np.empty(ix)
+    iz = margin  # 0-based index of the first interior cell
+    x[iz] = origin + d0 / 2.0
+    for i in range(iz + 1, ix):
+        x[i] = x[i - 1] + d0
+    for i in range(iz - 1, -1, -1):
+        x[i] = x[i + 1] - d0
+    dx, xm, dxm = grdrdy(x)
+    return x, dx, dxm
+
+
+def bbtoaa(bx: np.ndarray, by: np.ndarray, dxm: np.ndarray, dym: np.ndarray,
+           margin: int) -> np.ndarray:
+    """cans2d/common/bbtoaa.f:28-49: az by line integration from
+    (margin+1, margin+1); the recurrences run in the reference order."""
+    ix, jx = bx.shape
+    az = np.zeros((ix, jx), order="F")
+    m = margin  # 0-based index of Fortran index margin+1
+    az[m, m] = 0.0
+    for j in range(m + 1, jx):
+        az[m, j] = az[m, j - 1] + 0.5 * (bx[m, j - 1] + bx[m, j]) * dym[j - 1]
+    for j in range(m - 1, -1, -1):
+        az[m, j] = az[m, j + 1] - 0.5 * (bx[m, j] + bx[m, j + 1]) * dym[j]
+    # the i recurrences are independent per j: vectorised over j
+    for i in range(m + 1, ix):
+        az[i, :] = az[i - 1, :] - 0.5 * (by[i - 1, :] + by[i, :]) * dxm[i - 1]
+    for i in range(m - 1, -1, -1):
+        az[i, :] = az[i + 1, :] + 0.5 * (by[i, :] + by[i + 1, :]) * dxm[i]
+    return az
+
+
+def _farr(shape):
+    return np.zeros(shape, order="F")
+
+
+def _bc_all(nvar: int, x_kind: int, y_kind: int):
+    prog = []
+    for v in range(nvar):
+        prog += [(v, 0, x_kind, 0.0), (v, 1, x_kind, 0.0),
+                 (v, 2, y_kind, 0.0), (v, 3, y_kind, 0.0)]
+    return prog
+
+
+def _pack(solver, x, dx, dxm, y, dy, dym, fields, gm, qav, bc, **extra):
+    names = VARS[solver]
+    state = [np.asfortranarray(fields[k], dtype=np.float64) for k in names]
+    d = dict(solver=solver, solver_id=SOLVER_ID[solver], names=names, x=x, dx=dx,
+             dxm=dxm, y=y, dy=dy, dym=dym, state=state, gm=gm, qav=qav, margin=1,
+             bc=bc)
+    d.update(extra)
+    return d
+
+
+def orszag_tang(n: int = 512, solver: str = "mlw_m3"):
+    """2-D Orszag-Tang vortex: [0, 2pi]^2 periodic, gamma=5/3,
+    rho=25/(36 pi), p=5/(12 pi), v=(-sin y, sin x), B=(-sin y, sin 2x)/sqrt(4pi)
+    in Heaviside-Lorentz units, i.e. (-sin y, sin 2x) in CANS units."""
+    L = 2.0 * math.pi
+    x, dx, dxm = uniform_axis(n, L)
+    y, dy, dym = uniform_axis(n, L)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    shape = X.shape
+    f = {
+        "ro": np.full(shape, 25.0 / (36.0 * math.pi)),
+        "pr": np.full(shape, 5.0 / (12.0 * math.pi)),
+        "vx": -np.sin(Y), "vy": np.sin(X), "vz": np.zeros(shape),
+        "bx": SQ4PI * (-np.sin(Y) / SQ4PI), "by": SQ4PI * (np.sin(2.0 * X) / SQ4PI),
+        "bz": np.zeros(shape),
+    }
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, 1)
+    nvar = len(VARS[solver])
+    return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
+                 _bc_all(nvar, BD_PER, BD_PER), safety=0.4, dtmin=1e-10,
+                 tend=math.pi / 2.0, name=f"orszag_tang_{n}")
+
+
+def shear_layer(n: int = 256, beta: float = 1.0, seed: int = 4, ny: int | None = None,
+                solver: str = "mlw_m3"):
+    """Magnetised shear layer on [0,1]^2 (the md_mhdkh set-up shape,
+    cans2d/md_mhdkh/hdmlw/model.f:94-165): vx = 0.5 tanh((y-0.5)/0.05),
+    vy = 1e-3 sin(2 pi x + phase) with a seeded phase, rho=1, gamma=5/3,
+    B0 = sqrt(4pi)(1, 0.5, 0) and p = beta |B0_HL|^2 / 2.  Periodic in x,
+    bdsppy in y (md_mhdkh/hdmlw/bnd.f:11-39)."""
+    ny = ny or n
+    rng = np.random.default_rng(seed)
+    phase = float(rng.uniform(0.0, 2.0 * math.pi))
+    x, dx, dxm = uniform_axis(n, 1.0)
+    y, dy, dym = uniform_axis(ny, 1.0)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    shape = X.shape
+    b0 = np.array([1.0, 0.5, 0.0])
+    f = {
+        "ro": np.ones(shape),
+        "pr": np.full(shape, beta * float(b0 @ b0) / 2.0),
+        "vx": 0.5 * np.tanh((Y - 0.5) / 0.05),
+        "vy": 1e-3 * np.sin(2.0 * math.pi * X + phase),
+        "vz": np.zeros(shape),
+        "bx": np.full(shape, SQ4PI * b0[0]), "by": np.full(shape, SQ4PI * b0[1]),
+        "bz": np.zeros(shape),
+    }
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, 1)
+    nvar = len(VARS[solver])
+    return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
+                 _bc_all(nvar, BD_PER, BD_SPP), safety=0.4, dtmin=1e-10,
+                 tend=1e30, beta=beta, phase=phase, name=f"shear_layer_{n}x{ny}_b{beta:g}")
+
+
+def random_state(ix: int, jx: int, seed: int = 0, solver: str = "mlw_m3", amp: float = 0.05):
+    """Smooth state with seeded random perturbations on every variable, for
+    parity tests that exercise all terms of the step (non-uniform fields in
+    every component, including vz, bz and az)."""
+    rng = np.random.default_rng(seed)
+    x, dx, dxm = uniform_axis(ix - 2, 1.0)
+    y, dy, dym = uniform_axis(jx - 2, 1.0)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+
+    def smooth(scale):
+        kx, ky = rng.integers(1, 4, size=2)
+        ph = rng.uniform(0, 2 * math.pi, size=2)
+        base = np.sin(2 * math.pi * kx * X + ph[0]) * np.cos(2 * math.pi * ky * Y + ph[1])
+        return scale * (base + amp * rng.standard_normal(X.shape))
+
+    f = {
+        "ro": 1.0 + 0.3 * np.abs(smooth(1.0)),
+        "pr": 0.6 + 0.2 * np.abs(smooth(1.0)),
+        "vx": smooth(0.3), "vy": smooth(0.3), "vz": smooth(0.2),
+        "bx": SQ4PI * (0.8 + smooth(0.2)), "by": SQ4PI * smooth(0.3),
+        "bz": SQ4PI * smooth(0.2), "az": smooth(0.1),
+    }
+    nvar = len(VARS[solver])
+    return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
+                 _bc_all(nvar, BD_PER, BD_SPP), safety=0.4, dtmin=1e-10,
+                 tend=1e30, name=f"random_{ix}x{jx}_s{seed}")
+
+
+def copy_state(setup: dict):
+    return [a.copy(order="F") for a in setup["state"]]
