@@ -217,7 +217,11 @@ def run_ours(args, ws, rank, local):
         raise SystemExit("no usable sm_103 device")
     n = args.n
     s = setups.orszag_tang(n)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-null) stream: the run launches on it and the events,
+    # the L2 flush and the copies are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     run = drivers.make_run(s, exact=args.exact, stream=stream.cuda_stream)
     run.push(setups.copy_state(s))
     tile = run.autotune(5)

@@ -113,6 +113,50 @@ int cans_bdfrdx_2d(const int *mbnd, const int *margin, double *qq, const double 
 int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq, const double *dym, const int *ix, const int *jx); /* bdfrdy.f:2 */
 
 /* ------------------------------------------------------------------------ */
+/* 1. Drop-in entry points: 3-D                                              */
+/* ------------------------------------------------------------------------ */
+/* replaces subroutine mlw_m   (cans3d/hdmlw/mlw_m.f:2-3) */
+int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                  double *bx, double *by, double *bz, const double *dt,
+                  const double *qav, const double *gm, const double *dx,
+                  const double *dxm, const int *ix, const double *dy,
+                  const double *dym, const int *jx, const double *dz,
+                  const double *dzm, const int *kx);
+/* replaces subroutine cfl_m   (cans3d/common/cfl_m.f:2-3) */
+int cans_cfl_m_3d(double *dt, const double *safety, const double *dtmin,
+                  int *merr, const double *gm, const double *ro,
+                  const double *pr, const double *vx, const double *vy,
+                  const double *vz, const double *bx, const double *by,
+                  const double *bz, const double *dx, const int *ix,
+                  const double *dy, const int *jx, const double *dz,
+                  const int *kx);
+/* Ghost-cell fill, 3-D (cans3d/bc/bd*.f:2), same conventions as 2-D. */
+int cans_bdperx_3d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx, const int *kx); /* bdperx.f:2 */
+int cans_bdpery_3d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx, const int *kx); /* bdpery.f:2 */
+int cans_bdperz_3d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx, const int *kx); /* bdperz.f:2 */
+int cans_bdsppx_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsppx.f:2 */
+int cans_bdsppy_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsppy.f:2 */
+int cans_bdsppz_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsppz.f:2 */
+int cans_bdspnx_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdspnx.f:2 */
+int cans_bdspny_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdspny.f:2 */
+int cans_bdspnz_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdspnz.f:2 */
+int cans_bdsmpx_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsmpx.f:2 */
+int cans_bdsmpy_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsmpy.f:2 */
+int cans_bdsmpz_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsmpz.f:2 */
+int cans_bdsmnx_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsmnx.f:2 */
+int cans_bdsmny_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsmny.f:2 */
+int cans_bdsmnz_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdsmnz.f:2 */
+int cans_bdfrex_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdfrex.f:2 */
+int cans_bdfrey_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdfrey.f:2 */
+int cans_bdfrez_3d(const int *mbnd, const int *margin, double *qq, const int *ix, const int *jx, const int *kx);    /* bdfrez.f:2 */
+int cans_bdcnsx_3d(const int *mbnd, const int *margin, double *qq, const double *q0, const int *ix, const int *jx, const int *kx); /* bdcnsx.f:2 */
+int cans_bdcnsy_3d(const int *mbnd, const int *margin, double *qq, const double *q0, const int *ix, const int *jx, const int *kx); /* bdcnsy.f:2 */
+int cans_bdcnsz_3d(const int *mbnd, const int *margin, double *qq, const double *q0, const int *ix, const int *jx, const int *kx); /* bdcnsz.f:2 */
+int cans_bdfrdx_3d(const int *mbnd, const int *margin, double *qq, const double *dxm, const int *ix, const int *jx, const int *kx); /* bdfrdx.f:2 */
+int cans_bdfrdy_3d(const int *mbnd, const int *margin, double *qq, const double *dym, const int *ix, const int *jx, const int *kx); /* bdfrdy.f:2 */
+int cans_bdfrdz_3d(const int *mbnd, const int *margin, double *qq, const double *dzm, const int *ix, const int *jx, const int *kx); /* bdfrdz.f:2 */
+
+/* ------------------------------------------------------------------------ */
 /* 2. Residency registry                                                     */
 /* ------------------------------------------------------------------------ */
 /* Register `narr` host arrays of ix*jx*kx doubles each (jx = kx = 1 for
@@ -133,6 +177,7 @@ int cans_gpu_release(const double *any);
 /* ------------------------------------------------------------------------ */
 #define CANS_SOLVER_MLW_M_2D 0   /* mlw_m  2-D: ro,pr,vx,vy,bx,by,az         */
 #define CANS_SOLVER_MLW_M3_2D 1  /* mlw_m3 2-D: ro,pr,vx,vy,vz,bx,by,bz,az   */
+#define CANS_SOLVER_MLW_M_3D 2   /* mlw_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
 
 /* Boundary kinds, one per reference bd* family. */
 #define CANS_BD_NONE (-1)

@@ -151,6 +151,71 @@ def cfl_2d(setup, state, safety):
     return cfl_m(safety, setup["dtmin"], setup["gm"], *state[:6], setup["dx"], setup["dy"])
 
 
+def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):
+    ix, jx, kx = ro.shape
+    load().oracle_mlw_m_3d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], dt, qav, gm,
+                           P(dx), P(dxm), ix, P(dy), P(dym), jx, P(dz), P(dzm), kx)
+
+
+def cfl_m_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy, dz):
+    ix, jx, kx = ro.shape
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m_3d(C.byref(dt), safety, dtmin, C.byref(merr), gm,
+                           *[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
+                           P(dx), ix, P(dy), jx, P(dz), kx)
+    return dt.value, merr.value
+
+
+def bd_3d(kind, axis, mbnd, margin, qq, q0=0.0, dxm=None):
+    """One bd* call on a 3-D array; BD_PER does both faces like bdper?."""
+    lib = load()
+    dp = P(dxm) if dxm is not None else None
+    if kind == BD_PER:
+        lib.oracle_bd_3d(kind, axis, 0, margin, P(qq), q0, dp, *qq.shape)
+        lib.oracle_bd_3d(kind, axis, 1, margin, P(qq), q0, dp, *qq.shape)
+    else:
+        lib.oracle_bd_3d(kind, axis, mbnd, margin, P(qq), q0, dp, *qq.shape)
+
+
+def apply_bc_program_3d(state, program, margin, grid):
+    """Boundary program axis by axis (x, y, z), as the 3-D bnd routines do."""
+    for axis in (0, 1, 2):
+        dxm = grid["d" + "xyz"[axis] + "m"]
+        for var, face, kind, q0 in program:
+            if face // 2 != axis or kind < 0:
+                continue
+            load().oracle_bd_3d(kind, axis, face % 2, margin, P(state[var]), q0, P(dxm),
+                                *state[var].shape)
+
+
+def step_3d(setup, state, dt):
+    mlw_m_3d(*state, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"],
+             setup["dym"], setup["dz"], setup["dzm"])
+
+
+def cfl_3d(setup, state, safety):
+    return cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"], setup["dy"],
+                    setup["dz"])
+
+
+def run_3d(setup, state, nstop, tend=None, safety=None, t0=0.0):
+    """The 3-D model-package loop (cans3d/md_mhdshktb/hdmlw/main.f:167-182)."""
+    tend = setup.get("tend", 1e30) if tend is None else tend
+    safety = setup["safety"] if safety is None else safety
+    t, ns, dts = t0, 0, []
+    while True:
+        ns += 1
+        dt, merr = cfl_3d(setup, state, safety)
+        if merr:
+            return t, ns, merr, dts
+        t = t + dt
+        dts.append(dt)
+        step_3d(setup, state, dt)
+        apply_bc_program_3d(state, setup["bc"], setup["margin"], setup)
+        if not (ns < nstop and t < tend):
+            return t, ns, 0, dts
+
+
 def run_2d(setup, state, nstop, tend=None, safety=None, t0=0.0):
     """Restatement of the model-package loop (md_mhdkh/hdmlw/main.f:160-219):
     ns+=1; cfl; merr test; t+=dt; step; bnd; loop while ns<nstop and t<tend.

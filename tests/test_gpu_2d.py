@@ -90,7 +90,8 @@ def test_resident_loop_exact_100_steps(gpu, oracle_lib, case):
     t_ref, ns_ref, merr_ref, dts = oracle.run_2d(s, ref, 100)
     got = setups.copy_state(s)
     t, ns, merr, nexec = drivers.run_resident(s, got, 100, exact=True)
-    assert (ns, merr, nexec) == (ns_ref, merr_ref, 100)
+    # Orszag-Tang reaches tend = pi/2 before 100 steps, in both
+    assert (ns, merr, nexec) == (ns_ref, merr_ref, ns_ref)
     assert t == t_ref
     assert_same(s["names"], got, ref, case)
 

@@ -186,3 +186,57 @@ def test_ghost_fill_touches_only_ghosts(oracle_lib):
     a = q.copy(order="F")
     oracle_lib.bd(4, 0, 0, 1, a)          # bdsmnx lower: odd, boundary cell zero
     assert np.all(a[1, :] == 0.0) and np.array_equal(a[0, :], -q[2, :])
+
+
+def _exact_grid_3d(n=12, seed=4):
+    s = setups.random_state_3d(n + 2, n + 2, n + 2, seed=seed)
+    h = 1.0 / 16.0
+    x = (np.arange(n + 2) - 0.5) * h
+    d, _, dm = setups.grdrdy(x.copy())
+    for ax in "xyz":
+        s["d" + ax], s["d" + ax + "m"] = d.copy(), dm.copy()
+    s["bc"] = [(v, f, 0, 0.0) for v in range(8) for f in range(6)]
+    return s
+
+
+def test_3d_translation_commutes_with_step(oracle_lib):
+    s = _exact_grid_3d()
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_3d(st, s["bc"], 1, s)
+    sh = [np.asfortranarray(np.pad(np.roll(a[1:-1, 1:-1, 1:-1], (3, 5, 2), axis=(0, 1, 2)), 1))
+          for a in st]
+    oracle_lib.apply_bc_program_3d(sh, s["bc"], 1, s)
+    for _ in range(2):
+        for z in (st, sh):
+            oracle_lib.step_3d(s, z, 2e-3)
+            oracle_lib.apply_bc_program_3d(z, s["bc"], 1, s)
+    for k, a, b in zip(s["names"], st, sh):
+        assert np.array_equal(np.roll(a[1:-1, 1:-1, 1:-1], (3, 5, 2), axis=(0, 1, 2)),
+                              b[1:-1, 1:-1, 1:-1]), k
+
+
+def test_3d_periodic_conservation(oracle_lib):
+    s = _exact_grid_3d(n=14)
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_3d(st, s["bc"], 1, s)
+    tot = lambda a: a[1:-1, 1:-1, 1:-1].sum()  # noqa: E731
+    m0 = tot(st[0])
+    mx0 = tot(st[0] * st[2])
+    for _ in range(10):
+        dt, _ = oracle_lib.cfl_3d(s, st, 0.4)
+        oracle_lib.step_3d(s, st, dt)
+        oracle_lib.apply_bc_program_3d(st, s["bc"], 1, s)
+    assert abs(tot(st[0]) - m0) <= 1e-13 * m0
+    assert abs(tot(st[0] * st[2]) - mx0) <= 1e-12 * m0
+
+
+def test_3d_cfl_uses_single_precision_pi(oracle_lib):
+    s = setups.random_state_3d(10, 9, 8, seed=2)
+    ro, pr, vx, vy, vz, bx, by, bz = s["state"]
+    pai = float(np.float32(np.pi))
+    ca2 = (bx**2 + by**2 + bz**2) * (0.25 / pai) / ro
+    d = np.minimum(np.minimum(s["dx"][:, None, None], s["dy"][None, :, None]),
+                   s["dz"][None, None, :])
+    ref = 0.4 * np.min(d / np.sqrt(vx**2 + vy**2 + vz**2 + s["gm"] * pr / ro + ca2))
+    dt, merr = oracle_lib.cfl_3d(s, s["state"], 0.4)
+    assert merr == 0 and abs(dt - ref) <= 2e-15 * ref

@@ -25,6 +25,7 @@ CANS_ERR_ARG = 9400
 
 SOLVER_MLW_M_2D = 0
 SOLVER_MLW_M3_2D = 1
+SOLVER_MLW_M_3D = 2
 
 BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
 
@@ -71,6 +72,16 @@ def load() -> C.CDLL:
         "cans_run_profile": (i, [vp, i, _dp, _dp]),
         "cans_measure_fp64_tflops": (i, [_dp]),
     }
+    sig["cans_mlw_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip,
+                                             _dp, _dp, _ip])
+    sig["cans_cfl_m_3d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 +
+                            [_dp, _ip, _dp, _ip, _dp, _ip])
+    for ax in "xyz":
+        sig[f"cans_bdper{ax}_3d"] = (i, [_ip, _ip, _dp, _ip, _ip, _ip])
+        for fam in ("spp", "spn", "smp", "smn", "fre"):
+            sig[f"cans_bd{fam}{ax}_3d"] = (i, [_ip, _ip, _dp, _ip, _ip, _ip])
+        sig[f"cans_bdcns{ax}_3d"] = (i, [_ip, _ip, _dp, _dp, _ip, _ip, _ip])
+        sig[f"cans_bdfrd{ax}_3d"] = (i, [_ip, _ip, _dp, _dp, _ip, _ip, _ip])
     for name in ("bdperx", "bdpery"):
         sig[f"cans_{name}_2d"] = (i, [_ip, _ip, _dp, _ip, _ip])
     for fam in ("spp", "spn", "smp", "smn", "fre"):
@@ -192,6 +203,47 @@ def bd(kind: int, axis: int, mbnd: int, margin: int, qq: np.ndarray,
     return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _iref(ix), _iref(jx)), name)
 
 
+# ---- drop-in routines (3-D) ------------------------------------------------
+
+def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):
+    """cans3d/hdmlw/mlw_m.f:2 -- one mLW step of the 3-D state, in place."""
+    ix, jx, kx = ro.shape
+    return _check(load().cans_mlw_m_3d(*[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
+                                       _dref(dt), _dref(qav), _dref(gm), _ptr(dx), _ptr(dxm),
+                                       _iref(ix), _ptr(dy), _ptr(dym), _iref(jx), _ptr(dz),
+                                       _ptr(dzm), _iref(kx)), "mlw_m_3d")
+
+
+def cfl_m_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy, dz):
+    """cans3d/common/cfl_m.f:2 -- returns (dt, merr)."""
+    ix, jx, kx = ro.shape
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m_3d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                _dref(gm), *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
+                                _ptr(dx), _iref(ix), _ptr(dy), _iref(jx), _ptr(dz),
+                                _iref(kx)), "cfl_m_3d")
+    return dt.value, merr.value
+
+
+def bd_3d(kind: int, axis: int, mbnd: int, margin: int, qq: np.ndarray,
+          q0: float = 0.0, dxm: np.ndarray | None = None) -> int:
+    """One reference bd* call on a 3-D array (cans3d/bc/bd*.f)."""
+    lib = load()
+    ix, jx, kx = qq.shape
+    a = "xyz"[axis]
+    dims = (_iref(ix), _iref(jx), _iref(kx))
+    if kind == BD_PER:
+        f = getattr(lib, f"cans_bdper{a}_3d")
+        return _check(f(_iref(margin), _iref(margin), _ptr(qq), *dims), f"bdper{a}")
+    name = f"cans_bd{_BD_NAMES[kind]}{a}_3d"
+    f = getattr(lib, name)
+    if kind == BD_CNS:
+        return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _dref(q0), *dims), name)
+    if kind == BD_FRD:
+        return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _ptr(dxm), *dims), name)
+    return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), *dims), name)
+
+
 # ---- residency registry ----------------------------------------------------
 
 def register(arrays) -> None:
@@ -235,15 +287,19 @@ class Run:
                  exact: bool = False, tile: int = -1, stream: int | None = None):
         self.lib = load()
         self.solver = solver
-        self.nvar = 9 if solver == SOLVER_MLW_M3_2D else 7
-        self._keep = [np.ascontiguousarray(grid[k], dtype=np.float64)
-                      for k in ("dx", "dxm", "dy", "dym")]
-        dx, dxm, dy, dym = self._keep
-        d = _Desc(solver, dx.size, dy.size, 1, margin, gm, qav,
+        self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8}[solver]
+        three = solver == SOLVER_MLW_M_3D
+        keys = ("dx", "dxm", "dy", "dym") + (("dz", "dzm") if three else ())
+        self._keep = [np.ascontiguousarray(grid[k], dtype=np.float64) for k in keys]
+        dx, dxm, dy, dym = self._keep[:4]
+        dz, dzm = (self._keep[4], self._keep[5]) if three else (None, None)
+        d = _Desc(solver, dx.size, dy.size, dz.size if three else 1, margin, gm, qav,
                   dx.ctypes.data_as(_dp), dxm.ctypes.data_as(_dp),
-                  dy.ctypes.data_as(_dp), dym.ctypes.data_as(_dp), None, None,
+                  dy.ctypes.data_as(_dp), dym.ctypes.data_as(_dp),
+                  dz.ctypes.data_as(_dp) if three else None,
+                  dzm.ctypes.data_as(_dp) if three else None,
                   1 if exact else 0, tile, C.c_void_p(stream) if stream else None)
-        self.shape = (dx.size, dy.size)
+        self.shape = (dx.size, dy.size) + ((dz.size,) if three else ())
         h = C.c_void_p()
         _check(self.lib.cans_run_create(C.byref(h), C.byref(d)), "cans_run_create")
         self.h = h

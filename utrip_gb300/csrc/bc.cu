@@ -131,6 +131,16 @@ cudaError_t launch_bc2d(int nvar, double *S, int ix, int jx, const Axis &ax,
   return bc_axis(nvar, S, ix, jx, 1, 1, bc, ay.dm, ctl, s);
 }
 
+cudaError_t launch_bc3d(int nvar, double *S, int ix, int jx, int kx,
+                        const Axis &ax, const Axis &ay, const Axis &az,
+                        const BcTable &bc, const Ctl *ctl, cudaStream_t s) {
+  cudaError_t e = bc_axis(nvar, S, ix, jx, kx, 0, bc, ax.dm, ctl, s);
+  if (e != cudaSuccess) return e;
+  e = bc_axis(nvar, S, ix, jx, kx, 1, bc, ay.dm, ctl, s);
+  if (e != cudaSuccess) return e;
+  return bc_axis(nvar, S, ix, jx, kx, 2, bc, az.dm, ctl, s);
+}
+
 // A single reference bd* call on one array: thread per line.
 __global__ void k_bd_one(int kind, int axis, int mbnd, int m0, int m1,
                          double *q, double q0, const double *dxm, int n0,

@@ -106,6 +106,38 @@ __device__ __forceinline__ double warp_min(double v) {
   return v;
 }
 
+// End of one iteration of the reference loop and start of the next
+// (cans2d/md_mhdkh/hdmlw/main.f:161-173 and 191-219), run by one thread once
+// the step, the boundary fill and the CFL reduction of the new state are
+// complete: flip the state buffers, the output test, the loop test, then
+// ns+=1, dt = CFL minimum, the dtmin test, tp = t, t += dt.
+__device__ __forceinline__ void finish_iteration(Ctl *ctl) {
+  ctl->frame_blocks_done = 0;
+  ctl->cur ^= 1;
+  ctl->nexec += 1;
+  if (ctl->pause_on_output && ctl->dtout > 0.0) {
+    const long long nt1 = (long long)(ctl->tp / ctl->dtout);
+    const long long nt2 = (long long)(ctl->t / ctl->dtout);
+    if (nt1 < nt2) ctl->pause = 1;
+  }
+  if (!(ctl->ns < ctl->nstop && ctl->t < ctl->tend)) {
+    ctl->done = 1;
+    return;
+  }
+  ctl->ns += 1;
+  const unsigned long long bits = atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
+  const double dt = __longlong_as_double((long long)bits);
+  ctl->dt = dt;
+  ctl->cfl_bits = 0x7ff0000000000000ull;
+  if (dt < ctl->dtmin) {
+    ctl->merr = 9001;
+    ctl->done = 1;
+    return;
+  }
+  ctl->tp = ctl->t;
+  ctl->t = ctl->t + dt;
+}
+
 // Block-wide minimum reduced into one atomicMin.  All threads of the block
 // must call it; tid is the linear thread index, nthreads the block size.
 __device__ __forceinline__ void block_min_to(unsigned long long *addr,

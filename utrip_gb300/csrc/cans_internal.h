@@ -64,6 +64,24 @@ cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
                            const Phys &ph, int margin, Ctl *ctl,
                            cudaStream_t s);
 
+// ---- 3-D ------------------------------------------------------------------
+// mlw_m 3-D on 8 arrays (ro,pr,vx,vy,vz,bx,by,bz) of ix*jx*kx doubles.
+cudaError_t launch_mlw3d(bool exact, int tile, const double *A, double *B,
+                         int ix, int jx, int kx, const Axis &ax,
+                         const Axis &ay, const Axis &az, const Phys &ph,
+                         double dt, Ctl *ctl, Box3 box, cudaStream_t s);
+int mlw3d_tile_count();
+cudaError_t launch_cfl3d_full(bool exact, const double *S, int ix, int jx,
+                              int kx, const Axis &ax, const Axis &ay,
+                              const Axis &az, const Phys &ph, double safety,
+                              unsigned long long *out_bits, cudaStream_t s);
+cudaError_t launch_bc3d(int nvar, double *S, int ix, int jx, int kx,
+                        const Axis &ax, const Axis &ay, const Axis &az,
+                        const BcTable &bc, const Ctl *ctl, cudaStream_t s);
+cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
+                           const Axis &ay, const Axis &az, const Phys &ph,
+                           int margin, Ctl *ctl, cudaStream_t s);
+
 // ---- single bd* operation on one array (literal entry points) -------------
 // kind/axis/mbnd follow the reference routine; dims = (n0, n1, n2).
 cudaError_t launch_bd_one(int kind, int axis, int mbnd, int margin0,

@@ -451,6 +451,159 @@ extern "C" int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq,
 }
 
 // ---------------------------------------------------------------------------
+// 3-D drop-in entry points
+extern "C" int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy,
+                             double *vz, double *bx, double *by, double *bz,
+                             const double *dt, const double *qav,
+                             const double *gm, const double *dx,
+                             const double *dxm, const int *ix,
+                             const double *dy, const double *dym,
+                             const int *jx, const double *dz,
+                             const double *dzm, const int *kx) {
+  const int nx = *ix, ny = *jx, nz = *kx;
+  if (nx < 3 || ny < 3 || nz < 3) return CANS_ERR_ARG;
+  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, *qav);
+  const size_t n = (size_t)nx * ny * nz;
+  MirrorSet *m = resident_step_set(arrs, 8);
+  Scratch &sc = g_scratch;
+  DevAxis *dax = m ? &m->ax : &sc.ax, *day = m ? &m->ay : &sc.ay,
+          *daz = m ? &m->az : &sc.az;
+  if ((rc = dax->upload(nx, dx, dxm, s))) return rc;
+  if ((rc = day->upload(ny, dy, dym, s))) return rc;
+  if ((rc = daz->upload(nz, dz, dzm, s))) return rc;
+  if (m) {
+    CK(launch_mlw3d(exact_mode(), 0, m->buf[m->cur], m->buf[m->cur ^ 1], nx, ny,
+                    nz, dax->a, day->a, daz->a, ph, *dt, nullptr, Box3{}, s));
+    m->cur ^= 1;
+    return CANS_OK;
+  }
+  if ((rc = sc.ensure(8 * n))) return rc;
+  for (int v = 0; v < 8; v++)
+    CK(cudaMemcpyAsync(sc.A + v * n, arrs[v], sizeof(double) * n,
+                       cudaMemcpyHostToDevice, s));
+  CK(launch_mlw3d(exact_mode(), 0, sc.A, sc.B, nx, ny, nz, dax->a, day->a,
+                  daz->a, ph, *dt, nullptr, Box3{}, s));
+  for (int v = 0; v < 8; v++)
+    CK(cudaMemcpyAsync(arrs[v], sc.B + v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
+                             const double *dtmin, int *merr, const double *gm,
+                             const double *ro, const double *pr,
+                             const double *vx, const double *vy,
+                             const double *vz, const double *bx,
+                             const double *by, const double *bz,
+                             const double *dx, const int *ix,
+                             const double *dy, const int *jx,
+                             const double *dz, const int *kx) {
+  const int nx = *ix, ny = *jx, nz = *kx;
+  if (nx < 1 || ny < 1 || nz < 1) return CANS_ERR_ARG;
+  const double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, 0.0);
+  const size_t n = (size_t)nx * ny * nz;
+  MirrorSet *m = resident_step_set(const_cast<double *const *>(arrs), 8);
+  Scratch &sc = g_scratch;
+  DevAxis *dax = m ? &m->ax : &sc.ax, *day = m ? &m->ay : &sc.ay,
+          *daz = m ? &m->az : &sc.az;
+  if ((rc = dax->upload(nx, dx, dx, s))) return rc;
+  if ((rc = day->upload(ny, dy, dy, s))) return rc;
+  if ((rc = daz->upload(nz, dz, dz, s))) return rc;
+  const double *base;
+  unsigned long long *bits;
+  if (m) {
+    if (!m->bits) CK(cudaMalloc(&m->bits, sizeof(unsigned long long)));
+    base = m->buf[m->cur];
+    bits = m->bits;
+  } else {
+    if ((rc = sc.ensure(8 * n))) return rc;
+    for (int v = 0; v < 8; v++)
+      CK(cudaMemcpyAsync(sc.A + v * n, arrs[v], sizeof(double) * n,
+                         cudaMemcpyHostToDevice, s));
+    base = sc.A;
+    bits = sc.bits;
+  }
+  const double d0 = (double)1.e20f;
+  unsigned long long init;
+  std::memcpy(&init, &d0, sizeof init);
+  CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, s));
+  CK(launch_cfl3d_full(exact_mode(), base, nx, ny, nz, dax->a, day->a, daz->a,
+                       ph, *safety, bits, s));
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *dt = bits_to_double(out);
+  *merr = (*dt < *dtmin) ? 9001 : 0;
+  return CANS_OK;
+}
+
+#define CANS_BD3(NAME, KIND, AXIS)                                              \
+  extern "C" int NAME(const int *mbnd, const int *margin, double *qq,           \
+                      const int *ix, const int *jx, const int *kx) {            \
+    return bd_call(KIND, AXIS, *mbnd, *margin, *margin, qq, 0.0, nullptr, *ix,  \
+                   *jx, *kx);                                                    \
+  }
+CANS_BD3(cans_bdsppx_3d, BD_SPP, 0)
+CANS_BD3(cans_bdsppy_3d, BD_SPP, 1)
+CANS_BD3(cans_bdsppz_3d, BD_SPP, 2)
+CANS_BD3(cans_bdspnx_3d, BD_SPN, 0)
+CANS_BD3(cans_bdspny_3d, BD_SPN, 1)
+CANS_BD3(cans_bdspnz_3d, BD_SPN, 2)
+CANS_BD3(cans_bdsmpx_3d, BD_SMP, 0)
+CANS_BD3(cans_bdsmpy_3d, BD_SMP, 1)
+CANS_BD3(cans_bdsmpz_3d, BD_SMP, 2)
+CANS_BD3(cans_bdsmnx_3d, BD_SMN, 0)
+CANS_BD3(cans_bdsmny_3d, BD_SMN, 1)
+CANS_BD3(cans_bdsmnz_3d, BD_SMN, 2)
+CANS_BD3(cans_bdfrex_3d, BD_FRE, 0)
+CANS_BD3(cans_bdfrey_3d, BD_FRE, 1)
+CANS_BD3(cans_bdfrez_3d, BD_FRE, 2)
+#undef CANS_BD3
+
+#define CANS_BDPER3(NAME, AXIS)                                                 \
+  extern "C" int NAME(const int *margin0, const int *margin1, double *qq,       \
+                      const int *ix, const int *jx, const int *kx) {            \
+    int rc = bd_call(BD_PER, AXIS, 0, *margin0, *margin1, qq, 0.0, nullptr,     \
+                     *ix, *jx, *kx);                                             \
+    if (rc) return rc;                                                          \
+    return bd_call(BD_PER, AXIS, 1, *margin0, *margin1, qq, 0.0, nullptr, *ix,  \
+                   *jx, *kx);                                                    \
+  }
+CANS_BDPER3(cans_bdperx_3d, 0)
+CANS_BDPER3(cans_bdpery_3d, 1)
+CANS_BDPER3(cans_bdperz_3d, 2)
+#undef CANS_BDPER3
+
+#define CANS_BDQ3(NAME, KIND, AXIS, ARG)                                        \
+  extern "C" int NAME(const int *mbnd, const int *margin, double *qq,           \
+                      const double *ARG, const int *ix, const int *jx,          \
+                      const int *kx) {                                           \
+    return KIND == BD_CNS                                                        \
+               ? bd_call(KIND, AXIS, *mbnd, *margin, *margin, qq, *ARG,         \
+                         nullptr, *ix, *jx, *kx)                                 \
+               : bd_call(KIND, AXIS, *mbnd, *margin, *margin, qq, 0.0, ARG,     \
+                         *ix, *jx, *kx);                                         \
+  }
+CANS_BDQ3(cans_bdcnsx_3d, BD_CNS, 0, q0)
+CANS_BDQ3(cans_bdcnsy_3d, BD_CNS, 1, q0)
+CANS_BDQ3(cans_bdcnsz_3d, BD_CNS, 2, q0)
+CANS_BDQ3(cans_bdfrdx_3d, BD_FRD, 0, dxm)
+CANS_BDQ3(cans_bdfrdy_3d, BD_FRD, 1, dym)
+CANS_BDQ3(cans_bdfrdz_3d, BD_FRD, 2, dzm)
+#undef CANS_BDQ3
+
+// ---------------------------------------------------------------------------
 // Residency registry
 extern "C" int cans_gpu_register(double *const *arrays, const int *narr,
                                  const int *ix, const int *jx, const int *kx) {
@@ -526,6 +679,7 @@ extern "C" int cans_gpu_release(const double *any) {
 // Device-resident run handle
 struct cans_run {
   cans_run_desc d{};
+  int ndim = 2;
   int nvar = 0;
   size_t n = 0;
   Phys ph{};
@@ -548,28 +702,66 @@ int solver_nvar(int solver) {
   switch (solver) {
     case CANS_SOLVER_MLW_M_2D: return 7;
     case CANS_SOLVER_MLW_M3_2D: return 9;
+    case CANS_SOLVER_MLW_M_3D: return 8;
     default: return 0;
   }
+}
+int solver_ndim(int solver) { return solver == CANS_SOLVER_MLW_M_3D ? 3 : 2; }
+int tile_count(const cans_run *h) {
+  return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
+}
+
+// cells whose CFL the step kernel reduces: all but the frame of width
+// margin+1 that the boundary program may rewrite
+Box3 inner_box(const cans_run *h) {
+  const int w = h->bc.margin + 1;
+  Box3 b{};
+  b.lo[0] = w;
+  b.hi[0] = h->d.ix - 1 - w;
+  b.lo[1] = w;
+  b.hi[1] = h->d.jx - 1 - w;
+  b.lo[2] = h->ndim == 3 ? w : 0;
+  b.hi[2] = h->ndim == 3 ? h->d.kx - 1 - w : 0;
+  return b;
+}
+
+cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
+                        double dt, Ctl *ctl, Box3 box) {
+  if (h->ndim == 3)
+    return launch_mlw3d(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx,
+                        h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
+  return launch_mlw2d(h->d.solver, h->d.exact != 0, tile, A, B, h->d.ix,
+                      h->d.jx, h->ax.a, h->ay.a, h->ph, dt, ctl, box, h->s);
+}
+cudaError_t bc_kernels(cans_run *h, double *S, const Ctl *ctl) {
+  if (h->ndim == 3)
+    return launch_bc3d(h->nvar, S, h->d.ix, h->d.jx, h->d.kx, h->ax.a, h->ay.a,
+                       h->az.a, h->bc, ctl, h->s);
+  return launch_bc2d(h->nvar, S, h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->bc, ctl,
+                     h->s);
+}
+cudaError_t frame_kernel(cans_run *h) {
+  if (h->ndim == 3)
+    return launch_frame3d(h->d.exact != 0, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
+                          h->ay.a, h->az.a, h->ph, h->bc.margin, h->ctl, h->s);
+  return launch_frame2d(h->d.solver, h->d.exact != 0, nullptr, h->d.ix, h->d.jx,
+                        h->ax.a, h->ay.a, h->ph, h->bc.margin, h->ctl, h->s);
+}
+cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
+                            unsigned long long *bits) {
+  if (h->ndim == 3)
+    return launch_cfl3d_full(h->d.exact != 0, S, h->d.ix, h->d.jx, h->d.kx,
+                             h->ax.a, h->ay.a, h->az.a, h->ph, safety, bits, h->s);
+  return launch_cfl2d_full(h->d.solver, h->d.exact != 0, S, h->d.ix, h->d.jx,
+                           h->ax.a, h->ay.a, h->ph, safety, bits, h->s);
 }
 
 // Kernels of one loop iteration on the device: step, boundary program,
 // frame CFL (+ start of the next iteration).
 int enqueue_iteration(cans_run *h) {
-  const int ix = h->d.ix, jx = h->d.jx;
-  const int w = h->bc.margin + 1;
-  Box3 box{};
-  box.lo[0] = w;
-  box.hi[0] = ix - 1 - w;
-  box.lo[1] = w;
-  box.hi[1] = jx - 1 - w;
-  box.lo[2] = 0;
-  box.hi[2] = 0;
-  CK(launch_mlw2d(h->d.solver, h->d.exact != 0, h->tile, nullptr, nullptr, ix,
-                  jx, h->ax.a, h->ay.a, h->ph, 0.0, h->ctl, box, h->s));
-  CK(launch_bc2d(h->nvar, nullptr, ix, jx, h->ax.a, h->ay.a, h->bc, h->ctl,
-                 h->s));
-  CK(launch_frame2d(h->d.solver, h->d.exact != 0, nullptr, ix, jx, h->ax.a,
-                    h->ay.a, h->ph, h->bc.margin, h->ctl, h->s));
+  CK(step_kernel(h, h->tile, nullptr, nullptr, 0.0, h->ctl, inner_box(h)));
+  CK(bc_kernels(h, nullptr, h->ctl));
+  CK(frame_kernel(h));
   return CANS_OK;
 }
 
@@ -611,20 +803,34 @@ int read_ctl(cans_run *h) {
   return CANS_OK;
 }
 
+unsigned long long r4_1e20_bits() {
+  const double d = (double)1.e20f;  // the reference's starting minimum
+  unsigned long long b;
+  std::memcpy(&b, &d, sizeof b);
+  return b;
+}
+
 }  // namespace
 
 extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   if (!out || !d) return CANS_ERR_ARG;
   const int nvar = solver_nvar(d->solver);
-  if (nvar == 0 || d->ix < 3 || d->jx < 3 || d->kx != 1 || d->margin < 1)
-    return CANS_ERR_ARG;
+  if (nvar == 0 || d->margin < 1) return CANS_ERR_ARG;
+  const int ndim = solver_ndim(d->solver);
+  // every extent must exceed the two frames of margin+1 cells that the
+  // boundary program and the frame CFL work on
+  const int wmin = 2 * (d->margin + 1) + 1;
+  if (d->ix < wmin || d->jx < wmin) return CANS_ERR_ARG;
+  if (ndim == 2 && d->kx != 1) return CANS_ERR_ARG;
+  if (ndim == 3 && (d->kx < wmin || !d->dz || !d->dzm)) return CANS_ERR_ARG;
   if (!d->dx || !d->dxm || !d->dy || !d->dym) return CANS_ERR_ARG;
   auto *h = new cans_run();
   h->d = *d;
+  h->ndim = ndim;
   h->nvar = nvar;
-  h->n = (size_t)d->ix * d->jx;
+  h->n = (size_t)d->ix * d->jx * (ndim == 3 ? d->kx : 1);
   h->ph = make_phys(d->gm, d->qav);
-  h->tile = d->tile >= 0 && d->tile < mlw2d_tile_count() ? d->tile : 0;
+  h->tile = d->tile >= 0 && d->tile < tile_count(h) ? d->tile : 0;
   h->bc.margin = d->margin;
   for (int v = 0; v < kMaxVar; v++)
     for (int f = 0; f < 6; f++) {
@@ -653,6 +859,7 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(ctl)"));
   if ((rc = h->ax.upload(d->ix, d->dx, d->dxm, h->s))) return bail(rc);
   if ((rc = h->ay.upload(d->jx, d->dy, d->dym, h->s))) return bail(rc);
+  if (ndim == 3 && (rc = h->az.upload(d->kx, d->dz, d->dzm, h->s))) return bail(rc);
   std::memset(&h->host_ctl, 0, sizeof(Ctl));
   h->host_ctl.done = 1;
   h->host_ctl.buf[0] = h->buf[0];
@@ -682,7 +889,7 @@ extern "C" int cans_run_destroy(cans_run *h) {
 
 extern "C" int cans_run_set_bc(cans_run *h, int var, int face, int kind,
                                double q0) {
-  if (!h || var < 0 || var >= h->nvar || face < 0 || face >= 4 ||
+  if (!h || var < 0 || var >= h->nvar || face < 0 || face >= 2 * h->ndim ||
       kind < CANS_BD_NONE || kind > CANS_BD_FRD)
     return CANS_ERR_ARG;
   h->bc.kind[var][face] = kind;
@@ -745,16 +952,11 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
   c.pause = 0;
   c.frame_blocks_done = 0;
   c.nonfinite = 0;
-  {
-    double d = (double)1.e20f;  // the reference's starting minimum
-    std::memcpy(&c.cfl_bits, &d, sizeof d);
-  }
+  c.cfl_bits = r4_1e20_bits();
   h->host_ctl = c;
   CK(cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice,
                      h->s));
-  CK(launch_cfl2d_full(h->d.solver, h->d.exact != 0, h->buf[c.cur], h->d.ix,
-                       h->d.jx, h->ax.a, h->ay.a, h->ph, safety,
-                       &h->ctl->cfl_bits, h->s));
+  CK(cfl_full_kernel(h, h->buf[c.cur], safety, &h->ctl->cfl_bits));
   CK(launch_prepare(h->ctl, h->s));
   return CANS_OK;
 }
@@ -809,13 +1011,8 @@ extern "C" int cans_run_step(cans_run *h, const double *dt, int apply_bc) {
   int rc = read_ctl(h);
   if (rc) return rc;
   const int cur = h->host_ctl.cur;
-  Box3 box{};
-  CK(launch_mlw2d(h->d.solver, h->d.exact != 0, h->tile, h->buf[cur],
-                  h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph,
-                  *dt, nullptr, box, h->s));
-  if (apply_bc)
-    CK(launch_bc2d(h->nvar, h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a,
-                   h->ay.a, h->bc, nullptr, h->s));
+  CK(step_kernel(h, h->tile, h->buf[cur], h->buf[cur ^ 1], *dt, nullptr, Box3{}));
+  if (apply_bc) CK(bc_kernels(h, h->buf[cur ^ 1], nullptr));
   // flip the current buffer on the device copy of the control block
   const int nc = cur ^ 1;
   CK(cudaMemcpyAsync(&h->ctl->cur, &nc, sizeof nc, cudaMemcpyHostToDevice,
@@ -830,14 +1027,10 @@ extern "C" int cans_run_cfl(cans_run *h, double safety, double *dt) {
   int rc = read_ctl(h);
   if (rc) return rc;
   unsigned long long *bits = &h->ctl->cfl_bits;
-  unsigned long long save = h->host_ctl.cfl_bits;
-  double d0 = (double)1.e20f;
-  unsigned long long init;
-  std::memcpy(&init, &d0, sizeof init);
+  const unsigned long long save = h->host_ctl.cfl_bits;
+  const unsigned long long init = r4_1e20_bits();
   CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, h->s));
-  CK(launch_cfl2d_full(h->d.solver, h->d.exact != 0, h->buf[h->host_ctl.cur],
-                       h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph, safety, bits,
-                       h->s));
+  CK(cfl_full_kernel(h, h->buf[h->host_ctl.cur], safety, bits));
   unsigned long long out = 0;
   CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, h->s));
   CK(cudaMemcpyAsync(bits, &save, sizeof save, cudaMemcpyHostToDevice, h->s));
@@ -851,22 +1044,13 @@ extern "C" int cans_run_profile(cans_run *h, int iters, double *step_ms,
   if (!h || iters < 1 || !step_ms || !iter_ms) return CANS_ERR_ARG;
   std::vector<cudaEvent_t> ev(3 * (size_t)iters);
   for (auto &e : ev) CK(cudaEventCreate(&e));
-  const int ix = h->d.ix, jx = h->d.jx;
-  const int w = h->bc.margin + 1;
-  Box3 box{};
-  box.lo[0] = w;
-  box.hi[0] = ix - 1 - w;
-  box.lo[1] = w;
-  box.hi[1] = jx - 1 - w;
+  const Box3 box = inner_box(h);
   for (int k = 0; k < iters; k++) {
     CK(cudaEventRecord(ev[3 * k], h->s));
-    CK(launch_mlw2d(h->d.solver, h->d.exact != 0, h->tile, nullptr, nullptr, ix,
-                    jx, h->ax.a, h->ay.a, h->ph, 0.0, h->ctl, box, h->s));
+    CK(step_kernel(h, h->tile, nullptr, nullptr, 0.0, h->ctl, box));
     CK(cudaEventRecord(ev[3 * k + 1], h->s));
-    CK(launch_bc2d(h->nvar, nullptr, ix, jx, h->ax.a, h->ay.a, h->bc, h->ctl,
-                   h->s));
-    CK(launch_frame2d(h->d.solver, h->d.exact != 0, nullptr, ix, jx, h->ax.a,
-                      h->ay.a, h->ph, h->bc.margin, h->ctl, h->s));
+    CK(bc_kernels(h, nullptr, h->ctl));
+    CK(frame_kernel(h));
     CK(cudaEventRecord(ev[3 * k + 2], h->s));
   }
   CK(cudaStreamSynchronize(h->s));
@@ -889,24 +1073,20 @@ extern "C" int cans_run_autotune(cans_run *h, int trial_steps, int *tile) {
   int rc = read_ctl(h);
   if (rc) return rc;
   const int cur = h->host_ctl.cur;
-  double dt = 0.0;  // a zero step leaves the state unchanged; only timing
+  // the timing steps write only the other buffer, so the current state
+  // is left as it is
+  double dt = 0.0;
   if ((rc = cans_run_cfl(h, 0.4, &dt))) return rc;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   float best = 1e30f;
   int best_tile = h->tile;
-  Box3 box{};
-  for (int t = 0; t < mlw2d_tile_count(); t++) {
-    // warm-up launch, then timed launches
-    CK(launch_mlw2d(h->d.solver, h->d.exact != 0, t, h->buf[cur],
-                    h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph,
-                    dt, nullptr, box, h->s));
+  for (int t = 0; t < tile_count(h); t++) {
+    CK(step_kernel(h, t, h->buf[cur], h->buf[cur ^ 1], dt, nullptr, Box3{}));
     CK(cudaEventRecord(e0, h->s));
     for (int k = 0; k < trial_steps; k++)
-      CK(launch_mlw2d(h->d.solver, h->d.exact != 0, t, h->buf[cur],
-                      h->buf[cur ^ 1], h->d.ix, h->d.jx, h->ax.a, h->ay.a,
-                      h->ph, dt, nullptr, box, h->s));
+      CK(step_kernel(h, t, h->buf[cur], h->buf[cur ^ 1], dt, nullptr, Box3{}));
     CK(cudaEventRecord(e1, h->s));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;

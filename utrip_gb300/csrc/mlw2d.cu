@@ -630,33 +630,7 @@ __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
     const unsigned prev = atomicAdd(&ctl->frame_blocks_done, 1u);
     if (prev == gridDim.x - 1) {
       __threadfence();
-      ctl->frame_blocks_done = 0;
-      ctl->cur ^= 1;
-      ctl->nexec += 1;
-      // end of the reference loop body: output test, loop test, then the
-      // start of the next iteration (ns+=1, dt=cfl, dtmin test, t+=dt)
-      if (ctl->pause_on_output && ctl->dtout > 0.0) {
-        const long long nt1 = (long long)(ctl->tp / ctl->dtout);
-        const long long nt2 = (long long)(ctl->t / ctl->dtout);
-        if (nt1 < nt2) ctl->pause = 1;
-      }
-      if (!(ctl->ns < ctl->nstop && ctl->t < ctl->tend)) {
-        ctl->done = 1;
-        return;
-      }
-      ctl->ns += 1;
-      const unsigned long long bits =
-          atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
-      const double dt = __longlong_as_double((long long)bits);
-      ctl->dt = dt;
-      ctl->cfl_bits = 0x7ff0000000000000ull;
-      if (dt < ctl->dtmin) {
-        ctl->merr = 9001;
-        ctl->done = 1;
-        return;
-      }
-      ctl->tp = ctl->t;
-      ctl->t = ctl->t + dt;
+      finish_iteration(ctl);
     }
   }
 }

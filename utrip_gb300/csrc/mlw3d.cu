@@ -1,0 +1,658 @@
+// Fused 3-D modified Lax-Wendroff step (sm_103a, FP64).
+//
+// Replaces the body of cans3d/hdmlw/mlw_m.f:2-453 with its primitives
+// mlwhalf (cans3d/hdmlw/mlwhalf.f:38-65), mlwfull (mlwfull.f:34-52) and
+// mlwartv (mlwartv.f), and the CFL of cans3d/common/cfl_m.f:39-85.
+//
+// Each thread block owns a TX x TY column of cells and marches along z over
+// a chunk of planes.  One thread per cell of the (TX+2) x (TY+2) halo tile.
+// Shared memory holds a two-plane ring of cell data (conserved variables,
+// fluxes, E, velocity) and a two-plane ring of corner (half-step) fluxes;
+// the z-neighbour data of a thread's own column for plane k-1 stays in
+// registers.  Per plane k:
+//   (a) cells of plane k+1 (whole halo tile)               -> ring slot
+//   (b) corners of plane k+1/2 from planes k, k+1; AV faces of plane k
+//   (c) full step of plane k: central differences (mlwhalf part 1),
+//       corrector from corner planes k-1/2 and k+1/2 (mlwfull), artificial
+//       viscosity (mlwartv), update, back to primitives, CFL, write.
+// The state crosses HBM once in and once out: 8 arrays, 128 B per zone.
+#include <cuda_runtime.h>
+
+#include "cans_common.cuh"
+#include "cans_internal.h"
+
+namespace cans {
+
+namespace {
+
+// cell fields of one ring slot
+struct C3 {
+  static constexpr int RO = 0, EE = 1, RX = 2, RY = 3, RZ = 4, BX = 5, BY = 6,
+                       BZ = 7;
+  static constexpr int FXE = 8, FXRX = 9, FXRY = 10, FXRZ = 11;
+  static constexpr int FYE = 12, FYRX = 13, FYRY = 14, FYRZ = 15;
+  static constexpr int FZE = 16, FZRX = 17, FZRY = 18, FZRZ = 19;
+  static constexpr int EX = 20, EY = 21, EZ = 22, VX = 23, VY = 24, VZ = 25;
+  static constexpr int N = 26;
+};
+// corner fields of one ring slot
+struct K3 {
+  static constexpr int XRO = 0, YRO = 1, ZRO = 2, XEE = 3, YEE = 4, ZEE = 5;
+  static constexpr int XRX = 6, YRX = 7, ZRX = 8, XRY = 9, YRY = 10, ZRY = 11;
+  static constexpr int XRZ = 12, YRZ = 13, ZRZ = 14, EX = 15, EY = 16, EZ = 17;
+  static constexpr int N = 18;
+};
+// primitive arrays in global memory
+struct P3 {
+  static constexpr int RO = 0, PR = 1, VX = 2, VY = 3, VZ = 4, BX = 5, BY = 6,
+                       BZ = 7, N = 8;
+};
+
+template <int TX, int TY> struct Tile3 {
+  static constexpr int CX = TX + 2, CY = TY + 2, NC = CX * CY;
+  static constexpr int KX = TX + 1, KY = TY + 1, NK = KX * KY;
+  static constexpr int NQX = (TX + 1) * TY, NQY = TX * (TY + 1);
+  static constexpr int NT = NC;
+  static constexpr size_t smem_doubles =
+      2 * (size_t)C3::N * NC + 2 * (size_t)K3::N * NK + NQX + NQY + 32;
+  static constexpr size_t smem_bytes = smem_doubles * sizeof(double);
+};
+
+constexpr int NOF = -1;  // no flux in this direction
+
+// Flux sources of the 8 conserved variables, per direction: cell field
+// index (or NOF) and whether the stored value is negated.
+__device__ __forceinline__ void cell_flux_src(int v, int dir, int &f, bool &neg) {
+  // v: 0 ro 1 ee 2 rx 3 ry 4 rz 5 bx 6 by 7 bz
+  neg = false;
+  switch (v) {
+    case 0: f = dir == 0 ? C3::RX : dir == 1 ? C3::RY : C3::RZ; break;
+    case 1: f = dir == 0 ? C3::FXE : dir == 1 ? C3::FYE : C3::FZE; break;
+    case 2: f = dir == 0 ? C3::FXRX : dir == 1 ? C3::FYRX : C3::FZRX; break;
+    case 3: f = dir == 0 ? C3::FXRY : dir == 1 ? C3::FYRY : C3::FZRY; break;
+    case 4: f = dir == 0 ? C3::FXRZ : dir == 1 ? C3::FYRZ : C3::FZRZ; break;
+    case 5: f = dir == 0 ? NOF : dir == 1 ? C3::EZ : C3::EY; neg = (dir == 2); break;
+    case 6: f = dir == 0 ? C3::EZ : dir == 1 ? NOF : C3::EX; neg = (dir == 0); break;
+    default: f = dir == 0 ? C3::EY : dir == 1 ? C3::EX : NOF; neg = (dir == 1); break;
+  }
+}
+__device__ __forceinline__ void corner_flux_src(int v, int dir, int &f, bool &neg) {
+  neg = false;
+  switch (v) {
+    case 0: f = dir == 0 ? K3::XRO : dir == 1 ? K3::YRO : K3::ZRO; break;
+    case 1: f = dir == 0 ? K3::XEE : dir == 1 ? K3::YEE : K3::ZEE; break;
+    case 2: f = dir == 0 ? K3::XRX : dir == 1 ? K3::YRX : K3::ZRX; break;
+    case 3: f = dir == 0 ? K3::XRY : dir == 1 ? K3::YRY : K3::ZRY; break;
+    case 4: f = dir == 0 ? K3::XRZ : dir == 1 ? K3::YRZ : K3::ZRZ; break;
+    case 5: f = dir == 0 ? NOF : dir == 1 ? K3::EZ : K3::EY; neg = (dir == 2); break;
+    case 6: f = dir == 0 ? K3::EZ : dir == 1 ? NOF : K3::EX; neg = (dir == 0); break;
+    default: f = dir == 0 ? K3::EY : dir == 1 ? K3::EX : NOF; neg = (dir == 1); break;
+  }
+}
+
+// Cell stage: primitives of one cell -> conserved variables, E and the
+// cell fluxes of cans3d/hdmlw/mlw_m.f:74-202, into one ring slot.
+template <bool E>
+__device__ __forceinline__ void cell_stage(const double *__restrict__ A,
+                                           size_t n, size_t g, double *sl,
+                                           int NC, int c, const Phys &ph) {
+  using FT = F<E>;
+  const FT gm(ph.gm), gm1(ph.gm1), pi8i(ph.pi8i), pi4i(ph.pi4i);
+  const FT ro(A[P3::RO * n + g]), pr(A[P3::PR * n + g]);
+  const FT vx(A[P3::VX * n + g]), vy(A[P3::VY * n + g]), vz(A[P3::VZ * n + g]);
+  const FT bx(A[P3::BX * n + g]), by(A[P3::BY * n + g]), bz(A[P3::BZ * n + g]);
+  const FT vv = vx * vx + vy * vy + vz * vz;
+  const FT bb = bx * bx + by * by + bz * bz;
+  FT ee, ep;
+  if constexpr (E) {
+    ee = pr / gm1 + 0.5 * ro * vv + pi8i * bb;
+    ep = pr * gm / gm1 + 0.5 * ro * vv;
+  } else {
+    ee = pr * ph.gm1i + 0.5 * ro * vv + pi8i * bb;
+    ep = pr * ph.ggm1 + 0.5 * ro * vv;
+  }
+  const FT ex = -vy * bz + vz * by;
+  const FT ey = -vz * bx + vx * bz;
+  const FT ez = -vx * by + vy * bx;
+#define S(f) sl[(size_t)(f) * NC + c]
+  S(C3::RO) = ro.v; S(C3::EE) = ee.v;
+  S(C3::RX) = (ro * vx).v; S(C3::RY) = (ro * vy).v; S(C3::RZ) = (ro * vz).v;
+  S(C3::BX) = bx.v; S(C3::BY) = by.v; S(C3::BZ) = bz.v;
+  S(C3::EX) = ex.v; S(C3::EY) = ey.v; S(C3::EZ) = ez.v;
+  S(C3::VX) = vx.v; S(C3::VY) = vy.v; S(C3::VZ) = vz.v;
+  S(C3::FXE) = (ep * vx + (bz * ey - by * ez) * pi4i).v;
+  S(C3::FYE) = (ep * vy + (bx * ez - bz * ex) * pi4i).v;
+  S(C3::FZE) = (ep * vz + (by * ex - bx * ey) * pi4i).v;
+  S(C3::FXRX) = (ro * (vx * vx) + pr + pi8i * (by * by + bz * bz - bx * bx)).v;
+  S(C3::FYRX) = (ro * vx * vy - pi4i * bx * by).v;
+  S(C3::FZRX) = (ro * vx * vz - pi4i * bx * bz).v;
+  S(C3::FXRY) = (ro * vy * vx - pi4i * by * bx).v;
+  S(C3::FYRY) = (ro * (vy * vy) + pr + pi8i * (bx * bx + bz * bz - by * by)).v;
+  S(C3::FZRY) = (ro * vy * vz - pi4i * by * bz).v;
+  S(C3::FXRZ) = (ro * vz * vx - pi4i * bz * bx).v;
+  S(C3::FYRZ) = (ro * vz * vy - pi4i * bz * by).v;
+  S(C3::FZRZ) = (ro * (vz * vz) + pr + pi8i * (bx * bx + by * by - bz * bz)).v;
+#undef S
+}
+
+}  // namespace
+
+template <bool E, int TX, int TY>
+__global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
+    k_mlw3d(const double *__restrict__ A, double *__restrict__ B, int ix,
+            int jx, int kx, Axis ax, Axis ay, Axis az, Phys ph, double dt_arg,
+            Ctl *__restrict__ ctl, Box3 box, int kchunk) {
+  using T = Tile3<TX, TY>;
+  using FT = F<E>;
+  extern __shared__ double smem[];
+  double *scell = smem;                                   // [2][C3::N][NC]
+  double *scorn = scell + 2 * (size_t)C3::N * T::NC;      // [2][K3::N][NK]
+  double *sqx = scorn + 2 * (size_t)K3::N * T::NK;        // q*dxim of plane k
+  double *sqy = sqx + T::NQX;                             // q*dyim of plane k
+  double *sred = sqy + T::NQY;
+
+  if (ctl != nullptr) {
+    if (ctl->done | ctl->pause) return;
+    A = ctl->buf[ctl->cur];
+    B = ctl->buf[ctl->cur ^ 1];
+  }
+  const FT dt((ctl != nullptr) ? ctl->dt : dt_arg);
+  const size_t n = (size_t)ix * jx * kx;
+  const size_t plane = (size_t)ix * jx;
+  const int hx = threadIdx.x, hy = threadIdx.y;  // halo-tile coordinates
+  const int tid = hx + hy * T::CX;
+  const int i0 = 1 + blockIdx.x * TX, j0 = 1 + blockIdx.y * TY;
+  const int gi = i0 - 1 + hx, gj = j0 - 1 + hy;
+  const bool in_arr = (gi < ix) && (gj < jx);
+  const bool interior = hx >= 1 && hx <= TX && hy >= 1 && hy <= TY &&
+                        gi <= ix - 2 && gj <= jx - 2;
+  const int kb = 1 + blockIdx.z * kchunk;
+  const int ke = min(kx - 2, kb + kchunk - 1);
+  if (kb > ke) return;
+  const FT gm(ph.gm), gm1(ph.gm1), pi8i(ph.pi8i), pi4i(ph.pi4i);
+
+  auto cslot = [&](int k) { return scell + (size_t)(k & 1) * C3::N * T::NC; };
+  auto kslot = [&](int k) { return scorn + (size_t)(k & 1) * K3::N * T::NK; };
+
+  auto load_plane = [&](int k) {
+    double *sl = cslot(k);
+    if (in_arr) {
+      cell_stage<E>(A, n, (size_t)gi + (size_t)gj * ix + (size_t)k * plane, sl,
+                    T::NC, tid, ph);
+    } else {
+#pragma unroll 1
+      for (int f = 0; f < C3::N; f++) sl[(size_t)f * T::NC + tid] = 0.0;
+    }
+  };
+
+  // corner plane k+1/2 from cell planes k (lower) and k+1 (upper)
+  auto corner_plane = [&](int k) {
+    if (tid >= T::NK) return;
+    const int cx = tid % T::KX, cy = tid / T::KX;
+    const int a = i0 - 1 + cx, b = j0 - 1 + cy;  // lower corner cell
+    double *ks = kslot(k);
+#define KS(f) ks[(size_t)(f) * T::NK + tid]
+    if (a > ix - 2 || b > jx - 2) {
+#pragma unroll 1
+      for (int f = 0; f < K3::N; f++) KS(f) = 0.0;
+      return;
+    }
+    const double *L = cslot(k), *U = cslot(k + 1);
+    const int p00 = cx + cy * T::CX, p10 = p00 + 1, p01 = p00 + T::CX,
+              p11 = p01 + 1;
+    const FT dxim(ax.dim[a]), dyim(ay.dim[b]), dzim(az.dim[k]);
+    FT un[8];
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      const int su = v;  // conserved fields are 0..7
+      auto uL = [&](int p) { return FT(L[(size_t)su * T::NC + p]); };
+      auto uU = [&](int p) { return FT(U[(size_t)su * T::NC + p]); };
+      const FT uh = (uL(p10) + uL(p00) + uL(p11) + uL(p01) + uU(p10) + uU(p00) +
+                     uU(p11) + uU(p01)) * 0.125;
+      FT r = uh;
+      int f;
+      bool ng;
+      cell_flux_src(v, 0, f, ng);
+      if (f != NOF) {
+        auto fL = [&](int p) { FT x(L[(size_t)f * T::NC + p]); return ng ? -x : x; };
+        auto fU = [&](int p) { FT x(U[(size_t)f * T::NC + p]); return ng ? -x : x; };
+        const FT d = (fL(p10) - fL(p00) + fL(p11) - fL(p01) + fU(p10) - fU(p00) +
+                      fU(p11) - fU(p01)) * 0.25 * dxim;
+        r = r - dt * d;
+      }
+      cell_flux_src(v, 1, f, ng);
+      if (f != NOF) {
+        auto fL = [&](int p) { FT x(L[(size_t)f * T::NC + p]); return ng ? -x : x; };
+        auto fU = [&](int p) { FT x(U[(size_t)f * T::NC + p]); return ng ? -x : x; };
+        const FT d = (fL(p01) - fL(p00) + fL(p11) - fL(p10) + fU(p01) - fU(p00) +
+                      fU(p11) - fU(p10)) * 0.25 * dyim;
+        r = r - dt * d;
+      }
+      cell_flux_src(v, 2, f, ng);
+      if (f != NOF) {
+        auto fL = [&](int p) { FT x(L[(size_t)f * T::NC + p]); return ng ? -x : x; };
+        auto fU = [&](int p) { FT x(U[(size_t)f * T::NC + p]); return ng ? -x : x; };
+        const FT d = (fU(p00) - fL(p00) + fU(p10) - fL(p10) + fU(p01) - fL(p01) +
+                      fU(p11) - fL(p11)) * 0.25 * dzim;
+        r = r - dt * d;
+      }
+      un[v] = r;
+    }
+    const FT roh = un[0], eeh = un[1], rxh = un[2], ryh = un[3], rzh = un[4];
+    const FT bxh = un[5], byh = un[6], bzh = un[7];
+    FT vxh, vyh, vzh;
+    if constexpr (E) {
+      vxh = rxh / roh;
+      vyh = ryh / roh;
+      vzh = rzh / roh;
+    } else {
+      const FT rinv(1.0 / roh.v);
+      vxh = rxh * rinv;
+      vyh = ryh * rinv;
+      vzh = rzh * rinv;
+    }
+    const FT vv = vxh * vxh + vyh * vyh + vzh * vzh;
+    const FT bb = bxh * bxh + byh * byh + bzh * bzh;
+    const FT prh = gm1 * (eeh - 0.5 * roh * vv - pi8i * bb);
+    const FT exh = -vyh * bzh + vzh * byh;
+    const FT eyh = -vzh * bxh + vxh * bzh;
+    const FT ezh = -vxh * byh + vyh * bxh;
+    FT ep;
+    if constexpr (E) ep = prh * gm / gm1 + 0.5 * roh * vv;
+    else ep = prh * ph.ggm1 + 0.5 * roh * vv;
+    KS(K3::XRO) = (roh * vxh).v;
+    KS(K3::YRO) = (roh * vyh).v;
+    KS(K3::ZRO) = (roh * vzh).v;
+    KS(K3::XEE) = (ep * vxh + (bzh * eyh - byh * ezh) * pi4i).v;
+    KS(K3::YEE) = (ep * vyh + (bxh * ezh - bzh * exh) * pi4i).v;
+    KS(K3::ZEE) = (ep * vzh + (byh * exh - bxh * eyh) * pi4i).v;
+    KS(K3::XRX) = (roh * (vxh * vxh) + prh + pi8i * (byh * byh + bzh * bzh - bxh * bxh)).v;
+    KS(K3::YRX) = (roh * vxh * vyh - pi4i * bxh * byh).v;
+    KS(K3::ZRX) = (roh * vxh * vzh - pi4i * bxh * bzh).v;
+    KS(K3::XRY) = (roh * vyh * vxh - pi4i * byh * bxh).v;
+    KS(K3::YRY) = (roh * (vyh * vyh) + prh + pi8i * (bxh * bxh + bzh * bzh - byh * byh)).v;
+    KS(K3::ZRY) = (roh * vyh * vzh - pi4i * byh * bzh).v;
+    KS(K3::XRZ) = (roh * vzh * vxh - pi4i * bzh * bxh).v;
+    KS(K3::YRZ) = (roh * vzh * vyh - pi4i * bzh * byh).v;
+    KS(K3::ZRZ) = (roh * (vzh * vzh) + prh + pi8i * (bxh * bxh + byh * byh - bzh * bzh)).v;
+    KS(K3::EX) = exh.v;
+    KS(K3::EY) = eyh.v;
+    KS(K3::EZ) = ezh.v;
+#undef KS
+  };
+
+  // own-column data of plane k-1 kept for the z terms of plane k
+  double pu[8], pfz[8], pvz = 0.0;
+  auto save_prev = [&](int k) {
+    const double *sl = cslot(k);
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      pu[v] = sl[(size_t)v * T::NC + tid];
+      int f;
+      bool ng;
+      cell_flux_src(v, 2, f, ng);
+      double x = (f != NOF) ? sl[(size_t)f * T::NC + tid] : 0.0;
+      pfz[v] = ng ? -x : x;
+    }
+    pvz = sl[(size_t)C3::VZ * T::NC + tid];
+  };
+
+  // ---- prologue: planes kb-1 and kb, corner plane kb-1/2 -------------------
+  load_plane(kb - 1);
+  load_plane(kb);
+  __syncthreads();
+  if (interior) save_prev(kb - 1);
+  corner_plane(kb - 1);
+  __syncthreads();
+
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  const FT qav(ph.qav);
+
+  for (int k = kb; k <= ke; k++) {
+    // (a) cell plane k+1 (overwrites plane k-1, whose own-column data is saved)
+    load_plane(k + 1);
+    __syncthreads();
+    // (b) corner plane k+1/2 and the AV faces of plane k
+    corner_plane(k);
+    {
+      const double *sl = cslot(k);
+      for (int f = tid; f < T::NQX; f += T::NT) {
+        const int fx = f % (TX + 1), r = f / (TX + 1);
+        const int a = i0 - 1 + fx, b = j0 + r;
+        double v = 0.0;
+        if (a + 1 < ix && b < jx) {
+          const int cl = fx + (r + 1) * T::CX;
+          const FT q = qav * FT(ax.dm[a]) *
+                       max0(fabs_(FT(sl[(size_t)C3::VX * T::NC + cl + 1]) -
+                                  FT(sl[(size_t)C3::VX * T::NC + cl])) - CANS_AV_EPS);
+          v = (q * FT(ax.dim[a])).v;
+        }
+        sqx[f] = v;
+      }
+      for (int f = tid; f < T::NQY; f += T::NT) {
+        const int fx = f % TX, r = f / TX;
+        const int a = i0 + fx, b = j0 - 1 + r;
+        double v = 0.0;
+        if (a < ix && b + 1 < jx) {
+          const int cl = (fx + 1) + r * T::CX;
+          const FT q = qav * FT(ay.dm[b]) *
+                       max0(fabs_(FT(sl[(size_t)C3::VY * T::NC + cl + T::CX]) -
+                                  FT(sl[(size_t)C3::VY * T::NC + cl])) - CANS_AV_EPS);
+          v = (q * FT(ay.dim[b])).v;
+        }
+        sqy[f] = v;
+      }
+    }
+    __syncthreads();
+    // (c) full step of plane k
+    if (interior) {
+      const double *S0 = cslot(k), *S1 = cslot(k + 1);
+      const double *KL = kslot(k - 1), *KU = kslot(k);
+      const int c = tid, cE = c + 1, cW = c - 1, cN = c + T::CX, cS = c - T::CX;
+      const int lx = hx, ly = hy;
+      const int kSW = (lx - 1) + (ly - 1) * T::KX, kSE = kSW + 1;
+      const int kNW = kSW + T::KX, kNE = kNW + 1;
+      const FT hdt = 0.5 * dt;
+      const FT dxi(ax.di[gi]), dyi(ay.di[gj]), dzi(az.di[k]);
+      const FT hdx = 0.5 * dxi, hdy = 0.5 * dyi, hdz = 0.5 * dzi;
+      const FT ux0(ax.u0[gi]), ux1(ax.u1[gi]), uy0(ay.u0[gj]), uy1(ay.u1[gj]);
+      const FT uz0(az.u0[k]), uz1(az.u1[k]);
+      const FT qxe(sqx[lx + (ly - 1) * (TX + 1)]), qxw(sqx[lx - 1 + (ly - 1) * (TX + 1)]);
+      const FT qyn(sqy[(lx - 1) + ly * TX]), qys(sqy[(lx - 1) + (ly - 1) * TX]);
+      const FT vz0(S0[(size_t)C3::VZ * T::NC + c]), vz1(S1[(size_t)C3::VZ * T::NC + c]);
+      const FT qzu = qav * FT(az.dm[k]) * max0(fabs_(vz1 - vz0) - CANS_AV_EPS) * FT(az.dim[k]);
+      const FT qzd = qav * FT(az.dm[k - 1]) * max0(fabs_(vz0 - FT(pvz)) - CANS_AV_EPS) *
+                     FT(az.dim[k - 1]);
+      FT unew[8];
+#pragma unroll
+      for (int v = 0; v < 8; v++) {
+        FT du(0.0);
+        int f;
+        bool ng;
+        // mlwhalf part 1: x, y, z central differences
+        cell_flux_src(v, 0, f, ng);
+        if (f != NOF) {
+          FT a(S0[(size_t)f * T::NC + cE]), b(S0[(size_t)f * T::NC + cW]);
+          if (ng) { a = -a; b = -b; }
+          du = du - hdt * (hdx * (a - b));
+        }
+        cell_flux_src(v, 1, f, ng);
+        if (f != NOF) {
+          FT a(S0[(size_t)f * T::NC + cN]), b(S0[(size_t)f * T::NC + cS]);
+          if (ng) { a = -a; b = -b; }
+          du = du - hdt * (hdy * (a - b));
+        }
+        cell_flux_src(v, 2, f, ng);
+        if (f != NOF) {
+          FT a(S1[(size_t)f * T::NC + c]);
+          if (ng) a = -a;
+          du = du - hdt * (hdz * (a - FT(pfz[v])));
+        }
+        // mlwfull: corner planes k-1/2 (L) and k+1/2 (U)
+        corner_flux_src(v, 0, f, ng);
+        if (f != NOF) {
+          auto L = [&](int p) { FT x(KL[(size_t)f * T::NK + p]); return ng ? -x : x; };
+          auto U = [&](int p) { FT x(KU[(size_t)f * T::NK + p]); return ng ? -x : x; };
+          const FT dfdx = dxi * (uz0 * (uy0 * (L(kSE) - L(kSW)) + uy1 * (L(kNE) - L(kNW))) +
+                                 uz1 * (uy0 * (U(kSE) - U(kSW)) + uy1 * (U(kNE) - U(kNW))));
+          du = du - hdt * dfdx;
+        }
+        corner_flux_src(v, 1, f, ng);
+        if (f != NOF) {
+          auto L = [&](int p) { FT x(KL[(size_t)f * T::NK + p]); return ng ? -x : x; };
+          auto U = [&](int p) { FT x(KU[(size_t)f * T::NK + p]); return ng ? -x : x; };
+          const FT dfdy = dyi * (ux0 * (uz0 * (L(kNW) - L(kSW)) + uz1 * (U(kNW) - U(kSW))) +
+                                 ux1 * (uz0 * (L(kNE) - L(kSE)) + uz1 * (U(kNE) - U(kSE))));
+          du = du - hdt * dfdy;
+        }
+        corner_flux_src(v, 2, f, ng);
+        if (f != NOF) {
+          auto L = [&](int p) { FT x(KL[(size_t)f * T::NK + p]); return ng ? -x : x; };
+          auto U = [&](int p) { FT x(KU[(size_t)f * T::NK + p]); return ng ? -x : x; };
+          const FT dfdz = dzi * (uy0 * (ux0 * (U(kSW) - L(kSW)) + ux1 * (U(kSE) - L(kSE))) +
+                                 uy1 * (ux0 * (U(kNW) - L(kNW)) + ux1 * (U(kNE) - L(kNE))));
+          du = du - hdt * dfdz;
+        }
+        // mlwartv
+        const FT u(S0[(size_t)v * T::NC + c]);
+        du = du + dt * (dxi * (qxe * (FT(S0[(size_t)v * T::NC + cE]) - u) -
+                               qxw * (u - FT(S0[(size_t)v * T::NC + cW])))) +
+             dt * (dyi * (qyn * (FT(S0[(size_t)v * T::NC + cN]) - u) -
+                          qys * (u - FT(S0[(size_t)v * T::NC + cS])))) +
+             dt * (dzi * (qzu * (FT(S1[(size_t)v * T::NC + c]) - u) - qzd * (u - FT(pu[v]))));
+        unew[v] = u + du;
+      }
+      const FT ro = unew[0], ee = unew[1], rx = unew[2], ry = unew[3], rz = unew[4];
+      const FT bx = unew[5], by = unew[6], bz = unew[7];
+      FT vx, vy, vz;
+      if constexpr (E) {
+        vx = rx / ro;
+        vy = ry / ro;
+        vz = rz / ro;
+      } else {
+        const FT rinv(1.0 / ro.v);
+        vx = rx * rinv;
+        vy = ry * rinv;
+        vz = rz * rinv;
+      }
+      const FT vv = vx * vx + vy * vy + vz * vz;
+      const FT bb = bx * bx + by * by + bz * bz;
+      const FT pr = gm1 * (ee - 0.5 * ro * vv - pi8i * bb);
+      const size_t g = (size_t)gi + (size_t)gj * ix + (size_t)k * plane;
+      B[P3::RO * n + g] = ro.v;
+      B[P3::PR * n + g] = pr.v;
+      B[P3::VX * n + g] = vx.v;
+      B[P3::VY * n + g] = vy.v;
+      B[P3::VZ * n + g] = vz.v;
+      B[P3::BX * n + g] = bx.v;
+      B[P3::BY * n + g] = by.v;
+      B[P3::BZ * n + g] = bz.v;
+      if (ctl != nullptr && gi >= box.lo[0] && gi <= box.hi[0] && gj >= box.lo[1] &&
+          gj <= box.hi[1] && k >= box.lo[2] && k <= box.hi[2]) {
+        // cans3d/common/cfl_m.f:52-59 (pi in single precision)
+        const FT b2 = bx * bx + by * by + bz * bz;
+        const FT ca2 = b2 * FT(ph.pi4i_cfl) / ro;
+        const FT cs2 = gm * pr / ro;
+        const FT v2 = vx * vx + vy * vy + vz * vz;
+        const FT dmn = fmin_(fmin_(FT(ax.d[gi]), FT(ay.d[gj])), FT(az.d[k]));
+        const double dtq = (FT(ctl->safety) * (dmn / fsqrt(v2 + cs2 + ca2))).v;
+        if (dtq < dmin) dmin = dtq;
+      }
+      save_prev(k);
+    }
+    // ghost cells keep their input values (cans3d/hdmlw/mlw_m.f updates
+    // only 2..n-1); each is copied by the block owning its nearest interior
+    // cell, plane by plane, plus the z ghost planes at the chunk ends.
+    if (in_arr) {
+      const int ci = min(max(gi, 1), ix - 2), cj = min(max(gj, 1), jx - 2);
+      const bool owner = ci >= i0 && ci < i0 + TX && cj >= j0 && cj < j0 + TY;
+      if (owner) {
+        const bool xy_ghost = (gi == 0 || gi == ix - 1 || gj == 0 || gj == jx - 1);
+        auto copy = [&](int kk) {
+          const size_t g = (size_t)gi + (size_t)gj * ix + (size_t)kk * plane;
+#pragma unroll
+          for (int v = 0; v < P3::N; v++) B[v * n + g] = A[v * n + g];
+        };
+        if (xy_ghost) copy(k);
+        if (k == 1) copy(0);
+        if (k == kx - 2) copy(kx - 1);
+      }
+    }
+    __syncthreads();
+  }
+  if (ctl != nullptr) block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
+}
+
+namespace {
+template <bool E, int TX, int TY>
+cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
+                    const Axis &ax, const Axis &ay, const Axis &az,
+                    const Phys &ph, double dt, Ctl *ctl, Box3 box, int kchunk,
+                    cudaStream_t s) {
+  using T = Tile3<TX, TY>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)T::smem_bytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((ix - 2 + TX - 1) / TX, (jx - 2 + TY - 1) / TY,
+            (kx - 2 + kchunk - 1) / kchunk);
+  dim3 block(TX + 2, TY + 2);
+  k_mlw3d<E, TX, TY><<<grid, block, T::smem_bytes, s>>>(A, B, ix, jx, kx, ax, ay, az,
+                                                       ph, dt, ctl, box, kchunk);
+  count_launch();
+  return cudaGetLastError();
+}
+}  // namespace
+
+int mlw3d_tile_count() { return 3; }
+
+cudaError_t launch_mlw3d(bool exact, int tile, const double *A, double *B,
+                         int ix, int jx, int kx, const Axis &ax,
+                         const Axis &ay, const Axis &az, const Phys &ph,
+                         double dt, Ctl *ctl, Box3 box, cudaStream_t s) {
+  if (ix < 3 || jx < 3 || kx < 3) return cudaErrorInvalidValue;
+  // tile: 0 = 16x16 tiles, z chunks of 64; 1 = 16x16, chunks of 32;
+  //       2 = 16x8 tiles, chunks of 64
+  const int kchunk = (tile == 1) ? 32 : 64;
+  if (tile == 2)
+    return exact ? launch3<true, 16, 8>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box, kchunk, s)
+                 : launch3<false, 16, 8>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box, kchunk, s);
+  return exact ? launch3<true, 16, 16>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box, kchunk, s)
+               : launch3<false, 16, 16>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box, kchunk, s);
+}
+
+// ---------------------------------------------------------------------------
+// CFL over all cells (cans3d/common/cfl_m.f:39-85) and over the frame of cells
+// the boundary fill may rewrite, with the start of the next iteration.
+template <bool E>
+__device__ __forceinline__ double cfl3_cell(const double *__restrict__ S,
+                                            size_t n, size_t g, int i, int j,
+                                            int k, const Axis &ax,
+                                            const Axis &ay, const Axis &az,
+                                            const Phys &ph, double safety) {
+  using FT = F<E>;
+  const FT ro(S[P3::RO * n + g]), pr(S[P3::PR * n + g]);
+  const FT vx(S[P3::VX * n + g]), vy(S[P3::VY * n + g]), vz(S[P3::VZ * n + g]);
+  const FT bx(S[P3::BX * n + g]), by(S[P3::BY * n + g]), bz(S[P3::BZ * n + g]);
+  const FT b2 = bx * bx + by * by + bz * bz;
+  const FT ca2 = b2 * FT(ph.pi4i_cfl) / ro;
+  const FT cs2 = FT(ph.gm) * pr / ro;
+  const FT v2 = vx * vx + vy * vy + vz * vz;
+  const FT dmn = fmin_(fmin_(FT(ax.d[i]), FT(ay.d[j])), FT(az.d[k]));
+  return (FT(safety) * (dmn / fsqrt(v2 + cs2 + ca2))).v;
+}
+
+template <bool E>
+__global__ void k_cfl3d_full(const double *__restrict__ S, int ix, int jx,
+                             int kx, Axis ax, Axis ay, Axis az, Phys ph,
+                             double safety, unsigned long long *out) {
+  __shared__ double red[32];
+  const size_t plane = (size_t)ix * jx, n = plane * kx;
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n;
+       g += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(g / plane);
+    const size_t r = g % plane;
+    const int j = (int)(r / ix), i = (int)(r % ix);
+    const double d = cfl3_cell<E>(S, n, g, i, j, k, ax, ay, az, ph, safety);
+    if (d < dmin) dmin = d;
+  }
+  block_min_to(out, dmin, red, threadIdx.x, blockDim.x);
+}
+
+cudaError_t launch_cfl3d_full(bool exact, const double *S, int ix, int jx,
+                              int kx, const Axis &ax, const Axis &ay,
+                              const Axis &az, const Phys &ph, double safety,
+                              unsigned long long *out_bits, cudaStream_t s) {
+  const size_t n = (size_t)ix * jx * kx;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (exact) k_cfl3d_full<true><<<blocks, 256, 0, s>>>(S, ix, jx, kx, ax, ay, az, ph, safety, out_bits);
+  else k_cfl3d_full<false><<<blocks, 256, 0, s>>>(S, ix, jx, kx, ax, ay, az, ph, safety, out_bits);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Frame: cells with any index within w of its faces, enumerated as z slabs,
+// then y slabs of the remaining planes, then x slabs of the remaining rows.
+__device__ __forceinline__ void frame3_index(long long f, int ix, int jx, int kx,
+                                             int w, int &i, int &j, int &k) {
+  const long long zs = 2LL * w * ix * jx;
+  if (f < zs) {
+    const long long p = f / ((long long)ix * jx), r = f % ((long long)ix * jx);
+    k = (p < w) ? (int)p : (int)(kx - 2 * w + p);
+    j = (int)(r / ix);
+    i = (int)(r % ix);
+    return;
+  }
+  f -= zs;
+  const long long kin = kx - 2LL * w;
+  const long long ys = 2LL * w * ix * kin;
+  if (f < ys) {
+    const long long per = 2LL * w * ix;
+    k = (int)(w + f / per);
+    const long long r = f % per, jr = r / ix;
+    i = (int)(r % ix);
+    j = (jr < w) ? (int)jr : (int)(jx - 2 * w + jr);
+    return;
+  }
+  f -= ys;
+  const long long jin = jx - 2LL * w;
+  const long long per = 2LL * w * jin;
+  k = (int)(w + f / per);
+  const long long r = f % per;
+  j = (int)(w + r / (2 * w));
+  const int c = (int)(r % (2 * w));
+  i = (c < w) ? c : (ix - 2 * w + c);
+}
+
+template <bool E>
+__global__ void k_frame3d(int ix, int jx, int kx, Axis ax, Axis ay, Axis az,
+                          Phys ph, int w, Ctl *ctl) {
+  __shared__ double red[32];
+  if (ctl->done | ctl->pause) return;
+  const double *S = ctl->buf[ctl->cur ^ 1];
+  const size_t plane = (size_t)ix * jx, n = plane * kx;
+  const long long total = 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
+                          2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < total;
+       f += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    frame3_index(f, ix, jx, kx, w, i, j, k);
+    const size_t g = (size_t)i + (size_t)j * ix + (size_t)k * plane;
+    const double d = cfl3_cell<E>(S, n, g, i, j, k, ax, ay, az, ph, ctl->safety);
+    if (d < dmin) dmin = d;
+  }
+  block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&ctl->frame_blocks_done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      finish_iteration(ctl);
+    }
+  }
+}
+
+cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
+                           const Axis &ay, const Axis &az, const Phys &ph,
+                           int margin, Ctl *ctl, cudaStream_t s) {
+  const int w = margin + 1;
+  const long long total = 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
+                          2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
+  int blocks = (int)((total + 255) / 256);
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  if (exact) k_frame3d<true><<<blocks, 256, 0, s>>>(ix, jx, kx, ax, ay, az, ph, w, ctl);
+  else k_frame3d<false><<<blocks, 256, 0, s>>>(ix, jx, kx, ax, ay, az, ph, w, ctl);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace cans

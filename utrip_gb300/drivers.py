@@ -29,7 +29,25 @@ def _bnd(setup, state):
                 capi.bd(kind, axis, face % 2, margin, state[var], q0, dxm)
 
 
+def _bnd3(setup, state):
+    """3-D bnd: every x-face rule, then y, then z."""
+    margin = setup["margin"]
+    for axis in (0, 1, 2):
+        dxm = setup["d" + "xyz"[axis] + "m"]
+        for var, face, kind, q0 in setup["bc"]:
+            if face // 2 != axis or kind < 0:
+                continue
+            if kind == capi.BD_PER:
+                if face % 2 == 0:
+                    capi.bd_3d(kind, axis, 0, margin, state[var])
+            else:
+                capi.bd_3d(kind, axis, face % 2, margin, state[var], q0, dxm)
+
+
 def _cfl(setup, state, safety):
+    if setup["solver"] == "mlw_m_3d":
+        return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
+                             setup["dy"], setup["dz"])
     if setup["solver"] == "mlw_m3":
         return capi.cfl_m3(safety, setup["dtmin"], setup["gm"], *state[:8], setup["dx"],
                            setup["dy"])
@@ -38,7 +56,9 @@ def _cfl(setup, state, safety):
 
 def _step(setup, state, dt):
     args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
-    if setup["solver"] == "mlw_m3":
+    if setup["solver"] == "mlw_m_3d":
+        capi.mlw_m_3d(*state, dt, *args, setup["dz"], setup["dzm"])
+    elif setup["solver"] == "mlw_m3":
         capi.mlw_m3(*state, dt, *args)
     else:
         capi.mlw_m(*state, dt, *args)
@@ -61,7 +81,7 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             t = t + dt
             dts.append(dt)
             _step(setup, state, dt)
-            _bnd(setup, state)
+            (_bnd3 if setup["solver"] == "mlw_m_3d" else _bnd)(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
     finally:

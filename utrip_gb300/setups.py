@@ -185,5 +185,89 @@ def random_state(ix: int, jx: int, seed: int = 0, solver: str = "mlw_m3", amp: f
                  tend=1e30, name=f"random_{ix}x{jx}_s{seed}")
 
 
+VARS["mlw_m_3d"] = ["ro", "pr", "vx", "vy", "vz", "bx", "by", "bz"]
+SOLVER_ID["mlw_m_3d"] = 2
+
+
+def _bc_all3(nvar: int, kinds=(BD_PER, BD_PER, BD_PER)):
+    prog = []
+    for v in range(nvar):
+        for axis, kind in enumerate(kinds):
+            prog += [(v, 2 * axis, kind, 0.0), (v, 2 * axis + 1, kind, 0.0)]
+    return prog
+
+
+def _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, fields, gm, qav, bc, **extra):
+    names = VARS["mlw_m_3d"]
+    state = [np.asfortranarray(fields[k], dtype=np.float64) for k in names]
+    d = dict(solver="mlw_m_3d", solver_id=SOLVER_ID["mlw_m_3d"], names=names, x=x, dx=dx,
+             dxm=dxm, y=y, dy=dy, dym=dym, z=z, dz=dz, dzm=dzm, state=state, gm=gm, qav=qav,
+             margin=1, bc=bc)
+    d.update(extra)
+    return d
+
+
+def _periodic_pad(a: np.ndarray) -> np.ndarray:
+    return np.asfortranarray(np.pad(a, 1, mode="wrap"))
+
+
+def turbulence_3d(n: int = 256, seed: int = 3, kmax: float = 8.0, rms: float = 1e-2):
+    """3-D MHD at plasma beta 1 on [0,1]^3, periodic: rho=1, p=0.5,
+    B = sqrt(4pi)(1,0,0) (beta = 8 pi p / B^2 = 1), gamma=5/3, and a seeded
+    Gaussian random velocity whose Fourier modes are limited to integer
+    wavenumbers |k| <= kmax, rescaled to an rms speed of `rms`."""
+    rng = np.random.default_rng(seed)
+    k = np.fft.fftfreq(n, d=1.0 / n)
+    kz = np.fft.rfftfreq(n, d=1.0 / n)
+    KX, KY, KZ = np.meshgrid(k, k, kz, indexing="ij")
+    mask = (KX ** 2 + KY ** 2 + KZ ** 2) <= kmax ** 2
+    mask[0, 0, 0] = False
+    comps = []
+    for _ in range(3):
+        spec = np.zeros(mask.shape, dtype=np.complex128)
+        cnt = int(mask.sum())
+        spec[mask] = rng.standard_normal(cnt) + 1j * rng.standard_normal(cnt)
+        comps.append(np.fft.irfftn(spec, s=(n, n, n), axes=(0, 1, 2)))
+    v2 = sum(c ** 2 for c in comps)
+    scale = rms / math.sqrt(float(np.mean(v2)))
+    x, dx, dxm = uniform_axis(n, 1.0)
+    shape = (n + 2,) * 3
+    f = {
+        "ro": np.ones(shape), "pr": np.full(shape, 0.5),
+        "vx": _periodic_pad(comps[0] * scale), "vy": _periodic_pad(comps[1] * scale),
+        "vz": _periodic_pad(comps[2] * scale),
+        "bx": np.full(shape, SQ4PI), "by": np.zeros(shape), "bz": np.zeros(shape),
+    }
+    return _pack3(x, dx, dxm, x.copy(), dx.copy(), dxm.copy(), x.copy(), dx.copy(), dxm.copy(),
+                  f, 5.0 / 3.0, 3.0, _bc_all3(8), safety=0.4, dtmin=1e-10, tend=1e30,
+                  name=f"turbulence_{n}^3")
+
+
+def random_state_3d(ix: int, jx: int, kx: int, seed: int = 0, amp: float = 0.05):
+    """Seeded smooth-plus-noise 3-D state with every component non-zero, for
+    parity tests; periodic in x, bdspp in y, bdfre in z."""
+    rng = np.random.default_rng(seed)
+    x, dx, dxm = uniform_axis(ix - 2, 1.0)
+    y, dy, dym = uniform_axis(jx - 2, 1.0)
+    z, dz, dzm = uniform_axis(kx - 2, 1.0)
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+
+    def smooth(scale):
+        kk = rng.integers(1, 4, size=3)
+        ph = rng.uniform(0, 2 * math.pi, size=3)
+        base = (np.sin(2 * math.pi * kk[0] * X + ph[0]) * np.cos(2 * math.pi * kk[1] * Y + ph[1])
+                * np.cos(2 * math.pi * kk[2] * Z + ph[2]))
+        return scale * (base + amp * rng.standard_normal(X.shape))
+
+    f = {
+        "ro": 1.0 + 0.3 * np.abs(smooth(1.0)), "pr": 0.6 + 0.2 * np.abs(smooth(1.0)),
+        "vx": smooth(0.3), "vy": smooth(0.3), "vz": smooth(0.3),
+        "bx": SQ4PI * (0.8 + smooth(0.2)), "by": SQ4PI * smooth(0.3), "bz": SQ4PI * smooth(0.3),
+    }
+    return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, 5.0 / 3.0, 3.0,
+                  _bc_all3(8, (BD_PER, BD_SPP, 5)), safety=0.4, dtmin=1e-10, tend=1e30,
+                  name=f"random3d_{ix}x{jx}x{kx}_s{seed}")
+
+
 def copy_state(setup: dict):
     return [a.copy(order="F") for a in setup["state"]]
