@@ -113,6 +113,30 @@ int cans_bdfrdx_2d(const int *mbnd, const int *margin, double *qq, const double 
 int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq, const double *dym, const int *ix, const int *jx); /* bdfrdy.f:2 */
 
 /* ------------------------------------------------------------------------ */
+/* 1. Drop-in entry points: 1-D                                              */
+/* ------------------------------------------------------------------------ */
+/* replaces subroutine mlw_m   (cans1d/hdmlw/mlw_m.f:2) */
+int cans_mlw_m_1d(double *ro, double *pr, double *vx, double *vy, double *by,
+                  const double *bx, const double *bxm, const double *dt,
+                  const double *qav, const double *gm, const double *dx,
+                  const double *dxm, const int *ix);
+/* replaces subroutine cfl_m   (cans1d/common/cfl_m.f:2) */
+int cans_cfl_m_1d(double *dt, const double *safety, const double *dtmin,
+                  int *merr, const double *gm, const double *bx,
+                  const double *ro, const double *pr, const double *vx,
+                  const double *vy, const double *by, const double *dx,
+                  const int *ix);
+/* Ghost-cell fill, 1-D (cans1d/bc/bd*.f:2). */
+int cans_bdperx_1d(const int *margin0, const int *margin1, double *qq, const int *ix); /* bdperx.f:2 */
+int cans_bdsppx_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdsppx.f:2 */
+int cans_bdspnx_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdspnx.f:2 */
+int cans_bdsmpx_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdsmpx.f:2 */
+int cans_bdsmnx_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdsmnx.f:2 */
+int cans_bdfrex_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdfrex.f:2 */
+int cans_bdcnsx_1d(const int *mbnd, const int *margin, double *qq, const double *q0, const int *ix); /* bdcnsx.f:2 */
+int cans_bdfrdx_1d(const int *mbnd, const int *margin, double *qq, const double *dxm, const int *ix); /* bdfrdx.f:2 */
+
+/* ------------------------------------------------------------------------ */
 /* 1. Drop-in entry points: 3-D                                              */
 /* ------------------------------------------------------------------------ */
 /* replaces subroutine mlw_m   (cans3d/hdmlw/mlw_m.f:2-3) */
@@ -178,6 +202,7 @@ int cans_gpu_release(const double *any);
 #define CANS_SOLVER_MLW_M_2D 0   /* mlw_m  2-D: ro,pr,vx,vy,bx,by,az         */
 #define CANS_SOLVER_MLW_M3_2D 1  /* mlw_m3 2-D: ro,pr,vx,vy,vz,bx,by,bz,az   */
 #define CANS_SOLVER_MLW_M_3D 2   /* mlw_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
+#define CANS_SOLVER_MLW_M_1D 3   /* mlw_m  1-D: ro,pr,vx,vy,by (+ bx, bxm)   */
 
 /* Boundary kinds, one per reference bd* family. */
 #define CANS_BD_NONE (-1)
@@ -203,6 +228,7 @@ typedef struct {
   int exact;                  /* 1 = exact arithmetic policy                */
   int tile;                   /* tile configuration, -1 = library default   */
   void *stream;               /* cudaStream_t or NULL (library stream)      */
+  const double *bx, *bxm;     /* 1-D only: the constant bx(ix), bxm(ix)     */
 } cans_run_desc;
 
 typedef struct {

@@ -151,6 +151,58 @@ def cfl_2d(setup, state, safety):
     return cfl_m(safety, setup["dtmin"], setup["gm"], *state[:6], setup["dx"], setup["dy"])
 
 
+def mlw_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, dx, dxm):
+    load().oracle_mlw_m_1d(*[P(a) for a in (ro, pr, vx, vy, by, bx, bxm)], dt, qav, gm,
+                           P(dx), P(dxm), ro.size)
+
+
+def cfl_m_1d(safety, dtmin, gm, bx, ro, pr, vx, vy, by, dx):
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m_1d(C.byref(dt), safety, dtmin, C.byref(merr), gm, P(bx),
+                           *[P(a) for a in (ro, pr, vx, vy, by)], P(dx), ro.size)
+    return dt.value, merr.value
+
+
+def bd_1d(kind, mbnd, margin, qq, q0=0.0, dxm=None):
+    lib = load()
+    dp = P(dxm) if dxm is not None else None
+    if kind == BD_PER:
+        lib.oracle_bd_1d(kind, 0, margin, P(qq), q0, dp, qq.size)
+        lib.oracle_bd_1d(kind, 1, margin, P(qq), q0, dp, qq.size)
+    else:
+        lib.oracle_bd_1d(kind, mbnd, margin, P(qq), q0, dp, qq.size)
+
+
+def apply_bc_program_1d(state, program, margin, grid):
+    """cans1d/md_mhdshktb/hdmlw/bnd.f:9-19: every lower-face rule, then every
+    upper-face rule."""
+    for side in (0, 1):
+        for var, face, kind, q0 in program:
+            if face != side or kind < 0:
+                continue
+            load().oracle_bd_1d(kind, side, margin, P(state[var]), q0, P(grid["dxm"]),
+                                state[var].size)
+
+
+def run_1d(setup, state, nstop, tend=None, safety=None, t0=0.0):
+    """The 1-D model-package loop (cans1d/md_mhdshktb/hdmlw/main.f:139-199)."""
+    tend = setup.get("tend", 1e30) if tend is None else tend
+    safety = setup["safety"] if safety is None else safety
+    bx, bxm = setup["bx"], setup["bxm"]
+    t, ns, dts = t0, 0, []
+    while True:
+        ns += 1
+        dt, merr = cfl_m_1d(safety, setup["dtmin"], setup["gm"], bx, *state, setup["dx"])
+        if merr:
+            return t, ns, merr, dts
+        t = t + dt
+        dts.append(dt)
+        mlw_m_1d(*state, bx, bxm, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"])
+        apply_bc_program_1d(state, setup["bc"], setup["margin"], setup)
+        if not (ns < nstop and t < tend):
+            return t, ns, 0, dts
+
+
 def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):
     ix, jx, kx = ro.shape
     load().oracle_mlw_m_3d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], dt, qav, gm,

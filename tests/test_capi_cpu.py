@@ -48,4 +48,4 @@ def test_run_desc_layout_matches_header():
     # the ctypes mirror of cans_run_desc must keep the C field order
     fields = [f[0] for f in capi._Desc._fields_]
     assert fields == ["solver", "ix", "jx", "kx", "margin", "gm", "qav", "dx", "dxm", "dy",
-                      "dym", "dz", "dzm", "exact", "tile", "stream"]
+                      "dym", "dz", "dzm", "exact", "tile", "stream", "bx", "bxm"]

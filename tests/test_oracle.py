@@ -240,3 +240,39 @@ def test_3d_cfl_uses_single_precision_pi(oracle_lib):
     ref = 0.4 * np.min(d / np.sqrt(vx**2 + vy**2 + vz**2 + s["gm"] * pr / ro + ca2))
     dt, merr = oracle_lib.cfl_3d(s, s["state"], 0.4)
     assert merr == 0 and abs(dt - ref) <= 2e-15 * ref
+
+
+def test_1d_uniform_state_and_conservation(oracle_lib):
+    n = 64
+    h = 1.0 / 64
+    x = (np.arange(n + 2) - 0.5) * h
+    d, _, dm = setups.grdrdy(x.copy())
+    s = setups.random_state_1d(n + 2, seed=9)
+    s["dx"], s["dxm"] = d, dm
+    s["bxm"] = s["bx"].copy()
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_1d(st, s["bc"], 1, s)
+    m0 = st[0][1:-1].sum()
+    for _ in range(30):
+        dt, _ = oracle_lib.cfl_m_1d(0.4, 1e-10, s["gm"], s["bx"], *st, s["dx"])
+        oracle_lib.mlw_m_1d(*st, s["bx"], s["bxm"], dt, s["qav"], s["gm"], s["dx"], s["dxm"])
+        oracle_lib.apply_bc_program_1d(st, s["bc"], 1, s)
+    assert abs(st[0][1:-1].sum() - m0) <= 1e-13 * m0
+    u = [np.full(n + 2, c) for c in (1.2, 0.7, 0.1, -0.2, 0.9)]
+    for _ in range(3):
+        oracle_lib.mlw_m_1d(*u, s["bx"] * 0 + 1.0, s["bx"] * 0 + 1.0, 1e-3, 1.0, 2.0,
+                            s["dx"], s["dxm"])
+    assert all(np.all(a[1:-1] == a[1]) for a in u)
+
+
+def test_shock_tube_runs_to_tend_and_keeps_wall_condition(oracle_lib):
+    s = setups.shock_tube_1d(256)
+    st = setups.copy_state(s)
+    t, ns, merr, dts = oracle_lib.run_1d(s, st, 10 ** 6)
+    assert merr == 0 and t >= 0.1 and t - dts[-1] < 0.1
+    ro, pr, vx, vy, by = st
+    assert vx[1] == 0.0 and vx[-2] == 0.0 and vx[0] == -vx[2]
+    assert np.all(ro > 0) and np.all(pr > 0)
+    # the wave fan stays inside the box by t = 0.1: far cells keep their
+    # state up to round-off that spreads one cell per step
+    assert abs(ro[5] - 1.0) < 1e-8 and abs(ro[-6] - 0.125) < 1e-8

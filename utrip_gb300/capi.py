@@ -26,6 +26,7 @@ CANS_ERR_ARG = 9400
 SOLVER_MLW_M_2D = 0
 SOLVER_MLW_M3_2D = 1
 SOLVER_MLW_M_3D = 2
+SOLVER_MLW_M_1D = 3
 
 BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
 
@@ -76,6 +77,13 @@ def load() -> C.CDLL:
                                              _dp, _dp, _ip])
     sig["cans_cfl_m_3d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 +
                             [_dp, _ip, _dp, _ip, _dp, _ip])
+    sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
+    sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
+    sig["cans_bdperx_1d"] = (i, [_ip, _ip, _dp, _ip])
+    for fam in ("spp", "spn", "smp", "smn", "fre"):
+        sig[f"cans_bd{fam}x_1d"] = (i, [_ip, _ip, _dp, _ip])
+    sig["cans_bdcnsx_1d"] = (i, [_ip, _ip, _dp, _dp, _ip])
+    sig["cans_bdfrdx_1d"] = (i, [_ip, _ip, _dp, _dp, _ip])
     for ax in "xyz":
         sig[f"cans_bdper{ax}_3d"] = (i, [_ip, _ip, _dp, _ip, _ip, _ip])
         for fam in ("spp", "spn", "smp", "smn", "fre"):
@@ -203,6 +211,42 @@ def bd(kind: int, axis: int, mbnd: int, margin: int, qq: np.ndarray,
     return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _iref(ix), _iref(jx)), name)
 
 
+# ---- drop-in routines (1-D) ------------------------------------------------
+
+def mlw_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, dx, dxm):
+    """cans1d/hdmlw/mlw_m.f:2 -- one mLW step of the 1-D state, in place."""
+    ix = ro.size
+    return _check(load().cans_mlw_m_1d(*[_ptr(a) for a in (ro, pr, vx, vy, by, bx, bxm)],
+                                       _dref(dt), _dref(qav), _dref(gm), _ptr(dx), _ptr(dxm),
+                                       _iref(ix)), "mlw_m_1d")
+
+
+def cfl_m_1d(safety, dtmin, gm, bx, ro, pr, vx, vy, by, dx):
+    """cans1d/common/cfl_m.f:2 -- returns (dt, merr)."""
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m_1d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                _dref(gm), _ptr(bx), *[_ptr(a) for a in (ro, pr, vx, vy, by)],
+                                _ptr(dx), _iref(ro.size)), "cfl_m_1d")
+    return dt.value, merr.value
+
+
+def bd_1d(kind: int, mbnd: int, margin: int, qq: np.ndarray, q0: float = 0.0,
+          dxm: np.ndarray | None = None) -> int:
+    """One reference bd* call on a 1-D array (cans1d/bc/bd*.f)."""
+    lib = load()
+    ix = qq.size
+    if kind == BD_PER:
+        return _check(lib.cans_bdperx_1d(_iref(margin), _iref(margin), _ptr(qq), _iref(ix)),
+                      "bdperx")
+    name = f"cans_bd{_BD_NAMES[kind]}x_1d"
+    f = getattr(lib, name)
+    if kind == BD_CNS:
+        return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _dref(q0), _iref(ix)), name)
+    if kind == BD_FRD:
+        return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _ptr(dxm), _iref(ix)), name)
+    return _check(f(_iref(mbnd), _iref(margin), _ptr(qq), _iref(ix)), name)
+
+
 # ---- drop-in routines (3-D) ------------------------------------------------
 
 def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):
@@ -271,7 +315,8 @@ class _Desc(C.Structure):
     _fields_ = [("solver", C.c_int), ("ix", C.c_int), ("jx", C.c_int), ("kx", C.c_int),
                 ("margin", C.c_int), ("gm", C.c_double), ("qav", C.c_double),
                 ("dx", _dp), ("dxm", _dp), ("dy", _dp), ("dym", _dp), ("dz", _dp), ("dzm", _dp),
-                ("exact", C.c_int), ("tile", C.c_int), ("stream", C.c_void_p)]
+                ("exact", C.c_int), ("tile", C.c_int), ("stream", C.c_void_p),
+                ("bx", _dp), ("bxm", _dp)]
 
 
 class RunState(C.Structure):
@@ -287,19 +332,26 @@ class Run:
                  exact: bool = False, tile: int = -1, stream: int | None = None):
         self.lib = load()
         self.solver = solver
-        self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8}[solver]
+        self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8,
+                     SOLVER_MLW_M_1D: 5}[solver]
         three = solver == SOLVER_MLW_M_3D
-        keys = ("dx", "dxm", "dy", "dym") + (("dz", "dzm") if three else ())
-        self._keep = [np.ascontiguousarray(grid[k], dtype=np.float64) for k in keys]
-        dx, dxm, dy, dym = self._keep[:4]
-        dz, dzm = (self._keep[4], self._keep[5]) if three else (None, None)
-        d = _Desc(solver, dx.size, dy.size, dz.size if three else 1, margin, gm, qav,
-                  dx.ctypes.data_as(_dp), dxm.ctypes.data_as(_dp),
-                  dy.ctypes.data_as(_dp), dym.ctypes.data_as(_dp),
-                  dz.ctypes.data_as(_dp) if three else None,
-                  dzm.ctypes.data_as(_dp) if three else None,
-                  1 if exact else 0, tile, C.c_void_p(stream) if stream else None)
-        self.shape = (dx.size, dy.size) + ((dz.size,) if three else ())
+        one = solver == SOLVER_MLW_M_1D
+
+        def arr(k):
+            a = np.ascontiguousarray(grid[k], dtype=np.float64)
+            self._keep.append(a)
+            return a.ctypes.data_as(_dp)
+
+        self._keep = []
+        nx = np.asarray(grid["dx"]).size
+        ny = 1 if one else np.asarray(grid["dy"]).size
+        nz = np.asarray(grid["dz"]).size if three else 1
+        d = _Desc(solver, nx, ny, nz, margin, gm, qav, arr("dx"), arr("dxm"),
+                  None if one else arr("dy"), None if one else arr("dym"),
+                  arr("dz") if three else None, arr("dzm") if three else None,
+                  1 if exact else 0, tile, C.c_void_p(stream) if stream else None,
+                  arr("bx") if one else None, arr("bxm") if one else None)
+        self.shape = (nx,) if one else ((nx, ny) + ((nz,) if three else ()))
         h = C.c_void_p()
         _check(self.lib.cans_run_create(C.byref(h), C.byref(d)), "cans_run_create")
         self.h = h

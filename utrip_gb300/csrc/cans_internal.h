@@ -82,6 +82,19 @@ cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
                            const Axis &ay, const Axis &az, const Phys &ph,
                            int margin, Ctl *ctl, cudaStream_t s);
 
+// ---- 1-D ------------------------------------------------------------------
+// The whole 1-D loop (or one fixed-dt step) as one cluster launch, in place
+// on 5 arrays (ro,pr,vx,vy,by) of ix doubles.
+int mlw1d_cluster_size();
+cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
+                         const double *bxm, int ix, const Axis &ax,
+                         const Phys &ph, const BcTable &bc, Ctl *ctl,
+                         int max_steps, int fixed, double dt_fixed, int start,
+                         cudaStream_t s);
+cudaError_t launch_cfl1d(bool exact, const double *S, const double *bx, int ix,
+                         const Axis &ax, const Phys &ph, double safety,
+                         unsigned long long *out, cudaStream_t s);
+
 // ---- single bd* operation on one array (literal entry points) -------------
 // kind/axis/mbnd follow the reference routine; dims = (n0, n1, n2).
 cudaError_t launch_bd_one(int kind, int axis, int mbnd, int margin0,

@@ -451,6 +451,138 @@ extern "C" int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq,
 }
 
 // ---------------------------------------------------------------------------
+// 1-D drop-in entry points
+namespace {
+// device copies of the constant bx, bxm arrays of the 1-D step
+struct Dev1D {
+  double *bx = nullptr;
+  int cap = 0;
+  int upload(int ix, const double *hbx, const double *hbxm, cudaStream_t s) {
+    if (cap < ix) {
+      if (bx) cudaFree(bx);
+      bx = nullptr;
+      cap = 0;
+      CK(cudaMalloc(&bx, sizeof(double) * 2 * (size_t)ix));
+      cap = ix;
+    }
+    CK(cudaMemcpyAsync(bx, hbx, sizeof(double) * ix, cudaMemcpyHostToDevice, s));
+    if (hbxm)
+      CK(cudaMemcpyAsync(bx + ix, hbxm, sizeof(double) * ix, cudaMemcpyHostToDevice, s));
+    return CANS_OK;
+  }
+};
+Dev1D g_dev1d;
+}  // namespace
+
+extern "C" int cans_mlw_m_1d(double *ro, double *pr, double *vx, double *vy,
+                             double *by, const double *bx, const double *bxm,
+                             const double *dt, const double *qav,
+                             const double *gm, const double *dx,
+                             const double *dxm, const int *ix) {
+  const int n = *ix;
+  if (n < 2 * mlw1d_cluster_size() + 2) return CANS_ERR_ARG;
+  double *arrs[5] = {ro, pr, vx, vy, by};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, *qav);
+  BcTable bc{};
+  bc.margin = 1;
+  MirrorSet *m = resident_step_set(arrs, 5);
+  DevAxis *dax = m ? &m->ax : &g_scratch.ax;
+  if ((rc = dax->upload(n, dx, dxm, s))) return rc;
+  if ((rc = g_dev1d.upload(n, bx, bxm, s))) return rc;
+  double *S;
+  if (m) {
+    S = m->buf[m->cur];  // the 1-D kernel updates its state in place
+  } else {
+    if ((rc = g_scratch.ensure(5 * (size_t)n))) return rc;
+    for (int v = 0; v < 5; v++)
+      CK(cudaMemcpyAsync(g_scratch.A + (size_t)v * n, arrs[v], sizeof(double) * n,
+                         cudaMemcpyHostToDevice, s));
+    S = g_scratch.A;
+  }
+  CK(launch_mlw1d(exact_mode(), S, g_dev1d.bx, g_dev1d.bx + n, n, dax->a, ph, bc,
+                  nullptr, 1, 1, *dt, 0, s));
+  if (m) return CANS_OK;
+  for (int v = 0; v < 5; v++)
+    CK(cudaMemcpyAsync(arrs[v], g_scratch.A + (size_t)v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+extern "C" int cans_cfl_m_1d(double *dt, const double *safety,
+                             const double *dtmin, int *merr, const double *gm,
+                             const double *bx, const double *ro,
+                             const double *pr, const double *vx,
+                             const double *vy, const double *by,
+                             const double *dx, const int *ix) {
+  const int n = *ix;
+  if (n < 3) return CANS_ERR_ARG;
+  const double *arrs[5] = {ro, pr, vx, vy, by};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, 0.0);
+  MirrorSet *m = resident_step_set(const_cast<double *const *>(arrs), 5);
+  DevAxis *dax = m ? &m->ax : &g_scratch.ax;
+  if ((rc = dax->upload(n, dx, dx, s))) return rc;
+  if ((rc = g_dev1d.upload(n, bx, nullptr, s))) return rc;
+  if ((rc = g_scratch.ensure(5 * (size_t)n))) return rc;
+  const double *S;
+  if (m) {
+    S = m->buf[m->cur];
+  } else {
+    for (int v = 0; v < 5; v++)
+      CK(cudaMemcpyAsync(g_scratch.A + (size_t)v * n, arrs[v], sizeof(double) * n,
+                         cudaMemcpyHostToDevice, s));
+    S = g_scratch.A;
+  }
+  const double d0 = (double)1.e20f;
+  unsigned long long init;
+  std::memcpy(&init, &d0, sizeof init);
+  CK(cudaMemcpyAsync(g_scratch.bits, &init, sizeof init, cudaMemcpyHostToDevice, s));
+  CK(launch_cfl1d(exact_mode(), S, g_dev1d.bx, n, dax->a, ph, *safety,
+                  g_scratch.bits, s));
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(&out, g_scratch.bits, sizeof out, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *dt = bits_to_double(out);
+  *merr = (*dt < *dtmin) ? 9001 : 0;
+  return CANS_OK;
+}
+
+#define CANS_BD1(NAME, KIND)                                                    \
+  extern "C" int NAME(const int *mbnd, const int *margin, double *qq,           \
+                      const int *ix) {                                           \
+    return bd_call(KIND, 0, *mbnd, *margin, *margin, qq, 0.0, nullptr, *ix, 1,  \
+                   1);                                                           \
+  }
+CANS_BD1(cans_bdsppx_1d, BD_SPP)
+CANS_BD1(cans_bdspnx_1d, BD_SPN)
+CANS_BD1(cans_bdsmpx_1d, BD_SMP)
+CANS_BD1(cans_bdsmnx_1d, BD_SMN)
+CANS_BD1(cans_bdfrex_1d, BD_FRE)
+#undef CANS_BD1
+extern "C" int cans_bdperx_1d(const int *margin0, const int *margin1,
+                              double *qq, const int *ix) {
+  int rc = bd_call(BD_PER, 0, 0, *margin0, *margin1, qq, 0.0, nullptr, *ix, 1, 1);
+  if (rc) return rc;
+  return bd_call(BD_PER, 0, 1, *margin0, *margin1, qq, 0.0, nullptr, *ix, 1, 1);
+}
+extern "C" int cans_bdcnsx_1d(const int *mbnd, const int *margin, double *qq,
+                              const double *q0, const int *ix) {
+  return bd_call(BD_CNS, 0, *mbnd, *margin, *margin, qq, *q0, nullptr, *ix, 1, 1);
+}
+extern "C" int cans_bdfrdx_1d(const int *mbnd, const int *margin, double *qq,
+                              const double *dxm, const int *ix) {
+  return bd_call(BD_FRD, 0, *mbnd, *margin, *margin, qq, 0.0, dxm, *ix, 1, 1);
+}
+
+// ---------------------------------------------------------------------------
 // 3-D drop-in entry points
 extern "C" int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy,
                              double *vz, double *bx, double *by, double *bz,
@@ -694,6 +826,7 @@ struct cans_run {
   cudaGraphExec_t graph = nullptr;
   int graph_iters = 0;
   int graph_nodes = 0;
+  double *bx1 = nullptr;       // 1-D: device bx (ix) followed by bxm (ix)
 };
 
 namespace {
@@ -703,12 +836,22 @@ int solver_nvar(int solver) {
     case CANS_SOLVER_MLW_M_2D: return 7;
     case CANS_SOLVER_MLW_M3_2D: return 9;
     case CANS_SOLVER_MLW_M_3D: return 8;
+    case CANS_SOLVER_MLW_M_1D: return 5;
     default: return 0;
   }
 }
-int solver_ndim(int solver) { return solver == CANS_SOLVER_MLW_M_3D ? 3 : 2; }
+int solver_ndim(int solver) {
+  return solver == CANS_SOLVER_MLW_M_3D ? 3 : (solver == CANS_SOLVER_MLW_M_1D ? 1 : 2);
+}
 int tile_count(const cans_run *h) {
-  return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
+  return h->ndim == 3 ? mlw3d_tile_count() : (h->ndim == 1 ? 1 : mlw2d_tile_count());
+}
+// 1-D: the whole loop (or one fixed step) as one cluster launch, in place
+cudaError_t launch_1d(cans_run *h, int max_steps, int fixed, double dt,
+                      int start) {
+  return launch_mlw1d(h->d.exact != 0, h->buf[0], h->bx1, h->bx1 + h->d.ix,
+                      h->d.ix, h->ax.a, h->ph, h->bc, fixed ? nullptr : h->ctl,
+                      max_steps, fixed, dt, start, h->s);
 }
 
 // cells whose CFL the step kernel reduces: all but the frame of width
@@ -820,15 +963,21 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   // every extent must exceed the two frames of margin+1 cells that the
   // boundary program and the frame CFL work on
   const int wmin = 2 * (d->margin + 1) + 1;
-  if (d->ix < wmin || d->jx < wmin) return CANS_ERR_ARG;
-  if (ndim == 2 && d->kx != 1) return CANS_ERR_ARG;
-  if (ndim == 3 && (d->kx < wmin || !d->dz || !d->dzm)) return CANS_ERR_ARG;
-  if (!d->dx || !d->dxm || !d->dy || !d->dym) return CANS_ERR_ARG;
+  if (ndim == 1) {
+    if (d->ix < 2 * mlw1d_cluster_size() + 2 || d->jx != 1 || d->kx != 1 ||
+        !d->dx || !d->dxm || !d->bx || !d->bxm)
+      return CANS_ERR_ARG;
+  } else {
+    if (d->ix < wmin || d->jx < wmin) return CANS_ERR_ARG;
+    if (ndim == 2 && d->kx != 1) return CANS_ERR_ARG;
+    if (ndim == 3 && (d->kx < wmin || !d->dz || !d->dzm)) return CANS_ERR_ARG;
+    if (!d->dx || !d->dxm || !d->dy || !d->dym) return CANS_ERR_ARG;
+  }
   auto *h = new cans_run();
   h->d = *d;
   h->ndim = ndim;
   h->nvar = nvar;
-  h->n = (size_t)d->ix * d->jx * (ndim == 3 ? d->kx : 1);
+  h->n = (size_t)d->ix * (ndim >= 2 ? d->jx : 1) * (ndim == 3 ? d->kx : 1);
   h->ph = make_phys(d->gm, d->qav);
   h->tile = d->tile >= 0 && d->tile < tile_count(h) ? d->tile : 0;
   h->bc.margin = d->margin;
@@ -858,8 +1007,17 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   cudaError_t e = cudaMalloc(&h->ctl, sizeof(Ctl));
   if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(ctl)"));
   if ((rc = h->ax.upload(d->ix, d->dx, d->dxm, h->s))) return bail(rc);
-  if ((rc = h->ay.upload(d->jx, d->dy, d->dym, h->s))) return bail(rc);
+  if (ndim >= 2 && (rc = h->ay.upload(d->jx, d->dy, d->dym, h->s))) return bail(rc);
   if (ndim == 3 && (rc = h->az.upload(d->kx, d->dz, d->dzm, h->s))) return bail(rc);
+  if (ndim == 1) {
+    e = cudaMalloc(&h->bx1, sizeof(double) * 2 * (size_t)d->ix);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(bx)"));
+    e = cudaMemcpyAsync(h->bx1, d->bx, sizeof(double) * d->ix, cudaMemcpyHostToDevice, h->s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->bx1 + d->ix, d->bxm, sizeof(double) * d->ix,
+                          cudaMemcpyHostToDevice, h->s);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy(bx)"));
+  }
   std::memset(&h->host_ctl, 0, sizeof(Ctl));
   h->host_ctl.done = 1;
   h->host_ctl.buf[0] = h->buf[0];
@@ -879,6 +1037,7 @@ extern "C" int cans_run_destroy(cans_run *h) {
   for (int b = 0; b < 2; b++)
     if (h->buf[b]) cudaFree(h->buf[b]);
   if (h->ctl) cudaFree(h->ctl);
+  if (h->bx1) cudaFree(h->bx1);
   h->ax.release();
   h->ay.release();
   h->az.release();
@@ -956,6 +1115,10 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
   h->host_ctl = c;
   CK(cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice,
                      h->s));
+  if (h->ndim == 1) {  // first CFL and loop start inside the cluster kernel
+    CK(launch_1d(h, 0, 0, 0.0, 1));
+    return CANS_OK;
+  }
   CK(cfl_full_kernel(h, h->buf[c.cur], safety, &h->ctl->cfl_bits));
   CK(launch_prepare(h->ctl, h->s));
   return CANS_OK;
@@ -964,6 +1127,10 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
 extern "C" int cans_run_advance(cans_run *h, int iters) {
   if (!h || iters < 0) return CANS_ERR_ARG;
   if (iters == 0) return CANS_OK;
+  if (h->ndim == 1) {
+    CK(launch_1d(h, iters, 0, 0.0, 0));
+    return CANS_OK;
+  }
   const int chunk = iters < 32 ? iters : 32;
   if (!h->graph || h->graph_iters != chunk) {
     int rc = build_graph(h, chunk);
@@ -1010,6 +1177,12 @@ extern "C" int cans_run_step(cans_run *h, const double *dt, int apply_bc) {
   if (!h || !dt) return CANS_ERR_ARG;
   int rc = read_ctl(h);
   if (rc) return rc;
+  if (h->ndim == 1) {  // in place; the boundary program needs the loop kernel
+    if (apply_bc) return CANS_ERR_ARG;
+    CK(launch_1d(h, 1, 1, *dt, 0));
+    CK(cudaStreamSynchronize(h->s));
+    return CANS_OK;
+  }
   const int cur = h->host_ctl.cur;
   CK(step_kernel(h, h->tile, h->buf[cur], h->buf[cur ^ 1], *dt, nullptr, Box3{}));
   if (apply_bc) CK(bc_kernels(h, h->buf[cur ^ 1], nullptr));
@@ -1030,7 +1203,11 @@ extern "C" int cans_run_cfl(cans_run *h, double safety, double *dt) {
   const unsigned long long save = h->host_ctl.cfl_bits;
   const unsigned long long init = r4_1e20_bits();
   CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, h->s));
-  CK(cfl_full_kernel(h, h->buf[h->host_ctl.cur], safety, bits));
+  if (h->ndim == 1)
+    CK(launch_cfl1d(h->d.exact != 0, h->buf[0], h->bx1, h->d.ix, h->ax.a, h->ph,
+                    safety, bits, h->s));
+  else
+    CK(cfl_full_kernel(h, h->buf[h->host_ctl.cur], safety, bits));
   unsigned long long out = 0;
   CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, h->s));
   CK(cudaMemcpyAsync(bits, &save, sizeof save, cudaMemcpyHostToDevice, h->s));
@@ -1042,6 +1219,22 @@ extern "C" int cans_run_cfl(cans_run *h, double safety, double *dt) {
 extern "C" int cans_run_profile(cans_run *h, int iters, double *step_ms,
                                 double *iter_ms) {
   if (!h || iters < 1 || !step_ms || !iter_ms) return CANS_ERR_ARG;
+  if (h->ndim == 1) {  // one launch runs every iteration
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, h->s));
+    CK(launch_1d(h, iters, 0, 0.0, 0));
+    CK(cudaEventRecord(b, h->s));
+    CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *step_ms = ms;
+    *iter_ms = ms;
+    return CANS_OK;
+  }
   std::vector<cudaEvent_t> ev(3 * (size_t)iters);
   for (auto &e : ev) CK(cudaEventCreate(&e));
   const Box3 box = inner_box(h);
@@ -1070,6 +1263,10 @@ extern "C" int cans_run_profile(cans_run *h, int iters, double *step_ms,
 
 extern "C" int cans_run_autotune(cans_run *h, int trial_steps, int *tile) {
   if (!h || trial_steps < 1) return CANS_ERR_ARG;
+  if (h->ndim == 1) {  // a single configuration
+    if (tile) *tile = 0;
+    return CANS_OK;
+  }
   int rc = read_ctl(h);
   if (rc) return rc;
   const int cur = h->host_ctl.cur;

@@ -1,0 +1,481 @@
+// 1-D modified Lax-Wendroff time loop as one thread-block-cluster kernel
+// (sm_103a, FP64).
+//
+// Replaces the 1-D reference loop of cans1d/md_mhdshktb/hdmlw/main.f:139-152:
+// cfl_m (cans1d/common/cfl_m.f:42-71) -> t += dt -> mlw_m
+// (cans1d/hdmlw/mlw_m.f:2-215 with mlwhalf.f:33-46, mlwfull.f:30-33,
+// mlwartv.f:31-34) -> bnd (bdsppx / bdsmnx ...) -> output and loop tests.
+//
+// A 1-D grid of ~10^3 cells is far too small to fill the GPU and a kernel
+// per stage would be launch-bound, so the whole loop runs inside one launch of
+// a cluster of CS blocks.  Each block keeps its segment of the grid (plus one
+// halo cell per side) in shared memory for the whole run; after each step
+// neighbours exchange halo cells through distributed shared memory and the
+// CFL minimum is reduced across the cluster, so no host round trip happens
+// per step.  Three cluster barriers per step: after the update, after the
+// boundary fill, after the halo exchange and CFL reduction.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "cans_common.cuh"
+#include "cans_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace cans {
+
+namespace {
+// primitive order: ro pr vx vy by ; conserved order: ro ee rx ry by
+constexpr int NV1 = 5;
+}  // namespace
+
+struct Run1D {
+  double *S;             // global state, 5 arrays of ix (read at start, written at end)
+  const double *bx, *bxm;
+  Axis ax;
+  Phys ph;
+  BcTable bc;
+  Ctl *ctl;              // loop control (resident run) or nullptr
+  int ix;
+  int seg;               // interior cells per block
+  int lmax;              // seg + 2
+  int max_steps;         // steps this launch may take
+  int fixed;             // 1: one step with dt_fixed, no CFL / boundary fill
+  double dt_fixed;
+  int start;             // 1: compute the first CFL and start the loop
+};
+
+// one reference bd* rule on the global line, through an accessor
+template <class Get, class Put>
+__device__ void bd1_face(int kind, int mbnd, int m, int n, double q0,
+                         const double *dxm, Get get, Put put) {
+  if (kind < 0) return;
+  if (kind == BD_PER) {
+    const int b0 = 1 + m, b1 = n - m;
+    if (mbnd == 0)
+      for (int i = 1; i <= m; i++) put(b0 - i, get(b1 + 1 - i));
+    else
+      for (int i = 1; i <= m; i++) put(b1 + i, get(b0 - 1 + i));
+    return;
+  }
+  if (mbnd == 0) {
+    const int b = 1 + m;
+    switch (kind) {
+      case BD_SPP: for (int i = 1; i <= m; i++) put(b - i, get(b - 1 + i)); break;
+      case BD_SPN: for (int i = 1; i <= m; i++) put(b - i, -get(b - 1 + i)); break;
+      case BD_SMP: for (int i = 1; i <= m; i++) put(b - i, get(b + i)); break;
+      case BD_SMN:
+        for (int i = 1; i <= m; i++) put(b - i, -get(b + i));
+        put(b, 0.0);
+        break;
+      case BD_FRE: for (int i = 1; i <= m; i++) put(b - i, get(b)); break;
+      case BD_CNS: for (int i = 1; i <= m; i++) put(b - i, q0); break;
+      case BD_FRD:
+        for (int i = 1; i <= m; i++) {
+          const double dqq = __ddiv_rn(__dsub_rn(get(b + 1), get(b)), dxm[b - 1]);
+          put(b - i, __dsub_rn(get(b - i + 1), __dmul_rn(dqq, dxm[b - i - 1])));
+        }
+        break;
+      default: break;
+    }
+  } else {
+    const int b = n - m;
+    switch (kind) {
+      case BD_SPP: for (int i = 1; i <= m; i++) put(b + i, get(b + 1 - i)); break;
+      case BD_SPN: for (int i = 1; i <= m; i++) put(b + i, -get(b + 1 - i)); break;
+      case BD_SMP: for (int i = 1; i <= m; i++) put(b + i, get(b - i)); break;
+      case BD_SMN:
+        for (int i = 1; i <= m; i++) put(b + i, -get(b - i));
+        put(b, 0.0);
+        break;
+      case BD_FRE: for (int i = 1; i <= m; i++) put(b + i, get(b)); break;
+      case BD_CNS: for (int i = 1; i <= m; i++) put(b + i, q0); break;
+      case BD_FRD:
+        for (int i = 1; i <= m; i++) {
+          const double dqq = __ddiv_rn(__dsub_rn(get(b), get(b - 1)), dxm[b - 2]);
+          put(b + i, __dadd_rn(get(b + i - 1), __dmul_rn(dqq, dxm[b + i - 2])));
+        }
+        break;
+      default: break;
+    }
+  }
+}
+
+template <bool E>
+__global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
+  using FT = F<E>;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const int ix = p.ix, L = p.lmax;
+  extern __shared__ double sm[];
+  // layout: prim[2][5][L], U[5][L], FX[5][L], K[5][L], Q[L], slots[2][CS], red[32]
+  double *prim = sm;
+  double *U = prim + 2 * NV1 * L;
+  double *FX = U + NV1 * L;
+  double *K = FX + NV1 * L;
+  double *Q = K + NV1 * L;
+  double *slots = Q + L;
+  double *red = slots + 2 * CS;
+  __shared__ double s_dt, s_t, s_tp;
+  __shared__ long long s_ns, s_nexec;
+  __shared__ int s_done, s_merr, s_pause;
+
+  // interior cells (0-based 1..ix-2) split evenly; local l <-> global lo-1+l
+  const int lo = 1 + r * p.seg;
+  const int hi = min(ix - 2, lo + p.seg - 1);
+  const int nl = hi - lo + 3;  // local cells incl. one halo each side
+  const FT gm(p.ph.gm), gm1(p.ph.gm1), pi8i(p.ph.pi8i), pi4i(p.ph.pi4i),
+      qav(p.ph.qav);
+  const Axis &ax = p.ax;
+  const int NVS = NV1 * L;  // stride of one prim buffer
+
+  auto P = [&](int buf, int v, int l) -> double & {
+    return prim[(size_t)buf * NVS + (size_t)v * L + l];
+  };
+  // load own segment, halos and ghosts from global memory
+  for (int l = tid; l < nl; l += NT) {
+    const int g = lo - 1 + l;
+#pragma unroll
+    for (int v = 0; v < NV1; v++) P(0, v, l) = p.S[(size_t)v * ix + g];
+  }
+  if (tid == 0) {
+    if (p.ctl) {
+      s_dt = p.ctl->dt; s_t = p.ctl->t; s_tp = p.ctl->tp; s_ns = p.ctl->ns;
+      s_nexec = p.ctl->nexec; s_done = p.ctl->done; s_merr = p.ctl->merr;
+      s_pause = p.ctl->pause;
+    } else {
+      s_dt = p.dt_fixed; s_t = 0.0; s_tp = 0.0; s_ns = 0; s_nexec = 0;
+      s_done = 0; s_merr = 0; s_pause = 0;
+    }
+  }
+  int cur = 0;
+  __syncthreads();
+
+  // CFL of the own cells (cfl_m.f:53-60) reduced over the cluster into
+  // slots[par] of block 0; returns the minimum after a cluster barrier.
+  auto cluster_cfl = [&](int buf, int par) -> double {
+    double dmin = __longlong_as_double(0x7ff0000000000000LL);
+    const FT safety(p.ctl ? p.ctl->safety : 1.0), pi4c(p.ph.pi4i);
+    for (int l = 1 + tid; l <= nl - 2; l += NT) {
+      const int g = lo - 1 + l;
+      const FT ro(P(buf, 0, l)), pr(P(buf, 1, l)), vx(P(buf, 2, l)), by(P(buf, 4, l));
+      const FT bx(p.bx[g]);
+      const FT onero = 1.0 / ro;
+      const FT ca2 = (bx * bx + by * by) * pi4c * onero;
+      const FT cs2 = gm * pr * onero;
+      const FT dtcfl = FT(ax.d[g]) / (fabs_(vx) + fsqrt(cs2 + ca2));
+      const double dtq = (safety * dtcfl).v;
+      if (dtq < dmin || dmin != dmin) dmin = dtq;
+    }
+    dmin = warp_min(dmin);
+    if ((tid & 31) == 0) red[tid >> 5] = dmin;
+    __syncthreads();
+    if (tid == 0) {
+      double x = red[0];
+      for (int w = 1; w < (NT + 31) / 32; w++) x = (red[w] < x || x != x) ? red[w] : x;
+      double *dst = cluster.map_shared_rank(slots, 0);
+      dst[par * CS + r] = x;
+    }
+    cluster.sync();
+    double *src = cluster.map_shared_rank(slots, 0);
+    double m = (double)1.e20f;  // the reference's starting minimum
+    for (int k = 0; k < CS; k++) {
+      const double x = src[par * CS + k];
+      if (x < m) m = x;
+    }
+    return m;
+  };
+
+  int par = 0;
+  if (!p.fixed && p.start) {
+    const double dt0 = cluster_cfl(cur, par);
+    par ^= 1;
+    if (tid == 0) {  // first iteration always starts (do-while loop)
+      s_ns += 1;
+      s_dt = dt0;
+      if (dt0 < p.ctl->dtmin) {
+        s_merr = 9001;
+        s_done = 1;
+      } else {
+        s_tp = s_t;
+        s_t = s_t + dt0;
+      }
+    }
+    __syncthreads();
+  }
+
+  for (int step = 0; step < p.max_steps; step++) {
+    if (s_done || s_pause) break;
+    const FT dt(s_dt);
+    const int nb = cur ^ 1;
+    // ---- cell stage (mlw_m.f:37-73) --------------------------------------
+    for (int l = tid; l < nl; l += NT) {
+      const int g = lo - 1 + l;
+      const FT ro(P(cur, 0, l)), pr(P(cur, 1, l)), vx(P(cur, 2, l)), vy(P(cur, 3, l)),
+          by(P(cur, 4, l));
+      const FT bx(p.bx[g]);
+      const FT vv = vx * vx + vy * vy;
+      const FT bb = by * by;
+      FT ee, ep;
+      if constexpr (E) {
+        ee = pr / gm1 + 0.5 * ro * vv + pi8i * bb;
+        ep = pr * gm / gm1 + 0.5 * ro * vv;
+      } else {
+        ee = pr * p.ph.gm1i + 0.5 * ro * vv + pi8i * bb;
+        ep = pr * p.ph.ggm1 + 0.5 * ro * vv;
+      }
+      const FT rx = ro * vx;
+      const FT ez = -vx * by + vy * bx;
+      U[0 * L + l] = ro.v; U[1 * L + l] = ee.v; U[2 * L + l] = rx.v;
+      U[3 * L + l] = (ro * vy).v; U[4 * L + l] = by.v;
+      FX[0 * L + l] = rx.v;                                        // ro*vx
+      FX[1 * L + l] = (ep * vx - by * ez * pi4i).v;                 // :55
+      FX[2 * L + l] = (ro * (vx * vx) + pr + by * by * pi8i).v;     // :60-61
+      FX[3 * L + l] = (ro * vx * vy - bx * by * pi4i).v;            // :66
+      FX[4 * L + l] = (-ez).v;                                      // :71
+    }
+    __syncthreads();
+    // ---- corners (mlwhalf.f:42-46, mlw_m.f:74-110) and AV faces -----------
+    for (int l = tid; l < nl - 1; l += NT) {
+      const int g = lo - 1 + l;  // corner between g and g+1
+      const FT dxim(ax.dim[g]);
+      FT un[NV1];
+#pragma unroll
+      for (int v = 0; v < NV1; v++) {
+        const FT uh = 0.5 * (FT(U[v * L + l + 1]) + FT(U[v * L + l]));
+        const FT dfdx = dxim * (FT(FX[v * L + l + 1]) - FT(FX[v * L + l]));
+        un[v] = uh - dt * dfdx;
+      }
+      const FT roh = un[0], eeh = un[1], rxh = un[2], ryh = un[3], byh = un[4];
+      FT vxh, vyh;
+      if constexpr (E) {
+        vxh = rxh / roh;
+        vyh = ryh / roh;
+      } else {
+        const FT rinv(1.0 / roh.v);
+        vxh = rxh * rinv;
+        vyh = ryh * rinv;
+      }
+      const FT vv = vxh * vxh + vyh * vyh;
+      const FT bb = byh * byh;
+      const FT prh = gm1 * (eeh - 0.5 * roh * vv - pi8i * bb);
+      const FT bxm(p.bxm[g]);
+      const FT ezh = -vxh * byh + vyh * bxm;
+      FT eph;
+      if constexpr (E) eph = prh * gm / gm1 + 0.5 * roh * vv;
+      else eph = prh * p.ph.ggm1 + 0.5 * roh * vv;
+      K[0 * L + l] = (roh * vxh).v;
+      K[1 * L + l] = (eph * vxh - byh * ezh * pi4i).v;
+      K[2 * L + l] = (roh * (vxh * vxh) + prh + byh * byh * pi8i).v;
+      K[3 * L + l] = (roh * vxh * vyh - bxm * byh * pi4i).v;
+      K[4 * L + l] = (-ezh).v;
+      const FT q = qav * FT(ax.dm[g]) *
+                   max0(fabs_(FT(P(cur, 2, l + 1)) - FT(P(cur, 2, l))) - CANS_AV_EPS);
+      Q[l] = (q * dxim).v;
+    }
+    __syncthreads();
+    // ---- full step of the own cells ---------------------------------------
+    for (int l = 1 + tid; l <= nl - 2; l += NT) {
+      const int g = lo - 1 + l;
+      const FT hdt = 0.5 * dt, dxi(ax.di[g]);
+      const FT hdx = 0.5 * dxi;
+      FT u[NV1];
+#pragma unroll
+      for (int v = 0; v < NV1; v++) {
+        FT du(0.0);
+        du = du - hdt * (hdx * (FT(FX[v * L + l + 1]) - FT(FX[v * L + l - 1])));
+        du = du - hdt * (dxi * (FT(K[v * L + l]) - FT(K[v * L + l - 1])));
+        const FT uc(U[v * L + l]);
+        du = du + dt * (dxi * (FT(Q[l]) * (FT(U[v * L + l + 1]) - uc) -
+                               FT(Q[l - 1]) * (uc - FT(U[v * L + l - 1]))));
+        u[v] = uc + du;
+      }
+      const FT ro = u[0], ee = u[1], rx = u[2], ry = u[3], by = u[4];
+      FT vx, vy;
+      if constexpr (E) {
+        vx = rx / ro;
+        vy = ry / ro;
+      } else {
+        const FT rinv(1.0 / ro.v);
+        vx = rx * rinv;
+        vy = ry * rinv;
+      }
+      const FT pr = gm1 * (ee - 0.5 * ro * (vx * vx + vy * vy) - pi8i * (by * by));
+      P(nb, 0, l) = ro.v; P(nb, 1, l) = pr.v; P(nb, 2, l) = vx.v;
+      P(nb, 3, l) = vy.v; P(nb, 4, l) = by.v;
+    }
+    // ghost cells keep their values through the step
+    if (tid == 0) {
+      if (lo == 1)
+        for (int v = 0; v < NV1; v++) P(nb, v, 0) = P(cur, v, 0);
+      if (hi == ix - 2)
+        for (int v = 0; v < NV1; v++) P(nb, v, nl - 1) = P(cur, v, nl - 1);
+    }
+    cluster.sync();
+    if (p.fixed) {
+      cur = nb;
+      break;
+    }
+    // ---- boundary program (bnd.f:9-19): lower face by block 0, upper face
+    // by the last block; cells of other blocks are read through DSMEM -------
+    if (tid < NV1 && (r == 0 || r == CS - 1)) {
+      const int v = tid;
+      auto owner = [&](int g1) {  // 1-based global cell -> (rank, local)
+        const int g = g1 - 1;
+        int rr = (g <= 0) ? 0 : (g >= ix - 1 ? CS - 1 : (g - 1) / p.seg);
+        if (rr > CS - 1) rr = CS - 1;
+        const int l = g - (1 + rr * p.seg) + 1;
+        return make_int2(rr, l);
+      };
+      auto get = [&](int g1) -> double {
+        const int2 o = owner(g1);
+        double *base = cluster.map_shared_rank(prim, o.x);
+        return base[(size_t)nb * NVS + (size_t)v * L + o.y];
+      };
+      auto put = [&](int g1, double x) {
+        const int2 o = owner(g1);
+        P(nb, v, o.y) = x;  // faces only write cells of this block
+      };
+      if (r == 0)
+        bd1_face(p.bc.kind[v][0], 0, p.bc.margin, ix, p.bc.q0[v][0], ax.dm, get, put);
+      if (r == CS - 1)
+        bd1_face(p.bc.kind[v][1], 1, p.bc.margin, ix, p.bc.q0[v][1], ax.dm, get, put);
+    }
+    cluster.sync();
+    // ---- halo exchange and CFL of the new state ----------------------------
+    if (tid < NV1) {
+      if (r > 0) {
+        const double *nbp = cluster.map_shared_rank(prim, r - 1);
+        const int ln = p.seg;  // neighbour's last own cell (local index seg)
+        P(nb, tid, 0) = nbp[(size_t)nb * NVS + (size_t)tid * L + ln];
+      }
+      if (r < CS - 1) {
+        const double *nbp = cluster.map_shared_rank(prim, r + 1);
+        P(nb, tid, nl - 1) = nbp[(size_t)nb * NVS + (size_t)tid * L + 1];
+      }
+    }
+    __syncthreads();
+    const double dtn = cluster_cfl(nb, par);
+    par ^= 1;
+    cur = nb;
+    if (tid == 0) {
+      // end of the loop body (main.f:155-199) and start of the next
+      s_nexec += 1;
+      if (p.ctl->pause_on_output && p.ctl->dtout > 0.0) {
+        const long long nt1 = (long long)(s_tp / p.ctl->dtout);
+        const long long nt2 = (long long)(s_t / p.ctl->dtout);
+        if (nt1 < nt2) s_pause = 1;
+      }
+      if (!(s_ns < p.ctl->nstop && s_t < p.ctl->tend)) {
+        s_done = 1;
+      } else {
+        s_ns += 1;
+        s_dt = dtn;
+        if (dtn < p.ctl->dtmin) {
+          s_merr = 9001;
+          s_done = 1;
+        } else {
+          s_tp = s_t;
+          s_t = s_t + dtn;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // keep remote reads of this block's shared memory valid until all are done
+  cluster.sync();
+  // write the own segment (and ghosts) back
+  for (int l = tid; l < nl; l += NT) {
+    const int g = lo - 1 + l;
+    const bool own = (l >= 1 && l <= nl - 2) || (g == 0) || (g == ix - 1);
+    if (!own) continue;
+#pragma unroll
+    for (int v = 0; v < NV1; v++) p.S[(size_t)v * ix + g] = P(cur, v, l);
+  }
+  if (r == 0 && tid == 0 && p.ctl) {
+    p.ctl->dt = s_dt; p.ctl->t = s_t; p.ctl->tp = s_tp; p.ctl->ns = s_ns;
+    p.ctl->nexec = s_nexec; p.ctl->done = s_done; p.ctl->merr = s_merr;
+    p.ctl->pause = s_pause;
+  }
+}
+
+int mlw1d_cluster_size() { return 8; }
+
+// Host launcher: the cluster kernel over a state of 5 arrays of ix doubles,
+// updated in place.
+cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
+                         const double *bxm, int ix, const Axis &ax,
+                         const Phys &ph, const BcTable &bc, Ctl *ctl,
+                         int max_steps, int fixed, double dt_fixed, int start,
+                         cudaStream_t s) {
+  const int CS = mlw1d_cluster_size();
+  if (ix < 2 * CS + 2) return cudaErrorInvalidValue;
+  Run1D p{};
+  p.S = S; p.bx = bx; p.bxm = bxm; p.ax = ax; p.ph = ph; p.bc = bc; p.ctl = ctl;
+  p.ix = ix;
+  p.seg = (ix - 2 + CS - 1) / CS;
+  p.lmax = p.seg + 2;
+  p.max_steps = max_steps;
+  p.fixed = fixed;
+  p.dt_fixed = dt_fixed;
+  p.start = start;
+  // the last block must own at least margin+1 cells for the boundary rules
+  if ((ix - 2) - (CS - 1) * p.seg < bc.margin + 1 || p.seg < bc.margin + 1)
+    return cudaErrorInvalidValue;
+  const size_t smem = sizeof(double) * ((size_t)(2 * NV1 + 3 * NV1 + 1) * p.lmax + 2 * CS + 32);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  void (*kern)(Run1D) = exact ? k_mlw1d<true> : k_mlw1d<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(CS, 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, p);
+  count_launch();
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// Standalone 1-D CFL (cfl_m.f:42-71) on interior cells, one block.
+template <bool E>
+__global__ void k_cfl1d(const double *S, const double *bx, int ix, Axis ax,
+                        Phys ph, double safety, unsigned long long *out) {
+  using FT = F<E>;
+  __shared__ double red[32];
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  const FT gm(ph.gm), pi4i(ph.pi4i);
+  for (int g = 1 + threadIdx.x; g <= ix - 2; g += blockDim.x) {
+    const FT ro(S[g]), pr(S[(size_t)ix + g]), vx(S[2 * (size_t)ix + g]),
+        by(S[4 * (size_t)ix + g]), b(bx[g]);
+    const FT onero = 1.0 / ro;
+    const FT ca2 = (b * b + by * by) * pi4i * onero;
+    const FT cs2 = gm * pr * onero;
+    const FT dtcfl = FT(ax.d[g]) / (fabs_(vx) + fsqrt(cs2 + ca2));
+    const double dtq = (FT(safety) * dtcfl).v;
+    if (dtq < dmin) dmin = dtq;
+  }
+  block_min_to(out, dmin, red, threadIdx.x, blockDim.x);
+}
+
+cudaError_t launch_cfl1d(bool exact, const double *S, const double *bx, int ix,
+                         const Axis &ax, const Phys &ph, double safety,
+                         unsigned long long *out, cudaStream_t s) {
+  if (exact) k_cfl1d<true><<<1, 256, 0, s>>>(S, bx, ix, ax, ph, safety, out);
+  else k_cfl1d<false><<<1, 256, 0, s>>>(S, bx, ix, ax, ph, safety, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace cans

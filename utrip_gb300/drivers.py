@@ -44,7 +44,24 @@ def _bnd3(setup, state):
                 capi.bd_3d(kind, axis, face % 2, margin, state[var], q0, dxm)
 
 
+def _bnd1(setup, state):
+    """cans1d/md_mhdshktb/hdmlw/bnd.f:9-19: lower-face rules, then upper."""
+    margin = setup["margin"]
+    for side in (0, 1):
+        for var, face, kind, q0 in setup["bc"]:
+            if face != side or kind < 0:
+                continue
+            if kind == capi.BD_PER:
+                if side == 0:
+                    capi.bd_1d(kind, 0, margin, state[var])
+            else:
+                capi.bd_1d(kind, side, margin, state[var], q0, setup["dxm"])
+
+
 def _cfl(setup, state, safety):
+    if setup["solver"] == "mlw_m_1d":
+        return capi.cfl_m_1d(safety, setup["dtmin"], setup["gm"], setup["bx"], *state,
+                             setup["dx"])
     if setup["solver"] == "mlw_m_3d":
         return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
                              setup["dy"], setup["dz"])
@@ -55,6 +72,10 @@ def _cfl(setup, state, safety):
 
 
 def _step(setup, state, dt):
+    if setup["solver"] == "mlw_m_1d":
+        capi.mlw_m_1d(*state, setup["bx"], setup["bxm"], dt, setup["qav"], setup["gm"],
+                      setup["dx"], setup["dxm"])
+        return
     args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
     if setup["solver"] == "mlw_m_3d":
         capi.mlw_m_3d(*state, dt, *args, setup["dz"], setup["dzm"])
@@ -81,7 +102,7 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             t = t + dt
             dts.append(dt)
             _step(setup, state, dt)
-            (_bnd3 if setup["solver"] == "mlw_m_3d" else _bnd)(setup, state)
+            {"mlw_m_3d": _bnd3, "mlw_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
     finally:

@@ -269,5 +269,64 @@ def random_state_3d(ix: int, jx: int, kx: int, seed: int = 0, amp: float = 0.05)
                   name=f"random3d_{ix}x{jx}x{kx}_s{seed}")
 
 
+VARS["mlw_m_1d"] = ["ro", "pr", "vx", "vy", "by"]
+SOLVER_ID["mlw_m_1d"] = 3
+
+
+def shock_tube_1d(n: int = 1024, safety: float = 0.4, tend: float = 0.1):
+    """Brio-Wu-type MHD shock tube as cans1d/md_mhdshktb/hdmlw/model.f sets
+    it up: margin 1, dx0 = 1/n, cell izero = ix/2 centred at -dx0/2 (the
+    interface between cells ix/2 and ix/2+1 at x = 0; the box is [-0.5, 0.5],
+    a translation of [0, 1] with the interface at 0.5), gamma = 2.  Left
+    (x <= 0): rho=1, p=1, By=+sqrt(4pi); right: rho=0.125, p=0.1,
+    By=-sqrt(4pi); Bx = 0.75 sqrt(4pi).  bnd.f: bdsppx for ro, pr, vy, by and
+    bdsmnx for vx on both faces.  qav = 1 (main.f:149)."""
+    margin = 1
+    ix = n + 2 * margin
+    dx0 = 1.0 / float(np.float32(ix - 2 * margin))
+    dxm0 = np.full(ix, dx0)
+    x = np.empty(ix)
+    iz = ix // 2 - 1  # 0-based index of Fortran izero = ix/2
+    x[iz] = -dxm0[iz] / 2
+    for i in range(iz + 1, ix):
+        x[i] = x[i - 1] + dxm0[i - 1]
+    for i in range(iz - 1, -1, -1):
+        x[i] = x[i + 1] - dxm0[i]
+    dx, _, dxm = grdrdy(x)
+    left = x <= 0
+    f = {
+        "ro": np.where(left, 1.0, 0.125), "pr": np.where(left, 1.0, 0.1),
+        "vx": np.zeros(ix), "vy": np.zeros(ix),
+        "by": np.where(left, math.sqrt(4.0 * math.pi), -math.sqrt(4.0 * math.pi)),
+    }
+    bx = np.full(ix, 0.75 * math.sqrt(4.0 * math.pi))
+    bc = []
+    for v, name in enumerate(VARS["mlw_m_1d"]):
+        kind = BD_SMN if name == "vx" else BD_SPP
+        bc += [(v, 0, kind, 0.0), (v, 1, kind, 0.0)]
+    state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in VARS["mlw_m_1d"]]
+    return dict(solver="mlw_m_1d", solver_id=3, names=VARS["mlw_m_1d"], x=x, dx=dx, dxm=dxm,
+                bx=bx, bxm=bx.copy(), state=state, gm=2.0, qav=1.0, margin=margin, bc=bc,
+                safety=safety, dtmin=1e-10, tend=tend, dtout=0.01, name=f"shock_tube_{n}")
+
+
+def random_state_1d(ix: int, seed: int = 0):
+    """Smooth-plus-noise 1-D state for parity tests (every variable varies)."""
+    rng = np.random.default_rng(seed)
+    x, dx, dxm = uniform_axis(ix - 2, 1.0)
+    k = rng.integers(1, 4, size=5)
+    ph = rng.uniform(0, 2 * math.pi, size=5)
+    s = [np.sin(2 * math.pi * k[i] * x + ph[i]) + 0.05 * rng.standard_normal(ix) for i in range(5)]
+    f = {"ro": 1.0 + 0.3 * np.abs(s[0]), "pr": 0.6 + 0.2 * np.abs(s[1]), "vx": 0.3 * s[2],
+         "vy": 0.3 * s[3], "by": SQ4PI * 0.4 * s[4]}
+    bx = SQ4PI * (0.7 + 0.05 * np.sin(2 * math.pi * x))
+    bxm = SQ4PI * (0.7 + 0.05 * np.sin(2 * math.pi * (x + dxm / 2)))
+    bc = [(v, f_, BD_PER, 0.0) for v in range(5) for f_ in (0, 1)]
+    state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in VARS["mlw_m_1d"]]
+    return dict(solver="mlw_m_1d", solver_id=3, names=VARS["mlw_m_1d"], x=x, dx=dx, dxm=dxm,
+                bx=bx, bxm=bxm, state=state, gm=5.0 / 3.0, qav=3.0, margin=1, bc=bc,
+                safety=0.4, dtmin=1e-10, tend=1e30, name=f"random1d_{ix}_s{seed}")
+
+
 def copy_state(setup: dict):
     return [a.copy(order="F") for a in setup["state"]]
