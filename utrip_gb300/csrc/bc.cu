@@ -175,19 +175,10 @@ cudaError_t launch_bd_one(int kind, int axis, int mbnd, int margin0,
 __global__ void k_prepare(Ctl *ctl) {
   // The reference loop tests its condition at the end of the body, so the
   // first iteration always starts.
+  // It also restarts a loop paused at an output time.
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (ctl->done) return;
-  ctl->ns += 1;
-  const double dt = __longlong_as_double((long long)ctl->cfl_bits);
-  ctl->dt = dt;
-  ctl->cfl_bits = 0x7ff0000000000000ull;
-  if (dt < ctl->dtmin) {
-    ctl->merr = 9001;
-    ctl->done = 1;
-    return;
-  }
-  ctl->tp = ctl->t;
-  ctl->t = ctl->t + dt;
+  if (ctl->done || ctl->pause) return;
+  start_iteration(ctl);
 }
 
 cudaError_t launch_prepare(Ctl *ctl, cudaStream_t s) {

@@ -106,11 +106,29 @@ __device__ __forceinline__ double warp_min(double v) {
   return v;
 }
 
-// End of one iteration of the reference loop and start of the next
-// (cans2d/md_mhdkh/hdmlw/main.f:161-173 and 191-219), run by one thread once
-// the step, the boundary fill and the CFL reduction of the new state are
-// complete: flip the state buffers, the output test, the loop test, then
-// ns+=1, dt = CFL minimum, the dtmin test, tp = t, t += dt.
+// Start of a loop iteration (main.f:161-173): ns+=1, dt = CFL minimum held in
+// cfl_bits, the dtmin test, tp = t, t += dt.
+__device__ __forceinline__ void start_iteration(Ctl *ctl) {
+  ctl->ns += 1;
+  const unsigned long long bits = atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
+  const double dt = __longlong_as_double((long long)bits);
+  ctl->dt = dt;
+  ctl->cfl_bits = 0x7ff0000000000000ull;
+  if (dt < ctl->dtmin) {
+    ctl->merr = 9001;
+    ctl->done = 1;
+    return;
+  }
+  ctl->tp = ctl->t;
+  ctl->t = ctl->t + dt;
+}
+
+// End of one loop iteration (main.f:191-219), run by one thread once the
+// step, the boundary fill and the CFL reduction of the new state are
+// complete: flip the state buffers, the output test, the loop test, then the
+// start of the next iteration -- unless an output time was crossed, in which
+// case the loop pauses with t still the time of the state just written and
+// the next iteration starts when the host resumes it.
 __device__ __forceinline__ void finish_iteration(Ctl *ctl) {
   ctl->frame_blocks_done = 0;
   ctl->cur ^= 1;
@@ -124,18 +142,25 @@ __device__ __forceinline__ void finish_iteration(Ctl *ctl) {
     ctl->done = 1;
     return;
   }
-  ctl->ns += 1;
-  const unsigned long long bits = atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
-  const double dt = __longlong_as_double((long long)bits);
-  ctl->dt = dt;
-  ctl->cfl_bits = 0x7ff0000000000000ull;
-  if (dt < ctl->dtmin) {
-    ctl->merr = 9001;
-    ctl->done = 1;
-    return;
+  if (ctl->pause) return;
+  start_iteration(ctl);
+}
+
+// Block-wide minimum, valid on thread 0.  All threads of the block must call
+// it; the block size must be a multiple of 32.
+__device__ __forceinline__ double block_min(double v, double *red, int tid,
+                                            int nthreads) {
+  v = warp_min(v);
+  const int lane = tid & 31, w = tid >> 5;
+  const int nw = (nthreads + 31) >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double x = __longlong_as_double(0x7ff0000000000000LL);
+  if (w == 0) {
+    x = (lane < nw) ? red[lane] : x;
+    x = warp_min(x);
   }
-  ctl->tp = ctl->t;
-  ctl->t = ctl->t + dt;
+  return x;
 }
 
 // Block-wide minimum reduced into one atomicMin.  All threads of the block

@@ -1169,6 +1169,8 @@ extern "C" int cans_run_resume(cans_run *h) {
   int zero = 0;
   CK(cudaMemcpyAsync(&h->ctl->pause, &zero, sizeof zero, cudaMemcpyHostToDevice,
                      h->s));
+  // the iteration after the output starts now (a no-op when the loop ended)
+  CK(launch_prepare(h->ctl, h->s));
   CK(cudaStreamSynchronize(h->s));
   return CANS_OK;
 }

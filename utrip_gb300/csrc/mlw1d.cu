@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   double *Q = K + NV1 * L;
   double *slots = Q + L;
   double *red = slots + 2 * CS;
-  __shared__ double s_dt, s_t, s_tp;
+  __shared__ double s_dt, s_t, s_tp, s_pending;
   __shared__ long long s_ns, s_nexec;
   __shared__ int s_done, s_merr, s_pause;
 
@@ -368,9 +368,10 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
         const long long nt2 = (long long)(s_t / p.ctl->dtout);
         if (nt1 < nt2) s_pause = 1;
       }
+      s_pending = dtn;  // CFL of the state just written, for a later resume
       if (!(s_ns < p.ctl->nstop && s_t < p.ctl->tend)) {
         s_done = 1;
-      } else {
+      } else if (!s_pause) {
         s_ns += 1;
         s_dt = dtn;
         if (dtn < p.ctl->dtmin) {
@@ -398,6 +399,8 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
     p.ctl->dt = s_dt; p.ctl->t = s_t; p.ctl->tp = s_tp; p.ctl->ns = s_ns;
     p.ctl->nexec = s_nexec; p.ctl->done = s_done; p.ctl->merr = s_merr;
     p.ctl->pause = s_pause;
+    if (s_pause)  // resume starts the next iteration from this CFL minimum
+      p.ctl->cfl_bits = (unsigned long long)__double_as_longlong(s_pending);
   }
 }
 

@@ -201,7 +201,20 @@ __global__ void __launch_bounds__(TX *TY / 2, 1)
       const int d = a + T::CX;            // (i  ,j+1)
       const FT dxim(ax.dim[gi]), dyim(ay.dim[gj]);
       // mlwhalf part 2: un = avg4(u) - dt*dfdx - dt*dfdy   (mlwhalf.f:45-52)
+      const double cxk = dt.v * dxim.v * 0.5, cyk = dt.v * dyim.v * 0.5;
       auto pred = [&](int su, int sfx, int sfy, bool negx, bool negy) -> FT {
+        if constexpr (!E) {  // same predictor, fewer rounded operations
+          double r = 0.25 * ((SC(su, b) + SC(su, a)) + (SC(su, cc) + SC(su, d)));
+          if (sfx != NOFLUX) {
+            const double s = (SC(sfx, b) - SC(sfx, a)) + (SC(sfx, cc) - SC(sfx, d));
+            r = fma(negx ? cxk : -cxk, s, r);
+          }
+          if (sfy != NOFLUX) {
+            const double s = (SC(sfy, d) - SC(sfy, a)) + (SC(sfy, cc) - SC(sfy, b));
+            r = fma(negy ? cyk : -cyk, s, r);
+          }
+          return FT(r);
+        }
         const FT uh = 0.25 * (FT(SC(su, b)) + FT(SC(su, a)) + FT(SC(su, cc)) +
                               FT(SC(su, d)));
         FT un = uh;
@@ -369,28 +382,76 @@ __global__ void __launch_bounds__(TX *TY / 2, 1)
       return u + du;
     };
 
-    const FT ro = dstep(C::RO, C::RX, false, C::RY, false, K::XRO, false, K::YRO, false);
-    const FT ee = dstep(C::EE, C::FXE, false, C::FYE, false, K::XEE, false, K::YEE, false);
-    const FT rx = dstep(C::RX, C::FXRX, false, C::FYRX, false, K::XRX, false, K::YRX, false);
-    const FT ry = dstep(C::RY, C::FXRY, false, C::FYRY, false, K::XRY, false, K::YRY, false);
-    const FT bx = dstep(C::BX, NOFLUX, false, C::EZ, false, NOFLUX, false, K::EZ, false);
-    const FT by = dstep(C::BY, C::EZ, true, NOFLUX, false, K::EZ, true, NOFLUX, false);
+    // Fast policy: the new value of each conserved variable is a linear
+    // combination of 17 stencil values with per-cell coefficients, so it is
+    // evaluated as one chain of FMAs (mathematically the same update).
+    const double fcx = (hdt * hdx).v, fcy = (hdt * hdy).v;
+    const double fx0 = (hdt * dxi * uy0).v, fx1 = (hdt * dxi * uy1).v;
+    const double fy0 = (hdt * dyi * ux0).v, fy1 = (hdt * dyi * ux1).v;
+    const double ae = (dt * dxi * qxe).v, aw = (dt * dxi * qxw).v;
+    const double an = (dt * dyi * qyn).v, as = (dt * dyi * qys).v;
+    const double a1 = 1.0 - ((ae + aw) + (an + as));
+    auto fstep = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx,
+                     bool nkx, int kfy, bool nky) -> FT {
+      double r = a1 * SC(su, c);
+      r = fma(ae, SC(su, cE), r);
+      r = fma(aw, SC(su, cW), r);
+      r = fma(an, SC(su, cN), r);
+      r = fma(as, SC(su, cS), r);
+      if (sfx != NOFLUX) {
+        const double d = SC(sfx, cE) - SC(sfx, cW);
+        r = fma(negx ? fcx : -fcx, d, r);
+      }
+      if (sfy != NOFLUX) {
+        const double d = SC(sfy, cN) - SC(sfy, cS);
+        r = fma(negy ? fcy : -fcy, d, r);
+      }
+      if (kfx != NOFLUX) {
+        const double d0 = SK(kfx, kSE) - SK(kfx, kSW), d1 = SK(kfx, kNE) - SK(kfx, kNW);
+        r = fma(nkx ? fx0 : -fx0, d0, r);
+        r = fma(nkx ? fx1 : -fx1, d1, r);
+      }
+      if (kfy != NOFLUX) {
+        const double d0 = SK(kfy, kNW) - SK(kfy, kSW), d1 = SK(kfy, kNE) - SK(kfy, kSE);
+        r = fma(nky ? fy0 : -fy0, d0, r);
+        r = fma(nky ? fy1 : -fy1, d1, r);
+      }
+      return FT(r);
+    };
+    auto step_var = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx,
+                        bool nkx, int kfy, bool nky) -> FT {
+      if constexpr (E) return dstep(su, sfx, negx, sfy, negy, kfx, nkx, kfy, nky);
+      else return fstep(su, sfx, negx, sfy, negy, kfx, nkx, kfy, nky);
+    };
+    const FT ro = step_var(C::RO, C::RX, false, C::RY, false, K::XRO, false, K::YRO, false);
+    const FT ee = step_var(C::EE, C::FXE, false, C::FYE, false, K::XEE, false, K::YEE, false);
+    const FT rx = step_var(C::RX, C::FXRX, false, C::FYRX, false, K::XRX, false, K::YRX, false);
+    const FT ry = step_var(C::RY, C::FXRY, false, C::FYRY, false, K::XRY, false, K::YRY, false);
+    const FT bx = step_var(C::BX, NOFLUX, false, C::EZ, false, NOFLUX, false, K::EZ, false);
+    const FT by = step_var(C::BY, C::EZ, true, NOFLUX, false, K::EZ, true, NOFLUX, false);
     FT rz(0.0), bz(0.0);
     if constexpr (M3) {
-      rz = dstep(C::RZ, C::FXRZ, false, C::FYRZ, false, K::XRZ, false, K::YRZ, false);
-      bz = dstep(C::BZ, C::EY, false, C::EX, true, K::EY, false, K::EX, true);
+      rz = step_var(C::RZ, C::FXRZ, false, C::FYRZ, false, K::XRZ, false, K::YRZ, false);
+      bz = step_var(C::BZ, C::EY, false, C::EX, true, K::EY, false, K::EX, true);
     }
     // vector potential: mlwsrch part 1 + mlwsrcf with s = -ez, -ezh
     const size_t g = (size_t)gi + (size_t)gj * ix;
-    FT daz(0.0);
-    daz = daz + hdt * (-FT(SC(C::EZ, c)));
-    {
+    FT az;
+    if constexpr (E) {
+      FT daz(0.0);
+      daz = daz + hdt * (-FT(SC(C::EZ, c)));
       const FT ssw = -FT(SK(K::EZ, kSW)), sse = -FT(SK(K::EZ, kSE));
       const FT snw = -FT(SK(K::EZ, kNW)), sne = -FT(SK(K::EZ, kNE));
       const FT sh = uy0 * (ux0 * ssw + ux1 * sse) + uy1 * (ux0 * snw + ux1 * sne);
       daz = daz + hdt * sh;
+      az = FT(A[P::AZ * n + g]) + daz;
+    } else {
+      const double w0 = (hdt * uy0).v, w1 = (hdt * uy1).v;
+      double s = fma(ux0.v, SK(K::EZ, kSW), ux1.v * SK(K::EZ, kSE)) * w0;
+      s = fma(fma(ux0.v, SK(K::EZ, kNW), ux1.v * SK(K::EZ, kNE)), w1, s);
+      s = fma(hdt.v, SC(C::EZ, c), s);
+      az = FT(A[P::AZ * n + g] - s);
     }
-    const FT az = FT(A[P::AZ * n + g]) + daz;
 
     // back to primitives (mlw_m3.f:365-374)
     FT vx, vy, vz(0.0);
@@ -435,11 +496,21 @@ __global__ void __launch_bounds__(TX *TY / 2, 1)
         b2 = bx * bx + by * by;
         v2 = vx * vx + vy * vy;
       }
-      const FT ca2 = b2 * pi4i / ro;
-      const FT cs2 = gm * pr / ro;
-      const FT dtcfl = fmin_(FT(ax.d[gi]), FT(ay.d[gj])) / fsqrt(v2 + cs2 + ca2);
-      const double dtq = (FT(ctl->safety) * dtcfl).v;
-      if (dtq < dmin) dmin = dtq;
+      if constexpr (E) {
+        const FT ca2 = b2 * pi4i / ro;
+        const FT cs2 = gm * pr / ro;
+        const FT dtcfl = fmin_(FT(ax.d[gi]), FT(ay.d[gj])) / fsqrt(v2 + cs2 + ca2);
+        const double dtq = (FT(ctl->safety) * dtcfl).v;
+        if (dtq < dmin) dmin = dtq;
+      } else {
+        // min over cells of min(dx,dy)/sqrt(S) is 1/sqrt(max of
+        // S*max(1/dx^2, 1/dy^2)): no division or root per cell.  dmin holds
+        // minus the largest key; the block converts it once.
+        const double rinv = 1.0 / ro.v;  // folded with the one above
+        const double s = v2.v + fma(gm.v, pr.v, pi4i.v * b2.v) * rinv;
+        const double kk = s * fmax(dxi.v * dxi.v, dyi.v * dyi.v);
+        if (-kk < dmin) dmin = -kk;
+      }
     }
   }
 
@@ -459,7 +530,14 @@ __global__ void __launch_bounds__(TX *TY / 2, 1)
       for (int v = 0; v < P::N; v++) B[v * n + g] = A[v * n + g];
     }
   }
-  if (ctl != nullptr) block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
+  if (ctl != nullptr) {
+    if constexpr (E) {
+      block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
+    } else {
+      const double m = block_min(dmin, sred, tid, T::NT);  // -(largest key)
+      if (tid == 0 && m < 0.0) atomic_min_pos(&ctl->cfl_bits, ctl->safety / sqrt(-m));
+    }
+  }
 #undef SC
 #undef SK
 }

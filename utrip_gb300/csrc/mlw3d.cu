@@ -52,7 +52,9 @@ template <int TX, int TY> struct Tile3 {
   static constexpr int CX = TX + 2, CY = TY + 2, NC = CX * CY;
   static constexpr int KX = TX + 1, KY = TY + 1, NK = KX * KY;
   static constexpr int NQX = (TX + 1) * TY, NQY = TX * (TY + 1);
-  static constexpr int NT = NC;
+  // one thread per halo-tile cell, rounded up to whole warps so that every
+  // warp-level reduction sees 32 live lanes; the extra threads own no cell
+  static constexpr int NT = (NC + 31) / 32 * 32;
   static constexpr size_t smem_doubles =
       2 * (size_t)C3::N * NC + 2 * (size_t)K3::N * NK + NQX + NQY + 32;
   static constexpr size_t smem_bytes = smem_doubles * sizeof(double);
@@ -138,7 +140,7 @@ __device__ __forceinline__ void cell_stage(const double *__restrict__ A,
 }  // namespace
 
 template <bool E, int TX, int TY>
-__global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
+__global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     k_mlw3d(const double *__restrict__ A, double *__restrict__ B, int ix,
             int jx, int kx, Axis ax, Axis ay, Axis az, Phys ph, double dt_arg,
             Ctl *__restrict__ ctl, Box3 box, int kchunk) {
@@ -159,12 +161,13 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
   const FT dt((ctl != nullptr) ? ctl->dt : dt_arg);
   const size_t n = (size_t)ix * jx * kx;
   const size_t plane = (size_t)ix * jx;
-  const int hx = threadIdx.x, hy = threadIdx.y;  // halo-tile coordinates
-  const int tid = hx + hy * T::CX;
+  const int tid = threadIdx.x;
+  const bool cell = tid < T::NC;                 // this thread owns a cell
+  const int hx = tid % T::CX, hy = tid / T::CX;  // halo-tile coordinates
   const int i0 = 1 + blockIdx.x * TX, j0 = 1 + blockIdx.y * TY;
   const int gi = i0 - 1 + hx, gj = j0 - 1 + hy;
-  const bool in_arr = (gi < ix) && (gj < jx);
-  const bool interior = hx >= 1 && hx <= TX && hy >= 1 && hy <= TY &&
+  const bool in_arr = cell && (gi < ix) && (gj < jx);
+  const bool interior = cell && hx >= 1 && hx <= TX && hy >= 1 && hy <= TY &&
                         gi <= ix - 2 && gj <= jx - 2;
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kx - 2, kb + kchunk - 1);
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
     if (in_arr) {
       cell_stage<E>(A, n, (size_t)gi + (size_t)gj * ix + (size_t)k * plane, sl,
                     T::NC, tid, ph);
-    } else {
+    } else if (cell) {
 #pragma unroll 1
       for (int f = 0; f < C3::N; f++) sl[(size_t)f * T::NC + tid] = 0.0;
     }
@@ -202,6 +205,40 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
               p11 = p01 + 1;
     const FT dxim(ax.dim[a]), dyim(ay.dim[b]), dzim(az.dim[k]);
     FT un[8];
+    if constexpr (!E) {  // same predictor, fewer rounded operations
+      const double cxk = dt.v * dxim.v * 0.25, cyk = dt.v * dyim.v * 0.25,
+                   czk = dt.v * dzim.v * 0.25;
+#pragma unroll
+      for (int v = 0; v < 8; v++) {
+        const double *Lv = L + (size_t)v * T::NC, *Uv = U + (size_t)v * T::NC;
+        double r = 0.125 * (((Lv[p10] + Lv[p00]) + (Lv[p11] + Lv[p01])) +
+                            ((Uv[p10] + Uv[p00]) + (Uv[p11] + Uv[p01])));
+        int f;
+        bool ng;
+        cell_flux_src(v, 0, f, ng);
+        if (f != NOF) {
+          const double *a = L + (size_t)f * T::NC, *b = U + (size_t)f * T::NC;
+          const double s = ((a[p10] - a[p00]) + (a[p11] - a[p01])) +
+                           ((b[p10] - b[p00]) + (b[p11] - b[p01]));
+          r = fma(ng ? cxk : -cxk, s, r);
+        }
+        cell_flux_src(v, 1, f, ng);
+        if (f != NOF) {
+          const double *a = L + (size_t)f * T::NC, *b = U + (size_t)f * T::NC;
+          const double s = ((a[p01] - a[p00]) + (a[p11] - a[p10])) +
+                           ((b[p01] - b[p00]) + (b[p11] - b[p10]));
+          r = fma(ng ? cyk : -cyk, s, r);
+        }
+        cell_flux_src(v, 2, f, ng);
+        if (f != NOF) {
+          const double *a = L + (size_t)f * T::NC, *b = U + (size_t)f * T::NC;
+          const double s = ((b[p00] - a[p00]) + (b[p10] - a[p10])) +
+                           ((b[p01] - a[p01]) + (b[p11] - a[p11]));
+          r = fma(ng ? czk : -czk, s, r);
+        }
+        un[v] = FT(r);
+      }
+    } else {
 #pragma unroll
     for (int v = 0; v < 8; v++) {
       const int su = v;  // conserved fields are 0..7
@@ -237,6 +274,7 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
         r = r - dt * d;
       }
       un[v] = r;
+    }
     }
     const FT roh = un[0], eeh = un[1], rxh = un[2], ryh = un[3], rzh = un[4];
     const FT bxh = un[5], byh = un[6], bzh = un[7];
@@ -364,6 +402,75 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
       const FT qzd = qav * FT(az.dm[k - 1]) * max0(fabs_(vz0 - FT(pvz)) - CANS_AV_EPS) *
                      FT(az.dim[k - 1]);
       FT unew[8];
+      if constexpr (!E) {
+        // Fast policy: each new conserved value is a linear combination of
+        // 37 stencil values with per-cell coefficients, one chain of FMAs.
+        const double h = hdt.v;
+        const double fcx = h * hdx.v, fcy = h * hdy.v, fcz = h * hdz.v;
+        const double hx_ = h * dxi.v, hy_ = h * dyi.v, hz_ = h * dzi.v;
+        const double wxL0 = hx_ * uz0.v * uy0.v, wxL1 = hx_ * uz0.v * uy1.v;
+        const double wxU0 = hx_ * uz1.v * uy0.v, wxU1 = hx_ * uz1.v * uy1.v;
+        const double wyL0 = hy_ * ux0.v * uz0.v, wyU0 = hy_ * ux0.v * uz1.v;
+        const double wyL1 = hy_ * ux1.v * uz0.v, wyU1 = hy_ * ux1.v * uz1.v;
+        const double wzSW = hz_ * uy0.v * ux0.v, wzSE = hz_ * uy0.v * ux1.v;
+        const double wzNW = hz_ * uy1.v * ux0.v, wzNE = hz_ * uy1.v * ux1.v;
+        const double ae = dt.v * dxi.v * qxe.v, aw = dt.v * dxi.v * qxw.v;
+        const double an = dt.v * dyi.v * qyn.v, as = dt.v * dyi.v * qys.v;
+        const double au = dt.v * dzi.v * qzu.v, ad = dt.v * dzi.v * qzd.v;
+        const double a1 = 1.0 - (((ae + aw) + (an + as)) + (au + ad));
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+          const double *Sv = S0 + (size_t)v * T::NC;
+          double r = a1 * Sv[c];
+          r = fma(ae, Sv[cE], r);
+          r = fma(aw, Sv[cW], r);
+          r = fma(an, Sv[cN], r);
+          r = fma(as, Sv[cS], r);
+          r = fma(au, S1[(size_t)v * T::NC + c], r);
+          r = fma(ad, pu[v], r);
+          int f;
+          bool ng;
+          cell_flux_src(v, 0, f, ng);
+          if (f != NOF)
+            r = fma(ng ? fcx : -fcx, S0[(size_t)f * T::NC + cE] - S0[(size_t)f * T::NC + cW], r);
+          cell_flux_src(v, 1, f, ng);
+          if (f != NOF)
+            r = fma(ng ? fcy : -fcy, S0[(size_t)f * T::NC + cN] - S0[(size_t)f * T::NC + cS], r);
+          cell_flux_src(v, 2, f, ng);
+          if (f != NOF) {
+            const double up = ng ? -S1[(size_t)f * T::NC + c] : S1[(size_t)f * T::NC + c];
+            r = fma(-fcz, up - pfz[v], r);
+          }
+          corner_flux_src(v, 0, f, ng);
+          if (f != NOF) {
+            const double *L = KL + (size_t)f * T::NK, *U = KU + (size_t)f * T::NK;
+            const double sg = ng ? 1.0 : -1.0;
+            r = fma(sg * wxL0, L[kSE] - L[kSW], r);
+            r = fma(sg * wxL1, L[kNE] - L[kNW], r);
+            r = fma(sg * wxU0, U[kSE] - U[kSW], r);
+            r = fma(sg * wxU1, U[kNE] - U[kNW], r);
+          }
+          corner_flux_src(v, 1, f, ng);
+          if (f != NOF) {
+            const double *L = KL + (size_t)f * T::NK, *U = KU + (size_t)f * T::NK;
+            const double sg = ng ? 1.0 : -1.0;
+            r = fma(sg * wyL0, L[kNW] - L[kSW], r);
+            r = fma(sg * wyU0, U[kNW] - U[kSW], r);
+            r = fma(sg * wyL1, L[kNE] - L[kSE], r);
+            r = fma(sg * wyU1, U[kNE] - U[kSE], r);
+          }
+          corner_flux_src(v, 2, f, ng);
+          if (f != NOF) {
+            const double *L = KL + (size_t)f * T::NK, *U = KU + (size_t)f * T::NK;
+            const double sg = ng ? 1.0 : -1.0;
+            r = fma(sg * wzSW, U[kSW] - L[kSW], r);
+            r = fma(sg * wzSE, U[kSE] - L[kSE], r);
+            r = fma(sg * wzNW, U[kNW] - L[kNW], r);
+            r = fma(sg * wzNE, U[kNE] - L[kNE], r);
+          }
+          unew[v] = FT(r);
+        }
+      } else {
 #pragma unroll
       for (int v = 0; v < 8; v++) {
         FT du(0.0);
@@ -422,6 +529,7 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
              dt * (dzi * (qzu * (FT(S1[(size_t)v * T::NC + c]) - u) - qzd * (u - FT(pu[v]))));
         unew[v] = u + du;
       }
+      }
       const FT ro = unew[0], ee = unew[1], rx = unew[2], ry = unew[3], rz = unew[4];
       const FT bx = unew[5], by = unew[6], bz = unew[7];
       FT vx, vy, vz;
@@ -451,12 +559,21 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
           gj <= box.hi[1] && k >= box.lo[2] && k <= box.hi[2]) {
         // cans3d/common/cfl_m.f:52-59 (pi in single precision)
         const FT b2 = bx * bx + by * by + bz * bz;
-        const FT ca2 = b2 * FT(ph.pi4i_cfl) / ro;
-        const FT cs2 = gm * pr / ro;
         const FT v2 = vx * vx + vy * vy + vz * vz;
-        const FT dmn = fmin_(fmin_(FT(ax.d[gi]), FT(ay.d[gj])), FT(az.d[k]));
-        const double dtq = (FT(ctl->safety) * (dmn / fsqrt(v2 + cs2 + ca2))).v;
-        if (dtq < dmin) dmin = dtq;
+        if constexpr (E) {
+          const FT ca2 = b2 * FT(ph.pi4i_cfl) / ro;
+          const FT cs2 = gm * pr / ro;
+          const FT dmn = fmin_(fmin_(FT(ax.d[gi]), FT(ay.d[gj])), FT(az.d[k]));
+          const double dtq = (FT(ctl->safety) * (dmn / fsqrt(v2 + cs2 + ca2))).v;
+          if (dtq < dmin) dmin = dtq;
+        } else {
+          // largest S*max(1/dx^2,1/dy^2,1/dz^2) gives the smallest dt; dmin
+          // holds minus that key (see the block reduction below)
+          const double rinv = 1.0 / ro.v;
+          const double s = v2.v + fma(gm.v, pr.v, ph.pi4i_cfl * b2.v) * rinv;
+          const double kk = s * fmax(fmax(dxi.v * dxi.v, dyi.v * dyi.v), dzi.v * dzi.v);
+          if (-kk < dmin) dmin = -kk;
+        }
       }
       save_prev(k);
     }
@@ -480,7 +597,14 @@ __global__ void __launch_bounds__((TX + 2) * (TY + 2), 1)
     }
     __syncthreads();
   }
-  if (ctl != nullptr) block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
+  if (ctl != nullptr) {
+    if constexpr (E) {
+      block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
+    } else {
+      const double m = block_min(dmin, sred, tid, T::NT);  // -(largest key)
+      if (tid == 0 && m < 0.0) atomic_min_pos(&ctl->cfl_bits, ctl->safety / sqrt(-m));
+    }
+  }
 }
 
 namespace {
@@ -500,7 +624,7 @@ cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
   }
   dim3 grid((ix - 2 + TX - 1) / TX, (jx - 2 + TY - 1) / TY,
             (kx - 2 + kchunk - 1) / kchunk);
-  dim3 block(TX + 2, TY + 2);
+  dim3 block(T::NT);
   k_mlw3d<E, TX, TY><<<grid, block, T::smem_bytes, s>>>(A, B, ix, jx, kx, ax, ay, az,
                                                        ph, dt, ctl, box, kchunk);
   count_launch();
