@@ -47,7 +47,66 @@ def parse():
     p.add_argument("--n", type=int, default=N_CELLS)
     p.add_argument("--exact", action="store_true", help="exact arithmetic policy")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the secondary 3-D and 1-D workloads")
     return p.parse_args()
+
+
+def extra_workloads(stream, exact=False):
+    """Secondary measurements reported beside the headline: the 3-D beta=1
+    turbulence box (256^3 interior, 8 arrays, 128 B/zone) and the 1-D MHD
+    shock tube run to t = 0.1 as one cluster launch."""
+    import torch
+    from utrip_gb300 import capi, drivers, setups
+    out = {}
+    hbm_peak, _ = measured_peaks()
+    # ---- 3-D: 20 loop iterations timed with events, step kernel profiled
+    s3 = setups.turbulence_3d(256)
+    run = drivers.make_run(s3, exact=exact, stream=stream.cuda_stream)
+    run.push(s3["state"])
+    tile = run.autotune(2)
+    run.start(tend=1e30, nstop=10 ** 12, safety=s3["safety"], dtmin=s3["dtmin"])
+    run.advance(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    iters = 20
+    e0.record(stream)
+    run.advance(iters)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    step_ms, iter_ms = run.profile(10)
+    st = run.query()
+    zones = 256 ** 3
+    kstep = step_ms / 10
+    out["turbulence_256^3_mlw_m"] = {
+        "zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+        "step_kernel_ms": kstep, "tile": tile, "hbm_gbs": 128 * zones / (kstep * 1e-3) / 1e9,
+        "hbm_frac": 128 * zones / (kstep * 1e-3) / 1e9 / hbm_peak, "bytes_per_zone": 128,
+        "steps_done": int(st.nexec), "merr": int(st.merr)}
+    run.close()
+    del s3
+    # ---- 1-D: the whole shock-tube run to t = 0.1 in one cluster launch
+    s1 = setups.shock_tube_1d(1024)
+    run = drivers.make_run(s1, exact=exact, stream=stream.cuda_stream)
+    best = None
+    for _ in range(3):
+        run.push(s1["state"])
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run.start(tend=s1["tend"], nstop=10 ** 6, safety=s1["safety"], dtmin=s1["dtmin"])
+        run.advance(10 ** 6)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    st = run.query()
+    out["shock_tube_1024_to_t0.1_mlw_m_1d"] = {
+        "ms_to_tend": best, "steps": int(st.ns), "t": st.t, "merr": int(st.merr),
+        "us_per_step": best * 1e3 / max(1, st.ns),
+        "zone_updates_per_s": 1024 * st.ns / (best * 1e-3), "launches_per_run": 2}
+    run.close()
+    return out
 
 
 def dist_setup():
@@ -293,6 +352,7 @@ def run_ours(args, ws, rank, local):
     e2e_val = n * n * m * e2e_steps * ws / (e2e_ms * 1e-3)
     nbytes = run.nvar * (n + 2) * (n + 2) * 8
     run.close()
+    extras = None if args.no_extras else extra_workloads(stream, exact=args.exact)
 
     if rank != 0:
         return
@@ -317,6 +377,8 @@ def run_ours(args, ws, rank, local):
         "wall_s": wall,
         "clocks": clk.summary(),
     }
+    if extras is not None:
+        line["workloads"] = extras
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(n)
     print(json.dumps(line), flush=True)

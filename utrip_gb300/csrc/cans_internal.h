@@ -85,7 +85,7 @@ cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
 // ---- 1-D ------------------------------------------------------------------
 // The whole 1-D loop (or one fixed-dt step) as one cluster launch, in place
 // on 5 arrays (ro,pr,vx,vy,by) of ix doubles.
-int mlw1d_cluster_size();
+int mlw1d_min_cells();
 cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          const double *bxm, int ix, const Axis &ax,
                          const Phys &ph, const BcTable &bc, Ctl *ctl,

@@ -480,7 +480,7 @@ extern "C" int cans_mlw_m_1d(double *ro, double *pr, double *vx, double *vy,
                              const double *gm, const double *dx,
                              const double *dxm, const int *ix) {
   const int n = *ix;
-  if (n < 2 * mlw1d_cluster_size() + 2) return CANS_ERR_ARG;
+  if (n < mlw1d_min_cells()) return CANS_ERR_ARG;
   double *arrs[5] = {ro, pr, vx, vy, by};
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
@@ -964,7 +964,7 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   // boundary program and the frame CFL work on
   const int wmin = 2 * (d->margin + 1) + 1;
   if (ndim == 1) {
-    if (d->ix < 2 * mlw1d_cluster_size() + 2 || d->jx != 1 || d->kx != 1 ||
+    if (d->ix < mlw1d_min_cells() || d->jx != 1 || d->kx != 1 ||
         !d->dx || !d->dxm || !d->bx || !d->bxm)
       return CANS_ERR_ARG;
   } else {

@@ -37,8 +37,8 @@ struct Run1D {
   BcTable bc;
   Ctl *ctl;              // loop control (resident run) or nullptr
   int ix;
-  int seg;               // interior cells per block
-  int lmax;              // seg + 2
+  int q, rem;            // blocks r < rem own q+1 interior cells, the rest q
+  int lmax;              // q + 3: largest own count plus two halo cells
   int max_steps;         // steps this launch may take
   int fixed;             // 1: one step with dt_fixed, no CFL / boundary fill
   double dt_fixed;
@@ -123,8 +123,11 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   __shared__ int s_done, s_merr, s_pause;
 
   // interior cells (0-based 1..ix-2) split evenly; local l <-> global lo-1+l
-  const int lo = 1 + r * p.seg;
-  const int hi = min(ix - 2, lo + p.seg - 1);
+  // balanced split of the ix-2 interior cells over the cluster
+  auto first_cell = [&](int rr) { return 1 + rr * p.q + min(rr, p.rem); };
+  auto own_count = [&](int rr) { return p.q + (rr < p.rem ? 1 : 0); };
+  const int lo = first_cell(r);
+  const int hi = lo + own_count(r) - 1;
   const int nl = hi - lo + 3;  // local cells incl. one halo each side
   const FT gm(p.ph.gm), gm1(p.ph.gm1), pi8i(p.ph.pi8i), pi4i(p.ph.pi4i),
       qav(p.ph.qav);
@@ -324,9 +327,12 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
       const int v = tid;
       auto owner = [&](int g1) {  // 1-based global cell -> (rank, local)
         const int g = g1 - 1;
-        int rr = (g <= 0) ? 0 : (g >= ix - 1 ? CS - 1 : (g - 1) / p.seg);
-        if (rr > CS - 1) rr = CS - 1;
-        const int l = g - (1 + rr * p.seg) + 1;
+        int rr;
+        if (g <= 0) rr = 0;
+        else if (g >= ix - 1) rr = CS - 1;
+        else if (g - 1 < p.rem * (p.q + 1)) rr = (g - 1) / (p.q + 1);
+        else rr = p.rem + (g - 1 - p.rem * (p.q + 1)) / p.q;
+        const int l = g - first_cell(rr) + 1;
         return make_int2(rr, l);
       };
       auto get = [&](int g1) -> double {
@@ -348,7 +354,7 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
     if (tid < NV1) {
       if (r > 0) {
         const double *nbp = cluster.map_shared_rank(prim, r - 1);
-        const int ln = p.seg;  // neighbour's last own cell (local index seg)
+        const int ln = own_count(r - 1);  // neighbour's last own cell
         P(nb, tid, 0) = nbp[(size_t)nb * NVS + (size_t)tid * L + ln];
       }
       if (r < CS - 1) {
@@ -404,7 +410,17 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   }
 }
 
-int mlw1d_cluster_size() { return 8; }
+// Smallest grid the 1-D loop kernel accepts (one block of 4 interior cells).
+int mlw1d_min_cells() { return 6; }
+
+// Cluster size for ix cells: up to 8 blocks (the portable cluster limit),
+// each owning at least 4 interior cells so a face rule of margin <= 3 stays
+// inside its block.
+static int cluster_for(int ix) {
+  int cs = 8;
+  while (cs > 1 && (ix - 2) / cs < 4) cs >>= 1;
+  return cs;
+}
 
 // Host launcher: the cluster kernel over a state of 5 arrays of ix doubles,
 // updated in place.
@@ -413,20 +429,20 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          const Phys &ph, const BcTable &bc, Ctl *ctl,
                          int max_steps, int fixed, double dt_fixed, int start,
                          cudaStream_t s) {
-  const int CS = mlw1d_cluster_size();
-  if (ix < 2 * CS + 2) return cudaErrorInvalidValue;
+  if (ix < mlw1d_min_cells()) return cudaErrorInvalidValue;
+  const int CS = cluster_for(ix);
   Run1D p{};
   p.S = S; p.bx = bx; p.bxm = bxm; p.ax = ax; p.ph = ph; p.bc = bc; p.ctl = ctl;
   p.ix = ix;
-  p.seg = (ix - 2 + CS - 1) / CS;
-  p.lmax = p.seg + 2;
+  p.q = (ix - 2) / CS;
+  p.rem = (ix - 2) % CS;
+  p.lmax = p.q + 3;
   p.max_steps = max_steps;
   p.fixed = fixed;
   p.dt_fixed = dt_fixed;
   p.start = start;
-  // the last block must own at least margin+1 cells for the boundary rules
-  if ((ix - 2) - (CS - 1) * p.seg < bc.margin + 1 || p.seg < bc.margin + 1)
-    return cudaErrorInvalidValue;
+  // each block must own at least margin+1 cells for the boundary rules
+  if (p.q < bc.margin + 1) return cudaErrorInvalidValue;
   const size_t smem = sizeof(double) * ((size_t)(2 * NV1 + 3 * NV1 + 1) * p.lmax + 2 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   void (*kern)(Run1D) = exact ? k_mlw1d<true> : k_mlw1d<false>;
