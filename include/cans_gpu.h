@@ -93,6 +93,28 @@ int cans_cfl_m_2d(double *dt, const double *safety, const double *dtmin,
                   const double *bx, const double *by, const double *dx,
                   const int *ix, const double *dy, const int *jx);
 
+/* No counterpart in the reference.  cfl_m3 for callers that cannot allocate
+ * device memory (a host code whose pool owns all device memory, a run under a
+ * memory budget fixed at start-up, a caller that may not allocate while it
+ * times its steps).  Same arguments and result as cans_cfl_m3_2d, but ro..bz,
+ * dx and dy are DEVICE pointers the caller already holds; dt and merr are
+ * written on the host.  The library allocates nothing for it: its scratch is
+ * a fixed 32 KiB array in device memory, held by every GPU that loads the
+ * library until the process exits, which limits the grid to
+ * ix*jx <= 1,048,576 cells (larger grids return CANS_ERR_ARG).  The first
+ * call on a device looks up that array's device address; make the first call
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race; runs on the stream set by cans_set_stream (else
+ * the default stream) and waits for it. */
+int cans_cfl_m3_2d_noalloc(double *dt, const double *safety,
+                           const double *dtmin, int *merr, const double *gm,
+                           const double *ro, const double *pr,
+                           const double *vx, const double *vy,
+                           const double *vz, const double *bx,
+                           const double *by, const double *bz,
+                           const double *dx, const int *ix, const double *dy,
+                           const int *jx);
+
 /* Ghost-cell fill, 2-D (cans2d/bc/bd*.f:2).  bdper* take (margin0, margin1);
  * the others take (mbnd, margin) with mbnd 0 = lower face, 1 = upper face. */
 int cans_bdperx_2d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx); /* bdperx.f:2 */

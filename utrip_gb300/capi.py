@@ -71,6 +71,7 @@ def load() -> C.CDLL:
         "cans_run_cfl": (i, [vp, d, _dp]), "cans_run_autotune": (i, [vp, i, _ip]),
         "cans_run_device_state": (i, [vp, C.POINTER(_dp)]),
         "cans_run_profile": (i, [vp, i, _dp, _dp]),
+        "cans_cfl_m3_2d_noalloc": (i, [_dp, _dp, _dp, _ip, _dp] + [vp] * 8 + [vp, _ip, vp, _ip]),
         "cans_measure_fp64_tflops": (i, [_dp]),
     }
     sig["cans_mlw_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip,
@@ -174,6 +175,21 @@ def cfl_m3(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy):
     _check(load().cans_cfl_m3_2d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
                                  _dref(gm), *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
                                  _ptr(dx), _iref(ix), _ptr(dy), _iref(jx)), "cfl_m3")
+    return dt.value, merr.value
+
+
+def cfl_m3_noalloc(safety, dtmin, gm, dev_arrays, dev_dx, dev_dy, ix, jx):
+    """cfl_m3 on device arrays for callers that cannot allocate: dev_arrays
+    are the device addresses (ints) of ro,pr,vx,vy,vz,bx,by,bz (each ix*jx,
+    column-major), dev_dx / dev_dy those of dx(ix), dy(jx).  Returns
+    (dt, merr).  The library allocates nothing for this call."""
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m3_2d_noalloc(C.byref(dt), _dref(safety), _dref(dtmin),
+                                         C.byref(merr), _dref(gm),
+                                         *[C.c_void_p(int(p)) for p in dev_arrays],
+                                         C.c_void_p(int(dev_dx)), _iref(ix),
+                                         C.c_void_p(int(dev_dy)), _iref(jx)),
+           "cfl_m3_noalloc")
     return dt.value, merr.value
 
 

@@ -111,6 +111,11 @@ void build_axis_host(int n, const double *d, const double *dm, double *di,
                      double *dim, double *u0, double *u1);
 Phys make_phys(double gm, double qav);
 
+// The stream the drop-in entry points use if one exists already (set by
+// cans_set_stream or created by an earlier call), else the default stream;
+// never creates a stream.
+cudaStream_t configured_stream();
+
 // Kernel-launch counter (all launches issued by this library).
 void count_launch(int n = 1);
 unsigned long long launch_count();

@@ -346,6 +346,10 @@ extern "C" int cans_set_stream(void *stream) {
   return CANS_OK;
 }
 extern "C" const char *cans_last_error(void) { return g_last_error.c_str(); }
+cudaStream_t cans::configured_stream() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_stream;
+}
 extern "C" unsigned long long cans_launch_count(void) { return launch_count(); }
 extern "C" int cans_device_ok(void) {
   int dev = 0;
