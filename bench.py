@@ -106,7 +106,74 @@ def extra_workloads(stream, exact=False):
         "us_per_step": best * 1e3 / max(1, st.ns),
         "zone_updates_per_s": 1024 * st.ns / (best * 1e-3), "launches_per_run": 2}
     run.close()
+    out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
     return out
+
+
+def sweep_setups(nruns=64, seed=4):
+    """64 magnetised shear layers, sizes drawn from {128,192,256,384}^2 and
+    plasma beta log-uniform in [0.1, 10] (seeded)."""
+    from utrip_gb300 import setups
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([128, 192, 256, 384], size=nruns)
+    betas = 10.0 ** rng.uniform(-1.0, 1.0, size=nruns)
+    return [setups.shear_layer(int(n), beta=float(b), seed=seed + k)
+            for k, (n, b) in enumerate(zip(sizes, betas))], sizes, betas
+
+
+def beta_sweep(stream, exact=False, nsteps=1000):
+    """The batched sweep (one persistent step launch per iteration for all 64
+    runs, graph-replayed, autotuned) against the same 64 runs done one at a
+    time with plain launches (one launch per stage) and with graphs."""
+    import torch
+    from utrip_gb300 import capi, drivers
+    runs, sizes, betas = sweep_setups()
+    zones = float(sum(int(n) * int(n) for n in sizes)) * nsteps
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b = capi.Batch(runs, exact=exact, stream=stream.cuda_stream)
+    for g, s in enumerate(runs):
+        b.push(g, s["state"])
+    b.start(nstop=nsteps, safety=0.4, dtmin=1e-10)
+    cfg = b.autotune(2)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.advance(nsteps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1)
+    done = all(b.query(g).nexec == nsteps for g in range(len(runs)))
+    batch_final = [b.pull(g) for g in (0, len(runs) - 1)]
+    b.close()
+    single = {}
+    for mode in ("plain", "graph"):
+        total = 0.0
+        finals = []
+        for g, s in enumerate(runs):
+            run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+            run.set_graph(mode == "graph")
+            run.push(s["state"])
+            run.start(nstop=nsteps, safety=0.4, dtmin=1e-10)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            run.advance(nsteps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+            if g in (0, len(runs) - 1):
+                finals.append(run.pull())
+            run.close()
+        single[mode] = total
+        same = all(np.array_equal(x, y) for f1, f2 in zip(finals, batch_final)
+                   for x, y in zip(f1, f2))
+    return {"runs": len(runs), "steps_per_run": nsteps, "config": cfg,
+            "sizes": {str(k): int(np.sum(sizes == k)) for k in (128, 192, 256, 384)},
+            "beta_range": [float(betas.min()), float(betas.max())],
+            "batched_ms": batched_ms, "one_at_a_time_plain_ms": single["plain"],
+            "one_at_a_time_graph_ms": single["graph"],
+            "speedup_vs_plain": single["plain"] / batched_ms,
+            "speedup_vs_graph": single["graph"] / batched_ms,
+            "batched_zone_updates_per_s": zones / (batched_ms * 1e-3),
+            "all_runs_completed": bool(done), "batched_equals_single_bitwise": bool(same)}
 
 
 def dist_setup():

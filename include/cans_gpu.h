@@ -296,6 +296,40 @@ int cans_run_device_state(cans_run *h, double **dev);
  * *iter_ms = summed duration of whole iterations.  Synchronous. */
 int cans_run_profile(cans_run *h, int iters, double *step_ms, double *iter_ms);
 
+/* Advance with one kernel launch per stage instead of graph replays
+ * (use_graph = 0); the default is 1. */
+int cans_run_set_graph(cans_run *h, int use_graph);
+
+/* ------------------------------------------------------------------------ */
+/* 4. Batches of independent 2-D runs                                        */
+/* ------------------------------------------------------------------------ */
+/* Many 2-D runs of the same solver (sizes, gamma, metrics and boundary
+ * programs may differ) advanced together: each loop iteration of every run
+ * is one persistent step launch fed by a device work queue of (run, tile)
+ * items, two boundary-fill launches and one bookkeeping launch, replayed as
+ * a CUDA graph.  Each run keeps its own dt, t, ns and stop tests, and its
+ * results equal those of the same run done alone. */
+typedef struct cans_batch cans_batch;
+int cans_batch_create(cans_batch **b, int ngrids, const cans_run_desc *descs);
+int cans_batch_destroy(cans_batch *b);
+int cans_batch_set_bc(cans_batch *b, int grid, int var, int face, int kind,
+                      double q0);
+int cans_batch_push(cans_batch *b, int grid, double *const *host);
+int cans_batch_pull(cans_batch *b, int grid, double *const *host);
+/* Every run starts its loop: first CFL, ns=1, t=t0+dt. */
+int cans_batch_start(cans_batch *b, double t0, double tend, long long nstop,
+                     double safety, double dtmin);
+/* Enqueue `iters` iterations of every run (asynchronous); use_graph = 0
+ * launches the kernels one by one. */
+int cans_batch_advance(cans_batch *b, int iters, int use_graph);
+int cans_batch_query(cans_batch *b, int grid, cans_run_state *st);
+/* Tile shape / cells-per-thread configurations, and the choice among them. */
+int cans_batch_configs(void);
+int cans_batch_set_config(cans_batch *b, int config);
+/* Time every configuration on `trial_steps` steps and keep the fastest;
+ * call after cans_batch_start (the current states are left unchanged). */
+int cans_batch_autotune(cans_batch *b, int trial_steps, int *config);
+
 /* ------------------------------------------------------------------------ */
 /* Measurement                                                               */
 /* ------------------------------------------------------------------------ */

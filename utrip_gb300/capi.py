@@ -72,6 +72,15 @@ def load() -> C.CDLL:
         "cans_run_device_state": (i, [vp, C.POINTER(_dp)]),
         "cans_run_profile": (i, [vp, i, _dp, _dp]),
         "cans_cfl_m3_2d_noalloc": (i, [_dp, _dp, _dp, _ip, _dp] + [vp] * 8 + [vp, _ip, vp, _ip]),
+        "cans_run_set_graph": (i, [vp, i]),
+        "cans_batch_create": (i, [C.POINTER(vp), i, vp]), "cans_batch_destroy": (i, [vp]),
+        "cans_batch_set_bc": (i, [vp, i, i, i, i, d]),
+        "cans_batch_push": (i, [vp, i, C.POINTER(_dp)]),
+        "cans_batch_pull": (i, [vp, i, C.POINTER(_dp)]),
+        "cans_batch_start": (i, [vp, d, d, C.c_longlong, d, d]),
+        "cans_batch_advance": (i, [vp, i, i]), "cans_batch_query": (i, [vp, i, vp]),
+        "cans_batch_configs": (i, []), "cans_batch_set_config": (i, [vp, i]),
+        "cans_batch_autotune": (i, [vp, i, _ip]),
         "cans_measure_fp64_tflops": (i, [_dp]),
     }
     sig["cans_mlw_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip,
@@ -433,6 +442,9 @@ class Run:
         _check(self.lib.cans_run_autotune(self.h, trial_steps, C.byref(t)), "cans_run_autotune")
         return t.value
 
+    def set_graph(self, use_graph: bool):
+        _check(self.lib.cans_run_set_graph(self.h, 1 if use_graph else 0), "cans_run_set_graph")
+
     def profile(self, iters: int):
         """(summed step-kernel ms, summed iteration ms) over `iters` un-graphed
         iterations timed with CUDA events on the run's stream."""
@@ -446,3 +458,85 @@ def measure_fp64_tflops() -> float:
     x = C.c_double(0.0)
     _check(load().cans_measure_fp64_tflops(C.byref(x)), "cans_measure_fp64_tflops")
     return x.value
+
+
+def _desc_for(solver: int, grid: dict, gm: float, qav: float, margin: int, exact: bool,
+              tile: int, stream, keep: list):
+    def arr(k):
+        a = np.ascontiguousarray(grid[k], dtype=np.float64)
+        keep.append(a)
+        return a.ctypes.data_as(_dp)
+    return _Desc(solver, np.asarray(grid["dx"]).size, np.asarray(grid["dy"]).size, 1, margin,
+                 gm, qav, arr("dx"), arr("dxm"), arr("dy"), arr("dym"), None, None,
+                 1 if exact else 0, tile, C.c_void_p(stream) if stream else None, None, None)
+
+
+class Batch:
+    """Many independent 2-D runs advanced together (cans_batch_* API).
+
+    setups: list of set-up dicts of one solver (utrip_gb300.setups)."""
+
+    def __init__(self, setups_, exact: bool = False, stream: int | None = None):
+        self.lib = load()
+        self._keep = []
+        solver = setups_[0]["solver_id"]
+        self.nvar = 9 if solver == SOLVER_MLW_M3_2D else 7
+        descs = (_Desc * len(setups_))(*[
+            _desc_for(solver, s, s["gm"], s["qav"], s["margin"], exact, -1, stream, self._keep)
+            for s in setups_])
+        self.shapes = [s["state"][0].shape for s in setups_]
+        h = C.c_void_p()
+        _check(self.lib.cans_batch_create(C.byref(h), len(setups_), descs), "cans_batch_create")
+        self.h = h
+        for g, s in enumerate(setups_):
+            for var, face, kind, q0 in s["bc"]:
+                _check(self.lib.cans_batch_set_bc(self.h, g, var, face, kind, q0),
+                       "cans_batch_set_bc")
+
+    def close(self):
+        if self.h:
+            self.lib.cans_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def push(self, grid: int, arrays):
+        arr = (_dp * self.nvar)(*[_ptr(a) for a in arrays])
+        _check(self.lib.cans_batch_push(self.h, grid, arr), "cans_batch_push")
+
+    def pull(self, grid: int, arrays=None):
+        if arrays is None:
+            arrays = [np.zeros(self.shapes[grid], order="F") for _ in range(self.nvar)]
+        arr = (_dp * self.nvar)(*[_ptr(a) for a in arrays])
+        _check(self.lib.cans_batch_pull(self.h, grid, arr), "cans_batch_pull")
+        return arrays
+
+    def start(self, t0=0.0, tend=1e30, nstop=10 ** 12, safety=0.4, dtmin=1e-10):
+        _check(self.lib.cans_batch_start(self.h, t0, tend, nstop, safety, dtmin),
+               "cans_batch_start")
+
+    def advance(self, iters: int, use_graph: bool = True):
+        _check(self.lib.cans_batch_advance(self.h, iters, 1 if use_graph else 0),
+               "cans_batch_advance")
+
+    def query(self, grid: int) -> RunState:
+        st = RunState()
+        _check(self.lib.cans_batch_query(self.h, grid, C.byref(st)), "cans_batch_query")
+        return st
+
+    def set_config(self, config: int):
+        _check(self.lib.cans_batch_set_config(self.h, config), "cans_batch_set_config")
+
+    def autotune(self, trial_steps: int = 3) -> int:
+        c = C.c_int(0)
+        _check(self.lib.cans_batch_autotune(self.h, trial_steps, C.byref(c)),
+               "cans_batch_autotune")
+        return c.value
+
+
+def batch_configs() -> int:
+    return int(load().cans_batch_configs())

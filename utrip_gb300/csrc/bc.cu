@@ -11,77 +11,9 @@
 
 #include "cans_common.cuh"
 #include "cans_internal.h"
+#include "bc_line.cuh"
 
 namespace cans {
-
-// One rule on one line: q(l), l = 1..n, at stride `stride`.
-__device__ __forceinline__ void bd_line(int kind, int mbnd, int m0, int m1,
-                                        double *q, int n, size_t stride,
-                                        double q0, const double *dxm) {
-#define QL(l) q[(size_t)((l)-1) * stride]
-  if (kind == BD_PER) {  // bdperx(margin0, margin1)
-    const int b0 = 1 + m0, b1 = n - m1;
-    if (mbnd == 0)
-      for (int i = 1; i <= m0; i++) QL(b0 - i) = QL(b1 + 1 - i);
-    else
-      for (int i = 1; i <= m1; i++) QL(b1 + i) = QL(b0 - 1 + i);
-    return;
-  }
-  const int m = (mbnd == 0) ? m0 : m1;
-  if (mbnd == 0) {
-    const int b = 1 + m;
-    switch (kind) {
-      case BD_SPP: for (int i = 1; i <= m; i++) QL(b - i) = QL(b - 1 + i); break;
-      case BD_SPN: for (int i = 1; i <= m; i++) QL(b - i) = -QL(b - 1 + i); break;
-      case BD_SMP: for (int i = 1; i <= m; i++) QL(b - i) = QL(b + i); break;
-      case BD_SMN:
-        for (int i = 1; i <= m; i++) QL(b - i) = -QL(b + i);
-        QL(b) = 0.;
-        break;
-      case BD_FRE: for (int i = 1; i <= m; i++) QL(b - i) = QL(b); break;
-      case BD_CNS: for (int i = 1; i <= m; i++) QL(b - i) = q0; break;
-      case BD_FRD:
-        for (int i = 1; i <= m; i++) {
-          const double dqq = __ddiv_rn(__dsub_rn(QL(b + 1), QL(b)), dxm[b - 1]);
-          QL(b - i) = __dsub_rn(QL(b - i + 1), __dmul_rn(dqq, dxm[b - i - 1]));
-        }
-        break;
-      default: break;
-    }
-  } else {
-    const int b = n - m;
-    switch (kind) {
-      case BD_SPP: for (int i = 1; i <= m; i++) QL(b + i) = QL(b + 1 - i); break;
-      case BD_SPN: for (int i = 1; i <= m; i++) QL(b + i) = -QL(b + 1 - i); break;
-      case BD_SMP: for (int i = 1; i <= m; i++) QL(b + i) = QL(b - i); break;
-      case BD_SMN:
-        for (int i = 1; i <= m; i++) QL(b + i) = -QL(b - i);
-        QL(b) = 0.;
-        break;
-      case BD_FRE: for (int i = 1; i <= m; i++) QL(b + i) = QL(b); break;
-      case BD_CNS: for (int i = 1; i <= m; i++) QL(b + i) = q0; break;
-      case BD_FRD:
-        for (int i = 1; i <= m; i++) {
-          const double dqq = __ddiv_rn(__dsub_rn(QL(b), QL(b - 1)), dxm[b - 2]);
-          QL(b + i) = __dadd_rn(QL(b + i - 1), __dmul_rn(dqq, dxm[b + i - 2]));
-        }
-        break;
-      default: break;
-    }
-  }
-#undef QL
-}
-
-// Lines along `axis` of an (n0, n1, n2) array: line index -> base offset.
-__device__ __forceinline__ size_t line_base(int axis, long long line, int n0,
-                                            int n1) {
-  if (axis == 0) return (size_t)line * n0;                 // (j,k) -> j*n0 + k*n0*n1
-  if (axis == 1) {
-    const long long i = line % n0, k = line / n0;
-    return (size_t)i + (size_t)k * n0 * n1;
-  }
-  return (size_t)line;                                     // (i,j) plane index
-}
 
 // Boundary program of one axis over all variables: thread per (var, line).
 __global__ void k_bc_axis(int nvar, double *S, int n0, int n1, int n2,

@@ -831,6 +831,7 @@ struct cans_run {
   int graph_iters = 0;
   int graph_nodes = 0;
   double *bx1 = nullptr;       // 1-D: device bx (ix) followed by bxm (ix)
+  bool use_graph = true;       // replay iterations as a CUDA graph
 };
 
 namespace {
@@ -1135,6 +1136,13 @@ extern "C" int cans_run_advance(cans_run *h, int iters) {
     CK(launch_1d(h, iters, 0, 0.0, 0));
     return CANS_OK;
   }
+  if (!h->use_graph) {
+    for (int k = 0; k < iters; k++) {
+      int rc = enqueue_iteration(h);
+      if (rc) return rc;
+    }
+    return CANS_OK;
+  }
   const int chunk = iters < 32 ? iters : 32;
   if (!h->graph || h->graph_iters != chunk) {
     int rc = build_graph(h, chunk);
@@ -1150,6 +1158,12 @@ extern "C" int cans_run_advance(cans_run *h, int iters) {
     int rc = enqueue_iteration(h);
     if (rc) return rc;
   }
+  return CANS_OK;
+}
+
+extern "C" int cans_run_set_graph(cans_run *h, int use_graph) {
+  if (!h) return CANS_ERR_ARG;
+  h->use_graph = use_graph != 0;
   return CANS_OK;
 }
 
