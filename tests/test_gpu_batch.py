@@ -39,8 +39,17 @@ def test_batch_equals_single_runs(gpu, exact):
             got = b.pull(g)
             ref = setups.copy_state(s)
             t, ns, merr, nexec = drivers.run_resident(s, ref, 25, exact=exact)
-            assert (ns, nexec) == (25, 25) and st.t == t
-            _assert_same(s["names"], got, ref, f"grid {g}")
+            assert (ns, nexec) == (25, 25)
+            if exact:
+                assert st.t == t
+                _assert_same(s["names"], got, ref, f"grid {g}")
+            else:
+                # the fast policy leaves FMA contraction to the compiler, which
+                # may contract the batched and the single-run kernels apart
+                assert abs(st.t - t) <= 1e-13 * t
+                for k, a, r in zip(s["names"], got, ref):
+                    scale = max(float(np.max(np.abs(r))), 1e-300)
+                    assert float(np.max(np.abs(a - r))) <= 1e-12 * scale, (g, k)
     finally:
         b.close()
 
