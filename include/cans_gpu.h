@@ -201,6 +201,14 @@ int cans_bdcnsz_3d(const int *mbnd, const int *margin, double *qq, const double 
 int cans_bdfrdx_3d(const int *mbnd, const int *margin, double *qq, const double *dxm, const int *ix, const int *jx, const int *kx); /* bdfrdx.f:2 */
 int cans_bdfrdy_3d(const int *mbnd, const int *margin, double *qq, const double *dym, const int *ix, const int *jx, const int *kx); /* bdfrdy.f:2 */
 int cans_bdfrdz_3d(const int *mbnd, const int *margin, double *qq, const double *dzm, const int *ix, const int *jx, const int *kx); /* bdfrdz.f:2 */
+/* replaces subroutine roe_m   (cans3d/hdroe/roe_m.f:2): one Roe-MUSCL step
+ * (roeflux_m.f, tvdminmod.f) on 8 arrays; cells 3..n-2 are updated, margin 3
+ * as hdroe/main.f:5.  Extents must be >= 5. */
+int cans_roe_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                  double *bx, double *by, double *bz, const double *dt,
+                  const double *gm, const double *dx, const int *ix,
+                  const double *dy, const int *jx, const double *dz,
+                  const int *kx);
 
 /* ------------------------------------------------------------------------ */
 /* 2. Residency registry                                                     */
@@ -225,6 +233,7 @@ int cans_gpu_release(const double *any);
 #define CANS_SOLVER_MLW_M3_2D 1  /* mlw_m3 2-D: ro,pr,vx,vy,vz,bx,by,bz,az   */
 #define CANS_SOLVER_MLW_M_3D 2   /* mlw_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
 #define CANS_SOLVER_MLW_M_1D 3   /* mlw_m  1-D: ro,pr,vx,vy,by (+ bx, bxm)   */
+#define CANS_SOLVER_ROE_M_3D 4   /* roe_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
 
 /* Boundary kinds, one per reference bd* family. */
 #define CANS_BD_NONE (-1)

@@ -53,6 +53,7 @@ def load():
         lib.oracle_cfl_m_1d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 6 + [_dp, i]
         lib.oracle_mlw_m_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, _dp, i, _dp, _dp, i, _dp, _dp, i]
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
+        lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
         lib.oracle_set_threads.argtypes = [i]
         lib.oracle_get_threads.restype = i
         _lib = lib
@@ -240,7 +241,16 @@ def apply_bc_program_3d(state, program, margin, grid):
                                 *state[var].shape)
 
 
+def roe_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, gm, dx, dy, dz):
+    ix, jx, kx = ro.shape
+    load().oracle_roe_m_3d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], dt, gm,
+                           P(dx), ix, P(dy), jx, P(dz), kx)
+
+
 def step_3d(setup, state, dt):
+    if setup.get("solver") == "roe_m_3d":
+        roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])
+        return
     mlw_m_3d(*state, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"],
              setup["dym"], setup["dz"], setup["dzm"])
 
@@ -251,7 +261,8 @@ def cfl_3d(setup, state, safety):
 
 
 def run_3d(setup, state, nstop, tend=None, safety=None, t0=0.0):
-    """The 3-D model-package loop (cans3d/md_mhdshktb/hdmlw/main.f:167-182)."""
+    """The 3-D model-package loop (cans3d/md_mhdshktb/hdmlw/main.f:167-182;
+    hdroe/main.f:167-180 for the Roe solver)."""
     tend = setup.get("tend", 1e30) if tend is None else tend
     safety = setup["safety"] if safety is None else safety
     t, ns, dts = t0, 0, []

@@ -94,6 +94,12 @@ void oracle_cfl_m_3d(double *dt, double safety, double dtmin, int *merr,
                      const double *dz, int kx);
 void oracle_bd_3d(int kind, int axis, int mbnd, int margin, double *qq,
                   double q0, const double *dxm, int ix, int jx, int kx);
+/* Roe-MUSCL step (cans3d/hdroe/roe_m.f:2); see roe3d.c for the one
+ * deviation (a definite value where the reference reads unset memory). */
+void oracle_roe_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                     double *bx, double *by, double *bz, double dt, double gm,
+                     const double *dx, int ix, const double *dy, int jx,
+                     const double *dz, int kx);
 
 /* Boundary kinds (reference routine family in parentheses). */
 enum {

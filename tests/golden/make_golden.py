@@ -39,6 +39,21 @@ def case_2d(solver, ix, jx, seed, nsteps):
     return out
 
 
+def case_roe(ix, jx, kx, seed):
+    """One Roe-MUSCL step (cans3d/hdroe/roe_m.f) of a seeded 3-D state."""
+    s = setups.random_state_3d(ix, jx, kx, seed=seed, solver="roe_m_3d")
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dy", "dz"):
+        out["grid_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_3d(s, st, 0.4)
+    oracle.roe_m_3d(*st, dt, s["gm"], s["dx"], s["dy"], s["dz"])
+    out.update({"dt": np.array(dt), "gm": np.array(s["gm"])})
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def main():
     oracle.build()
     np.savez_compressed(OUT / "mlw_m3_2d_18x14.npz", **case_2d("mlw_m3", 18, 14, 11, 10))
@@ -55,6 +70,7 @@ def main():
                 oracle.bd(kind, axis, mbnd, 2, a, q0=0.75, dxm=dxm if axis == 0 else dym)
                 bc[f"k{kind}_a{axis}_m{mbnd}"] = a
     np.savez_compressed(OUT / "bd_2d_9x7.npz", q=q, dxm=dxm, dym=dym, **bc)
+    np.savez_compressed(OUT / "roe_m_3d_14x12x13.npz", **case_roe(14, 12, 13, 21))
     print("wrote fixtures to", OUT)
 
 

@@ -276,3 +276,119 @@ def test_shock_tube_runs_to_tend_and_keeps_wall_condition(oracle_lib):
     # the wave fan stays inside the box by t = 0.1: far cells keep their
     # state up to round-off that spreads one cell per step
     assert abs(ro[5] - 1.0) < 1e-8 and abs(ro[-6] - 0.125) < 1e-8
+
+
+# ---- Roe-MUSCL 3-D (cans3d/hdroe) -------------------------------------------
+
+def _roe_grid(n=12, seed=4):
+    """Periodic Roe state with margin 3 on an exactly representable grid."""
+    m = 3
+    s = setups.random_state_3d(n + 2 * m, n + 2 * m, n + 2 * m, seed=seed, solver="roe_m_3d")
+    h = 1.0 / 16.0
+    x = (np.arange(n + 2 * m) - 2.5) * h
+    d, _, dm = setups.grdrdy(x.copy())
+    for ax in "xyz":
+        s["d" + ax], s["d" + ax + "m"] = d.copy(), dm.copy()
+    s["bc"] = [(v, f, 0, 0.0) for v in range(8) for f in range(6)]
+    return s
+
+
+def _roe_step(oracle_lib, s, z, dt):
+    oracle_lib.step_3d(s, z, dt)
+    oracle_lib.apply_bc_program_3d(z, s["bc"], 3, s)
+
+
+def test_roe_uniform_state_changes_only_by_rounding(oracle_lib):
+    # equal fluxes on every face: the conserved variables keep their values;
+    # the primitives pass once through conserved form and back
+    s = _roe_grid(n=8)
+    st = [np.asfortranarray(np.full_like(a, a[7, 6, 5])) for a in s["state"]]
+    ref = [a.copy() for a in st]
+    oracle_lib.roe_m_3d(*st, 1e-3, s["gm"], s["dx"], s["dy"], s["dz"])
+    for k, a, b in zip(s["names"], st, ref):
+        assert float(np.max(np.abs(a - b))) <= 4e-16 * max(1.0, float(np.max(np.abs(b)))), k
+
+
+def test_roe_translation_commutes_with_step(oracle_lib):
+    s = _roe_grid()
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_3d(st, s["bc"], 3, s)
+    inner = (slice(3, -3),) * 3
+    sh = [np.asfortranarray(np.pad(np.roll(a[inner], (3, 5, 2), axis=(0, 1, 2)), 3)) for a in st]
+    oracle_lib.apply_bc_program_3d(sh, s["bc"], 3, s)
+    for _ in range(2):
+        for z in (st, sh):
+            _roe_step(oracle_lib, s, z, 2e-3)
+    for k, a, b in zip(s["names"], st, sh):
+        assert np.array_equal(np.roll(a[inner], (3, 5, 2), axis=(0, 1, 2)), b[inner]), k
+
+
+def test_roe_cyclic_axis_rotation(oracle_lib):
+    """(x, y, z) -> (y, z, x) of coordinates and vector components commutes
+    with the step to rounding: checks the per-axis argument rotation of
+    roe_m.f:96,146,196 and the normal-B rule of each axis."""
+    s = _roe_grid(n=10, seed=9)
+    st = setups.copy_state(s)
+
+    def rot(q):
+        ro, pr, vx, vy, vz, bx, by, bz = q
+        t = lambda a: np.asfortranarray(np.transpose(a, (2, 0, 1)))  # noqa: E731
+        return [t(ro), t(pr), t(vz), t(vx), t(vy), t(bz), t(bx), t(by)]
+
+    rs = rot(st)
+    for z in (st, rs):
+        oracle_lib.roe_m_3d(*z, 3e-3, s["gm"], s["dx"], s["dy"], s["dz"])
+    for k, a, b in zip(s["names"], rot(st), rs):
+        assert float(np.max(np.abs(a - b))) <= 1e-14 * float(np.max(np.abs(b))), k
+
+
+def test_roe_one_dimensional_state_stays_one_dimensional(oracle_lib):
+    # a state that varies along x only: the y and z faces carry equal left and
+    # right states, so their flux differences vanish exactly
+    s = _roe_grid(n=10, seed=2)
+    st = [np.asfortranarray(np.broadcast_to(a[:, 6:7, 6:7], a.shape).copy()) for a in s["state"]]
+    _roe_step(oracle_lib, s, st, 2e-3)
+    for k, a in zip(s["names"], st):
+        inner = a[3:-3, 3:-3, 3:-3]
+        assert np.array_equal(inner, np.broadcast_to(inner[:, :1, :1], inner.shape)), k
+
+
+def test_roe_periodic_conservation(oracle_lib):
+    s = _roe_grid(n=12, seed=5)
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_3d(st, s["bc"], 3, s)
+    inner = (slice(3, -3),) * 3
+    tot = lambda a: a[inner].sum()  # noqa: E731
+    m0, mx0, bx0 = tot(st[0]), tot(st[0] * st[2]), tot(st[5])
+    for _ in range(8):
+        dt, _ = oracle_lib.cfl_3d(s, st, 0.4)
+        _roe_step(oracle_lib, s, st, dt)
+    assert abs(tot(st[0]) - m0) <= 1e-13 * m0
+    assert abs(tot(st[0] * st[2]) - mx0) <= 1e-12 * m0
+    assert abs(tot(st[5]) - bx0) <= 1e-12 * abs(bx0)
+
+
+def test_roe_shock_tube_is_symmetric_and_bounded(oracle_lib):
+    """The oblique shock tube of md_mhdshktb/hdroe at 16^3 to t = 0.1: the
+    state depends on n.x only up to the grid, stays finite, keeps positive
+    density and pressure within the initial bounds (up to a small overshoot)
+    and moves mass across the discontinuity."""
+    s = setups.shock_tube_3d(16)
+    st = setups.copy_state(s)
+    t, ns, merr, dts = oracle_lib.run_3d(s, st, 100000)
+    assert merr == 0 and t >= 0.1 and ns == len(dts)
+    ro, pr = st[0], st[1]
+    assert np.isfinite(ro).all() and np.isfinite(pr).all()
+    assert 0.125 * 0.9 < ro.min() and ro.max() < 1.1
+    assert pr.min() > 0.0
+    assert not np.array_equal(ro, s["state"][0])
+
+
+def test_roe_oracle_matches_frozen_fixture(oracle_lib):
+    z = np.load(GOLD / "roe_m_3d_14x12x13.npz")
+    names = setups.VARS["roe_m_3d"]
+    st = [np.asfortranarray(z["in_" + k]) for k in names]
+    oracle_lib.roe_m_3d(*st, float(z["dt"]), float(z["gm"]), z["grid_dx"], z["grid_dy"],
+                        z["grid_dz"])
+    for k, a in zip(names, st):
+        assert np.array_equal(a, z["out_" + k]), k

@@ -27,6 +27,7 @@ SOLVER_MLW_M_2D = 0
 SOLVER_MLW_M3_2D = 1
 SOLVER_MLW_M_3D = 2
 SOLVER_MLW_M_1D = 3
+SOLVER_ROE_M_3D = 4
 
 BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
 
@@ -87,6 +88,7 @@ def load() -> C.CDLL:
                                              _dp, _dp, _ip])
     sig["cans_cfl_m_3d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 +
                             [_dp, _ip, _dp, _ip, _dp, _ip])
+    sig["cans_roe_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
     sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
     sig["cans_bdperx_1d"] = (i, [_ip, _ip, _dp, _ip])
@@ -294,6 +296,15 @@ def cfl_m_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy, dz):
     return dt.value, merr.value
 
 
+def roe_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, gm, dx, dy, dz):
+    """cans3d/hdroe/roe_m.f:2 -- one Roe-MUSCL step of the 3-D state, in place
+    (cells 3..n-2 updated, the others kept)."""
+    ix, jx, kx = ro.shape
+    return _check(load().cans_roe_m_3d(*[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)],
+                                       _dref(dt), _dref(gm), _ptr(dx), _iref(ix), _ptr(dy),
+                                       _iref(jx), _ptr(dz), _iref(kx)), "roe_m_3d")
+
+
 def bd_3d(kind: int, axis: int, mbnd: int, margin: int, qq: np.ndarray,
           q0: float = 0.0, dxm: np.ndarray | None = None) -> int:
     """One reference bd* call on a 3-D array (cans3d/bc/bd*.f)."""
@@ -358,8 +369,8 @@ class Run:
         self.lib = load()
         self.solver = solver
         self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8,
-                     SOLVER_MLW_M_1D: 5}[solver]
-        three = solver == SOLVER_MLW_M_3D
+                     SOLVER_MLW_M_1D: 5, SOLVER_ROE_M_3D: 8}[solver]
+        three = solver in (SOLVER_MLW_M_3D, SOLVER_ROE_M_3D)
         one = solver == SOLVER_MLW_M_1D
 
         def arr(k):

@@ -82,6 +82,18 @@ cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
                            const Axis &ay, const Axis &az, const Phys &ph,
                            int margin, Ctl *ctl, cudaStream_t s);
 
+// ---- 3-D Roe-MUSCL (roe_m) -------------------------------------------------
+// One two-stage step on 8 arrays (ro,pr,vx,vy,vz,bx,by,bz); A -> B, cells
+// outside 3..n-2 copied.  scratch holds roe3d_scratch_doubles(ix*jx*kx)
+// doubles (half-step primitives and the face fluxes of one stage).  With ctl
+// the kernels take dt and the buffers from it and reduce the CFL of `box`.
+size_t roe3d_scratch_doubles(size_t ncells);
+cudaError_t launch_roe3d(bool exact, const double *A, double *B,
+                         double *scratch, int ix, int jx, int kx,
+                         const Axis &ax, const Axis &ay, const Axis &az,
+                         const Phys &ph, double dt, Ctl *ctl, Box3 box,
+                         cudaStream_t s);
+
 // ---- 1-D ------------------------------------------------------------------
 // The whole 1-D loop (or one fixed-dt step) as one cluster launch, in place
 // on 5 arrays (ro,pr,vx,vy,by) of ix doubles.

@@ -161,6 +161,19 @@ struct Scratch {
     if (!bits) CK(cudaMalloc(&bits, sizeof(unsigned long long) * 2));
     return CANS_OK;
   }
+  // stage scratch of the Roe step (half-step primitives and face fluxes)
+  double *roe = nullptr;
+  size_t roe_cap = 0;
+  int ensure_roe(size_t ndoubles) {
+    if (roe_cap < ndoubles) {
+      if (roe) cudaFree(roe);
+      roe = nullptr;
+      roe_cap = 0;
+      CK(cudaMalloc(&roe, sizeof(double) * ndoubles));
+      roe_cap = ndoubles;
+    }
+    return CANS_OK;
+  }
 };
 Scratch g_scratch;
 
@@ -684,6 +697,54 @@ extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
   return CANS_OK;
 }
 
+// roe_m (cans3d/hdroe/roe_m.f:2): one Roe-MUSCL step, on the registered
+// mirrors when the 8 arrays are a resident set, else through the scratch.
+extern "C" int cans_roe_m_3d(double *ro, double *pr, double *vx, double *vy,
+                             double *vz, double *bx, double *by, double *bz,
+                             const double *dt, const double *gm,
+                             const double *dx, const int *ix,
+                             const double *dy, const int *jx,
+                             const double *dz, const int *kx) {
+  if (!ro || !pr || !vx || !vy || !vz || !bx || !by || !bz || !dt || !gm ||
+      !dx || !dy || !dz || !ix || !jx || !kx)
+    return CANS_ERR_ARG;
+  const int nx = *ix, ny = *jx, nz = *kx;
+  if (nx < 5 || ny < 5 || nz < 5) return CANS_ERR_ARG;
+  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, 0.0);
+  const size_t n = (size_t)nx * ny * nz;
+  MirrorSet *m = resident_step_set(arrs, 8);
+  Scratch &sc = g_scratch;
+  DevAxis *dax = m ? &m->ax : &sc.ax, *day = m ? &m->ay : &sc.ay,
+          *daz = m ? &m->az : &sc.az;
+  // roe_m reads dx, dy, dz only
+  if ((rc = dax->upload(nx, dx, dx, s))) return rc;
+  if ((rc = day->upload(ny, dy, dy, s))) return rc;
+  if ((rc = daz->upload(nz, dz, dz, s))) return rc;
+  if ((rc = sc.ensure_roe(roe3d_scratch_doubles(n)))) return rc;
+  if (m) {
+    CK(launch_roe3d(exact_mode(), m->buf[m->cur], m->buf[m->cur ^ 1], sc.roe, nx,
+                    ny, nz, dax->a, day->a, daz->a, ph, *dt, nullptr, Box3{}, s));
+    m->cur ^= 1;
+    return CANS_OK;
+  }
+  if ((rc = sc.ensure(8 * n))) return rc;
+  for (int v = 0; v < 8; v++)
+    CK(cudaMemcpyAsync(sc.A + v * n, arrs[v], sizeof(double) * n,
+                       cudaMemcpyHostToDevice, s));
+  CK(launch_roe3d(exact_mode(), sc.A, sc.B, sc.roe, nx, ny, nz, dax->a, day->a,
+                  daz->a, ph, *dt, nullptr, Box3{}, s));
+  for (int v = 0; v < 8; v++)
+    CK(cudaMemcpyAsync(arrs[v], sc.B + v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
 #define CANS_BD3(NAME, KIND, AXIS)                                              \
   extern "C" int NAME(const int *mbnd, const int *margin, double *qq,           \
                       const int *ix, const int *jx, const int *kx) {            \
@@ -831,6 +892,7 @@ struct cans_run {
   int graph_iters = 0;
   int graph_nodes = 0;
   double *bx1 = nullptr;       // 1-D: device bx (ix) followed by bxm (ix)
+  double *roe = nullptr;       // Roe: stage scratch (roe3d_scratch_doubles)
   bool use_graph = true;       // replay iterations as a CUDA graph
 };
 
@@ -842,14 +904,18 @@ int solver_nvar(int solver) {
     case CANS_SOLVER_MLW_M3_2D: return 9;
     case CANS_SOLVER_MLW_M_3D: return 8;
     case CANS_SOLVER_MLW_M_1D: return 5;
+    case CANS_SOLVER_ROE_M_3D: return 8;
     default: return 0;
   }
 }
 int solver_ndim(int solver) {
-  return solver == CANS_SOLVER_MLW_M_3D ? 3 : (solver == CANS_SOLVER_MLW_M_1D ? 1 : 2);
+  if (solver == CANS_SOLVER_MLW_M_3D || solver == CANS_SOLVER_ROE_M_3D) return 3;
+  return solver == CANS_SOLVER_MLW_M_1D ? 1 : 2;
 }
+bool is_roe(const cans_run *h) { return h->d.solver == CANS_SOLVER_ROE_M_3D; }
 int tile_count(const cans_run *h) {
-  return h->ndim == 3 ? mlw3d_tile_count() : (h->ndim == 1 ? 1 : mlw2d_tile_count());
+  if (is_roe(h) || h->ndim == 1) return 1;
+  return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
 }
 // 1-D: the whole loop (or one fixed step) as one cluster launch, in place
 cudaError_t launch_1d(cans_run *h, int max_steps, int fixed, double dt,
@@ -875,6 +941,9 @@ Box3 inner_box(const cans_run *h) {
 
 cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
                         double dt, Ctl *ctl, Box3 box) {
+  if (is_roe(h))
+    return launch_roe3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
+                        h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
   if (h->ndim == 3)
     return launch_mlw3d(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
@@ -964,6 +1033,9 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   if (!out || !d) return CANS_ERR_ARG;
   const int nvar = solver_nvar(d->solver);
   if (nvar == 0 || d->margin < 1) return CANS_ERR_ARG;
+  // the Roe step updates 3..n-2 and its stencil reaches three cells, so the
+  // boundary program must rewrite three layers (hdroe/main.f:5)
+  if (d->solver == CANS_SOLVER_ROE_M_3D && d->margin < 3) return CANS_ERR_ARG;
   const int ndim = solver_ndim(d->solver);
   // every extent must exceed the two frames of margin+1 cells that the
   // boundary program and the frame CFL work on
@@ -1023,6 +1095,10 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
                           cudaMemcpyHostToDevice, h->s);
     if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy(bx)"));
   }
+  if (is_roe(h)) {
+    e = cudaMalloc(&h->roe, sizeof(double) * roe3d_scratch_doubles(h->n));
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(roe scratch)"));
+  }
   std::memset(&h->host_ctl, 0, sizeof(Ctl));
   h->host_ctl.done = 1;
   h->host_ctl.buf[0] = h->buf[0];
@@ -1043,6 +1119,7 @@ extern "C" int cans_run_destroy(cans_run *h) {
     if (h->buf[b]) cudaFree(h->buf[b]);
   if (h->ctl) cudaFree(h->ctl);
   if (h->bx1) cudaFree(h->bx1);
+  if (h->roe) cudaFree(h->roe);
   h->ax.release();
   h->ay.release();
   h->az.release();

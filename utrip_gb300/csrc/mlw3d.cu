@@ -20,6 +20,7 @@
 
 #include "cans_common.cuh"
 #include "cans_internal.h"
+#include "cfl3.cuh"
 
 namespace cans {
 
@@ -42,12 +43,6 @@ struct K3 {
   static constexpr int XRZ = 12, YRZ = 13, ZRZ = 14, EX = 15, EY = 16, EZ = 17;
   static constexpr int N = 18;
 };
-// primitive arrays in global memory
-struct P3 {
-  static constexpr int RO = 0, PR = 1, VX = 2, VY = 3, VZ = 4, BX = 5, BY = 6,
-                       BZ = 7, N = 8;
-};
-
 template <int TX, int TY> struct Tile3 {
   static constexpr int CX = TX + 2, CY = TY + 2, NC = CX * CY;
   static constexpr int KX = TX + 1, KY = TY + 1, NK = KX * KY;
@@ -651,25 +646,8 @@ cudaError_t launch_mlw3d(bool exact, int tile, const double *A, double *B,
 
 // ---------------------------------------------------------------------------
 // CFL over all cells (cans3d/common/cfl_m.f:39-85) and over the frame of cells
-// the boundary fill may rewrite, with the start of the next iteration.
-template <bool E>
-__device__ __forceinline__ double cfl3_cell(const double *__restrict__ S,
-                                            size_t n, size_t g, int i, int j,
-                                            int k, const Axis &ax,
-                                            const Axis &ay, const Axis &az,
-                                            const Phys &ph, double safety) {
-  using FT = F<E>;
-  const FT ro(S[P3::RO * n + g]), pr(S[P3::PR * n + g]);
-  const FT vx(S[P3::VX * n + g]), vy(S[P3::VY * n + g]), vz(S[P3::VZ * n + g]);
-  const FT bx(S[P3::BX * n + g]), by(S[P3::BY * n + g]), bz(S[P3::BZ * n + g]);
-  const FT b2 = bx * bx + by * by + bz * bz;
-  const FT ca2 = b2 * FT(ph.pi4i_cfl) / ro;
-  const FT cs2 = FT(ph.gm) * pr / ro;
-  const FT v2 = vx * vx + vy * vy + vz * vz;
-  const FT dmn = fmin_(fmin_(FT(ax.d[i]), FT(ay.d[j])), FT(az.d[k]));
-  return (FT(safety) * (dmn / fsqrt(v2 + cs2 + ca2))).v;
-}
-
+// the boundary fill may rewrite, with the start of the next iteration
+// (per-cell expression in cfl3.cuh).
 template <bool E>
 __global__ void k_cfl3d_full(const double *__restrict__ S, int ix, int jx,
                              int kx, Axis ax, Axis ay, Axis az, Phys ph,

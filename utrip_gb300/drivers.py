@@ -2,7 +2,8 @@
 
 run_literal  -- the reference driver shape (cans2d/md_mhdkh/hdmlw/main.f:
                 160-219) calling the drop-in entry points once per step:
-                cfl_m3 -> t += dt -> mlw_m3 -> bnd.  With `resident=True` the
+                cfl_m3 -> t += dt -> mlw_m3 -> bnd (and the 1-D, 3-D
+                and Roe forms of the same loop).  With `resident=True` the
                 arrays are registered first, so the calls run on device
                 mirrors and only dt crosses to the host each step.
 run_resident -- the same loop kept on the device by the run handle and
@@ -62,7 +63,7 @@ def _cfl(setup, state, safety):
     if setup["solver"] == "mlw_m_1d":
         return capi.cfl_m_1d(safety, setup["dtmin"], setup["gm"], setup["bx"], *state,
                              setup["dx"])
-    if setup["solver"] == "mlw_m_3d":
+    if setup["solver"] in ("mlw_m_3d", "roe_m_3d"):
         return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
                              setup["dy"], setup["dz"])
     if setup["solver"] == "mlw_m3":
@@ -75,6 +76,9 @@ def _step(setup, state, dt):
     if setup["solver"] == "mlw_m_1d":
         capi.mlw_m_1d(*state, setup["bx"], setup["bxm"], dt, setup["qav"], setup["gm"],
                       setup["dx"], setup["dxm"])
+        return
+    if setup["solver"] == "roe_m_3d":
+        capi.roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])
         return
     args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
     if setup["solver"] == "mlw_m_3d":
@@ -102,7 +106,8 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             t = t + dt
             dts.append(dt)
             _step(setup, state, dt)
-            {"mlw_m_3d": _bnd3, "mlw_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
+            {"mlw_m_3d": _bnd3, "roe_m_3d": _bnd3,
+             "mlw_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
     finally:

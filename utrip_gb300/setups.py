@@ -16,7 +16,7 @@ import math
 
 import numpy as np
 
-from .capi import BD_PER, BD_SPP, BD_SMN, SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D
+from .capi import BD_PER, BD_SPP, BD_SMN, SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M_3D
 
 SQ4PI = math.sqrt(4.0 * math.pi)
 
@@ -187,6 +187,10 @@ def random_state(ix: int, jx: int, seed: int = 0, solver: str = "mlw_m3", amp: f
 
 VARS["mlw_m_3d"] = ["ro", "pr", "vx", "vy", "vz", "bx", "by", "bz"]
 SOLVER_ID["mlw_m_3d"] = 2
+VARS["roe_m_3d"] = VARS["mlw_m_3d"]
+SOLVER_ID["roe_m_3d"] = SOLVER_ROE_M_3D
+# ghost layers of each 3-D solver (hdmlw/main.f:5 and hdroe/main.f:5)
+MARGIN_3D = {"mlw_m_3d": 1, "roe_m_3d": 3}
 
 
 def _bc_all3(nvar: int, kinds=(BD_PER, BD_PER, BD_PER)):
@@ -197,25 +201,30 @@ def _bc_all3(nvar: int, kinds=(BD_PER, BD_PER, BD_PER)):
     return prog
 
 
-def _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, fields, gm, qav, bc, **extra):
-    names = VARS["mlw_m_3d"]
+def _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, fields, gm, qav, bc, solver="mlw_m_3d",
+           **extra):
+    names = VARS[solver]
     state = [np.asfortranarray(fields[k], dtype=np.float64) for k in names]
-    d = dict(solver="mlw_m_3d", solver_id=SOLVER_ID["mlw_m_3d"], names=names, x=x, dx=dx,
+    d = dict(solver=solver, solver_id=SOLVER_ID[solver], names=names, x=x, dx=dx,
              dxm=dxm, y=y, dy=dy, dym=dym, z=z, dz=dz, dzm=dzm, state=state, gm=gm, qav=qav,
-             margin=1, bc=bc)
+             margin=MARGIN_3D[solver], bc=bc)
     d.update(extra)
     return d
 
 
-def _periodic_pad(a: np.ndarray) -> np.ndarray:
-    return np.asfortranarray(np.pad(a, 1, mode="wrap"))
+def _periodic_pad(a: np.ndarray, margin: int = 1) -> np.ndarray:
+    return np.asfortranarray(np.pad(a, margin, mode="wrap"))
 
 
-def turbulence_3d(n: int = 256, seed: int = 3, kmax: float = 8.0, rms: float = 1e-2):
+def turbulence_3d(n: int = 256, seed: int = 3, kmax: float = 8.0, rms: float = 1e-2,
+                  solver: str = "mlw_m_3d"):
     """3-D MHD at plasma beta 1 on [0,1]^3, periodic: rho=1, p=0.5,
     B = sqrt(4pi)(1,0,0) (beta = 8 pi p / B^2 = 1), gamma=5/3, and a seeded
     Gaussian random velocity whose Fourier modes are limited to integer
-    wavenumbers |k| <= kmax, rescaled to an rms speed of `rms`."""
+    wavenumbers |k| <= kmax, rescaled to an rms speed of `rms`.  The interior
+    is the same for both 3-D solvers; the ghost layers are 1 (mlw_m_3d) or 3
+    (roe_m_3d) cells wide."""
+    m = MARGIN_3D[solver]
     rng = np.random.default_rng(seed)
     k = np.fft.fftfreq(n, d=1.0 / n)
     kz = np.fft.rfftfreq(n, d=1.0 / n)
@@ -230,26 +239,29 @@ def turbulence_3d(n: int = 256, seed: int = 3, kmax: float = 8.0, rms: float = 1
         comps.append(np.fft.irfftn(spec, s=(n, n, n), axes=(0, 1, 2)))
     v2 = sum(c ** 2 for c in comps)
     scale = rms / math.sqrt(float(np.mean(v2)))
-    x, dx, dxm = uniform_axis(n, 1.0)
-    shape = (n + 2,) * 3
+    x, dx, dxm = uniform_axis(n, 1.0, margin=m)
+    shape = (n + 2 * m,) * 3
     f = {
         "ro": np.ones(shape), "pr": np.full(shape, 0.5),
-        "vx": _periodic_pad(comps[0] * scale), "vy": _periodic_pad(comps[1] * scale),
-        "vz": _periodic_pad(comps[2] * scale),
+        "vx": _periodic_pad(comps[0] * scale, m), "vy": _periodic_pad(comps[1] * scale, m),
+        "vz": _periodic_pad(comps[2] * scale, m),
         "bx": np.full(shape, SQ4PI), "by": np.zeros(shape), "bz": np.zeros(shape),
     }
     return _pack3(x, dx, dxm, x.copy(), dx.copy(), dxm.copy(), x.copy(), dx.copy(), dxm.copy(),
-                  f, 5.0 / 3.0, 3.0, _bc_all3(8), safety=0.4, dtmin=1e-10, tend=1e30,
-                  name=f"turbulence_{n}^3")
+                  f, 5.0 / 3.0, 3.0, _bc_all3(8), solver=solver, safety=0.4, dtmin=1e-10,
+                  tend=1e30, name=f"turbulence_{n}^3")
 
 
-def random_state_3d(ix: int, jx: int, kx: int, seed: int = 0, amp: float = 0.05):
+def random_state_3d(ix: int, jx: int, kx: int, seed: int = 0, amp: float = 0.05,
+                    solver: str = "mlw_m_3d"):
     """Seeded smooth-plus-noise 3-D state with every component non-zero, for
-    parity tests; periodic in x, bdspp in y, bdfre in z."""
+    parity tests; periodic in x, bdspp in y, bdfre in z.  ix, jx, kx include
+    the ghost layers of the solver."""
     rng = np.random.default_rng(seed)
-    x, dx, dxm = uniform_axis(ix - 2, 1.0)
-    y, dy, dym = uniform_axis(jx - 2, 1.0)
-    z, dz, dzm = uniform_axis(kx - 2, 1.0)
+    m = MARGIN_3D[solver]
+    x, dx, dxm = uniform_axis(ix - 2 * m, 1.0, margin=m)
+    y, dy, dym = uniform_axis(jx - 2 * m, 1.0, margin=m)
+    z, dz, dzm = uniform_axis(kx - 2 * m, 1.0, margin=m)
     X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
 
     def smooth(scale):
@@ -265,8 +277,63 @@ def random_state_3d(ix: int, jx: int, kx: int, seed: int = 0, amp: float = 0.05)
         "bx": SQ4PI * (0.8 + smooth(0.2)), "by": SQ4PI * smooth(0.3), "bz": SQ4PI * smooth(0.3),
     }
     return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, 5.0 / 3.0, 3.0,
-                  _bc_all3(8, (BD_PER, BD_SPP, 5)), safety=0.4, dtmin=1e-10, tend=1e30,
-                  name=f"random3d_{ix}x{jx}x{kx}_s{seed}")
+                  _bc_all3(8, (BD_PER, BD_SPP, 5)), solver=solver, safety=0.4, dtmin=1e-10,
+                  tend=1e30, name=f"random3d_{ix}x{jx}x{kx}_s{seed}")
+
+
+def _r4(v: float) -> float:
+    """A Fortran real*4 literal or real*4 result, widened to double."""
+    return float(np.float32(v))
+
+
+def shock_tube_3d(n: int = 32, solver: str = "roe_m_3d", tend: float = 0.1):
+    """Oblique 3-D MHD shock tube as cans3d/md_mhdshktb/{hdroe,hdmlw}/model.f
+    sets it up: n^3 interior cells of size 1/n, izero = ix/2+1 centred at
+    dxm/2, gamma = 2; the discontinuity is the plane n.x = 0 with the normal
+    at theta = 60, phi = 30 degrees (real*4 60./180.); left rho=1, p=1, right
+    rho=0.125, p=0.1 (real*4 0.1); B = b0 (0.75 n +/- e) with e a unit vector
+    normal to n; v = 0.  bnd.f: bdfre on every face, margin 3 (hdroe) or 1
+    (hdmlw); tend = 0.1, safety 0.4 (main.f:25,167)."""
+    m = MARGIN_3D[solver]
+    ix = n + 2 * m
+    pi = math.acos(-1.0)
+
+    def axis():
+        dx0 = 1.0 / _r4(ix - 2 * m)
+        dxm = np.full(ix, dx0)
+        x = np.empty(ix)
+        iz = ix // 2  # 0-based index of izero = ix/2+1
+        x[iz] = dxm[iz] / 2.0
+        for i in range(iz + 1, ix):
+            x[i] = x[i - 1] + dxm[i - 1]
+        for i in range(iz - 1, -1, -1):
+            x[i] = x[i + 1] - dxm[i]
+        dx, _, dxm2 = grdrdy(x)
+        return x, dx, dxm2
+
+    x, dx, dxm = axis()
+    b0 = math.sqrt(4 * pi)
+    thini = _r4(_r4(60.0) / _r4(180.0)) * pi
+    phini = _r4(_r4(30.0) / _r4(180.0)) * pi
+    ux, uy, uz = math.sin(thini) * math.cos(phini), math.sin(thini) * math.sin(phini), \
+        math.cos(thini)
+    ebx0, eby0 = 1.0, 2.0
+    ebz0 = -(ebx0 * ux + eby0 * uy) / uz
+    ebb0 = math.sqrt(ebx0 ** 2 + eby0 ** 2 + ebz0 ** 2)
+    ebx, eby, ebz = ebx0 / ebb0, eby0 / ebb0, ebz0 / ebb0
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    left = (ux * X + uy * Y + uz * Z) <= 0.0
+    shape = (ix,) * 3
+    f = {
+        "ro": np.where(left, 1.0, 0.125), "pr": np.where(left, 1.0, _r4(0.1)),
+        "vx": np.zeros(shape), "vy": np.zeros(shape), "vz": np.zeros(shape),
+        "bx": np.where(left, b0 * 0.75 * ux + b0 * ebx, b0 * 0.75 * ux - b0 * ebx),
+        "by": np.where(left, b0 * 0.75 * uy + b0 * eby, b0 * 0.75 * uy - b0 * eby),
+        "bz": np.where(left, b0 * 0.75 * uz + b0 * ebz, b0 * 0.75 * uz - b0 * ebz),
+    }
+    return _pack3(x, dx, dxm, x.copy(), dx.copy(), dxm.copy(), x.copy(), dx.copy(), dxm.copy(),
+                  f, 2.0, 3.0, _bc_all3(8, (5, 5, 5)), solver=solver, safety=0.4, dtmin=1e-10,
+                  tend=tend, name=f"shock_tube_3d_{n}^3_{solver}")
 
 
 VARS["mlw_m_1d"] = ["ro", "pr", "vx", "vy", "by"]
