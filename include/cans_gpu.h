@@ -176,6 +176,19 @@ int cans_cfl_m_3d(double *dt, const double *safety, const double *dtmin,
                   const double *bz, const double *dx, const int *ix,
                   const double *dy, const int *jx, const double *dz,
                   const int *kx);
+/* replaces subroutine engine  (cansxx-nosupport/md_mhdshktb/hdhlld-x/
+ * engine.f:2): one two-stage HLLD step (hlld_mh.f, hlld_flux.f90,
+ * inp_const.f, inp_tvdminmod.f, adddfdx.f) on 8 arrays in Heaviside units
+ * with permeability mu.  mfdim[3]: 1 = active axis.  dxm, dym, dzm are
+ * accepted for the reference signature and not read.  An active axis needs
+ * an extent >= 4. */
+int cans_hlld_engine_3d(double *ro, double *pr, double *vx, double *vy,
+                        double *vz, double *bx, double *by, double *bz,
+                        const double *gm, const double *mu, const double *dt,
+                        const double *dx, const double *dxm, const double *dy,
+                        const double *dym, const double *dz, const double *dzm,
+                        const int *ix, const int *jx, const int *kx,
+                        const int *mfdim);
 /* Ghost-cell fill, 3-D (cans3d/bc/bd*.f:2), same conventions as 2-D. */
 int cans_bdperx_3d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx, const int *kx); /* bdperx.f:2 */
 int cans_bdpery_3d(const int *margin0, const int *margin1, double *qq, const int *ix, const int *jx, const int *kx); /* bdpery.f:2 */
@@ -234,6 +247,7 @@ int cans_gpu_release(const double *any);
 #define CANS_SOLVER_MLW_M_3D 2   /* mlw_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
 #define CANS_SOLVER_MLW_M_1D 3   /* mlw_m  1-D: ro,pr,vx,vy,by (+ bx, bxm)   */
 #define CANS_SOLVER_ROE_M_3D 4   /* roe_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
+#define CANS_SOLVER_HLLD_3D 5    /* HLLD engine: ro,pr,vx,vy,vz,bx,by,bz     */
 
 /* Boundary kinds, one per reference bd* family. */
 #define CANS_BD_NONE (-1)
@@ -260,6 +274,9 @@ typedef struct {
   int tile;                   /* tile configuration, -1 = library default   */
   void *stream;               /* cudaStream_t or NULL (library stream)      */
   const double *bx, *bxm;     /* 1-D only: the constant bx(ix), bxm(ix)     */
+  double mu;                  /* HLLD: permeability (0 = 1)                 */
+  int mfdim[3];               /* HLLD: active axes; all 0 = every axis with
+                                 an extent > 1                              */
 } cans_run_desc;
 
 typedef struct {

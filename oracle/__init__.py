@@ -54,6 +54,7 @@ def load():
         lib.oracle_mlw_m_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, _dp, i, _dp, _dp, i, _dp, _dp, i]
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
+        lib.oracle_hlld_engine_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, i, _dp, i, _dp, i, _ip]
         lib.oracle_set_threads.argtypes = [i]
         lib.oracle_get_threads.restype = i
         _lib = lib
@@ -247,7 +248,19 @@ def roe_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, gm, dx, dy, dz):
                            P(dx), ix, P(dy), jx, P(dz), kx)
 
 
+def hlld_engine_3d(ro, pr, vx, vy, vz, bx, by, bz, gm, mu, dt, dx, dy, dz, mfdim):
+    ix, jx, kx = ro.shape
+    md = (C.c_int * 3)(*mfdim)
+    load().oracle_hlld_engine_3d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], gm, mu,
+                                 dt, P(dx), ix, P(dy), jx, P(dz), kx,
+                                 C.cast(md, _ip))
+
+
 def step_3d(setup, state, dt):
+    if setup.get("solver") == "hlld_3d":
+        hlld_engine_3d(*state, setup["gm"], setup["mu"], dt, setup["dx"], setup["dy"],
+                       setup["dz"], setup["mfdim"])
+        return
     if setup.get("solver") == "roe_m_3d":
         roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])
         return

@@ -101,6 +101,16 @@ void oracle_roe_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                      const double *dx, int ix, const double *dy, int jx,
                      const double *dz, int kx);
 
+/* HLLD step of the cansxx engine (cansxx-nosupport/md_mhdshktb/hdhlld-x/
+ * engine.f:2), Heaviside units with permeability mu; mfdim[3] marks the
+ * active axes (1) as in the reference.  See hlld.c for the two places where
+ * the reference reads memory it never wrote. */
+void oracle_hlld_engine_3d(double *ro, double *pr, double *vx, double *vy,
+                           double *vz, double *bx, double *by, double *bz,
+                           double gm, double mu, double dt, const double *dx,
+                           int ix, const double *dy, int jx, const double *dz,
+                           int kx, const int *mfdim);
+
 /* Boundary kinds (reference routine family in parentheses). */
 enum {
   BD_PER = 0, /* periodic            (bdperx/bdpery/bdperz)          */

@@ -54,6 +54,22 @@ def case_roe(ix, jx, kx, seed):
     return out
 
 
+def case_hlld(ix, jx, kx, seed):
+    """One HLLD step (cansxx-nosupport/md_mhdshktb/hdhlld-x/engine.f) of a
+    seeded 3-D state in Heaviside units, every axis active."""
+    s = setups.random_state_3d(ix, jx, kx, seed=seed, solver="hlld_3d")
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dy", "dz"):
+        out["grid_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_3d(s, st, 0.4)
+    oracle.hlld_engine_3d(*st, s["gm"], s["mu"], dt, s["dx"], s["dy"], s["dz"], (1, 1, 1))
+    out.update({"dt": np.array(dt), "gm": np.array(s["gm"]), "mu": np.array(s["mu"])})
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def main():
     oracle.build()
     np.savez_compressed(OUT / "mlw_m3_2d_18x14.npz", **case_2d("mlw_m3", 18, 14, 11, 10))
@@ -71,6 +87,7 @@ def main():
                 bc[f"k{kind}_a{axis}_m{mbnd}"] = a
     np.savez_compressed(OUT / "bd_2d_9x7.npz", q=q, dxm=dxm, dym=dym, **bc)
     np.savez_compressed(OUT / "roe_m_3d_14x12x13.npz", **case_roe(14, 12, 13, 21))
+    np.savez_compressed(OUT / "hlld_3d_13x11x12.npz", **case_hlld(13, 11, 12, 22))
     print("wrote fixtures to", OUT)
 
 

@@ -44,8 +44,39 @@ def test_bad_sizes_are_rejected_without_a_device(lib):
     del z
 
 
-def test_run_desc_layout_matches_header():
-    # the ctypes mirror of cans_run_desc must keep the C field order
+def test_run_desc_layout_matches_header(tmp_path):
+    # the ctypes mirror of cans_run_desc must keep the C field order, offsets
+    # and size: compile the header with the host compiler and compare
     fields = [f[0] for f in capi._Desc._fields_]
     assert fields == ["solver", "ix", "jx", "kx", "margin", "gm", "qav", "dx", "dxm", "dy",
-                      "dym", "dz", "dzm", "exact", "tile", "stream", "bx", "bxm"]
+                      "dym", "dz", "dzm", "exact", "tile", "stream", "bx", "bxm", "mu",
+                      "mfdim"]
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    src = tmp_path / "layout.c"
+    body = "".join(f'  printf("%zu ", offsetof(cans_run_desc, {f}));\n' for f in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "cans_gpu.h"\n'
+                   "int main(void) {\n" + body +
+                   '  printf("%zu\\n", sizeof(cans_run_desc));\n  return 0;\n}\n')
+    exe = tmp_path / "layout"
+    inc = build.ROOT / "include"
+    subprocess.run([cc, f"-I{inc}", str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    want = [getattr(capi._Desc, f).offset for f in fields] + [C.sizeof(capi._Desc)]
+    assert out == want
+
+
+def test_hlld_and_roe_run_arguments_rejected_without_a_device(lib):
+    from utrip_gb300 import setups
+    s = setups.random_state_3d(12, 11, 10, seed=1, solver="roe_m_3d")
+    with pytest.raises(capi.CansError) as e:  # Roe needs three boundary layers
+        capi.Run(capi.SOLVER_ROE_M_3D, s, s["gm"], 0.0, margin=2)
+    assert e.value.code == capi.CANS_ERR_ARG
+    s = setups.shock_tube_hlld_1d(32)
+    with pytest.raises(capi.CansError) as e:  # y is one cell long: cannot be active
+        capi.Run(capi.SOLVER_HLLD_3D, s, s["gm"], 0.0, margin=3, mfdim=(1, 1, 0))
+    assert e.value.code == capi.CANS_ERR_ARG

@@ -392,3 +392,96 @@ def test_roe_oracle_matches_frozen_fixture(oracle_lib):
                         z["grid_dz"])
     for k, a in zip(names, st):
         assert np.array_equal(a, z["out_" + k]), k
+
+
+# ---- HLLD (cansxx-nosupport/hdhlld) ------------------------------------------
+
+def _hlld_grid(n=12, seed=4):
+    s = _roe_grid(n=n, seed=seed)
+    s.update(solver="hlld_3d", mu=1.0, mfdim=(1, 1, 1))
+    for k in (5, 6, 7):
+        s["state"][k] = np.asfortranarray(s["state"][k] / math.sqrt(4.0 * math.pi))
+    return s
+
+
+def test_hlld_uniform_state_changes_only_by_rounding(oracle_lib):
+    s = _hlld_grid(n=8)
+    st = [np.asfortranarray(np.full_like(a, a[7, 6, 5])) for a in s["state"]]
+    ref = [a.copy() for a in st]
+    oracle_lib.step_3d(s, st, 1e-3)
+    for k, a, b in zip(s["names"], st, ref):
+        assert float(np.max(np.abs(a - b))) <= 4e-16 * max(1.0, float(np.max(np.abs(b)))), k
+
+
+def test_hlld_translation_commutes_with_step(oracle_lib):
+    s = _hlld_grid()
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_3d(st, s["bc"], 3, s)
+    inner = (slice(3, -3),) * 3
+    sh = [np.asfortranarray(np.pad(np.roll(a[inner], (3, 5, 2), axis=(0, 1, 2)), 3)) for a in st]
+    oracle_lib.apply_bc_program_3d(sh, s["bc"], 3, s)
+    for _ in range(2):
+        for z in (st, sh):
+            oracle_lib.step_3d(s, z, 2e-3)
+            oracle_lib.apply_bc_program_3d(z, s["bc"], 3, s)
+    for k, a, b in zip(s["names"], st, sh):
+        assert np.array_equal(np.roll(a[inner], (3, 5, 2), axis=(0, 1, 2)), b[inner]), k
+
+
+def test_hlld_cyclic_axis_rotation(oracle_lib):
+    s = _hlld_grid(n=10, seed=9)
+    st = setups.copy_state(s)
+
+    def rot(q):
+        ro, pr, vx, vy, vz, bx, by, bz = q
+        t = lambda a: np.asfortranarray(np.transpose(a, (2, 0, 1)))  # noqa: E731
+        return [t(ro), t(pr), t(vz), t(vx), t(vy), t(bz), t(bx), t(by)]
+
+    rs = rot(st)
+    for z in (st, rs):
+        oracle_lib.step_3d(s, z, 3e-3)
+    inner = (slice(1, -1),) * 3  # the last x column differs by design (see hlld.c)
+    for k, a, b in zip(s["names"], rot(st), rs):
+        assert float(np.max(np.abs(a[inner] - b[inner]))) <= 1e-14 * float(np.max(np.abs(b))), k
+
+
+def test_hlld_periodic_conservation(oracle_lib):
+    s = _hlld_grid(n=12, seed=5)
+    st = setups.copy_state(s)
+    oracle_lib.apply_bc_program_3d(st, s["bc"], 3, s)
+    inner = (slice(3, -3),) * 3
+    tot = lambda a: a[inner].sum()  # noqa: E731
+    m0, mx0, bx0 = tot(st[0]), tot(st[0] * st[2]), tot(st[5])
+    for _ in range(8):
+        dt, _ = oracle_lib.cfl_3d(s, st, 0.4)
+        oracle_lib.step_3d(s, st, dt)
+        oracle_lib.apply_bc_program_3d(st, s["bc"], 3, s)
+    assert abs(tot(st[0]) - m0) <= 1e-13 * m0
+    assert abs(tot(st[0] * st[2]) - mx0) <= 1e-12 * m0
+    assert abs(tot(st[5]) - bx0) <= 1e-12 * abs(bx0)
+
+
+def test_hlld_brio_wu_structure(oracle_lib):
+    """hdhlld-x to t = 0.1: finite, positive, the left and right states
+    untouched far from the interface, the intermediate density between the
+    two initial densities and the tangential field reversed across."""
+    s = setups.shock_tube_hlld_1d(512)
+    st = setups.copy_state(s)
+    t, ns, merr, _ = oracle_lib.run_3d(s, st, 100000)
+    assert merr == 0 and t >= 0.1
+    ro, pr, by = st[0][:, 0, 0], st[1][:, 0, 0], st[6][:, 0, 0]
+    assert np.isfinite(ro).all() and pr.min() > 0.0
+    # the far states are reached only by the scheme's round-off precursors
+    assert abs(ro[5] - 1.0) < 1e-12 and abs(ro[-6] - 0.125) < 1e-12
+    assert 0.1 < ro.min() and ro.max() <= 1.0 + 1e-12
+    assert abs(by[5] - 1.0) < 1e-12 and abs(by[-6] + 1.0) < 1e-12
+
+
+def test_hlld_oracle_matches_frozen_fixture(oracle_lib):
+    z = np.load(GOLD / "hlld_3d_13x11x12.npz")
+    names = setups.VARS["hlld_3d"]
+    st = [np.asfortranarray(z["in_" + k]) for k in names]
+    oracle_lib.hlld_engine_3d(*st, float(z["gm"]), float(z["mu"]), float(z["dt"]),
+                              z["grid_dx"], z["grid_dy"], z["grid_dz"], (1, 1, 1))
+    for k, a in zip(names, st):
+        assert np.array_equal(a, z["out_" + k]), k

@@ -28,6 +28,7 @@ SOLVER_MLW_M3_2D = 1
 SOLVER_MLW_M_3D = 2
 SOLVER_MLW_M_1D = 3
 SOLVER_ROE_M_3D = 4
+SOLVER_HLLD_3D = 5
 
 BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
 
@@ -89,6 +90,7 @@ def load() -> C.CDLL:
     sig["cans_cfl_m_3d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 +
                             [_dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_roe_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _ip, _dp, _ip, _dp, _ip])
+    sig["cans_hlld_engine_3d"] = (i, [_dp] * 8 + [_dp] * 9 + [_ip] * 4)
     sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
     sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
     sig["cans_bdperx_1d"] = (i, [_ip, _ip, _dp, _ip])
@@ -296,6 +298,18 @@ def cfl_m_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy, dz):
     return dt.value, merr.value
 
 
+def hlld_engine_3d(ro, pr, vx, vy, vz, bx, by, bz, gm, mu, dt, dx, dxm, dy, dym, dz, dzm,
+                   mfdim=(1, 1, 1)):
+    """cansxx-nosupport/md_mhdshktb/hdhlld-x/engine.f:2 -- one HLLD step of the
+    3-D state in Heaviside units, in place; mfdim marks the active axes."""
+    ix, jx, kx = ro.shape
+    md = (C.c_int * 3)(*mfdim)
+    return _check(load().cans_hlld_engine_3d(
+        *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], _dref(gm), _dref(mu), _dref(dt),
+        _ptr(dx), _ptr(dxm), _ptr(dy), _ptr(dym), _ptr(dz), _ptr(dzm), _iref(ix), _iref(jx),
+        _iref(kx), C.cast(md, _ip)), "hlld_engine_3d")
+
+
 def roe_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, gm, dx, dy, dz):
     """cans3d/hdroe/roe_m.f:2 -- one Roe-MUSCL step of the 3-D state, in place
     (cells 3..n-2 updated, the others kept)."""
@@ -352,7 +366,7 @@ class _Desc(C.Structure):
                 ("margin", C.c_int), ("gm", C.c_double), ("qav", C.c_double),
                 ("dx", _dp), ("dxm", _dp), ("dy", _dp), ("dym", _dp), ("dz", _dp), ("dzm", _dp),
                 ("exact", C.c_int), ("tile", C.c_int), ("stream", C.c_void_p),
-                ("bx", _dp), ("bxm", _dp)]
+                ("bx", _dp), ("bxm", _dp), ("mu", C.c_double), ("mfdim", C.c_int * 3)]
 
 
 class RunState(C.Structure):
@@ -365,12 +379,13 @@ class Run:
     """Device-resident run of the reference time loop (cans_run_* API)."""
 
     def __init__(self, solver: int, grid: dict, gm: float, qav: float, margin: int = 1,
-                 exact: bool = False, tile: int = -1, stream: int | None = None):
+                 exact: bool = False, tile: int = -1, stream: int | None = None,
+                 mu: float = 1.0, mfdim=(0, 0, 0)):
         self.lib = load()
         self.solver = solver
         self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8,
-                     SOLVER_MLW_M_1D: 5, SOLVER_ROE_M_3D: 8}[solver]
-        three = solver in (SOLVER_MLW_M_3D, SOLVER_ROE_M_3D)
+                     SOLVER_MLW_M_1D: 5, SOLVER_ROE_M_3D: 8, SOLVER_HLLD_3D: 8}[solver]
+        three = solver in (SOLVER_MLW_M_3D, SOLVER_ROE_M_3D, SOLVER_HLLD_3D)
         one = solver == SOLVER_MLW_M_1D
 
         def arr(k):
@@ -386,7 +401,8 @@ class Run:
                   None if one else arr("dy"), None if one else arr("dym"),
                   arr("dz") if three else None, arr("dzm") if three else None,
                   1 if exact else 0, tile, C.c_void_p(stream) if stream else None,
-                  arr("bx") if one else None, arr("bxm") if one else None)
+                  arr("bx") if one else None, arr("bxm") if one else None,
+                  mu, (C.c_int * 3)(*mfdim))
         self.shape = (nx,) if one else ((nx, ny) + ((nz,) if three else ()))
         h = C.c_void_p()
         _check(self.lib.cans_run_create(C.byref(h), C.byref(d)), "cans_run_create")

@@ -94,6 +94,23 @@ cudaError_t launch_roe3d(bool exact, const double *A, double *B,
                          const Phys &ph, double dt, Ctl *ctl, Box3 box,
                          cudaStream_t s);
 
+// ---- 3-D HLLD (cansxx engine) ----------------------------------------------
+// One two-stage HLLD step on 8 arrays (Heaviside units, permeability mu);
+// A -> B for every cell.  mfdim[a] = 1 marks an active axis.  scratch holds
+// hlld3d_scratch_doubles(ix*jx*kx) doubles.  With ctl the kernels take dt and
+// the buffers from it; launch_hlld3d_finish then reduces the CFL of every
+// cell of the new state and ends the loop iteration.
+size_t hlld3d_scratch_doubles(size_t ncells);
+cudaError_t launch_hlld3d(bool exact, const double *A, double *B,
+                          double *scratch, int ix, int jx, int kx,
+                          const int *mfdim, const Axis &ax, const Axis &ay,
+                          const Axis &az, double gm, double mu, double dt,
+                          const Ctl *ctl, cudaStream_t s);
+cudaError_t launch_hlld3d_finish(bool exact, int ix, int jx, int kx,
+                                 const Axis &ax, const Axis &ay,
+                                 const Axis &az, const Phys &ph, Ctl *ctl,
+                                 cudaStream_t s);
+
 // ---- 1-D ------------------------------------------------------------------
 // The whole 1-D loop (or one fixed-dt step) as one cluster launch, in place
 // on 5 arrays (ro,pr,vx,vy,by) of ix doubles.

@@ -745,6 +745,62 @@ extern "C" int cans_roe_m_3d(double *ro, double *pr, double *vx, double *vy,
   return CANS_OK;
 }
 
+// engine (cansxx-nosupport/md_mhdshktb/hdhlld-x/engine.f:2): one HLLD step,
+// on the registered mirrors when the 8 arrays are a resident set.
+extern "C" int cans_hlld_engine_3d(double *ro, double *pr, double *vx,
+                                   double *vy, double *vz, double *bx,
+                                   double *by, double *bz, const double *gm,
+                                   const double *mu, const double *dt,
+                                   const double *dx, const double *dxm,
+                                   const double *dy, const double *dym,
+                                   const double *dz, const double *dzm,
+                                   const int *ix, const int *jx, const int *kx,
+                                   const int *mfdim) {
+  (void)dxm;
+  (void)dym;
+  (void)dzm;
+  if (!ro || !pr || !vx || !vy || !vz || !bx || !by || !bz || !gm || !mu ||
+      !dt || !dx || !dy || !dz || !ix || !jx || !kx || !mfdim)
+    return CANS_ERR_ARG;
+  const int nn[3] = {*ix, *jx, *kx};
+  for (int a = 0; a < 3; a++) {
+    if (nn[a] < 1 || (mfdim[a] == 1 && nn[a] < 4)) return CANS_ERR_ARG;
+  }
+  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const size_t n = (size_t)nn[0] * nn[1] * nn[2];
+  MirrorSet *m = resident_step_set(arrs, 8);
+  Scratch &sc = g_scratch;
+  DevAxis *dax = m ? &m->ax : &sc.ax, *day = m ? &m->ay : &sc.ay,
+          *daz = m ? &m->az : &sc.az;
+  // adddfdx reads dx, dy, dz only
+  if ((rc = dax->upload(nn[0], dx, dx, s))) return rc;
+  if ((rc = day->upload(nn[1], dy, dy, s))) return rc;
+  if ((rc = daz->upload(nn[2], dz, dz, s))) return rc;
+  if ((rc = sc.ensure_roe(hlld3d_scratch_doubles(n)))) return rc;
+  if (m) {
+    CK(launch_hlld3d(exact_mode(), m->buf[m->cur], m->buf[m->cur ^ 1], sc.roe,
+                     nn[0], nn[1], nn[2], mfdim, dax->a, day->a, daz->a, *gm, *mu,
+                     *dt, nullptr, s));
+    m->cur ^= 1;
+    return CANS_OK;
+  }
+  if ((rc = sc.ensure(8 * n))) return rc;
+  for (int v = 0; v < 8; v++)
+    CK(cudaMemcpyAsync(sc.A + v * n, arrs[v], sizeof(double) * n,
+                       cudaMemcpyHostToDevice, s));
+  CK(launch_hlld3d(exact_mode(), sc.A, sc.B, sc.roe, nn[0], nn[1], nn[2], mfdim,
+                   dax->a, day->a, daz->a, *gm, *mu, *dt, nullptr, s));
+  for (int v = 0; v < 8; v++)
+    CK(cudaMemcpyAsync(arrs[v], sc.B + v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
 #define CANS_BD3(NAME, KIND, AXIS)                                              \
   extern "C" int NAME(const int *mbnd, const int *margin, double *qq,           \
                       const int *ix, const int *jx, const int *kx) {            \
@@ -892,7 +948,9 @@ struct cans_run {
   int graph_iters = 0;
   int graph_nodes = 0;
   double *bx1 = nullptr;       // 1-D: device bx (ix) followed by bxm (ix)
-  double *roe = nullptr;       // Roe: stage scratch (roe3d_scratch_doubles)
+  double *roe = nullptr;       // Roe / HLLD: stage scratch
+  int mfdim[3] = {1, 1, 1};    // HLLD: active axes
+  double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
 };
 
@@ -905,16 +963,20 @@ int solver_nvar(int solver) {
     case CANS_SOLVER_MLW_M_3D: return 8;
     case CANS_SOLVER_MLW_M_1D: return 5;
     case CANS_SOLVER_ROE_M_3D: return 8;
+    case CANS_SOLVER_HLLD_3D: return 8;
     default: return 0;
   }
 }
 int solver_ndim(int solver) {
-  if (solver == CANS_SOLVER_MLW_M_3D || solver == CANS_SOLVER_ROE_M_3D) return 3;
+  if (solver == CANS_SOLVER_MLW_M_3D || solver == CANS_SOLVER_ROE_M_3D ||
+      solver == CANS_SOLVER_HLLD_3D)
+    return 3;
   return solver == CANS_SOLVER_MLW_M_1D ? 1 : 2;
 }
 bool is_roe(const cans_run *h) { return h->d.solver == CANS_SOLVER_ROE_M_3D; }
+bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
-  if (is_roe(h) || h->ndim == 1) return 1;
+  if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
   return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
 }
 // 1-D: the whole loop (or one fixed step) as one cluster launch, in place
@@ -941,6 +1003,10 @@ Box3 inner_box(const cans_run *h) {
 
 cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
                         double dt, Ctl *ctl, Box3 box) {
+  if (is_hlld(h))
+    return launch_hlld3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
+                         h->mfdim, h->ax.a, h->ay.a, h->az.a, h->ph.gm, h->mu, dt,
+                         ctl, h->s);
   if (is_roe(h))
     return launch_roe3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
@@ -958,6 +1024,9 @@ cudaError_t bc_kernels(cans_run *h, double *S, const Ctl *ctl) {
                      h->s);
 }
 cudaError_t frame_kernel(cans_run *h) {
+  if (is_hlld(h))  // the step reduces no CFL: every cell after the fill
+    return launch_hlld3d_finish(h->d.exact != 0, h->d.ix, h->d.jx, h->d.kx,
+                                h->ax.a, h->ay.a, h->az.a, h->ph, h->ctl, h->s);
   if (h->ndim == 3)
     return launch_frame3d(h->d.exact != 0, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
                           h->ay.a, h->az.a, h->ph, h->bc.margin, h->ctl, h->s);
@@ -1037,6 +1106,19 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   // boundary program must rewrite three layers (hdroe/main.f:5)
   if (d->solver == CANS_SOLVER_ROE_M_3D && d->margin < 3) return CANS_ERR_ARG;
   const int ndim = solver_ndim(d->solver);
+  // HLLD: active axes from mfdim (all 0: every axis longer than one cell);
+  // an inactive axis may have any extent, an active one needs the stencil
+  int mfdim[3] = {d->mfdim[0], d->mfdim[1], d->mfdim[2]};
+  if (d->solver == CANS_SOLVER_HLLD_3D) {
+    const int nn[3] = {d->ix, d->jx, d->kx};
+    if (!mfdim[0] && !mfdim[1] && !mfdim[2])
+      for (int a = 0; a < 3; a++) mfdim[a] = nn[a] > 1 ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+      if (nn[a] < 1 || (mfdim[a] == 1 && nn[a] < 2 * d->margin + 2)) return CANS_ERR_ARG;
+      if (mfdim[a] != 0 && mfdim[a] != 1) return CANS_ERR_ARG;
+    }
+    if (!d->dx || !d->dy || !d->dz || !d->dxm || !d->dym || !d->dzm) return CANS_ERR_ARG;
+  }
   // every extent must exceed the two frames of margin+1 cells that the
   // boundary program and the frame CFL work on
   const int wmin = 2 * (d->margin + 1) + 1;
@@ -1044,6 +1126,8 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     if (d->ix < mlw1d_min_cells() || d->jx != 1 || d->kx != 1 ||
         !d->dx || !d->dxm || !d->bx || !d->bxm)
       return CANS_ERR_ARG;
+  } else if (d->solver == CANS_SOLVER_HLLD_3D) {
+    // checked above
   } else {
     if (d->ix < wmin || d->jx < wmin) return CANS_ERR_ARG;
     if (ndim == 2 && d->kx != 1) return CANS_ERR_ARG;
@@ -1095,10 +1179,13 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
                           cudaMemcpyHostToDevice, h->s);
     if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy(bx)"));
   }
-  if (is_roe(h)) {
-    e = cudaMalloc(&h->roe, sizeof(double) * roe3d_scratch_doubles(h->n));
-    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(roe scratch)"));
+  if (is_roe(h) || is_hlld(h)) {
+    const size_t nd = is_roe(h) ? roe3d_scratch_doubles(h->n) : hlld3d_scratch_doubles(h->n);
+    e = cudaMalloc(&h->roe, sizeof(double) * nd);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(stage scratch)"));
   }
+  for (int a = 0; a < 3; a++) h->mfdim[a] = mfdim[a];
+  h->mu = d->mu > 0.0 ? d->mu : 1.0;
   std::memset(&h->host_ctl, 0, sizeof(Ctl));
   h->host_ctl.done = 1;
   h->host_ctl.buf[0] = h->buf[0];
@@ -1133,6 +1220,10 @@ extern "C" int cans_run_set_bc(cans_run *h, int var, int face, int kind,
   if (!h || var < 0 || var >= h->nvar || face < 0 || face >= 2 * h->ndim ||
       kind < CANS_BD_NONE || kind > CANS_BD_FRD)
     return CANS_ERR_ARG;
+  // a boundary rule reads and writes `margin` layers on both sides of the
+  // axis, so the axis must hold both frames and a cell between them
+  const int ext[3] = {h->d.ix, h->d.jx, h->d.kx};
+  if (kind != CANS_BD_NONE && ext[face / 2] < 2 * h->bc.margin + 1) return CANS_ERR_ARG;
   h->bc.kind[var][face] = kind;
   h->bc.q0[var][face] = q0;
   drop_graph(h);

@@ -63,7 +63,7 @@ def _cfl(setup, state, safety):
     if setup["solver"] == "mlw_m_1d":
         return capi.cfl_m_1d(safety, setup["dtmin"], setup["gm"], setup["bx"], *state,
                              setup["dx"])
-    if setup["solver"] in ("mlw_m_3d", "roe_m_3d"):
+    if setup["solver"] in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
         return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
                              setup["dy"], setup["dz"])
     if setup["solver"] == "mlw_m3":
@@ -79,6 +79,11 @@ def _step(setup, state, dt):
         return
     if setup["solver"] == "roe_m_3d":
         capi.roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])
+        return
+    if setup["solver"] == "hlld_3d":
+        capi.hlld_engine_3d(*state, setup["gm"], setup["mu"], dt, setup["dx"], setup["dxm"],
+                            setup["dy"], setup["dym"], setup["dz"], setup["dzm"],
+                            setup["mfdim"])
         return
     args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
     if setup["solver"] == "mlw_m_3d":
@@ -106,7 +111,7 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             t = t + dt
             dts.append(dt)
             _step(setup, state, dt)
-            {"mlw_m_3d": _bnd3, "roe_m_3d": _bnd3,
+            {"mlw_m_3d": _bnd3, "roe_m_3d": _bnd3, "hlld_3d": _bnd3,
              "mlw_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
@@ -118,7 +123,8 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
 
 def make_run(setup, exact=False, tile=-1, stream=None) -> capi.Run:
     run = capi.Run(setup["solver_id"], setup, setup["gm"], setup["qav"], setup["margin"],
-                   exact=exact, tile=tile, stream=stream)
+                   exact=exact, tile=tile, stream=stream, mu=setup.get("mu", 1.0),
+                   mfdim=setup.get("mfdim", (0, 0, 0)))
     run.set_bc_program(setup["bc"])
     return run
 

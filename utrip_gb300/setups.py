@@ -16,7 +16,8 @@ import math
 
 import numpy as np
 
-from .capi import BD_PER, BD_SPP, BD_SMN, SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M_3D
+from .capi import (BD_PER, BD_SPP, BD_SMN, SOLVER_HLLD_3D, SOLVER_MLW_M_2D,
+                   SOLVER_MLW_M3_2D, SOLVER_ROE_M_3D)
 
 SQ4PI = math.sqrt(4.0 * math.pi)
 
@@ -189,8 +190,14 @@ VARS["mlw_m_3d"] = ["ro", "pr", "vx", "vy", "vz", "bx", "by", "bz"]
 SOLVER_ID["mlw_m_3d"] = 2
 VARS["roe_m_3d"] = VARS["mlw_m_3d"]
 SOLVER_ID["roe_m_3d"] = SOLVER_ROE_M_3D
-# ghost layers of each 3-D solver (hdmlw/main.f:5 and hdroe/main.f:5)
-MARGIN_3D = {"mlw_m_3d": 1, "roe_m_3d": 3}
+VARS["hlld_3d"] = VARS["mlw_m_3d"]
+SOLVER_ID["hlld_3d"] = SOLVER_HLLD_3D
+# ghost layers of each 3-D solver (hdmlw/main.f:5, hdroe/main.f:5,
+# cansxx-nosupport/md_mhdshktb/hdhlld-x/main.f:5)
+MARGIN_3D = {"mlw_m_3d": 1, "roe_m_3d": 3, "hlld_3d": 3}
+# the HLLD engine works in Heaviside units (B^2/2): fields given in CANS units
+# (B^2/8pi) are divided by sqrt(4 pi) for it
+B_UNIT = {"mlw_m_3d": 1.0, "roe_m_3d": 1.0, "hlld_3d": 1.0 / math.sqrt(4.0 * math.pi)}
 
 
 def _bc_all3(nvar: int, kinds=(BD_PER, BD_PER, BD_PER)):
@@ -208,6 +215,8 @@ def _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, fields, gm, qav, bc, solver="mlw_
     d = dict(solver=solver, solver_id=SOLVER_ID[solver], names=names, x=x, dx=dx,
              dxm=dxm, y=y, dy=dy, dym=dym, z=z, dz=dz, dzm=dzm, state=state, gm=gm, qav=qav,
              margin=MARGIN_3D[solver], bc=bc)
+    if solver == "hlld_3d":
+        d.update(mu=1.0, mfdim=(1, 1, 1))
     d.update(extra)
     return d
 
@@ -217,13 +226,14 @@ def _periodic_pad(a: np.ndarray, margin: int = 1) -> np.ndarray:
 
 
 def turbulence_3d(n: int = 256, seed: int = 3, kmax: float = 8.0, rms: float = 1e-2,
-                  solver: str = "mlw_m_3d"):
+                  solver: str = "mlw_m_3d", b0=(1.0, 0.0, 0.0)):
     """3-D MHD at plasma beta 1 on [0,1]^3, periodic: rho=1, p=0.5,
     B = sqrt(4pi)(1,0,0) (beta = 8 pi p / B^2 = 1), gamma=5/3, and a seeded
     Gaussian random velocity whose Fourier modes are limited to integer
     wavenumbers |k| <= kmax, rescaled to an rms speed of `rms`.  The interior
     is the same for both 3-D solvers; the ghost layers are 1 (mlw_m_3d) or 3
-    (roe_m_3d) cells wide."""
+    (roe_m_3d, hlld_3d) cells wide; hlld_3d takes the field in Heaviside
+    units.  b0 is the unit direction of the mean field."""
     m = MARGIN_3D[solver]
     rng = np.random.default_rng(seed)
     k = np.fft.fftfreq(n, d=1.0 / n)
@@ -245,7 +255,9 @@ def turbulence_3d(n: int = 256, seed: int = 3, kmax: float = 8.0, rms: float = 1
         "ro": np.ones(shape), "pr": np.full(shape, 0.5),
         "vx": _periodic_pad(comps[0] * scale, m), "vy": _periodic_pad(comps[1] * scale, m),
         "vz": _periodic_pad(comps[2] * scale, m),
-        "bx": np.full(shape, SQ4PI), "by": np.zeros(shape), "bz": np.zeros(shape),
+        "bx": np.full(shape, SQ4PI * B_UNIT[solver] * b0[0]),
+        "by": np.full(shape, SQ4PI * B_UNIT[solver] * b0[1]),
+        "bz": np.full(shape, SQ4PI * B_UNIT[solver] * b0[2]),
     }
     return _pack3(x, dx, dxm, x.copy(), dx.copy(), dxm.copy(), x.copy(), dx.copy(), dxm.copy(),
                   f, 5.0 / 3.0, 3.0, _bc_all3(8), solver=solver, safety=0.4, dtmin=1e-10,
@@ -276,6 +288,8 @@ def random_state_3d(ix: int, jx: int, kx: int, seed: int = 0, amp: float = 0.05,
         "vx": smooth(0.3), "vy": smooth(0.3), "vz": smooth(0.3),
         "bx": SQ4PI * (0.8 + smooth(0.2)), "by": SQ4PI * smooth(0.3), "bz": SQ4PI * smooth(0.3),
     }
+    for k in ("bx", "by", "bz"):
+        f[k] = f[k] * B_UNIT[solver]
     return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, 5.0 / 3.0, 3.0,
                   _bc_all3(8, (BD_PER, BD_SPP, 5)), solver=solver, safety=0.4, dtmin=1e-10,
                   tend=1e30, name=f"random3d_{ix}x{jx}x{kx}_s{seed}")
@@ -397,3 +411,49 @@ def random_state_1d(ix: int, seed: int = 0):
 
 def copy_state(setup: dict):
     return [a.copy(order="F") for a in setup["state"]]
+
+
+def shock_tube_hlld_1d(n: int = 1024, tend: float = 0.1):
+    """The HLLD shock tube of cansxx-nosupport/md_mhdshktb/hdhlld-x
+    (model.f, bnd.f, main.f): ix = n + 6 (margin 3), jx = kx = 1, active axis
+    x only (mfdim = 1,0,0); gamma = 2, mu = 1, Heaviside units with
+    b0 = sqrt(2 mu/gm) = 1: left rho=1, p=1, B=(0.75, 1, 0), right rho=0.125,
+    p=0.1, B=(0.75, -1, 0), v=0, the interface at x=0 (izero = ix/2+1 centred
+    at dxm/2).  The cell size is 1/dble(max(ix-2*margin, ix)) = 1/ix, as the
+    model writes it; grdrdy2 gives dx = dxm.  bdfrex on both faces, margin 3;
+    the loop calls the 3-D cfl_m with safety 0.4, tend = 0.1."""
+    m = 3
+    ix, jx, kx = n + 2 * m, 1, 1
+
+    def axis(nx):
+        d0 = 1.0 / float(max(nx - 2 * m, nx))
+        dxm = np.full(nx, d0)
+        x = np.empty(nx)
+        iz = nx // 2  # 0-based index of izero = nx/2+1
+        x[iz] = dxm[iz] / 2.0
+        for i in range(iz + 1, nx):
+            x[i] = x[i - 1] + dxm[i - 1]
+        for i in range(iz - 1, -1, -1):
+            x[i] = x[i + 1] - dxm[i]
+        dx = np.empty(nx)
+        dx[1:] = 0.5 * (dxm[:-1] + dxm[1:])  # grdrdy2.f
+        dx[0] = dxm[0]
+        return x, dx, dxm
+
+    x, dx, dxm = axis(ix)
+    y, dy, dym = axis(jx)
+    z, dz, dzm = axis(kx)
+    gm, mu = 2.0, 1.0
+    b0 = math.sqrt(2.0 * mu / gm)
+    left = (x <= 0.0)[:, None, None] * np.ones((ix, jx, kx), dtype=bool)
+    f = {
+        "ro": np.where(left, 1.0, 0.125), "pr": np.where(left, 1.0, 0.1),
+        "vx": np.zeros((ix, jx, kx)), "vy": np.zeros((ix, jx, kx)), "vz": np.zeros((ix, jx, kx)),
+        "bx": np.where(left, b0 * 0.75 * 1.0 + b0 * 0.0, b0 * 0.75 * 1.0 - b0 * 0.0),
+        "by": np.where(left, b0 * 0.75 * 0.0 + b0 * 1.0, b0 * 0.75 * 0.0 - b0 * 1.0),
+        "bz": np.where(left, b0 * 0.75 * 0.0 + b0 * 0.0, b0 * 0.75 * 0.0 - b0 * 0.0),
+    }
+    bc = [(v, f_, 5, 0.0) for v in range(8) for f_ in (0, 1)]
+    return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, gm, 0.0, bc, solver="hlld_3d",
+                  mu=mu, mfdim=(1, 0, 0), safety=0.4, dtmin=1e-10, tend=tend,
+                  name=f"shock_tube_hlld_{n}")
