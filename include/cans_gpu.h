@@ -362,6 +362,34 @@ int cans_batch_autotune(cans_batch *b, int trial_steps, int *config);
 /* FP64 fused multiply-add throughput of the current device, TFLOP/s. */
 int cans_measure_fp64_tflops(double *tflops);
 
+/* ------------------------------------------------------------------------ */
+/* Discrete adjoint of the 2-D mlw_m3 run (no counterpart in the reference:  */
+/* the reverse sweep the differentiation pattern adds beside the step)       */
+/* ------------------------------------------------------------------------ */
+/* The run's current state is P_0; every call leaves it unchanged.  The step
+ * k+1 state is bnd(mlw_m3(P_k, dts[k])) with the run's boundary program.
+ * The objective is J = sum over the interior cells of (bx^2+by^2+bz^2)/(8 pi)
+ * dx(i) dy(j) of the final state.  Only CANS_SOLVER_MLW_M3_2D runs. */
+/* Forward run with the CFL step of cfl_m3 (safety as given): the dt of every
+ * step into dts[nsteps] and, if J is not NULL, the objective. */
+int cans_run_record_dts(cans_run *h, long long nsteps, double safety,
+                        double *dts, double *J);
+/* Forward run with the frozen dts: the objective only. */
+int cans_run_objective(cans_run *h, long long nsteps, const double *dts,
+                       double *J);
+/* Forward run and reverse sweep with binomial checkpointing in at most nsnap
+ * stored states (nsnap >= 2; the schedule minimises the recomputed steps):
+ * J, and dJ/dP_0 into grad[v] (host arrays of ix*jx doubles, one per state
+ * variable, NULL entries skipped; ghost cells included).  *nfwd (if not
+ * NULL) receives the number of forward steps executed. */
+int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts,
+                     int nsnap, double *J, double *const *grad,
+                     long long *nfwd);
+/* Transpose of the run's boundary program applied in place to host arrays
+ * (one per state variable): folds ghost-cell sensitivities into the cells
+ * they are copied from. */
+int cans_run_bc_transpose(cans_run *h, double *const *arrays);
+
 #ifdef __cplusplus
 }
 #endif

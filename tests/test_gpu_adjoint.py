@@ -1,0 +1,242 @@
+"""GPU tests of the discrete adjoint of the 2-D mlw_m3 run (the reverse sweep
+with binomial checkpointing, cans_run_adjoint): the transposed boundary fill
+passes the dot-product test, the gradient does not depend on the number of
+stored states, and directional derivatives match FP64 central finite
+differences of both the GPU forward and the CPU oracle (frozen dt sequence)."""
+import numpy as np
+import pytest
+
+import oracle
+from utrip_gb300 import capi, drivers, setups
+
+pytestmark = pytest.mark.gpu
+H = 1e-6
+EPS = float(np.finfo(np.float64).eps)
+
+
+def _close(ad, fd, J, h=H):
+    """Within 1e-6 of the central difference, beyond the difference's own
+    rounding error (a few ulps of J divided by 2h)."""
+    return abs(ad - fd) <= 1e-6 * abs(fd) + 8.0 * EPS * abs(J) / (2.0 * h)
+
+
+def _setup(n=32, ny=28, beta=1.0, seed=4, qav=0.0):
+    """Shear layer whose ghost cells already obey its boundary program (the
+    set-up fills them from the analytic profile), so that a perturbation of
+    the interior extended by the same program moves along a straight line.
+
+    The artificial viscosity q = qav dxm max(0, |dv| - 1e-4) switches on
+    where a velocity jump crosses 1e-4; the shear layer has jumps passing
+    through that value, so J has kinks close to the base point and a
+    central difference with h = 1e-6 can straddle one.  The smooth checks
+    therefore run with qav = 0; the viscosity path is checked on a state
+    whose jumps are far from the switch, and the kinks by their own test."""
+    s = setups.shear_layer(n, beta=beta, ny=ny, seed=seed)
+    s["qav"] = qav
+    oracle.apply_bc_program(s["state"], s["bc"], s["margin"], s)
+    return s
+
+
+def _fd(s, z, dts, h):
+    Js = []
+    for sg in (h, -h):
+        r = _run(s, [np.asfortranarray(a + sg * b) for a, b in zip(s["state"], z)])
+        try:
+            Js.append(r.objective(dts))
+        finally:
+            r.close()
+    return (Js[0] - Js[1]) / (2 * h), Js
+
+
+def _run(s, state=None, exact=False):
+    run = drivers.make_run(s, exact=exact)
+    run.push(state if state is not None else s["state"])
+    return run
+
+
+def _directional_state(s, d, h):
+    """P_0 + h d on the interior vy, ghosts refilled by the boundary program."""
+    st = setups.copy_state(s)
+    st[3][1:-1, 1:-1] += h * d
+    oracle.apply_bc_program(st, s["bc"], s["margin"], s)
+    return st
+
+
+def _extend(s, d):
+    """The direction d on the interior vy as a full state (ghosts by the same
+    linear boundary program)."""
+    z = [np.zeros_like(a) for a in s["state"]]
+    z[3][1:-1, 1:-1] = d
+    oracle.apply_bc_program(z, s["bc"], s["margin"], s)
+    return z
+
+
+def test_bc_transpose_dot_product(gpu, oracle_lib):
+    s = _setup()
+    rng = np.random.default_rng(1)
+    lam = [np.asfortranarray(rng.standard_normal(a.shape)) for a in s["state"]]
+    d = [np.asfortranarray(rng.standard_normal(a.shape)) for a in s["state"]]
+    bd = [a.copy(order="F") for a in d]
+    oracle.apply_bc_program(bd, s["bc"], s["margin"], s)
+    run = _run(s)
+    try:
+        lt = [a.copy(order="F") for a in lam]
+        run.bc_transpose(lt)
+    finally:
+        run.close()
+    lhs = sum(float(np.sum(a * b)) for a, b in zip(lt, d))
+    rhs = sum(float(np.sum(a * b)) for a, b in zip(lam, bd))
+    assert abs(lhs - rhs) <= 1e-12 * abs(rhs)
+
+
+def test_gradient_independent_of_stored_states(gpu):
+    s = _setup()
+    run = _run(s)
+    try:
+        dts, J0 = run.record_dts(24)
+        ref = None
+        nf_prev = None
+        for nsnap in (2, 3, 5, 25):
+            J, g, nf = run.adjoint(dts, nsnap=nsnap)
+            assert J == J0
+            if ref is None:
+                ref = g
+            else:
+                for a, b in zip(g, ref):
+                    assert np.array_equal(a, b)
+            if nf_prev is not None:
+                assert nf <= nf_prev  # more snapshots never cost more steps
+            nf_prev = nf
+        assert nf_prev == 2 * 24 - 1  # one stored state per step: no recomputation
+    finally:
+        run.close()
+
+
+def test_directional_derivative_matches_gpu_finite_differences(gpu):
+    s = _setup()
+    nsteps = 40
+    run = _run(s)
+    try:
+        dts, _ = run.record_dts(nsteps)
+        J, grad, _ = run.adjoint(dts, nsnap=6)
+    finally:
+        run.close()
+    rng = np.random.default_rng(5)
+    for _ in range(4):
+        d = rng.standard_normal((s["state"][0].shape[0] - 2, s["state"][0].shape[1] - 2))
+        ad = sum(float(np.sum(g * e)) for g, e in zip(grad, _extend(s, d)))
+        Js = []
+        for h in (H, -H):
+            r = _run(s, _directional_state(s, d, h))
+            try:
+                Js.append(r.objective(dts))
+            finally:
+                r.close()
+        fd = (Js[0] - Js[1]) / (2 * H)
+        assert _close(ad, fd, J), (ad, fd)
+
+
+def test_directional_derivative_matches_oracle_finite_differences(gpu, oracle_lib):
+    s = _setup(n=24, ny=20)
+    nsteps = 20
+    run = _run(s)
+    try:
+        dts, _ = run.record_dts(nsteps)
+        _, grad, _ = run.adjoint(dts, nsnap=4)
+    finally:
+        run.close()
+
+    def oracle_J(st):
+        for dt in dts:
+            oracle.step_2d(s, st, dt)
+            oracle.apply_bc_program(st, s["bc"], s["margin"], s)
+        bx, by, bz = st[5], st[6], st[7]
+        w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
+        e = (bx * bx + by * by + bz * bz)[1:-1, 1:-1]
+        return float(np.sum(e * w)) / np.pi / 8.0
+
+    rng = np.random.default_rng(9)
+    for _ in range(2):
+        d = rng.standard_normal((24, 20))
+        ad = sum(float(np.sum(g * e)) for g, e in zip(grad, _extend(s, d)))
+        jp, jm = oracle_J(_directional_state(s, d, H)), oracle_J(_directional_state(s, d, -H))
+        fd = (jp - jm) / (2 * H)
+        assert _close(ad, fd, jp), (ad, fd)
+
+
+def test_beta_derivative(gpu):
+    """p = 0.625 beta in every cell, so dJ/dbeta = 0.625 sum(dJ/dp)."""
+    beta = 1.0
+    s = _setup(beta=beta)
+    nsteps = 30
+    run = _run(s)
+    try:
+        dts, _ = run.record_dts(nsteps)
+        _, grad, _ = run.adjoint(dts, nsnap=8)
+    finally:
+        run.close()
+    ad = 0.625 * float(np.sum(grad[1]))
+    Js = []
+    for h in (H, -H):
+        sb = _setup(beta=beta + h)
+        r = _run(sb)
+        try:
+            Js.append(r.objective(dts))
+        finally:
+            r.close()
+    fd = (Js[0] - Js[1]) / (2 * H)
+    assert _close(ad, fd, Js[0]), (ad, fd)
+
+
+def test_viscosity_path_matches_finite_differences(gpu):
+    """A random state whose velocity jumps are all far above 1e-4: every AV
+    face is on and stays on, the objective is smooth there."""
+    s = setups.random_state(30, 26, seed=3)
+    oracle.apply_bc_program(s["state"], s["bc"], s["margin"], s)
+    run = _run(s)
+    try:
+        dts, _ = run.record_dts(5)
+        _, grad, _ = run.adjoint(dts, nsnap=3)
+    finally:
+        run.close()
+    rng = np.random.default_rng(2)
+    for v in range(8):
+        z = [np.zeros_like(a) for a in s["state"]]
+        z[v][1:-1, 1:-1] = rng.standard_normal((28, 24))
+        oracle.apply_bc_program(z, s["bc"], s["margin"], s)
+        ad = sum(float(np.sum(g * e)) for g, e in zip(grad, z))
+        fd, (jp, _) = _fd(s, z, dts, H)
+        assert _close(ad, fd, jp), (s["names"][v], ad, fd)
+
+
+def test_viscosity_kinks_on_the_shear_layer(gpu):
+    """With qav = 3 the shear-layer objective has kinks within 1e-6 of the
+    base point: the one-sided differences at h = 1e-6 disagree, the adjoint
+    (the derivative of the branches taken at the base point) lies between
+    them, and a central difference with h = 1e-8 recovers it."""
+    s = _setup(qav=3.0)
+    run = _run(s)
+    try:
+        dts, J0 = run.record_dts(40)
+        _, grad, _ = run.adjoint(dts, nsnap=6)
+    finally:
+        run.close()
+    d = np.random.default_rng(5).standard_normal((32, 28))
+    z = _extend(s, d)
+    ad = sum(float(np.sum(g * e)) for g, e in zip(grad, z))
+    _, (jp, jm) = _fd(s, z, dts, H)
+    fwd, bwd = (jp - J0) / H, (J0 - jm) / H
+    assert abs(fwd - bwd) > 1e-3 * abs(ad)
+    assert min(fwd, bwd) <= ad <= max(fwd, bwd)
+    fd8, _ = _fd(s, z, dts, 1e-8)
+    assert abs(fd8 - ad) <= 1e-5 * abs(ad)
+
+
+def test_adjoint_rejects_other_solvers(gpu):
+    s = setups.random_state_3d(12, 12, 12, seed=1)
+    run = drivers.make_run(s)
+    try:
+        with pytest.raises(capi.CansError):
+            run.record_dts(3)
+    finally:
+        run.close()

@@ -75,6 +75,11 @@ def load() -> C.CDLL:
         "cans_run_profile": (i, [vp, i, _dp, _dp]),
         "cans_cfl_m3_2d_noalloc": (i, [_dp, _dp, _dp, _ip, _dp] + [vp] * 8 + [vp, _ip, vp, _ip]),
         "cans_run_set_graph": (i, [vp, i]),
+        "cans_run_record_dts": (i, [vp, C.c_longlong, d, _dp, _dp]),
+        "cans_run_objective": (i, [vp, C.c_longlong, _dp, _dp]),
+        "cans_run_adjoint": (i, [vp, C.c_longlong, _dp, i, _dp, C.POINTER(_dp),
+                                 C.POINTER(C.c_longlong)]),
+        "cans_run_bc_transpose": (i, [vp, C.POINTER(_dp)]),
         "cans_batch_create": (i, [C.POINTER(vp), i, vp]), "cans_batch_destroy": (i, [vp]),
         "cans_batch_set_bc": (i, [vp, i, i, i, i, d]),
         "cans_batch_push": (i, [vp, i, C.POINTER(_dp)]),
@@ -479,6 +484,41 @@ class Run:
         _check(self.lib.cans_run_profile(self.h, iters, C.byref(a), C.byref(b)),
                "cans_run_profile")
         return a.value, b.value
+
+    # ---- discrete adjoint (2-D mlw_m3 runs) ----
+    def record_dts(self, nsteps: int, safety: float = 0.4):
+        """Forward run from the current state with the CFL time step; returns
+        (dts, J) -- the frozen dt sequence and the final magnetic energy."""
+        dts = np.zeros(nsteps)
+        J = C.c_double(0.0)
+        _check(self.lib.cans_run_record_dts(self.h, nsteps, safety, _ptr(dts), C.byref(J)),
+               "cans_run_record_dts")
+        return dts, J.value
+
+    def objective(self, dts) -> float:
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        J = C.c_double(0.0)
+        _check(self.lib.cans_run_objective(self.h, dts.size, _ptr(dts), C.byref(J)),
+               "cans_run_objective")
+        return J.value
+
+    def adjoint(self, dts, nsnap: int = 32):
+        """Reverse sweep with binomial checkpointing in nsnap stored states:
+        returns (J, grad, nfwd), grad the list of dJ/dP_0 arrays (ghosts
+        included) in the state's variable order."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        grad = [np.zeros(self.shape, order="F") for _ in range(self.nvar)]
+        arr = (_dp * self.nvar)(*[_ptr(g) for g in grad])
+        J = C.c_double(0.0)
+        nf = C.c_longlong(0)
+        _check(self.lib.cans_run_adjoint(self.h, dts.size, _ptr(dts), nsnap, C.byref(J), arr,
+                                         C.byref(nf)), "cans_run_adjoint")
+        return J.value, grad, nf.value
+
+    def bc_transpose(self, arrays):
+        """Transpose of the boundary program, in place on host arrays."""
+        arr = (_dp * self.nvar)(*[_ptr(a) for a in arrays])
+        _check(self.lib.cans_run_bc_transpose(self.h, arr), "cans_run_bc_transpose")
 
 
 def measure_fp64_tflops() -> float:

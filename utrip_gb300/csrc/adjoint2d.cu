@@ -1,0 +1,610 @@
+// Discrete adjoint of the 2.5-D mLW step (cans2d/hdmlw/mlw_m3.f:2-377) and of
+// the boundary fill, by hand: the transpose of the linearised step, applied to
+// an adjoint state lambda (one array per primitive variable), on the device.
+//
+// Forward step, in the stage form the reverse follows (1-based indices,
+// interior = 2..n-1 in both axes, dt frozen):
+//   (1) cell values of the input primitives P: conserved U, fluxes FX, FY
+//       (mlw_m3.f:107-202);
+//   (2) du = -0.25 dt (dxi (FX(i+1)-FX(i-1)) + dyi (FY(j+1)-FY(j-1)))   interior
+//       Uh(corner) = avg4(U) - dt dxim/2 (dx FX) - dt dyim/2 (dy FY)  (mlwhalf.f)
+//   (3) corner primitives Ph = prim(Uh), corner fluxes GX, GY (:214-310)
+//   (4) du -= 0.5 dt (dxi sum_uy (dx GX) + dyi sum_ux (dy GY))         (mlwfull.f)
+//   (5) q = qav dxm max(0, |dv| - 1e-4) on faces; du += dt dxi (q dxim dU - ...)
+//       for the 8 conserved variables (mlwartv.f, :324-345)
+//   (6) P' = prim(U + du) on the interior; other cells keep P (:349-374)
+// az is updated by sources of its own and feeds back into nothing, and the
+// objective does not read it, so its adjoint is identically zero.
+//
+// Reverse, given lambda' for P' after the boundary fill (bc_transpose first):
+//   k_adj_cells   a' = (dP'/dU')^T lambda' on the interior (= adjoint of du),
+//                 plus the cell values U, FX, FY of P for the kernels below
+//   k_adj_corners adjoint of GX, GY gathered from the four cells that read each
+//                 corner (transpose of (4)), then of Uh through (3)
+//   k_adj_gather  adjoint of U, FX, FY of every cell gathered from its corners
+//                 (transpose of the predictor), its neighbours (transpose of
+//                 the half step and of the viscosity in U), the adjoint of q
+//                 on its two faces per axis, then (dU,FX,FY/dP)^T; cells
+//                 outside the interior pass lambda' through unchanged.
+// Every transpose is a gather: no atomics, deterministic results.
+#include <cuda_runtime.h>
+
+#include "cans_common.cuh"
+#include "cans_internal.h"
+
+namespace cans {
+
+namespace {
+
+constexpr int kT = 128;
+// primitive slots of the state (mlw_m3 order) and conserved slots
+enum { P_RO = 0, P_PR, P_VX, P_VY, P_VZ, P_BX, P_BY, P_BZ, P_AZ };
+enum { C_RO = 0, C_EE, C_RX, C_RY, C_RZ, C_BX, C_BY, C_BZ };
+
+struct G2 {
+  int ix, jx;
+  size_t n;
+};
+
+__device__ __forceinline__ bool interior(const G2 &g, int i, int j) {
+  return i >= 1 && i <= g.ix - 2 && j >= 1 && j <= g.jx - 2;  // 0-based
+}
+
+// (1): conserved values and fluxes of one primitive state (mlw_m3.f:107-202)
+struct CellF {
+  double U[8], FX[8], FY[8];
+};
+__device__ __forceinline__ void cell_forward(const double *p, const Phys &ph,
+                                             CellF &o) {
+  const double ro = p[P_RO], pr = p[P_PR], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
+  const double bx = p[P_BX], by = p[P_BY], bz = p[P_BZ];
+  const double vv = vx * vx + vy * vy + vz * vz, bb = bx * bx + by * by + bz * bz;
+  const double ex = -vy * bz + vz * by, ey = -vz * bx + vx * bz, ez = -vx * by + vy * bx;
+  const double ep = pr * ph.ggm1 + 0.5 * ro * vv;
+  o.U[C_RO] = ro;
+  o.U[C_EE] = pr * ph.gm1i + 0.5 * ro * vv + ph.pi8i * bb;
+  o.U[C_RX] = ro * vx;
+  o.U[C_RY] = ro * vy;
+  o.U[C_RZ] = ro * vz;
+  o.U[C_BX] = bx;
+  o.U[C_BY] = by;
+  o.U[C_BZ] = bz;
+  o.FX[C_RO] = ro * vx;
+  o.FY[C_RO] = ro * vy;
+  o.FX[C_EE] = ep * vx + (bz * ey - by * ez) * ph.pi4i;
+  o.FY[C_EE] = ep * vy + (bx * ez - bz * ex) * ph.pi4i;
+  o.FX[C_RX] = ro * vx * vx + pr + ph.pi8i * (by * by + bz * bz - bx * bx);
+  o.FY[C_RX] = ro * vx * vy - ph.pi4i * bx * by;
+  o.FX[C_RY] = ro * vy * vx - ph.pi4i * by * bx;
+  o.FY[C_RY] = ro * vy * vy + pr + ph.pi8i * (bx * bx + bz * bz - by * by);
+  o.FX[C_RZ] = ro * vz * vx - ph.pi4i * bz * bx;
+  o.FY[C_RZ] = ro * vz * vy - ph.pi4i * bz * by;
+  o.FX[C_BX] = 0.0;
+  o.FY[C_BX] = ez;
+  o.FX[C_BY] = -ez;
+  o.FY[C_BY] = 0.0;
+  o.FX[C_BZ] = ey;
+  o.FY[C_BZ] = -ex;
+}
+
+// primitives of a conserved state (mlw_m3.f:214-223, 365-374)
+__device__ __forceinline__ void prim_forward(const double *u, const Phys &ph, double *p) {
+  const double ro = u[C_RO];
+  const double vx = u[C_RX] / ro, vy = u[C_RY] / ro, vz = u[C_RZ] / ro;
+  const double vv = vx * vx + vy * vy + vz * vz;
+  const double bb = u[C_BX] * u[C_BX] + u[C_BY] * u[C_BY] + u[C_BZ] * u[C_BZ];
+  p[P_RO] = ro;
+  p[P_PR] = ph.gm1 * (u[C_EE] - 0.5 * ro * vv - ph.pi8i * bb);
+  p[P_VX] = vx;
+  p[P_VY] = vy;
+  p[P_VZ] = vz;
+  p[P_BX] = u[C_BX];
+  p[P_BY] = u[C_BY];
+  p[P_BZ] = u[C_BZ];
+}
+
+// Transpose of (1): given the adjoints aU, aX, aY of U, FX, FY at the point
+// p, add (d(U,FX,FY)/dP)^T (aU, aX, aY) to ap.
+__device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
+                                             const double *aU, const double *aX,
+                                             const double *aY, double *ap) {
+  const double ro = p[P_RO], pr = p[P_PR], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
+  const double bx = p[P_BX], by = p[P_BY], bz = p[P_BZ];
+  const double vv = vx * vx + vy * vy + vz * vz;
+  const double ex = -vy * bz + vz * by, ey = -vz * bx + vx * bz, ez = -vx * by + vy * bx;
+  const double ep = pr * ph.ggm1 + 0.5 * ro * vv;
+  const double p4 = ph.pi4i, p8 = ph.pi8i;
+  double aro = 0, apr = 0, avx = 0, avy = 0, avz = 0, abx = 0, aby = 0, abz = 0;
+  double aep = 0, aex = 0, aey = 0, aez = 0, avv = 0, abb = 0;
+  // U
+  aro += aU[C_RO];
+  apr += aU[C_EE] * ph.gm1i;
+  aro += aU[C_EE] * 0.5 * vv;
+  avv += aU[C_EE] * 0.5 * ro;
+  abb += aU[C_EE] * p8;
+  aro += aU[C_RX] * vx + aU[C_RY] * vy + aU[C_RZ] * vz;
+  avx += aU[C_RX] * ro;
+  avy += aU[C_RY] * ro;
+  avz += aU[C_RZ] * ro;
+  abx += aU[C_BX];
+  aby += aU[C_BY];
+  abz += aU[C_BZ];
+  // FX
+  aro += aX[C_RO] * vx;
+  avx += aX[C_RO] * ro;
+  aep += aX[C_EE] * vx;
+  avx += aX[C_EE] * ep;
+  abz += aX[C_EE] * p4 * ey;
+  aey += aX[C_EE] * p4 * bz;
+  aby -= aX[C_EE] * p4 * ez;
+  aez -= aX[C_EE] * p4 * by;
+  aro += aX[C_RX] * vx * vx;
+  avx += aX[C_RX] * 2.0 * ro * vx;
+  apr += aX[C_RX];
+  aby += aX[C_RX] * p8 * 2.0 * by;
+  abz += aX[C_RX] * p8 * 2.0 * bz;
+  abx -= aX[C_RX] * p8 * 2.0 * bx;
+  aro += aX[C_RY] * vy * vx;
+  avy += aX[C_RY] * ro * vx;
+  avx += aX[C_RY] * ro * vy;
+  aby -= aX[C_RY] * p4 * bx;
+  abx -= aX[C_RY] * p4 * by;
+  aro += aX[C_RZ] * vz * vx;
+  avz += aX[C_RZ] * ro * vx;
+  avx += aX[C_RZ] * ro * vz;
+  abz -= aX[C_RZ] * p4 * bx;
+  abx -= aX[C_RZ] * p4 * bz;
+  aez -= aX[C_BY];
+  aey += aX[C_BZ];
+  // FY
+  aro += aY[C_RO] * vy;
+  avy += aY[C_RO] * ro;
+  aep += aY[C_EE] * vy;
+  avy += aY[C_EE] * ep;
+  abx += aY[C_EE] * p4 * ez;
+  aez += aY[C_EE] * p4 * bx;
+  abz -= aY[C_EE] * p4 * ex;
+  aex -= aY[C_EE] * p4 * bz;
+  aro += aY[C_RX] * vx * vy;
+  avx += aY[C_RX] * ro * vy;
+  avy += aY[C_RX] * ro * vx;
+  abx -= aY[C_RX] * p4 * by;
+  aby -= aY[C_RX] * p4 * bx;
+  aro += aY[C_RY] * vy * vy;
+  avy += aY[C_RY] * 2.0 * ro * vy;
+  apr += aY[C_RY];
+  abx += aY[C_RY] * p8 * 2.0 * bx;
+  abz += aY[C_RY] * p8 * 2.0 * bz;
+  aby -= aY[C_RY] * p8 * 2.0 * by;
+  aro += aY[C_RZ] * vz * vy;
+  avz += aY[C_RZ] * ro * vy;
+  avy += aY[C_RZ] * ro * vz;
+  abz -= aY[C_RZ] * p4 * by;
+  aby -= aY[C_RZ] * p4 * bz;
+  aez += aY[C_BX];
+  aex -= aY[C_BZ];
+  // ep, E, |v|^2, |B|^2
+  apr += aep * ph.ggm1;
+  aro += aep * 0.5 * vv;
+  avv += aep * 0.5 * ro;
+  avy -= aex * bz;
+  abz -= aex * vy;
+  avz += aex * by;
+  aby += aex * vz;
+  avz -= aey * bx;
+  abx -= aey * vz;
+  avx += aey * bz;
+  abz += aey * vx;
+  avx -= aez * by;
+  aby -= aez * vx;
+  avy += aez * bx;
+  abx += aez * vy;
+  avx += 2.0 * vx * avv;
+  avy += 2.0 * vy * avv;
+  avz += 2.0 * vz * avv;
+  abx += 2.0 * bx * abb;
+  aby += 2.0 * by * abb;
+  abz += 2.0 * bz * abb;
+  ap[P_RO] += aro;
+  ap[P_PR] += apr;
+  ap[P_VX] += avx;
+  ap[P_VY] += avy;
+  ap[P_VZ] += avz;
+  ap[P_BX] += abx;
+  ap[P_BY] += aby;
+  ap[P_BZ] += abz;
+}
+
+// Transpose of prim_forward at the point whose primitives are p: given ap,
+// return au = (dP/dU)^T ap.
+__device__ __forceinline__ void prim_reverse(const double *p, const Phys &ph,
+                                             const double *ap, double *au) {
+  const double ro = p[P_RO], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
+  const double vv = vx * vx + vy * vy + vz * vz;
+  const double apr = ap[P_PR];
+  const double avv = -ph.gm1 * 0.5 * ro * apr;
+  const double abb = -ph.gm1 * ph.pi8i * apr;
+  const double ri = 1.0 / ro;
+  const double avx = ap[P_VX] + 2.0 * vx * avv, avy = ap[P_VY] + 2.0 * vy * avv,
+               avz = ap[P_VZ] + 2.0 * vz * avv;
+  au[C_EE] = ph.gm1 * apr;
+  au[C_RX] = avx * ri;
+  au[C_RY] = avy * ri;
+  au[C_RZ] = avz * ri;
+  au[C_RO] = ap[P_RO] - ph.gm1 * 0.5 * vv * apr - (avx * vx + avy * vy + avz * vz) * ri;
+  au[C_BX] = ap[P_BX] + 2.0 * p[P_BX] * abb;
+  au[C_BY] = ap[P_BY] + 2.0 * p[P_BY] * abb;
+  au[C_BZ] = ap[P_BZ] + 2.0 * p[P_BZ] * abb;
+}
+
+__device__ __forceinline__ void load_prim(const double *S, size_t n, size_t c, double *p) {
+#pragma unroll
+  for (int v = 0; v < 8; v++) p[v] = S[v * n + c];
+}
+
+// a' on the interior, the cell values U, FX, FY of P everywhere
+__global__ void __launch_bounds__(kT)
+    k_adj_cells(const double *__restrict__ P, const double *__restrict__ R,
+                const double *__restrict__ lam, double *__restrict__ A1,
+                double *__restrict__ CU, G2 g, Phys ph) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= g.n) return;
+  const int i = (int)(c % g.ix), j = (int)(c / g.ix);
+  double p[8];
+  load_prim(P, g.n, c, p);
+  CellF f;
+  cell_forward(p, ph, f);
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    CU[v * g.n + c] = f.U[v];
+    CU[(8 + v) * g.n + c] = f.FX[v];
+    CU[(16 + v) * g.n + c] = f.FY[v];
+  }
+  double au[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (interior(g, i, j)) {
+    double r[8], ap[8];
+    load_prim(R, g.n, c, r);
+    load_prim(lam, g.n, c, ap);
+    prim_reverse(r, ph, ap, au);
+  }
+#pragma unroll
+  for (int v = 0; v < 8; v++) A1[v * g.n + c] = au[v];
+}
+
+// corners (p+1/2, q+1/2), p = 0..ix-2, q = 0..jx-2 (0-based), stored at p+q*ix
+__global__ void __launch_bounds__(kT)
+    k_adj_corners(const double *__restrict__ CU, const double *__restrict__ A1,
+                  double *__restrict__ A2, G2 g, Axis ax, Axis ay, Phys ph,
+                  double dt) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= g.n) return;
+  const int p = (int)(c % g.ix), q = (int)(c / g.ix);
+  double out[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (p <= g.ix - 2 && q <= g.jx - 2) {
+    const size_t c00 = c, c10 = c + 1, c01 = c + g.ix, c11 = c + g.ix + 1;
+    // forward corner state (mlwhalf.f part 2)
+    double uh[8];
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      const double *U = CU + v * g.n, *FX = CU + (8 + v) * g.n, *FY = CU + (16 + v) * g.n;
+      const double avg = 0.25 * (U[c10] + U[c00] + U[c11] + U[c01]);
+      const double dfdx = ax.dim[p] * (FX[c10] - FX[c00] + FX[c11] - FX[c01]) / 2;
+      const double dfdy = ay.dim[q] * (FY[c01] - FY[c00] + FY[c11] - FY[c10]) / 2;
+      uh[v] = avg - dt * dfdx - dt * dfdy;
+    }
+    double ph8[8];
+    prim_forward(uh, ph, ph8);
+    // adjoint of GX, GY at this corner: the cells (p,q), (p+1,q), (p,q+1),
+    // (p+1,q+1) that read it in mlwfull (0-based cell indices)
+    const bool i00 = interior(g, p, q), i10 = interior(g, p + 1, q),
+               i01 = interior(g, p, q + 1), i11 = interior(g, p + 1, q + 1);
+    const double hx0 = 0.5 * dt * ax.di[p], hx1 = 0.5 * dt * ax.di[p + 1];
+    const double hy0 = 0.5 * dt * ay.di[q], hy1 = 0.5 * dt * ay.di[q + 1];
+    double aX[8], aY[8];
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      const double *a = A1 + v * g.n;
+      const double l00 = i00 ? a[c00] : 0.0, l10 = i10 ? a[c10] : 0.0;
+      const double l01 = i01 ? a[c01] : 0.0, l11 = i11 ? a[c11] : 0.0;
+      aX[v] = -hx0 * ay.u1[q] * l00 + hx1 * ay.u1[q] * l10 - hx0 * ay.u0[q + 1] * l01 +
+              hx1 * ay.u0[q + 1] * l11;
+      aY[v] = -hy0 * ax.u1[p] * l00 - hy0 * ax.u0[p + 1] * l10 + hy1 * ax.u1[p] * l01 +
+              hy1 * ax.u0[p + 1] * l11;
+    }
+    double aP[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const double zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    cell_reverse(ph8, ph, zero8, aX, aY, aP);
+    prim_reverse(ph8, ph, aP, out);
+  }
+#pragma unroll
+  for (int v = 0; v < 8; v++) A2[v * g.n + c] = out[v];
+}
+
+// adjoint of P for every cell
+__global__ void __launch_bounds__(kT)
+    k_adj_gather(const double *__restrict__ P, const double *__restrict__ CU,
+                 const double *__restrict__ A1, const double *__restrict__ A2,
+                 const double *__restrict__ lam, double *__restrict__ out, G2 g,
+                 Axis ax, Axis ay, Phys ph, double dt) {
+  const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= g.n) return;
+  const int i = (int)(c % g.ix), j = (int)(c / g.ix);
+  const size_t n = g.n, sx = 1, sy = (size_t)g.ix;
+  double p[8];
+  load_prim(P, n, c, p);
+  const bool in_c = interior(g, i, j);
+  const bool in_xm = interior(g, i - 1, j), in_xp = interior(g, i + 1, j);
+  const bool in_ym = interior(g, i, j - 1), in_yp = interior(g, i, j + 1);
+  // corners around the cell: (i-1+1/2, j-1+1/2) .. (i+1/2, j+1/2)
+  const bool k_mm = i >= 1 && j >= 1, k_pm = i <= g.ix - 2 && j >= 1;
+  const bool k_mp = i >= 1 && j <= g.jx - 2, k_pp = i <= g.ix - 2 && j <= g.jx - 2;
+  // artificial-viscosity coefficients of the four faces (mlw_m3.f:324-334)
+  const double *VX = P + P_VX * n, *VY = P + P_VY * n;
+  double qxm = 0, qxp = 0, qym = 0, qyp = 0, gxm = 0, gxp = 0, gym = 0, gyp = 0;
+  const double eps = CANS_AV_EPS;
+  if (i >= 1) {
+    const double d = VX[c] - VX[c - sx];
+    const double e = fabs(d) - eps;
+    qxm = ph.qav * ax.dm[i - 1] * (e > 0.0 ? e : 0.0);
+    gxm = e > 0.0 ? ph.qav * ax.dm[i - 1] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+  }
+  if (i <= g.ix - 2) {
+    const double d = VX[c + sx] - VX[c];
+    const double e = fabs(d) - eps;
+    qxp = ph.qav * ax.dm[i] * (e > 0.0 ? e : 0.0);
+    gxp = e > 0.0 ? ph.qav * ax.dm[i] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+  }
+  if (j >= 1) {
+    const double d = VY[c] - VY[c - sy];
+    const double e = fabs(d) - eps;
+    qym = ph.qav * ay.dm[j - 1] * (e > 0.0 ? e : 0.0);
+    gym = e > 0.0 ? ph.qav * ay.dm[j - 1] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+  }
+  if (j <= g.jx - 2) {
+    const double d = VY[c + sy] - VY[c];
+    const double e = fabs(d) - eps;
+    qyp = ph.qav * ay.dm[j] * (e > 0.0 ? e : 0.0);
+    gyp = e > 0.0 ? ph.qav * ay.dm[j] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+  }
+  double aU[8], aX[8], aY[8];
+  double aqxm = 0, aqxp = 0, aqym = 0, aqyp = 0;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const double *a = A1 + v * n, *h = A2 + v * n, *U = CU + v * n;
+    const double l0 = in_c ? a[c] : 0.0;
+    const double lxm = in_xm ? a[c - sx] : 0.0, lxp = in_xp ? a[c + sx] : 0.0;
+    const double lym = in_ym ? a[c - sy] : 0.0, lyp = in_yp ? a[c + sy] : 0.0;
+    // U' = U + du on the interior
+    double au = l0;
+    // viscosity, linear in U (mlwartv.f)
+    if (in_c)
+      au -= dt * (ax.di[i] * (qxp * ax.dim[i] + (i >= 1 ? qxm * ax.dim[i - 1] : 0.0)) +
+                  ay.di[j] * (qyp * ay.dim[j] + (j >= 1 ? qym * ay.dim[j - 1] : 0.0))) * l0;
+    if (in_xm) au += dt * ax.di[i - 1] * qxm * ax.dim[i - 1] * lxm;
+    if (in_xp) au += dt * ax.di[i + 1] * qxp * ax.dim[i] * lxp;
+    if (in_ym) au += dt * ay.di[j - 1] * qym * ay.dim[j - 1] * lym;
+    if (in_yp) au += dt * ay.di[j + 1] * qyp * ay.dim[j] * lyp;
+    // corner predictor: 0.25 of each surrounding corner
+    double hmm = k_mm ? h[c - sx - sy] : 0.0, hpm = k_pm ? h[c - sy] : 0.0;
+    double hmp = k_mp ? h[c - sx] : 0.0, hpp = k_pp ? h[c] : 0.0;
+    au += 0.25 * (hmm + hpm + hmp + hpp);
+    aU[v] = au;
+    // half-step central differences (mlwhalf.f part 1)
+    double axv = 0.0, ayv = 0.0;
+    if (in_xm) axv -= 0.25 * dt * ax.di[i - 1] * lxm;
+    if (in_xp) axv += 0.25 * dt * ax.di[i + 1] * lxp;
+    if (in_ym) ayv -= 0.25 * dt * ay.di[j - 1] * lym;
+    if (in_yp) ayv += 0.25 * dt * ay.di[j + 1] * lyp;
+    // corner predictor: -dt dxim (FX(p+1)-FX(p) ...)/2, -dt dyim (...)/2
+    if (i >= 1) axv -= 0.5 * dt * ax.dim[i - 1] * (hmm + hmp);
+    if (i <= g.ix - 2) axv += 0.5 * dt * ax.dim[i] * (hpm + hpp);
+    if (j >= 1) ayv -= 0.5 * dt * ay.dim[j - 1] * (hmm + hpm);
+    if (j <= g.jx - 2) ayv += 0.5 * dt * ay.dim[j] * (hmp + hpp);
+    aX[v] = axv;
+    aY[v] = ayv;
+    // adjoint of the face coefficients q (viscosity, linear in q)
+    if (i >= 1) {
+      const double dU = U[c] - U[c - sx];
+      aqxm += dt * ax.dim[i - 1] * dU * ((in_xm ? ax.di[i - 1] * lxm : 0.0) - (in_c ? ax.di[i] * l0 : 0.0));
+    }
+    if (i <= g.ix - 2) {
+      const double dU = U[c + sx] - U[c];
+      aqxp += dt * ax.dim[i] * dU * ((in_c ? ax.di[i] * l0 : 0.0) - (in_xp ? ax.di[i + 1] * lxp : 0.0));
+    }
+    if (j >= 1) {
+      const double dU = U[c] - U[c - sy];
+      aqym += dt * ay.dim[j - 1] * dU * ((in_ym ? ay.di[j - 1] * lym : 0.0) - (in_c ? ay.di[j] * l0 : 0.0));
+    }
+    if (j <= g.jx - 2) {
+      const double dU = U[c + sy] - U[c];
+      aqyp += dt * ay.dim[j] * dU * ((in_c ? ay.di[j] * l0 : 0.0) - (in_yp ? ay.di[j + 1] * lyp : 0.0));
+    }
+  }
+  double ap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cell_reverse(p, ph, aU, aX, aY, ap);
+  // q(face) = qav dxm max(0, |v(+) - v(-)| - eps): the cell is (+) of the
+  // lower face and (-) of the upper face
+  ap[P_VX] += aqxm * gxm - aqxp * gxp;
+  ap[P_VY] += aqym * gym - aqyp * gyp;
+  // cells the step does not update pass the adjoint through
+  if (!in_c) {
+#pragma unroll
+    for (int v = 0; v < 8; v++) ap[v] += lam[v * n + c];
+  }
+#pragma unroll
+  for (int v = 0; v < 8; v++) out[v * n + c] = ap[v];
+  out[P_AZ * n + c] = 0.0;
+}
+
+// Transpose of the boundary program of one axis on one line, over all
+// variables: the rules of bd_line (bc_line.cuh) in reverse order, each
+// assignment dst = s*src turned into a(src) += s*a(dst), a(dst) = 0.
+__device__ void bd_line_t(int kind, int mbnd, int m, double *q, int n, size_t st,
+                          const double *dxm) {
+#define QL(l) q[(size_t)((l)-1) * st]
+  if (kind == BD_PER) {
+    const int b0 = 1 + m, b1 = n - m;
+    if (mbnd == 0)
+      for (int i = m; i >= 1; i--) { QL(b1 + 1 - i) += QL(b0 - i); QL(b0 - i) = 0.0; }
+    else
+      for (int i = m; i >= 1; i--) { QL(b0 - 1 + i) += QL(b1 + i); QL(b1 + i) = 0.0; }
+    return;
+  }
+  if (mbnd == 0) {
+    const int b = 1 + m;
+    switch (kind) {
+      case BD_SPP: for (int i = m; i >= 1; i--) { QL(b - 1 + i) += QL(b - i); QL(b - i) = 0.0; } break;
+      case BD_SPN: for (int i = m; i >= 1; i--) { QL(b - 1 + i) -= QL(b - i); QL(b - i) = 0.0; } break;
+      case BD_SMP: for (int i = m; i >= 1; i--) { QL(b + i) += QL(b - i); QL(b - i) = 0.0; } break;
+      case BD_SMN:
+        QL(b) = 0.0;
+        for (int i = m; i >= 1; i--) { QL(b + i) -= QL(b - i); QL(b - i) = 0.0; }
+        break;
+      case BD_FRE: for (int i = m; i >= 1; i--) { QL(b) += QL(b - i); QL(b - i) = 0.0; } break;
+      case BD_CNS: for (int i = m; i >= 1; i--) QL(b - i) = 0.0; break;
+      case BD_FRD: {
+        double adq = 0.0;  // q(b-i) = q(b-i+1) - dqq dxm(b-i), dqq = (q(b+1)-q(b))/dxm(b)
+        for (int i = m; i >= 1; i--) {
+          QL(b - i + 1) += QL(b - i);
+          adq -= QL(b - i) * dxm[b - i - 1];
+          QL(b - i) = 0.0;
+        }
+        QL(b + 1) += adq / dxm[b - 1];
+        QL(b) -= adq / dxm[b - 1];
+        break;
+      }
+      default: break;
+    }
+  } else {
+    const int b = n - m;
+    switch (kind) {
+      case BD_SPP: for (int i = m; i >= 1; i--) { QL(b + 1 - i) += QL(b + i); QL(b + i) = 0.0; } break;
+      case BD_SPN: for (int i = m; i >= 1; i--) { QL(b + 1 - i) -= QL(b + i); QL(b + i) = 0.0; } break;
+      case BD_SMP: for (int i = m; i >= 1; i--) { QL(b - i) += QL(b + i); QL(b + i) = 0.0; } break;
+      case BD_SMN:
+        QL(b) = 0.0;
+        for (int i = m; i >= 1; i--) { QL(b - i) -= QL(b + i); QL(b + i) = 0.0; }
+        break;
+      case BD_FRE: for (int i = m; i >= 1; i--) { QL(b) += QL(b + i); QL(b + i) = 0.0; } break;
+      case BD_CNS: for (int i = m; i >= 1; i--) QL(b + i) = 0.0; break;
+      case BD_FRD: {
+        double adq = 0.0;  // q(b+i) = q(b+i-1) + dqq dxm(b+i-1), dqq = (q(b)-q(b-1))/dxm(b-1)
+        for (int i = m; i >= 1; i--) {
+          QL(b + i - 1) += QL(b + i);
+          adq += QL(b + i) * dxm[b + i - 2];
+          QL(b + i) = 0.0;
+        }
+        QL(b) += adq / dxm[b - 2];
+        QL(b - 1) -= adq / dxm[b - 2];
+        break;
+      }
+      default: break;
+    }
+  }
+#undef QL
+}
+
+__global__ void k_bc2d_t(int nvar, double *L, int ix, int jx, int axis, BcTable bc,
+                         const double *dxm) {
+  const int n = axis == 0 ? ix : jx;
+  const size_t st = axis == 0 ? 1 : (size_t)ix;
+  const long long nlines = axis == 0 ? jx : ix;
+  const size_t nall = (size_t)ix * jx;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nlines * nvar;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(t / nlines);
+    const long long line = t % nlines;
+    double *q = L + (size_t)v * nall + (axis == 0 ? (size_t)line * ix : (size_t)line);
+    const int klo = bc.kind[v][2 * axis], khi = bc.kind[v][2 * axis + 1];
+    // the forward applies the lower then the upper rule: reverse order here
+    if (khi >= 0) bd_line_t(khi, 1, bc.margin, q, n, st, dxm);
+    if (klo >= 0) bd_line_t(klo, 0, bc.margin, q, n, st, dxm);
+  }
+}
+
+// J = sum over the interior of (bx^2+by^2+bz^2)/(8 pi) dx dy (block partial
+// sums, reduced in a fixed order by k_sum_final) and its gradient
+__global__ void __launch_bounds__(256)
+    k_objective(const double *__restrict__ P, double *__restrict__ lam,
+                double *__restrict__ part, G2 g, Axis ax, Axis ay, Phys ph) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.ix), j = (int)(c / g.ix);
+    const double bx = P[P_BX * g.n + c], by = P[P_BY * g.n + c], bz = P[P_BZ * g.n + c];
+    const bool in = interior(g, i, j);
+    const double w = in ? ax.d[i] * ay.d[j] : 0.0;
+    s += (bx * bx + by * by + bz * bz) * ph.pi8i * w;
+    if (lam) {
+#pragma unroll
+      for (int v = 0; v < 9; v++) lam[v * g.n + c] = 0.0;
+      lam[P_BX * g.n + c] = 2.0 * ph.pi8i * w * bx;
+      lam[P_BY * g.n + c] = 2.0 * ph.pi8i * w * by;
+      lam[P_BZ * g.n + c] = 2.0 * ph.pi8i * w * bz;
+    }
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_final(const double *part, int nb, double *out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += part[b];
+    *out = s;
+  }
+}
+
+}  // namespace
+
+size_t adj2d_scratch_doubles(size_t ncells) { return 40 * ncells + 1024; }
+
+cudaError_t launch_adj2d_step(const double *P, const double *R, const double *lam_in,
+                              double *lam_out, double *scratch, int ix, int jx,
+                              const Axis &ax, const Axis &ay, const Phys &ph,
+                              double dt, cudaStream_t s) {
+  G2 g{ix, jx, (size_t)ix * jx};
+  double *A1 = scratch, *A2 = scratch + 8 * g.n, *CU = scratch + 16 * g.n;
+  const unsigned blocks = (unsigned)((g.n + kT - 1) / kT);
+  k_adj_cells<<<blocks, kT, 0, s>>>(P, R, lam_in, A1, CU, g, ph);
+  k_adj_corners<<<blocks, kT, 0, s>>>(CU, A1, A2, g, ax, ay, ph, dt);
+  k_adj_gather<<<blocks, kT, 0, s>>>(P, CU, A1, A2, lam_in, lam_out, g, ax, ay, ph, dt);
+  count_launch(3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc2d_transpose(int nvar, double *lam, int ix, int jx,
+                                  const Axis &ax, const Axis &ay, const BcTable &bc,
+                                  cudaStream_t s) {
+  // the forward fills x, then y: transpose y first
+  for (int axis = 1; axis >= 0; axis--) {
+    const long long total = (long long)(axis == 0 ? jx : ix) * nvar;
+    int blocks = (int)((total + 127) / 128);
+    if (blocks < 1) blocks = 1;
+    k_bc2d_t<<<blocks, 128, 0, s>>>(nvar, lam, ix, jx, axis, bc, axis == 0 ? ax.dm : ay.dm);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_adj2d_objective(const double *P, double *lam, double *J,
+                                   double *scratch, int ix, int jx, const Axis &ax,
+                                   const Axis &ay, const Phys &ph, cudaStream_t s) {
+  G2 g{ix, jx, (size_t)ix * jx};
+  const int nb = 256;
+  double *part = scratch;
+  k_objective<<<nb, 256, 0, s>>>(P, lam, part, g, ax, ay, ph);
+  k_sum_final<<<1, 32, 0, s>>>(part, nb, J);
+  count_launch(2);
+  return cudaGetLastError();
+}
+
+}  // namespace cans

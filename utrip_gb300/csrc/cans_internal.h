@@ -111,6 +111,27 @@ cudaError_t launch_hlld3d_finish(bool exact, int ix, int jx, int kx,
                                  const Axis &az, const Phys &ph, Ctl *ctl,
                                  cudaStream_t s);
 
+// ---- discrete adjoint of the 2-D mlw_m3 step ---------------------------------
+// P: input state (9 arrays), R: the step's raw output, lam_in: adjoint of R
+// (after the transposed boundary fill), lam_out: adjoint of P.  scratch holds
+// adj2d_scratch_doubles(ix*jx) doubles.
+size_t adj2d_scratch_doubles(size_t ncells);
+cudaError_t launch_adj2d_step(const double *P, const double *R,
+                              const double *lam_in, double *lam_out,
+                              double *scratch, int ix, int jx, const Axis &ax,
+                              const Axis &ay, const Phys &ph, double dt,
+                              cudaStream_t s);
+// transpose of the 2-D boundary program, in place on nvar adjoint arrays
+cudaError_t launch_bc2d_transpose(int nvar, double *lam, int ix, int jx,
+                                  const Axis &ax, const Axis &ay,
+                                  const BcTable &bc, cudaStream_t s);
+// J = sum over the interior of |B|^2/(8 pi) dx dy into *J (device), and, if
+// lam is not null, dJ/dP into lam (9 arrays); scratch >= 256 doubles
+cudaError_t launch_adj2d_objective(const double *P, double *lam, double *J,
+                                   double *scratch, int ix, int jx,
+                                   const Axis &ax, const Axis &ay,
+                                   const Phys &ph, cudaStream_t s);
+
 // ---- 1-D ------------------------------------------------------------------
 // The whole 1-D loop (or one fixed-dt step) as one cluster launch, in place
 // on 5 arrays (ro,pr,vx,vy,by) of ix doubles.

@@ -1490,3 +1490,268 @@ extern "C" int cans_run_autotune(cans_run *h, int trial_steps, int *tile) {
   if (tile) *tile = best_tile;
   return CANS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Reverse sweep of the 2-D mlw_m3 run (discrete adjoint) with binomial
+// checkpointing.  The state of step k+1 is BC(step(P_k, dt_k)); dt is the
+// frozen sequence of the forward run.  The run's current state is P_0 and is
+// left unchanged.
+
+namespace {
+
+struct AdjWork {
+  size_t n9 = 0;
+  double *w[2] = {nullptr, nullptr};  // forward ping-pong buffers
+  double *R = nullptr;                // raw output of the recorded step
+  double *lam[2] = {nullptr, nullptr};
+  double *snap = nullptr;             // nsnap states
+  double *scr = nullptr;              // adjoint-kernel scratch
+  double *J = nullptr;                // objective (device)
+  unsigned long long *bits = nullptr;
+  int nsnap = 0;
+  std::vector<void *> owned;
+  ~AdjWork() {
+    for (void *p : owned) cudaFree(p);
+  }
+  int alloc(double **p, size_t nd) {
+    CK(cudaMalloc(p, sizeof(double) * nd));
+    owned.push_back(*p);
+    return CANS_OK;
+  }
+};
+
+bool adj_supported(const cans_run *h) { return h->d.solver == CANS_SOLVER_MLW_M3_2D; }
+
+int adj_setup(cans_run *h, AdjWork &W, int nsnap) {
+  W.n9 = h->n * (size_t)h->nvar;
+  W.nsnap = nsnap;
+  int rc;
+  for (int b = 0; b < 2; b++) {
+    if ((rc = W.alloc(&W.w[b], W.n9))) return rc;
+    if ((rc = W.alloc(&W.lam[b], W.n9))) return rc;
+  }
+  if ((rc = W.alloc(&W.R, W.n9))) return rc;
+  if (nsnap > 0 && (rc = W.alloc(&W.snap, W.n9 * (size_t)nsnap))) return rc;
+  if ((rc = W.alloc(&W.scr, adj2d_scratch_doubles(h->n)))) return rc;
+  if ((rc = W.alloc(&W.J, 1))) return rc;
+  double *b = nullptr;
+  if ((rc = W.alloc(&b, 1))) return rc;
+  W.bits = reinterpret_cast<unsigned long long *>(b);
+  return CANS_OK;
+}
+
+// Advance `steps` steps from the state A (not modified) starting at step k0;
+// the result ends in W.w[*which].
+int adj_advance(cans_run *h, AdjWork &W, const double *A, long long k0,
+                long long steps, const double *dts, int *which,
+                long long *nfwd) {
+  const double *src = A;
+  int cur = 0;
+  for (long long k = 0; k < steps; k++) {
+    double *dst = W.w[cur];
+    CK(step_kernel(h, h->tile, src, dst, dts[k0 + k], nullptr, Box3{}));
+    CK(bc_kernels(h, dst, nullptr));
+    src = dst;
+    cur ^= 1;
+    (*nfwd)++;
+  }
+  *which = steps > 0 ? (cur ^ 1) : -1;
+  return CANS_OK;
+}
+
+// Optimal binomial schedule: F(l, c) = minimal forward steps to reverse l
+// steps from a stored start with c free snapshots (Griewank's treeverse
+// recursion, solved by dynamic programming), and the first split of each.
+struct Plan {
+  int L = 0, C = 0;
+  std::vector<long long> F;
+  std::vector<int> split;
+  long long &f(int l, int c) { return F[(size_t)l * (C + 1) + c]; }
+  int &s(int l, int c) { return split[(size_t)l * (C + 1) + c]; }
+  void build(int L_, int C_) {
+    L = L_;
+    C = C_;
+    F.assign((size_t)(L + 1) * (C + 1), 0);
+    split.assign((size_t)(L + 1) * (C + 1), 0);
+    for (int l = 1; l <= L; l++) f(l, 0) = (long long)l * (l + 1) / 2;
+    for (int c = 1; c <= C; c++) {
+      f(1, c) = 1;
+      for (int l = 2; l <= L; l++) {
+        long long best = -1;
+        int bm = 1;
+        for (int m = 1; m < l; m++) {
+          const long long v = m + f(l - m, c - 1) + f(m, c);
+          if (best < 0 || v < best) {
+            best = v;
+            bm = m;
+          }
+        }
+        f(l, c) = best;
+        s(l, c) = bm;
+      }
+    }
+  }
+};
+
+struct AdjRun {
+  cans_run *h;
+  AdjWork &W;
+  Plan &P;
+  const double *dts;
+  long long L;
+  long long nfwd = 0;
+  bool have_J = false;
+};
+
+// Reverse steps [a, b): on entry W.lam[0] is the adjoint of the filled state
+// b, on exit that of state a.  The state a is in snapshot `slot`.
+int adj_reverse(AdjRun &r, long long a, long long b, int slot, int free_snaps) {
+  cans_run *h = r.h;
+  AdjWork &W = r.W;
+  const size_t n9 = W.n9;
+  const double *Sa = W.snap + n9 * (size_t)slot;
+  const long long l = b - a;
+  if (l == 1) {
+    // record: raw output R of step a
+    CK(step_kernel(h, h->tile, Sa, W.R, r.dts[a], nullptr, Box3{}));
+    r.nfwd++;
+    if (b == r.L && !r.have_J) {  // J and its gradient on the final state
+      CK(launch_adj2d_objective(W.R, W.lam[0], W.J, W.scr, h->d.ix, h->d.jx, h->ax.a,
+                                h->ay.a, h->ph, h->s));
+      r.have_J = true;
+    }
+    CK(launch_bc2d_transpose(h->nvar, W.lam[0], h->d.ix, h->d.jx, h->ax.a, h->ay.a,
+                             h->bc, h->s));
+    CK(launch_adj2d_step(Sa, W.R, W.lam[0], W.lam[1], W.scr, h->d.ix, h->d.jx, h->ax.a,
+                         h->ay.a, h->ph, r.dts[a], h->s));
+    std::swap(W.lam[0], W.lam[1]);
+    return CANS_OK;
+  }
+  if (free_snaps == 0) {  // recompute from a for every step, last first
+    for (long long k = b - 1; k >= a; k--) {
+      if (k == a) {
+        int rc = adj_reverse(r, a, a + 1, slot, 0);
+        if (rc) return rc;
+        break;
+      }
+      // place state k in the scratch slot past the stored ones
+      int which = -1;
+      int rc = adj_advance(h, W, Sa, a, k - a, r.dts, &which, &r.nfwd);
+      if (rc) return rc;
+      const int tmp = W.nsnap - 1;
+      CK(cudaMemcpyAsync(W.snap + n9 * (size_t)tmp, W.w[which], sizeof(double) * n9,
+                         cudaMemcpyDeviceToDevice, h->s));
+      rc = adj_reverse(r, k, k + 1, tmp, 0);
+      if (rc) return rc;
+    }
+    return CANS_OK;
+  }
+  const int m = r.P.s((int)l, free_snaps);
+  int which = -1;
+  int rc = adj_advance(h, W, Sa, a, m, r.dts, &which, &r.nfwd);
+  if (rc) return rc;
+  const int ns = slot + 1;  // snapshots are used as a stack
+  CK(cudaMemcpyAsync(W.snap + n9 * (size_t)ns, W.w[which], sizeof(double) * n9,
+                     cudaMemcpyDeviceToDevice, h->s));
+  if ((rc = adj_reverse(r, a + m, b, ns, free_snaps - 1))) return rc;
+  return adj_reverse(r, a, a + m, slot, free_snaps);
+}
+
+}  // namespace
+
+extern "C" int cans_run_record_dts(cans_run *h, long long nsteps, double safety,
+                                   double *dts, double *J) {
+  if (!h || nsteps < 1 || !dts || !adj_supported(h)) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  AdjWork W;
+  if ((rc = adj_setup(h, W, 0))) return rc;
+  const double *src = h->buf[h->host_ctl.cur];
+  int cur = 0;
+  const unsigned long long init = r4_1e20_bits();
+  for (long long k = 0; k < nsteps; k++) {
+    CK(cudaMemcpyAsync(W.bits, &init, sizeof init, cudaMemcpyHostToDevice, h->s));
+    CK(cfl_full_kernel(h, src, safety, W.bits));
+    unsigned long long out = 0;
+    CK(cudaMemcpyAsync(&out, W.bits, sizeof out, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    dts[k] = bits_to_double(out);
+    CK(step_kernel(h, h->tile, src, W.w[cur], dts[k], nullptr, Box3{}));
+    CK(bc_kernels(h, W.w[cur], nullptr));
+    src = W.w[cur];
+    cur ^= 1;
+  }
+  if (J) {
+    CK(launch_adj2d_objective(src, nullptr, W.J, W.scr, h->d.ix, h->d.jx, h->ax.a,
+                              h->ay.a, h->ph, h->s));
+    CK(cudaMemcpyAsync(J, W.J, sizeof(double), cudaMemcpyDeviceToHost, h->s));
+  }
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_objective(cans_run *h, long long nsteps, const double *dts,
+                                  double *J) {
+  if (!h || nsteps < 1 || !dts || !J || !adj_supported(h)) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  AdjWork W;
+  if ((rc = adj_setup(h, W, 0))) return rc;
+  int which = -1;
+  long long nf = 0;
+  if ((rc = adj_advance(h, W, h->buf[h->host_ctl.cur], 0, nsteps, dts, &which, &nf)))
+    return rc;
+  CK(launch_adj2d_objective(W.w[which], nullptr, W.J, W.scr, h->d.ix, h->d.jx, h->ax.a,
+                            h->ay.a, h->ph, h->s));
+  CK(cudaMemcpyAsync(J, W.J, sizeof(double), cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts,
+                                int nsnap, double *J, double *const *grad,
+                                long long *nfwd) {
+  if (!h || nsteps < 1 || !dts || nsnap < 2 || !adj_supported(h)) return CANS_ERR_ARG;
+  if (nsteps > (1LL << 20)) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  AdjWork W;
+  // nsnap stored states: the start plus nsnap-2 free ones, and one scratch
+  // slot for the no-free-snapshot case
+  if ((rc = adj_setup(h, W, nsnap))) return rc;
+  CK(cudaMemcpyAsync(W.snap, h->buf[h->host_ctl.cur], sizeof(double) * W.n9,
+                     cudaMemcpyDeviceToDevice, h->s));
+  static Plan plan;  // reused while (nsteps, nsnap) repeat
+  const int free_snaps = nsnap - 2;
+  if (plan.L != (int)nsteps || plan.C != free_snaps) plan.build((int)nsteps, free_snaps);
+  AdjRun r{h, W, plan, dts, nsteps};
+  if ((rc = adj_reverse(r, 0, nsteps, 0, free_snaps))) return rc;
+  if (J) CK(cudaMemcpyAsync(J, W.J, sizeof(double), cudaMemcpyDeviceToHost, h->s));
+  if (grad)
+    for (int v = 0; v < h->nvar; v++)
+      if (grad[v])
+        CK(cudaMemcpyAsync(grad[v], W.lam[0] + v * h->n, sizeof(double) * h->n,
+                           cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  if (nfwd) *nfwd = r.nfwd;
+  return CANS_OK;
+}
+
+extern "C" int cans_run_bc_transpose(cans_run *h, double *const *arrays) {
+  if (!h || !arrays || h->ndim != 2) return CANS_ERR_ARG;
+  const size_t n = h->n;
+  double *d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * n * h->nvar));
+  for (int v = 0; v < h->nvar; v++)
+    CK(cudaMemcpyAsync(d + v * n, arrays[v], sizeof(double) * n, cudaMemcpyHostToDevice,
+                       h->s));
+  cudaError_t e = launch_bc2d_transpose(h->nvar, d, h->d.ix, h->d.jx, h->ax.a, h->ay.a,
+                                        h->bc, h->s);
+  for (int v = 0; v < h->nvar && e == cudaSuccess; v++)
+    e = cudaMemcpyAsync(arrays[v], d + v * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                        h->s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail_cuda(e, "cans_run_bc_transpose");
+  return CANS_OK;
+}
