@@ -106,7 +106,185 @@ def extra_workloads(stream, exact=False):
         "us_per_step": best * 1e3 / max(1, st.ns),
         "zone_updates_per_s": 1024 * st.ns / (best * 1e-3), "launches_per_run": 2}
     run.close()
+    # ---- 3-D Roe-MUSCL and HLLD steps on the same turbulence box (margin 3)
+    for solver, safety in (("roe_m_3d", None), ("hlld_3d", 0.2)):
+        out[f"turbulence_256^3_{solver}"] = riemann_3d(stream, solver, safety, exact)
+    out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
+    out["adjoint_shear_256^2_2000_steps"] = adjoint_workload(stream)
+    return out
+
+
+def riemann_3d(stream, solver, safety, exact, iters=10):
+    """Two-stage Riemann-solver step on the 3-D beta = 1 box, 256^3 interior
+    cells + 3 ghost layers: loop iterations timed with events (graph), the
+    four step kernels profiled.  HLLD runs in Heaviside units; its reference
+    driver pairs that state with the CANS-unit cfl_m, which at safety 0.4 is
+    beyond the three-axis stability limit, so it runs at safety 0.2."""
+    import torch
+    from utrip_gb300 import drivers, setups
+    s = setups.turbulence_3d(256, solver=solver)
+    if safety is not None:
+        s["safety"] = safety
+    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    run.push(s["state"])
+    run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+    run.advance(2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run.advance(iters)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    step_ms, _ = run.profile(4)
+    st = run.query()
+    run.close()
+    zones = 256 ** 3
+    return {"zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+            "step_kernels_ms": step_ms / 4, "safety": s["safety"], "bound": "fp64",
+            "steps_done": int(st.nexec), "merr": int(st.merr),
+            "policy": "exact" if exact else "fast"}
+
+
+def hlld_brio_wu(stream, exact):
+    """The HLLD shock tube of md_mhdshktb/hdhlld-x (1024 cells, x only) run to
+    t = 0.1 on the device, graph-replayed."""
+    import torch
+    from utrip_gb300 import drivers, setups
+    s = setups.shock_tube_hlld_1d(1024)
+    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(3):
+        run.push(s["state"])
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run.start(tend=s["tend"], nstop=10 ** 6, safety=s["safety"], dtmin=s["dtmin"])
+        while not run.query().done:
+            run.advance(256)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    st = run.query()
+    run.close()
+    return {"ms_to_tend": best, "steps": int(st.ns), "t": st.t, "merr": int(st.merr),
+            "us_per_step": best * 1e3 / max(1, st.ns)}
+
+
+def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=1e-6):
+    """The differentiation pattern on the 2-D shear layer at beta = 1 (256^2,
+    mlw_m3, 2000 steps, J = final magnetic energy): the reverse sweep with
+    binomial checkpointing in 32 stored states timed against the forward run
+    of the same frozen dt sequence, and its directional derivatives checked
+    against FP64 central differences (h = 1e-6) of the GPU forward on 16
+    seeded directions of the initial vy field and of the CPU oracle on two;
+    dJ/dbeta the same way.  The artificial viscosity switches on where a
+    velocity jump crosses 1e-4 and the shear layer has jumps there, so the
+    check is also reported with qav = 0, where J is smooth."""
+    import torch
+    import oracle
+    from utrip_gb300 import drivers, setups
+
+    def base(beta, qav):
+        s = setups.shear_layer(256, beta=beta, seed=4)
+        s["qav"] = qav
+        oracle.apply_bc_program(s["state"], s["bc"], s["margin"], s)
+        return s
+
+    def objective(s, state, dts):
+        r = drivers.make_run(s, stream=stream.cuda_stream)
+        r.push([np.asfortranarray(a) for a in state])
+        try:
+            return r.objective(dts)
+        finally:
+            r.close()
+
+    def smooth_direction(rng, n, kmax=8):
+        """A seeded random field of unit RMS made of the Fourier modes
+        |k| <= kmax of the periodic box (the perturbation's own scale)."""
+        k = np.fft.fftfreq(n, d=1.0 / n)
+        kr = np.fft.rfftfreq(n, d=1.0 / n)
+        KX, KY = np.meshgrid(k, kr, indexing="ij")
+        mask = (KX ** 2 + KY ** 2) <= kmax ** 2
+        mask[0, 0] = False
+        spec = np.zeros(mask.shape, dtype=np.complex128)
+        spec[mask] = rng.standard_normal(int(mask.sum())) + 1j * rng.standard_normal(int(mask.sum()))
+        f = np.fft.irfft2(spec, s=(n, n))
+        return f / np.sqrt(np.mean(f ** 2))
+
+    def extend(s, d):
+        z = [np.zeros_like(a) for a in s["state"]]
+        z[3][1:-1, 1:-1] = d
+        oracle.apply_bc_program(z, s["bc"], s["margin"], s)
+        return z
+
+    out = {"nsteps": nsteps, "nsnap": nsnap, "h": h,
+           "directions": "seeded unit-RMS fields of the |k| <= 8 Fourier modes of vy"}
+    eps = float(np.finfo(np.float64).eps)
+    for qav in (3.0, 0.0):
+        s = base(1.0, qav)
+        run = drivers.make_run(s, stream=stream.cuda_stream)
+        run.push(s["state"])
+        dts, J = run.record_dts(nsteps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        run.objective(dts)  # warm-up
+        if qav == 3.0:
+            run.adjoint(dts, nsnap=nsnap)  # warm-up (builds the checkpoint schedule)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J_fwd = run.objective(dts)
+        fwd_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        J_adj, grad, nfwd = run.adjoint(dts, nsnap=nsnap)
+        adj_s = time.perf_counter() - t0
+        if qav == 3.0:  # the same reverse sweep with every state stored
+            run.adjoint(dts, nsnap=nsteps + 1)
+            t0 = time.perf_counter()
+            _, g_all, nfwd_all = run.adjoint(dts, nsnap=nsteps + 1)
+            out["store_all_states"] = {
+                "adjoint_s": time.perf_counter() - t0, "forward_steps_in_adjoint": int(nfwd_all),
+                "grad_equal_to_checkpointed": all(np.array_equal(a, b)
+                                                  for a, b in zip(g_all, grad))}
+        run.close()
+        rng = np.random.default_rng(5)
+        rel, within = [], 0
+        for k in range(ndir):
+            d = smooth_direction(rng, 256)
+            z = extend(s, d)
+            ad = sum(float(np.sum(g * e)) for g, e in zip(grad, z))
+            jp = objective(s, [a + h * b for a, b in zip(s["state"], z)], dts)
+            jm = objective(s, [a - h * b for a, b in zip(s["state"], z)], dts)
+            fd = (jp - jm) / (2 * h)
+            rel.append(abs(ad - fd) / abs(fd))
+            within += abs(ad - fd) <= 1e-6 * abs(fd) + 8 * eps * abs(J) / (2 * h)
+            if k < n_oracle_dirs and qav == 3.0:
+                def oracle_J(st):
+                    st = [np.asfortranarray(a) for a in st]
+                    for dt in dts:
+                        oracle.step_2d(s, st, dt)
+                        oracle.apply_bc_program(st, s["bc"], s["margin"], s)
+                    w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
+                    e = (st[5] ** 2 + st[6] ** 2 + st[7] ** 2)[1:-1, 1:-1]
+                    return float(np.sum(e * w)) / np.pi / 8.0
+                ojp = oracle_J([a + h * b for a, b in zip(s["state"], z)])
+                ojm = oracle_J([a - h * b for a, b in zip(s["state"], z)])
+                out.setdefault("oracle_fd_rel_err", []).append(abs(ad - (ojp - ojm) / (2 * h))
+                                                               / abs((ojp - ojm) / (2 * h)))
+        dbeta = 0.625 * float(np.sum(grad[1]))
+        jb = [objective(sb, sb["state"], dts) for sb in (base(1.0 + h, qav), base(1.0 - h, qav))]
+        fdb = (jb[0] - jb[1]) / (2 * h)
+        out[f"qav{qav:g}"] = {
+            "J": J, "J_replay_equal": J_fwd == J and J_adj == J,
+            "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
+            "forward_steps_in_adjoint": int(nfwd),
+            "fd_rel_err_max": max(rel), "fd_rel_err_median": float(np.median(rel)),
+            "fd_within_1e-6": f"{within}/{ndir}",
+            "dJ_dbeta": dbeta, "dJ_dbeta_fd": fdb, "dJ_dbeta_rel_err": abs(dbeta - fdb) / abs(fdb)}
+    if "store_all_states" in out:
+        out["store_all_states"]["adjoint_over_forward"] = (out["store_all_states"]["adjoint_s"]
+                                                           / out["qav3"]["forward_s"])
     return out
 
 
