@@ -49,7 +49,48 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary 3-D and 1-D workloads")
+    p.add_argument("--profile-case", default=None,
+                   choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch"],
+                   help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
+
+
+def profile_case(case, n):
+    """A small fixed case of one secondary path: a few device iterations of
+    the 3-D steps on an n^3 box, 20 reverse steps of the 2-D adjoint on n^2,
+    or 5 batched iterations of 8 shear layers; prints one JSON line."""
+    import torch
+    from utrip_gb300 import capi, drivers, setups
+    if case in ("mlw3d", "roe3d", "hlld3d"):
+        solver = {"mlw3d": "mlw_m_3d", "roe3d": "roe_m_3d", "hlld3d": "hlld_3d"}[case]
+        s = setups.turbulence_3d(n, solver=solver)
+        run = drivers.make_run(s)
+        run.push(s["state"])
+        run.start(nstop=3, safety=0.2, dtmin=1e-10)
+        run.advance(3)
+        st = run.query()
+        run.close()
+        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+    elif case == "adjoint2d":
+        s = setups.shear_layer(n, beta=1.0, seed=4)
+        run = drivers.make_run(s)
+        run.push(s["state"])
+        dts, J = run.record_dts(20)
+        J2, _, nf = run.adjoint(dts, nsnap=4)
+        run.close()
+        out = {"case": case, "n": n, "steps": 20, "J": J, "J_equal": J == J2, "nfwd": nf}
+    else:
+        runs = [setups.shear_layer(m, beta=b, seed=k) for k, (m, b) in
+                enumerate(zip([n, n // 2, n, n // 2] * 2, [0.2, 0.5, 1.0, 2.0] * 2))]
+        b = capi.Batch(runs)
+        for g, r in enumerate(runs):
+            b.push(g, r["state"])
+        b.start(nstop=5, safety=0.4, dtmin=1e-10)
+        b.advance(5)
+        out = {"case": case, "n": n, "runs": len(runs), "done": bool(b.query(0).done)}
+        b.close()
+    torch.cuda.synchronize()
+    print(json.dumps(out))
 
 
 def extra_workloads(stream, exact=False):
@@ -632,6 +673,9 @@ def run_ours(args, ws, rank, local):
 
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case, args.n)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
