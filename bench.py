@@ -142,10 +142,17 @@ def extra_workloads(stream, exact=False):
         ms = e0.elapsed_time(e1)
         best = ms if best is None else min(best, ms)
     st = run.query()
+    got = run.pull()
+    import oracle
+    ref = setups.copy_state(s1)
+    t_ref, ns_ref, _, _ = oracle.run_1d(s1, ref, 10 ** 6)
     out["shock_tube_1024_to_t0.1_mlw_m_1d"] = {
         "ms_to_tend": best, "steps": int(st.ns), "t": st.t, "merr": int(st.merr),
         "us_per_step": best * 1e3 / max(1, st.ns),
-        "zone_updates_per_s": 1024 * st.ns / (best * 1e-3), "launches_per_run": 2}
+        "zone_updates_per_s": 1024 * st.ns / (best * 1e-3), "launches_per_run": 2,
+        "oracle_steps": int(ns_ref),
+        "rel_linf_vs_oracle": {k: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+                               for k, a, b in zip(s1["names"], got, ref)}}
     run.close()
     # ---- 3-D Roe-MUSCL and HLLD steps on the same turbulence box (margin 3)
     for solver, safety in (("roe_m_3d", None), ("hlld_3d", 0.2)):
@@ -185,7 +192,29 @@ def riemann_3d(stream, solver, safety, exact, iters=10):
     return {"zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
             "step_kernels_ms": step_ms / 4, "safety": s["safety"], "bound": "fp64",
             "steps_done": int(st.nexec), "merr": int(st.merr),
-            "policy": "exact" if exact else "fast"}
+            "policy": "exact" if exact else "fast",
+            "cpu_oracle": cpu_sample_3d(solver, safety)}
+
+
+def cpu_sample_3d(solver, safety, n=96, steps=2):
+    """The CPU restatement of the reference step (the oracle, OpenMP over
+    every host thread) on a bounded sample of the same workload: the 96^3
+    turbulence box, one untimed step, then `steps` timed loop iterations."""
+    import oracle
+    from utrip_gb300 import setups
+    s = setups.turbulence_3d(n, solver=solver)
+    st = setups.copy_state(s)
+    sf = safety if safety is not None else s["safety"]
+    dt, _ = oracle.cfl_3d(s, st, sf)
+    oracle.step_3d(s, st, dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt, _ = oracle.cfl_3d(s, st, sf)
+        oracle.step_3d(s, st, dt)
+        oracle.apply_bc_program_3d(st, s["bc"], s["margin"], s)
+    el = time.perf_counter() - t0
+    return {"zone_updates_per_s": n ** 3 * steps / el, "cores": oracle.get_threads(),
+            "kind": "port", "sample": f"{steps} loop iterations of the {n}^3 box in {el:.2f} s"}
 
 
 def hlld_brio_wu(stream, exact):
@@ -394,6 +423,49 @@ def beta_sweep(stream, exact=False, nsteps=1000):
             "batched_zone_updates_per_s": zones / (batched_ms * 1e-3),
             "all_runs_completed": bool(done),
             "max_rel_diff_batched_vs_single": diff}
+
+
+def parity_check(n, stream, nsteps=100):
+    """The headline workload checked against the CPU oracle: 100 loop
+    iterations of Orszag-Tang n^2 from the same initial state, relative
+    L-infinity per variable of the fast policy and the number of cells that
+    differ in the exact policy; and the drift of the conserved totals (mass,
+    momentum, total energy, B) over the same run in the periodic box."""
+    import oracle
+    from utrip_gb300 import drivers, setups
+    s = setups.orszag_tang(n)
+    ref = setups.copy_state(s)
+    oracle.run_2d(s, ref, nsteps)
+    out = {"steps": nsteps}
+    for exact in (False, True):
+        got = setups.copy_state(s)
+        run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+        drivers.run_resident(s, got, nsteps, exact=exact, run=run)
+        run.close()
+        if exact:
+            out["exact_cells_differing"] = int(sum(int(np.sum(a != b)) for a, b in zip(got, ref)))
+        else:
+            # relative to the field's largest value; absolute for a field that
+            # is zero everywhere (vz, bz of this 2-D problem)
+            out["fast_rel_linf"] = {k: float(np.max(np.abs(a - b)) / (np.max(np.abs(b)) or 1.0))
+                                    for k, a, b in zip(s["names"], got, ref)}
+            fast = got
+
+    def totals(st):
+        ro, pr, vx, vy, vz, bx, by, bz = st[:8]
+        w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
+        inner = (slice(1, -1), slice(1, -1))
+        ee = pr / (s["gm"] - 1) + 0.5 * ro * (vx ** 2 + vy ** 2 + vz ** 2) + \
+            (bx ** 2 + by ** 2 + bz ** 2) / (8 * np.pi)
+        q = {"mass": ro, "energy": ee, "momentum_x": ro * vx, "momentum_y": ro * vy,
+             "bx": bx, "by": by}
+        return {k: float(np.sum(a[inner] * w)) for k, a in q.items()}
+    t0, t1 = totals(s["state"]), totals(fast)
+    out["conservation_drift"] = {k: (t1[k] - t0[k]) / max(abs(t0[k]), 1e-300) if abs(t0[k]) > 1e-12
+                                 else t1[k] - t0[k] for k in t0}
+    out["conservation_note"] = ("relative change of the interior totals over the run; "
+                                "absolute change where the total is zero")
+    return out
 
 
 def dist_setup():
@@ -639,6 +711,7 @@ def run_ours(args, ws, rank, local):
     e2e_val = n * n * m * e2e_steps * ws / (e2e_ms * 1e-3)
     nbytes = run.nvar * (n + 2) * (n + 2) * 8
     run.close()
+    parity = parity_check(n, stream) if rank == 0 and not args.no_extras else None
     extras = None if args.no_extras else extra_workloads(stream, exact=args.exact)
 
     if rank != 0:
@@ -664,6 +737,8 @@ def run_ours(args, ws, rank, local):
         "wall_s": wall,
         "clocks": clk.summary(),
     }
+    if parity is not None:
+        line["parity_vs_oracle"] = parity
     if extras is not None:
         line["workloads"] = extras
     if not args.no_cpu_baseline:

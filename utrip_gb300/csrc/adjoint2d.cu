@@ -366,58 +366,60 @@ __global__ void __launch_bounds__(kT)
     qyp = ph.qav * ay.dm[j] * (e > 0.0 ? e : 0.0);
     gyp = e > 0.0 ? ph.qav * ay.dm[j] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
   }
+  // coefficients shared by the 8 variables: viscosity in U (mlwartv.f),
+  // half-step differences (mlwhalf.f part 1), corner predictor (part 2),
+  // viscosity in q; zero where the reading cell is not updated
+  const double cxm = in_xm ? dt * ax.di[i - 1] * qxm * ax.dim[i - 1] : 0.0;
+  const double cxp = in_xp ? dt * ax.di[i + 1] * qxp * ax.dim[i] : 0.0;
+  const double cym = in_ym ? dt * ay.di[j - 1] * qym * ay.dim[j - 1] : 0.0;
+  const double cyp = in_yp ? dt * ay.di[j + 1] * qyp * ay.dim[j] : 0.0;
+  const double c0 =
+      in_c ? dt * (ax.di[i] * (qxp * ax.dim[i] + qxm * ax.dim[i - 1]) +
+                   ay.di[j] * (qyp * ay.dim[j] + qym * ay.dim[j - 1]))
+           : 0.0;
+  const bool av = (qxm != 0.0) | (qxp != 0.0) | (qym != 0.0) | (qyp != 0.0);
+  const double hxm = i >= 1 ? 0.25 * dt * ax.di[i - 1] : 0.0;
+  const double hxp = i <= g.ix - 2 ? 0.25 * dt * ax.di[i + 1] : 0.0;
+  const double hym = j >= 1 ? 0.25 * dt * ay.di[j - 1] : 0.0;
+  const double hyp = j <= g.jx - 2 ? 0.25 * dt * ay.di[j + 1] : 0.0;
+  const double pxm = i >= 1 ? 0.5 * dt * ax.dim[i - 1] : 0.0;
+  const double pxp = i <= g.ix - 2 ? 0.5 * dt * ax.dim[i] : 0.0;
+  const double pym = j >= 1 ? 0.5 * dt * ay.dim[j - 1] : 0.0;
+  const double pyp = j <= g.jx - 2 ? 0.5 * dt * ay.dim[j] : 0.0;
+  // d(du(o))/dq(face) per unit dU: the cell below the face gains, the cell
+  // above loses (in_* already folded in)
+  const double wxm_a = in_xm ? dt * ax.dim[i - 1] * ax.di[i - 1] : 0.0;
+  const double wxm_b = (in_c && i >= 1) ? dt * ax.dim[i - 1] * ax.di[i] : 0.0;
+  const double wxp_a = in_c ? dt * ax.dim[i] * ax.di[i] : 0.0;
+  const double wxp_b = in_xp ? dt * ax.dim[i] * ax.di[i + 1] : 0.0;
+  const double wym_a = in_ym ? dt * ay.dim[j - 1] * ay.di[j - 1] : 0.0;
+  const double wym_b = (in_c && j >= 1) ? dt * ay.dim[j - 1] * ay.di[j] : 0.0;
+  const double wyp_a = in_c ? dt * ay.dim[j] * ay.di[j] : 0.0;
+  const double wyp_b = in_yp ? dt * ay.dim[j] * ay.di[j + 1] : 0.0;
   double aU[8], aX[8], aY[8];
   double aqxm = 0, aqxp = 0, aqym = 0, aqyp = 0;
 #pragma unroll
   for (int v = 0; v < 8; v++) {
-    const double *a = A1 + v * n, *h = A2 + v * n, *U = CU + v * n;
+    const double *a = A1 + v * n, *h = A2 + v * n;
     const double l0 = in_c ? a[c] : 0.0;
     const double lxm = in_xm ? a[c - sx] : 0.0, lxp = in_xp ? a[c + sx] : 0.0;
     const double lym = in_ym ? a[c - sy] : 0.0, lyp = in_yp ? a[c + sy] : 0.0;
-    // U' = U + du on the interior
-    double au = l0;
-    // viscosity, linear in U (mlwartv.f)
-    if (in_c)
-      au -= dt * (ax.di[i] * (qxp * ax.dim[i] + (i >= 1 ? qxm * ax.dim[i - 1] : 0.0)) +
-                  ay.di[j] * (qyp * ay.dim[j] + (j >= 1 ? qym * ay.dim[j - 1] : 0.0))) * l0;
-    if (in_xm) au += dt * ax.di[i - 1] * qxm * ax.dim[i - 1] * lxm;
-    if (in_xp) au += dt * ax.di[i + 1] * qxp * ax.dim[i] * lxp;
-    if (in_ym) au += dt * ay.di[j - 1] * qym * ay.dim[j - 1] * lym;
-    if (in_yp) au += dt * ay.di[j + 1] * qyp * ay.dim[j] * lyp;
-    // corner predictor: 0.25 of each surrounding corner
-    double hmm = k_mm ? h[c - sx - sy] : 0.0, hpm = k_pm ? h[c - sy] : 0.0;
-    double hmp = k_mp ? h[c - sx] : 0.0, hpp = k_pp ? h[c] : 0.0;
-    au += 0.25 * (hmm + hpm + hmp + hpp);
+    const double hmm = k_mm ? h[c - sx - sy] : 0.0, hpm = k_pm ? h[c - sy] : 0.0;
+    const double hmp = k_mp ? h[c - sx] : 0.0, hpp = k_pp ? h[c] : 0.0;
+    const double ylo = hmm + hpm, yhi = hmp + hpp;  // corners below / above
+    // U' = U + du on the interior; 0.25 of each surrounding corner
+    double au = fma(0.25, ylo + yhi, l0);
+    if (av) au += cxm * lxm + cxp * lxp + cym * lym + cyp * lyp - c0 * l0;
     aU[v] = au;
-    // half-step central differences (mlwhalf.f part 1)
-    double axv = 0.0, ayv = 0.0;
-    if (in_xm) axv -= 0.25 * dt * ax.di[i - 1] * lxm;
-    if (in_xp) axv += 0.25 * dt * ax.di[i + 1] * lxp;
-    if (in_ym) ayv -= 0.25 * dt * ay.di[j - 1] * lym;
-    if (in_yp) ayv += 0.25 * dt * ay.di[j + 1] * lyp;
-    // corner predictor: -dt dxim (FX(p+1)-FX(p) ...)/2, -dt dyim (...)/2
-    if (i >= 1) axv -= 0.5 * dt * ax.dim[i - 1] * (hmm + hmp);
-    if (i <= g.ix - 2) axv += 0.5 * dt * ax.dim[i] * (hpm + hpp);
-    if (j >= 1) ayv -= 0.5 * dt * ay.dim[j - 1] * (hmm + hpm);
-    if (j <= g.jx - 2) ayv += 0.5 * dt * ay.dim[j] * (hmp + hpp);
-    aX[v] = axv;
-    aY[v] = ayv;
-    // adjoint of the face coefficients q (viscosity, linear in q)
-    if (i >= 1) {
-      const double dU = U[c] - U[c - sx];
-      aqxm += dt * ax.dim[i - 1] * dU * ((in_xm ? ax.di[i - 1] * lxm : 0.0) - (in_c ? ax.di[i] * l0 : 0.0));
-    }
-    if (i <= g.ix - 2) {
-      const double dU = U[c + sx] - U[c];
-      aqxp += dt * ax.dim[i] * dU * ((in_c ? ax.di[i] * l0 : 0.0) - (in_xp ? ax.di[i + 1] * lxp : 0.0));
-    }
-    if (j >= 1) {
-      const double dU = U[c] - U[c - sy];
-      aqym += dt * ay.dim[j - 1] * dU * ((in_ym ? ay.di[j - 1] * lym : 0.0) - (in_c ? ay.di[j] * l0 : 0.0));
-    }
-    if (j <= g.jx - 2) {
-      const double dU = U[c + sy] - U[c];
-      aqyp += dt * ay.dim[j] * dU * ((in_c ? ay.di[j] * l0 : 0.0) - (in_yp ? ay.di[j + 1] * lyp : 0.0));
+    aX[v] = hxp * lxp - hxm * lxm + pxp * (hpm + hpp) - pxm * (hmm + hmp);
+    aY[v] = hyp * lyp - hym * lym + pyp * yhi - pym * ylo;
+    if (av) {
+      const double *U = CU + v * n;
+      const double u0 = U[c];
+      if (qxm != 0.0) aqxm += (u0 - U[c - sx]) * (wxm_a * lxm - wxm_b * l0);
+      if (qxp != 0.0) aqxp += (U[c + sx] - u0) * (wxp_a * l0 - wxp_b * lxp);
+      if (qym != 0.0) aqym += (u0 - U[c - sy]) * (wym_a * lym - wym_b * l0);
+      if (qyp != 0.0) aqyp += (U[c + sy] - u0) * (wyp_a * l0 - wyp_b * lyp);
     }
   }
   double ap[8] = {0, 0, 0, 0, 0, 0, 0, 0};

@@ -413,13 +413,41 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
 // Smallest grid the 1-D loop kernel accepts (one block of 4 interior cells).
 int mlw1d_min_cells() { return 6; }
 
-// Cluster size for ix cells: up to 8 blocks (the portable cluster limit),
-// each owning at least 4 interior cells so a face rule of margin <= 3 stays
-// inside its block.
-static int cluster_for(int ix) {
-  int cs = 8;
+// Cluster size for ix cells: up to `cmax` blocks, each owning at least 4
+// interior cells so a face rule of margin <= 3 stays inside its block.  The
+// step is FP64-bound even at 10^3 cells (2 FP64 lanes per SM), so more SMs
+// per cluster shorten every step.
+static int cluster_for(int ix, int cmax) {
+  int cs = cmax;
   while (cs > 1 && (ix - 2) / cs < 4) cs >>= 1;
   return cs;
+}
+
+// Largest cluster the device co-schedules for this kernel: 16 blocks where
+// non-portable cluster sizes are available, else the portable 8.
+static int cluster_max(void (*kern)(Run1D), size_t smem) {
+  static int cached = 0;
+  if (cached) return cached;
+  int best = 8;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+      cudaSuccess) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(16, 1, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) == cudaSuccess && n > 0) best = 16;
+  }
+  cudaGetLastError();  // a refused query leaves no error behind
+  cached = best;
+  return best;
 }
 
 // Host launcher: the cluster kernel over a state of 5 arrays of ix doubles,
@@ -430,7 +458,11 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          int max_steps, int fixed, double dt_fixed, int start,
                          cudaStream_t s) {
   if (ix < mlw1d_min_cells()) return cudaErrorInvalidValue;
-  const int CS = cluster_for(ix);
+  void (*kern)(Run1D) = exact ? k_mlw1d<true> : k_mlw1d<false>;
+  // shared memory of the largest block the grid can have (16 blocks)
+  const size_t smem_probe =
+      sizeof(double) * ((size_t)(2 * NV1 + 3 * NV1 + 1) * ((ix - 2) / 16 + 4) + 32 + 32);
+  const int CS = cluster_for(ix, cluster_max(kern, smem_probe));
   Run1D p{};
   p.S = S; p.bx = bx; p.bxm = bxm; p.ax = ax; p.ph = ph; p.bc = bc; p.ctl = ctl;
   p.ix = ix;
@@ -445,10 +477,13 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
   if (p.q < bc.margin + 1) return cudaErrorInvalidValue;
   const size_t smem = sizeof(double) * ((size_t)(2 * NV1 + 3 * NV1 + 1) * p.lmax + 2 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  void (*kern)(Run1D) = exact ? k_mlw1d<true> : k_mlw1d<false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
+  if (CS > 8) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(CS, 1, 1);
   cfg.blockDim = dim3(256, 1, 1);
