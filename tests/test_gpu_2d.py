@@ -120,12 +120,16 @@ def test_literal_drop_in_loop_matches_oracle(gpu, oracle_lib):
         assert_same(s["names"], got, ref, f"literal resident={resident}")
 
 
-def test_all_tiles_agree_bitwise(gpu, oracle_lib):
-    s = setups.random_state(150, 77, seed=4)
+N_TILES_2D = 6  # 32x16, 32x8, 16x16, 64x8, 32x9 (one row per thread), 32x10
+
+
+@pytest.mark.parametrize("solver", ["mlw_m3", "mlw_m"])
+def test_all_tiles_agree_bitwise(gpu, oracle_lib, solver):
+    s = setups.random_state(150, 77, seed=4, solver=solver)
     ref = setups.copy_state(s)
     dt, _ = oracle.cfl_2d(s, ref, 0.4)
     oracle.step_2d(s, ref, dt)
-    for tile in range(4):
+    for tile in range(N_TILES_2D):
         run = drivers.make_run(s, exact=True, tile=tile)
         try:
             run.push(setups.copy_state(s))

@@ -59,16 +59,21 @@ template <bool E, bool M3>
 cudaError_t launch_sel(int tile, const double *A, double *B, int ix, int jx,
                        const Axis &ax, const Axis &ay, const Phys &ph,
                        double dt, Ctl *ctl, Box3 box, cudaStream_t s) {
+  // 32 x 9 and 32 x 10 give tile counts that fill whole waves of two blocks
+  // per SM on grids where 32 x 8 leaves a partly empty last wave (512^2:
+  // 1024 tiles = 3.4 waves of 304 blocks, 32 x 9: 912 = 3.0 waves)
   switch (tile) {
     case 1: return launch_tile<E, M3, 32, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 2: return launch_tile<E, M3, 16, 16>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 3: return launch_tile<E, M3, 64, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 4: return launch_tile<E, M3, 32, 9, 1>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 5: return launch_tile<E, M3, 32, 10>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     default: return launch_tile<E, M3, 32, 16>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
   }
 }
 }  // namespace
 
-int mlw2d_tile_count() { return 4; }
+int mlw2d_tile_count() { return 6; }
 
 cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
                          double *B, int ix, int jx, const Axis &ax,
