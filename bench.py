@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--mlw-steps", type=int, default=100)
     p.add_argument("--n", type=int, default=N_CELLS)
     p.add_argument("--exact", action="store_true", help="exact arithmetic policy")
+    p.add_argument("--tile", type=int, default=-1,
+                   help="2-D tile configuration (default: autotuned)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary 3-D and 1-D workloads")
@@ -640,9 +642,9 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     assert stream.cuda_stream != 0
-    run = drivers.make_run(s, exact=args.exact, stream=stream.cuda_stream)
+    run = drivers.make_run(s, exact=args.exact, stream=stream.cuda_stream, tile=args.tile)
     run.push(setups.copy_state(s))
-    tile = run.autotune(5)
+    tile = run.autotune(5) if args.tile < 0 else args.tile
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     m = args.mlw_steps
     total_iters = (args.warmup + args.steps) * m
