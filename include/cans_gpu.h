@@ -148,6 +148,20 @@ int cans_cfl_m_1d(double *dt, const double *safety, const double *dtmin,
                   const double *ro, const double *pr, const double *vx,
                   const double *vy, const double *by, const double *dx,
                   const int *ix);
+/* replaces subroutine mlw_m_bg (cans1d/hdmlw/mlw_m_bg.f:2-3): mLW step
+ * with gravity gx/gxm, flux-tube cross section sc/scm (gradients dsc/dscm)
+ * and distance from the rotation axis rr/rrm (gradients drr/drrm) */
+int cans_mlw_m_bg(double *ro, double *pr, double *vx, double *vy, double *by,
+                  const double *bx, const double *bxm, const double *dt,
+                  const double *qav, const double *gm, const double *gx,
+                  const double *gxm, const double *sc, const double *dsc,
+                  const double *scm, const double *dscm, const double *rr,
+                  const double *rrm, const double *drr, const double *drrm,
+                  const double *dx, const double *dxm, const int *ix);
+/* replaces subroutine chkdav  (cans1d/common/chkdav.f:2): da below floor is
+ * raised to it and vx set to zero there; n_events receives the count */
+int cans_chkdav(int *n_events, double *da, double *vx, const double *floor,
+                const int *ix);
 /* Ghost-cell fill, 1-D (cans1d/bc/bd*.f:2). */
 int cans_bdperx_1d(const int *margin0, const int *margin1, double *qq, const int *ix); /* bdperx.f:2 */
 int cans_bdsppx_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdsppx.f:2 */
@@ -248,6 +262,8 @@ int cans_gpu_release(const double *any);
 #define CANS_SOLVER_MLW_M_1D 3   /* mlw_m  1-D: ro,pr,vx,vy,by (+ bx, bxm)   */
 #define CANS_SOLVER_ROE_M_3D 4   /* roe_m  3-D: ro,pr,vx,vy,vz,bx,by,bz      */
 #define CANS_SOLVER_HLLD_3D 5    /* HLLD engine: ro,pr,vx,vy,vz,bx,by,bz     */
+#define CANS_SOLVER_MLW_M_BG_1D 6 /* mlw_m_bg 1-D: ro,pr,vx,vy,by (+ bx, bxm
+                                    and the ten gravity / flux-tube profiles) */
 
 /* Boundary kinds, one per reference bd* family. */
 #define CANS_BD_NONE (-1)
@@ -277,6 +293,22 @@ typedef struct {
   double mu;                  /* HLLD: permeability (0 = 1)                 */
   int mfdim[3];               /* HLLD: active axes; all 0 = every axis with
                                  an extent > 1                              */
+  /* mlw_m_bg (CANS_SOLVER_MLW_M_BG_1D): the static profiles of
+   * cans1d/hdmlw/mlw_m_bg.f:2-3, ix doubles each (gravity, cross section,
+   * distance from the rotation axis and their gradients) */
+  const double *gx, *gxm, *sc, *scm, *dsc, *dscm, *rr, *rrm, *drr, *drrm;
+  /* 1-D loops: chkdav (cans1d/common/chkdav.f:2) of ro, then pr, with
+   * `floor` after every boundary fill when chkdav = 1; the events are
+   * counted in cans_run_state.n_floor */
+  int chkdav;
+  double floor;
+  /* mlw_m_bg loops: the random torque source of the spicule model
+   * (cans1d/md_spicule/hdmlw/trqalfven.f:2) after every step when trq (the
+   * profile tanh((x-0.75)/0.075)-1, ix doubles) is not NULL; amplitude trq0,
+   * random stream keyed by seed */
+  const double *trq;
+  double trq0;
+  unsigned long long seed;
 } cans_run_desc;
 
 typedef struct {
@@ -286,6 +318,7 @@ typedef struct {
   int merr;                   /* 0 or 9001                                  */
   int done;                   /* 1 when tend/nstop/merr ended the loop      */
   int pause;                  /* 1 when an output time was crossed          */
+  long long n_floor;          /* chkdav events since cans_run_start         */
 } cans_run_state;
 
 int cans_run_create(cans_run **h, const cans_run_desc *d);

@@ -55,6 +55,17 @@ def load():
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
         lib.oracle_hlld_engine_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, i, _dp, i, _dp, i, _ip]
+        lib.oracle_mlw_m_bg_1d.argtypes = [_dp] * 7 + [d, d, d] + [_dp] * 12 + [i]
+        lib.oracle_chkdav.argtypes = [_dp, _dp, d, i]
+        lib.oracle_chkdav.restype = i
+        lib.oracle_torque_uniform.argtypes = [C.c_ulonglong, C.c_longlong, i, i]
+        lib.oracle_torque_uniform.restype = d
+        lib.oracle_trqalfven.argtypes = [_dp, d, _dp, _dp, d, C.c_ulonglong, C.c_longlong, i]
+        lib.oracle_spicule_run.argtypes = ([_dp] * 7 + [d, d] + [_dp] * 13 +
+                                           [d, C.c_ulonglong, i, d, i, _ip, i, d, d,
+                                            C.c_longlong, d, d, C.c_longlong, i, _dp,
+                                            C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)])
+        lib.oracle_spicule_run.restype = i
         lib.oracle_set_threads.argtypes = [i]
         lib.oracle_get_threads.restype = i
         _lib = lib
@@ -203,6 +214,89 @@ def run_1d(setup, state, nstop, tend=None, safety=None, t0=0.0):
         apply_bc_program_1d(state, setup["bc"], setup["margin"], setup)
         if not (ns < nstop and t < tend):
             return t, ns, 0, dts
+
+
+def mlw_m_bg(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, gx, gxm, sc, dsc, scm, dscm,
+             rr, rrm, drr, drrm, dx, dxm):
+    """cans1d/hdmlw/mlw_m_bg.f:2 (argument order of the reference)."""
+    load().oracle_mlw_m_bg_1d(*[P(a) for a in (ro, pr, vx, vy, by, bx, bxm)], dt, qav, gm,
+                              *[P(a) for a in (gx, gxm, sc, dsc, scm, dscm, rr, rrm, drr,
+                                               drrm, dx, dxm)], ro.size)
+
+
+def chkdav(da, vx, floor):
+    """cans1d/common/chkdav.f:2; returns n_events."""
+    return int(load().oracle_chkdav(P(da), P(vx), floor, da.size))
+
+
+def torque_uniform(seed, ns, g, ix):
+    return float(load().oracle_torque_uniform(seed, ns, g, ix))
+
+
+def trqalfven(vy, dt, trq, rr, trq0, seed, ns):
+    load().oracle_trqalfven(P(vy), dt, P(trq), P(rr), trq0, seed, ns, vy.size)
+
+
+def step_bg(setup, state, dt):
+    s = setup
+    mlw_m_bg(*state, s["bx"], s["bxm"], dt, s["qav"], s["gm"], s["gx"], s["gxm"], s["sc"],
+             s["dsc"], s["scm"], s["dscm"], s["rr"], s["rrm"], s["drr"], s["drrm"], s["dx"],
+             s["dxm"])
+
+
+def run_spicule_c(setup, state, nstop, tend=None, safety=None, t0=0.0, ns0=0, torque=True,
+                  floor=True):
+    """run_spicule without output pauses, the whole loop in C.  Returns
+    (t, ns, merr, n_floor_events)."""
+    s = setup
+    tend = s.get("tend", 1e30) if tend is None else tend
+    safety = s["safety"] if safety is None else safety
+    kind = np.full(10, -1, dtype=np.int32)
+    for var, face, k, q0 in s["bc"]:
+        if q0 != 0.0 or k in (BD_CNS, BD_FRD, BD_PER):
+            raise ValueError("the C loop takes the zero-constant bd kinds only")
+        kind[2 * var + face] = k
+    t, ns, nev = C.c_double(), C.c_longlong(), C.c_longlong()
+    merr = load().oracle_spicule_run(
+        *[P(a) for a in state], P(s["bx"]), P(s["bxm"]), s["qav"], s["gm"],
+        *[P(s[k]) for k in ("gx", "gxm", "sc", "dsc", "scm", "dscm", "rr", "rrm", "drr",
+                             "drrm", "dx", "dxm", "trq")],
+        s["trq0"], s["seed"], 1 if torque else 0, s["floor"], 1 if floor else 0,
+        kind.ctypes.data_as(_ip), s["margin"], safety, s["dtmin"], nstop, tend, t0, ns0,
+        state[0].size, C.byref(t), C.byref(ns), C.byref(nev))
+    return t.value, ns.value, int(merr), nev.value
+
+
+def run_spicule(setup, state, nstop, tend=None, safety=None, t0=0.0, ns0=0, torque=True,
+                floor=True, on_output=None):
+    """The spicule loop (cans1d/md_spicule/hdmlw/main.f:160-219): cfl_m,
+    t += dt, mlw_m_bg, trqalfven, bnd, chkdav of ro then pr, the output test
+    (on_output(ns, t) when int(tp/dtout) < int(t/dtout)) and the loop test.
+    Returns (t, ns, merr, dts, n_floor_events)."""
+    s = setup
+    tend = s.get("tend", 1e30) if tend is None else tend
+    safety = s["safety"] if safety is None else safety
+    fl = s["floor"] if floor else None
+    t, ns, dts, nev = t0, ns0, [], 0
+    while True:
+        ns += 1
+        dt, merr = cfl_m_1d(safety, s["dtmin"], s["gm"], s["bx"], *state, s["dx"])
+        if merr:
+            return t, ns, merr, dts, nev
+        tp = t
+        t = t + dt
+        dts.append(dt)
+        step_bg(s, state, dt)
+        if torque:
+            trqalfven(state[3], dt, s["trq"], s["rr"], s["trq0"], s["seed"], ns)
+        apply_bc_program_1d(state, s["bc"], s["margin"], s)
+        if fl is not None:
+            nev += chkdav(state[0], state[2], fl)
+            nev += chkdav(state[1], state[2], fl)
+        if on_output is not None and s.get("dtout", 0) > 0 and int(tp / s["dtout"]) < int(t / s["dtout"]):
+            on_output(ns, t)
+        if not (ns < nstop and t < tend):
+            return t, ns, 0, dts, nev
 
 
 def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):

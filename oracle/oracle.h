@@ -51,6 +51,32 @@ void oracle_cfl_m_1d(double *dt, double safety, double dtmin, int *merr,
                      const double *by, const double *dx, int ix);
 void oracle_bd_1d(int kind, int mbnd, int margin, double *qq, double q0,
                   const double *dxm, int ix);
+/* mlw_m_bg (cans1d/hdmlw/mlw_m_bg.f:2): gravity, flux-tube cross section and
+ * rotation; chkdav (cans1d/common/chkdav.f:2) returns the event count;
+ * trqalfven (cans1d/md_spicule/hdmlw/trqalfven.f:2) with a counter-based
+ * random stream in place of random_number (see mlw1d_bg.c). */
+void oracle_mlw_m_bg_1d(double *ro, double *pr, double *vx, double *vy, double *by,
+                        const double *bx, const double *bxm, double dt, double qav,
+                        double gm, const double *gx, const double *gxm,
+                        const double *sc, const double *dsc, const double *scm,
+                        const double *dscm, const double *rr, const double *rrm,
+                        const double *drr, const double *drrm, const double *dx,
+                        const double *dxm, int ix);
+int oracle_chkdav(double *da, double *vx, double floor_, int ix);
+double oracle_torque_uniform(unsigned long long seed, long long ns, int g, int ix);
+void oracle_trqalfven(double *vy, double dt, const double *trq, const double *rr,
+                      double trq0, unsigned long long seed, long long ns, int ix);
+int oracle_spicule_run(double *ro, double *pr, double *vx, double *vy, double *by,
+                       const double *bx, const double *bxm, double qav, double gm,
+                       const double *gx, const double *gxm, const double *sc,
+                       const double *dsc, const double *scm, const double *dscm,
+                       const double *rr, const double *rrm, const double *drr,
+                       const double *drrm, const double *dx, const double *dxm,
+                       const double *trq, double trq0, unsigned long long seed,
+                       int torque, double floor_, int chk, const int *kind,
+                       int margin, double safety, double dtmin, long long nstop,
+                       double tend, double t0, long long ns0, int ix,
+                       double *t_out, long long *ns_out, long long *nev_out);
 
 /* ---- 2-D  (cans2d) ------------------------------------------------------- */
 void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,

@@ -50,7 +50,8 @@ def test_run_desc_layout_matches_header(tmp_path):
     fields = [f[0] for f in capi._Desc._fields_]
     assert fields == ["solver", "ix", "jx", "kx", "margin", "gm", "qav", "dx", "dxm", "dy",
                       "dym", "dz", "dzm", "exact", "tile", "stream", "bx", "bxm", "mu",
-                      "mfdim"]
+                      "mfdim", "gx", "gxm", "sc", "scm", "dsc", "dscm", "rr", "rrm", "drr",
+                      "drrm", "chkdav", "floor", "trq", "trq0", "seed"]
     import shutil
     import subprocess
     cc = shutil.which("gcc") or shutil.which("cc")
@@ -68,6 +69,40 @@ def test_run_desc_layout_matches_header(tmp_path):
                                           text=True).stdout.split()]
     want = [getattr(capi._Desc, f).offset for f in fields] + [C.sizeof(capi._Desc)]
     assert out == want
+
+
+def test_run_state_layout_matches_header(tmp_path):
+    import shutil
+    import subprocess
+    fields = [f[0] for f in capi.RunState._fields_]
+    assert fields[-1] == "n_floor"
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    src = tmp_path / "state.c"
+    body = "".join(f'  printf("%zu ", offsetof(cans_run_state, {f}));\n' for f in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "cans_gpu.h"\n'
+                   "int main(void) {\n" + body +
+                   '  printf("%zu\\n", sizeof(cans_run_state));\n  return 0;\n}\n')
+    exe = tmp_path / "state"
+    subprocess.run([cc, f"-I{build.ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    assert out == [getattr(capi.RunState, f).offset for f in fields] + [C.sizeof(capi.RunState)]
+
+
+def test_mlw_m_bg_run_arguments_rejected_without_a_device(lib):
+    from utrip_gb300 import setups
+    s = setups.shock_tube_1d(64)
+    # the torque source needs the mlw_m_bg profiles
+    with pytest.raises(capi.CansError) as e:
+        capi.Run(capi.SOLVER_MLW_M_1D, s, s["gm"], s["qav"],
+                 torque={"trq": np.zeros(s["x"].size), "trq0": 1.0})
+    assert e.value.code == capi.CANS_ERR_ARG
+    # mlw_m_bg without its profiles
+    with pytest.raises(capi.CansError) as e:
+        capi.Run(capi.SOLVER_MLW_M_BG_1D, dict(s, gx=None), s["gm"], s["qav"])
+    assert e.value.code in (capi.CANS_ERR_ARG,)
 
 
 def test_hlld_and_roe_run_arguments_rejected_without_a_device(lib):

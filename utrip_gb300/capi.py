@@ -29,6 +29,7 @@ SOLVER_MLW_M_3D = 2
 SOLVER_MLW_M_1D = 3
 SOLVER_ROE_M_3D = 4
 SOLVER_HLLD_3D = 5
+SOLVER_MLW_M_BG_1D = 6
 
 BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
 
@@ -98,6 +99,8 @@ def load() -> C.CDLL:
     sig["cans_hlld_engine_3d"] = (i, [_dp] * 8 + [_dp] * 9 + [_ip] * 4)
     sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
     sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
+    sig["cans_mlw_m_bg"] = (i, [_dp] * 7 + [_dp, _dp, _dp] + [_dp] * 12 + [_ip])
+    sig["cans_chkdav"] = (i, [_ip, _dp, _dp, _dp, _ip])
     sig["cans_bdperx_1d"] = (i, [_ip, _ip, _dp, _ip])
     for fam in ("spp", "spn", "smp", "smn", "fre"):
         sig[f"cans_bd{fam}x_1d"] = (i, [_ip, _ip, _dp, _ip])
@@ -255,6 +258,26 @@ def mlw_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, dx, dxm):
                                        _iref(ix)), "mlw_m_1d")
 
 
+def mlw_m_bg(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, gx, gxm, sc, dsc, scm, dscm,
+             rr, rrm, drr, drrm, dx, dxm):
+    """cans1d/hdmlw/mlw_m_bg.f:2 -- one mLW step with gravity, flux-tube
+    cross section and rotation, in place (reference argument order)."""
+    ix = ro.size
+    return _check(load().cans_mlw_m_bg(*[_ptr(a) for a in (ro, pr, vx, vy, by, bx, bxm)],
+                                       _dref(dt), _dref(qav), _dref(gm),
+                                       *[_ptr(a) for a in (gx, gxm, sc, dsc, scm, dscm, rr,
+                                                           rrm, drr, drrm, dx, dxm)],
+                                       _iref(ix)), "mlw_m_bg")
+
+
+def chkdav(da, vx, floor):
+    """cans1d/common/chkdav.f:2 -- floor da, zero vx there; returns n_events."""
+    n = C.c_int(0)
+    _check(load().cans_chkdav(C.byref(n), _ptr(da), _ptr(vx), _dref(floor), _iref(da.size)),
+           "chkdav")
+    return n.value
+
+
 def cfl_m_1d(safety, dtmin, gm, bx, ro, pr, vx, vy, by, dx):
     """cans1d/common/cfl_m.f:2 -- returns (dt, merr)."""
     dt, merr = C.c_double(0.0), C.c_int(0)
@@ -366,18 +389,28 @@ def release(any_array) -> None:
 
 # ---- device-resident run handle --------------------------------------------
 
+def arr_of(keep: list, a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    keep.append(a)
+    return a.ctypes.data_as(_dp)
+
+
 class _Desc(C.Structure):
     _fields_ = [("solver", C.c_int), ("ix", C.c_int), ("jx", C.c_int), ("kx", C.c_int),
                 ("margin", C.c_int), ("gm", C.c_double), ("qav", C.c_double),
                 ("dx", _dp), ("dxm", _dp), ("dy", _dp), ("dym", _dp), ("dz", _dp), ("dzm", _dp),
                 ("exact", C.c_int), ("tile", C.c_int), ("stream", C.c_void_p),
-                ("bx", _dp), ("bxm", _dp), ("mu", C.c_double), ("mfdim", C.c_int * 3)]
+                ("bx", _dp), ("bxm", _dp), ("mu", C.c_double), ("mfdim", C.c_int * 3),
+                ("gx", _dp), ("gxm", _dp), ("sc", _dp), ("scm", _dp), ("dsc", _dp),
+                ("dscm", _dp), ("rr", _dp), ("rrm", _dp), ("drr", _dp), ("drrm", _dp),
+                ("chkdav", C.c_int), ("floor", C.c_double), ("trq", _dp),
+                ("trq0", C.c_double), ("seed", C.c_ulonglong)]
 
 
 class RunState(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("ns", C.c_longlong),
                 ("nexec", C.c_longlong), ("merr", C.c_int), ("done", C.c_int),
-                ("pause", C.c_int)]
+                ("pause", C.c_int), ("n_floor", C.c_longlong)]
 
 
 class Run:
@@ -385,13 +418,20 @@ class Run:
 
     def __init__(self, solver: int, grid: dict, gm: float, qav: float, margin: int = 1,
                  exact: bool = False, tile: int = -1, stream: int | None = None,
-                 mu: float = 1.0, mfdim=(0, 0, 0)):
+                 mu: float = 1.0, mfdim=(0, 0, 0), floor: float | None = None,
+                 torque: dict | None = None):
+        """grid holds dx, dxm (dy, dym, dz, dzm by dimension; bx, bxm in 1-D;
+        the ten BG_PROFILES of mlw_m_bg for SOLVER_MLW_M_BG_1D).  1-D loops
+        take floor (chkdav of ro and pr after each boundary fill) and, with
+        mlw_m_bg, torque = {"trq": profile, "trq0": amplitude, "seed": key}."""
         self.lib = load()
         self.solver = solver
         self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8,
-                     SOLVER_MLW_M_1D: 5, SOLVER_ROE_M_3D: 8, SOLVER_HLLD_3D: 8}[solver]
+                     SOLVER_MLW_M_1D: 5, SOLVER_ROE_M_3D: 8, SOLVER_HLLD_3D: 8,
+                     SOLVER_MLW_M_BG_1D: 5}[solver]
         three = solver in (SOLVER_MLW_M_3D, SOLVER_ROE_M_3D, SOLVER_HLLD_3D)
-        one = solver == SOLVER_MLW_M_1D
+        one = solver in (SOLVER_MLW_M_1D, SOLVER_MLW_M_BG_1D)
+        bgv = solver == SOLVER_MLW_M_BG_1D
 
         def arr(k):
             a = np.ascontiguousarray(grid[k], dtype=np.float64)
@@ -408,6 +448,16 @@ class Run:
                   1 if exact else 0, tile, C.c_void_p(stream) if stream else None,
                   arr("bx") if one else None, arr("bxm") if one else None,
                   mu, (C.c_int * 3)(*mfdim))
+        if bgv:
+            for k in ("gx", "gxm", "sc", "scm", "dsc", "dscm", "rr", "rrm", "drr", "drrm"):
+                if grid.get(k) is not None:  # a missing profile is rejected by the library
+                    setattr(d, k, arr(k))
+        if floor is not None:
+            d.chkdav, d.floor = 1, float(floor)
+        if torque is not None:
+            d.trq = arr_of(self._keep, torque["trq"])
+            d.trq0 = float(torque["trq0"])
+            d.seed = int(torque.get("seed", 0))
         self.shape = (nx,) if one else ((nx, ny) + ((nz,) if three else ()))
         h = C.c_void_p()
         _check(self.lib.cans_run_create(C.byref(h), C.byref(d)), "cans_run_create")

@@ -86,6 +86,7 @@ struct Ctl {
   double *buf[2];
   int cur;
   long long nexec;  // steps executed since the run started
+  unsigned long long nfloor;  // chkdav events since the run started
 };
 
 // Positive doubles order like their unsigned bit patterns.

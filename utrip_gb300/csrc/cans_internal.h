@@ -136,11 +136,28 @@ cudaError_t launch_adj2d_objective(const double *P, double *lam, double *J,
 // The whole 1-D loop (or one fixed-dt step) as one cluster launch, in place
 // on 5 arrays (ro,pr,vx,vy,by) of ix doubles.
 int mlw1d_min_cells();
+// Options of the 1-D loop: bg (10 arrays of ix: gx gxm sc scm dsc dscm rr
+// rrm drr drrm) selects the mlw_m_bg step; trq (ix, needs bg) adds the
+// torque source of the spicule model with amplitude trq0 and random-stream
+// key seed; chk applies chkdav of ro and pr with `floor` after each boundary
+// fill, counting the events into ctl->nfloor.  A fixed step uses bg only.
+struct Loop1D {
+  const double *bg = nullptr;
+  const double *trq = nullptr;
+  double trq0 = 0.0;
+  unsigned long long seed = 0;
+  double floor = 0.0;
+  int chk = 0;
+};
 cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
-                         const double *bxm, int ix, const Axis &ax,
-                         const Phys &ph, const BcTable &bc, Ctl *ctl,
-                         int max_steps, int fixed, double dt_fixed, int start,
-                         cudaStream_t s);
+                         const double *bxm, const Loop1D &opt, int ix,
+                         const Axis &ax, const Phys &ph, const BcTable &bc,
+                         Ctl *ctl, int max_steps, int fixed, double dt_fixed,
+                         int start, cudaStream_t s);
+// chkdav (cans1d/common/chkdav.f:68-76) on device arrays: da below floor is
+// raised to it and vx zeroed there; the count is added to *count (device).
+cudaError_t launch_chkdav(double *da, double *vx, double floor, size_t n,
+                          unsigned long long *count, cudaStream_t s);
 cudaError_t launch_cfl1d(bool exact, const double *S, const double *bx, int ix,
                          const Axis &ax, const Phys &ph, double safety,
                          unsigned long long *out, cudaStream_t s);

@@ -470,23 +470,30 @@ extern "C" int cans_bdfrdy_2d(const int *mbnd, const int *margin, double *qq,
 // ---------------------------------------------------------------------------
 // 1-D drop-in entry points
 namespace {
-// device copies of the constant bx, bxm arrays of the 1-D step
+// device copies of the constant arrays of the 1-D steps: bx, bxm and, for
+// mlw_m_bg, the ten profiles gx gxm sc scm dsc dscm rr rrm drr drrm
 struct Dev1D {
   double *bx = nullptr;
   int cap = 0;
-  int upload(int ix, const double *hbx, const double *hbxm, cudaStream_t s) {
+  int upload(int ix, const double *hbx, const double *hbxm, cudaStream_t s,
+             const double *const *prof = nullptr) {
     if (cap < ix) {
       if (bx) cudaFree(bx);
       bx = nullptr;
       cap = 0;
-      CK(cudaMalloc(&bx, sizeof(double) * 2 * (size_t)ix));
+      CK(cudaMalloc(&bx, sizeof(double) * 12 * (size_t)ix));
       cap = ix;
     }
     CK(cudaMemcpyAsync(bx, hbx, sizeof(double) * ix, cudaMemcpyHostToDevice, s));
     if (hbxm)
       CK(cudaMemcpyAsync(bx + ix, hbxm, sizeof(double) * ix, cudaMemcpyHostToDevice, s));
+    if (prof)
+      for (int k = 0; k < 10; k++)
+        CK(cudaMemcpyAsync(bg() + (size_t)k * ix, prof[k], sizeof(double) * ix,
+                           cudaMemcpyHostToDevice, s));
     return CANS_OK;
   }
+  double *bg() const { return bx + 2 * (size_t)cap; }
 };
 Dev1D g_dev1d;
 }  // namespace
@@ -520,13 +527,86 @@ extern "C" int cans_mlw_m_1d(double *ro, double *pr, double *vx, double *vy,
                          cudaMemcpyHostToDevice, s));
     S = g_scratch.A;
   }
-  CK(launch_mlw1d(exact_mode(), S, g_dev1d.bx, g_dev1d.bx + n, n, dax->a, ph, bc,
+  CK(launch_mlw1d(exact_mode(), S, g_dev1d.bx, g_dev1d.bx + n, Loop1D{}, n, dax->a, ph,
+                  bc, nullptr, 1, 1, *dt, 0, s));
+  if (m) return CANS_OK;
+  for (int v = 0; v < 5; v++)
+    CK(cudaMemcpyAsync(arrs[v], g_scratch.A + (size_t)v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+extern "C" int cans_mlw_m_bg(double *ro, double *pr, double *vx, double *vy,
+                             double *by, const double *bx, const double *bxm,
+                             const double *dt, const double *qav,
+                             const double *gm, const double *gx,
+                             const double *gxm, const double *sc,
+                             const double *dsc, const double *scm,
+                             const double *dscm, const double *rr,
+                             const double *rrm, const double *drr,
+                             const double *drrm, const double *dx,
+                             const double *dxm, const int *ix) {
+  const int n = *ix;
+  if (n < mlw1d_min_cells()) return CANS_ERR_ARG;
+  double *arrs[5] = {ro, pr, vx, vy, by};
+  const double *prof[10] = {gx, gxm, sc, scm, dsc, dscm, rr, rrm, drr, drrm};
+  for (const double *q : prof)
+    if (!q) return CANS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, *qav);
+  BcTable bc{};
+  bc.margin = 1;
+  MirrorSet *m = resident_step_set(arrs, 5);
+  DevAxis *dax = m ? &m->ax : &g_scratch.ax;
+  if ((rc = dax->upload(n, dx, dxm, s))) return rc;
+  if ((rc = g_dev1d.upload(n, bx, bxm, s, prof))) return rc;
+  double *S;
+  if (m) {
+    S = m->buf[m->cur];
+  } else {
+    if ((rc = g_scratch.ensure(5 * (size_t)n))) return rc;
+    for (int v = 0; v < 5; v++)
+      CK(cudaMemcpyAsync(g_scratch.A + (size_t)v * n, arrs[v], sizeof(double) * n,
+                         cudaMemcpyHostToDevice, s));
+    S = g_scratch.A;
+  }
+  Loop1D opt;
+  opt.bg = g_dev1d.bg();
+  CK(launch_mlw1d(exact_mode(), S, g_dev1d.bx, g_dev1d.bx + n, opt, n, dax->a, ph, bc,
                   nullptr, 1, 1, *dt, 0, s));
   if (m) return CANS_OK;
   for (int v = 0; v < 5; v++)
     CK(cudaMemcpyAsync(arrs[v], g_scratch.A + (size_t)v * n, sizeof(double) * n,
                        cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
+extern "C" int cans_chkdav(int *n_events, double *da, double *vx,
+                           const double *floor, const int *ix) {
+  if (!n_events || !da || !vx || !floor || *ix < 0) return CANS_ERR_ARG;
+  const size_t n = (size_t)*ix;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  if ((rc = g_scratch.ensure(2 * n + 1))) return rc;
+  double *dd = g_scratch.A, *dv = g_scratch.A + n;
+  unsigned long long *cnt = g_scratch.bits;
+  CK(cudaMemcpyAsync(dd, da, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dv, vx, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(cnt, 0, sizeof *cnt, s));
+  CK(launch_chkdav(dd, dv, *floor, n, cnt, s));
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(da, dd, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(vx, dv, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&out, cnt, sizeof out, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *n_events = (int)out;
   return CANS_OK;
 }
 
@@ -947,7 +1027,9 @@ struct cans_run {
   cudaGraphExec_t graph = nullptr;
   int graph_iters = 0;
   int graph_nodes = 0;
-  double *bx1 = nullptr;       // 1-D: device bx (ix) followed by bxm (ix)
+  double *bx1 = nullptr;       // 1-D: device bx, bxm, then (mlw_m_bg) the ten
+                               // profiles and the torque profile, ix each
+  Loop1D loop1d{};             // 1-D loop options (device pointers into bx1)
   double *roe = nullptr;       // Roe / HLLD: stage scratch
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
@@ -964,6 +1046,7 @@ int solver_nvar(int solver) {
     case CANS_SOLVER_MLW_M_1D: return 5;
     case CANS_SOLVER_ROE_M_3D: return 8;
     case CANS_SOLVER_HLLD_3D: return 8;
+    case CANS_SOLVER_MLW_M_BG_1D: return 5;
     default: return 0;
   }
 }
@@ -971,7 +1054,7 @@ int solver_ndim(int solver) {
   if (solver == CANS_SOLVER_MLW_M_3D || solver == CANS_SOLVER_ROE_M_3D ||
       solver == CANS_SOLVER_HLLD_3D)
     return 3;
-  return solver == CANS_SOLVER_MLW_M_1D ? 1 : 2;
+  return (solver == CANS_SOLVER_MLW_M_1D || solver == CANS_SOLVER_MLW_M_BG_1D) ? 1 : 2;
 }
 bool is_roe(const cans_run *h) { return h->d.solver == CANS_SOLVER_ROE_M_3D; }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
@@ -982,7 +1065,7 @@ int tile_count(const cans_run *h) {
 // 1-D: the whole loop (or one fixed step) as one cluster launch, in place
 cudaError_t launch_1d(cans_run *h, int max_steps, int fixed, double dt,
                       int start) {
-  return launch_mlw1d(h->d.exact != 0, h->buf[0], h->bx1, h->bx1 + h->d.ix,
+  return launch_mlw1d(h->d.exact != 0, h->buf[0], h->bx1, h->bx1 + h->d.ix, h->loop1d,
                       h->d.ix, h->ax.a, h->ph, h->bc, fixed ? nullptr : h->ctl,
                       max_steps, fixed, dt, start, h->s);
 }
@@ -1122,10 +1205,19 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   // every extent must exceed the two frames of margin+1 cells that the
   // boundary program and the frame CFL work on
   const int wmin = 2 * (d->margin + 1) + 1;
+  const bool bgv = d->solver == CANS_SOLVER_MLW_M_BG_1D;
+  const double *prof[10] = {d->gx, d->gxm, d->sc, d->scm, d->dsc,
+                            d->dscm, d->rr, d->rrm, d->drr, d->drrm};
   if (ndim == 1) {
     if (d->ix < mlw1d_min_cells() || d->jx != 1 || d->kx != 1 ||
         !d->dx || !d->dxm || !d->bx || !d->bxm)
       return CANS_ERR_ARG;
+    if (bgv)
+      for (const double *q : prof)
+        if (!q) return CANS_ERR_ARG;
+    // the torque source reads the rr profile of mlw_m_bg
+    if (d->trq && !bgv) return CANS_ERR_ARG;
+    if (d->chkdav != 0 && d->chkdav != 1) return CANS_ERR_ARG;
   } else if (d->solver == CANS_SOLVER_HLLD_3D) {
     // checked above
   } else {
@@ -1171,13 +1263,28 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   if (ndim >= 2 && (rc = h->ay.upload(d->jx, d->dy, d->dym, h->s))) return bail(rc);
   if (ndim == 3 && (rc = h->az.upload(d->kx, d->dz, d->dzm, h->s))) return bail(rc);
   if (ndim == 1) {
-    e = cudaMalloc(&h->bx1, sizeof(double) * 2 * (size_t)d->ix);
+    const size_t nx = (size_t)d->ix;
+    e = cudaMalloc(&h->bx1, sizeof(double) * 13 * nx);
     if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(bx)"));
-    e = cudaMemcpyAsync(h->bx1, d->bx, sizeof(double) * d->ix, cudaMemcpyHostToDevice, h->s);
+    e = cudaMemcpyAsync(h->bx1, d->bx, sizeof(double) * nx, cudaMemcpyHostToDevice, h->s);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(h->bx1 + d->ix, d->bxm, sizeof(double) * d->ix,
+      e = cudaMemcpyAsync(h->bx1 + nx, d->bxm, sizeof(double) * nx,
+                          cudaMemcpyHostToDevice, h->s);
+    for (int k = 0; bgv && k < 10 && e == cudaSuccess; k++)
+      e = cudaMemcpyAsync(h->bx1 + (2 + k) * nx, prof[k], sizeof(double) * nx,
+                          cudaMemcpyHostToDevice, h->s);
+    if (e == cudaSuccess && d->trq)
+      e = cudaMemcpyAsync(h->bx1 + 12 * nx, d->trq, sizeof(double) * nx,
                           cudaMemcpyHostToDevice, h->s);
     if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMemcpy(bx)"));
+    if (bgv) h->loop1d.bg = h->bx1 + 2 * nx;
+    if (d->trq) {
+      h->loop1d.trq = h->bx1 + 12 * nx;
+      h->loop1d.trq0 = d->trq0;
+      h->loop1d.seed = d->seed;
+    }
+    h->loop1d.chk = d->chkdav;
+    h->loop1d.floor = d->floor;
   }
   if (is_roe(h) || is_hlld(h)) {
     const size_t nd = is_roe(h) ? roe3d_scratch_doubles(h->n) : hlld3d_scratch_doubles(h->n);
@@ -1284,6 +1391,7 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
   c.pause = 0;
   c.frame_blocks_done = 0;
   c.nonfinite = 0;
+  c.nfloor = 0;
   c.cfl_bits = r4_1e20_bits();
   h->host_ctl = c;
   CK(cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice,
@@ -1347,6 +1455,7 @@ extern "C" int cans_run_query(cans_run *h, cans_run_state *st) {
   st->merr = c.merr;
   st->done = c.done;
   st->pause = c.pause;
+  st->n_floor = (long long)c.nfloor;
   return c.merr ? c.merr : CANS_OK;
 }
 

@@ -14,6 +14,15 @@
 // CFL minimum is reduced across the cluster, so no host round trip happens
 // per step.  Three cluster barriers per step: after the update, after the
 // boundary fill, after the halo exchange and CFL reduction.
+//
+// The BG variant is mlw_m_bg (cans1d/hdmlw/mlw_m_bg.f:2-271): the same
+// two-stage step on the cross-section-weighted variables (ro, e, rx, ry r,
+// by/r) x sc with gravity, cross-section and rotation sources added by
+// mlwsrch.f / mlwsrcf.f, and bx included in the energy.  The spicule loop
+// (cans1d/md_spicule/hdmlw/main.f:160-219) adds two options that any 1-D
+// loop may use: the torque source of trqalfven.f after the step, and the
+// chkdav floor of ro and pr after the boundary fill (one extra cluster
+// barrier), with the events counted in the control block.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -32,6 +41,12 @@ constexpr int NV1 = 5;
 struct Run1D {
   double *S;             // global state, 5 arrays of ix (read at start, written at end)
   const double *bx, *bxm;
+  const double *bg;      // BG: gx gxm sc scm dsc dscm rr rrm drr drrm (10 x ix)
+  const double *trq;     // torque profile trq(ix), or nullptr
+  double trq0;           // torque amplitude
+  unsigned long long seed;  // key of the torque's random stream
+  double floor;          // chkdav floor of ro and pr (used when chk)
+  int chk;
   Axis ax;
   Phys ph;
   BcTable bc;
@@ -101,7 +116,36 @@ __device__ void bd1_face(int kind, int mbnd, int m, int n, double q0,
   }
 }
 
+// Uniform deviate in [0, 1) for cell g of loop step ns: SplitMix64 (Steele,
+// Lea and Flood, "Fast splittable pseudorandom number generators", OOPSLA
+// 2014) of the counter ns*ix + g offset by the seed, top 53 bits.  Integer
+// arithmetic only, so every device and the host give the same stream.  It
+// stands in for the Fortran random_number of trqalfven.f:23, whose stream
+// belongs to the compiler's runtime library.
+__device__ __forceinline__ double torque_uniform(unsigned long long seed, long long ns,
+                                                 int g, int ix) {
+  unsigned long long z =
+      seed + ((unsigned long long)ns * (unsigned long long)ix + (unsigned long long)g + 1ull) *
+                 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return (double)(z >> 11) * 0x1.0p-53;
+}
+
+// trqalfven.f:25-36 for global cell g: vy + dt*trq0*q*trq with
+// q = 2 rr (anum - 0.5); cell ix takes q of cell ix-2 (trqalfven.f:30)
 template <bool E>
+__device__ __forceinline__ F<E> torque_add(const Run1D &p, F<E> vy, F<E> dt, long long ns,
+                                           int g) {
+  using FT = F<E>;
+  const int gq = (g == p.ix - 1) ? p.ix - 3 : g;
+  const FT anum(torque_uniform(p.seed, ns, gq, p.ix));
+  const FT q = 2.0 * FT(p.bg[6 * (size_t)p.ix + gq]) * (anum - 0.5);
+  return vy + dt * FT(p.trq0) * q * FT(p.trq[g]);
+}
+
+template <bool E, bool BG>
 __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   using FT = F<E>;
   cg::cluster_group cluster = cg::this_cluster();
@@ -110,14 +154,19 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   const int tid = threadIdx.x, NT = blockDim.x;
   const int ix = p.ix, L = p.lmax;
   extern __shared__ double sm[];
-  // layout: prim[2][5][L], U[5][L], FX[5][L], K[5][L], Q[L], slots[2][CS], red[32]
+  // layout: prim[2][5][L], U[5][L], FX[5][L], K[5][L], Q[L],
+  // (BG: SS[2][L] cell sources, SH[2][L] corner sources), slots[2][CS], red[32]
   double *prim = sm;
   double *U = prim + 2 * NV1 * L;
   double *FX = U + NV1 * L;
   double *K = FX + NV1 * L;
   double *Q = K + NV1 * L;
-  double *slots = Q + L;
+  double *SS = Q + L;
+  double *SH = SS + (BG ? 2 * L : 0);
+  double *slots = SH + (BG ? 2 * L : 0);
   double *red = slots + 2 * CS;
+  const double *bg = p.bg;
+  const size_t nx = (size_t)ix;
   __shared__ double s_dt, s_t, s_tp, s_pending;
   __shared__ long long s_ns, s_nexec;
   __shared__ int s_done, s_merr, s_pause;
@@ -212,8 +261,41 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   for (int step = 0; step < p.max_steps; step++) {
     if (s_done || s_pause) break;
     const FT dt(s_dt);
+    const long long ns_now = s_ns;
     const int nb = cur ^ 1;
-    // ---- cell stage (mlw_m.f:37-73) --------------------------------------
+    // ---- cell stage (mlw_m.f:37-73; mlw_m_bg.f:97-166) ---------------------
+    if constexpr (BG) {
+      for (int l = tid; l < nl; l += NT) {
+        const int g = lo - 1 + l;
+        const FT ro(P(cur, 0, l)), pr(P(cur, 1, l)), vx(P(cur, 2, l)), vy(P(cur, 3, l)),
+            by(P(cur, 4, l));
+        const FT bx(p.bx[g]), gx(bg[g]), sc(bg[2 * nx + g]), dsc(bg[4 * nx + g]),
+            rr(bg[6 * nx + g]), drr(bg[8 * nx + g]);
+        const FT vv = vx * vx + vy * vy;
+        const FT bb = by * by + bx * bx;
+        FT ee, ep;
+        if constexpr (E) {
+          ee = pr / gm1 + 0.5 * ro * vv + pi8i * bb;
+          ep = pr * gm / gm1 + 0.5 * ro * vv;
+        } else {
+          ee = pr * p.ph.gm1i + 0.5 * ro * vv + pi8i * bb;
+          ep = pr * p.ph.ggm1 + 0.5 * ro * vv;
+        }
+        const FT rx = ro * vx;
+        const FT ez = -vx * by + vy * bx;
+        const FT bbm = by * by - bx * bx;
+        U[0 * L + l] = (ro * sc).v; U[1 * L + l] = (ee * sc).v; U[2 * L + l] = (rx * sc).v;
+        U[3 * L + l] = (ro * vy * sc * rr).v; U[4 * L + l] = (by * sc / rr).v;
+        FX[0 * L + l] = (rx * sc).v;                                          // :121-122
+        FX[1 * L + l] = ((ep * vx - by * ez * pi4i) * sc).v;                  // :130-131
+        SS[0 * L + l] = (rx * gx * sc).v;                                     // :132-133
+        FX[2 * L + l] = ((ro * (vx * vx) + pr + bbm * pi8i) * sc).v;          // :144,147
+        SS[1 * L + l] = ((ro * gx + (ro * (vy * vy) - (by * by) * pi4i) / rr * drr) * sc +
+                         (pr + bb * pi8i) * dsc).v;                           // :145-148
+        FX[3 * L + l] = ((ro * vx * vy - bx * by * pi4i) * sc * rr).v;        // :155-156
+        FX[4 * L + l] = ((-ez) * sc / rr).v;                                  // :162-164
+      }
+    } else
     for (int l = tid; l < nl; l += NT) {
       const int g = lo - 1 + l;
       const FT ro(P(cur, 0, l)), pr(P(cur, 1, l)), vx(P(cur, 2, l)), vy(P(cur, 3, l)),
@@ -241,6 +323,59 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
     }
     __syncthreads();
     // ---- corners (mlwhalf.f:42-46, mlw_m.f:74-110) and AV faces -----------
+    if constexpr (BG) {
+      // mlwhalf + mlwsrch, conversion (mlw_m_bg.f:170-183), corner fluxes
+      // and sources (:188-234)
+      for (int l = tid; l < nl - 1; l += NT) {
+        const int g = lo - 1 + l;
+        const FT dxim(ax.dim[g]);
+        FT un[NV1];
+#pragma unroll
+        for (int v = 0; v < NV1; v++) {
+          const FT uh = 0.5 * (FT(U[v * L + l + 1]) + FT(U[v * L + l]));
+          const FT dfdx = dxim * (FT(FX[v * L + l + 1]) - FT(FX[v * L + l]));
+          un[v] = uh - dt * dfdx;
+        }
+        un[1] = un[1] + dt * (0.5 * (FT(SS[0 * L + l + 1]) + FT(SS[0 * L + l])));
+        un[2] = un[2] + dt * (0.5 * (FT(SS[1 * L + l + 1]) + FT(SS[1 * L + l])));
+        const FT scm(bg[3 * nx + g]), rrm(bg[7 * nx + g]), gxm(bg[nx + g]),
+            dscm(bg[5 * nx + g]), drrm(bg[9 * nx + g]), bxm(p.bxm[g]);
+        FT roh, eeh, vxh, vyh, byh;
+        if constexpr (E) {
+          roh = un[0] / scm;
+          eeh = un[1] / scm;
+          vxh = un[2] / un[0];
+          vyh = un[3] / un[0] / rrm;
+          byh = un[4] / scm * rrm;
+        } else {
+          const FT si(1.0 / scm.v), ri(1.0 / un[0].v);
+          roh = un[0] * si;
+          eeh = un[1] * si;
+          vxh = un[2] * ri;
+          vyh = un[3] * ri / rrm;
+          byh = un[4] * si * rrm;
+        }
+        const FT vv = vxh * vxh + vyh * vyh;
+        const FT bb = bxm * bxm + byh * byh;
+        const FT prh = gm1 * (eeh - 0.5 * roh * vv - pi8i * bb);
+        const FT ezh = -vxh * byh + vyh * bxm;
+        FT eph;
+        if constexpr (E) eph = prh * gm / gm1 + 0.5 * roh * vv;
+        else eph = prh * p.ph.ggm1 + 0.5 * roh * vv;
+        const FT bbm = byh * byh - bxm * bxm;
+        K[0 * L + l] = (roh * vxh * scm).v;
+        K[1 * L + l] = ((eph * vxh - byh * ezh * pi4i) * scm).v;
+        SH[0 * L + l] = (roh * vxh * gxm * scm).v;
+        K[2 * L + l] = ((roh * (vxh * vxh) + prh + bbm * pi8i) * scm).v;
+        SH[1 * L + l] = ((roh * gxm + (roh * (vyh * vyh) - (byh * byh) * pi4i) / rrm * drrm) * scm +
+                         (prh + bb * pi8i) * dscm).v;
+        K[3 * L + l] = ((roh * vxh * vyh - bxm * byh * pi4i) * scm * rrm).v;
+        K[4 * L + l] = ((-ezh) * scm / rrm).v;
+        const FT q = qav * FT(ax.dm[g]) *
+                     max0(fabs_(FT(P(cur, 2, l + 1)) - FT(P(cur, 2, l))) - CANS_AV_EPS);
+        Q[l] = (q * dxim).v;
+      }
+    } else
     for (int l = tid; l < nl - 1; l += NT) {
       const int g = lo - 1 + l;  // corner between g and g+1
       const FT dxim(ax.dim[g]);
@@ -280,6 +415,53 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
     }
     __syncthreads();
     // ---- full step of the own cells ---------------------------------------
+    if constexpr (BG) {
+      // mlwhalf/mlwsrch increments, mlwfull + mlwsrcf, mlwartv, then the
+      // update and conversion (mlw_m_bg.f:251-268) and the torque
+      for (int l = 1 + tid; l <= nl - 2; l += NT) {
+        const int g = lo - 1 + l;
+        const FT hdt = 0.5 * dt, dxi(ax.di[g]);
+        const FT hdx = 0.5 * dxi;
+        FT u[NV1];
+#pragma unroll
+        for (int v = 0; v < NV1; v++) {
+          FT du(0.0);
+          du = du - hdt * (hdx * (FT(FX[v * L + l + 1]) - FT(FX[v * L + l - 1])));
+          if (v == 1 || v == 2) du = du + hdt * FT(SS[(v - 1) * L + l]);
+          du = du - hdt * (dxi * (FT(K[v * L + l]) - FT(K[v * L + l - 1])));
+          if (v == 1 || v == 2)
+            du = du + hdt * (FT(ax.u0[g]) * FT(SH[(v - 1) * L + l - 1]) +
+                             FT(ax.u1[g]) * FT(SH[(v - 1) * L + l]));
+          const FT uc(U[v * L + l]);
+          du = du + dt * (dxi * (FT(Q[l]) * (FT(U[v * L + l + 1]) - uc) -
+                                 FT(Q[l - 1]) * (uc - FT(U[v * L + l - 1]))));
+          u[v] = uc + du;
+        }
+        const FT sc(bg[2 * nx + g]), rr(bg[6 * nx + g]), bx(p.bx[g]);
+        FT ro, ee, rx, ry, by, vx, vy;
+        if constexpr (E) {
+          ro = u[0] / sc;
+          ee = u[1] / sc;
+          rx = u[2] / sc;
+          ry = u[3] / sc / rr;
+          by = u[4] / sc * rr;
+          vx = rx / ro;
+          vy = ry / ro;
+        } else {
+          const FT si(1.0 / sc.v);
+          ro = u[0] * si;
+          ee = u[1] * si;
+          const FT rinv(1.0 / u[0].v);  // 1/(ro sc)
+          vx = u[2] * rinv;
+          vy = u[3] * rinv / rr;
+          by = u[4] * si * rr;
+        }
+        const FT pr = gm1 * (ee - 0.5 * ro * (vx * vx + vy * vy) - pi8i * (bx * bx + by * by));
+        if (p.trq) vy = torque_add<E>(p, vy, dt, ns_now, g);
+        P(nb, 0, l) = ro.v; P(nb, 1, l) = pr.v; P(nb, 2, l) = vx.v;
+        P(nb, 3, l) = vy.v; P(nb, 4, l) = by.v;
+      }
+    } else
     for (int l = 1 + tid; l <= nl - 2; l += NT) {
       const int g = lo - 1 + l;
       const FT hdt = 0.5 * dt, dxi(ax.di[g]);
@@ -309,12 +491,18 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
       P(nb, 0, l) = ro.v; P(nb, 1, l) = pr.v; P(nb, 2, l) = vx.v;
       P(nb, 3, l) = vy.v; P(nb, 4, l) = by.v;
     }
-    // ghost cells keep their values through the step
+    // ghost cells keep their values through the step; the torque source
+    // runs over every cell (trqalfven.f:35-37), ghosts included
     if (tid == 0) {
-      if (lo == 1)
+      if (lo == 1) {
         for (int v = 0; v < NV1; v++) P(nb, v, 0) = P(cur, v, 0);
-      if (hi == ix - 2)
+        if (BG && p.trq) P(nb, 3, 0) = torque_add<E>(p, FT(P(nb, 3, 0)), dt, ns_now, 0).v;
+      }
+      if (hi == ix - 2) {
         for (int v = 0; v < NV1; v++) P(nb, v, nl - 1) = P(cur, v, nl - 1);
+        if (BG && p.trq)
+          P(nb, 3, nl - 1) = torque_add<E>(p, FT(P(nb, 3, nl - 1)), dt, ns_now, ix - 1).v;
+      }
     }
     cluster.sync();
     if (p.fixed) {
@@ -350,6 +538,25 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
         bd1_face(p.bc.kind[v][1], 1, p.bc.margin, ix, p.bc.q0[v][1], ax.dm, get, put);
     }
     cluster.sync();
+    // ---- chkdav of ro, then pr (chkdav.f:68-76), every cell incl. ghosts ----
+    if (p.chk) {
+      unsigned int nev = 0;
+      const int l0 = (lo == 1) ? 0 : 1, l1 = (hi == ix - 2) ? nl - 1 : nl - 2;
+      for (int l = l0 + tid; l <= l1; l += NT) {
+        if (P(nb, 0, l) < p.floor) {
+          P(nb, 0, l) = p.floor;
+          P(nb, 2, l) = 0.0;
+          nev++;
+        }
+        if (P(nb, 1, l) < p.floor) {
+          P(nb, 1, l) = p.floor;
+          P(nb, 2, l) = 0.0;
+          nev++;
+        }
+      }
+      if (nev) atomicAdd(&p.ctl->nfloor, (unsigned long long)nev);
+      cluster.sync();
+    }
     // ---- halo exchange and CFL of the new state ----------------------------
     if (tid < NV1) {
       if (r > 0) {
@@ -426,7 +633,7 @@ static int cluster_for(int ix, int cmax) {
 // Largest cluster the device co-schedules for this kernel: 16 blocks where
 // non-portable cluster sizes are available, else the portable 8.
 static int cluster_max(void (*kern)(Run1D), size_t smem) {
-  static int cached = 0;
+  static int cached = 0;  // the same answer for every instance of the kernel
   if (cached) return cached;
   int best = 8;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
@@ -453,18 +660,28 @@ static int cluster_max(void (*kern)(Run1D), size_t smem) {
 // Host launcher: the cluster kernel over a state of 5 arrays of ix doubles,
 // updated in place.
 cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
-                         const double *bxm, int ix, const Axis &ax,
-                         const Phys &ph, const BcTable &bc, Ctl *ctl,
-                         int max_steps, int fixed, double dt_fixed, int start,
-                         cudaStream_t s) {
+                         const double *bxm, const Loop1D &opt, int ix,
+                         const Axis &ax, const Phys &ph, const BcTable &bc,
+                         Ctl *ctl, int max_steps, int fixed, double dt_fixed,
+                         int start, cudaStream_t s) {
   if (ix < mlw1d_min_cells()) return cudaErrorInvalidValue;
-  void (*kern)(Run1D) = exact ? k_mlw1d<true> : k_mlw1d<false>;
+  const bool bgv = opt.bg != nullptr;
+  // the torque reads the rr profile; the floor counts into the control block
+  if ((opt.trq && !bgv) || (opt.chk && !ctl && !fixed)) return cudaErrorInvalidValue;
+  void (*kern)(Run1D) = bgv ? (exact ? k_mlw1d<true, true> : k_mlw1d<false, true>)
+                            : (exact ? k_mlw1d<true, false> : k_mlw1d<false, false>);
+  const size_t per_cell = (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 4 : 0);
   // shared memory of the largest block the grid can have (16 blocks)
-  const size_t smem_probe =
-      sizeof(double) * ((size_t)(2 * NV1 + 3 * NV1 + 1) * ((ix - 2) / 16 + 4) + 32 + 32);
+  const size_t smem_probe = sizeof(double) * (per_cell * ((ix - 2) / 16 + 4) + 32 + 32);
   const int CS = cluster_for(ix, cluster_max(kern, smem_probe));
   Run1D p{};
   p.S = S; p.bx = bx; p.bxm = bxm; p.ax = ax; p.ph = ph; p.bc = bc; p.ctl = ctl;
+  p.bg = opt.bg;
+  p.trq = fixed ? nullptr : opt.trq;
+  p.trq0 = opt.trq0;
+  p.seed = opt.seed;
+  p.floor = opt.floor;
+  p.chk = fixed ? 0 : opt.chk;
   p.ix = ix;
   p.q = (ix - 2) / CS;
   p.rem = (ix - 2) % CS;
@@ -475,7 +692,7 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
   p.start = start;
   // each block must own at least margin+1 cells for the boundary rules
   if (p.q < bc.margin + 1) return cudaErrorInvalidValue;
-  const size_t smem = sizeof(double) * ((size_t)(2 * NV1 + 3 * NV1 + 1) * p.lmax + 2 * CS + 32);
+  const size_t smem = sizeof(double) * (per_cell * p.lmax + 2 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
@@ -528,6 +745,42 @@ cudaError_t launch_cfl1d(bool exact, const double *S, const double *bx, int ix,
                          unsigned long long *out, cudaStream_t s) {
   if (exact) k_cfl1d<true><<<1, 256, 0, s>>>(S, bx, ix, ax, ph, safety, out);
   else k_cfl1d<false><<<1, 256, 0, s>>>(S, bx, ix, ax, ph, safety, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace cans
+
+namespace cans {
+
+// chkdav on one array pair (the drop-in entry point); grid-stride loop,
+// one atomic per block for the count.
+__global__ void k_chkdav(double *da, double *vx, double floor, size_t n,
+                         unsigned long long *count) {
+  __shared__ unsigned int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  unsigned int mine = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    if (da[i] < floor) {
+      da[i] = floor;
+      vx[i] = 0.0;
+      mine++;
+    }
+  }
+  if (mine) atomicAdd(&cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0 && cnt) atomicAdd(count, (unsigned long long)cnt);
+}
+
+cudaError_t launch_chkdav(double *da, double *vx, double floor, size_t n,
+                          unsigned long long *count, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int threads = 256;
+  const size_t want = (n + threads - 1) / threads;
+  const int blocks = (int)(want < 1216 ? want : 1216);  // 8 blocks per SM at most
+  k_chkdav<<<blocks, threads, 0, s>>>(da, vx, floor, n, count);
   count_launch();
   return cudaGetLastError();
 }

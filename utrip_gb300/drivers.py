@@ -8,10 +8,16 @@ run_literal  -- the reference driver shape (cans2d/md_mhdkh/hdmlw/main.f:
                 mirrors and only dt crosses to the host each step.
 run_resident -- the same loop kept on the device by the run handle and
                 replayed as a CUDA graph; the host waits once at the end.
+run_spicule  -- the spicule model package (cans1d/md_spicule/hdmlw/main.f)
+                on the device, with its DAC output files and restart.
 """
 from __future__ import annotations
 
-from . import capi
+from pathlib import Path
+
+import numpy as np
+
+from . import capi, dac, setups
 
 
 def _bnd(setup, state):
@@ -60,7 +66,7 @@ def _bnd1(setup, state):
 
 
 def _cfl(setup, state, safety):
-    if setup["solver"] == "mlw_m_1d":
+    if setup["solver"] in ("mlw_m_1d", "mlw_m_bg_1d"):
         return capi.cfl_m_1d(safety, setup["dtmin"], setup["gm"], setup["bx"], *state,
                              setup["dx"])
     if setup["solver"] in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
@@ -73,6 +79,12 @@ def _cfl(setup, state, safety):
 
 
 def _step(setup, state, dt):
+    if setup["solver"] == "mlw_m_bg_1d":
+        s = setup
+        capi.mlw_m_bg(*state, s["bx"], s["bxm"], dt, s["qav"], s["gm"], s["gx"], s["gxm"],
+                      s["sc"], s["dsc"], s["scm"], s["dscm"], s["rr"], s["rrm"], s["drr"],
+                      s["drrm"], s["dx"], s["dxm"])
+        return
     if setup["solver"] == "mlw_m_1d":
         capi.mlw_m_1d(*state, setup["bx"], setup["bxm"], dt, setup["qav"], setup["gm"],
                       setup["dx"], setup["dxm"])
@@ -112,7 +124,7 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             dts.append(dt)
             _step(setup, state, dt)
             {"mlw_m_3d": _bnd3, "roe_m_3d": _bnd3, "hlld_3d": _bnd3,
-             "mlw_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
+             "mlw_m_1d": _bnd1, "mlw_m_bg_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
     finally:
@@ -121,10 +133,17 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             capi.release(state[0])
 
 
-def make_run(setup, exact=False, tile=-1, stream=None) -> capi.Run:
+def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True) -> capi.Run:
+    """Run handle for a set-up; a set-up with a "floor" gets the chkdav
+    option and one with a "trq" profile the torque source (each can be
+    switched off here)."""
+    fl = setup.get("floor") if floor else None
+    tq = None
+    if torque and setup.get("trq") is not None:
+        tq = {"trq": setup["trq"], "trq0": setup["trq0"], "seed": setup.get("seed", 0)}
     run = capi.Run(setup["solver_id"], setup, setup["gm"], setup["qav"], setup["margin"],
                    exact=exact, tile=tile, stream=stream, mu=setup.get("mu", 1.0),
-                   mfdim=setup.get("mfdim", (0, 0, 0)))
+                   mfdim=setup.get("mfdim", (0, 0, 0)), floor=fl, torque=tq)
     run.set_bc_program(setup["bc"])
     return run
 
@@ -150,3 +169,127 @@ def run_resident(setup, state, nstop, tend=None, safety=None, t0=0.0, exact=Fals
     finally:
         if own:
             run.close()
+
+
+# ---- the spicule model package ------------------------------------------------
+
+def _e10_3(v: float) -> str:
+    """Fortran E10.3: 0.ddd with a two-digit exponent, right-justified."""
+    v = float(v)
+    if v == 0.0:
+        body = "0.000E+00"
+    else:
+        digits, ex = ("%.2e" % abs(v)).split("e")
+        body = "0." + digits.replace(".", "") + "E%+03d" % (int(ex) + 1)
+        if v < 0:
+            body = "-" + body
+    return body.rjust(10)
+
+
+def _out_line(kind: str, ns: int, t: float, nd: int | None = None) -> str:
+    """main.f formats 913 / 915: (1x,' write    ','step=',i8,' time=',e10.3,' nd =',i3)."""
+    line = " " + (" write    " if kind == "write" else " stop     ") + "step=" + "%8d" % ns
+    line += " time=" + _e10_3(t)
+    if nd is not None:
+        line += " nd =" + "%3d" % nd
+    return line
+
+
+def run_spicule(out_dir, nx: int = 1024, tend: float = 100.0, dtout: float = 0.5,
+                nstop: int = 100000, mcont: int = 0, in_dir=None, exact: bool = False,
+                seed: int = 0, chunk: int = 20000, torque: bool = True):
+    """cans1d/md_spicule/hdmlw/main.f on the device.
+
+    Writes what the reference writes into out_dir: params.txt (ix, margin,
+    ztr, tcor, gm), the static profiles x, bx, bxm, sc, scm, gx, gxm, rr, rrm
+    (dacdef1d), the time series t, ro, pr, vx, vy, by (dacdef0s / dacdef1s)
+    with a record at the start, at every crossing of a multiple of dtout and
+    at the end (unless the last step wrote one), and out.txt.  With mcont=1
+    the state and time are the last record (at most the 1000th) of
+    in_dir/{t,ro,pr,vx,vy,by}.dac, as main.f:78-102 reads them.  The loop
+    runs as the 1-D cluster kernel, pausing on the device at output times.
+    Returns a dict with t, ns, merr, the number of records written and the
+    chkdav event count."""
+    s = setups.spicule_1d(nx, seed=seed, tend=tend, nstop=nstop, dtout=dtout)
+    ix, names = s["x"].size, s["names"]
+    out = Path(out_dir)
+    out.mkdir(parents=True, exist_ok=True)
+    outtxt = out / "out.txt"
+    outtxt.write_text("")
+
+    def say(line: str) -> None:
+        with open(outtxt, "a") as f:
+            f.write(line + "\n")
+
+    params = dac.DacParams(out / "params.txt")
+    ft = dac.dacdef0s(out / "t.dac")
+    fs = {k: dac.dacdef1s(out / f"{k}.dac", ix) for k in names}
+    params.puti("ix", ix)
+    params.puti("margin", s["margin"])
+    params.putd("ztr", s["ztr"])
+    params.putd("tcor", s["tcor"])
+    state = setups.copy_state(s)
+    t = 0.0
+    if mcont == 1:
+        src = Path(in_dir) if in_dir is not None else Path("in")
+        tt = dac.dacopnr(src / "t.dac", 0)
+        nrec = min(tt.nx, 1000)
+        if nrec > 0:
+            t = float(tt.records[nrec - 1])
+            for k, name in enumerate(names):
+                f = dac.dacopnr(src / f"{name}.dac", 1)
+                if f.dims != (ix,):
+                    raise dac.DacError(f"{name}.dac holds {f.dims[0]} cells, the model {ix}")
+                state[k][:] = f.records[min(nrec, f.nx) - 1]
+    for k in ("x", "bx", "bxm", "sc", "scm", "gx", "gxm", "rr", "rrm"):
+        dac.write_1d(out / f"{k}.dac", s[k])
+    params.putd("gm", s["gm"])
+    nd = 1
+
+    def write_records(ns_: int, t_: float) -> None:
+        nonlocal nd
+        ft.write(np.float64(t_))
+        for k, name in enumerate(names):
+            fs[name].write(state[k])
+        say(_out_line("write", ns_, t_, nd))
+        nd += 1
+
+    write_records(0, t)
+    run = make_run(s, exact=exact, torque=torque)
+    try:
+        run.push(state)
+        run.start(t0=t, tend=tend, nstop=nstop, safety=s["safety"], dtmin=s["dtmin"],
+                  dtout=dtout, pause_on_output=True)
+        wrote_last = False
+        while True:
+            st = run.query()
+            if st.pause:
+                run.pull(state)
+                write_records(int(st.ns), st.t)
+                wrote_last = True
+                if st.done:
+                    break
+                run.resume()
+                continue
+            if st.done:
+                break
+            wrote_last = False
+            run.advance(min(chunk, max(1, nstop - int(st.ns) + 1)))
+        st = run.query()
+        run.pull(state)
+        if not wrote_last or st.merr:
+            write_records(int(st.ns), st.t)
+        say(_out_line("stop", int(st.ns), st.t))
+        if st.merr == 0:
+            say("   ### normal stop ###")
+        else:
+            say("   ### abnormal stop ###")
+            say("   merr = %11d" % st.merr)
+        return {"t": st.t, "ns": int(st.ns), "merr": int(st.merr), "records": nd - 1,
+                "n_floor": int(st.n_floor), "state": state}
+    finally:
+        run.close()
+        ft.close()
+        for f in fs.values():
+            f.close()
+        params.close()

@@ -16,8 +16,8 @@ import math
 
 import numpy as np
 
-from .capi import (BD_PER, BD_SPP, BD_SMN, SOLVER_HLLD_3D, SOLVER_MLW_M_2D,
-                   SOLVER_MLW_M3_2D, SOLVER_ROE_M_3D)
+from .capi import (BD_FRE, BD_PER, BD_SMN, BD_SMP, BD_SPN, BD_SPP, SOLVER_HLLD_3D,
+                   SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M_3D)
 
 SQ4PI = math.sqrt(4.0 * math.pi)
 
@@ -457,3 +457,195 @@ def shock_tube_hlld_1d(n: int = 1024, tend: float = 0.1):
     return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, gm, 0.0, bc, solver="hlld_3d",
                   mu=mu, mfdim=(1, 0, 0), safety=0.4, dtmin=1e-10, tend=tend,
                   name=f"shock_tube_hlld_{n}")
+
+
+# ---- the spicule model (cans1d/md_spicule/hdmlw) ------------------------------
+
+VARS["mlw_m_bg_1d"] = ["ro", "pr", "vx", "vy", "by"]
+SOLVER_ID["mlw_m_bg_1d"] = 6
+# static profiles of mlw_m_bg (cans1d/hdmlw/mlw_m_bg.f:2-3), in the order the
+# run descriptor takes them
+BG_PROFILES = ["gx", "gxm", "sc", "scm", "dsc", "dscm", "rr", "rrm", "drr", "drrm"]
+
+
+def bd_host_1d(kind: int, mbnd: int, m: int, q: np.ndarray) -> None:
+    """One bd* rule on a host line in place (cans1d/bc/bdsppx.f, bdspnx.f,
+    bdsmpx.f, bdsmnx.f, bdfrex.f), for the set-up's static profiles.  The
+    indices below are the reference's 1-based ones."""
+    n = q.size
+
+    def get(i):
+        return q[i - 1]
+
+    def put(i, v):
+        q[i - 1] = v
+
+    if mbnd == 0:
+        b = 1 + m
+        for i in range(1, m + 1):
+            if kind == BD_SPP:
+                put(b - i, get(b - 1 + i))
+            elif kind == BD_SPN:
+                put(b - i, -get(b - 1 + i))
+            elif kind == BD_SMP:
+                put(b - i, get(b + i))
+            elif kind == BD_SMN:
+                put(b - i, -get(b + i))
+            elif kind == BD_FRE:
+                put(b - i, get(b))
+        if kind == BD_SMN:
+            put(b, 0.0)
+    else:
+        b = n - m
+        for i in range(1, m + 1):
+            if kind == BD_SPP:
+                put(b + i, get(b + 1 - i))
+            elif kind == BD_SPN:
+                put(b + i, -get(b + 1 - i))
+            elif kind == BD_SMP:
+                put(b + i, get(b - i))
+            elif kind == BD_SMN:
+                put(b + i, -get(b - i))
+            elif kind == BD_FRE:
+                put(b + i, get(b))
+        if kind == BD_SMN:
+            put(b, 0.0)
+
+
+def scrdy(sc: np.ndarray, scm: np.ndarray, dx: np.ndarray, dxm: np.ndarray):
+    """cans1d/common/scrdy.f:28-34: dsc(2..ix-1) and dscm(2..ix-2).  The
+    other entries are left at zero, the value the reference main program's
+    static arrays hold there."""
+    ix = sc.size
+    dsc = np.zeros(ix)
+    dscm = np.zeros(ix)
+    for i in range(2, ix):          # 1-based i = 2..ix-1
+        dsc[i - 1] = (scm[i - 1] - scm[i - 2]) / dx[i - 1]
+    for i in range(2, ix - 1):      # 1-based i = 2..ix-2
+        dscm[i - 1] = (sc[i] - sc[i - 1]) / dxm[i - 1]
+    return dsc, dscm
+
+
+def chkdav_host(da: np.ndarray, vx: np.ndarray, floor: float) -> int:
+    """cans1d/common/chkdav.f:68-76 on host arrays: values below `floor` are
+    raised to it and the velocity there set to zero; returns the count."""
+    low = da < floor
+    da[low] = floor
+    vx[low] = 0.0
+    return int(low.sum())
+
+
+def spicule_1d(nx: int = 1024, torque: float = 30.0, seed: int = 0, tend: float = 100.0,
+               nstop: int = 100000, dtout: float = 0.5):
+    """The spicule model: cans1d/md_spicule/hdmlw/model.f with the set-up
+    part of main.f (grdrdy, bnd, scrdy twice, bndsc, chkdav of ro and pr),
+    margin 1, ix = nx + 2.
+
+    Grid: dxm = 0.04 up to cell i1 = aint(2 ztr/dx0), then growing by 2 %
+    per cell up to 50 dx0; cell izero = 2 centred at dxm/2.  Gravity
+    -1/gm (1 - tanh((x-400)/10))/2 on cells and faces (both evaluated at the
+    cell position, model.f:104-110), then bdspnx / bdsmnx.  A temperature
+    step of width 0.5 at ztr = 15 from 1 to 300, hydrostatic density built
+    outward from the base cell with ro0 = 1, p = ro T / gm.  Flux tube:
+    rr = 1, bx uniform with beta = 1 at the bottom, cross section 1/bx.
+    Boundaries (bnd.f): bdsppx (vx: bdspnx) at the bottom, bdfrex at the top.
+    The loop (main.f:160-219): cfl_m with safety 0.8 and dtmin 1e-10,
+    mlw_m_bg with qav = 1, the torque source of trqalfven.f, bnd, chkdav of
+    ro and pr with floor 1e-9."""
+    margin = 1
+    ix = nx + 2 * margin
+    ztr = 15.0
+    gm = 5.0 / 3.0
+    # ---- grid (model.f:36-68) -------------------------------------------------
+    dx0 = 0.04
+    i1 = int(2.0 * ztr / dx0)
+    apx1 = 1.02
+    dxmax1 = 50.0 * dx0
+    dxm0 = np.full(ix, dx0)
+    if i1 < ix:
+        for i in range(i1 + 1, ix + 1):          # 1-based i1+1..ix
+            v = apx1 * dxm0[i - 2]
+            dxm0[i - 1] = dxmax1 if v > dxmax1 else v
+    bd_host_1d(BD_SMP, 0, margin - 1, dxm0)
+    izero = margin + 1
+    x = np.empty(ix)
+    x[izero - 1] = dxm0[izero - 1] / 2
+    for i in range(izero + 1, ix + 1):
+        x[i - 1] = x[i - 2] + dxm0[i - 2]
+    for i in range(izero - 1, 0, -1):
+        x[i - 1] = x[i] - dxm0[i - 1]
+    # ---- gravity (model.f:86-101) ---------------------------------------------
+    gl0 = 1.0 / gm
+    ro0, pr0, te0 = 1.0, 1.0 / gm, 1.0
+    tpho, wtr = te0, 0.5
+    zg0, wg0 = 400.0, 10.0
+    gx = -(gl0 * (1.0 - np.tanh((x - zg0) / wg0)) / 2)
+    gxm = gx.copy()
+    bd_host_1d(BD_SPN, 0, margin, gx)
+    bd_host_1d(BD_SMN, 0, margin - 1, gxm)
+    rr = np.ones(ix)
+    rrm = np.ones(ix)
+    # ---- hydrostatic atmosphere (model.f:113-148) ------------------------------
+    ac = 300.0
+    te = tpho * (1 + 0.5 * (ac - 1) * (np.tanh((x - ztr) / wtr) + 1.0))
+    ro1 = np.empty(ix)
+    i = izero + 1
+    h = 0.5 * gm * gxm[i - 2] * dxm0[i - 2] / 2
+    ro1[i - 1] = (te[i - 2] + h) / (te[i - 1] - h) * ro0
+    for i in range(izero + 2, ix + 1):
+        h = 0.5 * gm * gxm[i - 2] * dxm0[i - 2]
+        ro1[i - 1] = (te[i - 2] + h) / (te[i - 1] - h) * ro1[i - 2]
+    i = izero
+    h = 0.5 * gm * gxm[i - 1] * dxm0[i - 1] / 2
+    ro1[i - 1] = (te[i] - h) / (te[i - 1] + h) * ro0
+    for i in range(izero - 1, 0, -1):
+        h = 0.5 * gm * gxm[i - 1] * dxm0[i - 1]
+        ro1[i - 1] = ro1[i] * (te[i] - h) / (te[i - 1] + h)
+    pr1 = pr0 * (ro1 / ro0) * (te / te0)
+    # ---- field and flux tube (model.f:150-185) -------------------------------
+    pi = math.acos(-1.0)
+    onebeta = 1.0
+    bx = np.empty(ix)
+    bx[0] = math.sqrt(onebeta * 8 * pi * pr1[0])
+    bx[1:] = bx[0] * (rr[0] / rr[1:]) ** 2
+    bxm = np.empty(ix)
+    bxm[: ix - 1] = 0.5 * (bx[: ix - 1] + bx[1:])
+    bxm[ix - 1] = bxm[ix - 2]
+    sc = 1.0 / bx
+    scm = 1.0 / bxm
+    # ---- main.f:78-90: metrics, boundaries, cross-section derivatives ---------
+    dx, _, dxm = grdrdy(x)
+    f = {"ro": ro1.copy(), "pr": pr1.copy(), "vx": np.zeros(ix), "vy": np.zeros(ix),
+         "by": np.zeros(ix)}
+    bc = []
+    for v, name in enumerate(VARS["mlw_m_bg_1d"]):
+        bc.append((v, 0, BD_SPN if name == "vx" else BD_SPP, 0.0))
+    for v in range(5):
+        bc.append((v, 1, BD_FRE, 0.0))
+    for v, face, kind, _ in bc:
+        bd_host_1d(kind, face, margin, f[VARS["mlw_m_bg_1d"][v]])
+    dsc, dscm = scrdy(sc, scm, dx, dxm)
+    drr, drrm = scrdy(rr, rrm, dx, dxm)
+    # bndsc.f:9-19
+    bd_host_1d(BD_SPP, 0, margin, sc)
+    bd_host_1d(BD_SPN, 0, margin, dsc)
+    bd_host_1d(BD_SMP, 0, margin - 1, scm)
+    bd_host_1d(BD_SMN, 0, margin - 1, dscm)
+    bd_host_1d(BD_SPP, 1, margin, sc)
+    bd_host_1d(BD_SPN, 1, margin, dsc)
+    bd_host_1d(BD_SMP, 1, margin, scm)
+    bd_host_1d(BD_SMN, 1, margin, dscm)
+    floor = 1e-9
+    chkdav_host(f["ro"], f["vx"], floor)
+    chkdav_host(f["pr"], f["vx"], floor)
+    # torque profile of trqalfven.f:25-29 (the 0.075 is a real*4 literal)
+    trq = np.tanh((x - 0.75) / float(np.float32(0.075))) - 1
+    trq[ix - 1] = trq[ix - 3]
+    state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in VARS["mlw_m_bg_1d"]]
+    prof = dict(gx=gx, gxm=gxm, sc=sc, scm=scm, dsc=dsc, dscm=dscm, rr=rr, rrm=rrm,
+                drr=drr, drrm=drrm)
+    return dict(solver="mlw_m_bg_1d", solver_id=6, names=VARS["mlw_m_bg_1d"], x=x, dx=dx,
+                dxm=dxm, bx=bx, bxm=bxm, state=state, gm=gm, qav=1.0, margin=margin, bc=bc,
+                safety=0.8, dtmin=1e-10, tend=tend, nstop=nstop, dtout=dtout, floor=floor,
+                trq=trq, trq0=float(torque), seed=int(seed), ztr=ztr, tcor=200.0,
+                name=f"spicule_{nx}", **prof)
