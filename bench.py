@@ -160,6 +160,7 @@ def extra_workloads(stream, exact=False):
     for solver, safety in (("roe_m_3d", None), ("hlld_3d", 0.2)):
         out[f"turbulence_256^3_{solver}"] = riemann_3d(stream, solver, safety, exact)
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
+    out["spicule_1024_100000_steps_mlw_m_bg"] = spicule_workload(stream)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
     out["adjoint_shear_256^2_2000_steps"] = adjoint_workload(stream)
     return out
@@ -243,6 +244,53 @@ def hlld_brio_wu(stream, exact):
     run.close()
     return {"ms_to_tend": best, "steps": int(st.ns), "t": st.t, "merr": int(st.merr),
             "us_per_step": best * 1e3 / max(1, st.ns)}
+
+
+def spicule_workload(stream, nstop=100000, cpu_steps=4000):
+    """The reference's spicule run (cans1d/md_spicule/hdmlw: 1024 cells,
+    100000 iterations of cfl_m, mlw_m_bg, the random torque, bnd and chkdav)
+    as one cluster launch, in both arithmetic policies, against the output
+    the reference ships for this run (tests/golden/spicule_reference.npz:
+    the time reached and the ro, pr, vx profiles; vy and by follow the
+    random torque, whose stream differs) and against the oracle's loop
+    timed on a bounded sample of the same run on one host core."""
+    import torch
+    from utrip_gb300 import drivers, setups
+    import oracle
+    s = setups.spicule_1d()
+    gold = dict(np.load(ROOT / "tests" / "golden" / "spicule_reference.npz"))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res = {}
+    for policy, exact in (("fast", False), ("exact", True)):
+        run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+        run.push(s["state"])
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run.start(tend=s["tend"], nstop=nstop, safety=s["safety"], dtmin=s["dtmin"])
+        run.advance(nstop)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = run.query()
+        got = run.pull()
+        run.close()
+        t_ref = float(gold["t_records"][1])
+        l2 = {name: float(np.linalg.norm(got[k] - gold[f"{name}_records"][1]) /
+                          np.linalg.norm(gold[f"{name}_records"][1]))
+              for k, name in enumerate(s["names"]) if name in ("ro", "pr", "vx")}
+        res[policy] = {"ms": ms, "us_per_step": ms * 1e3 / max(1, st.ns), "steps": int(st.ns),
+                       "t": st.t, "merr": int(st.merr), "chkdav_events": int(st.n_floor),
+                       "zone_updates_per_s": 1024 * st.ns / (ms * 1e-3),
+                       "t_rel_diff_vs_reference_output": abs(st.t - t_ref) / t_ref,
+                       "rel_l2_vs_reference_output": l2}
+    ref = setups.copy_state(s)
+    t0 = time.perf_counter()
+    oracle.run_spicule_c(s, ref, cpu_steps)
+    cpu_s = time.perf_counter() - t0
+    res["cpu_oracle"] = {"us_per_step": cpu_s * 1e6 / cpu_steps, "cores": 1,
+                         "sample": f"first {cpu_steps} iterations of the same run"}
+    res["speedup_vs_cpu_oracle"] = res["cpu_oracle"]["us_per_step"] / res["fast"]["us_per_step"]
+    return res
 
 
 def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=1e-6):

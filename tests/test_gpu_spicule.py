@@ -134,13 +134,21 @@ def test_spicule_loop_with_floor_events_bitwise(gpu, oracle_lib):
     assert_bitwise(s["names"], got, ref, "floor loop")
 
 
-def test_spicule_loop_fast_within_tolerance(gpu, oracle_lib):
+@pytest.mark.parametrize("nsteps", [100, 1000])
+def test_spicule_loop_fast_within_tolerance(gpu, oracle_lib, nsteps):
+    """Fast policy against the oracle.  ro, pr, vy and by stay within 1e-10
+    (relative L-inf).  vx gets 1e-4: in the corona of this model the uniform
+    field's B^2/8pi is 1e6 times the gas pressure, so the last-bit rounding
+    of the total energy in any step reappears 1e6 times larger in p and
+    drives vx; injecting just that rounding into the oracle's own loop moves
+    vx by ~1e-5 (test_oracle.py::test_spicule_corona_amplifies_energy_rounding).
+    The exact policy equals the oracle bit for bit (the tests above)."""
     s = setups.spicule_1d(1024, seed=1)
     ref = setups.copy_state(s)
-    oracle.run_spicule_c(s, ref, 1000)
-    got, st = _loop_gpu(s, 1000, exact=False)
+    oracle.run_spicule_c(s, ref, nsteps)
+    got, st = _loop_gpu(s, nsteps, exact=False)
     for k, a, b in zip(s["names"], got, ref):
-        assert rel_linf(a, b) < 1e-10, k
+        assert rel_linf(a, b) < (1e-4 if k == "vx" else 1e-10), k
 
 
 def test_reference_spicule_run_exact_and_against_the_reference_output(gpu, oracle_lib):

@@ -581,3 +581,23 @@ def test_oracle_reproduces_the_reference_spicule_run(oracle_lib):
         else:
             ratio = np.sqrt(np.mean(st[k] ** 2) / np.mean(r ** 2))
             assert 0.3 < ratio < 3.0, (name, ratio)
+
+
+def test_spicule_corona_amplifies_energy_rounding(oracle_lib):
+    """The conditioning behind the fast-policy tolerance of the spicule loop:
+    perturbing the pressure each step by the rounding of the total energy
+    (one unit in the last place of e, times gm-1) moves vx by more than 1e-6
+    of its maximum within 100 steps, while ro and pr stay within 1e-12."""
+    s = setups.spicule_1d(1024, seed=1)
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    rng = np.random.default_rng(0)
+    ta = tb = 0.0
+    gm = s["gm"]
+    for k in range(100):
+        ta = oracle_lib.run_spicule_c(s, a, k + 1, t0=ta, ns0=k)[0]
+        tb = oracle_lib.run_spicule_c(s, b, k + 1, t0=tb, ns0=k)[0]
+        ro, pr, vx, vy, by = b
+        ee = pr / (gm - 1) + 0.5 * ro * (vx ** 2 + vy ** 2) + (s["bx"] ** 2 + by ** 2) / (8 * np.pi)
+        pr += (gm - 1) * ee * 1.1e-16 * rng.standard_normal(pr.size)
+    rel = [float(np.max(np.abs(x - y)) / np.max(np.abs(x))) for x, y in zip(a, b)]
+    assert rel[2] > 1e-6 and rel[0] < 1e-12 and rel[1] < 1e-12, rel

@@ -12,8 +12,10 @@
 // halo cell per side) in shared memory for the whole run; after each step
 // neighbours exchange halo cells through distributed shared memory and the
 // CFL minimum is reduced across the cluster, so no host round trip happens
-// per step.  Three cluster barriers per step: after the update, after the
-// boundary fill, after the halo exchange and CFL reduction.
+// per step.  One cluster barrier per step (the CFL reduction, which also
+// publishes the new cells for the halo exchange) when the boundary program
+// reads only the cells of the blocks that run it; a second one before the
+// boundary fill when a rule is periodic.
 //
 // The BG variant is mlw_m_bg (cans1d/hdmlw/mlw_m_bg.f:2-271): the same
 // two-stage step on the cross-section-weighted variables (ro, e, rx, ry r,
@@ -47,6 +49,7 @@ struct Run1D {
   unsigned long long seed;  // key of the torque's random stream
   double floor;          // chkdav floor of ro and pr (used when chk)
   int chk;
+  int bnd_local;         // 1: no boundary rule reads another block's cells
   Axis ax;
   Phys ph;
   BcTable bc;
@@ -504,11 +507,16 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
           P(nb, 3, nl - 1) = torque_add<E>(p, FT(P(nb, 3, nl - 1)), dt, ns_now, ix - 1).v;
       }
     }
-    cluster.sync();
     if (p.fixed) {
+      cluster.sync();
       cur = nb;
       break;
     }
+    // The boundary program reads only cells of the block that runs it unless
+    // a rule is periodic or reaches past that block's cells (bnd_local = 0);
+    // then it must wait for the whole cluster.
+    if (p.bnd_local) __syncthreads();
+    else cluster.sync();
     // ---- boundary program (bnd.f:9-19): lower face by block 0, upper face
     // by the last block; cells of other blocks are read through DSMEM -------
     if (tid < NV1 && (r == 0 || r == CS - 1)) {
@@ -537,7 +545,7 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
       if (r == CS - 1)
         bd1_face(p.bc.kind[v][1], 1, p.bc.margin, ix, p.bc.q0[v][1], ax.dm, get, put);
     }
-    cluster.sync();
+    __syncthreads();
     // ---- chkdav of ro, then pr (chkdav.f:68-76), every cell incl. ghosts ----
     if (p.chk) {
       unsigned int nev = 0;
@@ -555,9 +563,12 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
         }
       }
       if (nev) atomicAdd(&p.ctl->nfloor, (unsigned long long)nev);
-      cluster.sync();
+      __syncthreads();
     }
-    // ---- halo exchange and CFL of the new state ----------------------------
+    // ---- CFL of the own cells, reduced over the cluster; its cluster barrier
+    // also publishes every block's final cells for the halo exchange ---------
+    const double dtn = cluster_cfl(nb, par);
+    par ^= 1;
     if (tid < NV1) {
       if (r > 0) {
         const double *nbp = cluster.map_shared_rank(prim, r - 1);
@@ -569,9 +580,6 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
         P(nb, tid, nl - 1) = nbp[(size_t)nb * NVS + (size_t)tid * L + 1];
       }
     }
-    __syncthreads();
-    const double dtn = cluster_cfl(nb, par);
-    par ^= 1;
     cur = nb;
     if (tid == 0) {
       // end of the loop body (main.f:155-199) and start of the next
@@ -692,6 +700,12 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
   p.start = start;
   // each block must own at least margin+1 cells for the boundary rules
   if (p.q < bc.margin + 1) return cudaErrorInvalidValue;
+  // a face rule reads at most 2*margin cells in from its end of the line
+  // (bdsmp*: cell b+margin); block 0 and the last block own at least q cells
+  p.bnd_local = 2 * bc.margin <= p.q ? 1 : 0;
+  for (int v = 0; v < NV1; v++)
+    for (int f = 0; f < 2; f++)
+      if (bc.kind[v][f] == BD_PER) p.bnd_local = 0;
   const size_t smem = sizeof(double) * (per_cell * p.lmax + 2 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
