@@ -5,10 +5,13 @@ the same Python signatures as utrip_gb300.capi, plus a restatement of the
 model-package time loop (cans2d/md_mhdkh/hdmlw/main.f:160-219).  Only the
 tests, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use it.
 
-Parity status: parity unpinned against the Fortran itself (no Fortran
-compiler is available and the reference ships no golden vectors for this
-path); the restatement is pinned by invariants and frozen fixtures in
-tests/golden/.
+Parity status: the 1-D spicule loop (mlw_m_bg, chkdav, torque, bnd) is
+pinned against the output the reference ships for its spicule run
+(tests/golden/spicule_reference.npz, checked in tests/test_oracle.py and
+tests/test_dac.py).  The other routines are parity unpinned against the
+Fortran itself (no Fortran compiler is available and the reference ships no
+golden vectors for them); they are pinned by invariants and frozen fixtures
+in tests/golden/.
 """
 from __future__ import annotations
 

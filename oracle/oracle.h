@@ -6,12 +6,17 @@
  * used by the test-suite as the checker, by __graft_entry__.smoke() and by the
  * CPU-baseline leg of bench.py.  No product code path links or calls it.
  *
- * Parity status: parity unpinned against the Fortran itself.  No Fortran
- * compiler exists in the build or GPU environment and the reference ships no
- * golden vectors for mlw_m / mlw_m3 / cfl_m, so the restatement is pinned by
- * hand-checkable invariants instead (uniform-state invariance, mirror
- * symmetry, exact periodic conservation, linear-wave phase speed) and by the
- * committed fixtures in tests/golden/ that freeze its own outputs.
+ * Parity status.  The 1-D spicule loop (mlw_m_bg, chkdav, the torque, the
+ * boundary program) is pinned against the output the reference ships for its
+ * spicule run (tests/golden/spicule_reference.npz): the set-up to the last
+ * bits of an 80-bit evaluation, the 100000-step run to 2.6e-8 in time and
+ * 2e-4 in the density and pressure profiles.  The other routines are parity
+ * unpinned against the Fortran itself: no Fortran compiler exists in the
+ * build or GPU environment and the reference ships no golden vectors for
+ * mlw_m / mlw_m3 / roe_m / HLLD, so they are pinned by hand-checkable
+ * invariants instead (uniform-state invariance, mirror symmetry, exact
+ * periodic conservation, axis rotation) and by the committed fixtures in
+ * tests/golden/ that freeze their outputs.
  *
  * Fidelity rules followed throughout:
  *   - same loop bounds and the same left-to-right operation order as the
