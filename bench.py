@@ -159,6 +159,7 @@ def extra_workloads(stream, exact=False):
     # ---- 3-D Roe-MUSCL and HLLD steps on the same turbulence box (margin 3)
     for solver, safety in (("roe_m_3d", None), ("hlld_3d", 0.2)):
         out[f"turbulence_256^3_{solver}"] = riemann_3d(stream, solver, safety, exact)
+    out["orszag_tang_512^2_roe_m3"] = roe_2d(stream, exact)
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
     out["spicule_1024_100000_steps_mlw_m_bg"] = spicule_workload(stream)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
@@ -197,6 +198,43 @@ def riemann_3d(stream, solver, safety, exact, iters=10):
             "steps_done": int(st.nexec), "merr": int(st.merr),
             "policy": "exact" if exact else "fast",
             "cpu_oracle": cpu_sample_3d(solver, safety)}
+
+
+def roe_2d(stream, exact, n=512, iters=50, cpu_n=256, cpu_steps=300):
+    """The 2-D Roe-MUSCL step (roe_m3, margin 2) on the Orszag-Tang vortex of
+    the headline, loop iterations timed with events (graph), the four step
+    kernels profiled; the oracle on a bounded sample (cpu_n^2, all host
+    threads) beside it."""
+    import torch
+    import oracle
+    from utrip_gb300 import drivers, setups
+    s = setups.orszag_tang(n, solver="roe_m3")
+    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    run.push(s["state"])
+    run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+    run.advance(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run.advance(iters)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    step_ms, _ = run.profile(10)
+    st = run.query()
+    run.close()
+    c = setups.orszag_tang(cpu_n, solver="roe_m3")
+    cs = setups.copy_state(c)
+    t0 = time.perf_counter()
+    oracle.run_2d(c, cs, cpu_steps)
+    el = time.perf_counter() - t0
+    return {"zone_updates_per_s": n * n * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+            "step_kernels_ms": step_ms / 10, "bound": "fp64", "steps_done": int(st.nexec),
+            "merr": int(st.merr), "policy": "exact" if exact else "fast",
+            "cpu_oracle": {"zone_updates_per_s": cpu_n * cpu_n * cpu_steps / el,
+                           "cores": oracle.get_threads(), "kind": "port",
+                           "sample": f"{cpu_steps} loop iterations of the {cpu_n}^2 vortex "
+                                     f"in {el:.2f} s"}}
 
 
 def cpu_sample_3d(solver, safety, n=96, steps=2):

@@ -236,6 +236,14 @@ int cans_roe_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                   const double *gm, const double *dx, const int *ix,
                   const double *dy, const int *jx, const double *dz,
                   const int *kx);
+/* replaces subroutine roe_m3  (cans2d/hdroe/roe_m3.f:1): one 2-D Roe-MUSCL
+ * step (roeflux_m3.f, tvdminmod.f of cans2d/hdroe) on the 9 arrays,
+ * az advanced by the half-step E_z; cells 3..n-2 are updated (margin 2 or 3
+ * as the md_mhdkh / md_mhd3shktb Roe packages).  Extents must be >= 5. */
+int cans_roe_m3_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                   double *bx, double *by, double *bz, double *az,
+                   const double *dt, const double *gm, const double *dx,
+                   const int *ix, const double *dy, const int *jx);
 
 /* ------------------------------------------------------------------------ */
 /* 2. Residency registry                                                     */
@@ -264,6 +272,7 @@ int cans_gpu_release(const double *any);
 #define CANS_SOLVER_HLLD_3D 5    /* HLLD engine: ro,pr,vx,vy,vz,bx,by,bz     */
 #define CANS_SOLVER_MLW_M_BG_1D 6 /* mlw_m_bg 1-D: ro,pr,vx,vy,by (+ bx, bxm
                                     and the ten gravity / flux-tube profiles) */
+#define CANS_SOLVER_ROE_M3_2D 7  /* roe_m3 2-D: ro,pr,vx,vy,vz,bx,by,bz,az    */
 
 /* Boundary kinds, one per reference bd* family. */
 #define CANS_BD_NONE (-1)

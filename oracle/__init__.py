@@ -57,6 +57,7 @@ def load():
         lib.oracle_mlw_m_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, _dp, i, _dp, _dp, i, _dp, _dp, i]
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
+        lib.oracle_roe_m3_2d.argtypes = [_dp] * 9 + [d, d, _dp, i, _dp, i]
         lib.oracle_hlld_engine_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, i, _dp, i, _dp, i, _ip]
         lib.oracle_mlw_m_bg_1d.argtypes = [_dp] * 7 + [d, d, d] + [_dp] * 12 + [i]
         lib.oracle_chkdav.argtypes = [_dp, _dp, d, i]
@@ -153,7 +154,17 @@ def apply_bc_program(state, program, margin, grid=None):
                 bd(kind, axis, face % 2, margin, state[var], q0, dxm)
 
 
+def roe_m3(ro, pr, vx, vy, vz, bx, by, bz, az, dt, gm, dx, dy):
+    """cans2d/hdroe/roe_m3.f:1"""
+    ix, jx = ro.shape
+    load().oracle_roe_m3_2d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)], dt, gm,
+                            P(dx), ix, P(dy), jx)
+
+
 def step_2d(setup, state, dt):
+    if setup["solver"] == "roe_m3":
+        roe_m3(*state, dt, setup["gm"], setup["dx"], setup["dy"])
+        return
     args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
     if setup["solver"] == "mlw_m3":
         mlw_m3(*state, dt, *args)
@@ -162,7 +173,7 @@ def step_2d(setup, state, dt):
 
 
 def cfl_2d(setup, state, safety):
-    if setup["solver"] == "mlw_m3":
+    if setup["solver"] in ("mlw_m3", "roe_m3"):
         return cfl_m3(safety, setup["dtmin"], setup["gm"], *state[:8], setup["dx"], setup["dy"])
     return cfl_m(safety, setup["dtmin"], setup["gm"], *state[:6], setup["dx"], setup["dy"])
 

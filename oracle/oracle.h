@@ -132,6 +132,11 @@ void oracle_roe_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                      const double *dx, int ix, const double *dy, int jx,
                      const double *dz, int kx);
 
+/* 2-D Roe-MUSCL step roe_m3 (cans2d/hdroe/roe_m3.f:1) on ix*jx arrays. */
+void oracle_roe_m3_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                      double *bx, double *by, double *bz, double *az, double dt,
+                      double gm, const double *dx, int ix, const double *dy, int jx);
+
 /* HLLD step of the cansxx engine (cansxx-nosupport/md_mhdshktb/hdhlld-x/
  * engine.f:2), Heaviside units with permeability mu; mfdim[3] marks the
  * active axes (1) as in the reference.  See hlld.c for the two places where

@@ -47,4 +47,7 @@ static inline double *arena_get(oracle_arena *a, size_t total) {
   return a->buf;
 }
 
+/* Roe flux of one face (roe3d.c), shared by the 3-D and 2-D steps. */
+void oracle_roe_face(double gm, const double *L, const double *R, double *f, int fix);
+
 #endif

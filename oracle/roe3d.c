@@ -34,8 +34,10 @@ static inline double fsign(double a, double b) { return copysign(fabs(a), b); }
 
 /* roeflux_m.f:29-263 for one face.  L and R hold (ro, pr, vn, vt1, vt2, bn,
  * bt1, bt2) of the two sides in the frame of the face normal; f receives
- * (fro, fee, frn, frt1, frt2, fbt1, fbt2). */
-static void roe_face(double gm, const double *L, const double *R, double *f) {
+ * (fro, fee, frn, frt1, frt2, fbt1, fbt2).  fix = 1 is the 3-D routine;
+ * fix = 0 is roeflux_m3.f of cans1d/cans2d, whose slow-wave normalisation
+ * lacks the "+ 1 - sp2" of roeflux_m.f:79 (cans2d/hdroe/roeflux_m3.f:77). */
+void oracle_roe_face(double gm, const double *L, const double *R, double *f, int fix) {
   const double pi = acos(-1.0);
   const double pi4 = 4.0 * pi;
   const double pi4i = 1.0 / pi4;
@@ -97,7 +99,8 @@ static void roe_face(double gm, const double *L, const double *R, double *f) {
   double cfcs = fmax2(0.0, cfast2 - cslow2);
   double cfa = fmax2(0.0, cfast2 - cs2);
   double alphf = sp2 * sqrt(cfca / (cfcs + 1.0 - sp2)) + 1.0 - sp2;
-  double alphs = sp2 * sqrt(cfa / (cfcs + 1.0 - sp2)) + 1.0 - sp2;
+  double alphs = sp2 * sqrt(cfa / (cfcs + 1.0 - sp2));
+  if (fix) alphs = alphs + 1.0 - sp2;
   double sgnbx = fsign(1.0, bxbar);
 
   /* eigen value & entropy condition (:103-110) */
@@ -267,7 +270,7 @@ static void roeflux_axis(double *const *fl, double gm, const double *const *wl,
           R[2 + m] = wr[V_VX + r[m]][c];
           R[5 + m] = wr[V_BX + r[m]][c];
         }
-        roe_face(gm, L, R, f);
+        oracle_roe_face(gm, L, R, f, 1);
         fl[F_RO][c] = f[0];
         fl[F_EE][c] = f[1];
         for (int m = 0; m < 3; m++) fl[F_RX + r[m]][c] = f[2 + m];

@@ -1,6 +1,6 @@
 """Generate the frozen oracle fixtures in this directory.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [name ...]
 The fixtures freeze the CPU oracle's outputs on small seeded inputs so that a
 change to the oracle (and through it the exact-mode GPU parity) is caught.
 """
@@ -70,10 +70,23 @@ def case_hlld(ix, jx, kx, seed):
     return out
 
 
-def main():
-    oracle.build()
-    np.savez_compressed(OUT / "mlw_m3_2d_18x14.npz", **case_2d("mlw_m3", 18, 14, 11, 10))
-    np.savez_compressed(OUT / "mlw_m_2d_16x20.npz", **case_2d("mlw_m", 16, 20, 12, 10))
+def case_roe2(ix, jx, seed):
+    """One 2-D Roe-MUSCL step (cans2d/hdroe/roe_m3.f) of a seeded state,
+    margin 2 as the md_mhdkh Roe package."""
+    s = setups.random_state(ix, jx, seed=seed, solver="roe_m3")
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dy"):
+        out["grid_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_2d(s, st, 0.4)
+    oracle.roe_m3(*st, dt, s["gm"], s["dx"], s["dy"])
+    out.update({"dt": np.array(dt), "gm": np.array(s["gm"])})
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
+def bd_case():
     rng = np.random.default_rng(13)
     q = np.asfortranarray(rng.standard_normal((9, 7)))
     dxm = np.linspace(0.1, 0.2, 9)
@@ -85,11 +98,26 @@ def main():
                 a = q.copy(order="F")
                 oracle.bd(kind, axis, mbnd, 2, a, q0=0.75, dxm=dxm if axis == 0 else dym)
                 bc[f"k{kind}_a{axis}_m{mbnd}"] = a
-    np.savez_compressed(OUT / "bd_2d_9x7.npz", q=q, dxm=dxm, dym=dym, **bc)
-    np.savez_compressed(OUT / "roe_m_3d_14x12x13.npz", **case_roe(14, 12, 13, 21))
-    np.savez_compressed(OUT / "hlld_3d_13x11x12.npz", **case_hlld(13, 11, 12, 22))
-    print("wrote fixtures to", OUT)
+    return dict(q=q, dxm=dxm, dym=dym, **bc)
+
+
+FIXTURES = {
+    "mlw_m3_2d_18x14": lambda: case_2d("mlw_m3", 18, 14, 11, 10),
+    "mlw_m_2d_16x20": lambda: case_2d("mlw_m", 16, 20, 12, 10),
+    "bd_2d_9x7": bd_case,
+    "roe_m_3d_14x12x13": lambda: case_roe(14, 12, 13, 21),
+    "hlld_3d_13x11x12": lambda: case_hlld(13, 11, 12, 22),
+    "roe_m3_2d_17x15": lambda: case_roe2(17, 15, 23),
+}
+
+
+def main(names):
+    """Write the named fixtures (all of them when none is named)."""
+    oracle.build()
+    for name in names or FIXTURES:
+        np.savez_compressed(OUT / f"{name}.npz", **FIXTURES[name]())
+        print("wrote", OUT / f"{name}.npz")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

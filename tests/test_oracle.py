@@ -601,3 +601,107 @@ def test_spicule_corona_amplifies_energy_rounding(oracle_lib):
         pr += (gm - 1) * ee * 1.1e-16 * rng.standard_normal(pr.size)
     rel = [float(np.max(np.abs(x - y)) / np.max(np.abs(x))) for x, y in zip(a, b)]
     assert rel[2] > 1e-6 and rel[0] < 1e-12 and rel[1] < 1e-12, rel
+
+
+# ---- 2-D roe_m3 ---------------------------------------------------------------
+
+def _roe2(ix=16, jx=14, seed=3):
+    """Periodic 2-D Roe grid with margin 3 (md_mhd3shktb/hdroe/main.f:5):
+    the cells whose faces read the outer layer of half-step primitives are
+    then boundary cells, so the invariants hold over the interior."""
+    s = setups.random_state(ix, jx, seed=seed, solver="roe_m3", margin=3)
+    # one spacing per axis to the last bit, so that translations are exact
+    s["dx"] = np.full(ix, s["dx"][3])
+    s["dy"] = np.full(jx, s["dy"][3])
+    st = setups.copy_state(s)
+    s["bc"] = [(v, f, 0, 0.0) for v in range(9) for f in range(4)]  # periodic
+    oracle_lib_mod().apply_bc_program(st, s["bc"], s["margin"], s)
+    return s, st
+
+
+def oracle_lib_mod():
+    import oracle
+    return oracle
+
+
+def test_roe2d_uniform_state_changes_only_by_rounding(oracle_lib):
+    s, _ = _roe2()
+    vals = [1.1, 0.6, 0.1, -0.2, 0.05, 1.5, 0.7, 0.3, 0.25]
+    st = [np.asfortranarray(np.full(s["state"][0].shape, v)) for v in vals]
+    ref = [a.copy() for a in st]
+    oracle_lib.roe_m3(*st, 1e-3, s["gm"], s["dx"], s["dy"])
+    for k, a, b in zip(s["names"][:8], st, ref):
+        assert float(np.max(np.abs(a - b))) <= 4e-16 * max(1.0, float(np.max(np.abs(b)))), k
+
+
+def test_roe2d_translation_commutes_with_step(oracle_lib):
+    s, st = _roe2(18, 16)
+    m = s["margin"]
+    inner = (slice(m, -m),) * 2
+    sh = [np.asfortranarray(np.pad(np.roll(a[inner], (5, 3), axis=(0, 1)), m)) for a in st]
+    oracle_lib.apply_bc_program(sh, s["bc"], m, s)
+    for _ in range(2):
+        for z in (st, sh):
+            oracle_lib.roe_m3(*z, 2e-3, s["gm"], s["dx"], s["dy"])
+            oracle_lib.apply_bc_program(z, s["bc"], m, s)
+    for k, a, b in zip(s["names"], st, sh):
+        assert np.array_equal(np.roll(a[inner], (5, 3), axis=(0, 1)), b[inner]), k
+
+
+def test_roe2d_axis_swap(oracle_lib):
+    """x <-> y of coordinates and vector components (az -> -az) commutes with
+    the step to rounding: checks the swap of roe_m3.f:106-107 and the
+    normal-B rule of each axis."""
+    s, st = _roe2(16, 16, seed=8)
+    s["dy"] = s["dx"].copy()
+
+    def swap(q):
+        ro, pr, vx, vy, vz, bx, by, bz, az = q
+        t = lambda a: np.asfortranarray(a.T)  # noqa: E731
+        return [t(ro), t(pr), t(vy), t(vx), t(vz), t(by), t(bx), t(bz), -t(az)]
+
+    sw = swap(st)
+    for z in (st, sw):
+        oracle_lib.roe_m3(*z, 3e-3, s["gm"], s["dx"], s["dy"])
+    for k, a, b in zip(s["names"], swap(st), sw):
+        assert float(np.max(np.abs(a - b))) <= 1e-14 * float(np.max(np.abs(b))), k
+
+
+def test_roe2d_one_dimensional_state_stays_one_dimensional(oracle_lib):
+    s, _ = _roe2(16, 12, seed=2)
+    st = [np.asfortranarray(np.broadcast_to(a[:, 6:7], a.shape).copy()) for a in s["state"]]
+    oracle_lib.roe_m3(*st, 2e-3, s["gm"], s["dx"], s["dy"])
+    for k, a in zip(s["names"], st):
+        rows = a[:, 2:-2]  # the rows the step updates (3..jx-2)
+        assert np.array_equal(rows, np.broadcast_to(rows[:, :1], rows.shape)), k
+
+
+def test_roe2d_periodic_conservation(oracle_lib):
+    s, st = _roe2(20, 18, seed=5)
+    m = s["margin"]
+    inner = (slice(m, -m),) * 2
+    dx, dy = s["dx"][m:-m], s["dy"][m:-m]
+    vol = np.outer(dx, dy)
+
+    def totals(q):
+        ro, pr, vx, vy, vz, bx, by, bz, az = [a[inner] for a in q]
+        ee = pr / (s["gm"] - 1) + 0.5 * ro * (vx ** 2 + vy ** 2 + vz ** 2) + \
+            (bx ** 2 + by ** 2 + bz ** 2) / (8 * math.pi)
+        return [float(np.sum(x * vol)) for x in (ro, ee, ro * vx, ro * vy, ro * vz, bx, by, bz)]
+
+    t0 = totals(st)
+    for _ in range(3):
+        oracle_lib.roe_m3(*st, 2e-3, s["gm"], s["dx"], s["dy"])
+        oracle_lib.apply_bc_program(st, s["bc"], m, s)
+    t1 = totals(st)
+    for a, b in zip(t0, t1):
+        assert abs(a - b) <= 1e-12 * max(1.0, abs(a))
+
+
+def test_roe2d_oracle_matches_frozen_fixture(oracle_lib):
+    z = np.load(GOLD / "roe_m3_2d_17x15.npz")
+    names = setups.VARS["roe_m3"]
+    st = [np.asfortranarray(z["in_" + k]) for k in names]
+    oracle_lib.roe_m3(*st, float(z["dt"]), float(z["gm"]), z["grid_dx"], z["grid_dy"])
+    for k, a in zip(names, st):
+        assert np.array_equal(a, z["out_" + k]), k

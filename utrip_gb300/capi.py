@@ -30,6 +30,7 @@ SOLVER_MLW_M_1D = 3
 SOLVER_ROE_M_3D = 4
 SOLVER_HLLD_3D = 5
 SOLVER_MLW_M_BG_1D = 6
+SOLVER_ROE_M3_2D = 7
 
 BD_NONE, BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(-1, 8)
 
@@ -96,6 +97,7 @@ def load() -> C.CDLL:
     sig["cans_cfl_m_3d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 +
                             [_dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_roe_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _ip, _dp, _ip, _dp, _ip])
+    sig["cans_roe_m3_2d"] = (i, [_dp] * 9 + [_dp, _dp, _dp, _ip, _dp, _ip])
     sig["cans_hlld_engine_3d"] = (i, [_dp] * 8 + [_dp] * 9 + [_ip] * 4)
     sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
     sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
@@ -338,6 +340,15 @@ def hlld_engine_3d(ro, pr, vx, vy, vz, bx, by, bz, gm, mu, dt, dx, dxm, dy, dym,
         _iref(kx), C.cast(md, _ip)), "hlld_engine_3d")
 
 
+def roe_m3(ro, pr, vx, vy, vz, bx, by, bz, az, dt, gm, dx, dy):
+    """cans2d/hdroe/roe_m3.f:1 -- one 2-D Roe-MUSCL step of the nine arrays,
+    in place."""
+    ix, jx = ro.shape
+    return _check(load().cans_roe_m3_2d(*[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)],
+                                        _dref(dt), _dref(gm), _ptr(dx), _iref(ix), _ptr(dy),
+                                        _iref(jx)), "roe_m3")
+
+
 def roe_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, gm, dx, dy, dz):
     """cans3d/hdroe/roe_m.f:2 -- one Roe-MUSCL step of the 3-D state, in place
     (cells 3..n-2 updated, the others kept)."""
@@ -428,7 +439,7 @@ class Run:
         self.solver = solver
         self.nvar = {SOLVER_MLW_M_2D: 7, SOLVER_MLW_M3_2D: 9, SOLVER_MLW_M_3D: 8,
                      SOLVER_MLW_M_1D: 5, SOLVER_ROE_M_3D: 8, SOLVER_HLLD_3D: 8,
-                     SOLVER_MLW_M_BG_1D: 5}[solver]
+                     SOLVER_MLW_M_BG_1D: 5, SOLVER_ROE_M3_2D: 9}[solver]
         three = solver in (SOLVER_MLW_M_3D, SOLVER_ROE_M_3D, SOLVER_HLLD_3D)
         one = solver in (SOLVER_MLW_M_1D, SOLVER_MLW_M_BG_1D)
         bgv = solver == SOLVER_MLW_M_BG_1D

@@ -94,6 +94,13 @@ cudaError_t launch_roe3d(bool exact, const double *A, double *B,
                          const Phys &ph, double dt, Ctl *ctl, Box3 box,
                          cudaStream_t s);
 
+// 2-D roe_m3 (9 arrays ro,pr,vx,vy,vz,bx,by,bz,az of ix*jx); A -> B, cells
+// outside 3..n-2 copied; scratch of roe3d_scratch_doubles(ix*jx).
+cudaError_t launch_roe2d(bool exact, const double *A, double *B,
+                         double *scratch, int ix, int jx, const Axis &ax,
+                         const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
+                         Box3 box, cudaStream_t s);
+
 // ---- 3-D HLLD (cansxx engine) ----------------------------------------------
 // One two-stage HLLD step on 8 arrays (Heaviside units, permeability mu);
 // A -> B for every cell.  mfdim[a] = 1 marks an active axis.  scratch holds

@@ -825,6 +825,51 @@ extern "C" int cans_roe_m_3d(double *ro, double *pr, double *vx, double *vy,
   return CANS_OK;
 }
 
+// roe_m3 (cans2d/hdroe/roe_m3.f:1): one 2-D Roe-MUSCL step on the nine
+// arrays, on the registered mirrors when they are a resident set.
+extern "C" int cans_roe_m3_2d(double *ro, double *pr, double *vx, double *vy,
+                              double *vz, double *bx, double *by, double *bz,
+                              double *az, const double *dt, const double *gm,
+                              const double *dx, const int *ix,
+                              const double *dy, const int *jx) {
+  if (!ro || !pr || !vx || !vy || !vz || !bx || !by || !bz || !az || !dt || !gm ||
+      !dx || !dy || !ix || !jx)
+    return CANS_ERR_ARG;
+  const int nx = *ix, ny = *jx;
+  if (nx < 5 || ny < 5) return CANS_ERR_ARG;
+  double *arrs[9] = {ro, pr, vx, vy, vz, bx, by, bz, az};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  const Phys ph = make_phys(*gm, 0.0);
+  const size_t n = (size_t)nx * ny;
+  MirrorSet *m = resident_step_set(arrs, 9);
+  Scratch &sc = g_scratch;
+  DevAxis *dax = m ? &m->ax : &sc.ax, *day = m ? &m->ay : &sc.ay;
+  // roe_m3 reads dx, dy only
+  if ((rc = dax->upload(nx, dx, dx, s))) return rc;
+  if ((rc = day->upload(ny, dy, dy, s))) return rc;
+  if ((rc = sc.ensure_roe(roe3d_scratch_doubles(n)))) return rc;
+  if (m) {
+    CK(launch_roe2d(exact_mode(), m->buf[m->cur], m->buf[m->cur ^ 1], sc.roe, nx, ny,
+                    dax->a, day->a, ph, *dt, nullptr, Box3{}, s));
+    m->cur ^= 1;
+    return CANS_OK;
+  }
+  if ((rc = sc.ensure(9 * n))) return rc;
+  for (int v = 0; v < 9; v++)
+    CK(cudaMemcpyAsync(sc.A + v * n, arrs[v], sizeof(double) * n,
+                       cudaMemcpyHostToDevice, s));
+  CK(launch_roe2d(exact_mode(), sc.A, sc.B, sc.roe, nx, ny, dax->a, day->a, ph, *dt,
+                  nullptr, Box3{}, s));
+  for (int v = 0; v < 9; v++)
+    CK(cudaMemcpyAsync(arrs[v], sc.B + v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
 // engine (cansxx-nosupport/md_mhdshktb/hdhlld-x/engine.f:2): one HLLD step,
 // on the registered mirrors when the 8 arrays are a resident set.
 extern "C" int cans_hlld_engine_3d(double *ro, double *pr, double *vx,
@@ -1047,6 +1092,7 @@ int solver_nvar(int solver) {
     case CANS_SOLVER_ROE_M_3D: return 8;
     case CANS_SOLVER_HLLD_3D: return 8;
     case CANS_SOLVER_MLW_M_BG_1D: return 5;
+    case CANS_SOLVER_ROE_M3_2D: return 9;
     default: return 0;
   }
 }
@@ -1056,7 +1102,14 @@ int solver_ndim(int solver) {
     return 3;
   return (solver == CANS_SOLVER_MLW_M_1D || solver == CANS_SOLVER_MLW_M_BG_1D) ? 1 : 2;
 }
-bool is_roe(const cans_run *h) { return h->d.solver == CANS_SOLVER_ROE_M_3D; }
+bool is_roe(const cans_run *h) {
+  return h->d.solver == CANS_SOLVER_ROE_M_3D || h->d.solver == CANS_SOLVER_ROE_M3_2D;
+}
+// the 2-D kernels other than the step take the mlw_m3 layout (9 arrays,
+// cfl_m3): the Roe 2-D state is the same
+int layout2d(const cans_run *h) {
+  return h->d.solver == CANS_SOLVER_ROE_M3_2D ? CANS_SOLVER_MLW_M3_2D : h->d.solver;
+}
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
   if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
@@ -1090,6 +1143,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
     return launch_hlld3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
                          h->mfdim, h->ax.a, h->ay.a, h->az.a, h->ph.gm, h->mu, dt,
                          ctl, h->s);
+  if (is_roe(h) && h->ndim == 2)
+    return launch_roe2d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->ax.a,
+                        h->ay.a, h->ph, dt, ctl, box, h->s);
   if (is_roe(h))
     return launch_roe3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
@@ -1113,7 +1169,7 @@ cudaError_t frame_kernel(cans_run *h) {
   if (h->ndim == 3)
     return launch_frame3d(h->d.exact != 0, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
                           h->ay.a, h->az.a, h->ph, h->bc.margin, h->ctl, h->s);
-  return launch_frame2d(h->d.solver, h->d.exact != 0, nullptr, h->d.ix, h->d.jx,
+  return launch_frame2d(layout2d(h), h->d.exact != 0, nullptr, h->d.ix, h->d.jx,
                         h->ax.a, h->ay.a, h->ph, h->bc.margin, h->ctl, h->s);
 }
 cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
@@ -1121,7 +1177,7 @@ cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
   if (h->ndim == 3)
     return launch_cfl3d_full(h->d.exact != 0, S, h->d.ix, h->d.jx, h->d.kx,
                              h->ax.a, h->ay.a, h->az.a, h->ph, safety, bits, h->s);
-  return launch_cfl2d_full(h->d.solver, h->d.exact != 0, S, h->d.ix, h->d.jx,
+  return launch_cfl2d_full(layout2d(h), h->d.exact != 0, S, h->d.ix, h->d.jx,
                            h->ax.a, h->ay.a, h->ph, safety, bits, h->s);
 }
 
@@ -1188,6 +1244,8 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   // the Roe step updates 3..n-2 and its stencil reaches three cells, so the
   // boundary program must rewrite three layers (hdroe/main.f:5)
   if (d->solver == CANS_SOLVER_ROE_M_3D && d->margin < 3) return CANS_ERR_ARG;
+  // the 2-D roe_m3 updates 3..n-2: the md_mhdkh Roe package uses margin 2
+  if (d->solver == CANS_SOLVER_ROE_M3_2D && d->margin < 2) return CANS_ERR_ARG;
   const int ndim = solver_ndim(d->solver);
   // HLLD: active axes from mfdim (all 0: every axis longer than one cell);
   // an inactive axis may have any extent, an active one needs the stencil

@@ -8,6 +8,11 @@
 // bt1, bt2).  roe_m.f:96,146,196 rotates (x,y,z) -> (y,z,x) -> (z,x,y) for
 // the y and z faces, a cyclic rotation, so one routine serves all axes.
 //
+// FIX selects the slow-wave normalisation: cans3d/hdroe/roeflux_m.f:79 (the
+// 2006 fix) has alphs = sp2 sqrt(cfa/(cfcs+1-sp2)) + 1 - sp2; the 1-D and
+// 2-D roeflux_m3.f:77 keep alphs = sp2 sqrt(cfa/(cfcs+1-sp2)).  Otherwise the
+// three routines evaluate the same expressions.
+//
 // Policy E=true evaluates every expression in the order the Fortran does,
 // with separately rounded operations (bit-identical to a -ffp-contract=off
 // build of the same expressions).  E=false is the fast policy: the same
@@ -44,7 +49,7 @@ template <bool E> __device__ __forceinline__ F<E> flmt(F<E> a, F<E> b) {
   return fmax_(F<E>(0.0), fmin_(b * s, fabs_(a))) * s;
 }
 
-template <bool E>
+template <bool E, bool FIX = true>
 __device__ __forceinline__ void roe_flux_ref(const RoeK &K, const double *L,
                                              const double *R, double *f) {
   using T = F<E>;
@@ -100,7 +105,8 @@ __device__ __forceinline__ void roe_flux_ref(const RoeK &K, const double *L,
   const T cfcs = fmax_(T(0.0), cfast2 - cslow2);
   const T cfa = fmax_(T(0.0), cfast2 - cs2);
   const T alphf = sp2 * fsqrt(cfca / (cfcs + T(1.0) - sp2)) + T(1.0) - sp2;
-  const T alphs = sp2 * fsqrt(cfa / (cfcs + T(1.0) - sp2)) + T(1.0) - sp2;
+  T alphs = sp2 * fsqrt(cfa / (cfcs + T(1.0) - sp2));
+  if constexpr (FIX) alphs = alphs + T(1.0) - sp2;
   const T sgnbx = fsign_(T(1.0), bxbar);
   // eigen value & entropy condition (:103-110)
   const T eeps = (vxr - vxl + fabs_(vxr - vxl)) * T(2.5e-1);
@@ -237,6 +243,7 @@ __device__ __forceinline__ double sqrt_(double x) {
 }
 __device__ __forceinline__ double max_(double a, double b) { return a > b ? a : b; }
 
+template <bool FIX = true>
 __device__ __forceinline__ void roe_flux_fast(const RoeK &K, const double *L,
                                               const double *R, double *f) {
   const double rl = L[0], pl = L[1], ul = L[2], vl = L[3], wl = L[4];
@@ -294,7 +301,7 @@ __device__ __forceinline__ void roe_flux_fast(const RoeK &K, const double *L,
   const double cfa = max_(0.0, cfast2 - cs2);
   const double rden = rsq_(cfcs + 1.0 - sp2);
   const double alphf = sp2 * (sqrt_(cfca) * rden) + 1.0 - sp2;
-  const double alphs = sp2 * (sqrt_(cfa) * rden) + 1.0 - sp2;
+  const double alphs = FIX ? sp2 * (sqrt_(cfa) * rden) + 1.0 - sp2 : sp2 * (sqrt_(cfa) * rden);
   const double sg = copysign(1.0, bxb);
   // eigenvalues with the entropy floor
   const double du = ur - ul;

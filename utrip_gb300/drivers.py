@@ -72,7 +72,7 @@ def _cfl(setup, state, safety):
     if setup["solver"] in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
         return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
                              setup["dy"], setup["dz"])
-    if setup["solver"] == "mlw_m3":
+    if setup["solver"] in ("mlw_m3", "roe_m3"):
         return capi.cfl_m3(safety, setup["dtmin"], setup["gm"], *state[:8], setup["dx"],
                            setup["dy"])
     return capi.cfl_m(safety, setup["dtmin"], setup["gm"], *state[:6], setup["dx"], setup["dy"])
@@ -88,6 +88,9 @@ def _step(setup, state, dt):
     if setup["solver"] == "mlw_m_1d":
         capi.mlw_m_1d(*state, setup["bx"], setup["bxm"], dt, setup["qav"], setup["gm"],
                       setup["dx"], setup["dxm"])
+        return
+    if setup["solver"] == "roe_m3":
+        capi.roe_m3(*state, dt, setup["gm"], setup["dx"], setup["dy"])
         return
     if setup["solver"] == "roe_m_3d":
         capi.roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])

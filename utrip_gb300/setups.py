@@ -17,7 +17,7 @@ import math
 import numpy as np
 
 from .capi import (BD_FRE, BD_PER, BD_SMN, BD_SMP, BD_SPN, BD_SPP, SOLVER_HLLD_3D,
-                   SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M_3D)
+                   SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M3_2D, SOLVER_ROE_M_3D)
 
 SQ4PI = math.sqrt(4.0 * math.pi)
 
@@ -26,7 +26,11 @@ VARS = {
     "mlw_m3": ["ro", "pr", "vx", "vy", "vz", "bx", "by", "bz", "az"],
     "mlw_m": ["ro", "pr", "vx", "vy", "bx", "by", "az"],
 }
-SOLVER_ID = {"mlw_m": SOLVER_MLW_M_2D, "mlw_m3": SOLVER_MLW_M3_2D}
+VARS["roe_m3"] = VARS["mlw_m3"]
+SOLVER_ID = {"mlw_m": SOLVER_MLW_M_2D, "mlw_m3": SOLVER_MLW_M3_2D, "roe_m3": SOLVER_ROE_M3_2D}
+# ghost layers of each 2-D solver (md_mhdkh/hdmlw/main.f:5 and
+# md_mhdkh/hdroe/main.f:5)
+MARGIN_2D = {"mlw_m": 1, "mlw_m3": 1, "roe_m3": 2}
 
 
 def grdrdy(x: np.ndarray):
@@ -98,8 +102,8 @@ def _pack(solver, x, dx, dxm, y, dy, dym, fields, gm, qav, bc, **extra):
     names = VARS[solver]
     state = [np.asfortranarray(fields[k], dtype=np.float64) for k in names]
     d = dict(solver=solver, solver_id=SOLVER_ID[solver], names=names, x=x, dx=dx,
-             dxm=dxm, y=y, dy=dy, dym=dym, state=state, gm=gm, qav=qav, margin=1,
-             bc=bc)
+             dxm=dxm, y=y, dy=dy, dym=dym, state=state, gm=gm, qav=qav,
+             margin=MARGIN_2D[solver], bc=bc)
     d.update(extra)
     return d
 
@@ -109,8 +113,9 @@ def orszag_tang(n: int = 512, solver: str = "mlw_m3"):
     rho=25/(36 pi), p=5/(12 pi), v=(-sin y, sin x), B=(-sin y, sin 2x)/sqrt(4pi)
     in Heaviside-Lorentz units, i.e. (-sin y, sin 2x) in CANS units."""
     L = 2.0 * math.pi
-    x, dx, dxm = uniform_axis(n, L)
-    y, dy, dym = uniform_axis(n, L)
+    m = MARGIN_2D[solver]
+    x, dx, dxm = uniform_axis(n, L, m)
+    y, dy, dym = uniform_axis(n, L, m)
     X, Y = np.meshgrid(x, y, indexing="ij")
     shape = X.shape
     f = {
@@ -120,7 +125,7 @@ def orszag_tang(n: int = 512, solver: str = "mlw_m3"):
         "bx": SQ4PI * (-np.sin(Y) / SQ4PI), "by": SQ4PI * (np.sin(2.0 * X) / SQ4PI),
         "bz": np.zeros(shape),
     }
-    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, 1)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, m)
     nvar = len(VARS[solver])
     return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
                  _bc_all(nvar, BD_PER, BD_PER), safety=0.4, dtmin=1e-10,
@@ -137,8 +142,9 @@ def shear_layer(n: int = 256, beta: float = 1.0, seed: int = 4, ny: int | None =
     ny = ny or n
     rng = np.random.default_rng(seed)
     phase = float(rng.uniform(0.0, 2.0 * math.pi))
-    x, dx, dxm = uniform_axis(n, 1.0)
-    y, dy, dym = uniform_axis(ny, 1.0)
+    m = MARGIN_2D[solver]
+    x, dx, dxm = uniform_axis(n, 1.0, m)
+    y, dy, dym = uniform_axis(ny, 1.0, m)
     X, Y = np.meshgrid(x, y, indexing="ij")
     shape = X.shape
     b0 = np.array([1.0, 0.5, 0.0])
@@ -151,20 +157,23 @@ def shear_layer(n: int = 256, beta: float = 1.0, seed: int = 4, ny: int | None =
         "bx": np.full(shape, SQ4PI * b0[0]), "by": np.full(shape, SQ4PI * b0[1]),
         "bz": np.zeros(shape),
     }
-    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, 1)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, m)
     nvar = len(VARS[solver])
     return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
                  _bc_all(nvar, BD_PER, BD_SPP), safety=0.4, dtmin=1e-10,
                  tend=1e30, beta=beta, phase=phase, name=f"shear_layer_{n}x{ny}_b{beta:g}")
 
 
-def random_state(ix: int, jx: int, seed: int = 0, solver: str = "mlw_m3", amp: float = 0.05):
+def random_state(ix: int, jx: int, seed: int = 0, solver: str = "mlw_m3", amp: float = 0.05,
+                 margin: int | None = None):
     """Smooth state with seeded random perturbations on every variable, for
     parity tests that exercise all terms of the step (non-uniform fields in
-    every component, including vz, bz and az)."""
+    every component, including vz, bz and az).  margin defaults to the
+    solver's."""
     rng = np.random.default_rng(seed)
-    x, dx, dxm = uniform_axis(ix - 2, 1.0)
-    y, dy, dym = uniform_axis(jx - 2, 1.0)
+    m = margin or MARGIN_2D[solver]
+    x, dx, dxm = uniform_axis(ix - 2 * m, 1.0, m)
+    y, dy, dym = uniform_axis(jx - 2 * m, 1.0, m)
     X, Y = np.meshgrid(x, y, indexing="ij")
 
     def smooth(scale):
@@ -183,7 +192,7 @@ def random_state(ix: int, jx: int, seed: int = 0, solver: str = "mlw_m3", amp: f
     nvar = len(VARS[solver])
     return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
                  _bc_all(nvar, BD_PER, BD_SPP), safety=0.4, dtmin=1e-10,
-                 tend=1e30, name=f"random_{ix}x{jx}_s{seed}")
+                 tend=1e30, margin=m, name=f"random_{ix}x{jx}_s{seed}")
 
 
 VARS["mlw_m_3d"] = ["ro", "pr", "vx", "vy", "vz", "bx", "by", "bz"]
