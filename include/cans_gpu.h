@@ -158,6 +158,12 @@ int cans_mlw_m_bg(double *ro, double *pr, double *vx, double *vy, double *by,
                   const double *scm, const double *dscm, const double *rr,
                   const double *rrm, const double *drr, const double *drrm,
                   const double *dx, const double *dxm, const int *ix);
+/* replaces subroutine roe_m   (cans1d/hdroe/roe_m.f:2): one 1-D Roe-MUSCL
+ * step with the two-component roeflux_m.f; bx, bxm fixed; cells 3..ix-2
+ * are updated (margin 3 as md_mhdshktb/hdroe/main.f:5); ix >= 5 */
+int cans_roe_m_1d(double *ro, double *pr, double *vx, double *vy, double *by,
+                  const double *bx, const double *bxm, const double *dt,
+                  const double *gm, const double *dx, const int *ix);
 /* replaces subroutine chkdav  (cans1d/common/chkdav.f:2): da below floor is
  * raised to it and vx set to zero there; n_events receives the count */
 int cans_chkdav(int *n_events, double *da, double *vx, const double *floor,

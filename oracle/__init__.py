@@ -58,6 +58,7 @@ def load():
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m3_2d.argtypes = [_dp] * 9 + [d, d, _dp, i, _dp, i]
+        lib.oracle_roe_m_1d.argtypes = [_dp] * 7 + [d, d, _dp, i]
         lib.oracle_hlld_engine_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, i, _dp, i, _dp, i, _ip]
         lib.oracle_mlw_m_bg_1d.argtypes = [_dp] * 7 + [d, d, d] + [_dp] * 12 + [i]
         lib.oracle_chkdav.argtypes = [_dp, _dp, d, i]
@@ -183,6 +184,12 @@ def mlw_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, dx, dxm):
                            P(dx), P(dxm), ro.size)
 
 
+def roe_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, gm, dx):
+    """cans1d/hdroe/roe_m.f:2"""
+    load().oracle_roe_m_1d(*[P(a) for a in (ro, pr, vx, vy, by, bx, bxm)], dt, gm, P(dx),
+                           ro.size)
+
+
 def cfl_m_1d(safety, dtmin, gm, bx, ro, pr, vx, vy, by, dx):
     dt, merr = C.c_double(), C.c_int()
     load().oracle_cfl_m_1d(C.byref(dt), safety, dtmin, C.byref(merr), gm, P(bx),
@@ -224,7 +231,10 @@ def run_1d(setup, state, nstop, tend=None, safety=None, t0=0.0):
             return t, ns, merr, dts
         t = t + dt
         dts.append(dt)
-        mlw_m_1d(*state, bx, bxm, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"])
+        if setup["solver"] == "roe_m_1d":
+            roe_m_1d(*state, bx, bxm, dt, setup["gm"], setup["dx"])
+        else:
+            mlw_m_1d(*state, bx, bxm, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"])
         apply_bc_program_1d(state, setup["bc"], setup["margin"], setup)
         if not (ns < nstop and t < tend):
             return t, ns, 0, dts

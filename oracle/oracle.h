@@ -132,6 +132,11 @@ void oracle_roe_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                      const double *dx, int ix, const double *dy, int jx,
                      const double *dz, int kx);
 
+/* 1-D Roe-MUSCL step roe_m (cans1d/hdroe/roe_m.f:2), two-component. */
+void oracle_roe_m_1d(double *ro, double *pr, double *vx, double *vy, double *by,
+                     const double *bx, const double *bxm, double dt, double gm,
+                     const double *dx, int ix);
+
 /* 2-D Roe-MUSCL step roe_m3 (cans2d/hdroe/roe_m3.f:1) on ix*jx arrays. */
 void oracle_roe_m3_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
                       double *bx, double *by, double *bz, double *az, double dt,

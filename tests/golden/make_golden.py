@@ -86,6 +86,20 @@ def case_roe2(ix, jx, seed):
     return out
 
 
+def case_roe1(ix, seed):
+    """One 1-D Roe-MUSCL step (cans1d/hdroe/roe_m.f) of a seeded state."""
+    s = setups.random_state_1d(ix, seed=seed)
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    out.update(bx=s["bx"], bxm=s["bxm"], dx=s["dx"])
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_m_1d(0.5, 1e-10, 2.0, s["bx"], *st, s["dx"])
+    oracle.roe_m_1d(*st, s["bx"], s["bxm"], dt, 2.0, s["dx"])
+    out.update({"dt": np.array(dt), "gm": np.array(2.0)})
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def bd_case():
     rng = np.random.default_rng(13)
     q = np.asfortranarray(rng.standard_normal((9, 7)))
@@ -108,6 +122,7 @@ FIXTURES = {
     "roe_m_3d_14x12x13": lambda: case_roe(14, 12, 13, 21),
     "hlld_3d_13x11x12": lambda: case_hlld(13, 11, 12, 22),
     "roe_m3_2d_17x15": lambda: case_roe2(17, 15, 23),
+    "roe_m_1d_70": lambda: case_roe1(70, 24),
 }
 
 

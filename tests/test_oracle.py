@@ -705,3 +705,39 @@ def test_roe2d_oracle_matches_frozen_fixture(oracle_lib):
     oracle_lib.roe_m3(*st, float(z["dt"]), float(z["gm"]), z["grid_dx"], z["grid_dy"])
     for k, a in zip(names, st):
         assert np.array_equal(a, z["out_" + k]), k
+
+
+# ---- 1-D roe_m ----------------------------------------------------------------
+
+def test_roe1d_uniform_state_changes_only_by_rounding(oracle_lib):
+    s = setups.shock_tube_1d(32, solver="roe_m_1d")
+    n = s["x"].size
+    st = [np.full(n, v) for v in (1.2, 0.7, 0.1, -0.3, 0.9)]
+    ref = [a.copy() for a in st]
+    oracle_lib.roe_m_1d(*st, s["bx"], s["bxm"], 1e-3, s["gm"], s["dx"])
+    for a, b in zip(st, ref):
+        assert float(np.max(np.abs(a - b))) <= 4e-16 * max(1.0, float(np.max(np.abs(b))))
+
+
+def test_roe1d_brio_wu_keeps_far_states_and_wall_condition(oracle_lib):
+    """The md_mhdshktb/hdroe run to t = 0.1: the far states are untouched,
+    vx vanishes on the walls (bdsmnx), the density stays between the two
+    initial states' bounds and every value is finite."""
+    s = setups.shock_tube_1d(512, solver="roe_m_1d")
+    st = setups.copy_state(s)
+    t, ns, merr, _ = oracle_lib.run_1d(s, st, 10 ** 6)
+    assert merr == 0 and t >= 0.1 and 100 < ns < 1000
+    ro, pr, vx, vy, by = st
+    m = s["margin"]
+    assert np.all(np.isfinite(np.array(st)))
+    assert abs(ro[m + 5] - 1.0) < 1e-12 and abs(ro[-m - 6] - 0.125) < 1e-12
+    assert vx[m] == 0.0 and vx[-m - 1] == 0.0
+    assert 0.1 < ro.min() and ro.max() < 1.0 + 1e-9
+
+
+def test_roe1d_oracle_matches_frozen_fixture(oracle_lib):
+    z = np.load(GOLD / "roe_m_1d_70.npz")
+    st = [z["in_" + k].copy() for k in ("ro", "pr", "vx", "vy", "by")]
+    oracle_lib.roe_m_1d(*st, z["bx"], z["bxm"], float(z["dt"]), float(z["gm"]), z["dx"])
+    for k, a in zip(("ro", "pr", "vx", "vy", "by"), st):
+        assert np.array_equal(a, z["out_" + k]), k

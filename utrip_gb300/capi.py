@@ -103,6 +103,7 @@ def load() -> C.CDLL:
     sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
     sig["cans_mlw_m_bg"] = (i, [_dp] * 7 + [_dp, _dp, _dp] + [_dp] * 12 + [_ip])
     sig["cans_chkdav"] = (i, [_ip, _dp, _dp, _dp, _ip])
+    sig["cans_roe_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _ip])
     sig["cans_bdperx_1d"] = (i, [_ip, _ip, _dp, _ip])
     for fam in ("spp", "spn", "smp", "smn", "fre"):
         sig[f"cans_bd{fam}x_1d"] = (i, [_ip, _ip, _dp, _ip])
@@ -270,6 +271,13 @@ def mlw_m_bg(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, gx, gxm, sc, dsc, scm, ds
                                        *[_ptr(a) for a in (gx, gxm, sc, dsc, scm, dscm, rr,
                                                            rrm, drr, drrm, dx, dxm)],
                                        _iref(ix)), "mlw_m_bg")
+
+
+def roe_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, gm, dx):
+    """cans1d/hdroe/roe_m.f:2 -- one 1-D Roe-MUSCL step, in place."""
+    return _check(load().cans_roe_m_1d(*[_ptr(a) for a in (ro, pr, vx, vy, by, bx, bxm)],
+                                       _dref(dt), _dref(gm), _ptr(dx), _iref(ro.size)),
+                  "roe_m_1d")
 
 
 def chkdav(da, vx, floor):

@@ -101,6 +101,13 @@ cudaError_t launch_roe2d(bool exact, const double *A, double *B,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
                          Box3 box, cudaStream_t s);
 
+// 1-D roe_m (5 arrays ro,pr,vx,vy,by of ix; bx, bxm, dx device arrays);
+// A -> B, cells outside 3..ix-2 copied; scratch of roe1d_scratch_doubles(ix).
+size_t roe1d_scratch_doubles(size_t ncells);
+cudaError_t launch_roe1d(bool exact, const double *A, double *B, double *scratch,
+                         const double *bx, const double *bxm, const double *dx,
+                         int ix, double gm, double dt, cudaStream_t s);
+
 // ---- 3-D HLLD (cansxx engine) ----------------------------------------------
 // One two-stage HLLD step on 8 arrays (Heaviside units, permeability mu);
 // A -> B for every cell.  mfdim[a] = 1 marks an active axis.  scratch holds

@@ -586,6 +586,46 @@ extern "C" int cans_mlw_m_bg(double *ro, double *pr, double *vx, double *vy,
   return CANS_OK;
 }
 
+// roe_m (cans1d/hdroe/roe_m.f:2): one 1-D Roe-MUSCL step, on the registered
+// mirrors when the five arrays are a resident set.
+extern "C" int cans_roe_m_1d(double *ro, double *pr, double *vx, double *vy,
+                             double *by, const double *bx, const double *bxm,
+                             const double *dt, const double *gm,
+                             const double *dx, const int *ix) {
+  if (!ro || !pr || !vx || !vy || !by || !bx || !bxm || !dt || !gm || !dx || !ix)
+    return CANS_ERR_ARG;
+  const int n = *ix;
+  if (n < 5) return CANS_ERR_ARG;
+  double *arrs[5] = {ro, pr, vx, vy, by};
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  MirrorSet *m = resident_step_set(arrs, 5);
+  DevAxis *dax = m ? &m->ax : &g_scratch.ax;
+  if ((rc = dax->upload(n, dx, dx, s))) return rc;  // roe_m reads dx only
+  if ((rc = g_dev1d.upload(n, bx, bxm, s))) return rc;
+  if ((rc = g_scratch.ensure_roe(roe1d_scratch_doubles(n)))) return rc;
+  const double *dbx = g_dev1d.bx, *dbxm = g_dev1d.bx + n;
+  if (m) {
+    CK(launch_roe1d(exact_mode(), m->buf[m->cur], m->buf[m->cur ^ 1], g_scratch.roe, dbx,
+                    dbxm, dax->a.d, n, *gm, *dt, s));
+    m->cur ^= 1;
+    return CANS_OK;
+  }
+  if ((rc = g_scratch.ensure(5 * (size_t)n))) return rc;
+  for (int v = 0; v < 5; v++)
+    CK(cudaMemcpyAsync(g_scratch.A + (size_t)v * n, arrs[v], sizeof(double) * n,
+                       cudaMemcpyHostToDevice, s));
+  CK(launch_roe1d(exact_mode(), g_scratch.A, g_scratch.B, g_scratch.roe, dbx, dbxm,
+                  dax->a.d, n, *gm, *dt, s));
+  for (int v = 0; v < 5; v++)
+    CK(cudaMemcpyAsync(arrs[v], g_scratch.B + (size_t)v * n, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return CANS_OK;
+}
+
 extern "C" int cans_chkdav(int *n_events, double *da, double *vx,
                            const double *floor, const int *ix) {
   if (!n_events || !da || !vx || !floor || *ix < 0) return CANS_ERR_ARG;

@@ -66,7 +66,7 @@ def _bnd1(setup, state):
 
 
 def _cfl(setup, state, safety):
-    if setup["solver"] in ("mlw_m_1d", "mlw_m_bg_1d"):
+    if setup["solver"] in ("mlw_m_1d", "mlw_m_bg_1d", "roe_m_1d"):
         return capi.cfl_m_1d(safety, setup["dtmin"], setup["gm"], setup["bx"], *state,
                              setup["dx"])
     if setup["solver"] in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
@@ -84,6 +84,9 @@ def _step(setup, state, dt):
         capi.mlw_m_bg(*state, s["bx"], s["bxm"], dt, s["qav"], s["gm"], s["gx"], s["gxm"],
                       s["sc"], s["dsc"], s["scm"], s["dscm"], s["rr"], s["rrm"], s["drr"],
                       s["drrm"], s["dx"], s["dxm"])
+        return
+    if setup["solver"] == "roe_m_1d":
+        capi.roe_m_1d(*state, setup["bx"], setup["bxm"], dt, setup["gm"], setup["dx"])
         return
     if setup["solver"] == "mlw_m_1d":
         capi.mlw_m_1d(*state, setup["bx"], setup["bxm"], dt, setup["qav"], setup["gm"],
@@ -127,7 +130,8 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             dts.append(dt)
             _step(setup, state, dt)
             {"mlw_m_3d": _bnd3, "roe_m_3d": _bnd3, "hlld_3d": _bnd3,
-             "mlw_m_1d": _bnd1, "mlw_m_bg_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
+             "mlw_m_1d": _bnd1, "mlw_m_bg_1d": _bnd1,
+             "roe_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
     finally:

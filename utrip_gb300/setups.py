@@ -363,15 +363,20 @@ VARS["mlw_m_1d"] = ["ro", "pr", "vx", "vy", "by"]
 SOLVER_ID["mlw_m_1d"] = 3
 
 
-def shock_tube_1d(n: int = 1024, safety: float = 0.4, tend: float = 0.1):
+def shock_tube_1d(n: int = 1024, safety: float | None = None, tend: float = 0.1,
+                  solver: str = "mlw_m_1d"):
     """Brio-Wu-type MHD shock tube as cans1d/md_mhdshktb/hdmlw/model.f sets
     it up: margin 1, dx0 = 1/n, cell izero = ix/2 centred at -dx0/2 (the
     interface between cells ix/2 and ix/2+1 at x = 0; the box is [-0.5, 0.5],
     a translation of [0, 1] with the interface at 0.5), gamma = 2.  Left
     (x <= 0): rho=1, p=1, By=+sqrt(4pi); right: rho=0.125, p=0.1,
     By=-sqrt(4pi); Bx = 0.75 sqrt(4pi).  bnd.f: bdsppx for ro, pr, vy, by and
-    bdsmnx for vx on both faces.  qav = 1 (main.f:149)."""
-    margin = 1
+    bdsmnx for vx on both faces.  qav = 1 (main.f:149).  solver "roe_m_1d"
+    is the Roe package of the same model (md_mhdshktb/hdroe: margin 3, cfl
+    safety 1.0, main.f:5,139); the mLW package uses margin 1, safety 0.4."""
+    margin = 3 if solver == "roe_m_1d" else 1
+    if safety is None:
+        safety = 1.0 if solver == "roe_m_1d" else 0.4
     ix = n + 2 * margin
     dx0 = 1.0 / float(np.float32(ix - 2 * margin))
     dxm0 = np.full(ix, dx0)
@@ -395,9 +400,10 @@ def shock_tube_1d(n: int = 1024, safety: float = 0.4, tend: float = 0.1):
         kind = BD_SMN if name == "vx" else BD_SPP
         bc += [(v, 0, kind, 0.0), (v, 1, kind, 0.0)]
     state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in VARS["mlw_m_1d"]]
-    return dict(solver="mlw_m_1d", solver_id=3, names=VARS["mlw_m_1d"], x=x, dx=dx, dxm=dxm,
+    return dict(solver=solver, solver_id=3, names=VARS["mlw_m_1d"], x=x, dx=dx, dxm=dxm,
                 bx=bx, bxm=bx.copy(), state=state, gm=2.0, qav=1.0, margin=margin, bc=bc,
-                safety=safety, dtmin=1e-10, tend=tend, dtout=0.01, name=f"shock_tube_{n}")
+                safety=safety, dtmin=1e-10, tend=tend, dtout=0.01,
+                name=f"shock_tube_{n}" if solver == "mlw_m_1d" else f"shock_tube_{solver}_{n}")
 
 
 def random_state_1d(ix: int, seed: int = 0):
