@@ -73,6 +73,22 @@ int cans_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
                    const double *dt, const double *qav, const double *gm,
                    const double *dx, const double *dxm, const int *ix,
                    const double *dy, const double *dym, const int *jx);
+/* replaces subroutine mlw_m3_g (cans2d/hdmlw/mlw_m3_g.f:1) and mlw_m_g
+ * (cans2d/hdmlw/mlw_m_g.f:1): the steps with gravity; gx, gy at the cells,
+ * gxm, gym at the cell corners, ix*jx each */
+int cans_mlw_m3_g_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                     double *bx, double *by, double *bz, double *az,
+                     const double *dt, const double *qav, const double *gm,
+                     const double *gx, const double *gxm, const double *gy,
+                     const double *gym, const double *dx, const double *dxm,
+                     const int *ix, const double *dy, const double *dym,
+                     const int *jx);
+int cans_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
+                    double *by, double *az, const double *dt, const double *qav,
+                    const double *gm, const double *gx, const double *gxm,
+                    const double *gy, const double *gym, const double *dx,
+                    const double *dxm, const int *ix, const double *dy,
+                    const double *dym, const int *jx);
 /* replaces subroutine mlw_m   (cans2d/hdmlw/mlw_m.f:2-3) */
 int cans_mlw_m_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
                   double *by, double *az, const double *dt, const double *qav,
@@ -310,7 +326,10 @@ typedef struct {
                                  an extent > 1                              */
   /* mlw_m_bg (CANS_SOLVER_MLW_M_BG_1D): the static profiles of
    * cans1d/hdmlw/mlw_m_bg.f:2-3, ix doubles each (gravity, cross section,
-   * distance from the rotation axis and their gradients) */
+   * distance from the rotation axis and their gradients).  For the 2-D mLW
+   * solvers gx and gxm, with gy and gym below, are the gravity fields of
+   * mlw_m_g / mlw_m3_g (ix*jx doubles each; gxm, gym at the cell corners):
+   * when gx is set the run takes the step with gravity. */
   const double *gx, *gxm, *sc, *scm, *dsc, *dscm, *rr, *rrm, *drr, *drrm;
   /* 1-D loops: chkdav (cans1d/common/chkdav.f:2) of ro, then pr, with
    * `floor` after every boundary fill when chkdav = 1; the events are
@@ -324,6 +343,8 @@ typedef struct {
   const double *trq;
   double trq0;
   unsigned long long seed;
+  /* 2-D mLW with gravity: gy(ix,jx) at the cells, gym(ix,jx) at the corners */
+  const double *gy, *gym;
 } cans_run_desc;
 
 typedef struct {

@@ -45,6 +45,8 @@ def load():
         d, i = C.c_double, C.c_int
         lib.oracle_mlw_m3_2d.argtypes = [_dp] * 9 + [d, d, d, _dp, _dp, i, _dp, _dp, i]
         lib.oracle_mlw_m_2d.argtypes = [_dp] * 7 + [d, d, d, _dp, _dp, i, _dp, _dp, i]
+        lib.oracle_mlw_m3_g_2d.argtypes = [_dp] * 9 + [d, d, d] + [_dp] * 6 + [i, _dp, _dp, i]
+        lib.oracle_mlw_m_g_2d.argtypes = [_dp] * 7 + [d, d, d] + [_dp] * 6 + [i, _dp, _dp, i]
         lib.oracle_cfl_m3_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i]
         lib.oracle_cfl_m_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 6 + [_dp, i, _dp, i]
         lib.oracle_bd_2d.argtypes = [i, i, i, i, _dp, d, _dp, i, i]
@@ -162,7 +164,30 @@ def roe_m3(ro, pr, vx, vy, vz, bx, by, bz, az, dt, gm, dx, dy):
                             P(dx), ix, P(dy), jx)
 
 
+def mlw_m3_g(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, gx, gxm, gy, gym,
+             dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m3_g.f:1"""
+    ix, jx = ro.shape
+    load().oracle_mlw_m3_g_2d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)], dt, qav,
+                              gm, *[P(a) for a in (gx, gxm, gy, gym, dx, dxm)], ix, P(dy),
+                              P(dym), jx)
+
+
+def mlw_m_g(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m_g.f:1"""
+    ix, jx = ro.shape
+    load().oracle_mlw_m_g_2d(*[P(a) for a in (ro, pr, vx, vy, bx, by, az)], dt, qav, gm,
+                             *[P(a) for a in (gx, gxm, gy, gym, dx, dxm)], ix, P(dy), P(dym),
+                             jx)
+
+
 def step_2d(setup, state, dt):
+    if setup.get("gravity"):
+        g = [np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym")]
+        args = (setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"], setup["dy"],
+                setup["dym"])
+        (mlw_m3_g if setup["solver"] == "mlw_m3" else mlw_m_g)(*state, dt, *args)
+        return
     if setup["solver"] == "roe_m3":
         roe_m3(*state, dt, setup["gm"], setup["dx"], setup["dy"])
         return

@@ -9,6 +9,7 @@
  *   mlwartv   cans2d/hdmlw/mlwartv.f:225-233
  *   mlw_m3    cans2d/hdmlw/mlw_m3.f:64-374   (8 conserved variables + az)
  *   mlw_m     cans2d/hdmlw/mlw_m.f           (6 conserved variables + az)
+ *   mlw_m3_g, mlw_m_g  cans2d/hdmlw/mlw_m3_g.f, mlw_m_g.f (the same with gravity)
  *   cfl_m3    cans2d/common/cfl_m3.f:38-65
  *   cfl_m     cans2d/common/cfl_m.f:38-77
  *   bbtoaa    cans2d/common/bbtoaa.f:28-49
@@ -143,11 +144,15 @@ static void metrics2(const double *dx, const double *dxm, int ix,
 }
 
 /* cans2d/hdmlw/mlw_m3.f:2-377 */
-void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
-                      double *vz, double *bx, double *by, double *bz,
-                      double *az, double dt, double qav, double gm,
-                      const double *dx, const double *dxm, int ix,
-                      const double *dy, const double *dym, int jx) {
+/* With gx != NULL this is mlw_m3_g (cans2d/hdmlw/mlw_m3_g.f:1-393): the
+ * gravity sources of mlw_m3_g.f:95-121 (cells) and :194-220 (corners) are
+ * added through mlwsrch / mlwsrcf to the energy and the x, y momenta. */
+static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
+                        double *vz, double *bx, double *by, double *bz,
+                        double *az, double dt, double qav, double gm,
+                        const double *gx, const double *gxm, const double *gy,
+                        const double *gym, const double *dx, const double *dxm,
+                        int ix, const double *dy, const double *dym, int jx) {
   const size_t n = (size_t)ix * (size_t)jx;
   const size_t nm = (size_t)(ix > jx ? ix : jx);
   enum { NT = 37 };
@@ -222,6 +227,15 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = ep * vy[c] + (bx[c] * ez[c] - bz[c] * ex[c]) * pi4i;
     }
   mlwhalf2(ee, eeh, dee, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ss[c] = ro[c] * (vx[c] * gx[c] + vy[c] * gy[c]);
+      }
+    mlwsrch2(eeh, dee, dt, ss, ix, jx);
+  }
   /* x-momentum (:149-156) */
   OMP_FOR
   for (int j = 1; j <= jx; j++)
@@ -232,6 +246,15 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = ro[c] * vx[c] * vy[c] - pi4i * bx[c] * by[c];
     }
   mlwhalf2(rx, rxh, drx, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ss[c] = ro[c] * gx[c];
+      }
+    mlwsrch2(rxh, drx, dt, ss, ix, jx);
+  }
   /* y-momentum (:159-166) */
   OMP_FOR
   for (int j = 1; j <= jx; j++)
@@ -242,6 +265,15 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
               pi8i * (bx[c] * bx[c] + bz[c] * bz[c] - by[c] * by[c]);
     }
   mlwhalf2(ry, ryh, dry, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ss[c] = ro[c] * gy[c];
+      }
+    mlwsrch2(ryh, dry, dt, ss, ix, jx);
+  }
   /* z-momentum (:169-175) */
   OMP_FOR
   for (int j = 1; j <= jx; j++)
@@ -325,6 +357,15 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = ep * vyh[c] + (bxh[c] * ezh[c] - bzh[c] * exh[c]) * pi4i;
     }
   mlwfull2(dee, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        ss[c] = roh[c] * (vxh[c] * gxm[c] + vyh[c] * gym[c]);
+      }
+    mlwsrcf2(dee, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+  }
   /* x-momentum (:257-264) */
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
@@ -335,6 +376,15 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = roh[c] * vxh[c] * vyh[c] - pi4i * bxh[c] * byh[c];
     }
   mlwfull2(drx, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        ss[c] = roh[c] * gxm[c];
+      }
+    mlwsrcf2(drx, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+  }
   /* y-momentum (:267-274) */
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
@@ -345,6 +395,15 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
               pi8i * (bxh[c] * bxh[c] + bzh[c] * bzh[c] - byh[c] * byh[c]);
     }
   mlwfull2(dry, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        ss[c] = roh[c] * gym[c];
+      }
+    mlwsrcf2(dry, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+  }
   /* z-momentum (:277-283); the reference sweeps the whole array here, the
    * extra edge entries are never read by mlwfull. */
   OMP_FOR
@@ -442,10 +501,14 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
 }
 
 /* cans2d/hdmlw/mlw_m.f:2-324 (ro,pr,vx,vy,bx,by + az; no z components) */
-void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
-                     double *bx, double *by, double *az, double dt, double qav,
-                     double gm, const double *dx, const double *dxm, int ix,
-                     const double *dy, const double *dym, int jx) {
+/* With gx != NULL this is mlw_m_g (cans2d/hdmlw/mlw_m_g.f): gravity sources
+ * of mlw_m_g.f:96-122 and :175-201 through mlwsrch / mlwsrcf. */
+static void mlw_m_core(double *ro, double *pr, double *vx, double *vy,
+                       double *bx, double *by, double *az, double dt, double qav,
+                       double gm, const double *gx, const double *gxm,
+                       const double *gy, const double *gym, const double *dx,
+                       const double *dxm, int ix, const double *dy,
+                       const double *dym, int jx) {
   const size_t n = (size_t)ix * (size_t)jx;
   const size_t nm = (size_t)(ix > jx ? ix : jx);
   enum { NT = 27 };
@@ -510,6 +573,15 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = ep * vy[c] + bx[c] * ez[c] * pi4i;
     }
   mlwhalf2(ee, eeh, dee, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ss[c] = ro[c] * (vx[c] * gx[c] + vy[c] * gy[c]);
+      }
+    mlwsrch2(eeh, dee, dt, ss, ix, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx; j++)
     for (int i = 1; i <= ix; i++) {
@@ -519,6 +591,15 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = ro[c] * vx[c] * vy[c] - pi4i * bx[c] * by[c];
     }
   mlwhalf2(rx, rxh, drx, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ss[c] = ro[c] * gx[c];
+      }
+    mlwsrch2(rxh, drx, dt, ss, ix, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx; j++)
     for (int i = 1; i <= ix; i++) {
@@ -528,6 +609,15 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
               pi8i * (bx[c] * bx[c] - by[c] * by[c]);
     }
   mlwhalf2(ry, ryh, dry, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ss[c] = ro[c] * gy[c];
+      }
+    mlwsrch2(ryh, dry, dt, ss, ix, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx; j++)
     for (int i = 1; i <= ix; i++) {
@@ -583,6 +673,15 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = ep * vyh[c] + bxh[c] * ezh[c] * pi4i;
     }
   mlwfull2(dee, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        ss[c] = roh[c] * (vxh[c] * gxm[c] + vyh[c] * gym[c]);
+      }
+    mlwsrcf2(dee, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
     for (int i = 1; i <= ix - 1; i++) {
@@ -592,6 +691,15 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
       fy[c] = roh[c] * vxh[c] * vyh[c] - pi4i * bxh[c] * byh[c];
     }
   mlwfull2(drx, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        ss[c] = roh[c] * gxm[c];
+      }
+    mlwsrcf2(drx, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
     for (int i = 1; i <= ix - 1; i++) {
@@ -601,6 +709,15 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
               pi8i * (bxh[c] * bxh[c] - byh[c] * byh[c]);
     }
   mlwfull2(dry, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx);
+  if (gx) {
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        ss[c] = roh[c] * gym[c];
+      }
+    mlwsrcf2(dry, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
     for (int i = 1; i <= ix - 1; i++) {
@@ -667,6 +784,43 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
 
 /* cans2d/common/cfl_m3.f:38-65.  The per-cell dtq array and the serial
  * first-minimum scan give the same value as a min-reduction: min is exact. */
+void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
+                      double *vz, double *bx, double *by, double *bz,
+                      double *az, double dt, double qav, double gm,
+                      const double *dx, const double *dxm, int ix,
+                      const double *dy, const double *dym, int jx) {
+  mlw_m3_core(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, NULL, NULL, NULL, NULL,
+              dx, dxm, ix, dy, dym, jx);
+}
+
+void oracle_mlw_m3_g_2d(double *ro, double *pr, double *vx, double *vy,
+                        double *vz, double *bx, double *by, double *bz,
+                        double *az, double dt, double qav, double gm,
+                        const double *gx, const double *gxm, const double *gy,
+                        const double *gym, const double *dx, const double *dxm,
+                        int ix, const double *dy, const double *dym, int jx) {
+  mlw_m3_core(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, gx, gxm, gy, gym,
+              dx, dxm, ix, dy, dym, jx);
+}
+
+void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
+                     double *bx, double *by, double *az, double dt, double qav,
+                     double gm, const double *dx, const double *dxm, int ix,
+                     const double *dy, const double *dym, int jx) {
+  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, NULL, NULL, NULL, NULL, dx, dxm,
+             ix, dy, dym, jx);
+}
+
+void oracle_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
+                       double *bx, double *by, double *az, double dt, double qav,
+                       double gm, const double *gx, const double *gxm,
+                       const double *gy, const double *gym, const double *dx,
+                       const double *dxm, int ix, const double *dy,
+                       const double *dym, int jx) {
+  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, dx, dxm, ix,
+             dy, dym, jx);
+}
+
 void oracle_cfl_m3_2d(double *dt, double safety, double dtmin, int *merr,
                       double gm, const double *ro, const double *pr,
                       const double *vx, const double *vy, const double *vz,

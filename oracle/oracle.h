@@ -93,6 +93,21 @@ void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
                      double *bx, double *by, double *az, double dt, double qav,
                      double gm, const double *dx, const double *dxm, int ix,
                      const double *dy, const double *dym, int jx);
+/* mlw_m3_g (cans2d/hdmlw/mlw_m3_g.f:1) and mlw_m_g (cans2d/hdmlw/mlw_m_g.f:1):
+ * the steps with gravity; gx, gy at cells and gxm, gym at cell corners, all
+ * ix*jx. */
+void oracle_mlw_m3_g_2d(double *ro, double *pr, double *vx, double *vy,
+                        double *vz, double *bx, double *by, double *bz,
+                        double *az, double dt, double qav, double gm,
+                        const double *gx, const double *gxm, const double *gy,
+                        const double *gym, const double *dx, const double *dxm,
+                        int ix, const double *dy, const double *dym, int jx);
+void oracle_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
+                       double *bx, double *by, double *az, double dt, double qav,
+                       double gm, const double *gx, const double *gxm,
+                       const double *gy, const double *gym, const double *dx,
+                       const double *dxm, int ix, const double *dy,
+                       const double *dym, int jx);
 void oracle_cfl_m3_2d(double *dt, double safety, double dtmin, int *merr,
                       double gm, const double *ro, const double *pr,
                       const double *vx, const double *vy, const double *vz,

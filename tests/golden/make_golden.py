@@ -100,6 +100,24 @@ def case_roe1(ix, seed):
     return out
 
 
+def case_grav(solver, ix, jx, seed):
+    """One 2-D step with gravity (mlw_m_g / mlw_m3_g) of a seeded state with
+    seeded non-uniform gravity fields."""
+    s = setups.random_gravity(setups.random_state(ix, jx, seed=seed, solver=solver), seed + 1)
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dxm", "dy", "dym"):
+        out["grid_" + k] = s[k]
+    for k in ("gx", "gxm", "gy", "gym"):
+        out["grav_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_2d(s, st, 0.4)
+    oracle.step_2d(s, st, dt)
+    out["dt"] = np.array(dt)
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def bd_case():
     rng = np.random.default_rng(13)
     q = np.asfortranarray(rng.standard_normal((9, 7)))
@@ -123,6 +141,8 @@ FIXTURES = {
     "hlld_3d_13x11x12": lambda: case_hlld(13, 11, 12, 22),
     "roe_m3_2d_17x15": lambda: case_roe2(17, 15, 23),
     "roe_m_1d_70": lambda: case_roe1(70, 24),
+    "mlw_m_g_2d_19x16": lambda: case_grav("mlw_m", 19, 16, 25),
+    "mlw_m3_g_2d_17x18": lambda: case_grav("mlw_m3", 17, 18, 26),
 }
 
 

@@ -741,3 +741,51 @@ def test_roe1d_oracle_matches_frozen_fixture(oracle_lib):
     oracle_lib.roe_m_1d(*st, z["bx"], z["bxm"], float(z["dt"]), float(z["gm"]), z["dx"])
     for k, a in zip(("ro", "pr", "vx", "vy", "by"), st):
         assert np.array_equal(a, z["out_" + k]), k
+
+
+# ---- 2-D steps with gravity ----------------------------------------------------
+
+@pytest.mark.parametrize("solver", ["mlw_m", "mlw_m3"])
+def test_gravity_step_with_zero_fields_is_the_plain_step(oracle_lib, solver):
+    s = setups.random_state(20, 17, seed=4, solver=solver)
+    z = np.zeros(s["state"][0].shape, order="F")
+    g = dict(s, gravity=True, gx=z, gxm=z, gy=z, gym=z)
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    oracle_lib.step_2d(s, a, 2e-3)
+    oracle_lib.step_2d(g, b, 2e-3)
+    for k, x, y in zip(s["names"], a, b):
+        assert np.array_equal(x, y), k
+
+
+@pytest.mark.parametrize("solver", ["mlw_m", "mlw_m3"])
+def test_gravity_accelerates_a_uniform_state(oracle_lib, solver):
+    """Uniform state at rest, uniform g: the fluxes cancel, so one step gives
+    v = g dt (the half- and full-step sources of mlwsrch / mlwsrcf add up to
+    dt ro g) and leaves density and field unchanged."""
+    s = setups.random_state(16, 14, seed=2, solver=solver)
+    shape = s["state"][0].shape
+    vals = dict(ro=1.3, pr=0.8, vx=0.0, vy=0.0, vz=0.0, bx=0.4, by=-0.2, bz=0.1, az=0.0)
+    st = [np.asfortranarray(np.full(shape, vals[k])) for k in s["names"]]
+    gxv, gyv, dt = 0.3, -0.7, 1e-3
+    g = dict(s, gravity=True, qav=0.0,
+             gx=np.full(shape, gxv, order="F"), gxm=np.full(shape, gxv, order="F"),
+             gy=np.full(shape, gyv, order="F"), gym=np.full(shape, gyv, order="F"))
+    oracle_lib.step_2d(g, st, dt)
+    inner = (slice(1, -1), slice(1, -1))
+    vx, vy = st[s["names"].index("vx")], st[s["names"].index("vy")]
+    assert np.allclose(vx[inner], gxv * dt, rtol=1e-12, atol=0)
+    assert np.allclose(vy[inner], gyv * dt, rtol=1e-12, atol=0)
+    assert np.allclose(st[0][inner], 1.3, rtol=1e-14)
+
+
+def test_gravity_oracle_matches_frozen_fixture(oracle_lib):
+    for name, solver in (("mlw_m_g_2d_19x16", "mlw_m"), ("mlw_m3_g_2d_17x18", "mlw_m3")):
+        z = np.load(GOLD / f"{name}.npz")
+        names = setups.VARS[solver]
+        st = [np.asfortranarray(z["in_" + k]) for k in names]
+        g = {k: np.asfortranarray(z["grav_" + k]) for k in ("gx", "gxm", "gy", "gym")}
+        s = dict(solver=solver, gravity=True, qav=3.0, gm=5.0 / 3.0, **g,
+                 **{k: z["grid_" + k] for k in ("dx", "dxm", "dy", "dym")})
+        oracle_lib.step_2d(s, st, float(z["dt"]))
+        for k, a in zip(names, st):
+            assert np.array_equal(a, z["out_" + k]), (name, k)

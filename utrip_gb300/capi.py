@@ -97,6 +97,8 @@ def load() -> C.CDLL:
     sig["cans_cfl_m_3d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 8 +
                             [_dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_roe_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _ip, _dp, _ip, _dp, _ip])
+    sig["cans_mlw_m3_g_2d"] = (i, [_dp] * 9 + [_dp] * 7 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_mlw_m_g_2d"] = (i, [_dp] * 7 + [_dp] * 7 + [_dp, _dp, _ip, _dp, _dp, _ip])
     sig["cans_roe_m3_2d"] = (i, [_dp] * 9 + [_dp, _dp, _dp, _ip, _dp, _ip])
     sig["cans_hlld_engine_3d"] = (i, [_dp] * 8 + [_dp] * 9 + [_ip] * 4)
     sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
@@ -146,7 +148,9 @@ def _check(rc: int, where: str) -> int:
     return rc
 
 
-def _ptr(a: np.ndarray):
+def _ptr(a: np.ndarray | None):
+    if a is None:  # a NULL argument: the library rejects it
+        return None
     if a.dtype != np.float64 or not (a.flags.f_contiguous or a.ndim == 1):
         raise CansError(CANS_ERR_ARG, "array", "float64 Fortran-ordered arrays are required")
     return a.ctypes.data_as(_dp)
@@ -181,6 +185,25 @@ def mlw_m3(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, dx, dxm, dy, dym):
     return _check(lib.cans_mlw_m3_2d(*[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)],
                                      _dref(dt), _dref(qav), _dref(gm), _ptr(dx), _ptr(dxm),
                                      _iref(ix), _ptr(dy), _ptr(dym), _iref(jx)), "mlw_m3")
+
+
+def mlw_m3_g(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, gx, gxm, gy, gym,
+             dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m3_g.f:1 -- mlw_m3 with gravity, in place."""
+    ix, jx = ro.shape
+    return _check(load().cans_mlw_m3_g_2d(
+        *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)], _dref(dt), _dref(qav),
+        _dref(gm), *[_ptr(a) for a in (gx, gxm, gy, gym)], _ptr(dx), _ptr(dxm), _iref(ix),
+        _ptr(dy), _ptr(dym), _iref(jx)), "mlw_m3_g")
+
+
+def mlw_m_g(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m_g.f:1 -- mlw_m with gravity, in place."""
+    ix, jx = ro.shape
+    return _check(load().cans_mlw_m_g_2d(
+        *[_ptr(a) for a in (ro, pr, vx, vy, bx, by, az)], _dref(dt), _dref(qav), _dref(gm),
+        *[_ptr(a) for a in (gx, gxm, gy, gym)], _ptr(dx), _ptr(dxm), _iref(ix), _ptr(dy),
+        _ptr(dym), _iref(jx)), "mlw_m_g")
 
 
 def mlw_m(ro, pr, vx, vy, bx, by, az, dt, qav, gm, dx, dxm, dy, dym):
@@ -423,7 +446,7 @@ class _Desc(C.Structure):
                 ("gx", _dp), ("gxm", _dp), ("sc", _dp), ("scm", _dp), ("dsc", _dp),
                 ("dscm", _dp), ("rr", _dp), ("rrm", _dp), ("drr", _dp), ("drrm", _dp),
                 ("chkdav", C.c_int), ("floor", C.c_double), ("trq", _dp),
-                ("trq0", C.c_double), ("seed", C.c_ulonglong)]
+                ("trq0", C.c_double), ("seed", C.c_ulonglong), ("gy", _dp), ("gym", _dp)]
 
 
 class RunState(C.Structure):
@@ -467,6 +490,12 @@ class Run:
                   1 if exact else 0, tile, C.c_void_p(stream) if stream else None,
                   arr("bx") if one else None, arr("bxm") if one else None,
                   mu, (C.c_int * 3)(*mfdim))
+        if not one and not three and grid.get("gx") is not None:
+            # 2-D step with gravity: the four fields (ix*jx, Fortran order)
+            for k in ("gx", "gxm", "gy", "gym"):
+                a = np.asfortranarray(grid[k], dtype=np.float64)
+                self._keep.append(a)
+                setattr(d, k, a.ctypes.data_as(_dp))
         if bgv:
             for k in ("gx", "gxm", "sc", "scm", "dsc", "dscm", "rr", "rrm", "drr", "drrm"):
                 if grid.get(k) is not None:  # a missing profile is rejected by the library

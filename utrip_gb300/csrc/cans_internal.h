@@ -52,6 +52,13 @@ cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
                          Box3 box, cudaStream_t s);
 int mlw2d_tile_count();
+// The same steps with gravity (mlw_m_g / mlw_m3_g): grav holds gx, gxm, gy,
+// gym, ix*jx doubles each, on the device.
+cudaError_t launch_mlw2d_g(int solver, bool exact, int tile, const double *A,
+                           double *B, int ix, int jx, const Axis &ax,
+                           const Axis &ay, const Phys &ph, const double *grav,
+                           double dt, Ctl *ctl, Box3 box, cudaStream_t s);
+int mlw2d_g_tile_count();
 cudaError_t launch_cfl2d_full(int solver, bool exact, const double *S, int ix,
                               int jx, const Axis &ax, const Axis &ay,
                               const Phys &ph, double safety,

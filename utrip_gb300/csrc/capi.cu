@@ -174,6 +174,21 @@ struct Scratch {
     }
     return CANS_OK;
   }
+  // gravity fields gx, gxm, gy, gym of the 2-D steps with gravity
+  double *grav = nullptr;
+  size_t grav_cap = 0;
+  int upload_grav(const double *const *g, size_t n, cudaStream_t s) {
+    if (grav_cap < 4 * n) {
+      if (grav) cudaFree(grav);
+      grav = nullptr;
+      grav_cap = 0;
+      CK(cudaMalloc(&grav, sizeof(double) * 4 * n));
+      grav_cap = 4 * n;
+    }
+    for (int k = 0; k < 4; k++)
+      CK(cudaMemcpyAsync(grav + k * n, g[k], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    return CANS_OK;
+  }
 };
 Scratch g_scratch;
 
@@ -217,10 +232,16 @@ double bits_to_double(unsigned long long b) {
 }
 
 // ---- generic 2-D step (drop-in) -------------------------------------------
+// One 2-D step on host arrays or on their registered mirrors; with grav (gx,
+// gxm, gy, gym host arrays of ix*jx) the step with gravity.
 int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
            double gm, const double *dx, const double *dxm, int ix,
-           const double *dy, const double *dym, int jx) {
+           const double *dy, const double *dym, int jx,
+           const double *const *grav = nullptr) {
   if (ix < 3 || jx < 3) return CANS_ERR_ARG;
+  if (grav)
+    for (int k = 0; k < 4; k++)
+      if (!grav[k]) return CANS_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
   int rc = lib_stream(&s);
@@ -228,12 +249,18 @@ int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
   const Phys ph = make_phys(gm, qav);
   const size_t n = (size_t)ix * jx;
   Box3 box{};
+  if (grav && (rc = g_scratch.upload_grav(grav, n, s))) return rc;
+  auto step = [&](const double *A, double *B, const Axis &ax, const Axis &ay) {
+    return grav ? launch_mlw2d_g(solver, exact_mode(), 0, A, B, ix, jx, ax, ay, ph,
+                                 g_scratch.grav, dt, nullptr, box, s)
+                : launch_mlw2d(solver, exact_mode(), 0, A, B, ix, jx, ax, ay, ph, dt,
+                               nullptr, box, s);
+  };
   MirrorSet *m = resident_step_set(arrs, nvar);
   if (m) {
     if ((rc = m->ax.upload(ix, dx, dxm, s))) return rc;
     if ((rc = m->ay.upload(jx, dy, dym, s))) return rc;
-    CK(launch_mlw2d(solver, exact_mode(), 0, m->buf[m->cur], m->buf[m->cur ^ 1],
-                    ix, jx, m->ax.a, m->ay.a, ph, dt, nullptr, box, s));
+    CK(step(m->buf[m->cur], m->buf[m->cur ^ 1], m->ax.a, m->ay.a));
     m->cur ^= 1;
     return CANS_OK;
   }
@@ -243,8 +270,7 @@ int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
                        cudaMemcpyHostToDevice, s));
   if ((rc = g_scratch.ax.upload(ix, dx, dxm, s))) return rc;
   if ((rc = g_scratch.ay.upload(jx, dy, dym, s))) return rc;
-  CK(launch_mlw2d(solver, exact_mode(), 0, g_scratch.A, g_scratch.B, ix, jx,
-                  g_scratch.ax.a, g_scratch.ay.a, ph, dt, nullptr, box, s));
+  CK(step(g_scratch.A, g_scratch.B, g_scratch.ax.a, g_scratch.ay.a));
   for (int v = 0; v < nvar; v++)
     CK(cudaMemcpyAsync(arrs[v], g_scratch.B + v * n, sizeof(double) * n,
                        cudaMemcpyDeviceToHost, s));
@@ -383,6 +409,36 @@ extern "C" int cans_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
                               const int *jx) {
   double *arrs[9] = {ro, pr, vx, vy, vz, bx, by, bz, az};
   return step2d(1, arrs, 9, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx);
+}
+
+// mlw_m3_g (cans2d/hdmlw/mlw_m3_g.f:1): mlw_m3 with gravity
+extern "C" int cans_mlw_m3_g_2d(double *ro, double *pr, double *vx, double *vy,
+                                double *vz, double *bx, double *by, double *bz,
+                                double *az, const double *dt, const double *qav,
+                                const double *gm, const double *gx,
+                                const double *gxm, const double *gy,
+                                const double *gym, const double *dx,
+                                const double *dxm, const int *ix,
+                                const double *dy, const double *dym,
+                                const int *jx) {
+  double *arrs[9] = {ro, pr, vx, vy, vz, bx, by, bz, az};
+  const double *grav[4] = {gx, gxm, gy, gym};
+  return step2d(1, arrs, 9, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, grav);
+}
+
+// mlw_m_g (cans2d/hdmlw/mlw_m_g.f:1): mlw_m with gravity
+extern "C" int cans_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
+                               double *bx, double *by, double *az,
+                               const double *dt, const double *qav,
+                               const double *gm, const double *gx,
+                               const double *gxm, const double *gy,
+                               const double *gym, const double *dx,
+                               const double *dxm, const int *ix,
+                               const double *dy, const double *dym,
+                               const int *jx) {
+  double *arrs[7] = {ro, pr, vx, vy, bx, by, az};
+  const double *grav[4] = {gx, gxm, gy, gym};
+  return step2d(0, arrs, 7, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, grav);
 }
 
 extern "C" int cans_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
@@ -1116,6 +1172,7 @@ struct cans_run {
                                // profiles and the torque profile, ix each
   Loop1D loop1d{};             // 1-D loop options (device pointers into bx1)
   double *roe = nullptr;       // Roe / HLLD: stage scratch
+  double *grav = nullptr;      // 2-D mLW with gravity: gx gxm gy gym (n each)
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
@@ -1153,6 +1210,7 @@ int layout2d(const cans_run *h) {
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
   if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
+  if (h->grav) return mlw2d_g_tile_count();
   return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
 }
 // 1-D: the whole loop (or one fixed step) as one cluster launch, in place
@@ -1192,6 +1250,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (h->ndim == 3)
     return launch_mlw3d(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
+  if (h->grav)
+    return launch_mlw2d_g(h->d.solver, h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx,
+                          h->ax.a, h->ay.a, h->ph, h->grav, dt, ctl, box, h->s);
   return launch_mlw2d(h->d.solver, h->d.exact != 0, tile, A, B, h->d.ix,
                       h->d.jx, h->ax.a, h->ay.a, h->ph, dt, ctl, box, h->s);
 }
@@ -1304,6 +1365,9 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   // boundary program and the frame CFL work on
   const int wmin = 2 * (d->margin + 1) + 1;
   const bool bgv = d->solver == CANS_SOLVER_MLW_M_BG_1D;
+  // 2-D mLW with gx set: the steps with gravity (mlw_m_g / mlw_m3_g)
+  const bool grav2d = (d->solver == CANS_SOLVER_MLW_M_2D ||
+                       d->solver == CANS_SOLVER_MLW_M3_2D) && d->gx != nullptr;
   const double *prof[10] = {d->gx, d->gxm, d->sc, d->scm, d->dsc,
                             d->dscm, d->rr, d->rrm, d->drr, d->drrm};
   if (ndim == 1) {
@@ -1319,6 +1383,7 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   } else if (d->solver == CANS_SOLVER_HLLD_3D) {
     // checked above
   } else {
+    if (grav2d && (!d->gxm || !d->gy || !d->gym)) return CANS_ERR_ARG;
     if (d->ix < wmin || d->jx < wmin) return CANS_ERR_ARG;
     if (ndim == 2 && d->kx != 1) return CANS_ERR_ARG;
     if (ndim == 3 && (d->kx < wmin || !d->dz || !d->dzm)) return CANS_ERR_ARG;
@@ -1389,6 +1454,15 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     e = cudaMalloc(&h->roe, sizeof(double) * nd);
     if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(stage scratch)"));
   }
+  if (grav2d) {  // mlw_m_g / mlw_m3_g: the four gravity fields
+    const double *g[4] = {d->gx, d->gxm, d->gy, d->gym};
+    e = cudaMalloc(&h->grav, sizeof(double) * 4 * h->n);
+    for (int k = 0; k < 4 && e == cudaSuccess; k++)
+      e = cudaMemcpyAsync(h->grav + k * h->n, g[k], sizeof(double) * h->n,
+                          cudaMemcpyHostToDevice, h->s);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "gravity fields"));
+    h->tile = d->tile >= 0 && d->tile < tile_count(h) ? d->tile : 0;
+  }
   for (int a = 0; a < 3; a++) h->mfdim[a] = mfdim[a];
   h->mu = d->mu > 0.0 ? d->mu : 1.0;
   std::memset(&h->host_ctl, 0, sizeof(Ctl));
@@ -1412,6 +1486,7 @@ extern "C" int cans_run_destroy(cans_run *h) {
   if (h->ctl) cudaFree(h->ctl);
   if (h->bx1) cudaFree(h->bx1);
   if (h->roe) cudaFree(h->roe);
+  if (h->grav) cudaFree(h->grav);
   h->ax.release();
   h->ay.release();
   h->az.release();

@@ -17,6 +17,12 @@
 //            viscosity (mlwartv); u += du; back to primitives; write out.
 // The state crosses HBM once in and once out (9 arrays for mlw_m3).
 //
+// With G the tile is mlw_m3_g / mlw_m_g (cans2d/hdmlw/mlw_m3_g.f:95-121,
+// 194-220; mlw_m_g.f:96-122, 175-201): gravity sources ro (v.g), ro gx, ro gy
+// at the cells and the same of the half-step state at the corners enter the
+// energy and the x, y momenta through mlwsrch and mlwsrcf.  grav holds gx,
+// gxm, gy, gym (ix*jx each; gxm, gym at the corner (i+1/2, j+1/2)).
+//
 // In the exact policy every operation is the reference's, in its order, so
 // the result equals a -ffp-contract=off CPU build of the Fortran bit for bit.
 // Terms whose flux is identically zero (fx of bx, fy of by) are skipped: the
@@ -78,14 +84,15 @@ template <> struct Prim<false> {
 
 // TX x TY interior cells per tile; each thread updates RPT of them (rows
 // RPT apart), so a block has TX*TY/RPT threads.
-template <int TX, int TY, bool M3, int RPT = 2> struct Tile {
+template <int TX, int TY, bool M3, int RPT = 2, bool G = false> struct Tile {
   static constexpr int CX = TX + 2, CY = TY + 2, NC = CX * CY;
   static constexpr int KX = TX + 1, KY = TY + 1, NK = KX * KY;
   static constexpr int NQX = (TX + 1) * TY, NQY = TX * (TY + 1);
   static constexpr int NT = TX * TY / RPT;
+  // gravity: three source arrays at the cells and three at the corners
   static constexpr size_t smem_doubles =
       (size_t)CellSlots<M3>::N * NC + (size_t)CornerSlots<M3>::N * NK + NQX +
-      NQY + 32;
+      NQY + 32 + (G ? 3 * ((size_t)NC + NK) : 0);
   static constexpr size_t smem_bytes = smem_doubles * sizeof(double);
 };
 
@@ -98,13 +105,14 @@ constexpr int NOFLUX = -1;
 // single-grid kernel (one tile per block) and by the batched kernel (tiles
 // of many grids pulled from a work queue by persistent blocks).  If cfl_out
 // is non-null the CFL of the written cells inside `box` is reduced into it.
-template <bool E, bool M3, int TX, int TY, int RPT>
+template <bool E, bool M3, int TX, int TY, int RPT, bool G = false>
 __device__ __forceinline__ void tile_step(
     const double *__restrict__ A, double *__restrict__ B, int ix, int jx,
     const Axis &ax, const Axis &ay, const Phys &ph, double dtv, double safety,
     unsigned long long *cfl_out, const Box3 &box, int tile_x, int tile_y,
-    int ntiles_x, int ntiles_y, double *smem) {
-  using T = Tile<TX, TY, M3, RPT>;
+    int ntiles_x, int ntiles_y, double *smem,
+    const double *__restrict__ grav = nullptr) {
+  using T = Tile<TX, TY, M3, RPT, G>;
   using C = CellSlots<M3>;
   using K = CornerSlots<M3>;
   using P = Prim<M3>;
@@ -114,6 +122,8 @@ __device__ __forceinline__ void tile_step(
   double *sqx = sk + (size_t)K::N * T::NK;      // q*dxim  [TY][TX+1]
   double *sqy = sqx + T::NQX;                   // q*dyim  [TY+1][TX]
   double *sred = sqy + T::NQY;                  // reduction scratch (32)
+  double *sgc = sred + 32;                      // G: cell sources   [3][NC]
+  double *sgk = sgc + 3 * T::NC;                // G: corner sources [3][NK]
 
   // a persistent block may come here from another tile: its reads of
   // shared memory must be over before this tile writes it
@@ -127,6 +137,8 @@ __device__ __forceinline__ void tile_step(
 
 #define SC(slot, c) sc[(size_t)(slot) * T::NC + (c)]
 #define SK(slot, c) sk[(size_t)(slot) * T::NK + (c)]
+#define SGC(slot, c) sgc[(size_t)(slot) * T::NC + (c)]
+#define SGK(slot, c) sgk[(size_t)(slot) * T::NK + (c)]
 
   // ---------------- phase 1: cells of the halo tile ------------------------
   for (int c = tid; c < T::NC; c += T::NT) {
@@ -156,6 +168,12 @@ __device__ __forceinline__ void tile_step(
         ep = pr * ph.ggm1 + 0.5 * ro * vv;
       }
       const FT rx = ro * vx, ry = ro * vy;
+      if constexpr (G) {  // mlw_m3_g.f:95, 106, 117
+        const FT gxc(grav[g]), gyc(grav[2 * n + g]);
+        SGC(0, c) = (ro * (vx * gxc + vy * gyc)).v;
+        SGC(1, c) = (ro * gxc).v;
+        SGC(2, c) = (ro * gyc).v;
+      }
       SC(C::RO, c) = ro.v; SC(C::EE, c) = ee.v;
       SC(C::RX, c) = rx.v; SC(C::RY, c) = ry.v;
       SC(C::BX, c) = bx.v; SC(C::BY, c) = by.v;
@@ -190,6 +208,9 @@ __device__ __forceinline__ void tile_step(
     } else {
 #pragma unroll 1
       for (int s = 0; s < C::N; s++) SC(s, c) = 0.0;
+      if constexpr (G) {
+        SGC(0, c) = 0.0; SGC(1, c) = 0.0; SGC(2, c) = 0.0;
+      }
     }
   }
   __syncthreads();
@@ -237,9 +258,25 @@ __device__ __forceinline__ void tile_step(
         return un;
       };
       const FT roh = pred(C::RO, C::RX, C::RY, false, false);
-      const FT eeh = pred(C::EE, C::FXE, C::FYE, false, false);
-      const FT rxh = pred(C::RX, C::FXRX, C::FYRX, false, false);
-      const FT ryh = pred(C::RY, C::FXRY, C::FYRY, false, false);
+      FT eeh = pred(C::EE, C::FXE, C::FYE, false, false);
+      FT rxh = pred(C::RX, C::FXRX, C::FYRX, false, false);
+      FT ryh = pred(C::RY, C::FXRY, C::FYRY, false, false);
+      if constexpr (G) {
+        // mlwsrch part 2: un += dt * (average of the four cell sources)
+        auto srch = [&](int k, FT un) -> FT {
+          if constexpr (E) {
+            const FT sh = (FT(SGC(k, b)) + FT(SGC(k, a)) + FT(SGC(k, cc)) + FT(SGC(k, d))) /
+                          FT(4.0);
+            return un + dt * sh;
+          } else {
+            return FT(fma(dt.v, 0.25 * ((SGC(k, b) + SGC(k, a)) + (SGC(k, cc) + SGC(k, d))),
+                          un.v));
+          }
+        };
+        eeh = srch(0, eeh);
+        rxh = srch(1, rxh);
+        ryh = srch(2, ryh);
+      }
       const FT bxh = pred(C::BX, NOFLUX, C::EZ, false, false);
       const FT byh = pred(C::BY, C::EZ, NOFLUX, true, false);
       FT rzh(0.0), bzh(0.0);
@@ -271,6 +308,13 @@ __device__ __forceinline__ void tile_step(
       FT ep;
       if constexpr (E) ep = prh * gm / gm1 + 0.5 * roh * vv;
       else ep = prh * ph.ggm1 + 0.5 * roh * vv;
+      if constexpr (G) {  // corner sources (mlw_m3_g.f:194, 205, 216)
+        const size_t gk = (size_t)gi + (size_t)gj * ix;
+        const FT gxk(grav[n + gk]), gyk(grav[3 * n + gk]);
+        SGK(0, c) = (roh * (vxh * gxk + vyh * gyk)).v;
+        SGK(1, c) = (roh * gxk).v;
+        SGK(2, c) = (roh * gyk).v;
+      }
       SK(K::XRO, c) = (roh * vxh).v;
       SK(K::YRO, c) = (roh * vyh).v;
       if constexpr (M3) {
@@ -299,6 +343,9 @@ __device__ __forceinline__ void tile_step(
     } else {
 #pragma unroll 1
       for (int s = 0; s < K::N; s++) SK(s, c) = 0.0;
+      if constexpr (G) {
+        SGK(0, c) = 0.0; SGK(1, c) = 0.0; SGK(2, c) = 0.0;
+      }
     }
   }
   // artificial-viscosity face coefficients q*dxim (mlw_m3.f:325-334; the
@@ -353,7 +400,7 @@ __device__ __forceinline__ void tile_step(
     // du for one conserved variable: half-step central difference,
     // corrector and artificial viscosity, in the reference order.
     auto dstep = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx,
-                     bool nkx, int kfy, bool nky) -> FT {
+                     bool nkx, int kfy, bool nky, int gs) -> FT {
       FT du(0.0);
       // mlwhalf part 1 (mlwhalf.f:36-41)
       if (sfx != NOFLUX) {
@@ -366,6 +413,8 @@ __device__ __forceinline__ void tile_step(
         if (negy) { fn = -fn; fs = -fs; }
         du = du - hdt * (hdy * (fn - fs));
       }
+      // mlwsrch part 1: du += dt/2 * s (gravity)
+      if (G && gs >= 0) du = du + hdt * FT(SGC(gs, c));
       // mlwfull (mlwfull.f:136-146)
       if (kfx != NOFLUX) {
         FT sw(SK(kfx, kSW)), se(SK(kfx, kSE)), nw(SK(kfx, kNW)), ne(SK(kfx, kNE));
@@ -378,6 +427,12 @@ __device__ __forceinline__ void tile_step(
         if (nky) { sw = -sw; se = -se; nw = -nw; ne = -ne; }
         const FT dfdy = dyi * (ux0 * (nw - sw) + ux1 * (ne - se));
         du = du - hdt * dfdy;
+      }
+      // mlwsrcf: du += dt/2 * (corner sources weighted to the cell)
+      if (G && gs >= 0) {
+        const FT sh = uy0 * (ux0 * FT(SGK(gs, kSW)) + ux1 * FT(SGK(gs, kSE))) +
+                      uy1 * (ux0 * FT(SGK(gs, kNW)) + ux1 * FT(SGK(gs, kNE)));
+        du = du + hdt * sh;
       }
       // mlwartv (mlwartv.f:225-233)
       const FT u(SC(su, c));
@@ -396,8 +451,14 @@ __device__ __forceinline__ void tile_step(
     const double an = (dt * dyi * qyn).v, as = (dt * dyi * qys).v;
     const double a1 = 1.0 - ((ae + aw) + (an + as));
     auto fstep = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx,
-                     bool nkx, int kfy, bool nky) -> FT {
+                     bool nkx, int kfy, bool nky, int gs) -> FT {
       double r = a1 * SC(su, c);
+      if (G && gs >= 0) {
+        r = fma(hdt.v, SGC(gs, c), r);
+        const double w0 = (hdt * uy0).v, w1 = (hdt * uy1).v;
+        r = fma(w0, fma(ux0.v, SGK(gs, kSW), ux1.v * SGK(gs, kSE)), r);
+        r = fma(w1, fma(ux0.v, SGK(gs, kNW), ux1.v * SGK(gs, kNE)), r);
+      }
       r = fma(ae, SC(su, cE), r);
       r = fma(aw, SC(su, cW), r);
       r = fma(an, SC(su, cN), r);
@@ -423,14 +484,16 @@ __device__ __forceinline__ void tile_step(
       return FT(r);
     };
     auto step_var = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx,
-                        bool nkx, int kfy, bool nky) -> FT {
-      if constexpr (E) return dstep(su, sfx, negx, sfy, negy, kfx, nkx, kfy, nky);
-      else return fstep(su, sfx, negx, sfy, negy, kfx, nkx, kfy, nky);
+                        bool nkx, int kfy, bool nky, int gs = -1) -> FT {
+      if constexpr (E) return dstep(su, sfx, negx, sfy, negy, kfx, nkx, kfy, nky, gs);
+      else return fstep(su, sfx, negx, sfy, negy, kfx, nkx, kfy, nky, gs);
     };
     const FT ro = step_var(C::RO, C::RX, false, C::RY, false, K::XRO, false, K::YRO, false);
-    const FT ee = step_var(C::EE, C::FXE, false, C::FYE, false, K::XEE, false, K::YEE, false);
-    const FT rx = step_var(C::RX, C::FXRX, false, C::FYRX, false, K::XRX, false, K::YRX, false);
-    const FT ry = step_var(C::RY, C::FXRY, false, C::FYRY, false, K::XRY, false, K::YRY, false);
+    const FT ee = step_var(C::EE, C::FXE, false, C::FYE, false, K::XEE, false, K::YEE, false, 0);
+    const FT rx =
+        step_var(C::RX, C::FXRX, false, C::FYRX, false, K::XRX, false, K::YRX, false, 1);
+    const FT ry =
+        step_var(C::RY, C::FXRY, false, C::FYRY, false, K::XRY, false, K::YRY, false, 2);
     const FT bx = step_var(C::BX, NOFLUX, false, C::EZ, false, NOFLUX, false, K::EZ, false);
     const FT by = step_var(C::BY, C::EZ, true, NOFLUX, false, K::EZ, true, NOFLUX, false);
     FT rz(0.0), bz(0.0);
@@ -543,6 +606,8 @@ __device__ __forceinline__ void tile_step(
   }
 #undef SC
 #undef SK
+#undef SGC
+#undef SGK
 }
 
 }  // namespace cans

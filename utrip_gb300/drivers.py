@@ -103,6 +103,12 @@ def _step(setup, state, dt):
                             setup["dy"], setup["dym"], setup["dz"], setup["dzm"],
                             setup["mfdim"])
         return
+    if setup.get("gravity"):
+        g = [setup[k] for k in ("gx", "gxm", "gy", "gym")]
+        args = (setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"], setup["dy"],
+                setup["dym"])
+        (capi.mlw_m3_g if setup["solver"] == "mlw_m3" else capi.mlw_m_g)(*state, dt, *args)
+        return
     args = (setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"], setup["dym"])
     if setup["solver"] == "mlw_m_3d":
         capi.mlw_m_3d(*state, dt, *args, setup["dz"], setup["dzm"])

@@ -16,7 +16,7 @@ import math
 
 import numpy as np
 
-from .capi import (BD_FRE, BD_PER, BD_SMN, BD_SMP, BD_SPN, BD_SPP, SOLVER_HLLD_3D,
+from .capi import (BD_FRD, BD_FRE, BD_PER, BD_SMN, BD_SMP, BD_SPN, BD_SPP, SOLVER_HLLD_3D,
                    SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M3_2D, SOLVER_ROE_M_3D)
 
 SQ4PI = math.sqrt(4.0 * math.pi)
@@ -664,3 +664,95 @@ def spicule_1d(nx: int = 1024, torque: float = 30.0, seed: int = 0, tend: float 
                 safety=0.8, dtmin=1e-10, tend=tend, nstop=nstop, dtout=dtout, floor=floor,
                 trq=trq, trq0=float(torque), seed=int(seed), ztr=ztr, tcor=200.0,
                 name=f"spicule_{nx}", **prof)
+
+
+# ---- 2-D steps with gravity (mlw_m_g / mlw_m3_g) -------------------------------
+
+def mhd_gravity_wave(n: int = 64, solver: str = "mlw_m", amp: float = 0.5):
+    """The MHD gravity-wave model of cans2d/md_mhdgwave/hdmlw (model.f, bnd.f,
+    main.f:161-176): x in [0, 5], y in [-2, 6], margin 1, gamma 5/3,
+    uniform gravity gy = -1/gm on cells and corners, an isothermal
+    hydrostatic atmosphere built outward from the cell jzero with the
+    discrete balance of model.f, a vertical field with 1/beta = 0.05, and a
+    Gaussian pressure pulse of relative amplitude amp and width 0.2 at the
+    origin.  Boundaries: x symmetric (vx, bx odd), y free with constant
+    gradient for ro and pr and odd vy.  cfl_m safety 0.4, qav 3, tend 7.
+    solver "mlw_m3" adds vz = bz = 0."""
+    margin = 1
+    ix = jx = n + 2 * margin
+    gm = 5.0 / 3.0
+    ymax, ymin, xmax = 6.0, -2.0, 5.0
+    pi = math.acos(-1.0)
+    dx0 = xmax / float(ix - margin * 2)
+    dxm0 = np.full(ix, dx0)
+    izero = margin + 1
+    x = np.empty(ix)
+    x[izero - 1] = dxm0[izero - 1] / 2.0
+    for i in range(izero + 1, ix + 1):
+        x[i - 1] = x[i - 2] + dxm0[i - 2]
+    for i in range(izero - 1, 0, -1):
+        x[i - 1] = x[i] - dxm0[i - 1]
+    dy0 = (ymax - ymin) / float(jx - margin * 2)
+    dym0 = np.full(jx, dy0)
+    jzero = int(-ymin / dy0) + margin + 1
+    y = np.empty(jx)
+    y[jzero - 1] = dym0[jzero - 1] / 2.0
+    for j in range(jzero + 1, jx + 1):
+        y[j - 1] = y[j - 2] + dym0[j - 2]
+    for j in range(jzero - 1, 0, -1):
+        y[j - 1] = y[j] - dym0[j - 1]
+    g0 = -1.0 / gm
+    gym0 = np.full(jx, g0)
+    tem0 = np.ones(jx)
+    den0 = np.empty(jx)
+    pre0 = np.empty(jx)
+    den0[jzero - 1] = 1.0
+    pre0[jzero - 1] = 1.0 / gm * tem0[jzero - 1]
+    for j in range(jzero + 1, jx + 1):
+        h = 0.5 * gm * gym0[j - 2] * dym0[j - 2]
+        den0[j - 1] = den0[j - 2] * (tem0[j - 2] + h) / (tem0[j - 1] - h)
+        pre0[j - 1] = pre0[jzero - 1] * (den0[j - 1] / den0[jzero - 1]) * \
+            (tem0[j - 1] / tem0[jzero - 1])
+    for j in range(jzero - 1, 0, -1):
+        h = 0.5 * gm * gym0[j - 1] * dym0[j - 1]
+        den0[j - 1] = den0[j] * (tem0[j] - h) / (tem0[j - 1] + h)
+        pre0[j - 1] = pre0[jzero - 1] * (den0[j - 1] / den0[jzero - 1]) * \
+            (tem0[j - 1] / tem0[jzero - 1])
+    betai = float(np.float32(0.05))
+    bb0 = math.sqrt(8 * pi * 1 / gm * betai)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    shape = (ix, jx)
+    wexp = float(np.float32(0.2))
+    ss = np.sqrt(X ** 2 + Y ** 2)
+    f = {"ro": np.broadcast_to(den0, shape).copy(),
+         "pr": np.broadcast_to(pre0, shape) * (1 + amp * np.exp(-(ss / wexp) ** 2)),
+         "vx": np.zeros(shape), "vy": np.zeros(shape), "vz": np.zeros(shape),
+         "bx": np.zeros(shape), "by": np.full(shape, bb0), "bz": np.zeros(shape)}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, margin)
+    names = VARS[solver]
+    bc = []
+    for v, name in enumerate(names):
+        bc.append((v, 0, BD_SPN if name in ("vx", "bx") else BD_SPP, 0.0))
+        bc.append((v, 1, BD_SPN if name in ("vx", "bx") else BD_SPP, 0.0))
+    for v, name in enumerate(names):
+        kind = BD_FRD if name in ("ro", "pr") else (BD_SPN if name == "vy" else BD_FRE)
+        bc.append((v, 2, kind, 0.0))
+        bc.append((v, 3, kind, 0.0))
+    grav = dict(gx=np.zeros(shape, order="F"), gxm=np.zeros(shape, order="F"),
+                gy=np.full(shape, g0, order="F"), gym=np.full(shape, g0, order="F"))
+    return _pack(solver, x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+                 tend=7.0, gravity=True, name=f"mhd_gravity_wave_{n}_{solver}", **grav)
+
+
+def random_gravity(s: dict, seed: int = 0, scale: float = 0.3) -> dict:
+    """Seeded non-uniform gravity fields on a 2-D set-up (every source term
+    of mlw_m_g / mlw_m3_g non-zero): returns a copy with gx, gxm, gy, gym."""
+    rng = np.random.default_rng(seed)
+    shape = s["state"][0].shape
+    out = dict(s)
+    for k in ("gx", "gxm", "gy", "gym"):
+        out[k] = np.asfortranarray(scale * rng.standard_normal(shape))
+    out["gravity"] = True
+    return out
