@@ -597,6 +597,33 @@ cudaError_t launch_bc2d_transpose(int nvar, double *lam, int ix, int jx,
   return cudaSuccess;
 }
 
+// Raw output of a step rebuilt from the two filled states around it: the
+// step writes every cell but the outer layer, which it copies from its input,
+// and a boundary program of margin 1 without bdsmn* rules then rewrites only
+// that layer.  So R = P_next inside, P_cur on the outer layer.
+__global__ void k_adj_merge(const double *__restrict__ P_next,
+                            const double *__restrict__ P_cur, double *__restrict__ R,
+                            int nvar, int ix, int jx) {
+  const size_t n = (size_t)ix * jx;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n * nvar;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = t % n;
+    const int i = (int)(c % ix), j = (int)(c / ix);
+    const bool edge = i == 0 || i == ix - 1 || j == 0 || j == jx - 1;
+    R[t] = edge ? P_cur[t] : P_next[t];
+  }
+}
+
+cudaError_t launch_adj2d_merge(const double *P_next, const double *P_cur, double *R,
+                               int nvar, int ix, int jx, cudaStream_t s) {
+  const size_t total = (size_t)ix * jx * nvar;
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_adj_merge<<<(unsigned)blocks, 256, 0, s>>>(P_next, P_cur, R, nvar, ix, jx);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_adj2d_objective(const double *P, double *lam, double *J,
                                    double *scratch, int ix, int jx, const Axis &ax,
                                    const Axis &ay, const Phys &ph, cudaStream_t s) {

@@ -142,6 +142,10 @@ cudaError_t launch_adj2d_step(const double *P, const double *R,
                               double *scratch, int ix, int jx, const Axis &ax,
                               const Axis &ay, const Phys &ph, double dt,
                               cudaStream_t s);
+// raw output of a step (margin 1, no bdsmn* rule) from the filled states
+// before (P_cur: outer layer) and after it (P_next: every other cell)
+cudaError_t launch_adj2d_merge(const double *P_next, const double *P_cur, double *R,
+                               int nvar, int ix, int jx, cudaStream_t s);
 // transpose of the 2-D boundary program, in place on nvar adjoint arrays
 cudaError_t launch_bc2d_transpose(int nvar, double *lam, int ix, int jx,
                                   const Axis &ax, const Axis &ay,

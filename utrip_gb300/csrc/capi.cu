@@ -1785,6 +1785,8 @@ struct AdjWork {
   size_t n9 = 0;
   double *w[2] = {nullptr, nullptr};  // forward ping-pong buffers
   double *R = nullptr;                // raw output of the recorded step
+  double *next = nullptr;             // filled state after the step being reversed
+  long long next_k = -1;              // its step index (-1: none)
   double *lam[2] = {nullptr, nullptr};
   double *snap = nullptr;             // nsnap states
   double *scr = nullptr;              // adjoint-kernel scratch
@@ -1813,6 +1815,7 @@ int adj_setup(cans_run *h, AdjWork &W, int nsnap) {
     if ((rc = W.alloc(&W.lam[b], W.n9))) return rc;
   }
   if ((rc = W.alloc(&W.R, W.n9))) return rc;
+  if (nsnap > 0 && (rc = W.alloc(&W.next, W.n9))) return rc;
   if (nsnap > 0 && (rc = W.alloc(&W.snap, W.n9 * (size_t)nsnap))) return rc;
   if ((rc = W.alloc(&W.scr, adj2d_scratch_doubles(h->n)))) return rc;
   if ((rc = W.alloc(&W.J, 1))) return rc;
@@ -1844,20 +1847,24 @@ int adj_advance(cans_run *h, AdjWork &W, const double *A, long long k0,
 // Optimal binomial schedule: F(l, c) = minimal forward steps to reverse l
 // steps from a stored start with c free snapshots (Griewank's treeverse
 // recursion, solved by dynamic programming), and the first split of each.
+// `leaf` is the forward cost of reversing one step from its stored input: 1
+// when the step is re-run for its raw output, 0 when that output is rebuilt
+// from the state after it.
 struct Plan {
-  int L = 0, C = 0;
+  int L = 0, C = 0, leaf = -1;
   std::vector<long long> F;
   std::vector<int> split;
   long long &f(int l, int c) { return F[(size_t)l * (C + 1) + c]; }
   int &s(int l, int c) { return split[(size_t)l * (C + 1) + c]; }
-  void build(int L_, int C_) {
+  void build(int L_, int C_, int leaf_) {
     L = L_;
     C = C_;
+    leaf = leaf_;
     F.assign((size_t)(L + 1) * (C + 1), 0);
     split.assign((size_t)(L + 1) * (C + 1), 0);
-    for (int l = 1; l <= L; l++) f(l, 0) = (long long)l * (l + 1) / 2;
+    for (int l = 1; l <= L; l++) f(l, 0) = (long long)l * (l - 1) / 2 + (long long)l * leaf;
     for (int c = 1; c <= C; c++) {
-      f(1, c) = 1;
+      f(1, c) = leaf;
       for (int l = 2; l <= L; l++) {
         long long best = -1;
         int bm = 1;
@@ -1883,7 +1890,19 @@ struct AdjRun {
   long long L;
   long long nfwd = 0;
   bool have_J = false;
+  bool merge = false;  // raw outputs from consecutive states (no re-run)
 };
+
+// The raw output of step k is the next filled state inside and the state k
+// on the outer layer when the boundary program only rewrites that layer:
+// margin 1 and no bdsmn* rule (which also zeroes the boundary cell).
+bool adj_can_merge(const cans_run *h) {
+  if (h->bc.margin != 1) return false;
+  for (int v = 0; v < h->nvar; v++)
+    for (int f = 0; f < 4; f++)
+      if (h->bc.kind[v][f] == BD_SMN) return false;
+  return true;
+}
 
 // Reverse steps [a, b): on entry W.lam[0] is the adjoint of the filled state
 // b, on exit that of state a.  The state a is in snapshot `slot`.
@@ -1894,9 +1913,14 @@ int adj_reverse(AdjRun &r, long long a, long long b, int slot, int free_snaps) {
   const double *Sa = W.snap + n9 * (size_t)slot;
   const long long l = b - a;
   if (l == 1) {
-    // record: raw output R of step a
-    CK(step_kernel(h, h->tile, Sa, W.R, r.dts[a], nullptr, Box3{}));
-    r.nfwd++;
+    // raw output R of step a: rebuilt from the states a and a+1 when the
+    // reverse sweep has just left state a+1, else by re-running the step
+    if (r.merge && W.next_k == b) {
+      CK(launch_adj2d_merge(W.next, Sa, W.R, h->nvar, h->d.ix, h->d.jx, h->s));
+    } else {
+      CK(step_kernel(h, h->tile, Sa, W.R, r.dts[a], nullptr, Box3{}));
+      r.nfwd++;
+    }
     if (b == r.L && !r.have_J) {  // J and its gradient on the final state
       CK(launch_adj2d_objective(W.R, W.lam[0], W.J, W.scr, h->d.ix, h->d.jx, h->ax.a,
                                 h->ay.a, h->ph, h->s));
@@ -1907,6 +1931,10 @@ int adj_reverse(AdjRun &r, long long a, long long b, int slot, int free_snaps) {
     CK(launch_adj2d_step(Sa, W.R, W.lam[0], W.lam[1], W.scr, h->d.ix, h->d.jx, h->ax.a,
                          h->ay.a, h->ph, r.dts[a], h->s));
     std::swap(W.lam[0], W.lam[1]);
+    if (r.merge) {  // state a is the next one of the step reversed after this
+      CK(cudaMemcpyAsync(W.next, Sa, sizeof(double) * n9, cudaMemcpyDeviceToDevice, h->s));
+      W.next_k = a;
+    }
     return CANS_OK;
   }
   if (free_snaps == 0) {  // recompute from a for every step, last first
@@ -2005,8 +2033,11 @@ extern "C" int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts
                      cudaMemcpyDeviceToDevice, h->s));
   static Plan plan;  // reused while (nsteps, nsnap) repeat
   const int free_snaps = nsnap - 2;
-  if (plan.L != (int)nsteps || plan.C != free_snaps) plan.build((int)nsteps, free_snaps);
+  const bool merge = adj_can_merge(h);
+  if (plan.L != (int)nsteps || plan.C != free_snaps || plan.leaf != (merge ? 0 : 1))
+    plan.build((int)nsteps, free_snaps, merge ? 0 : 1);
   AdjRun r{h, W, plan, dts, nsteps};
+  r.merge = merge;
   if ((rc = adj_reverse(r, 0, nsteps, 0, free_snaps))) return rc;
   if (J) CK(cudaMemcpyAsync(J, W.J, sizeof(double), cudaMemcpyDeviceToHost, h->s));
   if (grad)
