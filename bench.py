@@ -52,7 +52,8 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary 3-D and 1-D workloads")
     p.add_argument("--profile-case", default=None,
-                   choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch"],
+                   choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
+                            "gravity2d", "spicule"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
@@ -63,7 +64,26 @@ def profile_case(case, n):
     or 5 batched iterations of 8 shear layers; prints one JSON line."""
     import torch
     from utrip_gb300 import capi, drivers, setups
-    if case in ("mlw3d", "roe3d", "hlld3d"):
+    if case in ("roe2d", "gravity2d"):
+        s = (setups.orszag_tang(n, solver="roe_m3") if case == "roe2d"
+             else setups.mhd_gravity_wave(n, solver="mlw_m3"))
+        run = drivers.make_run(s)
+        run.push(s["state"])
+        run.start(nstop=3, safety=s["safety"], dtmin=1e-10)
+        run.advance(3)
+        st = run.query()
+        run.close()
+        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+    elif case == "spicule":
+        s = setups.spicule_1d(n)
+        run = drivers.make_run(s)
+        run.push(s["state"])
+        run.start(nstop=200, tend=s["tend"], safety=s["safety"], dtmin=s["dtmin"])
+        run.advance(200)
+        st = run.query()
+        run.close()
+        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+    elif case in ("mlw3d", "roe3d", "hlld3d"):
         solver = {"mlw3d": "mlw_m_3d", "roe3d": "roe_m_3d", "hlld3d": "hlld_3d"}[case]
         s = setups.turbulence_3d(n, solver=solver)
         run = drivers.make_run(s)
