@@ -715,9 +715,13 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
   }
+  // one thread per cell of the block's segment (whole warps, 256 at most):
+  // threads without a cell would only wait at the barriers of every stage
+  int nt = ((p.lmax + 31) / 32) * 32;
+  nt = nt < 32 ? 32 : (nt > 256 ? 256 : nt);
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(CS, 1, 1);
-  cfg.blockDim = dim3(256, 1, 1);
+  cfg.blockDim = dim3(nt, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
