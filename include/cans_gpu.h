@@ -89,6 +89,53 @@ int cans_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
                     const double *gy, const double *gym, const double *dx,
                     const double *dxm, const int *ix, const double *dy,
                     const double *dym, const int *jx);
+/* replaces subroutine mlw_m3_e (cans2d/hdmlw/mlw_m3_e.f:2-3) and mlw_m_e
+ * (cans2d/hdmlw/mlw_m_e.f:2-3): the resistive steps; et at the cells, etm at
+ * the cell corners, ix*jx each.  The reference leaves the current density
+ * on the outer ring of cells, and the half-step field at corner ix / row jx,
+ * undefined; both are taken as zero. */
+int cans_mlw_m3_e_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                     double *bx, double *by, double *bz, double *az,
+                     const double *dt, const double *qav, const double *gm,
+                     const double *et, const double *etm, const double *dx,
+                     const double *dxm, const int *ix, const double *dy,
+                     const double *dym, const int *jx);
+int cans_mlw_m_e_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
+                    double *by, double *az, const double *dt, const double *qav,
+                    const double *gm, const double *et, const double *etm,
+                    const double *dx, const double *dxm, const int *ix,
+                    const double *dy, const double *dym, const int *jx);
+/* replaces subroutine mlw_m3_ge (cans2d/hdmlw/mlw_m3_ge.f:2-3) and mlw_m_ge
+ * (cans2d/hdmlw/mlw_m_ge.f:2-3): gravity and resistivity together */
+int cans_mlw_m3_ge_2d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                      double *bx, double *by, double *bz, double *az,
+                      const double *dt, const double *qav, const double *gm,
+                      const double *gx, const double *gxm, const double *gy,
+                      const double *gym, const double *et, const double *etm,
+                      const double *dx, const double *dxm, const int *ix,
+                      const double *dy, const double *dym, const int *jx);
+int cans_mlw_m_ge_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
+                     double *by, double *az, const double *dt, const double *qav,
+                     const double *gm, const double *gx, const double *gxm,
+                     const double *gy, const double *gym, const double *et,
+                     const double *etm, const double *dx, const double *dxm,
+                     const int *ix, const double *dy, const double *dym,
+                     const int *jx);
+/* replaces subroutine cfl_m3_e (cans2d/common/cfl_m3_e.f:2-3) and cfl_m_e
+ * (cans2d/common/cfl_m_e.f:2-3): the wave limit and the resistive diffusion
+ * limit safety*0.5*min(dx,dy)**2/max(et,1.e-5) */
+int cans_cfl_m3_e_2d(double *dt, const double *safety, const double *dtmin,
+                     int *merr, const double *gm, const double *ro,
+                     const double *pr, const double *vx, const double *vy,
+                     const double *vz, const double *bx, const double *by,
+                     const double *bz, const double *et, const double *dx,
+                     const int *ix, const double *dy, const int *jx);
+int cans_cfl_m_e_2d(double *dt, const double *safety, const double *dtmin,
+                    int *merr, const double *gm, const double *ro,
+                    const double *pr, const double *vx, const double *vy,
+                    const double *bx, const double *by, const double *et,
+                    const double *dx, const int *ix, const double *dy,
+                    const int *jx);
 /* replaces subroutine mlw_m   (cans2d/hdmlw/mlw_m.f:2-3) */
 int cans_mlw_m_2d(double *ro, double *pr, double *vx, double *vy, double *bx,
                   double *by, double *az, const double *dt, const double *qav,
@@ -345,6 +392,10 @@ typedef struct {
   unsigned long long seed;
   /* 2-D mLW with gravity: gy(ix,jx) at the cells, gym(ix,jx) at the corners */
   const double *gy, *gym;
+  /* 2-D mLW with resistivity (mlw_m_e / mlw_m3_e, with gx also mlw_m_ge /
+   * mlw_m3_ge): et(ix,jx) at the cells, etm(ix,jx) at the corners; the time
+   * step then includes the diffusion limit of cfl_m_e / cfl_m3_e */
+  const double *et, *etm;
 } cans_run_desc;
 
 typedef struct {

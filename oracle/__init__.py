@@ -48,6 +48,9 @@ def load():
         lib.oracle_mlw_m3_g_2d.argtypes = [_dp] * 9 + [d, d, d] + [_dp] * 6 + [i, _dp, _dp, i]
         lib.oracle_mlw_m_g_2d.argtypes = [_dp] * 7 + [d, d, d] + [_dp] * 6 + [i, _dp, _dp, i]
         lib.oracle_cfl_m3_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i]
+        lib.oracle_mlw_m3_ge_2d.argtypes = [_dp] * 9 + [d, d, d] + [_dp] * 8 + [i, _dp, _dp, i]
+        lib.oracle_mlw_m_ge_2d.argtypes = [_dp] * 7 + [d, d, d] + [_dp] * 8 + [i, _dp, _dp, i]
+        lib.oracle_cfl_m3_e_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 9 + [_dp, i, _dp, i]
         lib.oracle_cfl_m_2d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 6 + [_dp, i, _dp, i]
         lib.oracle_bd_2d.argtypes = [i, i, i, i, _dp, d, _dp, i, i]
         lib.oracle_bd_1d.argtypes = [i, i, i, _dp, d, _dp, i]
@@ -181,7 +184,57 @@ def mlw_m_g(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, dx, dxm, 
                              jx)
 
 
+def _Pn(a):
+    return None if a is None else P(a)
+
+
+def mlw_m3_e(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, et, etm, dx, dxm, dy, dym,
+             gx=None, gxm=None, gy=None, gym=None):
+    """cans2d/hdmlw/mlw_m3_e.f:2 (with gx..gym: mlw_m3_ge.f:2)"""
+    ix, jx = ro.shape
+    load().oracle_mlw_m3_ge_2d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)], dt,
+                               qav, gm, *[_Pn(a) for a in (gx, gxm, gy, gym)], P(et),
+                               P(etm), P(dx), P(dxm), ix, P(dy), P(dym), jx)
+
+
+def mlw_m_e(ro, pr, vx, vy, bx, by, az, dt, qav, gm, et, etm, dx, dxm, dy, dym,
+            gx=None, gxm=None, gy=None, gym=None):
+    """cans2d/hdmlw/mlw_m_e.f:2 (with gx..gym: mlw_m_ge.f:2)"""
+    ix, jx = ro.shape
+    load().oracle_mlw_m_ge_2d(*[P(a) for a in (ro, pr, vx, vy, bx, by, az)], dt, qav, gm,
+                              *[_Pn(a) for a in (gx, gxm, gy, gym)], P(et), P(etm), P(dx),
+                              P(dxm), ix, P(dy), P(dym), jx)
+
+
+def cfl_m3_e(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, et, dx, dy):
+    """cans2d/common/cfl_m3_e.f:2"""
+    ix, jx = ro.shape
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m3_e_2d(C.byref(dt), safety, dtmin, C.byref(merr), gm,
+                              *[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, et)],
+                              P(dx), ix, P(dy), jx)
+    return dt.value, merr.value
+
+
+def cfl_m_e(safety, dtmin, gm, ro, pr, vx, vy, bx, by, et, dx, dy):
+    """cans2d/common/cfl_m_e.f:2"""
+    ix, jx = ro.shape
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m3_e_2d(C.byref(dt), safety, dtmin, C.byref(merr), gm,
+                              P(ro), P(pr), P(vx), P(vy), None, P(bx), P(by), None, P(et),
+                              P(dx), ix, P(dy), jx)
+    return dt.value, merr.value
+
+
 def step_2d(setup, state, dt):
+    if setup.get("et") is not None:
+        e = [np.asfortranarray(setup[k]) for k in ("et", "etm")]
+        g = ([np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym")]
+             if setup.get("gravity") else [None] * 4)
+        (mlw_m3_e if setup["solver"] == "mlw_m3" else mlw_m_e)(
+            *state, dt, setup["qav"], setup["gm"], *e, setup["dx"], setup["dxm"], setup["dy"],
+            setup["dym"], *g)
+        return
     if setup.get("gravity"):
         g = [np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym")]
         args = (setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"], setup["dy"],
@@ -199,6 +252,13 @@ def step_2d(setup, state, dt):
 
 
 def cfl_2d(setup, state, safety):
+    if setup.get("et") is not None:
+        et = np.asfortranarray(setup["et"])
+        if setup["solver"] == "mlw_m3":
+            return cfl_m3_e(safety, setup["dtmin"], setup["gm"], *state[:8], et, setup["dx"],
+                            setup["dy"])
+        return cfl_m_e(safety, setup["dtmin"], setup["gm"], *state[:6], et, setup["dx"],
+                       setup["dy"])
     if setup["solver"] in ("mlw_m3", "roe_m3"):
         return cfl_m3(safety, setup["dtmin"], setup["gm"], *state[:8], setup["dx"], setup["dy"])
     return cfl_m(safety, setup["dtmin"], setup["gm"], *state[:6], setup["dx"], setup["dy"])

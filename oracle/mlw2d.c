@@ -10,10 +10,17 @@
  *   mlw_m3    cans2d/hdmlw/mlw_m3.f:64-374   (8 conserved variables + az)
  *   mlw_m     cans2d/hdmlw/mlw_m.f           (6 conserved variables + az)
  *   mlw_m3_g, mlw_m_g  cans2d/hdmlw/mlw_m3_g.f, mlw_m_g.f (the same with gravity)
+ *   mlw_m3_e, mlw_m_e  cans2d/hdmlw/mlw_m3_e.f, mlw_m_e.f (with resistivity)
+ *   mlw_m3_ge, mlw_m_ge cans2d/hdmlw/mlw_m3_ge.f, mlw_m_ge.f (both)
+ *   bbtocz, bbtocx, bbtocy  cans2d/common/bbtocz.f:30-41, bbtocx.f:29-33,
+ *             bbtocy.f:29-33 (current density)
+ *   cfl_m3_e, cfl_m_e  cans2d/common/cfl_m3_e.f:49-86, cfl_m_e.f:47-84
  *   cfl_m3    cans2d/common/cfl_m3.f:38-65
  *   cfl_m     cans2d/common/cfl_m.f:38-77
  *   bbtoaa    cans2d/common/bbtoaa.f:28-49
  */
+#include <string.h>
+
 #include "oracle.h"
 #include "oracle_common.h"
 
@@ -120,6 +127,52 @@ static void mlwartv2(const double *u, double *du, double dt, const double *qx,
                      (u[I2(i, j)] - u[I2(i, j - 1)])));
 }
 
+/* cans2d/common/bbtocz.f:30-41: z current density at the cells (or corners)
+ * 2..ix-1, 2..jx-1 from a 3x3 stencil of bx, by.  Entries outside that
+ * range are not written. */
+static void bbtocz2(double *cz, const double *bx, const double *by,
+                    const double *dx, const double *dy, int ix, int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++)
+      cz[I2(i, j)] =
+          (by[I2(i + 1, j)] - by[I2(i - 1, j)]) / dx[I1(i)] / 2.0 / 2.0 +
+          (by[I2(i + 1, j + 1)] - by[I2(i - 1, j + 1)]) / dx[I1(i)] / 2.0 / 4.0 +
+          (by[I2(i + 1, j - 1)] - by[I2(i - 1, j - 1)]) / dx[I1(i)] / 2.0 / 4.0 -
+          (bx[I2(i, j + 1)] - bx[I2(i, j - 1)]) / dy[I1(j)] / 2.0 / 2.0 -
+          (bx[I2(i + 1, j + 1)] - bx[I2(i + 1, j - 1)]) / dy[I1(j)] / 2.0 / 4.0 -
+          (bx[I2(i - 1, j + 1)] - bx[I2(i - 1, j - 1)]) / dy[I1(j)] / 2.0 / 4.0;
+}
+
+/* cans2d/common/bbtocx.f:29-33 */
+static void bbtocx2(double *cx, const double *bz, const double *dy, int ix,
+                    int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++)
+      cx[I2(i, j)] = (bz[I2(i, j + 1)] - bz[I2(i, j - 1)]) / dy[I1(j)] / 2.0;
+}
+
+/* cans2d/common/bbtocy.f:29-33 */
+static void bbtocy2(double *cy, const double *bz, const double *dx, int ix,
+                    int jx) {
+  OMP_FOR
+  for (int j = 2; j <= jx - 1; j++)
+    for (int i = 2; i <= ix - 1; i++)
+      cy[I2(i, j)] = -(bz[I2(i + 1, j)] - bz[I2(i - 1, j)]) / dx[I1(i)] / 2.0;
+}
+
+/* The resistive steps leave two sets of values undefined: the current
+ * density on the outer ring of cells (bbtocz writes 2..ix-1 only) and the
+ * half-step field at corner ix / row jx, which mlwhalf never sets but the
+ * corner bbtocz reads for corner ix-1.  Both are taken as zero here; in
+ * the md_recon and md_reccnd set-ups et and etm vanish there, so nothing
+ * depends on them. */
+static void zero_edge_corners(double *a, int ix, int jx) {
+  for (int j = 1; j <= jx; j++) a[I2(ix, j)] = 0.0;
+  for (int i = 1; i <= ix; i++) a[I2(i, jx)] = 0.0;
+}
+
 /* Metric set-up shared by mlw_m and mlw_m3 (mlw_m3.f:70-86). */
 static void metrics2(const double *dx, const double *dxm, int ix,
                      const double *dy, const double *dym, int jx, double *dxi,
@@ -151,11 +204,12 @@ static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
                         double *vz, double *bx, double *by, double *bz,
                         double *az, double dt, double qav, double gm,
                         const double *gx, const double *gxm, const double *gy,
-                        const double *gym, const double *dx, const double *dxm,
+                        const double *gym, const double *et, const double *etm,
+                        const double *dx, const double *dxm,
                         int ix, const double *dy, const double *dym, int jx) {
   const size_t n = (size_t)ix * (size_t)jx;
   const size_t nm = (size_t)(ix > jx ? ix : jx);
-  enum { NT = 37 };
+  enum { NT = 43 };
   double *w = arena_get(&arena2d, NT * n + 8 * nm);
   double *t[NT];
   for (int a = 0; a < NT; a++) t[a] = w + a * n;
@@ -168,6 +222,8 @@ static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
   double *dro = t[23], *dee = t[24], *drx = t[25], *dry = t[26], *drz = t[27];
   double *dbx = t[28], *dby = t[29], *dbz = t[30], *daz = t[31];
   double *fx = t[32], *qx = t[33], *fy = t[34], *qy = t[35], *ss = t[36];
+  double *cx = t[37], *cy = t[38], *cz = t[39];
+  double *cxh = t[40], *cyh = t[41], *czh = t[42];
   double *m = w + NT * n;
   double *dxi = m, *dxim = m + nm, *ux0 = m + 2 * nm, *ux1 = m + 3 * nm;
   double *dyi = m + 4 * nm, *dyim = m + 5 * nm, *uy0 = m + 6 * nm,
@@ -206,6 +262,22 @@ static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
       ey[c] = -vz[c] * bx[c] + vx[c] * bz[c];
       ez[c] = -vx[c] * by[c] + vy[c] * bx[c];
     }
+  if (et) {  /* mlw_m3_e.f:124-132: E += et * J */
+    memset(cx, 0, n * sizeof(double));
+    memset(cy, 0, n * sizeof(double));
+    memset(cz, 0, n * sizeof(double));
+    bbtocx2(cx, bz, dy, ix, jx);
+    bbtocy2(cy, bz, dx, ix, jx);
+    bbtocz2(cz, bx, by, dx, dy, ix, jx);
+    OMP_FOR
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I2(i, j);
+        ex[c] = -vy[c] * bz[c] + vz[c] * by[c] + et[c] * cx[c];
+        ey[c] = -vz[c] * bx[c] + vx[c] * bz[c] + et[c] * cy[c];
+        ez[c] = -vx[c] * by[c] + vy[c] * bx[c] + et[c] * cz[c];
+      }
+  }
 
   /* density (:129-135) */
   OMP_FOR
@@ -336,6 +408,25 @@ static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
       eyh[c] = -vzh[c] * bxh[c] + vxh[c] * bzh[c];
       ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c];
     }
+  if (et) {  /* mlw_m3_e.f:236-244: Eh += etm * Jh at the corners */
+    zero_edge_corners(bxh, ix, jx);
+    zero_edge_corners(byh, ix, jx);
+    zero_edge_corners(bzh, ix, jx);
+    memset(cxh, 0, n * sizeof(double));
+    memset(cyh, 0, n * sizeof(double));
+    memset(czh, 0, n * sizeof(double));
+    bbtocx2(cxh, bzh, dym, ix, jx);
+    bbtocy2(cyh, bzh, dxm, ix, jx);
+    bbtocz2(czh, bxh, byh, dxm, dym, ix, jx);
+    OMP_FOR
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        size_t c = I2(i, j);
+        exh[c] = -vyh[c] * bzh[c] + vzh[c] * byh[c] + etm[c] * cxh[c];
+        eyh[c] = -vzh[c] * bxh[c] + vxh[c] * bzh[c] + etm[c] * cyh[c];
+        ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c] + etm[c] * czh[c];
+      }
+  }
 
   /* full step: density (:235-241) */
   OMP_FOR
@@ -506,12 +597,13 @@ static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
 static void mlw_m_core(double *ro, double *pr, double *vx, double *vy,
                        double *bx, double *by, double *az, double dt, double qav,
                        double gm, const double *gx, const double *gxm,
-                       const double *gy, const double *gym, const double *dx,
+                       const double *gy, const double *gym, const double *et,
+                       const double *etm, const double *dx,
                        const double *dxm, int ix, const double *dy,
                        const double *dym, int jx) {
   const size_t n = (size_t)ix * (size_t)jx;
   const size_t nm = (size_t)(ix > jx ? ix : jx);
-  enum { NT = 27 };
+  enum { NT = 29 };
   double *w = arena_get(&arena2d, NT * n + 8 * nm);
   double *t[NT];
   for (int a = 0; a < NT; a++) t[a] = w + a * n;
@@ -522,6 +614,7 @@ static void mlw_m_core(double *ro, double *pr, double *vx, double *vy,
   double *dro = t[15], *dee = t[16], *drx = t[17], *dry = t[18];
   double *dbx = t[19], *dby = t[20], *daz = t[21];
   double *fx = t[22], *qx = t[23], *fy = t[24], *qy = t[25], *ss = t[26];
+  double *cz = t[27], *czh = t[28];
   double *m = w + NT * n;
   double *dxi = m, *dxim = m + nm, *ux0 = m + 2 * nm, *ux1 = m + 3 * nm;
   double *dyi = m + 4 * nm, *dyim = m + 5 * nm, *uy0 = m + 6 * nm,
@@ -549,11 +642,16 @@ static void mlw_m_core(double *ro, double *pr, double *vx, double *vy,
       rx[c] = ro[c] * vx[c];
       ry[c] = ro[c] * vy[c];
     }
+  if (et) {  /* mlw_m_e.f:125-129: ez += et * cz */
+    memset(cz, 0, n * sizeof(double));
+    bbtocz2(cz, bx, by, dx, dy, ix, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx; j++)
     for (int i = 1; i <= ix; i++) {
       size_t c = I2(i, j);
-      ez[c] = -vx[c] * by[c] + vy[c] * bx[c];
+      ez[c] = et ? -vx[c] * by[c] + vy[c] * bx[c] + et[c] * cz[c]
+                 : -vx[c] * by[c] + vy[c] * bx[c];
     }
   OMP_FOR
   for (int j = 1; j <= jx; j++)
@@ -649,11 +747,18 @@ static void mlw_m_core(double *ro, double *pr, double *vx, double *vy,
       double bb = bxh[c] * bxh[c] + byh[c] * byh[c];
       prh[c] = (gm - 1) * (eeh[c] - 0.5 * roh[c] * vv - pi8i * bb);
     }
+  if (et) {  /* mlw_m_e.f:216-220: ezh += etm * czh */
+    zero_edge_corners(bxh, ix, jx);
+    zero_edge_corners(byh, ix, jx);
+    memset(czh, 0, n * sizeof(double));
+    bbtocz2(czh, bxh, byh, dxm, dym, ix, jx);
+  }
   OMP_FOR
   for (int j = 1; j <= jx; j++)
     for (int i = 1; i <= ix; i++) {
       size_t c = I2(i, j);
-      ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c];
+      ezh[c] = et ? -vxh[c] * byh[c] + vyh[c] * bxh[c] + etm[c] * czh[c]
+                  : -vxh[c] * byh[c] + vyh[c] * bxh[c];
     }
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
@@ -790,7 +895,7 @@ void oracle_mlw_m3_2d(double *ro, double *pr, double *vx, double *vy,
                       const double *dx, const double *dxm, int ix,
                       const double *dy, const double *dym, int jx) {
   mlw_m3_core(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, NULL, NULL, NULL, NULL,
-              dx, dxm, ix, dy, dym, jx);
+              NULL, NULL, dx, dxm, ix, dy, dym, jx);
 }
 
 void oracle_mlw_m3_g_2d(double *ro, double *pr, double *vx, double *vy,
@@ -800,15 +905,15 @@ void oracle_mlw_m3_g_2d(double *ro, double *pr, double *vx, double *vy,
                         const double *gym, const double *dx, const double *dxm,
                         int ix, const double *dy, const double *dym, int jx) {
   mlw_m3_core(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, gx, gxm, gy, gym,
-              dx, dxm, ix, dy, dym, jx);
+              NULL, NULL, dx, dxm, ix, dy, dym, jx);
 }
 
 void oracle_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
                      double *bx, double *by, double *az, double dt, double qav,
                      double gm, const double *dx, const double *dxm, int ix,
                      const double *dy, const double *dym, int jx) {
-  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, NULL, NULL, NULL, NULL, dx, dxm,
-             ix, dy, dym, jx);
+  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, NULL, NULL, NULL, NULL, NULL,
+             NULL, dx, dxm, ix, dy, dym, jx);
 }
 
 void oracle_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
@@ -817,8 +922,70 @@ void oracle_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
                        const double *gy, const double *gym, const double *dx,
                        const double *dxm, int ix, const double *dy,
                        const double *dym, int jx) {
-  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, dx, dxm, ix,
-             dy, dym, jx);
+  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, NULL, NULL,
+             dx, dxm, ix, dy, dym, jx);
+}
+
+/* mlw_m3_e / mlw_m3_ge (cans2d/hdmlw/mlw_m3_e.f:2, mlw_m3_ge.f:2): gx NULL
+ * gives the step without gravity. */
+void oracle_mlw_m3_ge_2d(double *ro, double *pr, double *vx, double *vy,
+                         double *vz, double *bx, double *by, double *bz,
+                         double *az, double dt, double qav, double gm,
+                         const double *gx, const double *gxm, const double *gy,
+                         const double *gym, const double *et, const double *etm,
+                         const double *dx, const double *dxm, int ix,
+                         const double *dy, const double *dym, int jx) {
+  mlw_m3_core(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, gx, gxm, gy, gym,
+              et, etm, dx, dxm, ix, dy, dym, jx);
+}
+
+/* mlw_m_e / mlw_m_ge (cans2d/hdmlw/mlw_m_e.f:2, mlw_m_ge.f:2) */
+void oracle_mlw_m_ge_2d(double *ro, double *pr, double *vx, double *vy,
+                        double *bx, double *by, double *az, double dt, double qav,
+                        double gm, const double *gx, const double *gxm,
+                        const double *gy, const double *gym, const double *et,
+                        const double *etm, const double *dx, const double *dxm,
+                        int ix, const double *dy, const double *dym, int jx) {
+  mlw_m_core(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, et, etm,
+             dx, dxm, ix, dy, dym, jx);
+}
+
+/* cfl_m3_e / cfl_m_e (cans2d/common/cfl_m3_e.f:49-86, cfl_m_e.f:47-84): the
+ * wave limit of cfl_m3 / cfl_m and the diffusion limit
+ * safety*0.5*dmesh**2/max(et,etmin), etmin the single-precision 1.e-5.
+ * bz, vz NULL gives cfl_m_e. */
+void oracle_cfl_m3_e_2d(double *dt, double safety, double dtmin, int *merr,
+                        double gm, const double *ro, const double *pr,
+                        const double *vx, const double *vy, const double *vz,
+                        const double *bx, const double *by, const double *bz,
+                        const double *et, const double *dx, int ix,
+                        const double *dy, int jx) {
+  const double pi = acos(-1.0);
+  const double pi4i = 1. / pi / 4.;
+  const double etmin = (double)1.e-5f;
+  double dmin = R4_1E20;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(min : dmin) schedule(static)
+#endif
+  for (int j = 1; j <= jx; j++)
+    for (int i = 1; i <= ix; i++) {
+      size_t c = I2(i, j);
+      double dmesh = fmin2(dx[I1(i)], dy[I1(j)]);
+      double b2 = bz ? bx[c] * bx[c] + by[c] * by[c] + bz[c] * bz[c]
+                     : bx[c] * bx[c] + by[c] * by[c];
+      double ca2 = b2 * pi4i / ro[c];
+      double cs2 = gm * pr[c] / ro[c];
+      double v2 = vz ? vx[c] * vx[c] + vy[c] * vy[c] + vz[c] * vz[c]
+                     : vx[c] * vx[c] + vy[c] * vy[c];
+      double dtcfl = dmesh / sqrt(v2 + cs2 + ca2);
+      double dtwav = safety * dtcfl;
+      double dtdif = safety * 0.5 * (dmesh * dmesh) / fmax2(et[c], etmin);
+      double dtq = fmin2(dtwav, dtdif);
+      if (dtq < dmin) dmin = dtq;
+    }
+  *dt = dmin;
+  *merr = 0;
+  if (*dt < dtmin) *merr = 9001;
 }
 
 void oracle_cfl_m3_2d(double *dt, double safety, double dtmin, int *merr,

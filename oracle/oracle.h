@@ -108,6 +108,31 @@ void oracle_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
                        const double *gy, const double *gym, const double *dx,
                        const double *dxm, int ix, const double *dy,
                        const double *dym, int jx);
+/* mlw_m3_e / mlw_m3_ge and mlw_m_e / mlw_m_ge (cans2d/hdmlw/mlw_m3_e.f:2,
+ * mlw_m3_ge.f:2, mlw_m_e.f:2, mlw_m_ge.f:2): resistivity et at the cells and
+ * etm at the corners (ix*jx each); gx..gym NULL for the steps without
+ * gravity. */
+void oracle_mlw_m3_ge_2d(double *ro, double *pr, double *vx, double *vy,
+                         double *vz, double *bx, double *by, double *bz,
+                         double *az, double dt, double qav, double gm,
+                         const double *gx, const double *gxm, const double *gy,
+                         const double *gym, const double *et, const double *etm,
+                         const double *dx, const double *dxm, int ix,
+                         const double *dy, const double *dym, int jx);
+void oracle_mlw_m_ge_2d(double *ro, double *pr, double *vx, double *vy,
+                        double *bx, double *by, double *az, double dt, double qav,
+                        double gm, const double *gx, const double *gxm,
+                        const double *gy, const double *gym, const double *et,
+                        const double *etm, const double *dx, const double *dxm,
+                        int ix, const double *dy, const double *dym, int jx);
+/* cfl_m3_e / cfl_m_e (cans2d/common/cfl_m3_e.f:2, cfl_m_e.f:2); vz, bz NULL
+ * for cfl_m_e */
+void oracle_cfl_m3_e_2d(double *dt, double safety, double dtmin, int *merr,
+                        double gm, const double *ro, const double *pr,
+                        const double *vx, const double *vy, const double *vz,
+                        const double *bx, const double *by, const double *bz,
+                        const double *et, const double *dx, int ix,
+                        const double *dy, int jx);
 void oracle_cfl_m3_2d(double *dt, double safety, double dtmin, int *merr,
                       double gm, const double *ro, const double *pr,
                       const double *vx, const double *vy, const double *vz,

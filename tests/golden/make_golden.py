@@ -118,6 +118,28 @@ def case_grav(solver, ix, jx, seed):
     return out
 
 
+def case_res(solver, ix, jx, seed, grav):
+    """One resistive 2-D step (mlw_m_e / mlw_m3_e, with gravity mlw_m_ge /
+    mlw_m3_ge) of a seeded state with seeded resistivity, dt from cfl_m_e /
+    cfl_m3_e."""
+    s = setups.random_resistivity(
+        setups.random_state(ix, jx, seed=seed, solver=solver, margin=2), seed + 1)
+    if grav:
+        s = setups.random_gravity(s, seed + 2)
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dxm", "dy", "dym"):
+        out["grid_" + k] = s[k]
+    for k in ("et", "etm") + (("gx", "gxm", "gy", "gym") if grav else ()):
+        out["src_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_2d(s, st, 0.4)
+    oracle.step_2d(s, st, dt)
+    out["dt"] = np.array(dt)
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def bd_case():
     rng = np.random.default_rng(13)
     q = np.asfortranarray(rng.standard_normal((9, 7)))
@@ -143,6 +165,8 @@ FIXTURES = {
     "roe_m_1d_70": lambda: case_roe1(70, 24),
     "mlw_m_g_2d_19x16": lambda: case_grav("mlw_m", 19, 16, 25),
     "mlw_m3_g_2d_17x18": lambda: case_grav("mlw_m3", 17, 18, 26),
+    "mlw_m_e_2d_18x17": lambda: case_res("mlw_m", 18, 17, 27, False),
+    "mlw_m3_ge_2d_17x19": lambda: case_res("mlw_m3", 17, 19, 28, True),
 }
 
 

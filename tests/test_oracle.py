@@ -789,3 +789,113 @@ def test_gravity_oracle_matches_frozen_fixture(oracle_lib):
         oracle_lib.step_2d(s, st, float(z["dt"]))
         for k, a in zip(names, st):
             assert np.array_equal(a, z["out_" + k]), (name, k)
+
+
+# ---- resistive 2-D steps (mlw_m_e, mlw_m3_e, mlw_m_ge, mlw_m3_ge) ------------
+
+@pytest.mark.parametrize("solver", ["mlw_m", "mlw_m3"])
+@pytest.mark.parametrize("grav", [False, True])
+def test_resistive_step_with_zero_resistivity_is_the_plain_step(oracle_lib, solver, grav):
+    s = setups.random_state(20, 17, seed=5, solver=solver, margin=2)
+    if grav:
+        s = setups.random_gravity(s, 6)
+    z = np.zeros(s["state"][0].shape, order="F")
+    e = dict(s, et=z, etm=z)
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    oracle_lib.step_2d(s, a, 2e-3)
+    oracle_lib.step_2d(e, b, 2e-3)
+    for k, x, y in zip(s["names"], a, b):
+        assert np.array_equal(x, y), k
+
+
+@pytest.mark.parametrize("solver", ["mlw_m", "mlw_m3"])
+def test_resistive_step_diffuses_a_field_ripple(oracle_lib, solver):
+    """v = 0, bx = 0, by = a sin(2 pi x) with uniform resistivity eta: the
+    induction equation reduces to d(by)/dt = eta d2(by)/dx2 (E = eta J,
+    J = d(by)/dx in these units), so one step lowers the ripple by
+    eta k^2 dt to the accuracy of the 3x3 current stencil.  In mlw_m3 a
+    ripple of bz decays at the same rate through the x and y currents."""
+    s = setups.random_state(68, 12, seed=7, solver=solver, margin=2)
+    shape = s["state"][0].shape
+    X = np.broadcast_to(s["x"][:, None], shape)
+    a0, eta, dt = 1e-3, 0.01, 1e-3
+    k = 2 * math.pi
+    vals = {n: np.zeros(shape) for n in s["names"]}
+    vals["ro"][:] = 1.0
+    vals["pr"][:] = 1.0
+    vals["by"] = a0 * np.sin(k * X)
+    if solver == "mlw_m3":
+        vals["bz"] = a0 * np.cos(k * X)
+    st = [np.asfortranarray(vals[n]) for n in s["names"]]
+    e = dict(s, qav=0.0, et=np.full(shape, eta, order="F"), etm=np.full(shape, eta, order="F"))
+    before = setups.copy_state(dict(s, state=st))
+    oracle_lib.step_2d(e, st, dt)
+    inner = (slice(4, -4), slice(3, -3))
+    for name in ("by", "bz") if solver == "mlw_m3" else ("by",):
+        v = s["names"].index(name)
+        got = (st[v] - before[v])[inner]
+        want = (-eta * k * k * dt * before[v])[inner]
+        assert np.max(np.abs(got - want)) < 0.02 * np.max(np.abs(want)), name
+
+
+@pytest.mark.parametrize("solver", ["mlw_m", "mlw_m3"])
+def test_cfl_e_matches_a_numpy_restatement(oracle_lib, solver):
+    """cfl_m_e / cfl_m3_e (cans2d/common/cfl_m_e.f:47-84): min over cells of
+    min(safety*dmesh/sqrt(v2+cs2+ca2), safety*0.5*dmesh**2/max(et,etmin)),
+    etmin the single-precision 1.e-5; the resistivity is large enough that
+    the diffusion limit binds."""
+    s = setups.random_resistivity(setups.random_state(30, 26, seed=8, solver=solver,
+                                                      margin=2), 9, scale=0.5)
+    st = s["state"]
+    nm = s["names"]
+    g = {n: st[nm.index(n)] for n in nm}
+    pi4i = 1.0 / math.acos(-1.0) / 4.0
+    b2 = g["bx"] * g["bx"] + g["by"] * g["by"]
+    v2 = g["vx"] * g["vx"] + g["vy"] * g["vy"]
+    if solver == "mlw_m3":
+        b2 = b2 + g["bz"] * g["bz"]
+        v2 = v2 + g["vz"] * g["vz"]
+    ca2 = b2 * pi4i / g["ro"]
+    cs2 = s["gm"] * g["pr"] / g["ro"]
+    dmesh = np.minimum(s["dx"][:, None], s["dy"][None, :])
+    dtwav = 0.4 * (dmesh / np.sqrt(v2 + cs2 + ca2))
+    dtdif = 0.4 * 0.5 * (dmesh * dmesh) / np.maximum(s["et"], float(np.float32(1e-5)))
+    want = float(np.min(np.minimum(dtwav, dtdif)))
+    assert want < float(np.min(dtwav))  # the diffusion limit binds
+    dt, merr = oracle_lib.cfl_2d(s, st, 0.4)
+    assert merr == 0 and dt == want
+
+
+def test_resistive_oracle_matches_frozen_fixture(oracle_lib):
+    for name, solver, grav in (("mlw_m_e_2d_18x17", "mlw_m", False),
+                               ("mlw_m3_ge_2d_17x19", "mlw_m3", True)):
+        z = np.load(GOLD / f"{name}.npz")
+        names = setups.VARS[solver]
+        st = [np.asfortranarray(z["in_" + k]) for k in names]
+        src = {k[4:]: np.asfortranarray(z[k]) for k in z.files if k.startswith("src_")}
+        s = dict(solver=solver, gravity=grav, qav=3.0, gm=5.0 / 3.0, dtmin=1e-10, **src,
+                 **{k: z["grid_" + k] for k in ("dx", "dxm", "dy", "dym")})
+        dt, _ = oracle_lib.cfl_2d(s, st, 0.4)
+        assert dt == float(z["dt"]), name
+        oracle_lib.step_2d(s, st, dt)
+        for k, a in zip(names, st):
+            assert np.array_equal(a, z["out_" + k]), (name, k)
+
+
+def test_reconnection_setup_follows_the_model(oracle_lib):
+    """md_recon/hdmlw/model.f: pressure balance p + by^2/(8 pi) = (1+betai)/gm,
+    ro = p gm, resistivity only inside r < 0.8 with its peak etai = 0.03 at
+    the origin, and one loop step keeps the solution finite."""
+    s = setups.magnetic_reconnection(32)
+    g = dict(zip(s["names"], s["state"]))
+    tot = g["pr"] + g["by"] ** 2 / (8 * math.pi)
+    assert np.allclose(tot, 11.0 / (5.0 / 3.0), rtol=1e-14)
+    assert np.array_equal(g["ro"], g["pr"] * (5.0 / 3.0))
+    X = np.broadcast_to(s["x"][:, None], g["ro"].shape)
+    Y = np.broadcast_to(s["y"][None, :], g["ro"].shape)
+    rr = np.sqrt(X * X + Y * Y)
+    assert np.all(s["et"][rr >= 0.8] == 0.0) and np.all(s["et"][rr < 0.8] > 0.0)
+    assert 0.0 < s["et"].max() < 0.03
+    st = setups.copy_state(s)
+    t, ns, merr, dts = oracle_lib.run_2d(s, st, 5)
+    assert ns == 5 and merr == 0 and all(np.all(np.isfinite(a)) for a in st)

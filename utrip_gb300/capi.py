@@ -99,6 +99,12 @@ def load() -> C.CDLL:
     sig["cans_roe_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_mlw_m3_g_2d"] = (i, [_dp] * 9 + [_dp] * 7 + [_dp, _dp, _ip, _dp, _dp, _ip])
     sig["cans_mlw_m_g_2d"] = (i, [_dp] * 7 + [_dp] * 7 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_mlw_m3_e_2d"] = (i, [_dp] * 9 + [_dp] * 5 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_mlw_m_e_2d"] = (i, [_dp] * 7 + [_dp] * 5 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_mlw_m3_ge_2d"] = (i, [_dp] * 9 + [_dp] * 9 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_mlw_m_ge_2d"] = (i, [_dp] * 7 + [_dp] * 9 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_cfl_m3_e_2d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 9 + [_dp, _ip, _dp, _ip])
+    sig["cans_cfl_m_e_2d"] = (i, [_dp, _dp, _dp, _ip, _dp] + [_dp] * 7 + [_dp, _ip, _dp, _ip])
     sig["cans_roe_m3_2d"] = (i, [_dp] * 9 + [_dp, _dp, _dp, _ip, _dp, _ip])
     sig["cans_hlld_engine_3d"] = (i, [_dp] * 8 + [_dp] * 9 + [_ip] * 4)
     sig["cans_mlw_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _dp, _dp, _ip])
@@ -204,6 +210,59 @@ def mlw_m_g(ro, pr, vx, vy, bx, by, az, dt, qav, gm, gx, gxm, gy, gym, dx, dxm, 
         *[_ptr(a) for a in (ro, pr, vx, vy, bx, by, az)], _dref(dt), _dref(qav), _dref(gm),
         *[_ptr(a) for a in (gx, gxm, gy, gym)], _ptr(dx), _ptr(dxm), _iref(ix), _ptr(dy),
         _ptr(dym), _iref(jx)), "mlw_m_g")
+
+
+def mlw_m3_e(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, et, etm, dx, dxm, dy, dym,
+             gx=None, gxm=None, gy=None, gym=None):
+    """cans2d/hdmlw/mlw_m3_e.f:2 -- mlw_m3 with resistivity et (cells) and
+    etm (corners), in place; with gx..gym mlw_m3_ge (mlw_m3_ge.f:2)."""
+    ix, jx = ro.shape
+    st = [_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)]
+    tail = (_ptr(et), _ptr(etm), _ptr(dx), _ptr(dxm), _iref(ix), _ptr(dy), _ptr(dym),
+            _iref(jx))
+    if gx is None:
+        return _check(load().cans_mlw_m3_e_2d(*st, _dref(dt), _dref(qav), _dref(gm), *tail),
+                      "mlw_m3_e")
+    return _check(load().cans_mlw_m3_ge_2d(*st, _dref(dt), _dref(qav), _dref(gm),
+                                           *[_ptr(a) for a in (gx, gxm, gy, gym)], *tail),
+                  "mlw_m3_ge")
+
+
+def mlw_m_e(ro, pr, vx, vy, bx, by, az, dt, qav, gm, et, etm, dx, dxm, dy, dym,
+            gx=None, gxm=None, gy=None, gym=None):
+    """cans2d/hdmlw/mlw_m_e.f:2 -- mlw_m with resistivity, in place; with
+    gx..gym mlw_m_ge (mlw_m_ge.f:2)."""
+    ix, jx = ro.shape
+    st = [_ptr(a) for a in (ro, pr, vx, vy, bx, by, az)]
+    tail = (_ptr(et), _ptr(etm), _ptr(dx), _ptr(dxm), _iref(ix), _ptr(dy), _ptr(dym),
+            _iref(jx))
+    if gx is None:
+        return _check(load().cans_mlw_m_e_2d(*st, _dref(dt), _dref(qav), _dref(gm), *tail),
+                      "mlw_m_e")
+    return _check(load().cans_mlw_m_ge_2d(*st, _dref(dt), _dref(qav), _dref(gm),
+                                          *[_ptr(a) for a in (gx, gxm, gy, gym)], *tail),
+                  "mlw_m_ge")
+
+
+def cfl_m3_e(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, et, dx, dy):
+    """cans2d/common/cfl_m3_e.f:2 -- returns (dt, merr)."""
+    ix, jx = ro.shape
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m3_e_2d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                   _dref(gm),
+                                   *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, et)],
+                                   _ptr(dx), _iref(ix), _ptr(dy), _iref(jx)), "cfl_m3_e")
+    return dt.value, merr.value
+
+
+def cfl_m_e(safety, dtmin, gm, ro, pr, vx, vy, bx, by, et, dx, dy):
+    """cans2d/common/cfl_m_e.f:2 -- returns (dt, merr)."""
+    ix, jx = ro.shape
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m_e_2d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                  _dref(gm), *[_ptr(a) for a in (ro, pr, vx, vy, bx, by, et)],
+                                  _ptr(dx), _iref(ix), _ptr(dy), _iref(jx)), "cfl_m_e")
+    return dt.value, merr.value
 
 
 def mlw_m(ro, pr, vx, vy, bx, by, az, dt, qav, gm, dx, dxm, dy, dym):
@@ -446,7 +505,8 @@ class _Desc(C.Structure):
                 ("gx", _dp), ("gxm", _dp), ("sc", _dp), ("scm", _dp), ("dsc", _dp),
                 ("dscm", _dp), ("rr", _dp), ("rrm", _dp), ("drr", _dp), ("drrm", _dp),
                 ("chkdav", C.c_int), ("floor", C.c_double), ("trq", _dp),
-                ("trq0", C.c_double), ("seed", C.c_ulonglong), ("gy", _dp), ("gym", _dp)]
+                ("trq0", C.c_double), ("seed", C.c_ulonglong), ("gy", _dp), ("gym", _dp),
+                ("et", _dp), ("etm", _dp)]
 
 
 class RunState(C.Structure):
@@ -493,7 +553,22 @@ class Run:
         if not one and not three and grid.get("gx") is not None:
             # 2-D step with gravity: the four fields (ix*jx, Fortran order)
             for k in ("gx", "gxm", "gy", "gym"):
+                if grid.get(k) is None:  # NULL: the library rejects the set-up
+                    continue
                 a = np.asfortranarray(grid[k], dtype=np.float64)
+                if a.shape != (nx, ny):
+                    raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {(nx, ny)}")
+                self._keep.append(a)
+                setattr(d, k, a.ctypes.data_as(_dp))
+        if not one and not three and grid.get("et") is not None:
+            # resistive 2-D step: et at the cells, etm at the corners (a
+            # missing etm stays NULL and the library rejects the set-up)
+            for k in ("et", "etm"):
+                if grid.get(k) is None:
+                    continue
+                a = np.asfortranarray(grid[k], dtype=np.float64)
+                if a.shape != (nx, ny):
+                    raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {(nx, ny)}")
                 self._keep.append(a)
                 setattr(d, k, a.ctypes.data_as(_dp))
         if bgv:
@@ -631,9 +706,17 @@ def _desc_for(solver: int, grid: dict, gm: float, qav: float, margin: int, exact
         a = np.ascontiguousarray(grid[k], dtype=np.float64)
         keep.append(a)
         return a.ctypes.data_as(_dp)
-    return _Desc(solver, np.asarray(grid["dx"]).size, np.asarray(grid["dy"]).size, 1, margin,
-                 gm, qav, arr("dx"), arr("dxm"), arr("dy"), arr("dym"), None, None,
-                 1 if exact else 0, tile, C.c_void_p(stream) if stream else None, None, None)
+    d = _Desc(solver, np.asarray(grid["dx"]).size, np.asarray(grid["dy"]).size, 1, margin,
+              gm, qav, arr("dx"), arr("dxm"), arr("dy"), arr("dym"), None, None,
+              1 if exact else 0, tile, C.c_void_p(stream) if stream else None, None, None)
+    # source-term fields are passed on so that a solver without them (the
+    # batch) refuses the set-up instead of running the plain step
+    for k in ("gx", "gxm", "gy", "gym", "et", "etm"):
+        if grid.get(k) is not None and (k[0] != "g" or grid.get("gravity")):
+            a = np.asfortranarray(grid[k], dtype=np.float64)
+            keep.append(a)
+            setattr(d, k, a.ctypes.data_as(_dp))
+    return d
 
 
 class Batch:

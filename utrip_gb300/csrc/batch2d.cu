@@ -375,6 +375,8 @@ extern "C" int cans_batch_create(cans_batch **out, int ngrids,
     if (d.solver != solver || d.margin != descs[0].margin || d.exact != descs[0].exact ||
         d.ix < wmin || d.jx < wmin || d.kx != 1 || !d.dx || !d.dxm || !d.dy || !d.dym)
       return CANS_ERR_ARG;
+    // the batch runs the plain mlw_m / mlw_m3 step: no source-term variant
+    if (d.gx || d.et || d.etm) return CANS_ERR_ARG;
   }
   auto *b = new cans_batch();
   b->ngrids = ngrids;

@@ -87,6 +87,9 @@ struct Ctl {
   int cur;
   long long nexec;  // steps executed since the run started
   unsigned long long nfloor;  // chkdav events since the run started
+  // resistive runs: the smallest diffusion limit of the time step over the
+  // cells (cfl_m_e.f:61), a constant of the run; 0 = none
+  unsigned long long dtdif_bits;
 };
 
 // Positive doubles order like their unsigned bit patterns.
@@ -112,7 +115,11 @@ __device__ __forceinline__ double warp_min(double v) {
 __device__ __forceinline__ void start_iteration(Ctl *ctl) {
   ctl->ns += 1;
   const unsigned long long bits = atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
-  const double dt = __longlong_as_double((long long)bits);
+  double dt = __longlong_as_double((long long)bits);
+  if (ctl->dtdif_bits) {  // min over cells of min(dtwav, dtdif)
+    const double dd = __longlong_as_double((long long)ctl->dtdif_bits);
+    if (dd < dt) dt = dd;
+  }
   ctl->dt = dt;
   ctl->cfl_bits = 0x7ff0000000000000ull;
   if (dt < ctl->dtmin) {

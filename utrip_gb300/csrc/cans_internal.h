@@ -59,6 +59,19 @@ cudaError_t launch_mlw2d_g(int solver, bool exact, int tile, const double *A,
                            const Axis &ay, const Phys &ph, const double *grav,
                            double dt, Ctl *ctl, Box3 box, cudaStream_t s);
 int mlw2d_g_tile_count();
+// Resistive 2-D mLW steps (mlw2d_e.cu): eta = et, etm (ix*jx each), res the
+// eta*J scratch of mlw2d_e_scratch_doubles doubles, grav optional.
+size_t mlw2d_e_scratch_doubles(int solver, int ix, int jx);
+cudaError_t launch_mlw2d_e(int solver, bool exact, const double *A, double *B, int ix,
+                           int jx, const Axis &ax, const Axis &ay, const Phys &ph,
+                           const double *grav, const double *eta, double *res,
+                           double dt, Ctl *ctl, Box3 box, cudaStream_t s);
+// cfl_m_e / cfl_m3_e over all cells into out_bits; wave = 0 reduces the
+// diffusion limit alone.
+cudaError_t launch_cfl2d_e(int solver, bool exact, const double *S, int ix, int jx,
+                           const Axis &ax, const Axis &ay, const Phys &ph,
+                           const double *et, double safety, int wave,
+                           unsigned long long *out_bits, cudaStream_t s);
 cudaError_t launch_cfl2d_full(int solver, bool exact, const double *S, int ix,
                               int jx, const Axis &ax, const Axis &ay,
                               const Phys &ph, double safety,

@@ -189,6 +189,29 @@ struct Scratch {
       CK(cudaMemcpyAsync(grav + k * n, g[k], sizeof(double) * n, cudaMemcpyHostToDevice, s));
     return CANS_OK;
   }
+  // resistivity (et, then etm) of the resistive 2-D steps, and their eta*J
+  // fields (nres doubles)
+  double *eta = nullptr, *res = nullptr;
+  size_t eta_cap = 0, res_cap = 0;
+  int upload_eta(const double *const *e, int k, size_t n, size_t nres, cudaStream_t s) {
+    if (eta_cap < 2 * n) {
+      if (eta) cudaFree(eta);
+      eta = nullptr;
+      eta_cap = 0;
+      CK(cudaMalloc(&eta, sizeof(double) * 2 * n));
+      eta_cap = 2 * n;
+    }
+    if (res_cap < nres) {
+      if (res) cudaFree(res);
+      res = nullptr;
+      res_cap = 0;
+      CK(cudaMalloc(&res, sizeof(double) * nres));
+      res_cap = nres;
+    }
+    for (int q = 0; q < k; q++)
+      CK(cudaMemcpyAsync(eta + q * n, e[q], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    return CANS_OK;
+  }
 };
 Scratch g_scratch;
 
@@ -233,15 +256,17 @@ double bits_to_double(unsigned long long b) {
 
 // ---- generic 2-D step (drop-in) -------------------------------------------
 // One 2-D step on host arrays or on their registered mirrors; with grav (gx,
-// gxm, gy, gym host arrays of ix*jx) the step with gravity.
+// gxm, gy, gym host arrays of ix*jx) the step with gravity, with eta (et,
+// etm) the resistive step.
 int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
            double gm, const double *dx, const double *dxm, int ix,
            const double *dy, const double *dym, int jx,
-           const double *const *grav = nullptr) {
+           const double *const *grav = nullptr, const double *const *eta = nullptr) {
   if (ix < 3 || jx < 3) return CANS_ERR_ARG;
   if (grav)
     for (int k = 0; k < 4; k++)
       if (!grav[k]) return CANS_ERR_ARG;
+  if (eta && (!eta[0] || !eta[1])) return CANS_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
   int rc = lib_stream(&s);
@@ -250,7 +275,14 @@ int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
   const size_t n = (size_t)ix * jx;
   Box3 box{};
   if (grav && (rc = g_scratch.upload_grav(grav, n, s))) return rc;
+  if (eta && (rc = g_scratch.upload_eta(eta, 2, n, mlw2d_e_scratch_doubles(solver, ix, jx),
+                                        s)))
+    return rc;
   auto step = [&](const double *A, double *B, const Axis &ax, const Axis &ay) {
+    if (eta)
+      return launch_mlw2d_e(solver, exact_mode(), A, B, ix, jx, ax, ay, ph,
+                            grav ? g_scratch.grav : nullptr, g_scratch.eta, g_scratch.res,
+                            dt, nullptr, box, s);
     return grav ? launch_mlw2d_g(solver, exact_mode(), 0, A, B, ix, jx, ax, ay, ph,
                                  g_scratch.grav, dt, nullptr, box, s)
                 : launch_mlw2d(solver, exact_mode(), 0, A, B, ix, jx, ax, ay, ph, dt,
@@ -278,9 +310,10 @@ int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
   return CANS_OK;
 }
 
+// cfl_m3 / cfl_m; with et (host, ix*jx) cfl_m3_e / cfl_m_e.
 int cfl2d(int solver, double *dt, double safety, double dtmin, int *merr,
           double gm, const double *const *arrs, int nvar, const double *dx,
-          int ix, const double *dy, int jx) {
+          int ix, const double *dy, int jx, const double *et = nullptr) {
   if (ix < 1 || jx < 1) return CANS_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
@@ -322,8 +355,14 @@ int cfl2d(int solver, double *dt, double safety, double dtmin, int *merr,
     return b;
   }();
   CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, s));
-  CK(launch_cfl2d_full(solver, exact_mode(), base, ix, jx, ax, ay, ph, safety,
-                       bits, s));
+  if (et) {
+    if ((rc = g_scratch.upload_eta(&et, 1, n, 0, s))) return rc;
+    CK(launch_cfl2d_e(solver, exact_mode(), base, ix, jx, ax, ay, ph, g_scratch.eta, safety,
+                      1, bits, s));
+  } else {
+    CK(launch_cfl2d_full(solver, exact_mode(), base, ix, jx, ax, ay, ph, safety,
+                         bits, s));
+  }
   unsigned long long out = 0;
   CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -439,6 +478,96 @@ extern "C" int cans_mlw_m_g_2d(double *ro, double *pr, double *vx, double *vy,
   double *arrs[7] = {ro, pr, vx, vy, bx, by, az};
   const double *grav[4] = {gx, gxm, gy, gym};
   return step2d(0, arrs, 7, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, grav);
+}
+
+// mlw_m3_e (cans2d/hdmlw/mlw_m3_e.f:2): mlw_m3 with resistivity
+extern "C" int cans_mlw_m3_e_2d(double *ro, double *pr, double *vx, double *vy,
+                                double *vz, double *bx, double *by, double *bz,
+                                double *az, const double *dt, const double *qav,
+                                const double *gm, const double *et,
+                                const double *etm, const double *dx,
+                                const double *dxm, const int *ix,
+                                const double *dy, const double *dym,
+                                const int *jx) {
+  double *arrs[9] = {ro, pr, vx, vy, vz, bx, by, bz, az};
+  const double *eta[2] = {et, etm};
+  return step2d(1, arrs, 9, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, nullptr, eta);
+}
+
+// mlw_m_e (cans2d/hdmlw/mlw_m_e.f:2): mlw_m with resistivity
+extern "C" int cans_mlw_m_e_2d(double *ro, double *pr, double *vx, double *vy,
+                               double *bx, double *by, double *az,
+                               const double *dt, const double *qav,
+                               const double *gm, const double *et,
+                               const double *etm, const double *dx,
+                               const double *dxm, const int *ix,
+                               const double *dy, const double *dym,
+                               const int *jx) {
+  double *arrs[7] = {ro, pr, vx, vy, bx, by, az};
+  const double *eta[2] = {et, etm};
+  return step2d(0, arrs, 7, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, nullptr, eta);
+}
+
+// mlw_m3_ge (cans2d/hdmlw/mlw_m3_ge.f:2): mlw_m3 with gravity and resistivity
+extern "C" int cans_mlw_m3_ge_2d(double *ro, double *pr, double *vx, double *vy,
+                                 double *vz, double *bx, double *by, double *bz,
+                                 double *az, const double *dt, const double *qav,
+                                 const double *gm, const double *gx,
+                                 const double *gxm, const double *gy,
+                                 const double *gym, const double *et,
+                                 const double *etm, const double *dx,
+                                 const double *dxm, const int *ix,
+                                 const double *dy, const double *dym,
+                                 const int *jx) {
+  double *arrs[9] = {ro, pr, vx, vy, vz, bx, by, bz, az};
+  const double *grav[4] = {gx, gxm, gy, gym};
+  const double *eta[2] = {et, etm};
+  return step2d(1, arrs, 9, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, grav, eta);
+}
+
+// mlw_m_ge (cans2d/hdmlw/mlw_m_ge.f:2): mlw_m with gravity and resistivity
+extern "C" int cans_mlw_m_ge_2d(double *ro, double *pr, double *vx, double *vy,
+                                double *bx, double *by, double *az,
+                                const double *dt, const double *qav,
+                                const double *gm, const double *gx,
+                                const double *gxm, const double *gy,
+                                const double *gym, const double *et,
+                                const double *etm, const double *dx,
+                                const double *dxm, const int *ix,
+                                const double *dy, const double *dym,
+                                const int *jx) {
+  double *arrs[7] = {ro, pr, vx, vy, bx, by, az};
+  const double *grav[4] = {gx, gxm, gy, gym};
+  const double *eta[2] = {et, etm};
+  return step2d(0, arrs, 7, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, grav, eta);
+}
+
+// cfl_m3_e (cans2d/common/cfl_m3_e.f:2)
+extern "C" int cans_cfl_m3_e_2d(double *dt, const double *safety,
+                                const double *dtmin, int *merr,
+                                const double *gm, const double *ro,
+                                const double *pr, const double *vx,
+                                const double *vy, const double *vz,
+                                const double *bx, const double *by,
+                                const double *bz, const double *et,
+                                const double *dx, const int *ix,
+                                const double *dy, const int *jx) {
+  if (!et) return CANS_ERR_ARG;
+  const double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  return cfl2d(1, dt, *safety, *dtmin, merr, *gm, arrs, 8, dx, *ix, dy, *jx, et);
+}
+
+// cfl_m_e (cans2d/common/cfl_m_e.f:2)
+extern "C" int cans_cfl_m_e_2d(double *dt, const double *safety,
+                               const double *dtmin, int *merr, const double *gm,
+                               const double *ro, const double *pr,
+                               const double *vx, const double *vy,
+                               const double *bx, const double *by,
+                               const double *et, const double *dx,
+                               const int *ix, const double *dy, const int *jx) {
+  if (!et) return CANS_ERR_ARG;
+  const double *arrs[6] = {ro, pr, vx, vy, bx, by};
+  return cfl2d(0, dt, *safety, *dtmin, merr, *gm, arrs, 6, dx, *ix, dy, *jx, et);
 }
 
 extern "C" int cans_mlw_m_2d(double *ro, double *pr, double *vx, double *vy,
@@ -1173,6 +1302,8 @@ struct cans_run {
   Loop1D loop1d{};             // 1-D loop options (device pointers into bx1)
   double *roe = nullptr;       // Roe / HLLD: stage scratch
   double *grav = nullptr;      // 2-D mLW with gravity: gx gxm gy gym (n each)
+  double *eta = nullptr;       // 2-D mLW with resistivity: et, etm (n each)
+  double *res = nullptr;       //   and the eta*J fields of each step
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
@@ -1209,7 +1340,7 @@ int layout2d(const cans_run *h) {
 }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
-  if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
+  if (is_roe(h) || is_hlld(h) || h->ndim == 1 || h->eta) return 1;
   if (h->grav) return mlw2d_g_tile_count();
   return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
 }
@@ -1250,6 +1381,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (h->ndim == 3)
     return launch_mlw3d(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
+  if (h->eta)
+    return launch_mlw2d_e(h->d.solver, h->d.exact != 0, A, B, h->d.ix, h->d.jx, h->ax.a,
+                          h->ay.a, h->ph, h->grav, h->eta, h->res, dt, ctl, box, h->s);
   if (h->grav)
     return launch_mlw2d_g(h->d.solver, h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx,
                           h->ax.a, h->ay.a, h->ph, h->grav, dt, ctl, box, h->s);
@@ -1278,6 +1412,9 @@ cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
   if (h->ndim == 3)
     return launch_cfl3d_full(h->d.exact != 0, S, h->d.ix, h->d.jx, h->d.kx,
                              h->ax.a, h->ay.a, h->az.a, h->ph, safety, bits, h->s);
+  if (h->eta)
+    return launch_cfl2d_e(h->d.solver, h->d.exact != 0, S, h->d.ix, h->d.jx, h->ax.a,
+                          h->ay.a, h->ph, h->eta, safety, 1, bits, h->s);
   return launch_cfl2d_full(layout2d(h), h->d.exact != 0, S, h->d.ix, h->d.jx,
                            h->ax.a, h->ay.a, h->ph, safety, bits, h->s);
 }
@@ -1366,8 +1503,11 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   const int wmin = 2 * (d->margin + 1) + 1;
   const bool bgv = d->solver == CANS_SOLVER_MLW_M_BG_1D;
   // 2-D mLW with gx set: the steps with gravity (mlw_m_g / mlw_m3_g)
-  const bool grav2d = (d->solver == CANS_SOLVER_MLW_M_2D ||
-                       d->solver == CANS_SOLVER_MLW_M3_2D) && d->gx != nullptr;
+  const bool mlw2d = d->solver == CANS_SOLVER_MLW_M_2D || d->solver == CANS_SOLVER_MLW_M3_2D;
+  const bool grav2d = mlw2d && d->gx != nullptr;
+  // 2-D mLW with et set: the resistive steps (mlw_m_e / mlw_m3_e)
+  const bool eta2d = mlw2d && d->et != nullptr;
+  if ((d->et || d->etm) && !(eta2d && d->etm)) return CANS_ERR_ARG;
   const double *prof[10] = {d->gx, d->gxm, d->sc, d->scm, d->dsc,
                             d->dscm, d->rr, d->rrm, d->drr, d->drrm};
   if (ndim == 1) {
@@ -1463,6 +1603,18 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     if (e != cudaSuccess) return bail(fail_cuda(e, "gravity fields"));
     h->tile = d->tile >= 0 && d->tile < tile_count(h) ? d->tile : 0;
   }
+  if (eta2d) {  // mlw_m_e / mlw_m3_e: et, etm and the eta*J scratch
+    e = cudaMalloc(&h->eta, sizeof(double) * 2 * h->n);
+    if (e == cudaSuccess)
+      e = cudaMalloc(&h->res, sizeof(double) * mlw2d_e_scratch_doubles(d->solver, d->ix, d->jx));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->eta, d->et, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->eta + h->n, d->etm, sizeof(double) * h->n,
+                          cudaMemcpyHostToDevice, h->s);
+    if (e != cudaSuccess) return bail(fail_cuda(e, "resistivity fields"));
+    h->tile = 0;
+  }
   for (int a = 0; a < 3; a++) h->mfdim[a] = mfdim[a];
   h->mu = d->mu > 0.0 ? d->mu : 1.0;
   std::memset(&h->host_ctl, 0, sizeof(Ctl));
@@ -1487,6 +1639,8 @@ extern "C" int cans_run_destroy(cans_run *h) {
   if (h->bx1) cudaFree(h->bx1);
   if (h->roe) cudaFree(h->roe);
   if (h->grav) cudaFree(h->grav);
+  if (h->eta) cudaFree(h->eta);
+  if (h->res) cudaFree(h->res);
   h->ax.release();
   h->ay.release();
   h->az.release();
@@ -1566,9 +1720,14 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
   c.nonfinite = 0;
   c.nfloor = 0;
   c.cfl_bits = r4_1e20_bits();
+  c.dtdif_bits = h->eta ? 0x7ff0000000000000ull : 0ull;
   h->host_ctl = c;
   CK(cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice,
                      h->s));
+  if (h->eta)  // the diffusion limit depends on et, the mesh and safety only
+    CK(launch_cfl2d_e(h->d.solver, h->d.exact != 0, h->buf[c.cur], h->d.ix, h->d.jx,
+                      h->ax.a, h->ay.a, h->ph, h->eta, safety, 0, &h->ctl->dtdif_bits,
+                      h->s));
   if (h->ndim == 1) {  // first CFL and loop start inside the cluster kernel
     CK(launch_1d(h, 0, 0, 0.0, 1));
     return CANS_OK;
@@ -1804,7 +1963,10 @@ struct AdjWork {
   }
 };
 
-bool adj_supported(const cans_run *h) { return h->d.solver == CANS_SOLVER_MLW_M3_2D; }
+// the adjoint is that of the plain mlw_m3 step: no gravity, no resistivity
+bool adj_supported(const cans_run *h) {
+  return h->d.solver == CANS_SOLVER_MLW_M3_2D && !h->grav && !h->eta;
+}
 
 int adj_setup(cans_run *h, AdjWork &W, int nsnap) {
   W.n9 = h->n * (size_t)h->nvar;

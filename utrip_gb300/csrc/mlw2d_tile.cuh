@@ -23,6 +23,14 @@
 // energy and the x, y momenta through mlwsrch and mlwsrcf.  grav holds gx,
 // gxm, gy, gym (ix*jx each; gxm, gym at the corner (i+1/2, j+1/2)).
 //
+// With R the tile is the resistive step mlw_m3_e / mlw_m_e (and with G as
+// well mlw_m3_ge / mlw_m_ge; cans2d/hdmlw/mlw_m3_e.f:124-132, 236-244,
+// mlw_m_e.f:125-129, 216-220): res holds eta J at the cells and at the
+// corners, computed beforehand by the kernels of mlw2d_e.cu, and each is
+// added to E = -v x B where the reference adds et*c and etm*ch.  res is
+// [x, y, z at the cells, x, y, z at the corners] (ix*jx each) for mlw_m3 and
+// [z at the cells, z at the corners] for mlw_m.
+//
 // In the exact policy every operation is the reference's, in its order, so
 // the result equals a -ffp-contract=off CPU build of the Fortran bit for bit.
 // Terms whose flux is identically zero (fx of bx, fy of by) are skipped: the
@@ -105,13 +113,14 @@ constexpr int NOFLUX = -1;
 // single-grid kernel (one tile per block) and by the batched kernel (tiles
 // of many grids pulled from a work queue by persistent blocks).  If cfl_out
 // is non-null the CFL of the written cells inside `box` is reduced into it.
-template <bool E, bool M3, int TX, int TY, int RPT, bool G = false>
+template <bool E, bool M3, int TX, int TY, int RPT, bool G = false, bool R = false>
 __device__ __forceinline__ void tile_step(
     const double *__restrict__ A, double *__restrict__ B, int ix, int jx,
     const Axis &ax, const Axis &ay, const Phys &ph, double dtv, double safety,
     unsigned long long *cfl_out, const Box3 &box, int tile_x, int tile_y,
     int ntiles_x, int ntiles_y, double *smem,
-    const double *__restrict__ grav = nullptr) {
+    const double *__restrict__ grav = nullptr,
+    const double *__restrict__ res = nullptr) {
   using T = Tile<TX, TY, M3, RPT, G>;
   using C = CellSlots<M3>;
   using K = CornerSlots<M3>;
@@ -180,9 +189,14 @@ __device__ __forceinline__ void tile_step(
       SC(C::VX, c) = vx.v; SC(C::VY, c) = vy.v;
       if constexpr (M3) {
         const FT rz = ro * vz;
-        const FT ex = -vy * bz + vz * by;              // mlw_m3.f:119-121
-        const FT ey = -vz * bx + vx * bz;
-        const FT ez = -vx * by + vy * bx;
+        FT ex = -vy * bz + vz * by;                    // mlw_m3.f:119-121
+        FT ey = -vz * bx + vx * bz;
+        FT ez = -vx * by + vy * bx;
+        if constexpr (R) {                             // mlw_m3_e.f:130-132
+          ex = ex + FT(res[g]);
+          ey = ey + FT(res[n + g]);
+          ez = ez + FT(res[2 * n + g]);
+        }
         SC(C::RZ, c) = rz.v; SC(C::BZ, c) = bz.v;
         SC(C::EX, c) = ex.v; SC(C::EY, c) = ey.v; SC(C::EZ, c) = ez.v;
         // energy flux (:141-143)
@@ -196,7 +210,8 @@ __device__ __forceinline__ void tile_step(
         SC(C::FXRZ, c) = (ro * vz * vx - pi4i * bz * bx).v;
         SC(C::FYRZ, c) = (ro * vz * vy - pi4i * bz * by).v;
       } else {
-        const FT ez = -vx * by + vy * bx;              // mlw_m.f:70
+        FT ez = -vx * by + vy * bx;                    // mlw_m.f:70
+        if constexpr (R) ez = ez + FT(res[g]);         // mlw_m_e.f:129
         SC(C::EZ, c) = ez.v;
         SC(C::FXE, c) = (ep * vx - by * ez * pi4i).v;  // mlw_m.f:85-86
         SC(C::FYE, c) = (ep * vy + bx * ez * pi4i).v;
@@ -317,10 +332,16 @@ __device__ __forceinline__ void tile_step(
       }
       SK(K::XRO, c) = (roh * vxh).v;
       SK(K::YRO, c) = (roh * vyh).v;
+      [[maybe_unused]] const size_t gk = (size_t)gi + (size_t)gj * ix;
       if constexpr (M3) {
-        const FT exh = -vyh * bzh + vzh * byh;
-        const FT eyh = -vzh * bxh + vxh * bzh;
-        const FT ezh = -vxh * byh + vyh * bxh;
+        FT exh = -vyh * bzh + vzh * byh;
+        FT eyh = -vzh * bxh + vxh * bzh;
+        FT ezh = -vxh * byh + vyh * bxh;
+        if constexpr (R) {                             // mlw_m3_e.f:242-244
+          exh = exh + FT(res[3 * n + gk]);
+          eyh = eyh + FT(res[4 * n + gk]);
+          ezh = ezh + FT(res[5 * n + gk]);
+        }
         SK(K::EX, c) = exh.v; SK(K::EY, c) = eyh.v; SK(K::EZ, c) = ezh.v;
         SK(K::XEE, c) = (ep * vxh + (bzh * eyh - byh * ezh) * pi4i).v;
         SK(K::YEE, c) = (ep * vyh + (bxh * ezh - bzh * exh) * pi4i).v;
@@ -331,7 +352,8 @@ __device__ __forceinline__ void tile_step(
         SK(K::XRZ, c) = (roh * vzh * vxh - pi4i * bzh * bxh).v;
         SK(K::YRZ, c) = (roh * vzh * vyh - pi4i * bzh * byh).v;
       } else {
-        const FT ezh = -vxh * byh + vyh * bxh;
+        FT ezh = -vxh * byh + vyh * bxh;
+        if constexpr (R) ezh = ezh + FT(res[n + gk]);  // mlw_m_e.f:220
         SK(K::EZ, c) = ezh.v;
         SK(K::XEE, c) = (ep * vxh - byh * ezh * pi4i).v;
         SK(K::YEE, c) = (ep * vyh + bxh * ezh * pi4i).v;

@@ -72,6 +72,13 @@ def _cfl(setup, state, safety):
     if setup["solver"] in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
         return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
                              setup["dy"], setup["dz"])
+    if setup.get("et") is not None:  # cfl_m3_e / cfl_m_e
+        et = np.asfortranarray(setup["et"])
+        if setup["solver"] == "mlw_m3":
+            return capi.cfl_m3_e(safety, setup["dtmin"], setup["gm"], *state[:8], et,
+                                 setup["dx"], setup["dy"])
+        return capi.cfl_m_e(safety, setup["dtmin"], setup["gm"], *state[:6], et, setup["dx"],
+                            setup["dy"])
     if setup["solver"] in ("mlw_m3", "roe_m3"):
         return capi.cfl_m3(safety, setup["dtmin"], setup["gm"], *state[:8], setup["dx"],
                            setup["dy"])
@@ -102,6 +109,14 @@ def _step(setup, state, dt):
         capi.hlld_engine_3d(*state, setup["gm"], setup["mu"], dt, setup["dx"], setup["dxm"],
                             setup["dy"], setup["dym"], setup["dz"], setup["dzm"],
                             setup["mfdim"])
+        return
+    if setup.get("et") is not None:  # mlw_m3_e / mlw_m_e, with gravity _ge
+        e = [np.asfortranarray(setup[k]) for k in ("et", "etm")]
+        g = ([np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym")]
+             if setup.get("gravity") else [None] * 4)
+        (capi.mlw_m3_e if setup["solver"] == "mlw_m3" else capi.mlw_m_e)(
+            *state, dt, setup["qav"], setup["gm"], *e, setup["dx"], setup["dxm"], setup["dy"],
+            setup["dym"], *g)
         return
     if setup.get("gravity"):
         g = [setup[k] for k in ("gx", "gxm", "gy", "gym")]

@@ -756,3 +756,82 @@ def random_gravity(s: dict, seed: int = 0, scale: float = 0.3) -> dict:
         out[k] = np.asfortranarray(scale * rng.standard_normal(shape))
     out["gravity"] = True
     return out
+
+
+def random_resistivity(s: dict, seed: int = 0, scale: float = 0.02) -> dict:
+    """Seeded non-negative resistivity on a 2-D set-up (et at the cells, etm
+    at the corners, every resistive term of mlw_m_e / mlw_m3_e non-zero):
+    returns a copy with et and etm."""
+    rng = np.random.default_rng(seed)
+    shape = s["state"][0].shape
+    out = dict(s)
+    for k in ("et", "etm"):
+        out[k] = np.asfortranarray(scale * (0.5 + rng.random(shape)))
+    return out
+
+
+def magnetic_reconnection(n: int = 128):
+    """The magnetic-reconnection model of cans2d/md_recon/hdmlw (model.f,
+    bnd.f, main.f:161-176): x in [0, 5], y in [0, 20] on n x n cells with two
+    ghost layers, gamma 5/3, a Harris-type current sheet by =
+    sqrt(8 pi betai/gm) tanh(x/0.5) with betai = 10 in pressure balance, and
+    a localised resistivity etai (2 r^3 - 3 retai r^2)/retai^3 + etai inside
+    r < retai = 0.8 of the origin (et at the cells, etm at the corners; zero
+    elsewhere).  Boundaries: symmetric about x = 0 and y = 0 (vx, by odd at
+    x = 0; vy, bx odd at y = 0), the same rules at the outer faces with bx
+    odd at the outer x face.  cfl_m_e safety 0.4, qav 3, tend 23."""
+    margin = 2
+    ix = jx = n + 2 * margin
+    gm = 5.0 / 3.0
+    pi = math.acos(-1.0)
+    xmax, ymax = 5.0, 20.0
+
+    def axis(length, nn):
+        d0 = length / float(nn - margin * 2)
+        dm = np.full(nn, d0)
+        iz = margin + 1
+        x = np.empty(nn)
+        x[iz - 1] = dm[iz - 1] / 2.0
+        for i in range(iz + 1, nn + 1):
+            x[i - 1] = x[i - 2] + dm[i - 2]
+        for i in range(iz - 1, 0, -1):
+            x[i - 1] = x[i] - dm[i - 1]
+        return x, dm
+
+    x, dxm0 = axis(xmax, ix)
+    y, dym0 = axis(ymax, jx)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    etai, retai = 0.03, 0.8
+
+    def eta(rr):
+        # etai*(2*rr**3-3*retai*rr**2)/retai**3+etai (model.f), integer
+        # powers as repeated products
+        r3 = rr * rr * rr
+        v = etai * (2.0 * r3 - (3.0 * retai) * (rr * rr)) / (retai * retai * retai) + etai
+        return np.where(rr < retai, v, 0.0)
+
+    rr = np.sqrt(X * X + Y * Y)
+    et = eta(rr)
+    Xm = X + (dxm0 / 2.0)[:, None]
+    Ym = Y + (dym0 / 2.0)[None, :]
+    etm = eta(np.sqrt(Xm * Xm + Ym * Ym))
+    betai = 10.0
+    by = np.sqrt(betai * pi * 8 / gm) * np.tanh(X / 0.5)
+    pr = 1 / gm * (1 + betai) - by * by / pi / 8.0
+    f = {"ro": pr * gm, "pr": pr, "vx": np.zeros(X.shape), "vy": np.zeros(X.shape),
+         "bx": np.zeros(X.shape), "by": by}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, margin)
+    names = VARS["mlw_m"]
+    # bnd.f: per face, the rule of each variable (SPN = odd about the face)
+    odd = {0: ("vx", "by"), 1: ("vx", "bx"), 2: ("vy", "bx"), 3: ("vy", "bx")}
+    bc = []
+    for face in range(4):
+        for v, name in enumerate(names):
+            bc.append((v, face, BD_SPN if name in odd[face] else BD_SPP, 0.0))
+    s = _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+              tend=23.0, dtout=1.0, margin=margin, name=f"magnetic_reconnection_{n}")
+    s["et"] = np.asfortranarray(et)
+    s["etm"] = np.asfortranarray(etm)
+    return s
