@@ -53,7 +53,7 @@ def parse():
                    help="skip the secondary 3-D and 1-D workloads")
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
-                            "gravity2d", "spicule"],
+                            "gravity2d", "resistive2d", "spicule"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
@@ -64,9 +64,10 @@ def profile_case(case, n):
     or 5 batched iterations of 8 shear layers; prints one JSON line."""
     import torch
     from utrip_gb300 import capi, drivers, setups
-    if case in ("roe2d", "gravity2d"):
-        s = (setups.orszag_tang(n, solver="roe_m3") if case == "roe2d"
-             else setups.mhd_gravity_wave(n, solver="mlw_m3"))
+    if case in ("roe2d", "gravity2d", "resistive2d"):
+        s = {"roe2d": lambda: setups.orszag_tang(n, solver="roe_m3"),
+             "gravity2d": lambda: setups.mhd_gravity_wave(n, solver="mlw_m3"),
+             "resistive2d": lambda: setups.magnetic_reconnection(n)}[case]()
         run = drivers.make_run(s)
         run.push(s["state"])
         run.start(nstop=3, safety=s["safety"], dtmin=1e-10)
@@ -180,6 +181,11 @@ def extra_workloads(stream, exact=False):
     for solver, safety in (("roe_m_3d", None), ("hlld_3d", 0.2)):
         out[f"turbulence_256^3_{solver}"] = riemann_3d(stream, solver, safety, exact)
     out["orszag_tang_512^2_roe_m3"] = roe_2d(stream, exact)
+    out["mhd_gravity_wave_512^2_mlw_m3_g"] = loop_2d(
+        stream, exact, lambda m: setups.mhd_gravity_wave(m, solver="mlw_m3"), 512, 100, 256, 500,
+        "gravity-wave model")
+    out["reconnection_512^2_mlw_m_e"] = loop_2d(
+        stream, exact, setups.magnetic_reconnection, 512, 100, 256, 500, "reconnection model")
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
     out["spicule_1024_100000_steps_mlw_m_bg"] = spicule_workload(stream)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
@@ -225,10 +231,19 @@ def roe_2d(stream, exact, n=512, iters=50, cpu_n=256, cpu_steps=300):
     the headline, loop iterations timed with events (graph), the four step
     kernels profiled; the oracle on a bounded sample (cpu_n^2, all host
     threads) beside it."""
+    from utrip_gb300 import setups
+    return loop_2d(stream, exact, lambda m: setups.orszag_tang(m, solver="roe_m3"), n, iters,
+                   cpu_n, cpu_steps, "vortex")
+
+
+def loop_2d(stream, exact, make, n, iters, cpu_n, cpu_steps, what):
+    """A 2-D model loop on the device (graph-replayed iterations timed with
+    events, step kernels profiled) and the oracle on a bounded sample of the
+    same model (cpu_n^2, all host threads)."""
     import torch
     import oracle
     from utrip_gb300 import drivers, setups
-    s = setups.orszag_tang(n, solver="roe_m3")
+    s = make(n)
     run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
     run.push(s["state"])
     run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
@@ -243,7 +258,7 @@ def roe_2d(stream, exact, n=512, iters=50, cpu_n=256, cpu_steps=300):
     step_ms, _ = run.profile(10)
     st = run.query()
     run.close()
-    c = setups.orszag_tang(cpu_n, solver="roe_m3")
+    c = make(cpu_n)
     cs = setups.copy_state(c)
     t0 = time.perf_counter()
     oracle.run_2d(c, cs, cpu_steps)
@@ -253,7 +268,7 @@ def roe_2d(stream, exact, n=512, iters=50, cpu_n=256, cpu_steps=300):
             "merr": int(st.merr), "policy": "exact" if exact else "fast",
             "cpu_oracle": {"zone_updates_per_s": cpu_n * cpu_n * cpu_steps / el,
                            "cores": oracle.get_threads(), "kind": "port",
-                           "sample": f"{cpu_steps} loop iterations of the {cpu_n}^2 vortex "
+                           "sample": f"{cpu_steps} loop iterations of the {cpu_n}^2 {what} "
                                      f"in {el:.2f} s"}}
 
 

@@ -47,6 +47,17 @@ __device__ __forceinline__ F<E> curl_z(BX bx, BY by, F<E> hx, F<E> hy) {
   return t1 + t2 + t3 - t4 - t5 - t6;
 }
 
+// The same current with the reciprocal spacings hxi = 1/hx, hyi = 1/hy and
+// the stencil regrouped (fast policy: no division).
+template <class BX, class BY>
+__device__ __forceinline__ double curl_z_fast(BX bx, BY by, double hxi, double hyi) {
+  const double sx = fma(0.25, by(1, 0) - by(-1, 0),
+                        0.125 * ((by(1, 1) - by(-1, 1)) + (by(1, -1) - by(-1, -1))));
+  const double sy = fma(0.25, bx(0, 1) - bx(0, -1),
+                        0.125 * ((bx(1, 1) - bx(1, -1)) + (bx(-1, 1) - bx(-1, -1))));
+  return fma(hxi, sx, -hyi * sy);
+}
+
 template <bool M3> struct NRes { static constexpr int value = M3 ? 3 : 1; };
 
 // et*J at the cells (mlw_m_e.f:125-129, mlw_m3_e.f:124-132).
@@ -62,23 +73,37 @@ __global__ void __launch_bounds__(256)
     A = ctl->buf[ctl->cur];
   }
   const size_t n = (size_t)ix * jx;
-  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n;
-       g += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(g % ix), j = (int)(g / ix);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= ix || j >= jx) return;
+  const size_t g = (size_t)i + (size_t)j * ix;
+  {
     double rx = 0.0, ry = 0.0, rz = 0.0;
     if (i >= 1 && i <= ix - 2 && j >= 1 && j <= jx - 2) {
-      const FT hx(ax.d[i]), hy(ay.d[j]);
-      const FT e(et[g]);
-      auto bx = [&](int di, int dj) { return FT(A[P::BX * n + g + di + (long long)dj * ix]); };
-      auto by = [&](int di, int dj) { return FT(A[P::BY * n + g + di + (long long)dj * ix]); };
-      rz = (e * curl_z<E>(bx, by, hx, hy)).v;
-      if constexpr (M3) {
-        const double *bz = A + P::BZ * n;
-        // bbtocx.f:31, bbtocy.f:31
-        const FT cx = (FT(bz[g + ix]) - FT(bz[g - ix])) / hy * 0.5;
-        const FT cy = -((FT(bz[g + 1]) - FT(bz[g - 1])) / hx * 0.5);
-        rx = (e * cx).v;
-        ry = (e * cy).v;
+      const double *bxa = A + P::BX * n + g, *bya = A + P::BY * n + g;
+      auto bx = [&](int di, int dj) { return bxa[di + (long long)dj * ix]; };
+      auto by = [&](int di, int dj) { return bya[di + (long long)dj * ix]; };
+      const double *bz = A + (M3 ? P::BZ : 0) * n;  // read by mlw_m3_e only
+      if constexpr (E) {
+        const FT hx(ax.d[i]), hy(ay.d[j]);
+        const FT e(et[g]);
+        auto fbx = [&](int di, int dj) { return FT(bx(di, dj)); };
+        auto fby = [&](int di, int dj) { return FT(by(di, dj)); };
+        rz = (e * curl_z<E>(fbx, fby, hx, hy)).v;
+        if constexpr (M3) {
+          // bbtocx.f:31, bbtocy.f:31
+          const FT cx = (FT(bz[g + ix]) - FT(bz[g - ix])) / hy * 0.5;
+          const FT cy = -((FT(bz[g + 1]) - FT(bz[g - 1])) / hx * 0.5);
+          rx = (e * cx).v;
+          ry = (e * cy).v;
+        }
+      } else {
+        const double hxi = ax.di[i], hyi = ay.di[j], e = et[g];
+        rz = e * curl_z_fast(bx, by, hxi, hyi);
+        if constexpr (M3) {
+          rx = e * (0.5 * hyi) * (bz[g + ix] - bz[g - ix]);
+          ry = -e * (0.5 * hxi) * (bz[g + 1] - bz[g - 1]);
+        }
       }
     }
     if constexpr (M3) {
@@ -185,17 +210,28 @@ __global__ void __launch_bounds__(KT *KT)
   double rx = 0.0, ry = 0.0, rz = 0.0;
   if (ki >= 1 && kj >= 1) {
     const int h = (lx + 1) + (ly + 1) * KH;
-    const FT hxm(ax.dm[ki]), hym(ay.dm[kj]);
-    const FT e(etm[gk]);
-    auto bxh = [&](int di, int dj) { return FT(sh[h + di + dj * KH]); };
-    auto byh = [&](int di, int dj) { return FT(sh[KH * KH + h + di + dj * KH]); };
-    rz = (e * curl_z<E>(bxh, byh, hxm, hym)).v;
-    if constexpr (M3) {
-      const double *bzh = sh + 2 * KH * KH;
-      const FT cx = (FT(bzh[h + KH]) - FT(bzh[h - KH])) / hym * 0.5;
-      const FT cy = -((FT(bzh[h + 1]) - FT(bzh[h - 1])) / hxm * 0.5);
-      rx = (e * cx).v;
-      ry = (e * cy).v;
+    auto bxh = [&](int di, int dj) { return sh[h + di + dj * KH]; };
+    auto byh = [&](int di, int dj) { return sh[KH * KH + h + di + dj * KH]; };
+    const double *bzh = sh + 2 * KH * KH;
+    if constexpr (E) {
+      const FT hxm(ax.dm[ki]), hym(ay.dm[kj]);
+      const FT e(etm[gk]);
+      auto fbx = [&](int di, int dj) { return FT(bxh(di, dj)); };
+      auto fby = [&](int di, int dj) { return FT(byh(di, dj)); };
+      rz = (e * curl_z<E>(fbx, fby, hxm, hym)).v;
+      if constexpr (M3) {
+        const FT cx = (FT(bzh[h + KH]) - FT(bzh[h - KH])) / hym * 0.5;
+        const FT cy = -((FT(bzh[h + 1]) - FT(bzh[h - 1])) / hxm * 0.5);
+        rx = (e * cx).v;
+        ry = (e * cy).v;
+      }
+    } else {
+      const double hxi = ax.dim[ki], hyi = ay.dim[kj], e = etm[gk];
+      rz = e * curl_z_fast(bxh, byh, hxi, hyi);
+      if constexpr (M3) {
+        rx = e * (0.5 * hyi) * (bzh[h + KH] - bzh[h - KH]);
+        ry = -e * (0.5 * hxi) * (bzh[h + 1] - bzh[h - 1]);
+      }
     }
   }
   if constexpr (M3) {
@@ -246,9 +282,8 @@ cudaError_t launch_e(const double *A, double *B, int ix, int jx, const Axis &ax,
     attr_set = true;
   }
   const size_t n = (size_t)ix * jx;
-  int blocks = (int)((n + 255) / 256);
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  k_res_cells<E, M3><<<blocks, 256, 0, s>>>(A, ix, jx, ax, ay, eta, res, ctl);
+  dim3 gc((ix + 31) / 32, (jx + 7) / 8);
+  k_res_cells<E, M3><<<gc, dim3(32, 8), 0, s>>>(A, ix, jx, ax, ay, eta, res, ctl);
   count_launch();
   dim3 gk((ix - 1 + KT - 1) / KT, (jx - 1 + KT - 1) / KT);
   k_res_corners<E, M3><<<gk, KT * KT, 0, s>>>(A, ix, jx, ax, ay, eta + n, res, dt, ctl);
