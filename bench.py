@@ -184,6 +184,9 @@ def extra_workloads(stream, exact=False):
     out["mhd_gravity_wave_512^2_mlw_m3_g"] = loop_2d(
         stream, exact, lambda m: setups.mhd_gravity_wave(m, solver="mlw_m3"), 512, 100, 256, 500,
         "gravity-wave model")
+    out["emerging_flux_256x64x256_mlw_m_g"] = loop_3d(
+        stream, exact, setups.emerging_flux_3d, (256, 64, 256), 20, (64, 16, 64), 20,
+        "emerging-flux model")
     out["reconnection_512^2_mlw_m_e"] = loop_2d(
         stream, exact, setups.magnetic_reconnection, 512, 100, 256, 500, "reconnection model")
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
@@ -270,6 +273,43 @@ def loop_2d(stream, exact, make, n, iters, cpu_n, cpu_steps, what):
                            "cores": oracle.get_threads(), "kind": "port",
                            "sample": f"{cpu_steps} loop iterations of the {cpu_n}^2 {what} "
                                      f"in {el:.2f} s"}}
+
+
+def loop_3d(stream, exact, make, shape, iters, cpu_shape, cpu_steps, what):
+    """A 3-D model loop on the device (graph-replayed iterations timed with
+    events, step kernels profiled) and the oracle on a bounded sample of the
+    same model (all host threads)."""
+    import torch
+    import oracle
+    from utrip_gb300 import drivers, setups
+    s = make(*shape)
+    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    run.push(s["state"])
+    run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+    run.advance(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run.advance(iters)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    step_ms, _ = run.profile(5)
+    st = run.query()
+    run.close()
+    zones = int(np.prod(shape))
+    c = make(*cpu_shape)
+    cs = setups.copy_state(c)
+    t0 = time.perf_counter()
+    oracle.run_3d(c, cs, cpu_steps)
+    el = time.perf_counter() - t0
+    return {"zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+            "step_kernels_ms": step_ms / 5, "bound": "fp64", "steps_done": int(st.nexec),
+            "merr": int(st.merr), "policy": "exact" if exact else "fast",
+            "cpu_oracle": {"zone_updates_per_s": int(np.prod(cpu_shape)) * cpu_steps / el,
+                           "cores": oracle.get_threads(), "kind": "port",
+                           "sample": f"{cpu_steps} loop iterations of the "
+                                     f"{'x'.join(map(str, cpu_shape))} {what} in {el:.2f} s"}}
 
 
 def cpu_sample_3d(solver, safety, n=96, steps=2):

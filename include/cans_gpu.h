@@ -251,6 +251,17 @@ int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                   const double *dxm, const int *ix, const double *dy,
                   const double *dym, const int *jx, const double *dz,
                   const double *dzm, const int *kx);
+/* replaces subroutine mlw_m_g (cans3d/hdmlw/mlw_m_g.f:2-4): the 3-D step with
+ * gravity; gx, gy, gz at the cells, gxm, gym, gzm at the cell corners,
+ * ix*jx*kx each */
+int cans_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                    double *bx, double *by, double *bz, const double *dt,
+                    const double *qav, const double *gm, const double *gx,
+                    const double *gxm, const double *gy, const double *gym,
+                    const double *gz, const double *gzm, const double *dx,
+                    const double *dxm, const int *ix, const double *dy,
+                    const double *dym, const int *jx, const double *dz,
+                    const double *dzm, const int *kx);
 /* replaces subroutine cfl_m   (cans3d/common/cfl_m.f:2-3) */
 int cans_cfl_m_3d(double *dt, const double *safety, const double *dtmin,
                   int *merr, const double *gm, const double *ro,
@@ -396,6 +407,9 @@ typedef struct {
    * mlw_m3_ge): et(ix,jx) at the cells, etm(ix,jx) at the corners; the time
    * step then includes the diffusion limit of cfl_m_e / cfl_m3_e */
   const double *et, *etm;
+  /* 3-D mLW with gravity (mlw_m_g, cans3d/hdmlw/mlw_m_g.f): gx, gxm, gy, gym
+   * above and gz, gzm here, ix*jx*kx each (the *m fields at the corners) */
+  const double *gz, *gzm;
 } cans_run_desc;
 
 typedef struct {

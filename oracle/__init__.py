@@ -60,6 +60,8 @@ def load():
         lib.oracle_mlw_m_1d.argtypes = [_dp] * 7 + [d, d, d, _dp, _dp, i]
         lib.oracle_cfl_m_1d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 6 + [_dp, i]
         lib.oracle_mlw_m_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, _dp, i, _dp, _dp, i, _dp, _dp, i]
+        lib.oracle_mlw_m_g_3d.argtypes = ([_dp] * 8 + [d, d, d] + [_dp] * 6 +
+                                          [_dp, _dp, i, _dp, _dp, i, _dp, _dp, i])
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m3_2d.argtypes = [_dp] * 9 + [d, d, _dp, i, _dp, i]
@@ -414,6 +416,15 @@ def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, 
                            P(dx), P(dxm), ix, P(dy), P(dym), jx, P(dz), P(dzm), kx)
 
 
+def mlw_m_g_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, gx, gxm, gy, gym, gz, gzm,
+               dx, dxm, dy, dym, dz, dzm):
+    """cans3d/hdmlw/mlw_m_g.f:2"""
+    ix, jx, kx = ro.shape
+    load().oracle_mlw_m_g_3d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], dt, qav, gm,
+                             *[P(a) for a in (gx, gxm, gy, gym, gz, gzm)], P(dx), P(dxm), ix,
+                             P(dy), P(dym), jx, P(dz), P(dzm), kx)
+
+
 def cfl_m_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy, dz):
     ix, jx, kx = ro.shape
     dt, merr = C.c_double(), C.c_int()
@@ -466,6 +477,11 @@ def step_3d(setup, state, dt):
         return
     if setup.get("solver") == "roe_m_3d":
         roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])
+        return
+    if setup.get("gravity"):
+        g = [np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym", "gz", "gzm")]
+        mlw_m_g_3d(*state, dt, setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"],
+                   setup["dy"], setup["dym"], setup["dz"], setup["dzm"])
         return
     mlw_m_3d(*state, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"], setup["dy"],
              setup["dym"], setup["dz"], setup["dzm"])

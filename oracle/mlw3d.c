@@ -6,6 +6,8 @@
  *   mlwfull   cans3d/hdmlw/mlwfull.f:34-52
  *   mlwartv   cans3d/hdmlw/mlwartv.f
  *   mlw_m     cans3d/hdmlw/mlw_m.f:2-453
+ *   mlw_m_g   cans3d/hdmlw/mlw_m_g.f:2-469 (with gravity), with
+ *   mlwsrch   cans3d/hdmlw/mlwsrch.f:32-50 and mlwsrcf cans3d/hdmlw/mlwsrcf.f:35-45
  *   cfl_m     cans3d/common/cfl_m.f:39-85 (pi in single precision)
  */
 #include "oracle.h"
@@ -114,21 +116,67 @@ static void mlwartv3(const double *u, double *du, double dt, const double *qx,
                        (A(u, i, j, k) - A(u, i, j, k - 1))));
 }
 
+/* cans3d/hdmlw/mlwsrch.f:32-50 */
+static void mlwsrch3(double *un, double *du, double dt, const double *s, int ix,
+                     int jx, int kx) {
+  OMP_FOR
+  for (int k = 2; k <= kx - 1; k++)
+    for (int j = 2; j <= jx - 1; j++)
+      for (int i = 2; i <= ix - 1; i++)
+        A(du, i, j, k) = A(du, i, j, k) + 0.5 * dt * A(s, i, j, k);
+  OMP_FOR
+  for (int k = 1; k <= kx - 1; k++)
+    for (int j = 1; j <= jx - 1; j++)
+      for (int i = 1; i <= ix - 1; i++) {
+        double sh = (A(s, i + 1, j, k) + A(s, i, j, k) + A(s, i + 1, j + 1, k) +
+                     A(s, i, j + 1, k) + A(s, i + 1, j, k + 1) + A(s, i, j, k + 1) +
+                     A(s, i + 1, j + 1, k + 1) + A(s, i, j + 1, k + 1)) /
+                    8;
+        A(un, i, j, k) = A(un, i, j, k) + dt * sh;
+      }
+}
+
+/* cans3d/hdmlw/mlwsrcf.f:35-45 */
+static void mlwsrcf3(double *du, double dt, const double *s, const double *ux0,
+                     const double *ux1, int ix, const double *uy0,
+                     const double *uy1, int jx, const double *uz0,
+                     const double *uz1, int kx) {
+  OMP_FOR
+  for (int k = 2; k <= kx - 1; k++)
+    for (int j = 2; j <= jx - 1; j++)
+      for (int i = 2; i <= ix - 1; i++) {
+        double sh =
+            uz0[I1(k)] * (uy0[I1(j)] * (ux0[I1(i)] * A(s, i - 1, j - 1, k - 1) +
+                                        ux1[I1(i)] * A(s, i, j - 1, k - 1)) +
+                          uy1[I1(j)] * (ux0[I1(i)] * A(s, i - 1, j, k - 1) +
+                                        ux1[I1(i)] * A(s, i, j, k - 1))) +
+            uz1[I1(k)] * (uy0[I1(j)] * (ux0[I1(i)] * A(s, i - 1, j - 1, k) +
+                                        ux1[I1(i)] * A(s, i, j - 1, k)) +
+                          uy1[I1(j)] * (ux0[I1(i)] * A(s, i - 1, j, k) +
+                                        ux1[I1(i)] * A(s, i, j, k)));
+        A(du, i, j, k) = A(du, i, j, k) + 0.5 * dt * sh;
+      }
+}
+
 #define LOOP3(k0, k1, j0, j1, i0, i1)                                          \
   OMP_FOR                                                                      \
   for (int k = k0; k <= k1; k++)                                               \
     for (int j = j0; j <= j1; j++)                                             \
       for (int i = i0; i <= i1; i++)
 
-/* cans3d/hdmlw/mlw_m.f:2-453 */
-void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
-                     double *bx, double *by, double *bz, double dt, double qav,
-                     double gm, const double *dx, const double *dxm, int ix,
-                     const double *dy, const double *dym, int jx,
-                     const double *dz, const double *dzm, int kx) {
+/* cans3d/hdmlw/mlw_m.f:2-453.  With g (gx, gxm, gy, gym, gz, gzm) this is
+ * mlw_m_g (cans3d/hdmlw/mlw_m_g.f:2-469): the gravity sources of
+ * mlw_m_g.f:135-196 at the cells and :289-350 at the corners enter the energy
+ * and the three momenta through mlwsrch / mlwsrcf. */
+static void mlw_m_3d_core(double *ro, double *pr, double *vx, double *vy, double *vz,
+                          double *bx, double *by, double *bz, double dt, double qav,
+                          double gm, const double *const *g, const double *dx,
+                          const double *dxm, int ix, const double *dy,
+                          const double *dym, int jx, const double *dz,
+                          const double *dzm, int kx) {
   const size_t n = (size_t)ix * (size_t)jx * (size_t)kx;
   const size_t nm = (size_t)(ix > jx ? (ix > kx ? ix : kx) : (jx > kx ? jx : kx));
-  enum { NT = 36 };
+  enum { NT = 37 };
   double *w = arena_get(&arena3d, NT * n + 12 * nm);
   double *t[NT];
   for (int a = 0; a < NT; a++) t[a] = w + a * n;
@@ -141,7 +189,7 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
   double *dro = t[22], *dee = t[23], *drx = t[24], *dry = t[25], *drz = t[26];
   double *dbx = t[27], *dby = t[28], *dbz = t[29];
   double *fx = t[30], *qx = t[31], *fy = t[32], *qy = t[33], *fz = t[34],
-         *qz = t[35];
+         *qz = t[35], *ss = t[36];
   double *m = w + NT * n;
   double *dxi = m, *dxim = m + nm, *ux0 = m + 2 * nm, *ux1 = m + 3 * nm;
   double *dyi = m + 4 * nm, *dyim = m + 5 * nm, *uy0 = m + 6 * nm,
@@ -215,6 +263,13 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     fz[c] = ep * vz[c] + (by[c] * ex[c] - bx[c] * ey[c]) * pi4i;
   }
   HALF3(ee, eeh, dee);
+  if (g) {  /* mlw_m_g.f:135-142 */
+    LOOP3(1, kx, 1, jx, 1, ix) {
+      size_t c = I3(i, j, k);
+      ss[c] = ro[c] * (vx[c] * g[0][c] + vy[c] * g[2][c] + vz[c] * g[4][c]);
+    }
+    mlwsrch3(eeh, dee, dt, ss, ix, jx, kx);
+  }
   LOOP3(1, kx, 1, jx, 1, ix) {
     size_t c = I3(i, j, k);
     fx[c] = ro[c] * (vx[c] * vx[c]) + pr[c] +
@@ -223,6 +278,10 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     fz[c] = ro[c] * vx[c] * vz[c] - pi4i * bx[c] * bz[c];
   }
   HALF3(rx, rxh, drx);
+  if (g) {  /* mlw_m_g.f:154-160 */
+    LOOP3(1, kx, 1, jx, 1, ix) ss[I3(i, j, k)] = ro[I3(i, j, k)] * g[0][I3(i, j, k)];
+    mlwsrch3(rxh, drx, dt, ss, ix, jx, kx);
+  }
   LOOP3(1, kx, 1, jx, 1, ix) {
     size_t c = I3(i, j, k);
     fx[c] = ro[c] * vy[c] * vx[c] - pi4i * by[c] * bx[c];
@@ -231,6 +290,10 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     fz[c] = ro[c] * vy[c] * vz[c] - pi4i * by[c] * bz[c];
   }
   HALF3(ry, ryh, dry);
+  if (g) {  /* mlw_m_g.f:172-178 */
+    LOOP3(1, kx, 1, jx, 1, ix) ss[I3(i, j, k)] = ro[I3(i, j, k)] * g[2][I3(i, j, k)];
+    mlwsrch3(ryh, dry, dt, ss, ix, jx, kx);
+  }
   LOOP3(1, kx, 1, jx, 1, ix) {
     size_t c = I3(i, j, k);
     fx[c] = ro[c] * vz[c] * vx[c] - pi4i * bz[c] * bx[c];
@@ -239,6 +302,10 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
             pi8i * (bx[c] * bx[c] + by[c] * by[c] - bz[c] * bz[c]);
   }
   HALF3(rz, rzh, drz);
+  if (g) {  /* mlw_m_g.f:190-196 */
+    LOOP3(1, kx, 1, jx, 1, ix) ss[I3(i, j, k)] = ro[I3(i, j, k)] * g[4][I3(i, j, k)];
+    mlwsrch3(rzh, drz, dt, ss, ix, jx, kx);
+  }
   LOOP3(1, kx, 1, jx, 1, ix) {
     size_t c = I3(i, j, k);
     fx[c] = 0.;
@@ -296,6 +363,13 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     fz[c] = ep * vzh[c] + (byh[c] * exh[c] - bxh[c] * eyh[c]) * pi4i;
   }
   FULL3(dee);
+  if (g) {  /* mlw_m_g.f:289-296 */
+    LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) {
+      size_t c = I3(i, j, k);
+      ss[c] = roh[c] * (vxh[c] * g[1][c] + vyh[c] * g[3][c] + vzh[c] * g[5][c]);
+    }
+    mlwsrcf3(dee, dt, ss, ux0, ux1, ix, uy0, uy1, jx, uz0, uz1, kx);
+  }
   LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) {
     size_t c = I3(i, j, k);
     fx[c] = roh[c] * (vxh[c] * vxh[c]) + prh[c] +
@@ -304,6 +378,10 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     fz[c] = roh[c] * vxh[c] * vzh[c] - pi4i * bxh[c] * bzh[c];
   }
   FULL3(drx);
+  if (g) {  /* mlw_m_g.f:308-314 */
+    LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) ss[I3(i, j, k)] = roh[I3(i, j, k)] * g[1][I3(i, j, k)];
+    mlwsrcf3(drx, dt, ss, ux0, ux1, ix, uy0, uy1, jx, uz0, uz1, kx);
+  }
   LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) {
     size_t c = I3(i, j, k);
     fx[c] = roh[c] * vyh[c] * vxh[c] - pi4i * byh[c] * bxh[c];
@@ -312,6 +390,10 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     fz[c] = roh[c] * vyh[c] * vzh[c] - pi4i * byh[c] * bzh[c];
   }
   FULL3(dry);
+  if (g) {  /* mlw_m_g.f:326-332 */
+    LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) ss[I3(i, j, k)] = roh[I3(i, j, k)] * g[3][I3(i, j, k)];
+    mlwsrcf3(dry, dt, ss, ux0, ux1, ix, uy0, uy1, jx, uz0, uz1, kx);
+  }
   /* the reference sweeps j and i over the full range here (:286-297) */
   LOOP3(1, kx - 1, 1, jx, 1, ix) {
     size_t c = I3(i, j, k);
@@ -321,6 +403,10 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
             pi8i * (bxh[c] * bxh[c] + byh[c] * byh[c] - bzh[c] * bzh[c]);
   }
   FULL3(drz);
+  if (g) {  /* mlw_m_g.f:344-350 */
+    LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) ss[I3(i, j, k)] = roh[I3(i, j, k)] * g[5][I3(i, j, k)];
+    mlwsrcf3(drz, dt, ss, ux0, ux1, ix, uy0, uy1, jx, uz0, uz1, kx);
+  }
   LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) {
     size_t c = I3(i, j, k);
     fx[c] = 0.;
@@ -385,6 +471,28 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
     double bb = bx[c] * bx[c] + by[c] * by[c] + bz[c] * bz[c];
     pr[c] = (gm - 1) * (ee[c] - 0.5 * ro[c] * vv - pi8i * bb);
   }
+}
+
+void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                     double *bx, double *by, double *bz, double dt, double qav,
+                     double gm, const double *dx, const double *dxm, int ix,
+                     const double *dy, const double *dym, int jx,
+                     const double *dz, const double *dzm, int kx) {
+  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, NULL, dx, dxm, ix, dy, dym,
+                jx, dz, dzm, kx);
+}
+
+/* cans3d/hdmlw/mlw_m_g.f:2-4 */
+void oracle_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                       double *bx, double *by, double *bz, double dt, double qav,
+                       double gm, const double *gx, const double *gxm,
+                       const double *gy, const double *gym, const double *gz,
+                       const double *gzm, const double *dx, const double *dxm,
+                       int ix, const double *dy, const double *dym, int jx,
+                       const double *dz, const double *dzm, int kx) {
+  const double *g[6] = {gx, gxm, gy, gym, gz, gzm};
+  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, g, dx, dxm, ix, dy, dym, jx,
+                dz, dzm, kx);
 }
 
 /* cans3d/common/cfl_m.f:39-85; pai = acos(-1.0) is evaluated in single

@@ -157,6 +157,15 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                      double gm, const double *dx, const double *dxm, int ix,
                      const double *dy, const double *dym, int jx,
                      const double *dz, const double *dzm, int kx);
+/* mlw_m_g (cans3d/hdmlw/mlw_m_g.f:2-4): the 3-D step with gravity; gx, gy,
+ * gz at the cells, gxm, gym, gzm at the cell corners, ix*jx*kx each */
+void oracle_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                       double *bx, double *by, double *bz, double dt, double qav,
+                       double gm, const double *gx, const double *gxm,
+                       const double *gy, const double *gym, const double *gz,
+                       const double *gzm, const double *dx, const double *dxm,
+                       int ix, const double *dy, const double *dym, int jx,
+                       const double *dz, const double *dzm, int kx);
 void oracle_cfl_m_3d(double *dt, double safety, double dtmin, int *merr,
                      double gm, const double *ro, const double *pr,
                      const double *vx, const double *vy, const double *vz,

@@ -140,6 +140,24 @@ def case_res(solver, ix, jx, seed, grav):
     return out
 
 
+def case_grav3(ix, jx, kx, seed):
+    """One 3-D step with gravity (cans3d/hdmlw/mlw_m_g.f) of a seeded state
+    with seeded non-uniform gravity fields."""
+    s = setups.random_gravity(setups.random_state_3d(ix, jx, kx, seed=seed), seed + 1)
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dxm", "dy", "dym", "dz", "dzm"):
+        out["grid_" + k] = s[k]
+    for k in ("gx", "gxm", "gy", "gym", "gz", "gzm"):
+        out["grav_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_3d(s, st, 0.4)
+    oracle.step_3d(s, st, dt)
+    out["dt"] = np.array(dt)
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def bd_case():
     rng = np.random.default_rng(13)
     q = np.asfortranarray(rng.standard_normal((9, 7)))
@@ -167,6 +185,7 @@ FIXTURES = {
     "mlw_m3_g_2d_17x18": lambda: case_grav("mlw_m3", 17, 18, 26),
     "mlw_m_e_2d_18x17": lambda: case_res("mlw_m", 18, 17, 27, False),
     "mlw_m3_ge_2d_17x19": lambda: case_res("mlw_m3", 17, 19, 28, True),
+    "mlw_m_g_3d_13x12x14": lambda: case_grav3(13, 12, 14, 29),
 }
 
 

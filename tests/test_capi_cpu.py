@@ -51,7 +51,7 @@ def test_run_desc_layout_matches_header(tmp_path):
     assert fields == ["solver", "ix", "jx", "kx", "margin", "gm", "qav", "dx", "dxm", "dy",
                       "dym", "dz", "dzm", "exact", "tile", "stream", "bx", "bxm", "mu",
                       "mfdim", "gx", "gxm", "sc", "scm", "dsc", "dscm", "rr", "rrm", "drr",
-                      "drrm", "chkdav", "floor", "trq", "trq0", "seed", "gy", "gym", "et", "etm"]
+                      "drrm", "chkdav", "floor", "trq", "trq0", "seed", "gy", "gym", "et", "etm", "gz", "gzm"]
     import shutil
     import subprocess
     cc = shutil.which("gcc") or shutil.which("cc")

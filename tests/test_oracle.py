@@ -899,3 +899,68 @@ def test_reconnection_setup_follows_the_model(oracle_lib):
     st = setups.copy_state(s)
     t, ns, merr, dts = oracle_lib.run_2d(s, st, 5)
     assert ns == 5 and merr == 0 and all(np.all(np.isfinite(a)) for a in st)
+
+
+# ---- 3-D step with gravity (cans3d/hdmlw/mlw_m_g.f) ----------------------------
+
+def test_gravity_3d_with_zero_fields_is_the_plain_step(oracle_lib):
+    s = setups.random_state_3d(14, 12, 13, seed=3)
+    z = np.zeros(s["state"][0].shape, order="F")
+    g = dict(s, gravity=True, gx=z, gxm=z, gy=z, gym=z, gz=z, gzm=z)
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    oracle_lib.step_3d(s, a, 1e-3)
+    oracle_lib.step_3d(g, b, 1e-3)
+    for k, x, y in zip(s["names"], a, b):
+        assert np.array_equal(x, y), k
+
+
+def test_gravity_3d_accelerates_a_uniform_state(oracle_lib):
+    """Uniform state at rest, uniform g: one step gives v = g dt in all three
+    components (mlwsrch at the cells and corners, mlwsrcf back to the cells)
+    and leaves density and field unchanged."""
+    s = setups.random_state_3d(12, 11, 10, seed=2)
+    shape = s["state"][0].shape
+    vals = dict(ro=1.3, pr=0.8, vx=0.0, vy=0.0, vz=0.0, bx=0.4, by=-0.2, bz=0.1)
+    st = [np.asfortranarray(np.full(shape, vals[k])) for k in s["names"]]
+    gv, dt = (0.3, -0.7, 0.45), 1e-3
+    g = dict(s, gravity=True, qav=0.0)
+    for k, v in zip(("gx", "gy", "gz"), gv):
+        g[k] = np.full(shape, v, order="F")
+        g[k + "m"] = np.full(shape, v, order="F")
+    oracle_lib.step_3d(g, st, dt)
+    inner = (slice(1, -1),) * 3
+    for name, v in zip(("vx", "vy", "vz"), gv):
+        assert np.allclose(st[s["names"].index(name)][inner], v * dt, rtol=1e-12, atol=0)
+    assert np.allclose(st[0][inner], 1.3, rtol=1e-14)
+
+
+def test_gravity_3d_oracle_matches_frozen_fixture(oracle_lib):
+    z = np.load(GOLD / "mlw_m_g_3d_13x12x14.npz")
+    names = setups.VARS["mlw_m_3d"]
+    st = [np.asfortranarray(z["in_" + k]) for k in names]
+    g = {k: np.asfortranarray(z["grav_" + k]) for k in ("gx", "gxm", "gy", "gym", "gz", "gzm")}
+    s = dict(solver="mlw_m_3d", gravity=True, qav=3.0, gm=5.0 / 3.0, **g,
+             **{k: z["grid_" + k] for k in ("dx", "dxm", "dy", "dym", "dz", "dzm")})
+    oracle_lib.step_3d(s, st, float(z["dt"]))
+    for k, a in zip(names, st):
+        assert np.array_equal(a, z["out_" + k]), k
+
+
+def test_emerging_flux_setup_follows_the_model(oracle_lib):
+    """md_efr/hdmlw/model.f: horizontally uniform stratification with the
+    flux sheet bx^2/(8 pi p) = rbeta0 (1/4 inside -2 < z < 0), gravity
+    -1/gm along z, the z faces of ro and pr held at the initial ghost
+    values, and a short loop stays finite."""
+    s = setups.emerging_flux_3d(32, 2, 32)
+    g = dict(zip(s["names"], s["state"]))
+    assert np.all(g["ro"] == g["ro"][:1, :1, :]) and np.all(g["pr"] == g["pr"][:1, :1, :])
+    beta_inv = g["bx"] ** 2 / (8 * math.pi * g["pr"])
+    zc = np.abs(s["z"] + 1.0).argmin()
+    assert abs(beta_inv[5, 1, zc] - 0.25) < 0.02
+    assert np.all(s["gz"] == -0.6) and not np.any(s["gx"])
+    cns = [(v, f, q) for v, f, k, q in s["bc"] if k == setups.BD_CNS]
+    assert sorted((v, f) for v, f, _ in cns) == [(0, 4), (0, 5), (1, 4), (1, 5)]
+    assert dict(((v, f), q) for v, f, q in cns)[(1, 4)] == g["pr"][0, 0, 0]
+    st = setups.copy_state(s)
+    t, ns, merr, _ = oracle_lib.run_3d(s, st, 10)
+    assert ns == 10 and merr == 0 and all(np.all(np.isfinite(a)) for a in st)

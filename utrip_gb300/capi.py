@@ -98,6 +98,8 @@ def load() -> C.CDLL:
                             [_dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_roe_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _ip, _dp, _ip, _dp, _ip])
     sig["cans_mlw_m3_g_2d"] = (i, [_dp] * 9 + [_dp] * 7 + [_dp, _dp, _ip, _dp, _dp, _ip])
+    sig["cans_mlw_m_g_3d"] = (i, [_dp] * 8 + [_dp] * 9 + [_dp, _dp, _ip, _dp, _dp, _ip,
+                                                           _dp, _dp, _ip])
     sig["cans_mlw_m_g_2d"] = (i, [_dp] * 7 + [_dp] * 7 + [_dp, _dp, _ip, _dp, _dp, _ip])
     sig["cans_mlw_m3_e_2d"] = (i, [_dp] * 9 + [_dp] * 5 + [_dp, _dp, _ip, _dp, _dp, _ip])
     sig["cans_mlw_m_e_2d"] = (i, [_dp] * 7 + [_dp] * 5 + [_dp, _dp, _ip, _dp, _dp, _ip])
@@ -398,6 +400,17 @@ def bd_1d(kind: int, mbnd: int, margin: int, qq: np.ndarray, q0: float = 0.0,
 
 # ---- drop-in routines (3-D) ------------------------------------------------
 
+def mlw_m_g_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, gx, gxm, gy, gym, gz, gzm,
+               dx, dxm, dy, dym, dz, dzm):
+    """cans3d/hdmlw/mlw_m_g.f:2 -- the 3-D step with gravity, in place."""
+    ix, jx, kx = ro.shape
+    return _check(load().cans_mlw_m_g_3d(
+        *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], _dref(dt), _dref(qav),
+        _dref(gm), *[_ptr(a) for a in (gx, gxm, gy, gym, gz, gzm)], _ptr(dx), _ptr(dxm),
+        _iref(ix), _ptr(dy), _ptr(dym), _iref(jx), _ptr(dz), _ptr(dzm), _iref(kx)),
+        "mlw_m_g_3d")
+
+
 def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):
     """cans3d/hdmlw/mlw_m.f:2 -- one mLW step of the 3-D state, in place."""
     ix, jx, kx = ro.shape
@@ -506,7 +519,7 @@ class _Desc(C.Structure):
                 ("dscm", _dp), ("rr", _dp), ("rrm", _dp), ("drr", _dp), ("drrm", _dp),
                 ("chkdav", C.c_int), ("floor", C.c_double), ("trq", _dp),
                 ("trq0", C.c_double), ("seed", C.c_ulonglong), ("gy", _dp), ("gym", _dp),
-                ("et", _dp), ("etm", _dp)]
+                ("et", _dp), ("etm", _dp), ("gz", _dp), ("gzm", _dp)]
 
 
 class RunState(C.Structure):
@@ -550,14 +563,15 @@ class Run:
                   1 if exact else 0, tile, C.c_void_p(stream) if stream else None,
                   arr("bx") if one else None, arr("bxm") if one else None,
                   mu, (C.c_int * 3)(*mfdim))
-        if not one and not three and grid.get("gx") is not None:
-            # 2-D step with gravity: the four fields (ix*jx, Fortran order)
-            for k in ("gx", "gxm", "gy", "gym"):
+        if not one and grid.get("gx") is not None:
+            # step with gravity: four fields (2-D) or six (3-D), Fortran order
+            shape = (nx, ny, nz) if three else (nx, ny)
+            for k in ("gx", "gxm", "gy", "gym") + (("gz", "gzm") if three else ()):
                 if grid.get(k) is None:  # NULL: the library rejects the set-up
                     continue
                 a = np.asfortranarray(grid[k], dtype=np.float64)
-                if a.shape != (nx, ny):
-                    raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {(nx, ny)}")
+                if a.shape != shape:
+                    raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {shape}")
                 self._keep.append(a)
                 setattr(d, k, a.ctypes.data_as(_dp))
         if not one and not three and grid.get("et") is not None:

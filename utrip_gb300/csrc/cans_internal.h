@@ -90,6 +90,12 @@ cudaError_t launch_mlw3d(bool exact, int tile, const double *A, double *B,
                          int ix, int jx, int kx, const Axis &ax,
                          const Axis &ay, const Axis &az, const Phys &ph,
                          double dt, Ctl *ctl, Box3 box, cudaStream_t s);
+// 3-D mlw_m_g (mlw3d.cu): grav = gx, gxm, gy, gym, gz, gzm (n each)
+int mlw3d_g_tile_count();
+cudaError_t launch_mlw3d_g(bool exact, int tile, const double *A, double *B, int ix,
+                           int jx, int kx, const Axis &ax, const Axis &ay, const Axis &az,
+                           const Phys &ph, const double *grav, double dt, Ctl *ctl,
+                           Box3 box, cudaStream_t s);
 int mlw3d_tile_count();
 cudaError_t launch_cfl3d_full(bool exact, const double *S, int ix, int jx,
                               int kx, const Axis &ax, const Axis &ay,

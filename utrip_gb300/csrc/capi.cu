@@ -174,18 +174,19 @@ struct Scratch {
     }
     return CANS_OK;
   }
-  // gravity fields gx, gxm, gy, gym of the 2-D steps with gravity
+  // gravity fields of the steps with gravity: gx, gxm, gy, gym (2-D), and
+  // gz, gzm (3-D)
   double *grav = nullptr;
   size_t grav_cap = 0;
-  int upload_grav(const double *const *g, size_t n, cudaStream_t s) {
-    if (grav_cap < 4 * n) {
+  int upload_grav(const double *const *g, size_t n, cudaStream_t s, int nf = 4) {
+    if (grav_cap < nf * n) {
       if (grav) cudaFree(grav);
       grav = nullptr;
       grav_cap = 0;
-      CK(cudaMalloc(&grav, sizeof(double) * 4 * n));
-      grav_cap = 4 * n;
+      CK(cudaMalloc(&grav, sizeof(double) * nf * n));
+      grav_cap = nf * n;
     }
-    for (int k = 0; k < 4; k++)
+    for (int k = 0; k < nf; k++)
       CK(cudaMemcpyAsync(grav + k * n, g[k], sizeof(double) * n, cudaMemcpyHostToDevice, s));
     return CANS_OK;
   }
@@ -906,22 +907,22 @@ extern "C" int cans_bdfrdx_1d(const int *mbnd, const int *margin, double *qq,
 
 // ---------------------------------------------------------------------------
 // 3-D drop-in entry points
-extern "C" int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy,
-                             double *vz, double *bx, double *by, double *bz,
-                             const double *dt, const double *qav,
-                             const double *gm, const double *dx,
-                             const double *dxm, const int *ix,
-                             const double *dy, const double *dym,
-                             const int *jx, const double *dz,
-                             const double *dzm, const int *kx) {
-  const int nx = *ix, ny = *jx, nz = *kx;
+namespace {
+// One 3-D mLW step on host arrays or their registered mirrors; with grav
+// (gx, gxm, gy, gym, gz, gzm host arrays) the step with gravity.
+int step3d(double *const *arrs, double dt, double qav, double gm, const double *dx,
+           const double *dxm, int nx, const double *dy, const double *dym, int ny,
+           const double *dz, const double *dzm, int nz,
+           const double *const *grav = nullptr) {
   if (nx < 3 || ny < 3 || nz < 3) return CANS_ERR_ARG;
-  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  if (grav)
+    for (int k = 0; k < 6; k++)
+      if (!grav[k]) return CANS_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
   int rc = lib_stream(&s);
   if (rc) return rc;
-  const Phys ph = make_phys(*gm, *qav);
+  const Phys ph = make_phys(gm, qav);
   const size_t n = (size_t)nx * ny * nz;
   MirrorSet *m = resident_step_set(arrs, 8);
   Scratch &sc = g_scratch;
@@ -930,9 +931,15 @@ extern "C" int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy,
   if ((rc = dax->upload(nx, dx, dxm, s))) return rc;
   if ((rc = day->upload(ny, dy, dym, s))) return rc;
   if ((rc = daz->upload(nz, dz, dzm, s))) return rc;
+  if (grav && (rc = sc.upload_grav(grav, n, s, 6))) return rc;
+  auto step = [&](const double *A, double *B) {
+    return grav ? launch_mlw3d_g(exact_mode(), 0, A, B, nx, ny, nz, dax->a, day->a, daz->a,
+                                 ph, sc.grav, dt, nullptr, Box3{}, s)
+                : launch_mlw3d(exact_mode(), 0, A, B, nx, ny, nz, dax->a, day->a, daz->a,
+                               ph, dt, nullptr, Box3{}, s);
+  };
   if (m) {
-    CK(launch_mlw3d(exact_mode(), 0, m->buf[m->cur], m->buf[m->cur ^ 1], nx, ny,
-                    nz, dax->a, day->a, daz->a, ph, *dt, nullptr, Box3{}, s));
+    CK(step(m->buf[m->cur], m->buf[m->cur ^ 1]));
     m->cur ^= 1;
     return CANS_OK;
   }
@@ -940,13 +947,42 @@ extern "C" int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy,
   for (int v = 0; v < 8; v++)
     CK(cudaMemcpyAsync(sc.A + v * n, arrs[v], sizeof(double) * n,
                        cudaMemcpyHostToDevice, s));
-  CK(launch_mlw3d(exact_mode(), 0, sc.A, sc.B, nx, ny, nz, dax->a, day->a,
-                  daz->a, ph, *dt, nullptr, Box3{}, s));
+  CK(step(sc.A, sc.B));
   for (int v = 0; v < 8; v++)
     CK(cudaMemcpyAsync(arrs[v], sc.B + v * n, sizeof(double) * n,
                        cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   return CANS_OK;
+}
+}  // namespace
+
+extern "C" int cans_mlw_m_3d(double *ro, double *pr, double *vx, double *vy,
+                             double *vz, double *bx, double *by, double *bz,
+                             const double *dt, const double *qav,
+                             const double *gm, const double *dx,
+                             const double *dxm, const int *ix,
+                             const double *dy, const double *dym,
+                             const int *jx, const double *dz,
+                             const double *dzm, const int *kx) {
+  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  return step3d(arrs, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, dz, dzm, *kx);
+}
+
+// mlw_m_g (cans3d/hdmlw/mlw_m_g.f:2-4): the 3-D step with gravity
+extern "C" int cans_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy,
+                               double *vz, double *bx, double *by, double *bz,
+                               const double *dt, const double *qav,
+                               const double *gm, const double *gx,
+                               const double *gxm, const double *gy,
+                               const double *gym, const double *gz,
+                               const double *gzm, const double *dx,
+                               const double *dxm, const int *ix,
+                               const double *dy, const double *dym,
+                               const int *jx, const double *dz,
+                               const double *dzm, const int *kx) {
+  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  const double *grav[6] = {gx, gxm, gy, gym, gz, gzm};
+  return step3d(arrs, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, dz, dzm, *kx, grav);
 }
 
 extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
@@ -1301,7 +1337,7 @@ struct cans_run {
                                // profiles and the torque profile, ix each
   Loop1D loop1d{};             // 1-D loop options (device pointers into bx1)
   double *roe = nullptr;       // Roe / HLLD: stage scratch
-  double *grav = nullptr;      // 2-D mLW with gravity: gx gxm gy gym (n each)
+  double *grav = nullptr;      // mLW with gravity: gx gxm gy gym (gz gzm), n each
   double *eta = nullptr;       // 2-D mLW with resistivity: et, etm (n each)
   double *res = nullptr;       //   and the eta*J fields of each step
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
@@ -1341,7 +1377,7 @@ int layout2d(const cans_run *h) {
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
   if (is_roe(h) || is_hlld(h) || h->ndim == 1 || h->eta) return 1;
-  if (h->grav) return mlw2d_g_tile_count();
+  if (h->grav) return h->ndim == 3 ? mlw3d_g_tile_count() : mlw2d_g_tile_count();
   return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
 }
 // 1-D: the whole loop (or one fixed step) as one cluster launch, in place
@@ -1378,6 +1414,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (is_roe(h))
     return launch_roe3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
+  if (h->ndim == 3 && h->grav)
+    return launch_mlw3d_g(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
+                          h->ay.a, h->az.a, h->ph, h->grav, dt, ctl, box, h->s);
   if (h->ndim == 3)
     return launch_mlw3d(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
@@ -1498,13 +1537,23 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     }
     if (!d->dx || !d->dy || !d->dz || !d->dxm || !d->dym || !d->dzm) return CANS_ERR_ARG;
   }
-  // every extent must exceed the two frames of margin+1 cells that the
-  // boundary program and the frame CFL work on
-  const int wmin = 2 * (d->margin + 1) + 1;
   const bool bgv = d->solver == CANS_SOLVER_MLW_M_BG_1D;
   // 2-D mLW with gx set: the steps with gravity (mlw_m_g / mlw_m3_g)
   const bool mlw2d = d->solver == CANS_SOLVER_MLW_M_2D || d->solver == CANS_SOLVER_MLW_M3_2D;
+  // every extent must hold the two frames of margin+1 cells that the
+  // boundary program and the frame CFL work on; the mLW steps need nothing
+  // between them (an axis of exactly two frames, as the thin y axis of the
+  // md_efr model, leaves the whole CFL to the frame kernel), the Roe and
+  // HLLD stencils one more cell
+  const int wmin = 2 * (d->margin + 1) +
+                   ((mlw2d || d->solver == CANS_SOLVER_MLW_M_3D) ? 0 : 1);
   const bool grav2d = mlw2d && d->gx != nullptr;
+  // 3-D mLW with gx set: mlw_m_g (six fields)
+  const bool grav3d = d->solver == CANS_SOLVER_MLW_M_3D && d->gx != nullptr;
+  if ((d->gz || d->gzm) && !grav3d) return CANS_ERR_ARG;
+  if (grav3d && (!d->gxm || !d->gy || !d->gym || !d->gz || !d->gzm)) return CANS_ERR_ARG;
+  // a solver without a gravity step refuses the fields instead of ignoring them
+  if ((d->gx || d->gy) && !(grav2d || grav3d || bgv)) return CANS_ERR_ARG;
   // 2-D mLW with et set: the resistive steps (mlw_m_e / mlw_m3_e)
   const bool eta2d = mlw2d && d->et != nullptr;
   if ((d->et || d->etm) && !(eta2d && d->etm)) return CANS_ERR_ARG;
@@ -1594,10 +1643,11 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     e = cudaMalloc(&h->roe, sizeof(double) * nd);
     if (e != cudaSuccess) return bail(fail_cuda(e, "cudaMalloc(stage scratch)"));
   }
-  if (grav2d) {  // mlw_m_g / mlw_m3_g: the four gravity fields
-    const double *g[4] = {d->gx, d->gxm, d->gy, d->gym};
-    e = cudaMalloc(&h->grav, sizeof(double) * 4 * h->n);
-    for (int k = 0; k < 4 && e == cudaSuccess; k++)
+  if (grav2d || grav3d) {  // mlw_m_g / mlw_m3_g: four gravity fields, 3-D six
+    const double *g[6] = {d->gx, d->gxm, d->gy, d->gym, d->gz, d->gzm};
+    const int nf = grav3d ? 6 : 4;
+    e = cudaMalloc(&h->grav, sizeof(double) * nf * h->n);
+    for (int k = 0; k < nf && e == cudaSuccess; k++)
       e = cudaMemcpyAsync(h->grav + k * h->n, g[k], sizeof(double) * h->n,
                           cudaMemcpyHostToDevice, h->s);
     if (e != cudaSuccess) return bail(fail_cuda(e, "gravity fields"));

@@ -16,6 +16,13 @@
 //       corrector from corner planes k-1/2 and k+1/2 (mlwfull), artificial
 //       viscosity (mlwartv), update, back to primitives, CFL, write.
 // The state crosses HBM once in and once out: 8 arrays, 128 B per zone.
+//
+// With G the kernel is mlw_m_g (cans3d/hdmlw/mlw_m_g.f:2-469): the gravity
+// sources ro (v.g), ro gx, ro gy, ro gz of each cell plane (mlw_m_g.f:135-196)
+// and the same of each half-step corner plane (:289-350) get two-plane rings
+// of their own and enter the energy and the three momenta through mlwsrch
+// (cans3d/hdmlw/mlwsrch.f:32-50) and mlwsrcf (mlwsrcf.f:35-45).  grav holds
+// gx, gxm, gy, gym, gz, gzm (ix*jx*kx each; the *m fields at the corners).
 #include <cuda_runtime.h>
 
 #include "cans_common.cuh"
@@ -43,15 +50,17 @@ struct K3 {
   static constexpr int XRZ = 12, YRZ = 13, ZRZ = 14, EX = 15, EY = 16, EZ = 17;
   static constexpr int N = 18;
 };
-template <int TX, int TY> struct Tile3 {
+template <int TX, int TY, bool G = false> struct Tile3 {
   static constexpr int CX = TX + 2, CY = TY + 2, NC = CX * CY;
   static constexpr int KX = TX + 1, KY = TY + 1, NK = KX * KY;
   static constexpr int NQX = (TX + 1) * TY, NQY = TX * (TY + 1);
   // one thread per halo-tile cell, rounded up to whole warps so that every
   // warp-level reduction sees 32 live lanes; the extra threads own no cell
   static constexpr int NT = (NC + 31) / 32 * 32;
+  // gravity: four source fields per cell plane and per corner plane
   static constexpr size_t smem_doubles =
-      2 * (size_t)C3::N * NC + 2 * (size_t)K3::N * NK + NQX + NQY + 32;
+      2 * (size_t)C3::N * NC + 2 * (size_t)K3::N * NK + NQX + NQY + 32 +
+      (G ? 2 * 4 * ((size_t)NC + NK) : 0);
   static constexpr size_t smem_bytes = smem_doubles * sizeof(double);
 };
 
@@ -134,12 +143,13 @@ __device__ __forceinline__ void cell_stage(const double *__restrict__ A,
 
 }  // namespace
 
-template <bool E, int TX, int TY>
+template <bool E, int TX, int TY, bool G = false>
 __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     k_mlw3d(const double *__restrict__ A, double *__restrict__ B, int ix,
             int jx, int kx, Axis ax, Axis ay, Axis az, Phys ph, double dt_arg,
-            Ctl *__restrict__ ctl, Box3 box, int kchunk) {
-  using T = Tile3<TX, TY>;
+            Ctl *__restrict__ ctl, Box3 box, int kchunk,
+            const double *__restrict__ grav = nullptr) {
+  using T = Tile3<TX, TY, G>;
   using FT = F<E>;
   extern __shared__ double smem[];
   double *scell = smem;                                   // [2][C3::N][NC]
@@ -147,6 +157,8 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
   double *sqx = scorn + 2 * (size_t)K3::N * T::NK;        // q*dxim of plane k
   double *sqy = sqx + T::NQX;                             // q*dyim of plane k
   double *sred = sqy + T::NQY;
+  double *sgc = sred + 32;                                // G: [2][4][NC]
+  double *sgk = sgc + 2 * 4 * (size_t)T::NC;              // G: [2][4][NK]
 
   if (ctl != nullptr) {
     if (ctl->done | ctl->pause) return;
@@ -171,15 +183,32 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
 
   auto cslot = [&](int k) { return scell + (size_t)(k & 1) * C3::N * T::NC; };
   auto kslot = [&](int k) { return scorn + (size_t)(k & 1) * K3::N * T::NK; };
+  auto gcslot = [&](int k) { return sgc + (size_t)(k & 1) * 4 * T::NC; };
+  auto gkslot = [&](int k) { return sgk + (size_t)(k & 1) * 4 * T::NK; };
 
   auto load_plane = [&](int k) {
     double *sl = cslot(k);
     if (in_arr) {
-      cell_stage<E>(A, n, (size_t)gi + (size_t)gj * ix + (size_t)k * plane, sl,
-                    T::NC, tid, ph);
+      const size_t g = (size_t)gi + (size_t)gj * ix + (size_t)k * plane;
+      cell_stage<E>(A, n, g, sl, T::NC, tid, ph);
+      if constexpr (G) {  // mlw_m_g.f:135-136, 154, 172, 190
+        const FT ro(sl[(size_t)C3::RO * T::NC + tid]);
+        const FT vx(sl[(size_t)C3::VX * T::NC + tid]), vy(sl[(size_t)C3::VY * T::NC + tid]);
+        const FT vz(sl[(size_t)C3::VZ * T::NC + tid]);
+        const FT gx(grav[g]), gy(grav[2 * n + g]), gz(grav[4 * n + g]);
+        double *gs = gcslot(k);
+        gs[tid] = (ro * (vx * gx + vy * gy + vz * gz)).v;
+        gs[T::NC + tid] = (ro * gx).v;
+        gs[2 * T::NC + tid] = (ro * gy).v;
+        gs[3 * T::NC + tid] = (ro * gz).v;
+      }
     } else if (cell) {
 #pragma unroll 1
       for (int f = 0; f < C3::N; f++) sl[(size_t)f * T::NC + tid] = 0.0;
+      if constexpr (G) {
+        double *gs = gcslot(k);
+        for (int f = 0; f < 4; f++) gs[f * T::NC + tid] = 0.0;
+      }
     }
   };
 
@@ -193,6 +222,10 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     if (a > ix - 2 || b > jx - 2) {
 #pragma unroll 1
       for (int f = 0; f < K3::N; f++) KS(f) = 0.0;
+      if constexpr (G) {
+        double *gk = gkslot(k);
+        for (int f = 0; f < 4; f++) gk[f * T::NK + tid] = 0.0;
+      }
       return;
     }
     const double *L = cslot(k), *U = cslot(k + 1);
@@ -271,6 +304,24 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
       un[v] = r;
     }
     }
+    if constexpr (G) {
+      // mlwsrch part 2 (mlwsrch.f:41-47): un += dt * (average of the eight
+      // cell sources around the corner), energy and the three momenta
+      const double *gL = gcslot(k), *gU = gcslot(k + 1);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const double *l = gL + q * T::NC, *u = gU + q * T::NC;
+        if constexpr (E) {
+          const FT sh = (FT(l[p10]) + FT(l[p00]) + FT(l[p11]) + FT(l[p01]) + FT(u[p10]) +
+                         FT(u[p00]) + FT(u[p11]) + FT(u[p01])) * 0.125;
+          un[1 + q] = un[1 + q] + dt * sh;
+        } else {
+          const double sh = ((l[p10] + l[p00]) + (l[p11] + l[p01])) +
+                            ((u[p10] + u[p00]) + (u[p11] + u[p01]));
+          un[1 + q] = FT(fma(dt.v * 0.125, sh, un[1 + q].v));
+        }
+      }
+    }
     const FT roh = un[0], eeh = un[1], rxh = un[2], ryh = un[3], rzh = un[4];
     const FT bxh = un[5], byh = un[6], bzh = un[7];
     FT vxh, vyh, vzh;
@@ -311,6 +362,15 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     KS(K3::EX) = exh.v;
     KS(K3::EY) = eyh.v;
     KS(K3::EZ) = ezh.v;
+    if constexpr (G) {  // corner sources (mlw_m_g.f:289-290, 308, 326, 344)
+      const size_t gc = (size_t)a + (size_t)b * ix + (size_t)k * plane;
+      const FT gxm(grav[n + gc]), gym(grav[3 * n + gc]), gzm(grav[5 * n + gc]);
+      double *gk = gkslot(k);
+      gk[tid] = (roh * (vxh * gxm + vyh * gym + vzh * gzm)).v;
+      gk[T::NK + tid] = (roh * gxm).v;
+      gk[2 * T::NK + tid] = (roh * gym).v;
+      gk[3 * T::NK + tid] = (roh * gzm).v;
+    }
 #undef KS
   };
 
@@ -463,6 +523,18 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
             r = fma(sg * wzNW, U[kNW] - L[kNW], r);
             r = fma(sg * wzNE, U[kNE] - L[kNE], r);
           }
+          if constexpr (G) {
+            if (v >= 1 && v <= 4) {  // mlwsrch part 1 and mlwsrcf
+              const int q = v - 1;
+              r = fma(h, gcslot(k)[q * T::NC + c], r);
+              const double *gl = gkslot(k - 1) + q * T::NK, *gu = gkslot(k) + q * T::NK;
+              const double sl_ = fma(uy0.v, fma(ux0.v, gl[kSW], ux1.v * gl[kSE]),
+                                     uy1.v * fma(ux0.v, gl[kNW], ux1.v * gl[kNE]));
+              const double su_ = fma(uy0.v, fma(ux0.v, gu[kSW], ux1.v * gu[kSE]),
+                                     uy1.v * fma(ux0.v, gu[kNW], ux1.v * gu[kNE]));
+              r = fma(h, fma(uz0.v, sl_, uz1.v * su_), r);
+            }
+          }
           unew[v] = FT(r);
         }
       } else {
@@ -490,6 +562,8 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
           if (ng) a = -a;
           du = du - hdt * (hdz * (a - FT(pfz[v])));
         }
+        // mlwsrch part 1 (mlwsrch.f:35): du += 0.5*dt*s
+        if (G && v >= 1 && v <= 4) du = du + hdt * FT(gcslot(k)[(v - 1) * T::NC + c]);
         // mlwfull: corner planes k-1/2 (L) and k+1/2 (U)
         corner_flux_src(v, 0, f, ng);
         if (f != NOF) {
@@ -514,6 +588,15 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
           const FT dfdz = dzi * (uy0 * (ux0 * (U(kSW) - L(kSW)) + ux1 * (U(kSE) - L(kSE))) +
                                  uy1 * (ux0 * (U(kNW) - L(kNW)) + ux1 * (U(kNE) - L(kNE))));
           du = du - hdt * dfdz;
+        }
+        // mlwsrcf (mlwsrcf.f:38-42): du += 0.5*dt*(corner sources to the cell)
+        if (G && v >= 1 && v <= 4) {
+          const double *gl = gkslot(k - 1) + (v - 1) * T::NK, *gu = gkslot(k) + (v - 1) * T::NK;
+          const FT sh = uz0 * (uy0 * (ux0 * FT(gl[kSW]) + ux1 * FT(gl[kSE])) +
+                               uy1 * (ux0 * FT(gl[kNW]) + ux1 * FT(gl[kNE]))) +
+                        uz1 * (uy0 * (ux0 * FT(gu[kSW]) + ux1 * FT(gu[kSE])) +
+                               uy1 * (ux0 * FT(gu[kNW]) + ux1 * FT(gu[kNE])));
+          du = du + hdt * sh;
         }
         // mlwartv
         const FT u(S0[(size_t)v * T::NC + c]);
@@ -603,15 +686,15 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
 }
 
 namespace {
-template <bool E, int TX, int TY>
+template <bool E, int TX, int TY, bool G = false>
 cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
                     const Axis &ax, const Axis &ay, const Axis &az,
                     const Phys &ph, double dt, Ctl *ctl, Box3 box, int kchunk,
-                    cudaStream_t s) {
-  using T = Tile3<TX, TY>;
+                    cudaStream_t s, const double *grav = nullptr) {
+  using T = Tile3<TX, TY, G>;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY>,
+    cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY, G>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)T::smem_bytes);
     if (e != cudaSuccess) return e;
@@ -620,12 +703,28 @@ cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
   dim3 grid((ix - 2 + TX - 1) / TX, (jx - 2 + TY - 1) / TY,
             (kx - 2 + kchunk - 1) / kchunk);
   dim3 block(T::NT);
-  k_mlw3d<E, TX, TY><<<grid, block, T::smem_bytes, s>>>(A, B, ix, jx, kx, ax, ay, az,
-                                                       ph, dt, ctl, box, kchunk);
+  k_mlw3d<E, TX, TY, G><<<grid, block, T::smem_bytes, s>>>(A, B, ix, jx, kx, ax, ay, az,
+                                                          ph, dt, ctl, box, kchunk, grav);
   count_launch();
   return cudaGetLastError();
 }
 }  // namespace
+
+// mlw_m_g: the gravity rings do not fit beside a 16 x 16 tile (222 KB), so
+// the step with gravity runs 16 x 8 tiles (143 KB), z chunks of 64 or 32.
+int mlw3d_g_tile_count() { return 2; }
+
+cudaError_t launch_mlw3d_g(bool exact, int tile, const double *A, double *B, int ix,
+                           int jx, int kx, const Axis &ax, const Axis &ay, const Axis &az,
+                           const Phys &ph, const double *grav, double dt, Ctl *ctl,
+                           Box3 box, cudaStream_t s) {
+  if (ix < 3 || jx < 3 || kx < 3 || grav == nullptr) return cudaErrorInvalidValue;
+  const int kchunk = (tile == 1) ? 32 : 64;
+  return exact ? launch3<true, 16, 8, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box,
+                                            kchunk, s, grav)
+               : launch3<false, 16, 8, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box,
+                                             kchunk, s, grav);
+}
 
 int mlw3d_tile_count() { return 3; }
 

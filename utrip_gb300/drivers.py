@@ -118,6 +118,11 @@ def _step(setup, state, dt):
             *state, dt, setup["qav"], setup["gm"], *e, setup["dx"], setup["dxm"], setup["dy"],
             setup["dym"], *g)
         return
+    if setup.get("gravity") and setup["solver"] == "mlw_m_3d":  # 3-D mlw_m_g
+        g = [np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym", "gz", "gzm")]
+        capi.mlw_m_g_3d(*state, dt, setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"],
+                        setup["dy"], setup["dym"], setup["dz"], setup["dzm"])
+        return
     if setup.get("gravity"):
         g = [setup[k] for k in ("gx", "gxm", "gy", "gym")]
         args = (setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"], setup["dy"],

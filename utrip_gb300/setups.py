@@ -16,7 +16,8 @@ import math
 
 import numpy as np
 
-from .capi import (BD_FRD, BD_FRE, BD_PER, BD_SMN, BD_SMP, BD_SPN, BD_SPP, SOLVER_HLLD_3D,
+from .capi import (BD_CNS, BD_FRD, BD_FRE, BD_PER, BD_SMN, BD_SMP, BD_SPN, BD_SPP,
+                   SOLVER_HLLD_3D,
                    SOLVER_MLW_M_2D, SOLVER_MLW_M3_2D, SOLVER_ROE_M3_2D, SOLVER_ROE_M_3D)
 
 SQ4PI = math.sqrt(4.0 * math.pi)
@@ -747,12 +748,14 @@ def mhd_gravity_wave(n: int = 64, solver: str = "mlw_m", amp: float = 0.5):
 
 
 def random_gravity(s: dict, seed: int = 0, scale: float = 0.3) -> dict:
-    """Seeded non-uniform gravity fields on a 2-D set-up (every source term
-    of mlw_m_g / mlw_m3_g non-zero): returns a copy with gx, gxm, gy, gym."""
+    """Seeded non-uniform gravity fields on a 2-D or 3-D set-up (every source
+    term of mlw_m_g / mlw_m3_g, or of the 3-D mlw_m_g, non-zero): returns a
+    copy with gx, gxm, gy, gym (and gz, gzm in 3-D)."""
     rng = np.random.default_rng(seed)
     shape = s["state"][0].shape
     out = dict(s)
-    for k in ("gx", "gxm", "gy", "gym"):
+    keys = ("gx", "gxm", "gy", "gym") + (("gz", "gzm") if len(shape) == 3 else ())
+    for k in keys:
         out[k] = np.asfortranarray(scale * rng.standard_normal(shape))
     out["gravity"] = True
     return out
@@ -835,3 +838,102 @@ def magnetic_reconnection(n: int = 128):
     s["et"] = np.asfortranarray(et)
     s["etm"] = np.asfortranarray(etm)
     return s
+
+
+def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
+    """The 3-D emerging-flux model of cans3d/md_efr/hdmlw (model.f, pertub.f,
+    bnd.f, main.f:174-191): x in [0, 40], y in [0, 2], z in [-4, 40] on
+    nx x ny x nz cells with one ghost layer (the reference runs 128 x 2 x
+    128), gamma 5/3, uniform gravity gz = -1/gm on cells and corners, a
+    convection zone / photosphere / corona temperature profile, a horizontal
+    flux sheet bx = sqrt(8 pi p rbeta) with 1/beta = rbetaf = 1/4 between
+    z = -2 and 0 in magnetohydrostatic balance (the discrete balance of
+    model.f), and a vz perturbation of amplitude 0.05 (pertub.f).
+    Boundaries: x and y symmetric (vx, by, bz odd at the x faces; vy, by odd
+    at the y faces); at the z faces vz and bz odd, vx, vy, bx, by even, and
+    ro, pr held at their initial ghost values (bdiniz, which for this
+    horizontally uniform state is the constant rule bdcnsz).  cfl_m safety
+    0.4, qav 3, tend 80, dtout 1."""
+    margin = 1
+    ix, jx, kx = nx + 2 * margin, ny + 2 * margin, nz + 2 * margin
+    gm = 5.0 / 3.0
+    pi = math.acos(-1.0)
+    ztr, zmax, zmin, xmax, ymax = 10.0, 40.0, -4.0, 40.0, 2.0
+
+    def axis(n, d0, iz):
+        dm = np.full(n, d0)
+        x = np.empty(n)
+        x[iz - 1] = dm[iz - 1] / 2.0
+        for i in range(iz + 1, n + 1):
+            x[i - 1] = x[i - 2] + dm[i - 2]
+        for i in range(iz - 1, 0, -1):
+            x[i - 1] = x[i] - dm[i - 1]
+        return x, dm
+
+    # dx0 = xmax/real(ix-margin*2): the count converted in single precision
+    x, _ = axis(ix, xmax / float(np.float32(ix - 2 * margin)), margin + 1)
+    y, _ = axis(jx, ymax / float(np.float32(jx - 2 * margin)), margin + 1)
+    dz0 = (zmax - zmin) / float(np.float32(kx - 2 * margin))
+    kzero = int(-zmin / dz0) + margin + 1
+    z, dzm0 = axis(kx, dz0, kzero)
+    g0 = -1.0 / gm
+    gzm0 = np.full(kx, g0)
+    wtr, tcor, tadg, zcnv = 0.5, 25.0, 2.0, 0.0
+    tem0 = (1.0 - tadg * (gm - 1.0) / gm * (z - zcnv) * 0.5 * (1 - np.tanh(z - zcnv))
+            + 0.5 * (tcor - 1.0) * (np.tanh((z - ztr) / wtr) + 1.0))
+    zf1, zf2, rbetaf = -2.0, -0.0, 1 / 4.0
+    af1 = (np.tanh((z - zf1) / 0.5) + 1.0) / 2
+    af2 = (-np.tanh((z - zf2) / 0.5) + 1.0) / 2
+    rbeta0 = rbetaf * af1 * af2
+    den0 = np.empty(kx)
+    pre0 = np.empty(kx)
+    kz = kzero - 1
+    den0[kz] = 1.0
+    pre0[kz] = 1.0 / gm * tem0[kz]
+    for k in range(kz + 1, kx):
+        h = 0.5 * gm * gzm0[k - 1] * dzm0[k - 1]
+        den0[k] = den0[k - 1] * ((1 + rbeta0[k - 1]) * tem0[k - 1] + h) / \
+            ((1 + rbeta0[k]) * tem0[k] - h)
+        pre0[k] = pre0[kz] * (den0[k] / den0[kz]) * (tem0[k] / tem0[kz])
+    for k in range(kz - 1, -1, -1):
+        h = 0.5 * gm * gzm0[k] * dzm0[k]
+        den0[k] = den0[k + 1] * ((1 + rbeta0[k + 1]) * tem0[k + 1] - h) / \
+            ((1 + rbeta0[k]) * tem0[k] + h)
+        pre0[k] = pre0[kz] * (den0[k] / den0[kz]) * (tem0[k] / tem0[kz])
+    if not (np.all(den0 > 0) and np.all(pre0 > 0)):
+        # the discrete balance needs tem0 > 0.5 gm |g| dz across the
+        # photosphere: about 48 cells or more along z
+        raise ValueError(f"nz = {nz} is too coarse for the stratification of md_efr")
+    bmx0 = np.sqrt(8 * pi * pre0 * rbeta0)
+    shape = (ix, jx, kx)
+    X = np.broadcast_to(x[:, None, None], shape)
+    Z = np.broadcast_to(z[None, None, :], shape)
+    # pertub.f: amp = 0.05 (single precision), xptb = 20, z between -2 and 0
+    amp, xptb, zptb1, zptb2, wptb = float(np.float32(0.05)), 20.0, -2.0, 0.0, 0.5
+    vz = (amp * np.cos(2 * pi * X / xptb) * 0.5
+          * (np.tanh((X + 0.75 * xptb) / wptb) - np.tanh((X - 0.75 * xptb) / wptb)) * 0.5
+          * (np.tanh((Z - zptb1) / wptb) - np.tanh((Z - zptb2) / wptb)))
+    f = {"ro": np.broadcast_to(den0, shape).copy(), "pr": np.broadcast_to(pre0, shape).copy(),
+         "vx": np.zeros(shape), "vy": np.zeros(shape), "vz": 0.0 + vz,
+         "bx": np.broadcast_to(bmx0, shape).copy(), "by": np.zeros(shape),
+         "bz": np.zeros(shape)}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    dz, _, dzm = grdrdy(z)
+    names = VARS["mlw_m_3d"]
+    odd = {0: ("vx", "by", "bz"), 1: ("vy", "by"), 2: ("vz", "bz")}
+    bc = []
+    for axis_ in range(3):
+        for face in (2 * axis_, 2 * axis_ + 1):
+            for v, name in enumerate(names):
+                if axis_ == 2 and name in ("ro", "pr"):
+                    base = den0 if name == "ro" else pre0
+                    bc.append((v, face, BD_CNS, float(base[0 if face == 4 else kx - 1])))
+                else:
+                    bc.append((v, face, BD_SPN if name in odd[axis_] else BD_SPP, 0.0))
+    grav = dict(gx=np.zeros(shape, order="F"), gxm=np.zeros(shape, order="F"),
+                gy=np.zeros(shape, order="F"), gym=np.zeros(shape, order="F"),
+                gz=np.full(shape, g0, order="F"), gzm=np.full(shape, g0, order="F"))
+    return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, gm, 3.0, bc, safety=0.4,
+                  dtmin=1e-10, tend=80.0, dtout=1.0, gravity=True,
+                  name=f"emerging_flux_{nx}x{ny}x{nz}", **grav)
