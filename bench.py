@@ -53,7 +53,7 @@ def parse():
                    help="skip the secondary 3-D and 1-D workloads")
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
-                            "gravity2d", "resistive2d", "spicule"],
+                            "gravity2d", "resistive2d", "gravity3d", "spicule"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
@@ -81,6 +81,15 @@ def profile_case(case, n):
         run.push(s["state"])
         run.start(nstop=200, tend=s["tend"], safety=s["safety"], dtmin=s["dtmin"])
         run.advance(200)
+        st = run.query()
+        run.close()
+        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+    elif case == "gravity3d":
+        s = setups.emerging_flux_3d(n, max(2, n // 4), n)
+        run = drivers.make_run(s)
+        run.push(s["state"])
+        run.start(nstop=3, safety=s["safety"], dtmin=s["dtmin"])
+        run.advance(3)
         st = run.query()
         run.close()
         out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
@@ -185,7 +194,7 @@ def extra_workloads(stream, exact=False):
         stream, exact, lambda m: setups.mhd_gravity_wave(m, solver="mlw_m3"), 512, 100, 256, 500,
         "gravity-wave model")
     out["emerging_flux_256x64x256_mlw_m_g"] = loop_3d(
-        stream, exact, setups.emerging_flux_3d, (256, 64, 256), 20, (64, 16, 64), 20,
+        stream, exact, setups.emerging_flux_3d, (256, 64, 256), 20, (96, 32, 96), 100,
         "emerging-flux model")
     out["reconnection_512^2_mlw_m_e"] = loop_2d(
         stream, exact, setups.magnetic_reconnection, 512, 100, 256, 500, "reconnection model")
@@ -285,6 +294,8 @@ def loop_3d(stream, exact, make, shape, iters, cpu_shape, cpu_steps, what):
     s = make(*shape)
     run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
     run.push(s["state"])
+    tile = run.autotune(2)
+    run.push(s["state"])
     run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
     run.advance(3)
     torch.cuda.synchronize()
@@ -304,8 +315,9 @@ def loop_3d(stream, exact, make, shape, iters, cpu_shape, cpu_steps, what):
     oracle.run_3d(c, cs, cpu_steps)
     el = time.perf_counter() - t0
     return {"zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
-            "step_kernels_ms": step_ms / 5, "bound": "fp64", "steps_done": int(st.nexec),
-            "merr": int(st.merr), "policy": "exact" if exact else "fast",
+            "step_kernels_ms": step_ms / 5, "tile": tile, "bound": "fp64",
+            "steps_done": int(st.nexec), "merr": int(st.merr),
+            "policy": "exact" if exact else "fast",
             "cpu_oracle": {"zone_updates_per_s": int(np.prod(cpu_shape)) * cpu_steps / el,
                            "cores": oracle.get_threads(), "kind": "port",
                            "sample": f"{cpu_steps} loop iterations of the "
