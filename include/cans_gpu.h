@@ -39,7 +39,7 @@ extern "C" {
 
 #define CANS_OK 0
 #define CANS_ERR_DTMIN 9001    /* dt < dtmin, as the reference merr=9001 */
-#define CANS_ERR_NONFINITE 9100
+#define CANS_ERR_NONFINITE 9100 /* a loop with stop_on_bad met a bad cell */
 #define CANS_ERR_CUDA 9200     /* CUDA failure; see cans_last_error()     */
 #define CANS_ERR_TIMEOUT 9300  /* a bounded device wait gave up           */
 #define CANS_ERR_ARG 9400      /* invalid argument                        */
@@ -410,6 +410,12 @@ typedef struct {
   /* 3-D mLW with gravity (mlw_m_g, cans3d/hdmlw/mlw_m_g.f): gx, gxm, gy, gym
    * above and gz, gzm here, ix*jx*kx each (the *m fields at the corners) */
   const double *gz, *gzm;
+  /* Loop-state check: the CFL of every step counts the thread blocks that
+   * met a cell with a non-positive density or pressure, or a non-finite value
+   * (cans_run_state.n_bad); the reference's scan just skips such a cell.
+   * stop_on_bad = 1 ends the loop at the start of the next iteration with
+   * merr = CANS_ERR_NONFINITE. */
+  int stop_on_bad;
 } cans_run_desc;
 
 typedef struct {
@@ -420,6 +426,8 @@ typedef struct {
   int done;                   /* 1 when tend/nstop/merr ended the loop      */
   int pause;                  /* 1 when an output time was crossed          */
   long long n_floor;          /* chkdav events since cans_run_start         */
+  long long n_bad;            /* blocks whose CFL met a bad cell (see
+                                 cans_run_desc.stop_on_bad) since the start */
 } cans_run_state;
 
 int cans_run_create(cans_run **h, const cans_run_desc *d);

@@ -51,7 +51,8 @@ def test_run_desc_layout_matches_header(tmp_path):
     assert fields == ["solver", "ix", "jx", "kx", "margin", "gm", "qav", "dx", "dxm", "dy",
                       "dym", "dz", "dzm", "exact", "tile", "stream", "bx", "bxm", "mu",
                       "mfdim", "gx", "gxm", "sc", "scm", "dsc", "dscm", "rr", "rrm", "drr",
-                      "drrm", "chkdav", "floor", "trq", "trq0", "seed", "gy", "gym", "et", "etm", "gz", "gzm"]
+                      "drrm", "chkdav", "floor", "trq", "trq0", "seed", "gy", "gym", "et", "etm", "gz", "gzm",
+                      "stop_on_bad"]
     import shutil
     import subprocess
     cc = shutil.which("gcc") or shutil.which("cc")
@@ -75,7 +76,7 @@ def test_run_state_layout_matches_header(tmp_path):
     import shutil
     import subprocess
     fields = [f[0] for f in capi.RunState._fields_]
-    assert fields[-1] == "n_floor"
+    assert fields[-1] == "n_bad"
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no host C compiler")

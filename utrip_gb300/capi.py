@@ -20,6 +20,7 @@ LIB_PATH = _build.LIBDIR / _build.LIBNAME
 
 CANS_OK = 0
 CANS_ERR_DTMIN = 9001
+CANS_ERR_NONFINITE = 9100
 CANS_ERR_CUDA = 9200
 CANS_ERR_ARG = 9400
 
@@ -519,13 +520,14 @@ class _Desc(C.Structure):
                 ("dscm", _dp), ("rr", _dp), ("rrm", _dp), ("drr", _dp), ("drrm", _dp),
                 ("chkdav", C.c_int), ("floor", C.c_double), ("trq", _dp),
                 ("trq0", C.c_double), ("seed", C.c_ulonglong), ("gy", _dp), ("gym", _dp),
-                ("et", _dp), ("etm", _dp), ("gz", _dp), ("gzm", _dp)]
+                ("et", _dp), ("etm", _dp), ("gz", _dp), ("gzm", _dp),
+                ("stop_on_bad", C.c_int)]
 
 
 class RunState(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("ns", C.c_longlong),
                 ("nexec", C.c_longlong), ("merr", C.c_int), ("done", C.c_int),
-                ("pause", C.c_int), ("n_floor", C.c_longlong)]
+                ("pause", C.c_int), ("n_floor", C.c_longlong), ("n_bad", C.c_longlong)]
 
 
 class Run:
@@ -534,7 +536,7 @@ class Run:
     def __init__(self, solver: int, grid: dict, gm: float, qav: float, margin: int = 1,
                  exact: bool = False, tile: int = -1, stream: int | None = None,
                  mu: float = 1.0, mfdim=(0, 0, 0), floor: float | None = None,
-                 torque: dict | None = None):
+                 torque: dict | None = None, stop_on_bad: bool = False):
         """grid holds dx, dxm (dy, dym, dz, dzm by dimension; bx, bxm in 1-D;
         the ten BG_PROFILES of mlw_m_bg for SOLVER_MLW_M_BG_1D).  1-D loops
         take floor (chkdav of ro and pr after each boundary fill) and, with
@@ -591,6 +593,7 @@ class Run:
                     setattr(d, k, arr(k))
         if floor is not None:
             d.chkdav, d.floor = 1, float(floor)
+        d.stop_on_bad = 1 if stop_on_bad else 0
         if torque is not None:
             d.trq = arr_of(self._keep, torque["trq"])
             d.trq0 = float(torque["trq0"])
@@ -641,7 +644,7 @@ class Run:
     def query(self) -> RunState:
         st = RunState()
         rc = self.lib.cans_run_query(self.h, C.byref(st))
-        if rc not in (CANS_OK, CANS_ERR_DTMIN):
+        if rc not in (CANS_OK, CANS_ERR_DTMIN, CANS_ERR_NONFINITE):
             _check(rc, "cans_run_query")
         return st
 

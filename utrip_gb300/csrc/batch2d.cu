@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(TX *TY / RPT, 1)
     tile_step<E, M3, TX, TY, RPT>(ctl->buf[ctl->cur], ctl->buf[ctl->cur ^ 1], G.ix,
                                   G.jx, G.ax, G.ay, G.ph, ctl->dt, ctl->safety,
                                   &ctl->cfl_bits, G.box, t % G.ntx, t / G.ntx,
-                                  G.ntx, G.nty, smem);
+                                  G.ntx, G.nty, smem, nullptr, nullptr, &ctl->nonfinite);
   }
 }
 
@@ -119,6 +119,7 @@ __global__ void k_frame_batch(const BatchGrid *__restrict__ grids, int margin,
   const long long total = nrow + (jx - 2LL * w) * 2LL * w;
   const FT gm(G.ph.gm), pi4i(G.ph.pi4i), safety(ctl->safety);
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;
   for (long long f = threadIdx.x; f < total; f += blockDim.x) {
     int i, j;
     if (f < nrow) {
@@ -149,7 +150,9 @@ __global__ void k_frame_batch(const BatchGrid *__restrict__ grids, int margin,
     const FT dtcfl = fmin_(FT(G.ax.d[i]), FT(G.ay.d[j])) / fsqrt(v2 + cs2 + ca2);
     const double dtq = (safety * dtcfl).v;
     if (dtq < dmin) dmin = dtq;
+    bad |= bad_cell(ro.v, pr.v, dtq);
   }
+  count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
   block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) finish_iteration(ctl);
@@ -248,6 +251,7 @@ struct cans_batch {
     BcTable bc{};
     Phys ph{};
     Axis ax, ay;
+    int stop_on_bad = 0;
   };
   std::vector<Grid> g;
   std::vector<BatchGrid> hgrids;
@@ -402,6 +406,7 @@ extern "C" int cans_batch_create(cans_batch **out, int ngrids,
     const cans_run_desc &d = descs[r];
     auto &G = b->g[r];
     G.ix = d.ix;
+    G.stop_on_bad = d.stop_on_bad ? 1 : 0;
     G.jx = d.jx;
     G.n = (size_t)d.ix * d.jx;
     G.ph = make_phys(d.gm, d.qav);
@@ -517,6 +522,9 @@ extern "C" int cans_batch_start(cans_batch *b, double t0, double tend, long long
     c.done = 0;
     c.pause = 0;
     c.frame_blocks_done = 0;
+    c.nonfinite = 0;
+    c.nfloor = 0;
+    c.stop_on_bad = G.stop_on_bad;
     c.cfl_bits = r4_1e20();
     BK(cudaMemcpyAsync(G.ctl, &c, sizeof c, cudaMemcpyHostToDevice, b->s));
     BK(launch_cfl2d_full(b->solver, b->exact != 0, G.buf[c.cur], G.ix, G.jx, G.ax, G.ay,
@@ -588,6 +596,8 @@ extern "C" int cans_batch_query(cans_batch *b, int grid, cans_run_state *st) {
   st->merr = c.merr;
   st->done = c.done;
   st->pause = c.pause;
+  st->n_floor = 0;
+  st->n_bad = c.nonfinite;
   return CANS_OK;
 }
 

@@ -79,7 +79,8 @@ struct Ctl {
   int pause;        // 1: an output time was crossed; host clears it
   int pause_on_output;
   unsigned int frame_blocks_done;  // last-block detection in the frame kernel
-  int nonfinite;    // count of non-finite / non-positive pressures seen
+  int nonfinite;    // blocks whose CFL saw a bad cell (below) since the start
+  int stop_on_bad;  // 1: a bad cell ends the loop with merr = 9100
   // Double-buffered state: a step reads buf[cur] and writes buf[cur^1]; the
   // frame kernel flips cur once the boundary fill and CFL are done, so the
   // same captured graph serves every iteration.
@@ -113,6 +114,11 @@ __device__ __forceinline__ double warp_min(double v) {
 // Start of a loop iteration (main.f:161-173): ns+=1, dt = CFL minimum held in
 // cfl_bits, the dtmin test, tp = t, t += dt.
 __device__ __forceinline__ void start_iteration(Ctl *ctl) {
+  if (ctl->stop_on_bad && ctl->nonfinite) {  // the state just written is bad
+    ctl->merr = 9100;  // CANS_ERR_NONFINITE
+    ctl->done = 1;
+    return;
+  }
   ctl->ns += 1;
   const unsigned long long bits = atomicAdd(&ctl->cfl_bits, 0ull);  // coherent read
   double dt = __longlong_as_double((long long)bits);
@@ -152,6 +158,19 @@ __device__ __forceinline__ void finish_iteration(Ctl *ctl) {
   }
   if (ctl->pause) return;
   start_iteration(ctl);
+}
+
+// A cell the CFL cannot use: density or pressure not positive, or a time
+// step that is not a number (a non-finite value anywhere in the cell).  The
+// reference scan skips such a cell (`dtq .lt. dt` is false for a NaN); here
+// it is also counted.
+__device__ __forceinline__ bool bad_cell(double ro, double pr, double dtq) {
+  return !(ro > 0.0) || !(pr > 0.0) || dtq != dtq;
+}
+// One count per block that saw a bad cell.  All threads of the block must
+// call it; tid is the linear thread index.
+__device__ __forceinline__ void count_bad_block(bool bad, int *count, int tid) {
+  if (__syncthreads_or(bad) && tid == 0) atomicAdd(count, 1);
 }
 
 // Block-wide minimum, valid on thread 0.  All threads of the block must call

@@ -1768,6 +1768,7 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
   c.pause = 0;
   c.frame_blocks_done = 0;
   c.nonfinite = 0;
+  c.stop_on_bad = h->d.stop_on_bad ? 1 : 0;
   c.nfloor = 0;
   c.cfl_bits = r4_1e20_bits();
   c.dtdif_bits = h->eta ? 0x7ff0000000000000ull : 0ull;
@@ -1838,6 +1839,7 @@ extern "C" int cans_run_query(cans_run *h, cans_run_state *st) {
   st->done = c.done;
   st->pause = c.pause;
   st->n_floor = (long long)c.nfloor;
+  st->n_bad = c.nonfinite;
   return c.merr ? c.merr : CANS_OK;
 }
 

@@ -239,13 +239,16 @@ __global__ void k_hlld_finish(Geo g, Axis ax, Axis ay, Axis az, Phys ph, Ctl *ct
   if (ctl->done | ctl->pause) return;
   const double *S = ctl->buf[ctl->cur ^ 1];
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n;
        c += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     cell_index(g, c, i, j, k);
     const double d = cfl3_cell<E>(S, g.n, c, i, j, k, ax, ay, az, ph, ctl->safety);
     if (d < dmin) dmin = d;
+    bad |= bad_cell(S[P3::RO * g.n + c], S[P3::PR * g.n + c], d);
   }
+  count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
   block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) {

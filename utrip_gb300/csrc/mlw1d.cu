@@ -158,7 +158,8 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   const int ix = p.ix, L = p.lmax;
   extern __shared__ double sm[];
   // layout: prim[2][5][L], U[5][L], FX[5][L], K[5][L], Q[L],
-  // (BG: SS[2][L] cell sources, SH[2][L] corner sources), slots[2][CS], red[32]
+  // (BG: SS[2][L] cell sources, SH[2][L] corner sources), slots[2][CS],
+  // bad[2][CS], red[32]
   double *prim = sm;
   double *U = prim + 2 * NV1 * L;
   double *FX = U + NV1 * L;
@@ -167,7 +168,8 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   double *SS = Q + L;
   double *SH = SS + (BG ? 2 * L : 0);
   double *slots = SH + (BG ? 2 * L : 0);
-  double *red = slots + 2 * CS;
+  double *bslots = slots + 2 * CS;  // per block: 1 if its CFL saw a bad cell
+  double *red = bslots + 2 * CS;
   const double *bg = p.bg;
   const size_t nx = (size_t)ix;
   __shared__ double s_dt, s_t, s_tp, s_pending;
@@ -209,9 +211,12 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   __syncthreads();
 
   // CFL of the own cells (cfl_m.f:53-60) reduced over the cluster into
-  // slots[par] of block 0; returns the minimum after a cluster barrier.
-  auto cluster_cfl = [&](int buf, int par) -> double {
+  // slots[par] of block 0; returns the minimum after a cluster barrier, and
+  // in any_bad whether a cell of any block had a non-positive density or
+  // pressure or a time step that is not a number (counted in ctl->nonfinite).
+  auto cluster_cfl = [&](int buf, int par, bool &any_bad) -> double {
     double dmin = __longlong_as_double(0x7ff0000000000000LL);
+    bool bad = false;
     const FT safety(p.ctl ? p.ctl->safety : 1.0), pi4c(p.ph.pi4i);
     for (int l = 1 + tid; l <= nl - 2; l += NT) {
       const int g = lo - 1 + l;
@@ -223,29 +228,37 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
       const FT dtcfl = FT(ax.d[g]) / (fabs_(vx) + fsqrt(cs2 + ca2));
       const double dtq = (safety * dtcfl).v;
       if (dtq < dmin || dmin != dmin) dmin = dtq;
+      bad |= bad_cell(ro.v, pr.v, dtq);
     }
     dmin = warp_min(dmin);
     if ((tid & 31) == 0) red[tid >> 5] = dmin;
-    __syncthreads();
+    const int blk_bad = __syncthreads_or(bad);
     if (tid == 0) {
       double x = red[0];
       for (int w = 1; w < (NT + 31) / 32; w++) x = (red[w] < x || x != x) ? red[w] : x;
       double *dst = cluster.map_shared_rank(slots, 0);
       dst[par * CS + r] = x;
+      double *dstb = cluster.map_shared_rank(bslots, 0);
+      dstb[par * CS + r] = blk_bad ? 1.0 : 0.0;
+      if (blk_bad && p.ctl) atomicAdd(&p.ctl->nonfinite, 1);
     }
     cluster.sync();
     double *src = cluster.map_shared_rank(slots, 0);
+    double *srcb = cluster.map_shared_rank(bslots, 0);
     double m = (double)1.e20f;  // the reference's starting minimum
+    any_bad = false;
     for (int k = 0; k < CS; k++) {
       const double x = src[par * CS + k];
       if (x < m) m = x;
+      any_bad |= srcb[par * CS + k] != 0.0;
     }
     return m;
   };
 
   int par = 0;
   if (!p.fixed && p.start) {
-    const double dt0 = cluster_cfl(cur, par);
+    bool bad0;
+    const double dt0 = cluster_cfl(cur, par, bad0);
     par ^= 1;
     if (tid == 0) {  // first iteration always starts (do-while loop)
       s_ns += 1;
@@ -567,7 +580,8 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
     }
     // ---- CFL of the own cells, reduced over the cluster; its cluster barrier
     // also publishes every block's final cells for the halo exchange ---------
-    const double dtn = cluster_cfl(nb, par);
+    bool badn;
+    const double dtn = cluster_cfl(nb, par, badn);
     par ^= 1;
     if (tid < NV1) {
       if (r > 0) {
@@ -591,6 +605,9 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
       }
       s_pending = dtn;  // CFL of the state just written, for a later resume
       if (!(s_ns < p.ctl->nstop && s_t < p.ctl->tend)) {
+        s_done = 1;
+      } else if (!s_pause && p.ctl->stop_on_bad && badn) {
+        s_merr = 9100;  // CANS_ERR_NONFINITE: the state just written has a bad cell
         s_done = 1;
       } else if (!s_pause) {
         s_ns += 1;
@@ -680,7 +697,7 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                             : (exact ? k_mlw1d<true, false> : k_mlw1d<false, false>);
   const size_t per_cell = (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 4 : 0);
   // shared memory of the largest block the grid can have (16 blocks)
-  const size_t smem_probe = sizeof(double) * (per_cell * ((ix - 2) / 16 + 4) + 32 + 32);
+  const size_t smem_probe = sizeof(double) * (per_cell * ((ix - 2) / 16 + 4) + 64 + 32);
   const int CS = cluster_for(ix, cluster_max(kern, smem_probe));
   Run1D p{};
   p.S = S; p.bx = bx; p.bxm = bxm; p.ax = ax; p.ph = ph; p.bc = bc; p.ctl = ctl;
@@ -706,7 +723,7 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
   for (int v = 0; v < NV1; v++)
     for (int f = 0; f < 2; f++)
       if (bc.kind[v][f] == BD_PER) p.bnd_local = 0;
-  const size_t smem = sizeof(double) * (per_cell * p.lmax + 2 * CS + 32);
+  const size_t smem = sizeof(double) * (per_cell * p.lmax + 4 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);

@@ -29,7 +29,8 @@ __global__ void __launch_bounds__(TX *TY / RPT, 1)
     cfl = &ctl->cfl_bits;
   }
   tile_step<E, M3, TX, TY, RPT>(A, B, ix, jx, ax, ay, ph, dt, safety, cfl, box,
-                                blockIdx.x, blockIdx.y, gridDim.x, gridDim.y, smem);
+                                blockIdx.x, blockIdx.y, gridDim.x, gridDim.y, smem,
+                                nullptr, nullptr, ctl ? &ctl->nonfinite : nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -161,6 +162,7 @@ __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
   const long long inner_rows = jx - 2LL * w;
   const long long total = nrow + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;
   const FT gm(ph.gm), pi4i(ph.pi4i);
   for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
        f < total; f += (long long)gridDim.x * blockDim.x) {
@@ -194,7 +196,9 @@ __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
     const FT dtcfl = fmin_(FT(ax.d[i]), FT(ay.d[j])) / fsqrt(v2 + cs2 + ca2);
     const double dtq = (FT(ctl->safety) * dtcfl).v;
     if (dtq < dmin) dmin = dtq;
+    bad |= bad_cell(ro.v, pr.v, dtq);
   }
+  count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
   block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) {

@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(ETX *ETY / ERPT, 1)
   }
   tile_step<E, M3, ETX, ETY, ERPT, G, true>(A, B, ix, jx, ax, ay, ph, dt, safety, cfl,
                                             box, blockIdx.x, blockIdx.y, gridDim.x,
-                                            gridDim.y, smem, grav, res);
+                                            gridDim.y, smem, grav, res,
+                                            ctl ? &ctl->nonfinite : nullptr);
 }
 
 template <bool E, bool M3, bool G>

@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(TX *TY / RPT, 1)
   }
   tile_step<E, M3, TX, TY, RPT, true>(A, B, ix, jx, ax, ay, ph, dt, safety, cfl, box,
                                       blockIdx.x, blockIdx.y, gridDim.x, gridDim.y,
-                                      smem, grav);
+                                      smem, grav, nullptr,
+                                      ctl ? &ctl->nonfinite : nullptr);
 }
 
 namespace {

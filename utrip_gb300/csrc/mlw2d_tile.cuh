@@ -120,7 +120,7 @@ __device__ __forceinline__ void tile_step(
     unsigned long long *cfl_out, const Box3 &box, int tile_x, int tile_y,
     int ntiles_x, int ntiles_y, double *smem,
     const double *__restrict__ grav = nullptr,
-    const double *__restrict__ res = nullptr) {
+    const double *__restrict__ res = nullptr, int *bad_out = nullptr) {
   using T = Tile<TX, TY, M3, RPT, G>;
   using C = CellSlots<M3>;
   using K = CornerSlots<M3>;
@@ -401,6 +401,7 @@ __device__ __forceinline__ void tile_step(
 
   // ---------------- phase 3: full step on the tile's own cells -------------
   double dmin = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+  bool bad = false;  // a cell of the new state the CFL cannot use
   const int lx = tid % TX + 1;
 #pragma unroll 1
   for (int rr = 0; rr < RPT; rr++) {
@@ -591,6 +592,7 @@ __device__ __forceinline__ void tile_step(
         const FT dtcfl = fmin_(FT(ax.d[gi]), FT(ay.d[gj])) / fsqrt(v2 + cs2 + ca2);
         const double dtq = (FT(safety) * dtcfl).v;
         if (dtq < dmin) dmin = dtq;
+        bad |= bad_cell(ro.v, pr.v, dtq);
       } else {
         // min over cells of min(dx,dy)/sqrt(S) is 1/sqrt(max of
         // S*max(1/dx^2, 1/dy^2)): no division or root per cell.  dmin holds
@@ -599,6 +601,7 @@ __device__ __forceinline__ void tile_step(
         const double s = v2.v + fma(gm.v, pr.v, pi4i.v * b2.v) * rinv;
         const double kk = s * fmax(dxi.v * dxi.v, dyi.v * dyi.v);
         if (-kk < dmin) dmin = -kk;
+        bad |= bad_cell(ro.v, pr.v, kk);
       }
     }
   }
@@ -619,6 +622,7 @@ __device__ __forceinline__ void tile_step(
     }
   }
   if (cfl_out != nullptr) {
+    if (bad_out != nullptr) count_bad_block(bad, bad_out, tid);
     if constexpr (E) {
       block_min_to(cfl_out, dmin, sred, tid, T::NT);
     } else {

@@ -399,6 +399,7 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
   __syncthreads();
 
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;  // a cell of the new state the CFL cannot use
   const FT qav(ph.qav);
 
   for (int k = kb; k <= ke; k++) {
@@ -644,6 +645,7 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
           const FT dmn = fmin_(fmin_(FT(ax.d[gi]), FT(ay.d[gj])), FT(az.d[k]));
           const double dtq = (FT(ctl->safety) * (dmn / fsqrt(v2 + cs2 + ca2))).v;
           if (dtq < dmin) dmin = dtq;
+          bad |= bad_cell(ro.v, pr.v, dtq);
         } else {
           // largest S*max(1/dx^2,1/dy^2,1/dz^2) gives the smallest dt; dmin
           // holds minus that key (see the block reduction below)
@@ -651,6 +653,7 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
           const double s = v2.v + fma(gm.v, pr.v, ph.pi4i_cfl * b2.v) * rinv;
           const double kk = s * fmax(fmax(dxi.v * dxi.v, dyi.v * dyi.v), dzi.v * dzi.v);
           if (-kk < dmin) dmin = -kk;
+          bad |= bad_cell(ro.v, pr.v, kk);
         }
       }
       save_prev(k);
@@ -676,6 +679,7 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     __syncthreads();
   }
   if (ctl != nullptr) {
+    count_bad_block(bad, &ctl->nonfinite, tid);
     if constexpr (E) {
       block_min_to(&ctl->cfl_bits, dmin, sred, tid, T::NT);
     } else {
@@ -827,6 +831,7 @@ __global__ void k_frame3d(int ix, int jx, int kx, Axis ax, Axis ay, Axis az,
   const long long total = 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
                           2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;
   for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < total;
        f += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -834,7 +839,9 @@ __global__ void k_frame3d(int ix, int jx, int kx, Axis ax, Axis ay, Axis az,
     const size_t g = (size_t)i + (size_t)j * ix + (size_t)k * plane;
     const double d = cfl3_cell<E>(S, n, g, i, j, k, ax, ay, az, ph, ctl->safety);
     if (d < dmin) dmin = d;
+    bad |= bad_cell(S[P3::RO * n + g], S[P3::PR * n + g], d);
   }
+  count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
   block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) {

@@ -370,6 +370,7 @@ __global__ void __launch_bounds__(kRoeThreads)
   }
   const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;  // a cell of the new state the CFL cannot use
   if (c < g.n) {
     int i, j, k;
     cell_index(g, c, i, j, k);
@@ -409,9 +410,13 @@ __global__ void __launch_bounds__(kRoeThreads)
         dmin = cfl3_cell<E>(B, g.n, c, i, j, k, ax, ay, az, ph, ctl->safety);
       else
         dmin = cfl2_cell<E>(B, g.n, c, i, j, ax, ay, ph, ctl->safety);
+      bad = bad_cell(p[P3::RO], p[P3::PR], dmin);
     }
   }
-  if (ctl) block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
+  if (ctl) {
+    count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
+    block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
+  }
 }
 
 template <bool E, int ND>

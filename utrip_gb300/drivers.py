@@ -166,7 +166,8 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             capi.release(state[0])
 
 
-def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True) -> capi.Run:
+def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True,
+             stop_on_bad=False) -> capi.Run:
     """Run handle for a set-up; a set-up with a "floor" gets the chkdav
     option and one with a "trq" profile the torque source (each can be
     switched off here)."""
@@ -176,7 +177,8 @@ def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True) 
         tq = {"trq": setup["trq"], "trq0": setup["trq0"], "seed": setup.get("seed", 0)}
     run = capi.Run(setup["solver_id"], setup, setup["gm"], setup["qav"], setup["margin"],
                    exact=exact, tile=tile, stream=stream, mu=setup.get("mu", 1.0),
-                   mfdim=setup.get("mfdim", (0, 0, 0)), floor=fl, torque=tq)
+                   mfdim=setup.get("mfdim", (0, 0, 0)), floor=fl, torque=tq,
+                   stop_on_bad=stop_on_bad)
     run.set_bc_program(setup["bc"])
     return run
 
