@@ -410,7 +410,7 @@ typedef struct {
   /* 3-D mLW with gravity (mlw_m_g, cans3d/hdmlw/mlw_m_g.f): gx, gxm, gy, gym
    * above and gz, gzm here, ix*jx*kx each (the *m fields at the corners) */
   const double *gz, *gzm;
-  /* Loop-state check: the CFL of every step counts the thread blocks that
+  /* Loop-state check: the CFL of every step counts the warps that
    * met a cell with a non-positive density or pressure, or a non-finite value
    * (cans_run_state.n_bad); the reference's scan just skips such a cell.
    * stop_on_bad = 1 ends the loop at the start of the next iteration with
@@ -426,7 +426,7 @@ typedef struct {
   int done;                   /* 1 when tend/nstop/merr ended the loop      */
   int pause;                  /* 1 when an output time was crossed          */
   long long n_floor;          /* chkdav events since cans_run_start         */
-  long long n_bad;            /* blocks whose CFL met a bad cell (see
+  long long n_bad;            /* warps whose CFL met a bad cell (see
                                  cans_run_desc.stop_on_bad) since the start */
 } cans_run_state;
 

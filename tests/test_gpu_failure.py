@@ -4,7 +4,7 @@ pressure in one interior cell), and the GPU only does arithmetic on it.
 
 The reference's CFL scan skips a cell whose time step is not a number
 (cfl_m.f: `if (dtq .lt. dt)`), and its loop carries on.  The resident loop
-does the same by default and counts the thread blocks whose CFL met a cell
+does the same by default and counts the warps whose CFL met a cell
 with a non-positive density or pressure or a non-finite value
 (cans_run_state.n_bad); with stop_on_bad the loop ends at the start of the
 next iteration with merr = CANS_ERR_NONFINITE."""

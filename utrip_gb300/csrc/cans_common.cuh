@@ -79,7 +79,7 @@ struct Ctl {
   int pause;        // 1: an output time was crossed; host clears it
   int pause_on_output;
   unsigned int frame_blocks_done;  // last-block detection in the frame kernel
-  int nonfinite;    // blocks whose CFL saw a bad cell (below) since the start
+  int nonfinite;    // warps whose CFL saw a bad cell (below) since the start
   int stop_on_bad;  // 1: a bad cell ends the loop with merr = 9100
   // Double-buffered state: a step reads buf[cur] and writes buf[cur^1]; the
   // frame kernel flips cur once the boundary fill and CFL are done, so the
@@ -164,13 +164,20 @@ __device__ __forceinline__ void finish_iteration(Ctl *ctl) {
 // step that is not a number (a non-finite value anywhere in the cell).  The
 // reference scan skips such a cell (`dtq .lt. dt` is false for a NaN); here
 // it is also counted.
+// The tests are integer compares of the bit patterns, kept off the FP64
+// pipe that bounds the step kernels: x > 0 (NaN excluded, +inf included)
+// is 0 < bits <= bits(+inf) as a signed integer, and x is a NaN when its
+// magnitude bits exceed those of +inf.
 __device__ __forceinline__ bool bad_cell(double ro, double pr, double dtq) {
-  return !(ro > 0.0) || !(pr > 0.0) || dtq != dtq;
+  constexpr long long kInf = 0x7ff0000000000000LL;
+  const long long a = __double_as_longlong(ro), b = __double_as_longlong(pr);
+  const long long c = __double_as_longlong(dtq) & 0x7fffffffffffffffLL;
+  return a <= 0 || a > kInf || b <= 0 || b > kInf || c > kInf;
 }
-// One count per block that saw a bad cell.  All threads of the block must
-// call it; tid is the linear thread index.
+// One count per warp that saw a bad cell (a vote, no block barrier).  All
+// 32 threads of the warp must call it; tid is the linear thread index.
 __device__ __forceinline__ void count_bad_block(bool bad, int *count, int tid) {
-  if (__syncthreads_or(bad) && tid == 0) atomicAdd(count, 1);
+  if (__ballot_sync(0xffffffffu, bad) != 0u && (tid & 31) == 0) atomicAdd(count, 1);
 }
 
 // Block-wide minimum, valid on thread 0.  All threads of the block must call
