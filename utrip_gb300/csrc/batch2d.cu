@@ -502,6 +502,7 @@ extern "C" int cans_batch_pull(cans_batch *b, int grid, double *const *host) {
 
 extern "C" int cans_batch_start(cans_batch *b, double t0, double tend, long long nstop,
                                 double safety, double dtmin) {
+  NvtxRange nvtx("cans_batch_start");
   if (!b) return CANS_ERR_ARG;
   for (int r = 0; r < b->ngrids; r++) {
     auto &G = b->g[r];
@@ -539,6 +540,7 @@ extern "C" int cans_batch_start(cans_batch *b, double t0, double tend, long long
 }
 
 extern "C" int cans_batch_advance(cans_batch *b, int iters, int use_graph) {
+  NvtxRange nvtx("cans_batch_advance");
   if (!b || iters < 0) return CANS_ERR_ARG;
   if (!use_graph) {
     for (int k = 0; k < iters; k++) {

@@ -6,8 +6,18 @@
 #include <stdint.h>
 
 #include "cans_common.cuh"
+#include <nvtx3/nvToolsExt.h>
 
 namespace cans {
+
+// NVTX range over one host API call (a no-op unless a profiler such as nsys
+// or ncu --nvtx is attached); the names are the C-ABI entry points.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Device copies of the per-axis metric arrays of the reference step
 // (cans2d/hdmlw/mlw_m3.f:70-86): spacing d/dm, their inverses di/dim and

@@ -263,6 +263,7 @@ int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
            double gm, const double *dx, const double *dxm, int ix,
            const double *dy, const double *dym, int jx,
            const double *const *grav = nullptr, const double *const *eta = nullptr) {
+  NvtxRange nvtx("mLW 2-D drop-in step");
   if (ix < 3 || jx < 3) return CANS_ERR_ARG;
   if (grav)
     for (int k = 0; k < 4; k++)
@@ -315,6 +316,7 @@ int step2d(int solver, double *const *arrs, int nvar, double dt, double qav,
 int cfl2d(int solver, double *dt, double safety, double dtmin, int *merr,
           double gm, const double *const *arrs, int nvar, const double *dx,
           int ix, const double *dy, int jx, const double *et = nullptr) {
+  NvtxRange nvtx("2-D drop-in CFL");
   if (ix < 1 || jx < 1) return CANS_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
@@ -914,6 +916,7 @@ int step3d(double *const *arrs, double dt, double qav, double gm, const double *
            const double *dxm, int nx, const double *dy, const double *dym, int ny,
            const double *dz, const double *dzm, int nz,
            const double *const *grav = nullptr) {
+  NvtxRange nvtx("mLW 3-D drop-in step");
   if (nx < 3 || ny < 3 || nz < 3) return CANS_ERR_ARG;
   if (grav)
     for (int k = 0; k < 6; k++)
@@ -1515,6 +1518,7 @@ unsigned long long r4_1e20_bits() {
 }  // namespace
 
 extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
+  NvtxRange nvtx("cans_run_create");
   if (!out || !d) return CANS_ERR_ARG;
   const int nvar = solver_nvar(d->solver);
   if (nvar == 0 || d->margin < 1) return CANS_ERR_ARG;
@@ -1715,6 +1719,7 @@ extern "C" int cans_run_set_bc(cans_run *h, int var, int face, int kind,
 }
 
 extern "C" int cans_run_push(cans_run *h, double *const *host) {
+  NvtxRange nvtx("cans_run_push");
   if (!h || !host) return CANS_ERR_ARG;
   int rc = read_ctl(h);  // learn which buffer is current
   if (rc) return rc;
@@ -1726,6 +1731,7 @@ extern "C" int cans_run_push(cans_run *h, double *const *host) {
 }
 
 extern "C" int cans_run_pull(cans_run *h, double *const *host) {
+  NvtxRange nvtx("cans_run_pull");
   if (!h || !host) return CANS_ERR_ARG;
   int rc = read_ctl(h);  // learn which buffer is current
   if (rc) return rc;
@@ -1749,6 +1755,7 @@ extern "C" int cans_run_device_state(cans_run *h, double **dev) {
 extern "C" int cans_run_start(cans_run *h, double t0, double tend,
                               long long nstop, double safety, double dtmin,
                               double dtout, int pause_on_output) {
+  NvtxRange nvtx("cans_run_start");
   if (!h) return CANS_ERR_ARG;
   int rc = read_ctl(h);
   if (rc) return rc;
@@ -1789,6 +1796,7 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
 }
 
 extern "C" int cans_run_advance(cans_run *h, int iters) {
+  NvtxRange nvtx("cans_run_advance");
   if (!h || iters < 0) return CANS_ERR_ARG;
   if (iters == 0) return CANS_OK;
   if (h->ndim == 1) {
@@ -1855,6 +1863,7 @@ extern "C" int cans_run_resume(cans_run *h) {
 }
 
 extern "C" int cans_run_step(cans_run *h, const double *dt, int apply_bc) {
+  NvtxRange nvtx("cans_run_step");
   if (!h || !dt) return CANS_ERR_ARG;
   int rc = read_ctl(h);
   if (rc) return rc;
@@ -1877,6 +1886,7 @@ extern "C" int cans_run_step(cans_run *h, const double *dt, int apply_bc) {
 }
 
 extern "C" int cans_run_cfl(cans_run *h, double safety, double *dt) {
+  NvtxRange nvtx("cans_run_cfl");
   if (!h || !dt) return CANS_ERR_ARG;
   int rc = read_ctl(h);
   if (rc) return rc;
@@ -1943,6 +1953,7 @@ extern "C" int cans_run_profile(cans_run *h, int iters, double *step_ms,
 }
 
 extern "C" int cans_run_autotune(cans_run *h, int trial_steps, int *tile) {
+  NvtxRange nvtx("cans_run_autotune");
   if (!h || trial_steps < 1) return CANS_ERR_ARG;
   if (h->ndim == 1) {  // a single configuration
     if (tile) *tile = 0;
@@ -2185,6 +2196,7 @@ int adj_reverse(AdjRun &r, long long a, long long b, int slot, int free_snaps) {
 
 extern "C" int cans_run_record_dts(cans_run *h, long long nsteps, double safety,
                                    double *dts, double *J) {
+  NvtxRange nvtx("cans_run_record_dts");
   if (!h || nsteps < 1 || !dts || !adj_supported(h)) return CANS_ERR_ARG;
   int rc = read_ctl(h);
   if (rc) return rc;
@@ -2216,6 +2228,7 @@ extern "C" int cans_run_record_dts(cans_run *h, long long nsteps, double safety,
 
 extern "C" int cans_run_objective(cans_run *h, long long nsteps, const double *dts,
                                   double *J) {
+  NvtxRange nvtx("cans_run_objective");
   if (!h || nsteps < 1 || !dts || !J || !adj_supported(h)) return CANS_ERR_ARG;
   int rc = read_ctl(h);
   if (rc) return rc;
@@ -2235,6 +2248,7 @@ extern "C" int cans_run_objective(cans_run *h, long long nsteps, const double *d
 extern "C" int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts,
                                 int nsnap, double *J, double *const *grad,
                                 long long *nfwd) {
+  NvtxRange nvtx("cans_run_adjoint");
   if (!h || nsteps < 1 || !dts || nsnap < 2 || !adj_supported(h)) return CANS_ERR_ARG;
   if (nsteps > (1LL << 20)) return CANS_ERR_ARG;
   int rc = read_ctl(h);
