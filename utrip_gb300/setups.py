@@ -109,12 +109,13 @@ def _pack(solver, x, dx, dxm, y, dy, dym, fields, gm, qav, bc, **extra):
     return d
 
 
-def orszag_tang(n: int = 512, solver: str = "mlw_m3"):
+def orszag_tang(n: int = 512, solver: str = "mlw_m3", margin: int | None = None):
     """2-D Orszag-Tang vortex: [0, 2pi]^2 periodic, gamma=5/3,
     rho=25/(36 pi), p=5/(12 pi), v=(-sin y, sin x), B=(-sin y, sin 2x)/sqrt(4pi)
-    in Heaviside-Lorentz units, i.e. (-sin y, sin 2x) in CANS units."""
+    in Heaviside-Lorentz units, i.e. (-sin y, sin 2x) in CANS units.  margin
+    defaults to the solver's."""
     L = 2.0 * math.pi
-    m = MARGIN_2D[solver]
+    m = margin or MARGIN_2D[solver]
     x, dx, dxm = uniform_axis(n, L, m)
     y, dy, dym = uniform_axis(n, L, m)
     X, Y = np.meshgrid(x, y, indexing="ij")
@@ -129,7 +130,7 @@ def orszag_tang(n: int = 512, solver: str = "mlw_m3"):
     f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, m)
     nvar = len(VARS[solver])
     return _pack(solver, x, dx, dxm, y, dy, dym, f, 5.0 / 3.0, 3.0,
-                 _bc_all(nvar, BD_PER, BD_PER), safety=0.4, dtmin=1e-10,
+                 _bc_all(nvar, BD_PER, BD_PER), safety=0.4, dtmin=1e-10, margin=m,
                  tend=math.pi / 2.0, name=f"orszag_tang_{n}")
 
 
