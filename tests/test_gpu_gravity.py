@@ -91,3 +91,16 @@ def test_fast_policy_100_steps_within_tolerance(gpu, oracle_lib):
     drivers.run_resident(s, got, 100, exact=False)
     for k, a, b in zip(s["names"], got, ref):
         assert rel_linf(a, b) < 1e-10, (k, rel_linf(a, b))
+
+
+def test_emerging_flux_2d_loop_exact_bitwise(gpu, oracle_lib):
+    """cans2d/md_efr: the Parker-unstable flux sheet at 64 x 128 (the
+    reference's size), 100 iterations of cfl_m -> mlw_m_g -> bnd with the
+    held y faces."""
+    s = setups.emerging_flux_2d(64, 128)
+    ref = setups.copy_state(s)
+    t, ns, merr, _ = oracle.run_2d(s, ref, 100)
+    got = setups.copy_state(s)
+    out = drivers.run_resident(s, got, 100, exact=True)
+    assert out == (t, ns, merr, ns)
+    assert_same(s["names"], got, ref, "emerging flux 2-D")

@@ -964,3 +964,16 @@ def test_emerging_flux_setup_follows_the_model(oracle_lib):
     st = setups.copy_state(s)
     t, ns, merr, _ = oracle_lib.run_3d(s, st, 10)
     assert ns == 10 and merr == 0 and all(np.all(np.isfinite(a)) for a in st)
+
+
+def test_emerging_flux_2d_setup_matches_the_3d_column(oracle_lib):
+    """cans2d/md_efr and cans3d/md_efr build the same vertical structure
+    (y vertical in 2-D, z in 3-D) from the same recurrence."""
+    s2 = setups.emerging_flux_2d(16, 64)
+    s3 = setups.emerging_flux_3d(16, 2, 64)
+    assert np.array_equal(s2["y"], s3["z"])
+    assert np.array_equal(s2["state"][0][0, :], s3["state"][0][0, 0, :])
+    assert np.array_equal(s2["state"][4][0, :], s3["state"][5][0, 0, :])  # bx
+    st = setups.copy_state(s2)
+    t, ns, merr, _ = oracle_lib.run_2d(s2, st, 10)
+    assert ns == 10 and merr == 0 and all(np.all(np.isfinite(a)) for a in st)

@@ -841,44 +841,15 @@ def magnetic_reconnection(n: int = 128):
     return s
 
 
-def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
-    """The 3-D emerging-flux model of cans3d/md_efr/hdmlw (model.f, pertub.f,
-    bnd.f, main.f:174-191): x in [0, 40], y in [0, 2], z in [-4, 40] on
-    nx x ny x nz cells with one ghost layer (the reference runs 128 x 2 x
-    128), gamma 5/3, uniform gravity gz = -1/gm on cells and corners, a
-    convection zone / photosphere / corona temperature profile, a horizontal
-    flux sheet bx = sqrt(8 pi p rbeta) with 1/beta = rbetaf = 1/4 between
-    z = -2 and 0 in magnetohydrostatic balance (the discrete balance of
-    model.f), and a vz perturbation of amplitude 0.05 (pertub.f).
-    Boundaries: x and y symmetric (vx, by, bz odd at the x faces; vy, by odd
-    at the y faces); at the z faces vz and bz odd, vx, vy, bx, by even, and
-    ro, pr held at their initial ghost values (bdiniz, which for this
-    horizontally uniform state is the constant rule bdcnsz).  cfl_m safety
-    0.4, qav 3, tend 80, dtout 1."""
-    margin = 1
-    ix, jx, kx = nx + 2 * margin, ny + 2 * margin, nz + 2 * margin
-    gm = 5.0 / 3.0
+def _efr_column(z, dzm0, kzero, gm, nz):
+    """The vertical structure of the md_efr models (model.f): temperature
+    tem0 of the convection zone, photosphere and corona, the flux-sheet
+    profile rbeta0 = 1/beta, and density, pressure and field bmx0 in the
+    discrete magnetohydrostatic balance built outward from cell kzero."""
     pi = math.acos(-1.0)
-    ztr, zmax, zmin, xmax, ymax = 10.0, 40.0, -4.0, 40.0, 2.0
-
-    def axis(n, d0, iz):
-        dm = np.full(n, d0)
-        x = np.empty(n)
-        x[iz - 1] = dm[iz - 1] / 2.0
-        for i in range(iz + 1, n + 1):
-            x[i - 1] = x[i - 2] + dm[i - 2]
-        for i in range(iz - 1, 0, -1):
-            x[i - 1] = x[i] - dm[i - 1]
-        return x, dm
-
-    # dx0 = xmax/real(ix-margin*2): the count converted in single precision
-    x, _ = axis(ix, xmax / float(np.float32(ix - 2 * margin)), margin + 1)
-    y, _ = axis(jx, ymax / float(np.float32(jx - 2 * margin)), margin + 1)
-    dz0 = (zmax - zmin) / float(np.float32(kx - 2 * margin))
-    kzero = int(-zmin / dz0) + margin + 1
-    z, dzm0 = axis(kx, dz0, kzero)
+    ztr = 10.0
     g0 = -1.0 / gm
-    gzm0 = np.full(kx, g0)
+    gzm0 = np.full(z.size, g0)
     wtr, tcor, tadg, zcnv = 0.5, 25.0, 2.0, 0.0
     tem0 = (1.0 - tadg * (gm - 1.0) / gm * (z - zcnv) * 0.5 * (1 - np.tanh(z - zcnv))
             + 0.5 * (tcor - 1.0) * (np.tanh((z - ztr) / wtr) + 1.0))
@@ -886,6 +857,7 @@ def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
     af1 = (np.tanh((z - zf1) / 0.5) + 1.0) / 2
     af2 = (-np.tanh((z - zf2) / 0.5) + 1.0) / 2
     rbeta0 = rbetaf * af1 * af2
+    kx = z.size
     den0 = np.empty(kx)
     pre0 = np.empty(kx)
     kz = kzero - 1
@@ -903,19 +875,110 @@ def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
         pre0[k] = pre0[kz] * (den0[k] / den0[kz]) * (tem0[k] / tem0[kz])
     if not (np.all(den0 > 0) and np.all(pre0 > 0)):
         # the discrete balance needs tem0 > 0.5 gm |g| dz across the
-        # photosphere: about 48 cells or more along z
-        raise ValueError(f"nz = {nz} is too coarse for the stratification of md_efr")
+        # photosphere: about 48 cells or more along the vertical
+        raise ValueError(f"{nz} cells are too coarse for the stratification of md_efr")
     bmx0 = np.sqrt(8 * pi * pre0 * rbeta0)
+    return den0, pre0, bmx0
+
+
+def _efr_perturbation(X, Z):
+    """pertub.f: amp = 0.05 (single precision), xptb = 20, between z = -2
+    and 0, on the vertical velocity."""
+    pi = math.acos(-1.0)
+    amp, xptb, zptb1, zptb2, wptb = float(np.float32(0.05)), 20.0, -2.0, 0.0, 0.5
+    return (amp * np.cos(2 * pi * X / xptb) * 0.5
+            * (np.tanh((X + 0.75 * xptb) / wptb) - np.tanh((X - 0.75 * xptb) / wptb)) * 0.5
+            * (np.tanh((Z - zptb1) / wptb) - np.tanh((Z - zptb2) / wptb)))
+
+
+def _efr_axis(n, d0, iz):
+    dm = np.full(n, d0)
+    x = np.empty(n)
+    x[iz - 1] = dm[iz - 1] / 2.0
+    for i in range(iz + 1, n + 1):
+        x[i - 1] = x[i - 2] + dm[i - 2]
+    for i in range(iz - 1, 0, -1):
+        x[i - 1] = x[i] - dm[i - 1]
+    return x, dm
+
+
+def emerging_flux_2d(nx: int = 64, ny: int = 128):
+    """The 2-D emerging-flux model of cans2d/md_efr/hdmlw (model.f, pertub.f,
+    bnd.f, main.f:160-183): the vertical structure of the 3-D model along y
+    in [-4, 40], x in [0, 40], nx x ny cells (the reference runs 64 x 128)
+    with one ghost layer, gravity gy = -1/gm, the flux sheet bx, a vy
+    perturbation, az from bbtoaa.  Boundaries: x symmetric (vx, by odd); at
+    the y faces vy, by odd, vx, bx, az even, and ro, pr held at their initial
+    ghost values (bdiniy, the constant rule bdcnsy for this horizontally
+    uniform state).  mlw_m_g, cfl_m safety 0.4, qav 3, tend 80."""
+    margin = 1
+    ix, jx = nx + 2 * margin, ny + 2 * margin
+    gm = 5.0 / 3.0
+    ymax, ymin, xmax = 40.0, -4.0, 40.0
+    x, _ = _efr_axis(ix, xmax / float(ix - 2 * margin), margin + 1)
+    dy0 = (ymax - ymin) / float(jx - 2 * margin)
+    jzero = int(-ymin / dy0) + margin + 1
+    y, dym0 = _efr_axis(jx, dy0, jzero)
+    den0, pre0, bmx0 = _efr_column(y, dym0, jzero, gm, ny)
+    shape = (ix, jx)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    f = {"ro": np.broadcast_to(den0, shape).copy(), "pr": np.broadcast_to(pre0, shape).copy(),
+         "vx": np.zeros(shape), "vy": 0.0 + _efr_perturbation(X, Y),
+         "bx": np.broadcast_to(bmx0, shape).copy(), "by": np.zeros(shape)}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, margin)
+    names = VARS["mlw_m"]
+    bc = []
+    for face in (0, 1):
+        for v, name in enumerate(names):
+            bc.append((v, face, BD_SPN if name in ("vx", "by") else BD_SPP, 0.0))
+    for face in (2, 3):
+        for v, name in enumerate(names):
+            if name in ("ro", "pr"):
+                base = den0 if name == "ro" else pre0
+                bc.append((v, face, BD_CNS, float(base[0 if face == 2 else jx - 1])))
+            else:
+                bc.append((v, face, BD_SPN if name in ("vy", "by") else BD_SPP, 0.0))
+    g0 = -1.0 / gm
+    grav = dict(gx=np.zeros(shape, order="F"), gxm=np.zeros(shape, order="F"),
+                gy=np.full(shape, g0, order="F"), gym=np.full(shape, g0, order="F"))
+    return _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+                 tend=80.0, dtout=1.0, gravity=True, name=f"emerging_flux_{nx}x{ny}",
+                 **grav)
+
+
+def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
+    """The 3-D emerging-flux model of cans3d/md_efr/hdmlw (model.f, pertub.f,
+    bnd.f, main.f:174-191): x in [0, 40], y in [0, 2], z in [-4, 40] on
+    nx x ny x nz cells with one ghost layer (the reference runs 128 x 2 x
+    128), gamma 5/3, uniform gravity gz = -1/gm on cells and corners, a
+    convection zone / photosphere / corona temperature profile, a horizontal
+    flux sheet bx = sqrt(8 pi p rbeta) with 1/beta = rbetaf = 1/4 between
+    z = -2 and 0 in magnetohydrostatic balance (the discrete balance of
+    model.f), and a vz perturbation of amplitude 0.05 (pertub.f).
+    Boundaries: x and y symmetric (vx, by, bz odd at the x faces; vy, by odd
+    at the y faces); at the z faces vz and bz odd, vx, vy, bx, by even, and
+    ro, pr held at their initial ghost values (bdiniz, which for this
+    horizontally uniform state is the constant rule bdcnsz).  cfl_m safety
+    0.4, qav 3, tend 80, dtout 1."""
+    margin = 1
+    ix, jx, kx = nx + 2 * margin, ny + 2 * margin, nz + 2 * margin
+    gm = 5.0 / 3.0
+    zmax, zmin, xmax, ymax = 40.0, -4.0, 40.0, 2.0
+    # dx0 = xmax/real(ix-margin*2): the count converted in single precision
+    x, _ = _efr_axis(ix, xmax / float(np.float32(ix - 2 * margin)), margin + 1)
+    y, _ = _efr_axis(jx, ymax / float(np.float32(jx - 2 * margin)), margin + 1)
+    dz0 = (zmax - zmin) / float(np.float32(kx - 2 * margin))
+    kzero = int(-zmin / dz0) + margin + 1
+    z, dzm0 = _efr_axis(kx, dz0, kzero)
+    den0, pre0, bmx0 = _efr_column(z, dzm0, kzero, gm, nz)
+    g0 = -1.0 / gm
     shape = (ix, jx, kx)
     X = np.broadcast_to(x[:, None, None], shape)
     Z = np.broadcast_to(z[None, None, :], shape)
-    # pertub.f: amp = 0.05 (single precision), xptb = 20, z between -2 and 0
-    amp, xptb, zptb1, zptb2, wptb = float(np.float32(0.05)), 20.0, -2.0, 0.0, 0.5
-    vz = (amp * np.cos(2 * pi * X / xptb) * 0.5
-          * (np.tanh((X + 0.75 * xptb) / wptb) - np.tanh((X - 0.75 * xptb) / wptb)) * 0.5
-          * (np.tanh((Z - zptb1) / wptb) - np.tanh((Z - zptb2) / wptb)))
     f = {"ro": np.broadcast_to(den0, shape).copy(), "pr": np.broadcast_to(pre0, shape).copy(),
-         "vx": np.zeros(shape), "vy": np.zeros(shape), "vz": 0.0 + vz,
+         "vx": np.zeros(shape), "vy": np.zeros(shape), "vz": 0.0 + _efr_perturbation(X, Z),
          "bx": np.broadcast_to(bmx0, shape).copy(), "by": np.zeros(shape),
          "bz": np.zeros(shape)}
     dx, _, dxm = grdrdy(x)
