@@ -88,7 +88,7 @@ def test_rejects_missing_fields(gpu):
         drivers.make_run(roe)
 
 
-@pytest.mark.parametrize("tile", [0, 1, 2])
+@pytest.mark.parametrize("tile", [0, 1, 2, 3])
 def test_emerging_flux_loop_exact_bitwise(gpu, oracle_lib, tile):
     """md_efr at 48 x 2 x 48 (the reference's thin y axis): 40 iterations of
     cfl_m -> mlw_m_g -> bnd on the device."""

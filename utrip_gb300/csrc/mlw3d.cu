@@ -715,16 +715,22 @@ cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
 }  // namespace
 
 // mlw_m_g: the gravity rings do not fit beside a 16 x 16 tile (222 KB), so
-// the step with gravity runs 16 x 8 tiles (143 KB; z chunks of 64 or 32) or
-// 16 x 12 tiles (202 KB; chunks of 64).
-int mlw3d_g_tile_count() { return 3; }
+// the step with gravity runs 16 x 8 tiles (143 KB, 6 warps; z chunks of 64
+// or 32), 16 x 12 tiles (202 KB, 8 warps) or 24 x 8 tiles (208 KB, 9 warps;
+// chunks of 32).
+int mlw3d_g_tile_count() { return 4; }
 
 cudaError_t launch_mlw3d_g(bool exact, int tile, const double *A, double *B, int ix,
                            int jx, int kx, const Axis &ax, const Axis &ay, const Axis &az,
                            const Phys &ph, const double *grav, double dt, Ctl *ctl,
                            Box3 box, cudaStream_t s) {
   if (ix < 3 || jx < 3 || kx < 3 || grav == nullptr) return cudaErrorInvalidValue;
-  const int kchunk = (tile == 1) ? 32 : 64;
+  const int kchunk = (tile == 1 || tile == 3) ? 32 : 64;
+  if (tile == 3)
+    return exact ? launch3<true, 24, 8, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box,
+                                              kchunk, s, grav)
+                 : launch3<false, 24, 8, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl,
+                                               box, kchunk, s, grav);
   if (tile == 2)
     return exact ? launch3<true, 16, 12, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box,
                                                kchunk, s, grav)
