@@ -306,7 +306,10 @@ def apply_bc_program_1d(state, program, margin, grid):
 
 
 def run_1d(setup, state, nstop, tend=None, safety=None, t0=0.0):
-    """The 1-D model-package loop (cans1d/md_mhdshktb/hdmlw/main.f:139-199)."""
+    """The 1-D model-package loop (cans1d/md_mhdshktb/hdmlw/main.f:139-199),
+    with the set-up's step: mlw_m, roe_m or mlw_m_bg (the md_mhdwind loop,
+    cans1d/md_mhdwind/hdmlw/main.f:160-176; the spicule loop with its torque
+    and floor is run_spicule)."""
     tend = setup.get("tend", 1e30) if tend is None else tend
     safety = setup["safety"] if safety is None else safety
     bx, bxm = setup["bx"], setup["bxm"]
@@ -320,6 +323,8 @@ def run_1d(setup, state, nstop, tend=None, safety=None, t0=0.0):
         dts.append(dt)
         if setup["solver"] == "roe_m_1d":
             roe_m_1d(*state, bx, bxm, dt, setup["gm"], setup["dx"])
+        elif setup["solver"] == "mlw_m_bg_1d":
+            step_bg(setup, state, dt)
         else:
             mlw_m_1d(*state, bx, bxm, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"])
         apply_bc_program_1d(state, setup["bc"], setup["margin"], setup)

@@ -204,3 +204,17 @@ def test_run_spicule_files_and_restart(gpu, oracle_lib, tmp_path):
     assert_bitwise(["ro", "pr", "vx", "vy", "by"], c["state"], a["state"], "restart")
     t0 = dac.dacopnr(tmp_path / "c" / "t.dac", 0).records[0]
     assert t0 == dac.dacopnr(tmp_path / "b" / "t.dac", 0).records[-1]
+
+
+def test_mhd_wind_loop_exact_bitwise(gpu, oracle_lib):
+    """cans1d/md_mhdwind: the rotating magnetised wind on the stretched grid
+    (1024 cells, held base values, free outer face), 2000 iterations of
+    cfl_m -> mlw_m_bg -> bnd in one cluster launch, against the oracle."""
+    s = setups.mhd_wind_1d(1024)
+    ref = setups.copy_state(s)
+    t, ns, merr, _ = oracle.run_1d(s, ref, 2000)
+    got = setups.copy_state(s)
+    out = drivers.run_resident(s, got, 2000, exact=True)
+    assert out == (t, ns, merr, ns)
+    for k, a, b in zip(s["names"], got, ref):
+        assert np.array_equal(a, b), k

@@ -977,3 +977,20 @@ def test_emerging_flux_2d_setup_matches_the_3d_column(oracle_lib):
     st = setups.copy_state(s2)
     t, ns, merr, _ = oracle_lib.run_2d(s2, st, 10)
     assert ns == 10 and merr == 0 and all(np.all(np.isfinite(a)) for a in st)
+
+
+def test_mhd_wind_setup_follows_the_model(oracle_lib):
+    """md_mhdwind/hdmlw/model.f: the grid stretches by 1.006 per cell from
+    x = 6, bx ~ 1/x^2 with bx^2/(8 pi p) = 0.1 at the base, sc = 1/bx, and the
+    base holds ro = 1, pr = 1/gm, vy = 0.15."""
+    s = setups.mhd_wind_1d(256)
+    x, bx = s["x"], s["bx"]
+    assert np.allclose(s["dxm"][2:-2] / s["dxm"][1:-3], 1.006, rtol=1e-9)
+    assert np.allclose(bx * x * x, bx[1] * x[1] * x[1], rtol=1e-13)
+    assert np.array_equal(s["sc"], 1.0 / bx)
+    g = dict(zip(s["names"], s["state"]))
+    assert abs(bx[1] ** 2 / (8 * math.pi * g["pr"][1]) - 0.1) < 1e-7
+    assert g["ro"][0] == 1.0 and g["pr"][0] == 1.0 / 1.2
+    st = setups.copy_state(s)
+    t, ns, merr, _ = oracle_lib.run_1d(s, st, 50)
+    assert ns == 50 and merr == 0 and st[3][0] == 0.15

@@ -1001,3 +1001,79 @@ def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
     return _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, gm, 3.0, bc, safety=0.4,
                   dtmin=1e-10, tend=80.0, dtout=1.0, gravity=True,
                   name=f"emerging_flux_{nx}x{ny}x{nz}", **grav)
+
+
+def mhd_wind_1d(nx: int = 1024):
+    """The magnetised stellar-wind model of cans1d/md_mhdwind/hdmlw (model.f,
+    bnd.f, bndsc.f, main.f:70-80, 160-176), the Weber-Davis problem: a
+    rotating star of radius rstar = 6, gamma 1.2, point-mass gravity
+    gx = -(1/gm) rstar^2/x^2, a radial field bx ~ 1/x^2 with 1/beta = 0.1 at
+    the base, a flux tube of cross section sc = 1/bx, distance from the axis
+    rr = x, an exponential atmosphere to x = 12 and a tenuous ISM beyond, on a
+    grid stretched by 1.006 per cell (nx cells from x = 6, dx0 = 10/nx).
+    Boundaries: at the base ro = 1, pr = 1/gm and the rotation vy = vstar =
+    0.15 held, vx and by free; the outer face free.  mlw_m_bg with qav 2,
+    cfl_m safety 1.0, tend 2000 (the wind settles to a steady state)."""
+    margin = 1
+    ix = nx + 2 * margin
+    gm, rstar, vstar = 1.2, 6.0, 0.15
+    pi = math.acos(-1.0)
+    dx0 = 10.0 / float(np.float32(ix - 2 * margin))
+    ratx = 1.006
+    dxm0 = np.full(ix, dx0)
+    for i in range(1, ix):
+        dxm0[i] = dxm0[i - 1] * ratx
+    izero = margin + 1
+    x = np.empty(ix)
+    x[izero - 1] = rstar + dxm0[izero - 1] / 2.0
+    for i in range(izero + 1, ix + 1):
+        x[i - 1] = x[i - 2] + dxm0[i - 2]
+    for i in range(izero - 1, 0, -1):
+        x[i - 1] = x[i] - dxm0[i - 1]
+    gx = -1 / gm * (rstar * rstar) / (x * x)
+    xh = x + 0.5 * dxm0
+    gxm = -1 / gm * (rstar * rstar) / (xh * xh)
+    rr = x.copy()
+    rrm = x + dxm0 / 2
+    rhs = 2.0 * rstar
+    roism, teism = 1.0e-8, 1.0e-2
+    ro = (np.exp(rstar * (rstar / x - 1)) * (1 - np.tanh((x - rhs) / 0.5)) / 2
+          + roism * (1 + np.tanh((x - rhs) / 0.5)) / 2)
+    te = teism + (1 - teism) * (1 - (x - rhs) / (x[ix - margin - 1] - rhs))
+    te = np.where(x <= rhs, 1.0, te)
+    pr = ro * te / gm
+    betai = float(np.float32(0.1))
+    bx0 = math.sqrt(betai * pr[izero - 1] * 8 * pi)
+    x0 = x[izero - 1]
+    bx = bx0 * (x0 * x0) / (x * x)
+    bxm = bx0 * (x0 * x0) / ((x + dxm0 / 2) * (x + dxm0 / 2))
+    sc = 1.0 / bx
+    scm = 1.0 / bxm
+    dx, _, dxm = grdrdy(x)
+    f = {"ro": ro, "pr": pr, "vx": np.zeros(ix), "vy": np.zeros(ix), "by": np.zeros(ix)}
+    names = VARS["mlw_m_bg_1d"]
+    # bnd.f: base ro = 1, pr = 1/gm, vy = vstar held, vx and by free; outer free
+    held = {"ro": 1.0, "pr": 1.0 / gm, "vy": vstar}
+    bc = []
+    for v, name in enumerate(names):
+        bc.append((v, 0, BD_CNS, held[name]) if name in held else (v, 0, BD_FRE, 0.0))
+        bc.append((v, 1, BD_FRE, 0.0))
+    for v, face, kind, q0 in bc:
+        a = f[names[v]]
+        if kind == BD_CNS:
+            a[:margin] = q0
+        else:
+            bd_host_1d(kind, face, margin, a)
+    dsc, dscm = scrdy(sc, scm, dx, dxm)
+    drr, drrm = scrdy(rr, rrm, dx, dxm)
+    # bndsc.f: dsc free at both faces, dscm free at the outer face
+    bd_host_1d(BD_FRE, 0, margin, dsc)
+    bd_host_1d(BD_FRE, 1, margin, dsc)
+    bd_host_1d(BD_FRE, 1, margin, dscm)
+    state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in names]
+    prof = dict(gx=gx, gxm=gxm, sc=sc, scm=scm, dsc=dsc, dscm=dscm, rr=rr, rrm=rrm,
+                drr=drr, drrm=drrm)
+    return dict(solver="mlw_m_bg_1d", solver_id=6, names=names, x=x, dx=dx, dxm=dxm,
+                bx=bx, bxm=bxm, state=state, gm=gm, qav=2.0, margin=margin, bc=bc,
+                safety=1.0, dtmin=1e-10, tend=2000.0, dtout=100.0, vstar=vstar,
+                name=f"mhd_wind_{nx}", **prof)
