@@ -120,3 +120,45 @@ def test_linear_wave_phase_speed_gpu(gpu, oracle_lib, kind, var):
     assert merr == 0 and t >= 0.25
     got = phase_speed(s, st, var, t)
     assert abs(got - c) < 2e-3 * c, (kind, got, c)
+
+
+def friedrichs_ratios(s, state, t):
+    """Outermost pressure peak along rays from the pulse centre (every 15
+    degrees) divided by the fast-mode distance c_f(theta) t, theta the angle
+    to the field: the fronts of cans2d/md_mhdwave trace the Friedrichs
+    diagram of mhdwave_analytic.pro."""
+    from scipy.interpolate import RegularGridInterpolator
+    gm = s["gm"]
+    cs2 = 1.0                                        # gm p / rho
+    ca2 = (8 * math.pi / gm * float(np.float32(0.5))) / (4 * math.pi)
+    f = RegularGridInterpolator((s["x"], s["y"]), state[1] - 1 / gm)
+    out = []
+    for deg in range(0, 180, 15):
+        phi = math.radians(deg)
+        r = np.linspace(0.05, 0.45, 1601)
+        v = f(np.stack([r * math.cos(phi), r * math.sin(phi)], axis=1))
+        peaks = [k for k in range(1, r.size - 1)
+                 if v[k] >= v[k - 1] and v[k] >= v[k + 1] and v[k] > 0.2 * v.max()]
+        c = math.cos(phi - s["thini"])
+        cf = math.sqrt(0.5 * (cs2 + ca2 + math.sqrt((cs2 + ca2) ** 2 - 4 * cs2 * ca2 * c * c)))
+        out.append(r[peaks[-1]] / (cf * t))
+    return np.array(out)
+
+
+def test_friedrichs_diagram_oracle(oracle_lib):
+    pytest.importorskip("scipy")
+    s = setups.mhd_wave_2d(128)
+    st = setups.copy_state(s)
+    t, ns, merr, _ = oracle_lib.run_2d(s, st, 10 ** 6, tend=0.25)
+    ratios = friedrichs_ratios(s, st, t)
+    assert np.all(np.abs(ratios - 1) < 0.05), ratios
+
+
+@pytest.mark.gpu
+def test_friedrichs_diagram_gpu(gpu):
+    pytest.importorskip("scipy")
+    s = setups.mhd_wave_2d(256)
+    st = setups.copy_state(s)
+    t, ns, merr, _ = drivers.run_resident(s, st, 10 ** 6, tend=0.25)
+    ratios = friedrichs_ratios(s, st, t)
+    assert np.all(np.abs(ratios - 1) < 0.03), ratios

@@ -1077,3 +1077,48 @@ def mhd_wind_1d(nx: int = 1024):
                 bx=bx, bxm=bxm, state=state, gm=gm, qav=2.0, margin=margin, bc=bc,
                 safety=1.0, dtmin=1e-10, tend=2000.0, dtout=100.0, vstar=vstar,
                 name=f"mhd_wind_{nx}", **prof)
+
+
+def mhd_wave_2d(n: int = 64):
+    """The MHD wave model of cans2d/md_mhdwave/hdmlw (model.f, bnd.f,
+    main.f:155-171): a Gaussian pressure pulse (relative amplitude 0.1,
+    width 0.02) at the centre of [-0.5, 0.5]^2 (n x n cells, one ghost
+    layer), rho = 1, gamma 5/3, c_s = 1, a uniform field at 60 degrees to x
+    with 1/beta = 0.5 (c_a^2 = 0.6), free boundaries, mlw_m with qav 3, cfl_m
+    safety 0.4, tend 1.  Its fronts trace the Friedrichs diagram of the
+    reference's mhdwave_analytic.pro."""
+    margin = 1
+    ix = jx = n + 2 * margin
+    gm = 5.0 / 3.0
+    pi = math.acos(-1.0)
+
+    def axis(nn):
+        d0 = 1.0 / float(nn - 2 * margin)
+        dm = np.full(nn, d0)
+        iz = nn // 2 + 1
+        x = np.empty(nn)
+        x[iz - 1] = dm[iz - 1] / 2.0
+        for i in range(iz + 1, nn + 1):
+            x[i - 1] = x[i - 2] + dm[i - 2]
+        for i in range(iz - 1, 0, -1):
+            x[i - 1] = x[i] - dm[i - 1]
+        return x
+
+    x, y = axis(ix), axis(jx)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    betai = float(np.float32(0.5))
+    b0 = math.sqrt(8 * pi / gm * betai)
+    thini = float(np.float32(60.0)) / float(np.float32(180.0)) * pi
+    wexp = float(np.float32(0.02))
+    amp = 0.1
+    ss = np.sqrt(X * X + Y * Y)
+    f = {"ro": np.ones(X.shape), "pr": 1 / gm + amp / gm * np.exp(-((ss / wexp) ** 2)),
+         "bx": np.full(X.shape, b0 * math.cos(thini)),
+         "by": np.full(X.shape, b0 * math.sin(thini)),
+         "vx": np.zeros(X.shape), "vy": np.zeros(X.shape)}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, margin)
+    bc = _bc_all(len(VARS["mlw_m"]), BD_FRE, BD_FRE)
+    return _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+                 tend=1.0, margin=margin, thini=thini, name=f"mhd_wave_{n}")
