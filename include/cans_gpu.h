@@ -231,6 +231,13 @@ int cans_roe_m_1d(double *ro, double *pr, double *vx, double *vy, double *by,
  * raised to it and vx set to zero there; n_events receives the count */
 int cans_chkdav(int *n_events, double *da, double *vx, const double *floor,
                 const int *ix);
+/* replaces subroutine chkdav (cans2d/common/chkdav.f:2 and
+ * cans3d/common/chkdav.f:2): da below floor is raised to it and the velocity
+ * components set to zero there; n_events receives the count */
+int cans_chkdav_2d(int *n_events, double *da, double *vx, double *vy,
+                   const double *floor, const int *ix, const int *jx);
+int cans_chkdav_3d(int *n_events, double *da, double *vx, double *vy, double *vz,
+                   const double *floor, const int *ix, const int *jx, const int *kx);
 /* Ghost-cell fill, 1-D (cans1d/bc/bd*.f:2). */
 int cans_bdperx_1d(const int *margin0, const int *margin1, double *qq, const int *ix); /* bdperx.f:2 */
 int cans_bdsppx_1d(const int *mbnd, const int *margin, double *qq, const int *ix);    /* bdsppx.f:2 */
@@ -389,9 +396,9 @@ typedef struct {
    * mlw_m_g / mlw_m3_g (ix*jx doubles each; gxm, gym at the cell corners):
    * when gx is set the run takes the step with gravity. */
   const double *gx, *gxm, *sc, *scm, *dsc, *dscm, *rr, *rrm, *drr, *drrm;
-  /* 1-D loops: chkdav (cans1d/common/chkdav.f:2) of ro, then pr, with
-   * `floor` after every boundary fill when chkdav = 1; the events are
-   * counted in cans_run_state.n_floor */
+  /* chkdav (cans1d/common/chkdav.f:2 and its 2-D / 3-D twins) of ro, then
+   * pr, with `floor` after every boundary fill when chkdav = 1; the events
+   * are counted in cans_run_state.n_floor */
   int chkdav;
   double floor;
   /* mlw_m_bg loops: the random torque source of the spicule model

@@ -328,6 +328,8 @@ def run_1d(setup, state, nstop, tend=None, safety=None, t0=0.0):
         else:
             mlw_m_1d(*state, bx, bxm, dt, setup["qav"], setup["gm"], setup["dx"], setup["dxm"])
         apply_bc_program_1d(state, setup["bc"], setup["margin"], setup)
+        if setup.get("floor") is not None:
+            chkdav_state(setup, state)
         if not (ns < nstop and t < tend):
             return t, ns, 0, dts
 
@@ -343,6 +345,31 @@ def mlw_m_bg(ro, pr, vx, vy, by, bx, bxm, dt, qav, gm, gx, gxm, sc, dsc, scm, ds
 def chkdav(da, vx, floor):
     """cans1d/common/chkdav.f:2; returns n_events."""
     return int(load().oracle_chkdav(P(da), P(vx), floor, da.size))
+
+
+def chkdav_nd(da, vels, floor):
+    """cans2d/common/chkdav.f:33-44 and cans3d/common/chkdav.f: da below floor
+    is raised to it and the velocity components set to zero there (a
+    pointwise rule, so the array order of the scan does not matter); returns
+    n_events."""
+    mask = da < floor
+    da[mask] = floor
+    for v in vels:
+        v[mask] = 0.0
+    return int(np.count_nonzero(mask))
+
+
+def chkdav_state(setup, state):
+    """chkdav of ro, then pr, as the model packages call it after bnd
+    (cans2d/md_efr/hdmlw/main.f:183-185); velocities vx, vy (and vz in 3-D,
+    vx alone in 1-D)."""
+    floor = setup["floor"]
+    names = setup["names"]
+    if state[0].ndim == 1:
+        return (chkdav(state[0], state[2], floor) + chkdav(state[1], state[2], floor))
+    vel = [state[names.index(k)] for k in (("vx", "vy", "vz") if state[0].ndim == 3
+                                            else ("vx", "vy"))]
+    return chkdav_nd(state[0], vel, floor) + chkdav_nd(state[1], vel, floor)
 
 
 def torque_uniform(seed, ns, g, ix):
@@ -512,6 +539,8 @@ def run_3d(setup, state, nstop, tend=None, safety=None, t0=0.0):
         dts.append(dt)
         step_3d(setup, state, dt)
         apply_bc_program_3d(state, setup["bc"], setup["margin"], setup)
+        if setup.get("floor") is not None:
+            chkdav_state(setup, state)
         if not (ns < nstop and t < tend):
             return t, ns, 0, dts
 
@@ -532,5 +561,7 @@ def run_2d(setup, state, nstop, tend=None, safety=None, t0=0.0):
         dts.append(dt)
         step_2d(setup, state, dt)
         apply_bc_program(state, setup["bc"], setup["margin"], setup)
+        if setup.get("floor") is not None:
+            chkdav_state(setup, state)
         if not (ns < nstop and t < tend):
             return t, ns, 0, dts

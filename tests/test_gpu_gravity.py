@@ -104,3 +104,75 @@ def test_emerging_flux_2d_loop_exact_bitwise(gpu, oracle_lib):
     out = drivers.run_resident(s, got, 100, exact=True)
     assert out == (t, ns, merr, ns)
     assert_same(s["names"], got, ref, "emerging flux 2-D")
+
+
+def test_parker_instability_loop_exact_bitwise(gpu, oracle_lib):
+    """cans2d/md_parkerinst at the reference's 64 x 128: 100 iterations of
+    cfl_m -> mlw_m_g -> bnd -> chkdav (ro, pr; floor 1e-9) on the device."""
+    s = setups.parker_instability(64, 128)
+    ref = setups.copy_state(s)
+    t, ns, merr, _ = oracle.run_2d(s, ref, 100)
+    got = setups.copy_state(s)
+    out = drivers.run_resident(s, got, 100, exact=True)
+    assert out == (t, ns, merr, ns)
+    assert_same(s["names"], got, ref, "Parker instability")
+
+
+def oracle_loop_with_events(s, state, nstop):
+    """oracle.run_2d with the chkdav events counted."""
+    events, ns, t = 0, 0, 0.0
+    while True:
+        ns += 1
+        dt, _ = oracle.cfl_2d(s, state, s["safety"])
+        t += dt
+        oracle.step_2d(s, state, dt)
+        oracle.apply_bc_program(state, s["bc"], s["margin"], s)
+        events += oracle.chkdav_state(s, state)
+        if not (ns < nstop and t < s["tend"]):
+            return t, ns, events
+
+
+def test_chkdav_floor_events_exact(gpu, oracle_lib):
+    """A floor above the coronal density of the Parker set-up makes chkdav
+    act in every iteration: the resident loop floors ro and pr and zeroes
+    vx, vy where the oracle does, and counts the same events."""
+    s = dict(setups.parker_instability(48, 96), floor=0.012)
+    ref = setups.copy_state(s)
+    t, ns, events = oracle_loop_with_events(s, ref, 40)
+    assert events > 0
+    got = setups.copy_state(s)
+    run = drivers.make_run(s, exact=True)
+    try:
+        run.push(got)
+        run.start(tend=s["tend"], nstop=40, safety=s["safety"], dtmin=s["dtmin"])
+        run.advance(41)
+        st = run.query()
+        run.pull(got)
+    finally:
+        run.close()
+    assert (st.t, st.ns, st.merr) == (t, ns, 0)
+    assert st.n_floor == events
+    assert_same(s["names"], got, ref, "chkdav loop")
+
+
+@pytest.mark.parametrize("resident", [False, True])
+def test_chkdav_drop_in_2d_3d(gpu, oracle_lib, resident):
+    rng = np.random.default_rng(3)
+    for shape in ((23, 17), (9, 11, 13)):
+        da = np.asfortranarray(rng.random(shape))
+        vel = [np.asfortranarray(rng.standard_normal(shape)) for _ in shape]
+        ref = [da.copy(order="F")] + [v.copy(order="F") for v in vel]
+        n_ref = oracle.chkdav_nd(ref[0], ref[1:], 0.3)
+        got = [da] + vel
+        if resident:
+            capi.register(got)
+        try:
+            fn = capi.chkdav_3d if len(shape) == 3 else capi.chkdav_2d
+            n = fn(*got, 0.3)
+        finally:
+            if resident:
+                capi.pull(got[0])
+                capi.release(got[0])
+        assert n == n_ref > 0
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)

@@ -114,6 +114,8 @@ def load() -> C.CDLL:
     sig["cans_cfl_m_1d"] = (i, [_dp, _dp, _dp, _ip, _dp, _dp] + [_dp] * 5 + [_dp, _ip])
     sig["cans_mlw_m_bg"] = (i, [_dp] * 7 + [_dp, _dp, _dp] + [_dp] * 12 + [_ip])
     sig["cans_chkdav"] = (i, [_ip, _dp, _dp, _dp, _ip])
+    sig["cans_chkdav_2d"] = (i, [_ip, _dp, _dp, _dp, _dp, _ip, _ip])
+    sig["cans_chkdav_3d"] = (i, [_ip, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _ip])
     sig["cans_roe_m_1d"] = (i, [_dp] * 7 + [_dp, _dp, _dp, _ip])
     sig["cans_bdperx_1d"] = (i, [_ip, _ip, _dp, _ip])
     for fam in ("spp", "spn", "smp", "smn", "fre"):
@@ -363,6 +365,24 @@ def roe_m_1d(ro, pr, vx, vy, by, bx, bxm, dt, gm, dx):
     return _check(load().cans_roe_m_1d(*[_ptr(a) for a in (ro, pr, vx, vy, by, bx, bxm)],
                                        _dref(dt), _dref(gm), _ptr(dx), _iref(ro.size)),
                   "roe_m_1d")
+
+
+def chkdav_2d(da, vx, vy, floor):
+    """cans2d/common/chkdav.f:2 -- floor da, zero vx, vy there; returns n_events."""
+    n = C.c_int(0)
+    ix, jx = da.shape
+    _check(load().cans_chkdav_2d(C.byref(n), _ptr(da), _ptr(vx), _ptr(vy), _dref(floor),
+                                 _iref(ix), _iref(jx)), "chkdav_2d")
+    return n.value
+
+
+def chkdav_3d(da, vx, vy, vz, floor):
+    """cans3d/common/chkdav.f:2 -- floor da, zero vx, vy, vz there."""
+    n = C.c_int(0)
+    ix, jx, kx = da.shape
+    _check(load().cans_chkdav_3d(C.byref(n), _ptr(da), _ptr(vx), _ptr(vy), _ptr(vz),
+                                 _dref(floor), _iref(ix), _iref(jx), _iref(kx)), "chkdav_3d")
+    return n.value
 
 
 def chkdav(da, vx, floor):

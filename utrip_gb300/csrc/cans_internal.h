@@ -92,7 +92,7 @@ cudaError_t launch_bc2d(int nvar, double *S, int ix, int jx, const Axis &ax,
 cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
                            int jx, const Axis &ax, const Axis &ay,
                            const Phys &ph, int margin, Ctl *ctl,
-                           cudaStream_t s);
+                           cudaStream_t s, int all = 0);
 
 // ---- 3-D ------------------------------------------------------------------
 // mlw_m 3-D on 8 arrays (ro,pr,vx,vy,vz,bx,by,bz) of ix*jx*kx doubles.
@@ -116,7 +116,7 @@ cudaError_t launch_bc3d(int nvar, double *S, int ix, int jx, int kx,
                         const BcTable &bc, const Ctl *ctl, cudaStream_t s);
 cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
                            const Axis &ay, const Axis &az, const Phys &ph,
-                           int margin, Ctl *ctl, cudaStream_t s);
+                           int margin, Ctl *ctl, cudaStream_t s, int all = 0);
 
 // ---- 3-D Roe-MUSCL (roe_m) -------------------------------------------------
 // One two-stage step on 8 arrays (ro,pr,vx,vy,vz,bx,by,bz); A -> B, cells
@@ -210,6 +210,12 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          int start, cudaStream_t s);
 // chkdav (cans1d/common/chkdav.f:68-76) on device arrays: da below floor is
 // raised to it and vx zeroed there; the count is added to *count (device).
+// chkdav of 2-D / 3-D states (mlw1d.cu): na density-like slots a0, a1 of S
+// (n doubles each) floored in turn, each event zeroing nv velocity slots from
+// v0; with ctl S is the state the loop's step just wrote.
+cudaError_t launch_chkdav_nd(double *S, size_t n, int na, int a0, int a1, int nv, int v0,
+                             double floor, const Ctl *ctl, unsigned long long *count,
+                             cudaStream_t s);
 cudaError_t launch_chkdav(double *da, double *vx, double floor, size_t n,
                           unsigned long long *count, cudaStream_t s);
 cudaError_t launch_cfl1d(bool exact, const double *S, const double *bx, int ix,

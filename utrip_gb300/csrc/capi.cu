@@ -838,6 +838,69 @@ extern "C" int cans_chkdav(int *n_events, double *da, double *vx,
   return CANS_OK;
 }
 
+namespace {
+// chkdav of a 2-D / 3-D array and its nv velocity components, on their
+// registered mirrors (velocities in consecutive slots of one set) or on host
+// copies.
+int chkdav_nd(int *n_events, double *da, double *const *vel, int nv, double floor,
+              size_t n) {
+  if (!n_events || !da || !vel) return CANS_ERR_ARG;
+  for (int v = 0; v < nv; v++)
+    if (!vel[v]) return CANS_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s;
+  int rc = lib_stream(&s);
+  if (rc) return rc;
+  if ((rc = g_scratch.ensure((size_t)(nv + 1) * n))) return rc;
+  unsigned long long *cnt = g_scratch.bits;
+  CK(cudaMemsetAsync(cnt, 0, sizeof *cnt, s));
+  int va = -1, v0 = -1;
+  MirrorSet *m = find_set(da, &va);
+  bool resident = m != nullptr && find_set(vel[0], &v0) == m;
+  for (int v = 1; resident && v < nv; v++) {
+    int vv = -1;
+    resident = find_set(vel[v], &vv) == m && vv == v0 + v;
+  }
+  if (resident && m->n == n) {
+    CK(launch_chkdav_nd(m->buf[m->cur], n, 1, va, va, nv, v0, floor, nullptr, cnt, s));
+  } else {
+    double *S = g_scratch.A;
+    CK(cudaMemcpyAsync(S, da, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    for (int v = 0; v < nv; v++)
+      CK(cudaMemcpyAsync(S + (1 + v) * n, vel[v], sizeof(double) * n,
+                         cudaMemcpyHostToDevice, s));
+    CK(launch_chkdav_nd(S, n, 1, 0, 0, nv, 1, floor, nullptr, cnt, s));
+    CK(cudaMemcpyAsync(da, S, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    for (int v = 0; v < nv; v++)
+      CK(cudaMemcpyAsync(vel[v], S + (1 + v) * n, sizeof(double) * n,
+                         cudaMemcpyDeviceToHost, s));
+  }
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(&out, cnt, sizeof out, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *n_events = (int)out;
+  return CANS_OK;
+}
+}  // namespace
+
+// chkdav (cans2d/common/chkdav.f:2): da below floor raised to it, vx and vy
+// set to zero there
+extern "C" int cans_chkdav_2d(int *n_events, double *da, double *vx, double *vy,
+                              const double *floor, const int *ix, const int *jx) {
+  if (!floor || !ix || !jx || *ix < 0 || *jx < 0) return CANS_ERR_ARG;
+  double *vel[2] = {vx, vy};
+  return chkdav_nd(n_events, da, vel, 2, *floor, (size_t)*ix * *jx);
+}
+
+// chkdav (cans3d/common/chkdav.f:2): the same with vx, vy and vz
+extern "C" int cans_chkdav_3d(int *n_events, double *da, double *vx, double *vy,
+                              double *vz, const double *floor, const int *ix,
+                              const int *jx, const int *kx) {
+  if (!floor || !ix || !jx || !kx || *ix < 0 || *jx < 0 || *kx < 0) return CANS_ERR_ARG;
+  double *vel[3] = {vx, vy, vz};
+  return chkdav_nd(n_events, da, vel, 3, *floor, (size_t)*ix * *jx * *kx);
+}
+
 extern "C" int cans_cfl_m_1d(double *dt, const double *safety,
                              const double *dtmin, int *merr, const double *gm,
                              const double *bx, const double *ro,
@@ -1392,10 +1455,18 @@ cudaError_t launch_1d(cans_run *h, int max_steps, int fixed, double dt,
 }
 
 // cells whose CFL the step kernel reduces: all but the frame of width
-// margin+1 that the boundary program may rewrite
+// margin+1 that the boundary program may rewrite; none when chkdav may
+// change cells after the fill (the frame kernel then reduces every cell)
 Box3 inner_box(const cans_run *h) {
   const int w = h->bc.margin + 1;
   Box3 b{};
+  if (h->d.chkdav && h->ndim >= 2) {
+    for (int a = 0; a < 3; a++) {
+      b.lo[a] = 1;
+      b.hi[a] = 0;
+    }
+    return b;
+  }
   b.lo[0] = w;
   b.hi[0] = h->d.ix - 1 - w;
   b.lo[1] = w;
@@ -1445,9 +1516,11 @@ cudaError_t frame_kernel(cans_run *h) {
                                 h->ax.a, h->ay.a, h->az.a, h->ph, h->ctl, h->s);
   if (h->ndim == 3)
     return launch_frame3d(h->d.exact != 0, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
-                          h->ay.a, h->az.a, h->ph, h->bc.margin, h->ctl, h->s);
+                          h->ay.a, h->az.a, h->ph, h->bc.margin, h->ctl, h->s,
+                          h->d.chkdav ? 1 : 0);
   return launch_frame2d(layout2d(h), h->d.exact != 0, nullptr, h->d.ix, h->d.jx,
-                        h->ax.a, h->ay.a, h->ph, h->bc.margin, h->ctl, h->s);
+                        h->ax.a, h->ay.a, h->ph, h->bc.margin, h->ctl, h->s,
+                        h->d.chkdav ? 1 : 0);
 }
 cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
                             unsigned long long *bits) {
@@ -1466,6 +1539,12 @@ cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
 int enqueue_iteration(cans_run *h) {
   CK(step_kernel(h, h->tile, nullptr, nullptr, 0.0, h->ctl, inner_box(h)));
   CK(bc_kernels(h, nullptr, h->ctl));
+  // chkdav of ro, then pr, after the boundary fill (cans2d/md_efr/hdmlw/
+  // main.f:183-185): velocities zeroed where a floor applies (vx, vy in 2-D,
+  // also vz in 3-D)
+  if (h->d.chkdav)
+    CK(launch_chkdav_nd(nullptr, h->n, 2, 0, 1, h->ndim == 3 ? 3 : 2, 2, h->d.floor, h->ctl,
+                        &h->ctl->nfloor, h->s));
   CK(frame_kernel(h));
   return CANS_OK;
 }
@@ -1541,6 +1620,7 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     }
     if (!d->dx || !d->dy || !d->dz || !d->dxm || !d->dym || !d->dzm) return CANS_ERR_ARG;
   }
+  if (d->chkdav != 0 && d->chkdav != 1) return CANS_ERR_ARG;
   const bool bgv = d->solver == CANS_SOLVER_MLW_M_BG_1D;
   // 2-D mLW with gx set: the steps with gravity (mlw_m_g / mlw_m3_g)
   const bool mlw2d = d->solver == CANS_SOLVER_MLW_M_2D || d->solver == CANS_SOLVER_MLW_M3_2D;
@@ -1572,7 +1652,6 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
         if (!q) return CANS_ERR_ARG;
     // the torque source reads the rr profile of mlw_m_bg
     if (d->trq && !bgv) return CANS_ERR_ARG;
-    if (d->chkdav != 0 && d->chkdav != 1) return CANS_ERR_ARG;
   } else if (d->solver == CANS_SOLVER_HLLD_3D) {
     // checked above
   } else {
@@ -2026,9 +2105,10 @@ struct AdjWork {
   }
 };
 
-// the adjoint is that of the plain mlw_m3 step: no gravity, no resistivity
+// the adjoint is that of the plain mlw_m3 step and boundary fill: no
+// gravity, no resistivity, no chkdav floor
 bool adj_supported(const cans_run *h) {
-  return h->d.solver == CANS_SOLVER_MLW_M3_2D && !h->grav && !h->eta;
+  return h->d.solver == CANS_SOLVER_MLW_M3_2D && !h->grav && !h->eta && !h->d.chkdav;
 }
 
 int adj_setup(cans_run *h, AdjWork &W, int nsnap) {

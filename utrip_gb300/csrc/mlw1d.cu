@@ -809,6 +809,51 @@ __global__ void k_chkdav(double *da, double *vx, double floor, size_t n,
   if (threadIdx.x == 0 && cnt) atomicAdd(count, (unsigned long long)cnt);
 }
 
+// chkdav of the 2-D and 3-D model packages (cans2d/common/chkdav.f:33-44,
+// cans3d/common/chkdav.f): where da < floor, da = floor and the velocity
+// components vel[0..nv-1] are set to zero.  With ctl the arrays are slots of
+// the state the step just wrote (da = slot a[0], then a[1]; velocities at
+// slots v0..), and the kernel is a no-op once the loop is done or paused.
+__global__ void k_chkdav_nd(double *S, size_t n, int na, int a0, int a1, int nv, int v0,
+                            double floor, const Ctl *ctl, unsigned long long *count) {
+  __shared__ unsigned int cnt;
+  if (ctl != nullptr) {
+    if (ctl->done | ctl->pause) return;
+    S = ctl->buf[ctl->cur ^ 1];
+  }
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  unsigned int mine = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll 1
+    for (int q = 0; q < na; q++) {  // chkdav of ro, then of pr
+      double *da = S + (size_t)(q == 0 ? a0 : a1) * n;
+      if (da[i] < floor) {
+        da[i] = floor;
+#pragma unroll 1
+        for (int v = 0; v < nv; v++) S[(size_t)(v0 + v) * n + i] = 0.0;
+        mine++;
+      }
+    }
+  }
+  if (mine) atomicAdd(&cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0 && cnt) atomicAdd(count, (unsigned long long)cnt);
+}
+
+cudaError_t launch_chkdav_nd(double *S, size_t n, int na, int a0, int a1, int nv, int v0,
+                             double floor, const Ctl *ctl, unsigned long long *count,
+                             cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int threads = 256;
+  const size_t want = (n + threads - 1) / threads;
+  const int blocks = (int)(want < 1216 ? want : 1216);
+  k_chkdav_nd<<<blocks, threads, 0, s>>>(S, n, na, a0, a1, nv, v0, floor, ctl, count);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_chkdav(double *da, double *vx, double floor, size_t n,
                           unsigned long long *count, cudaStream_t s) {
   if (n == 0) return cudaSuccess;

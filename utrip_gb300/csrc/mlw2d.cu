@@ -147,9 +147,11 @@ cudaError_t launch_cfl2d_full(int solver, bool exact, const double *S, int ix,
 // CFL over the frame of cells the boundary fill may have rewritten (ghost
 // layers plus the first interior layer), then the start of the next loop
 // iteration by the last block to finish.
+// With all = 1 the CFL covers every cell: a loop whose chkdav changes cells
+// after the step reduces its CFL here alone.
 template <bool E, bool M3>
 __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
-                          Axis ax, Axis ay, Phys ph, int w, Ctl *ctl) {
+                          Axis ax, Axis ay, Phys ph, int w, int all, Ctl *ctl) {
   using FT = F<E>;
   using P = Prim<M3>;
   __shared__ double red[32];
@@ -160,14 +162,18 @@ __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
   // i >= ix-w of the remaining rows
   const long long nrow = 2LL * w * ix;
   const long long inner_rows = jx - 2LL * w;
-  const long long total = nrow + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
+  const long long total =
+      all ? (long long)ix * jx : nrow + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
   bool bad = false;
   const FT gm(ph.gm), pi4i(ph.pi4i);
   for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
        f < total; f += (long long)gridDim.x * blockDim.x) {
     int i, j;
-    if (f < nrow) {
+    if (all) {
+      i = (int)(f % ix);
+      j = (int)(f / ix);
+    } else if (f < nrow) {
       const long long r = f / ix;
       i = (int)(f % ix);
       j = (r < w) ? (int)r : (int)(jx - 2 * w + r);
@@ -214,18 +220,18 @@ __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
 cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
                            int jx, const Axis &ax, const Axis &ay,
                            const Phys &ph, int margin, Ctl *ctl,
-                           cudaStream_t s) {
+                           cudaStream_t s, int all) {
   const int w = margin + 1;
-  const long long total = 2LL * w * ix + 2LL * w * (jx - 2LL * w);
+  const long long total = all ? (long long)ix * jx : 2LL * w * ix + 2LL * w * (jx - 2LL * w);
   int blocks = (int)((total + 255) / 256);
   if (blocks < 1) blocks = 1;
-  if (blocks > 152) blocks = 152;
+  if (blocks > (all ? 152 * 4 : 152)) blocks = all ? 152 * 4 : 152;
   if (solver == 1) {
-    if (exact) k_frame2d<true, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
-    else k_frame2d<false, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
+    if (exact) k_frame2d<true, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, all, ctl);
+    else k_frame2d<false, true><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, all, ctl);
   } else {
-    if (exact) k_frame2d<true, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
-    else k_frame2d<false, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, ctl);
+    if (exact) k_frame2d<true, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, all, ctl);
+    else k_frame2d<false, false><<<blocks, 256, 0, s>>>(S, ix, jx, ax, ay, ph, w, all, ctl);
   }
   count_launch();
   return cudaGetLastError();

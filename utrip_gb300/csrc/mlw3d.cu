@@ -827,21 +827,29 @@ __device__ __forceinline__ void frame3_index(long long f, int ix, int jx, int kx
   i = (c < w) ? c : (ix - 2 * w + c);
 }
 
+// With all = 1 the CFL covers every cell (a loop with chkdav after the fill).
 template <bool E>
 __global__ void k_frame3d(int ix, int jx, int kx, Axis ax, Axis ay, Axis az,
-                          Phys ph, int w, Ctl *ctl) {
+                          Phys ph, int w, int all, Ctl *ctl) {
   __shared__ double red[32];
   if (ctl->done | ctl->pause) return;
   const double *S = ctl->buf[ctl->cur ^ 1];
   const size_t plane = (size_t)ix * jx, n = plane * kx;
-  const long long total = 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
-                          2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
+  const long long total = all ? (long long)n
+                              : 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
+                                    2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
   bool bad = false;
   for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < total;
        f += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
-    frame3_index(f, ix, jx, kx, w, i, j, k);
+    if (all) {
+      i = (int)(f % ix);
+      j = (int)((f / ix) % jx);
+      k = (int)(f / ((long long)ix * jx));
+    } else {
+      frame3_index(f, ix, jx, kx, w, i, j, k);
+    }
     const size_t g = (size_t)i + (size_t)j * ix + (size_t)k * plane;
     const double d = cfl3_cell<E>(S, n, g, i, j, k, ax, ay, az, ph, ctl->safety);
     if (d < dmin) dmin = d;
@@ -862,15 +870,16 @@ __global__ void k_frame3d(int ix, int jx, int kx, Axis ax, Axis ay, Axis az,
 
 cudaError_t launch_frame3d(bool exact, int ix, int jx, int kx, const Axis &ax,
                            const Axis &ay, const Axis &az, const Phys &ph,
-                           int margin, Ctl *ctl, cudaStream_t s) {
+                           int margin, Ctl *ctl, cudaStream_t s, int all) {
   const int w = margin + 1;
-  const long long total = 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
-                          2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
+  const long long total = all ? (long long)ix * jx * kx
+                              : 2LL * w * ix * jx + 2LL * w * ix * (kx - 2LL * w) +
+                                    2LL * w * (jx - 2LL * w) * (kx - 2LL * w);
   int blocks = (int)((total + 255) / 256);
   if (blocks < 1) blocks = 1;
   if (blocks > 152 * 4) blocks = 152 * 4;
-  if (exact) k_frame3d<true><<<blocks, 256, 0, s>>>(ix, jx, kx, ax, ay, az, ph, w, ctl);
-  else k_frame3d<false><<<blocks, 256, 0, s>>>(ix, jx, kx, ax, ay, az, ph, w, ctl);
+  if (exact) k_frame3d<true><<<blocks, 256, 0, s>>>(ix, jx, kx, ax, ay, az, ph, w, all, ctl);
+  else k_frame3d<false><<<blocks, 256, 0, s>>>(ix, jx, kx, ax, ay, az, ph, w, all, ctl);
   count_launch();
   return cudaGetLastError();
 }

@@ -51,6 +51,22 @@ def _bnd3(setup, state):
                 capi.bd_3d(kind, axis, face % 2, margin, state[var], q0, dxm)
 
 
+def _chkdav(setup, state):
+    """chkdav of ro, then pr, after bnd (cans2d/md_efr/hdmlw/main.f:183-185)."""
+    fl, names = setup["floor"], setup["names"]
+    if state[0].ndim == 1:
+        capi.chkdav(state[0], state[2], fl)
+        capi.chkdav(state[1], state[2], fl)
+        return
+    three = state[0].ndim == 3
+    v = [state[names.index(k)] for k in (("vx", "vy", "vz") if three else ("vx", "vy"))]
+    for q in (0, 1):
+        if three:
+            capi.chkdav_3d(state[q], v[0], v[1], v[2], fl)
+        else:
+            capi.chkdav_2d(state[q], v[0], v[1], fl)
+
+
 def _bnd1(setup, state):
     """cans1d/md_mhdshktb/hdmlw/bnd.f:9-19: lower-face rules, then upper."""
     margin = setup["margin"]
@@ -158,6 +174,8 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
             {"mlw_m_3d": _bnd3, "roe_m_3d": _bnd3, "hlld_3d": _bnd3,
              "mlw_m_1d": _bnd1, "mlw_m_bg_1d": _bnd1,
              "roe_m_1d": _bnd1}.get(setup["solver"], _bnd)(setup, state)
+            if setup.get("floor") is not None:
+                _chkdav(setup, state)
             if not (ns < nstop and t < tend):
                 return t, ns, 0, dts
     finally:

@@ -910,7 +910,8 @@ def emerging_flux_2d(nx: int = 64, ny: int = 128):
     perturbation, az from bbtoaa.  Boundaries: x symmetric (vx, by odd); at
     the y faces vy, by odd, vx, bx, az even, and ro, pr held at their initial
     ghost values (bdiniy, the constant rule bdcnsy for this horizontally
-    uniform state).  mlw_m_g, cfl_m safety 0.4, qav 3, tend 80."""
+    uniform state).  mlw_m_g, cfl_m safety 0.4, qav 3, tend 80, and chkdav
+    of ro and pr with floor 1e-9 after every boundary fill."""
     margin = 1
     ix, jx = nx + 2 * margin, ny + 2 * margin
     gm = 5.0 / 3.0
@@ -943,9 +944,10 @@ def emerging_flux_2d(nx: int = 64, ny: int = 128):
     g0 = -1.0 / gm
     grav = dict(gx=np.zeros(shape, order="F"), gxm=np.zeros(shape, order="F"),
                 gy=np.full(shape, g0, order="F"), gym=np.full(shape, g0, order="F"))
+    # main.f:183-185: chkdav of ro and pr with floor 1e-9 after every bnd
     return _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
-                 tend=80.0, dtout=1.0, gravity=True, name=f"emerging_flux_{nx}x{ny}",
-                 **grav)
+                 tend=80.0, dtout=1.0, gravity=True, floor=1e-9,
+                 name=f"emerging_flux_{nx}x{ny}", **grav)
 
 
 def emerging_flux_3d(nx: int = 128, ny: int = 2, nz: int = 128):
@@ -1122,3 +1124,85 @@ def mhd_wave_2d(n: int = 64):
     bc = _bc_all(len(VARS["mlw_m"]), BD_FRE, BD_FRE)
     return _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
                  tend=1.0, margin=margin, thini=thini, name=f"mhd_wave_{n}")
+
+
+def parker_instability(nx: int = 64, ny: int = 128):
+    """The Parker-instability model of cans2d/md_parkerinst/hdmlw (model.f,
+    pertub.f, bnd.f, main.f:160-180): a gravitationally stratified disk on
+    [-50, 50] x [-25, 25] (nx x ny cells, one ghost layer) with gravity
+    gy = -(1/gm) tanh(y/0.5) towards the midplane, a cool layer (T = 1)
+    under a corona (T = 25) beyond |y| = 6, a horizontal field with
+    1/beta = 5 inside |y| < 2.5 in the discrete magnetohydrostatic balance
+    of model.f, and a vy perturbation of amplitude 0.1 (pertub.f).
+    Boundaries: x periodic, y symmetric (vy, by odd).  mlw_m_g with qav 3,
+    cfl_m safety 0.4, chkdav of ro and pr with floor 1e-9, tend 60."""
+    margin = 1
+    ix, jx = nx + 2 * margin, ny + 2 * margin
+    gm = 5.0 / 3.0
+    pi = math.acos(-1.0)
+    f32 = lambda v: float(np.float32(v))  # noqa: E731  (real*4 literals)
+
+    def axis(nn, lo, hi):
+        d0 = (hi - lo) / float(nn - 2 * margin)
+        dm = np.full(nn, d0)
+        iz = nn // 2 + 1
+        x = np.empty(nn)
+        x[iz - 1] = dm[iz - 1] / 2.0
+        for i in range(iz + 1, nn + 1):
+            x[i - 1] = x[i - 2] + dm[i - 2]
+        for i in range(iz - 1, 0, -1):
+            x[i - 1] = x[i] - dm[i - 1]
+        return x, dm
+
+    x, _ = axis(ix, -50.0, 50.0)
+    y, dym0 = axis(jx, -25.0, 25.0)
+    g0 = -1.0 / gm
+    wg0 = f32(0.5)
+    gym0 = g0 * np.tanh((y + 0.5 * dym0) / wg0)
+    ytr, wtr, tcor = f32(6.0), f32(0.5), f32(25.0)
+    tem0 = 1.0 + 0.5 * (tcor - 1.0) * (np.tanh((np.abs(y) - ytr) / wtr) + 1.0)
+    yf1, yf2, wf0 = f32(-2.5), f32(2.5), f32(0.5)
+    rbetaf = f32(f32(1.0) / np.float32(0.2))  # 1.0/0.2 evaluated in single precision
+    af1 = (np.tanh((y - yf1) / wf0) + 1.0) / 2
+    af2 = (-np.tanh((y - yf2) / wf0) + 1.0) / 2
+    rbeta0 = np.abs(rbetaf * af1 * af2)
+    jz = jx // 2  # 0-based index of Fortran jzero = jx/2+1
+    den0, pre0 = np.empty(jx), np.empty(jx)
+    den0[jz] = 1.0
+    pre0[jz] = 1.0 / gm * tem0[jz]
+    for j in range(jz + 1, jx):
+        h = 0.5 * gm * gym0[j - 1] * dym0[j - 1]
+        den0[j] = den0[j - 1] * ((1 + rbeta0[j - 1]) * tem0[j - 1] + h) / \
+            ((1 + rbeta0[j]) * tem0[j] - h)
+        pre0[j] = pre0[jz] * (den0[j] / den0[jz]) * (tem0[j] / tem0[jz])
+    for j in range(jz - 1, -1, -1):
+        h = 0.5 * gm * gym0[j] * dym0[j]
+        den0[j] = den0[j + 1] * ((1 + rbeta0[j + 1]) * tem0[j + 1] - h) / \
+            ((1 + rbeta0[j]) * tem0[j] + h)
+        pre0[j] = pre0[jz] * (den0[j] / den0[jz]) * (tem0[j] / tem0[jz])
+    bmx0 = np.sqrt(8 * pi * pre0 * rbeta0)
+    shape = (ix, jx)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    amp, xptb, yptb1, yptb2, wptb = f32(0.1), f32(20.0), f32(-4.0), f32(4.0), f32(0.5)
+    vy = (amp * np.cos(2 * pi * X / xptb) * 0.5
+          * (np.tanh((X + 0.75 * xptb) / wptb) - np.tanh((X - 0.75 * xptb) / wptb)) * 0.5
+          * (np.tanh((Y - yptb1) / wptb) - np.tanh((Y - yptb2) / wptb)))
+    f = {"ro": np.broadcast_to(den0, shape).copy(), "pr": np.broadcast_to(pre0, shape).copy(),
+         "vx": np.zeros(shape), "vy": 0.0 + vy,
+         "bx": np.broadcast_to(bmx0, shape).copy(), "by": np.zeros(shape)}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, margin)
+    names = VARS["mlw_m"]
+    bc = []
+    for v, name in enumerate(names):
+        bc += [(v, 0, BD_PER, 0.0), (v, 1, BD_PER, 0.0)]
+    for v, name in enumerate(names):
+        kind = BD_SPN if name in ("vy", "by") else BD_SPP
+        bc += [(v, 2, kind, 0.0), (v, 3, kind, 0.0)]
+    grav = dict(gx=np.zeros(shape, order="F"), gxm=np.zeros(shape, order="F"),
+                gy=np.asfortranarray(np.broadcast_to(g0 * np.tanh(y / wg0), shape)),
+                gym=np.asfortranarray(np.broadcast_to(gym0, shape)))
+    return _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+                 tend=60.0, dtout=2.0, gravity=True, floor=1e-9,
+                 name=f"parker_instability_{nx}x{ny}", **grav)
