@@ -200,3 +200,16 @@ def test_full_size_512_fast_vs_exact_and_conservation(gpu):
     # periodic box: total mass is conserved to rounding
     m0 = s["state"][0][1:-1, 1:-1].sum()
     assert abs(a[0][1:-1, 1:-1].sum() - m0) <= 1e-12 * m0
+
+
+def test_oblique_shock_tube_to_tend_exact_bitwise(gpu, oracle_lib):
+    """cans2d/md_mhd3shktb at the reference's 64 x 64: the whole run to
+    t = 0.1 (cfl_m3 -> mlw_m3 -> free boundaries) on the device."""
+    s = setups.oblique_shock_tube_2d(64)
+    ref = setups.copy_state(s)
+    t, ns, merr, _ = oracle.run_2d(s, ref, 10 ** 6)
+    got = setups.copy_state(s)
+    out = drivers.run_resident(s, got, 10 ** 6, exact=True)
+    assert out == (t, ns, merr, ns) and t >= 0.1
+    for k, a, b in zip(s["names"], got, ref):
+        assert np.array_equal(a, b), k

@@ -1206,3 +1206,51 @@ def parker_instability(nx: int = 64, ny: int = 128):
     return _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
                  tend=60.0, dtout=2.0, gravity=True, floor=1e-9,
                  name=f"parker_instability_{nx}x{ny}", **grav)
+
+
+def oblique_shock_tube_2d(n: int = 64):
+    """The oblique MHD shock tube of cans2d/md_mhd3shktb/hdmlw (model.f,
+    bnd.f, main.f:165-180): the Brio-Wu states (rho 1 / 0.125, p 1 / 0.1,
+    bz +-b0) joined by a tanh of width 0.02 across the line
+    x cos(60 deg) + y sin(60 deg) = 0 of [-0.5, 0.5]^2 (n x n cells, one
+    ghost layer), an in-plane field 0.75 b0 along that normal,
+    b0 = sqrt(8 pi/gm), gamma 2, free boundaries; mlw_m3 with qav 3, cfl_m3
+    safety 0.4, tend 0.1."""
+    margin = 1
+    ix = jx = n + 2 * margin
+    gm = 2.0
+    pi = math.acos(-1.0)
+    f32 = lambda v: float(np.float32(v))  # noqa: E731  (real*4 literals)
+
+    def axis(nn):
+        d0 = 1.0 / float(nn - 2 * margin)
+        dm = np.full(nn, d0)
+        iz = nn // 2 + 1
+        x = np.empty(nn)
+        x[iz - 1] = dm[iz - 1] / 2.0
+        for i in range(iz + 1, nn + 1):
+            x[i - 1] = x[i - 2] + dm[i - 2]
+        for i in range(iz - 1, 0, -1):
+            x[i - 1] = x[i] - dm[i - 1]
+        return x
+
+    x, y = axis(ix), axis(jx)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    b0 = math.sqrt(8 * pi / gm)
+    thini = f32(60.0) / f32(180.0) * pi
+    b00 = f32(0.75) * b0
+    wtr = f32(0.02)
+    ro0, ro1, pr0, pr1 = 1.0, f32(0.125), 1.0, f32(0.1)
+    bz0, bz1 = +b0, -b0
+    ss = X * math.cos(thini) + Y * math.sin(thini)
+    w = (1 + np.tanh(ss / wtr)) / 2
+    f = {"ro": ro0 + (ro1 - ro0) * w, "pr": pr0 + (pr1 - pr0) * w,
+         "bx": np.full(X.shape, b00 * math.cos(thini)),
+         "by": np.full(X.shape, b00 * math.sin(thini)), "bz": bz0 + (bz1 - bz0) * w,
+         "vx": np.zeros(X.shape), "vy": np.zeros(X.shape), "vz": np.zeros(X.shape)}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    f["az"] = bbtoaa(np.asfortranarray(f["bx"]), np.asfortranarray(f["by"]), dxm, dym, margin)
+    bc = _bc_all(len(VARS["mlw_m3"]), BD_FRE, BD_FRE)
+    return _pack("mlw_m3", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+                 tend=0.1, margin=margin, name=f"oblique_shock_tube_{n}")
