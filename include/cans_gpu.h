@@ -269,6 +269,17 @@ int cans_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                     const double *dxm, const int *ix, const double *dy,
                     const double *dym, const int *jx, const double *dz,
                     const double *dzm, const int *kx);
+/* replaces subroutine mlw_m_e (cans3d/hdmlw/mlw_m_e.f:2-3): the 3-D
+ * resistive step; et at the cells, etm at the cell corners, ix*jx*kx each.
+ * J on the outer layer of cells and of corners is taken as zero (the
+ * reference leaves it undefined there). */
+int cans_mlw_m_e_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                    double *bx, double *by, double *bz, const double *dt,
+                    const double *qav, const double *gm, const double *et,
+                    const double *etm, const double *dx, const double *dxm,
+                    const int *ix, const double *dy, const double *dym,
+                    const int *jx, const double *dz, const double *dzm,
+                    const int *kx);
 /* replaces subroutine cfl_m   (cans3d/common/cfl_m.f:2-3) */
 int cans_cfl_m_3d(double *dt, const double *safety, const double *dtmin,
                   int *merr, const double *gm, const double *ro,
@@ -277,6 +288,15 @@ int cans_cfl_m_3d(double *dt, const double *safety, const double *dtmin,
                   const double *bz, const double *dx, const int *ix,
                   const double *dy, const int *jx, const double *dz,
                   const int *kx);
+/* replaces subroutine cfl_m_e (cans3d/common/cfl_m_e.f:2-4): cfl_m with the
+ * diffusion limit safety*0.5*min(dx,dy,dz)**2/max(et,1.d-10) */
+int cans_cfl_m_e_3d(double *dt, const double *safety, const double *dtmin,
+                    int *merr, const double *gm, const double *ro,
+                    const double *pr, const double *vx, const double *vy,
+                    const double *vz, const double *bx, const double *by,
+                    const double *bz, const double *et, const double *dx,
+                    const int *ix, const double *dy, const int *jx,
+                    const double *dz, const int *kx);
 /* replaces subroutine engine  (cansxx-nosupport/md_mhdshktb/hdhlld-x/
  * engine.f:2): one two-stage HLLD step (hlld_mh.f, hlld_flux.f90,
  * inp_const.f, inp_tvdminmod.f, adddfdx.f) on 8 arrays in Heaviside units
@@ -410,9 +430,10 @@ typedef struct {
   unsigned long long seed;
   /* 2-D mLW with gravity: gy(ix,jx) at the cells, gym(ix,jx) at the corners */
   const double *gy, *gym;
-  /* 2-D mLW with resistivity (mlw_m_e / mlw_m3_e, with gx also mlw_m_ge /
-   * mlw_m3_ge): et(ix,jx) at the cells, etm(ix,jx) at the corners; the time
-   * step then includes the diffusion limit of cfl_m_e / cfl_m3_e */
+  /* mLW with resistivity (2-D mlw_m_e / mlw_m3_e, with gx also mlw_m_ge /
+   * mlw_m3_ge; 3-D mlw_m_e, without gravity): et at the cells, etm at the
+   * corners, ix*jx(*kx) each; the time step then includes the diffusion
+   * limit of cfl_m_e / cfl_m3_e */
   const double *et, *etm;
   /* 3-D mLW with gravity (mlw_m_g, cans3d/hdmlw/mlw_m_g.f): gx, gxm, gy, gym
    * above and gz, gzm here, ix*jx*kx each (the *m fields at the corners) */

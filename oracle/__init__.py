@@ -62,6 +62,10 @@ def load():
         lib.oracle_mlw_m_3d.argtypes = [_dp] * 8 + [d, d, d, _dp, _dp, i, _dp, _dp, i, _dp, _dp, i]
         lib.oracle_mlw_m_g_3d.argtypes = ([_dp] * 8 + [d, d, d] + [_dp] * 6 +
                                           [_dp, _dp, i, _dp, _dp, i, _dp, _dp, i])
+        lib.oracle_mlw_m_e_3d.argtypes = ([_dp] * 8 + [d, d, d] + [_dp] * 2 +
+                                          [_dp, _dp, i, _dp, _dp, i, _dp, _dp, i])
+        lib.oracle_cfl_m_e_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 9 + [_dp, i, _dp, i,
+                                                                              _dp, i]
         lib.oracle_cfl_m_3d.argtypes = [_dp, d, d, _ip, d] + [_dp] * 8 + [_dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m_3d.argtypes = [_dp] * 8 + [d, d, _dp, i, _dp, i, _dp, i]
         lib.oracle_roe_m3_2d.argtypes = [_dp] * 9 + [d, d, _dp, i, _dp, i]
@@ -457,6 +461,25 @@ def mlw_m_g_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, gx, gxm, gy, gym, gz
                              P(dy), P(dym), jx, P(dz), P(dzm), kx)
 
 
+def mlw_m_e_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, et, etm, dx, dxm, dy, dym,
+               dz, dzm):
+    """cans3d/hdmlw/mlw_m_e.f:2"""
+    ix, jx, kx = ro.shape
+    load().oracle_mlw_m_e_3d(*[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], dt, qav, gm,
+                             P(et), P(etm), P(dx), P(dxm), ix, P(dy), P(dym), jx, P(dz),
+                             P(dzm), kx)
+
+
+def cfl_m_e_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, et, dx, dy, dz):
+    """cans3d/common/cfl_m_e.f:2"""
+    ix, jx, kx = ro.shape
+    dt, merr = C.c_double(), C.c_int()
+    load().oracle_cfl_m_e_3d(C.byref(dt), safety, dtmin, C.byref(merr), gm,
+                             *[P(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, et)],
+                             P(dx), ix, P(dy), jx, P(dz), kx)
+    return dt.value, merr.value
+
+
 def cfl_m_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, dx, dy, dz):
     ix, jx, kx = ro.shape
     dt, merr = C.c_double(), C.c_int()
@@ -510,6 +533,11 @@ def step_3d(setup, state, dt):
     if setup.get("solver") == "roe_m_3d":
         roe_m_3d(*state, dt, setup["gm"], setup["dx"], setup["dy"], setup["dz"])
         return
+    if setup.get("et") is not None:
+        mlw_m_e_3d(*state, dt, setup["qav"], setup["gm"], np.asfortranarray(setup["et"]),
+                   np.asfortranarray(setup["etm"]), setup["dx"], setup["dxm"], setup["dy"],
+                   setup["dym"], setup["dz"], setup["dzm"])
+        return
     if setup.get("gravity"):
         g = [np.asfortranarray(setup[k]) for k in ("gx", "gxm", "gy", "gym", "gz", "gzm")]
         mlw_m_g_3d(*state, dt, setup["qav"], setup["gm"], *g, setup["dx"], setup["dxm"],
@@ -520,6 +548,9 @@ def step_3d(setup, state, dt):
 
 
 def cfl_3d(setup, state, safety):
+    if setup.get("et") is not None:
+        return cfl_m_e_3d(safety, setup["dtmin"], setup["gm"], *state,
+                          np.asfortranarray(setup["et"]), setup["dx"], setup["dy"], setup["dz"])
     return cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"], setup["dy"],
                     setup["dz"])
 

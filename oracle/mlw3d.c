@@ -8,8 +8,13 @@
  *   mlw_m     cans3d/hdmlw/mlw_m.f:2-453
  *   mlw_m_g   cans3d/hdmlw/mlw_m_g.f:2-469 (with gravity), with
  *   mlwsrch   cans3d/hdmlw/mlwsrch.f:32-50 and mlwsrcf cans3d/hdmlw/mlwsrcf.f:35-45
+ *   mlw_m_e   cans3d/hdmlw/mlw_m_e.f:2-473 (with resistivity), with
+ *   bbtocx/y/z cans3d/common/bbtocx.f:29-35, bbtocy.f, bbtocz.f
+ *   cfl_m_e   cans3d/common/cfl_m_e.f (diffusion limit, etmin 1.d-10)
  *   cfl_m     cans3d/common/cfl_m.f:39-85 (pi in single precision)
  */
+#include <string.h>
+
 #include "oracle.h"
 #include "oracle_common.h"
 
@@ -158,6 +163,34 @@ static void mlwsrcf3(double *du, double dt, const double *s, const double *ux0,
       }
 }
 
+/* cans3d/common/bbtocx.f:29-35 (and bbtocy.f, bbtocz.f by cyclic
+ * permutation): c = (b2(+1 along axis 1) - b2(-1)) / d1 / 2
+ *                 - (b1(+1 along axis 2) - b1(-1)) / d2 / 2
+ * on the cells 2..n-1 of every axis; s1, s2 are the index strides of the two
+ * axes and d1, d2 their spacings at the point. */
+static void bbtoc3(double *c, const double *b1, const double *b2, const double *d1,
+                   int a1, const double *d2, int a2, int ix, int jx, int kx) {
+  const size_t st[3] = {1, (size_t)ix, (size_t)ix * (size_t)jx};
+  OMP_FOR
+  for (int k = 2; k <= kx - 1; k++)
+    for (int j = 2; j <= jx - 1; j++)
+      for (int i = 2; i <= ix - 1; i++) {
+        const int idx[3] = {i, j, k};
+        const size_t g = I3(i, j, k);
+        c[g] = (b2[g + st[a1]] - b2[g - st[a1]]) / d1[I1(idx[a1])] / 2.0 -
+               (b1[g + st[a2]] - b1[g - st[a2]]) / d2[I1(idx[a2])] / 2.0;
+      }
+}
+
+/* the half-step field of corners ix, jx or kx is never set by mlwhalf; the
+ * corner currents read it for the last corner of each axis, and take zero */
+static void zero_top_corners(double *a, int ix, int jx, int kx) {
+  for (int k = 1; k <= kx; k++)
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++)
+        if (i == ix || j == jx || k == kx) a[I3(i, j, k)] = 0.0;
+}
+
 #define LOOP3(k0, k1, j0, j1, i0, i1)                                          \
   OMP_FOR                                                                      \
   for (int k = k0; k <= k1; k++)                                               \
@@ -170,13 +203,14 @@ static void mlwsrcf3(double *du, double dt, const double *s, const double *ux0,
  * and the three momenta through mlwsrch / mlwsrcf. */
 static void mlw_m_3d_core(double *ro, double *pr, double *vx, double *vy, double *vz,
                           double *bx, double *by, double *bz, double dt, double qav,
-                          double gm, const double *const *g, const double *dx,
+                          double gm, const double *const *g, const double *et,
+                          const double *etm, const double *dx,
                           const double *dxm, int ix, const double *dy,
                           const double *dym, int jx, const double *dz,
                           const double *dzm, int kx) {
   const size_t n = (size_t)ix * (size_t)jx * (size_t)kx;
   const size_t nm = (size_t)(ix > jx ? (ix > kx ? ix : kx) : (jx > kx ? jx : kx));
-  enum { NT = 37 };
+  enum { NT = 40 };
   double *w = arena_get(&arena3d, NT * n + 12 * nm);
   double *t[NT];
   for (int a = 0; a < NT; a++) t[a] = w + a * n;
@@ -190,6 +224,7 @@ static void mlw_m_3d_core(double *ro, double *pr, double *vx, double *vy, double
   double *dbx = t[27], *dby = t[28], *dbz = t[29];
   double *fx = t[30], *qx = t[31], *fy = t[32], *qy = t[33], *fz = t[34],
          *qz = t[35], *ss = t[36];
+  double *cx = t[37], *cy = t[38], *cz = t[39];
   double *m = w + NT * n;
   double *dxi = m, *dxim = m + nm, *ux0 = m + 2 * nm, *ux1 = m + 3 * nm;
   double *dyi = m + 4 * nm, *dyim = m + 5 * nm, *uy0 = m + 6 * nm,
@@ -244,6 +279,18 @@ static void mlw_m_3d_core(double *ro, double *pr, double *vx, double *vy, double
     ex[c] = -vy[c] * bz[c] + vz[c] * by[c];
     ey[c] = -vz[c] * bx[c] + vx[c] * bz[c];
     ez[c] = -vx[c] * by[c] + vy[c] * bx[c];
+  }
+  if (et) {  /* mlw_m_e.f:103-115: E += et * J */
+    memset(cx, 0, 3 * n * sizeof(double));
+    bbtoc3(cx, by, bz, dy, 1, dz, 2, ix, jx, kx);
+    bbtoc3(cy, bz, bx, dz, 2, dx, 0, ix, jx, kx);
+    bbtoc3(cz, bx, by, dx, 0, dy, 1, ix, jx, kx);
+    LOOP3(1, kx, 1, jx, 1, ix) {
+      size_t c = I3(i, j, k);
+      ex[c] = -vy[c] * bz[c] + vz[c] * by[c] + et[c] * cx[c];
+      ey[c] = -vz[c] * bx[c] + vx[c] * bz[c] + et[c] * cy[c];
+      ez[c] = -vx[c] * by[c] + vy[c] * bx[c] + et[c] * cz[c];
+    }
   }
 #define HALF3(u, un, du)                                                       \
   mlwhalf3(u, un, du, dt, fx, dxi, dxim, ix, fy, dyi, dyim, jx, fz, dzi, dzim, kx)
@@ -343,6 +390,21 @@ static void mlw_m_3d_core(double *ro, double *pr, double *vx, double *vy, double
     exh[c] = -vyh[c] * bzh[c] + vzh[c] * byh[c];
     eyh[c] = -vzh[c] * bxh[c] + vxh[c] * bzh[c];
     ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c];
+  }
+  if (et) {  /* mlw_m_e.f:257-270: Eh += etm * Jh at the corners */
+    zero_top_corners(bxh, ix, jx, kx);
+    zero_top_corners(byh, ix, jx, kx);
+    zero_top_corners(bzh, ix, jx, kx);
+    memset(cx, 0, 3 * n * sizeof(double));
+    bbtoc3(cx, byh, bzh, dym, 1, dzm, 2, ix, jx, kx);
+    bbtoc3(cy, bzh, bxh, dzm, 2, dxm, 0, ix, jx, kx);
+    bbtoc3(cz, bxh, byh, dxm, 0, dym, 1, ix, jx, kx);
+    LOOP3(1, kx - 1, 1, jx - 1, 1, ix - 1) {
+      size_t c = I3(i, j, k);
+      exh[c] = -vyh[c] * bzh[c] + vzh[c] * byh[c] + etm[c] * cx[c];
+      eyh[c] = -vzh[c] * bxh[c] + vxh[c] * bzh[c] + etm[c] * cy[c];
+      ezh[c] = -vxh[c] * byh[c] + vyh[c] * bxh[c] + etm[c] * cz[c];
+    }
   }
 #define FULL3(du)                                                              \
   mlwfull3(du, dt, fx, dxi, ux0, ux1, ix, fy, dyi, uy0, uy1, jx, fz, dzi, uz0, \
@@ -478,8 +540,8 @@ void oracle_mlw_m_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
                      double gm, const double *dx, const double *dxm, int ix,
                      const double *dy, const double *dym, int jx,
                      const double *dz, const double *dzm, int kx) {
-  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, NULL, dx, dxm, ix, dy, dym,
-                jx, dz, dzm, kx);
+  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, NULL, NULL, NULL, dx, dxm, ix,
+                dy, dym, jx, dz, dzm, kx);
 }
 
 /* cans3d/hdmlw/mlw_m_g.f:2-4 */
@@ -491,8 +553,52 @@ void oracle_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy, double *v
                        int ix, const double *dy, const double *dym, int jx,
                        const double *dz, const double *dzm, int kx) {
   const double *g[6] = {gx, gxm, gy, gym, gz, gzm};
-  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, g, dx, dxm, ix, dy, dym, jx,
-                dz, dzm, kx);
+  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, g, NULL, NULL, dx, dxm, ix, dy,
+                dym, jx, dz, dzm, kx);
+}
+
+/* cans3d/hdmlw/mlw_m_e.f:2-3 */
+void oracle_mlw_m_e_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                       double *bx, double *by, double *bz, double dt, double qav,
+                       double gm, const double *et, const double *etm, const double *dx,
+                       const double *dxm, int ix, const double *dy, const double *dym,
+                       int jx, const double *dz, const double *dzm, int kx) {
+  mlw_m_3d_core(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, NULL, et, etm, dx, dxm, ix, dy,
+                dym, jx, dz, dzm, kx);
+}
+
+/* cans3d/common/cfl_m_e.f: the wave limit of cfl_m (single-precision pi)
+ * and the diffusion limit safety*0.5*dmesh**2/max(et,1.d-10) */
+void oracle_cfl_m_e_3d(double *dt, double safety, double dtmin, int *merr, double gm,
+                       const double *ro, const double *pr, const double *vx,
+                       const double *vy, const double *vz, const double *bx,
+                       const double *by, const double *bz, const double *et,
+                       const double *dx, int ix, const double *dy, int jx,
+                       const double *dz, int kx) {
+  const double pai = (double)acosf(-1.0f);
+  const double onep4 = 0.25 / pai;
+  double dmin = R4_1E20;
+#ifdef _OPENMP
+#pragma omp parallel for reduction(min : dmin) schedule(static)
+#endif
+  for (int k = 1; k <= kx; k++)
+    for (int j = 1; j <= jx; j++)
+      for (int i = 1; i <= ix; i++) {
+        size_t c = I3(i, j, k);
+        double dmesh = fmin2(fmin2(dx[I1(i)], dy[I1(j)]), dz[I1(k)]);
+        double b2 = bx[c] * bx[c] + by[c] * by[c] + bz[c] * bz[c];
+        double ca2 = b2 * onep4 / ro[c];
+        double cs2 = gm * pr[c] / ro[c];
+        double v2 = vx[c] * vx[c] + vy[c] * vy[c] + vz[c] * vz[c];
+        double dtcfl = dmesh / sqrt(v2 + cs2 + ca2);
+        double dtwav = safety * dtcfl;
+        double dtdif = safety * 0.5 * (dmesh * dmesh) / fmax2(et[c], 1.e-10);
+        double dtq = fmin2(dtwav, dtdif);
+        if (dtq < dmin) dmin = dtq;
+      }
+  *dt = dmin;
+  *merr = 0;
+  if (*dt < dtmin) *merr = 9001;
 }
 
 /* cans3d/common/cfl_m.f:39-85; pai = acos(-1.0) is evaluated in single

@@ -166,6 +166,19 @@ void oracle_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy, double *v
                        const double *gzm, const double *dx, const double *dxm,
                        int ix, const double *dy, const double *dym, int jx,
                        const double *dz, const double *dzm, int kx);
+/* mlw_m_e (cans3d/hdmlw/mlw_m_e.f:2-3): the 3-D step with resistivity et
+ * (cells) and etm (corners); cfl_m_e (cans3d/common/cfl_m_e.f) */
+void oracle_mlw_m_e_3d(double *ro, double *pr, double *vx, double *vy, double *vz,
+                       double *bx, double *by, double *bz, double dt, double qav,
+                       double gm, const double *et, const double *etm, const double *dx,
+                       const double *dxm, int ix, const double *dy, const double *dym,
+                       int jx, const double *dz, const double *dzm, int kx);
+void oracle_cfl_m_e_3d(double *dt, double safety, double dtmin, int *merr, double gm,
+                       const double *ro, const double *pr, const double *vx,
+                       const double *vy, const double *vz, const double *bx,
+                       const double *by, const double *bz, const double *et,
+                       const double *dx, int ix, const double *dy, int jx,
+                       const double *dz, int kx);
 void oracle_cfl_m_3d(double *dt, double safety, double dtmin, int *merr,
                      double gm, const double *ro, const double *pr,
                      const double *vx, const double *vy, const double *vz,

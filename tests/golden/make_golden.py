@@ -158,6 +158,24 @@ def case_grav3(ix, jx, kx, seed):
     return out
 
 
+def case_res3(ix, jx, kx, seed):
+    """One resistive 3-D step (cans3d/hdmlw/mlw_m_e.f) of a seeded state with
+    seeded resistivity, dt from cfl_m_e (cans3d/common/cfl_m_e.f)."""
+    s = setups.random_resistivity(setups.random_state_3d(ix, jx, kx, seed=seed), seed + 1)
+    out = {"in_" + k: a for k, a in zip(s["names"], s["state"])}
+    for k in ("dx", "dxm", "dy", "dym", "dz", "dzm"):
+        out["grid_" + k] = s[k]
+    for k in ("et", "etm"):
+        out["src_" + k] = s[k]
+    st = setups.copy_state(s)
+    dt, _ = oracle.cfl_3d(s, st, 0.4)
+    oracle.step_3d(s, st, dt)
+    out["dt"] = np.array(dt)
+    for k, a in zip(s["names"], st):
+        out["out_" + k] = a
+    return out
+
+
 def bd_case():
     rng = np.random.default_rng(13)
     q = np.asfortranarray(rng.standard_normal((9, 7)))
@@ -186,6 +204,7 @@ FIXTURES = {
     "mlw_m_e_2d_18x17": lambda: case_res("mlw_m", 18, 17, 27, False),
     "mlw_m3_ge_2d_17x19": lambda: case_res("mlw_m3", 17, 19, 28, True),
     "mlw_m_g_3d_13x12x14": lambda: case_grav3(13, 12, 14, 29),
+    "mlw_m_e_3d_12x13x11": lambda: case_res3(12, 13, 11, 30),
 }
 
 

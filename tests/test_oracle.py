@@ -946,6 +946,83 @@ def test_gravity_3d_oracle_matches_frozen_fixture(oracle_lib):
         assert np.array_equal(a, z["out_" + k]), k
 
 
+# ---- 3-D resistive step (cans3d/hdmlw/mlw_m_e.f, cfl_m_e.f) -------------------
+
+def test_resistive_3d_with_zero_eta_is_the_plain_step(oracle_lib):
+    s = setups.random_state_3d(13, 12, 11, seed=4)
+    z = np.zeros(s["state"][0].shape, order="F")
+    e = dict(s, et=z, etm=z)
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    oracle_lib.step_3d(s, a, 1e-3)
+    oracle_lib.step_3d(e, b, 1e-3)
+    for k, x, y in zip(s["names"], a, b):
+        assert np.array_equal(x, y), k
+
+
+def test_resistive_3d_changes_the_step(oracle_lib):
+    s = setups.random_resistivity(setups.random_state_3d(13, 12, 11, seed=4), seed=5)
+    plain = dict(s, et=None, etm=None)
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    oracle_lib.step_3d(plain, a, 1e-3)
+    oracle_lib.step_3d(s, b, 1e-3)
+    names = s["names"]
+    for k in ("bx", "by", "bz", "pr"):
+        assert not np.array_equal(a[names.index(k)], b[names.index(k)]), k
+    assert np.array_equal(a[0], b[0])  # the density equation has no resistive term
+
+
+def test_cfl_m_e_3d_diffusion_limit(oracle_lib):
+    """cfl_m_e.f:56-67: with et = 0 (floored at 1.d-10) the wave limit of
+    cfl_m; with a large uniform et the diffusion limit
+    safety*0.5*min(dx,dy,dz)**2/et."""
+    s = setups.random_state_3d(12, 11, 10, seed=6)
+    st = s["state"]
+    z = np.zeros(st[0].shape, order="F")
+    dt0, _ = oracle_lib.cfl_3d(s, st, 0.4)
+    dte, _ = oracle_lib.cfl_3d(dict(s, et=z), st, 0.4)
+    assert dte == dt0
+    big = np.full(st[0].shape, 50.0, order="F")
+    dtb, _ = oracle_lib.cfl_3d(dict(s, et=big), st, 0.4)
+    dmin = min(s["dx"].min(), s["dy"].min(), s["dz"].min())
+    assert dtb == pytest.approx(0.4 * 0.5 * dmin * dmin / 50.0, rel=1e-15)
+
+
+def test_resistive_3d_oracle_matches_frozen_fixture(oracle_lib):
+    z = np.load(GOLD / "mlw_m_e_3d_12x13x11.npz")
+    names = setups.VARS["mlw_m_3d"]
+    st = [np.asfortranarray(z["in_" + k]) for k in names]
+    s = dict(solver="mlw_m_3d", qav=3.0, gm=5.0 / 3.0,
+             et=np.asfortranarray(z["src_et"]), etm=np.asfortranarray(z["src_etm"]),
+             **{k: z["grid_" + k] for k in ("dx", "dxm", "dy", "dym", "dz", "dzm")})
+    oracle_lib.step_3d(s, st, float(z["dt"]))
+    for k, a in zip(names, st):
+        assert np.array_equal(a, z["out_" + k]), k
+
+
+def test_reconnection_3d_stays_nearly_uniform_in_z(oracle_lib):
+    """cans3d/md_recon: the current sheet and the resistivity do not depend
+    on z and the z faces are symmetric, so the planes stay equal up to the
+    footprint of the current taken as zero on the outer layer of cells and
+    corners (the reference leaves it undefined there): after 30 iterations
+    the planes agree to 1e-3 of each field's scale, vz and bz stay below
+    1e-5 of the field strength, and the resistive sheet has set up flows."""
+    s = setups.magnetic_reconnection_3d(32, 4)
+    st = setups.copy_state(s)
+    t, ns, merr, _ = oracle_lib.run_3d(s, st, 30)
+    assert ns == 30 and merr == 0
+    g = dict(zip(s["names"], st))
+    bmax = float(np.max(np.abs(g["by"])))
+    for k, a in g.items():
+        assert np.all(np.isfinite(a)), k
+        if k in ("vz", "bz"):
+            assert np.max(np.abs(a)) < 1e-5 * bmax, k
+            continue
+        scale = float(np.max(np.abs(a)))
+        for kk in range(a.shape[2]):
+            assert np.max(np.abs(a[:, :, kk] - a[:, :, 2])) <= 1e-3 * scale, (k, kk)
+    assert np.max(np.abs(g["vx"])) > 1e-3 and np.max(np.abs(g["vy"])) > 1e-3
+
+
 def test_emerging_flux_setup_follows_the_model(oracle_lib):
     """md_efr/hdmlw/model.f: horizontally uniform stratification with the
     flux sheet bx^2/(8 pi p) = rbeta0 (1/4 inside -2 < z < 0), gravity

@@ -432,6 +432,28 @@ def mlw_m_g_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, gx, gxm, gy, gym, gz
         "mlw_m_g_3d")
 
 
+def mlw_m_e_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, et, etm, dx, dxm, dy, dym, dz,
+               dzm):
+    """cans3d/hdmlw/mlw_m_e.f:2 -- the 3-D resistive step, in place."""
+    ix, jx, kx = ro.shape
+    return _check(load().cans_mlw_m_e_3d(
+        *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz)], _dref(dt), _dref(qav),
+        _dref(gm), _ptr(et), _ptr(etm), _ptr(dx), _ptr(dxm), _iref(ix), _ptr(dy), _ptr(dym),
+        _iref(jx), _ptr(dz), _ptr(dzm), _iref(kx)), "mlw_m_e_3d")
+
+
+def cfl_m_e_3d(safety, dtmin, gm, ro, pr, vx, vy, vz, bx, by, bz, et, dx, dy, dz):
+    """cans3d/common/cfl_m_e.f:2 -- returns (dt, merr)."""
+    ix, jx, kx = ro.shape
+    dt, merr = C.c_double(0.0), C.c_int(0)
+    _check(load().cans_cfl_m_e_3d(C.byref(dt), _dref(safety), _dref(dtmin), C.byref(merr),
+                                  _dref(gm),
+                                  *[_ptr(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, et)],
+                                  _ptr(dx), _iref(ix), _ptr(dy), _iref(jx), _ptr(dz),
+                                  _iref(kx)), "cfl_m_e_3d")
+    return dt.value, merr.value
+
+
 def mlw_m_3d(ro, pr, vx, vy, vz, bx, by, bz, dt, qav, gm, dx, dxm, dy, dym, dz, dzm):
     """cans3d/hdmlw/mlw_m.f:2 -- one mLW step of the 3-D state, in place."""
     ix, jx, kx = ro.shape
@@ -596,15 +618,16 @@ class Run:
                     raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {shape}")
                 self._keep.append(a)
                 setattr(d, k, a.ctypes.data_as(_dp))
-        if not one and not three and grid.get("et") is not None:
-            # resistive 2-D step: et at the cells, etm at the corners (a
-            # missing etm stays NULL and the library rejects the set-up)
+        if not one and grid.get("et") is not None:
+            # resistive step: et at the cells, etm at the corners (a missing
+            # etm stays NULL and the library rejects the set-up)
+            shape = (nx, ny, nz) if three else (nx, ny)
             for k in ("et", "etm"):
                 if grid.get(k) is None:
                     continue
                 a = np.asfortranarray(grid[k], dtype=np.float64)
-                if a.shape != (nx, ny):
-                    raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {(nx, ny)}")
+                if a.shape != shape:
+                    raise CansError(CANS_ERR_ARG, k, f"{k} must have shape {shape}")
                 self._keep.append(a)
                 setattr(d, k, a.ctypes.data_as(_dp))
         if bgv:

@@ -107,6 +107,24 @@ cudaError_t launch_mlw3d_g(bool exact, int tile, const double *A, double *B, int
                            const Phys &ph, const double *grav, double dt, Ctl *ctl,
                            Box3 box, cudaStream_t s);
 int mlw3d_tile_count();
+// 3-D mlw_m_e, the step kernel part (mlw3d.cu): res = et*J at the cells and
+// etm*Jh at the corners (x, y, z each, n doubles per component)
+cudaError_t launch_mlw3d_res(bool exact, int tile, const double *A, double *B, int ix,
+                             int jx, int kx, const Axis &ax, const Axis &ay, const Axis &az,
+                             const Phys &ph, const double *res, double dt, Ctl *ctl,
+                             Box3 box, cudaStream_t s);
+// 3-D mlw_m_e (mlw3d_e.cu): eta = et, etm (n each); res scratch of
+// mlw3d_e_scratch_doubles doubles; the tile as launch_mlw3d_res
+size_t mlw3d_e_scratch_doubles(int ix, int jx, int kx);
+cudaError_t launch_mlw3d_e(bool exact, int tile, const double *A, double *B, int ix, int jx,
+                           int kx, const Axis &ax, const Axis &ay, const Axis &az,
+                           const Phys &ph, const double *eta, double *res, double dt,
+                           Ctl *ctl, Box3 box, cudaStream_t s);
+// cfl_m_e 3-D: min over the cells of the wave (wave = 1) and diffusion limits
+cudaError_t launch_cfl3d_e(bool exact, const double *S, int ix, int jx, int kx,
+                           const Axis &ax, const Axis &ay, const Axis &az, const Phys &ph,
+                           const double *et, double safety, int wave,
+                           unsigned long long *out_bits, cudaStream_t s);
 cudaError_t launch_cfl3d_full(bool exact, const double *S, int ix, int jx,
                               int kx, const Axis &ax, const Axis &ay,
                               const Axis &az, const Phys &ph, double safety,

@@ -974,16 +974,18 @@ extern "C" int cans_bdfrdx_1d(const int *mbnd, const int *margin, double *qq,
 // 3-D drop-in entry points
 namespace {
 // One 3-D mLW step on host arrays or their registered mirrors; with grav
-// (gx, gxm, gy, gym, gz, gzm host arrays) the step with gravity.
+// (gx, gxm, gy, gym, gz, gzm host arrays) the step with gravity, with eta
+// (et, etm host arrays) the resistive step.
 int step3d(double *const *arrs, double dt, double qav, double gm, const double *dx,
            const double *dxm, int nx, const double *dy, const double *dym, int ny,
            const double *dz, const double *dzm, int nz,
-           const double *const *grav = nullptr) {
+           const double *const *grav = nullptr, const double *const *eta = nullptr) {
   NvtxRange nvtx("mLW 3-D drop-in step");
   if (nx < 3 || ny < 3 || nz < 3) return CANS_ERR_ARG;
   if (grav)
     for (int k = 0; k < 6; k++)
       if (!grav[k]) return CANS_ERR_ARG;
+  if (eta && (!eta[0] || !eta[1])) return CANS_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
   int rc = lib_stream(&s);
@@ -998,7 +1000,12 @@ int step3d(double *const *arrs, double dt, double qav, double gm, const double *
   if ((rc = day->upload(ny, dy, dym, s))) return rc;
   if ((rc = daz->upload(nz, dz, dzm, s))) return rc;
   if (grav && (rc = sc.upload_grav(grav, n, s, 6))) return rc;
+  if (eta && (rc = sc.upload_eta(eta, 2, n, mlw3d_e_scratch_doubles(nx, ny, nz), s)))
+    return rc;
   auto step = [&](const double *A, double *B) {
+    if (eta)
+      return launch_mlw3d_e(exact_mode(), 0, A, B, nx, ny, nz, dax->a, day->a, daz->a, ph,
+                            sc.eta, sc.res, dt, nullptr, Box3{}, s);
     return grav ? launch_mlw3d_g(exact_mode(), 0, A, B, nx, ny, nz, dax->a, day->a, daz->a,
                                  ph, sc.grav, dt, nullptr, Box3{}, s)
                 : launch_mlw3d(exact_mode(), 0, A, B, nx, ny, nz, dax->a, day->a, daz->a,
@@ -1051,23 +1058,33 @@ extern "C" int cans_mlw_m_g_3d(double *ro, double *pr, double *vx, double *vy,
   return step3d(arrs, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, dz, dzm, *kx, grav);
 }
 
-extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
-                             const double *dtmin, int *merr, const double *gm,
-                             const double *ro, const double *pr,
-                             const double *vx, const double *vy,
-                             const double *vz, const double *bx,
-                             const double *by, const double *bz,
-                             const double *dx, const int *ix,
-                             const double *dy, const int *jx,
-                             const double *dz, const int *kx) {
-  const int nx = *ix, ny = *jx, nz = *kx;
+// mlw_m_e (cans3d/hdmlw/mlw_m_e.f:2-3): the 3-D resistive step
+extern "C" int cans_mlw_m_e_3d(double *ro, double *pr, double *vx, double *vy,
+                               double *vz, double *bx, double *by, double *bz,
+                               const double *dt, const double *qav,
+                               const double *gm, const double *et,
+                               const double *etm, const double *dx,
+                               const double *dxm, const int *ix,
+                               const double *dy, const double *dym,
+                               const int *jx, const double *dz,
+                               const double *dzm, const int *kx) {
+  double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  const double *eta[2] = {et, etm};
+  return step3d(arrs, *dt, *qav, *gm, dx, dxm, *ix, dy, dym, *jx, dz, dzm, *kx, nullptr,
+                eta);
+}
+
+namespace {
+// cfl_m (et == nullptr) and cfl_m_e 3-D on host arrays or their mirrors
+int cfl3d(double *dt, double safety, double dtmin, int *merr, double gm,
+          const double *const *arrs, const double *et, const double *dx, int nx,
+          const double *dy, int ny, const double *dz, int nz) {
   if (nx < 1 || ny < 1 || nz < 1) return CANS_ERR_ARG;
-  const double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
   std::lock_guard<std::mutex> lk(g_mu);
   cudaStream_t s;
   int rc = lib_stream(&s);
   if (rc) return rc;
-  const Phys ph = make_phys(*gm, 0.0);
+  const Phys ph = make_phys(gm, 0.0);
   const size_t n = (size_t)nx * ny * nz;
   MirrorSet *m = resident_step_set(const_cast<double *const *>(arrs), 8);
   Scratch &sc = g_scratch;
@@ -1076,6 +1093,7 @@ extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
   if ((rc = dax->upload(nx, dx, dx, s))) return rc;
   if ((rc = day->upload(ny, dy, dy, s))) return rc;
   if ((rc = daz->upload(nz, dz, dz, s))) return rc;
+  if (et && (rc = sc.upload_eta(&et, 1, n, 0, s))) return rc;
   const double *base;
   unsigned long long *bits;
   if (m) {
@@ -1094,14 +1112,48 @@ extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
   unsigned long long init;
   std::memcpy(&init, &d0, sizeof init);
   CK(cudaMemcpyAsync(bits, &init, sizeof init, cudaMemcpyHostToDevice, s));
-  CK(launch_cfl3d_full(exact_mode(), base, nx, ny, nz, dax->a, day->a, daz->a,
-                       ph, *safety, bits, s));
+  if (et)
+    CK(launch_cfl3d_e(exact_mode(), base, nx, ny, nz, dax->a, day->a, daz->a, ph,
+                      g_scratch.eta, safety, 1, bits, s));
+  else
+    CK(launch_cfl3d_full(exact_mode(), base, nx, ny, nz, dax->a, day->a, daz->a,
+                         ph, safety, bits, s));
   unsigned long long out = 0;
   CK(cudaMemcpyAsync(&out, bits, sizeof out, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   *dt = bits_to_double(out);
-  *merr = (*dt < *dtmin) ? 9001 : 0;
+  *merr = (*dt < dtmin) ? 9001 : 0;
   return CANS_OK;
+}
+}  // namespace
+
+extern "C" int cans_cfl_m_3d(double *dt, const double *safety,
+                             const double *dtmin, int *merr, const double *gm,
+                             const double *ro, const double *pr,
+                             const double *vx, const double *vy,
+                             const double *vz, const double *bx,
+                             const double *by, const double *bz,
+                             const double *dx, const int *ix,
+                             const double *dy, const int *jx,
+                             const double *dz, const int *kx) {
+  const double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  return cfl3d(dt, *safety, *dtmin, merr, *gm, arrs, nullptr, dx, *ix, dy, *jx, dz, *kx);
+}
+
+// cfl_m_e (cans3d/common/cfl_m_e.f:2-4): the 3-D time step with the
+// diffusion limit of the resistivity et
+extern "C" int cans_cfl_m_e_3d(double *dt, const double *safety,
+                               const double *dtmin, int *merr, const double *gm,
+                               const double *ro, const double *pr,
+                               const double *vx, const double *vy,
+                               const double *vz, const double *bx,
+                               const double *by, const double *bz,
+                               const double *et, const double *dx, const int *ix,
+                               const double *dy, const int *jx,
+                               const double *dz, const int *kx) {
+  if (!et) return CANS_ERR_ARG;
+  const double *arrs[8] = {ro, pr, vx, vy, vz, bx, by, bz};
+  return cfl3d(dt, *safety, *dtmin, merr, *gm, arrs, et, dx, *ix, dy, *jx, dz, *kx);
 }
 
 // roe_m (cans3d/hdroe/roe_m.f:2): one Roe-MUSCL step, on the registered
@@ -1404,7 +1456,7 @@ struct cans_run {
   Loop1D loop1d{};             // 1-D loop options (device pointers into bx1)
   double *roe = nullptr;       // Roe / HLLD: stage scratch
   double *grav = nullptr;      // mLW with gravity: gx gxm gy gym (gz gzm), n each
-  double *eta = nullptr;       // 2-D mLW with resistivity: et, etm (n each)
+  double *eta = nullptr;       // mLW with resistivity: et, etm (n each)
   double *res = nullptr;       //   and the eta*J fields of each step
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
@@ -1442,7 +1494,8 @@ int layout2d(const cans_run *h) {
 }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
-  if (is_roe(h) || is_hlld(h) || h->ndim == 1 || h->eta) return 1;
+  if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
+  if (h->eta) return h->ndim == 3 ? mlw3d_tile_count() : 1;
   if (h->grav) return h->ndim == 3 ? mlw3d_g_tile_count() : mlw2d_g_tile_count();
   return h->ndim == 3 ? mlw3d_tile_count() : mlw2d_tile_count();
 }
@@ -1488,6 +1541,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (is_roe(h))
     return launch_roe3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
+  if (h->ndim == 3 && h->eta)
+    return launch_mlw3d_e(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
+                          h->ay.a, h->az.a, h->ph, h->eta, h->res, dt, ctl, box, h->s);
   if (h->ndim == 3 && h->grav)
     return launch_mlw3d_g(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
                           h->ay.a, h->az.a, h->ph, h->grav, dt, ctl, box, h->s);
@@ -1524,6 +1580,9 @@ cudaError_t frame_kernel(cans_run *h) {
 }
 cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
                             unsigned long long *bits) {
+  if (h->ndim == 3 && h->eta)
+    return launch_cfl3d_e(h->d.exact != 0, S, h->d.ix, h->d.jx, h->d.kx, h->ax.a, h->ay.a,
+                          h->az.a, h->ph, h->eta, safety, 1, bits, h->s);
   if (h->ndim == 3)
     return launch_cfl3d_full(h->d.exact != 0, S, h->d.ix, h->d.jx, h->d.kx,
                              h->ax.a, h->ay.a, h->az.a, h->ph, safety, bits, h->s);
@@ -1638,9 +1697,12 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
   if (grav3d && (!d->gxm || !d->gy || !d->gym || !d->gz || !d->gzm)) return CANS_ERR_ARG;
   // a solver without a gravity step refuses the fields instead of ignoring them
   if ((d->gx || d->gy) && !(grav2d || grav3d || bgv)) return CANS_ERR_ARG;
-  // 2-D mLW with et set: the resistive steps (mlw_m_e / mlw_m3_e)
+  // mLW with et set: the resistive steps (2-D mlw_m_e / mlw_m3_e, with or
+  // without gravity; 3-D mlw_m_e, which has no gravity variant)
   const bool eta2d = mlw2d && d->et != nullptr;
-  if ((d->et || d->etm) && !(eta2d && d->etm)) return CANS_ERR_ARG;
+  const bool eta3d = d->solver == CANS_SOLVER_MLW_M_3D && d->et != nullptr;
+  if ((d->et || d->etm) && !((eta2d || eta3d) && d->etm)) return CANS_ERR_ARG;
+  if (eta3d && grav3d) return CANS_ERR_ARG;
   const double *prof[10] = {d->gx, d->gxm, d->sc, d->scm, d->dsc,
                             d->dscm, d->rr, d->rrm, d->drr, d->drrm};
   if (ndim == 1) {
@@ -1736,17 +1798,18 @@ extern "C" int cans_run_create(cans_run **out, const cans_run_desc *d) {
     if (e != cudaSuccess) return bail(fail_cuda(e, "gravity fields"));
     h->tile = d->tile >= 0 && d->tile < tile_count(h) ? d->tile : 0;
   }
-  if (eta2d) {  // mlw_m_e / mlw_m3_e: et, etm and the eta*J scratch
+  if (eta2d || eta3d) {  // mlw_m_e / mlw_m3_e: et, etm and the eta*J scratch
+    const size_t nres = eta3d ? mlw3d_e_scratch_doubles(d->ix, d->jx, d->kx)
+                              : mlw2d_e_scratch_doubles(d->solver, d->ix, d->jx);
     e = cudaMalloc(&h->eta, sizeof(double) * 2 * h->n);
-    if (e == cudaSuccess)
-      e = cudaMalloc(&h->res, sizeof(double) * mlw2d_e_scratch_doubles(d->solver, d->ix, d->jx));
+    if (e == cudaSuccess) e = cudaMalloc(&h->res, sizeof(double) * nres);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h->eta, d->et, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(h->eta + h->n, d->etm, sizeof(double) * h->n,
                           cudaMemcpyHostToDevice, h->s);
     if (e != cudaSuccess) return bail(fail_cuda(e, "resistivity fields"));
-    h->tile = 0;
+    h->tile = d->tile >= 0 && d->tile < tile_count(h) ? d->tile : 0;
   }
   for (int a = 0; a < 3; a++) h->mfdim[a] = mfdim[a];
   h->mu = d->mu > 0.0 ? d->mu : 1.0;
@@ -1861,7 +1924,11 @@ extern "C" int cans_run_start(cans_run *h, double t0, double tend,
   h->host_ctl = c;
   CK(cudaMemcpyAsync(h->ctl, &h->host_ctl, sizeof(Ctl), cudaMemcpyHostToDevice,
                      h->s));
-  if (h->eta)  // the diffusion limit depends on et, the mesh and safety only
+  if (h->eta && h->ndim == 3)  // the diffusion limit: et, the mesh and safety only
+    CK(launch_cfl3d_e(h->d.exact != 0, h->buf[c.cur], h->d.ix, h->d.jx, h->d.kx, h->ax.a,
+                      h->ay.a, h->az.a, h->ph, h->eta, safety, 0, &h->ctl->dtdif_bits,
+                      h->s));
+  else if (h->eta)
     CK(launch_cfl2d_e(h->d.solver, h->d.exact != 0, h->buf[c.cur], h->d.ix, h->d.jx,
                       h->ax.a, h->ay.a, h->ph, h->eta, safety, 0, &h->ctl->dtdif_bits,
                       h->s));

@@ -21,8 +21,8 @@
 //
 // The reference leaves J undefined on the outer ring of cells (bbtocz
 // writes 2..ix-1, 2..jx-1) and reads, for corner ix-1, the half-step B of
-// corner ix, which mlwhalf never sets.  Both are taken as zero; the
-// resistivity of md_recon and md_reccnd vanishes there.
+// corner ix, which mlwhalf never sets.  Both are taken as zero (the
+// reference reads uninitialised memory there).
 #include <cuda_runtime.h>
 
 #include "cans_common.cuh"

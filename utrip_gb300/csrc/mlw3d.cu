@@ -23,6 +23,11 @@
 // of their own and enter the energy and the three momenta through mlwsrch
 // (cans3d/hdmlw/mlwsrch.f:32-50) and mlwsrcf (mlwsrcf.f:35-45).  grav holds
 // gx, gxm, gy, gym, gz, gzm (ix*jx*kx each; the *m fields at the corners).
+//
+// With R the kernel is mlw_m_e (cans3d/hdmlw/mlw_m_e.f:103-115, 257-270): res
+// holds eta J at the cells (x, y, z) and at the corners (x, y, z), ix*jx*kx
+// each, computed beforehand by the kernels of mlw3d_e.cu, and each is added
+// to E = -v x B where the reference adds et*c and etm*ch.
 #include <cuda_runtime.h>
 
 #include "cans_common.cuh"
@@ -98,10 +103,11 @@ __device__ __forceinline__ void corner_flux_src(int v, int dir, int &f, bool &ne
 
 // Cell stage: primitives of one cell -> conserved variables, E and the
 // cell fluxes of cans3d/hdmlw/mlw_m.f:74-202, into one ring slot.
-template <bool E>
+template <bool E, bool R = false>
 __device__ __forceinline__ void cell_stage(const double *__restrict__ A,
                                            size_t n, size_t g, double *sl,
-                                           int NC, int c, const Phys &ph) {
+                                           int NC, int c, const Phys &ph,
+                                           const double *__restrict__ res = nullptr) {
   using FT = F<E>;
   const FT gm(ph.gm), gm1(ph.gm1), pi8i(ph.pi8i), pi4i(ph.pi4i);
   const FT ro(A[P3::RO * n + g]), pr(A[P3::PR * n + g]);
@@ -117,9 +123,14 @@ __device__ __forceinline__ void cell_stage(const double *__restrict__ A,
     ee = pr * ph.gm1i + 0.5 * ro * vv + pi8i * bb;
     ep = pr * ph.ggm1 + 0.5 * ro * vv;
   }
-  const FT ex = -vy * bz + vz * by;
-  const FT ey = -vz * bx + vx * bz;
-  const FT ez = -vx * by + vy * bx;
+  FT ex = -vy * bz + vz * by;
+  FT ey = -vz * bx + vx * bz;
+  FT ez = -vx * by + vy * bx;
+  if constexpr (R) {  // mlw_m_e.f:110-115
+    ex = ex + FT(res[g]);
+    ey = ey + FT(res[n + g]);
+    ez = ez + FT(res[2 * n + g]);
+  }
 #define S(f) sl[(size_t)(f) * NC + c]
   S(C3::RO) = ro.v; S(C3::EE) = ee.v;
   S(C3::RX) = (ro * vx).v; S(C3::RY) = (ro * vy).v; S(C3::RZ) = (ro * vz).v;
@@ -143,12 +154,13 @@ __device__ __forceinline__ void cell_stage(const double *__restrict__ A,
 
 }  // namespace
 
-template <bool E, int TX, int TY, bool G = false>
+template <bool E, int TX, int TY, bool G = false, bool R = false>
 __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     k_mlw3d(const double *__restrict__ A, double *__restrict__ B, int ix,
             int jx, int kx, Axis ax, Axis ay, Axis az, Phys ph, double dt_arg,
             Ctl *__restrict__ ctl, Box3 box, int kchunk,
-            const double *__restrict__ grav = nullptr) {
+            const double *__restrict__ grav = nullptr,
+            const double *__restrict__ res = nullptr) {
   using T = Tile3<TX, TY, G>;
   using FT = F<E>;
   extern __shared__ double smem[];
@@ -190,7 +202,7 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     double *sl = cslot(k);
     if (in_arr) {
       const size_t g = (size_t)gi + (size_t)gj * ix + (size_t)k * plane;
-      cell_stage<E>(A, n, g, sl, T::NC, tid, ph);
+      cell_stage<E, R>(A, n, g, sl, T::NC, tid, ph, res);
       if constexpr (G) {  // mlw_m_g.f:135-136, 154, 172, 190
         const FT ro(sl[(size_t)C3::RO * T::NC + tid]);
         const FT vx(sl[(size_t)C3::VX * T::NC + tid]), vy(sl[(size_t)C3::VY * T::NC + tid]);
@@ -338,9 +350,15 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     const FT vv = vxh * vxh + vyh * vyh + vzh * vzh;
     const FT bb = bxh * bxh + byh * byh + bzh * bzh;
     const FT prh = gm1 * (eeh - 0.5 * roh * vv - pi8i * bb);
-    const FT exh = -vyh * bzh + vzh * byh;
-    const FT eyh = -vzh * bxh + vxh * bzh;
-    const FT ezh = -vxh * byh + vyh * bxh;
+    FT exh = -vyh * bzh + vzh * byh;
+    FT eyh = -vzh * bxh + vxh * bzh;
+    FT ezh = -vxh * byh + vyh * bxh;
+    if constexpr (R) {  // mlw_m_e.f:264-269
+      const size_t gc = (size_t)a + (size_t)b * ix + (size_t)k * plane;
+      exh = exh + FT(res[3 * n + gc]);
+      eyh = eyh + FT(res[4 * n + gc]);
+      ezh = ezh + FT(res[5 * n + gc]);
+    }
     FT ep;
     if constexpr (E) ep = prh * gm / gm1 + 0.5 * roh * vv;
     else ep = prh * ph.ggm1 + 0.5 * roh * vv;
@@ -690,15 +708,16 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
 }
 
 namespace {
-template <bool E, int TX, int TY, bool G = false>
+template <bool E, int TX, int TY, bool G = false, bool R = false>
 cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
                     const Axis &ax, const Axis &ay, const Axis &az,
                     const Phys &ph, double dt, Ctl *ctl, Box3 box, int kchunk,
-                    cudaStream_t s, const double *grav = nullptr) {
+                    cudaStream_t s, const double *grav = nullptr,
+                    const double *res = nullptr) {
   using T = Tile3<TX, TY, G>;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY, G>,
+    cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY, G, R>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)T::smem_bytes);
     if (e != cudaSuccess) return e;
@@ -707,8 +726,8 @@ cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
   dim3 grid((ix - 2 + TX - 1) / TX, (jx - 2 + TY - 1) / TY,
             (kx - 2 + kchunk - 1) / kchunk);
   dim3 block(T::NT);
-  k_mlw3d<E, TX, TY, G><<<grid, block, T::smem_bytes, s>>>(A, B, ix, jx, kx, ax, ay, az,
-                                                          ph, dt, ctl, box, kchunk, grav);
+  k_mlw3d<E, TX, TY, G, R><<<grid, block, T::smem_bytes, s>>>(
+      A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box, kchunk, grav, res);
   count_launch();
   return cudaGetLastError();
 }
@@ -743,6 +762,24 @@ cudaError_t launch_mlw3d_g(bool exact, int tile, const double *A, double *B, int
 }
 
 int mlw3d_tile_count() { return 3; }
+
+// The step of mlw_m_e given the eta J fields res (6 arrays): the plain step's
+// tiles (no extra shared memory).
+cudaError_t launch_mlw3d_res(bool exact, int tile, const double *A, double *B, int ix,
+                             int jx, int kx, const Axis &ax, const Axis &ay, const Axis &az,
+                             const Phys &ph, const double *res, double dt, Ctl *ctl,
+                             Box3 box, cudaStream_t s) {
+  const int kchunk = (tile == 1) ? 32 : 64;
+  if (tile == 2)
+    return exact ? launch3<true, 16, 8, false, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt,
+                                                     ctl, box, kchunk, s, nullptr, res)
+                 : launch3<false, 16, 8, false, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt,
+                                                      ctl, box, kchunk, s, nullptr, res);
+  return exact ? launch3<true, 16, 16, false, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl,
+                                                    box, kchunk, s, nullptr, res)
+               : launch3<false, 16, 16, false, true>(A, B, ix, jx, kx, ax, ay, az, ph, dt,
+                                                     ctl, box, kchunk, s, nullptr, res);
+}
 
 cudaError_t launch_mlw3d(bool exact, int tile, const double *A, double *B,
                          int ix, int jx, int kx, const Axis &ax,

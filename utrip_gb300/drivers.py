@@ -85,6 +85,10 @@ def _cfl(setup, state, safety):
     if setup["solver"] in ("mlw_m_1d", "mlw_m_bg_1d", "roe_m_1d"):
         return capi.cfl_m_1d(safety, setup["dtmin"], setup["gm"], setup["bx"], *state,
                              setup["dx"])
+    if setup["solver"] == "mlw_m_3d" and setup.get("et") is not None:  # cfl_m_e 3-D
+        return capi.cfl_m_e_3d(safety, setup["dtmin"], setup["gm"], *state,
+                               np.asfortranarray(setup["et"]), setup["dx"], setup["dy"],
+                               setup["dz"])
     if setup["solver"] in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
         return capi.cfl_m_3d(safety, setup["dtmin"], setup["gm"], *state, setup["dx"],
                              setup["dy"], setup["dz"])
@@ -125,6 +129,11 @@ def _step(setup, state, dt):
         capi.hlld_engine_3d(*state, setup["gm"], setup["mu"], dt, setup["dx"], setup["dxm"],
                             setup["dy"], setup["dym"], setup["dz"], setup["dzm"],
                             setup["mfdim"])
+        return
+    if setup.get("et") is not None and setup["solver"] == "mlw_m_3d":  # 3-D mlw_m_e
+        e = [np.asfortranarray(setup[k]) for k in ("et", "etm")]
+        capi.mlw_m_e_3d(*state, dt, setup["qav"], setup["gm"], *e, setup["dx"], setup["dxm"],
+                        setup["dy"], setup["dym"], setup["dz"], setup["dzm"])
         return
     if setup.get("et") is not None:  # mlw_m3_e / mlw_m_e, with gravity _ge
         e = [np.asfortranarray(setup[k]) for k in ("et", "etm")]

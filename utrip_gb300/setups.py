@@ -763,9 +763,9 @@ def random_gravity(s: dict, seed: int = 0, scale: float = 0.3) -> dict:
 
 
 def random_resistivity(s: dict, seed: int = 0, scale: float = 0.02) -> dict:
-    """Seeded non-negative resistivity on a 2-D set-up (et at the cells, etm
-    at the corners, every resistive term of mlw_m_e / mlw_m3_e non-zero):
-    returns a copy with et and etm."""
+    """Seeded non-negative resistivity on a 2-D or 3-D set-up (et at the
+    cells, etm at the corners, every resistive term of mlw_m_e / mlw_m3_e or
+    of the 3-D mlw_m_e non-zero): returns a copy with et and etm."""
     rng = np.random.default_rng(seed)
     shape = s["state"][0].shape
     out = dict(s)
@@ -836,6 +836,72 @@ def magnetic_reconnection(n: int = 128):
             bc.append((v, face, BD_SPN if name in odd[face] else BD_SPP, 0.0))
     s = _pack("mlw_m", x, dx, dxm, y, dy, dym, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
               tend=23.0, dtout=1.0, margin=margin, name=f"magnetic_reconnection_{n}")
+    s["et"] = np.asfortranarray(et)
+    s["etm"] = np.asfortranarray(etm)
+    return s
+
+
+def magnetic_reconnection_3d(n: int = 128, nz: int = 4):
+    """The 3-D magnetic-reconnection model of cans3d/md_recon/hdmlw (model.f,
+    bnd.f, main.f:167-186): the current sheet of the 2-D model (x in [0, 5],
+    y in [0, 20]) extended over z in [0, 2], n x n x nz cells with two ghost
+    layers, the same localised resistivity in every z plane, cfl_m_e ->
+    mlw_m_e -> bnd with safety 0.4, qav 3, tend 23.  Boundaries (bnd.f): at
+    x = 0 vx, by, bz odd; at the outer x face vx, bx odd; at y = 0 vy, bx, bz
+    odd; at the outer y face vy, vz, bx odd; at both z faces vz, bz odd; the
+    other variables even."""
+    margin = 2
+    ix = jx = n + 2 * margin
+    kx = nz + 2 * margin
+    gm = 5.0 / 3.0
+    pi = math.acos(-1.0)
+
+    def axis(length, nn):
+        d0 = length / float(nn - margin * 2)
+        dm = np.full(nn, d0)
+        iz = margin + 1
+        c = np.empty(nn)
+        c[iz - 1] = dm[iz - 1] / 2.0
+        for i in range(iz + 1, nn + 1):
+            c[i - 1] = c[i - 2] + dm[i - 2]
+        for i in range(iz - 1, 0, -1):
+            c[i - 1] = c[i] - dm[i - 1]
+        return c, dm
+
+    x, dxm0 = axis(5.0, ix)
+    y, dym0 = axis(20.0, jx)
+    z, _ = axis(2.0, kx)
+    X, Y, _ = np.meshgrid(x, y, z, indexing="ij")
+    etai, retai = 0.03, 0.8
+
+    def eta(rr):
+        # etai*(2*rr**3-3*retai*rr**2)/retai**3+etai (model.f:67-74), integer
+        # powers as repeated products
+        r3 = rr * rr * rr
+        v = etai * (2.0 * r3 - (3.0 * retai) * (rr * rr)) / (retai * retai * retai) + etai
+        return np.where(rr < retai, v, 0.0)
+
+    et = eta(np.sqrt(X * X + Y * Y))
+    Xm = X + (dxm0 / 2.0)[:, None, None]
+    Ym = Y + (dym0 / 2.0)[None, :, None]
+    etm = eta(np.sqrt(Xm * Xm + Ym * Ym))
+    betai = 10.0
+    by = np.sqrt(betai * pi * 8 / gm) * np.tanh(X / 0.5)
+    pr = 1 / gm * (1 + betai) - by * by / pi / 8.0
+    zero = np.zeros(X.shape)
+    f = {"ro": pr * gm, "pr": pr, "vx": zero, "vy": zero, "vz": zero, "bx": zero, "by": by,
+         "bz": zero}
+    dx, _, dxm = grdrdy(x)
+    dy, _, dym = grdrdy(y)
+    dz, _, dzm = grdrdy(z)
+    names = VARS["mlw_m_3d"]
+    odd = {0: ("vx", "by", "bz"), 1: ("vx", "bx"), 2: ("vy", "bx", "bz"),
+           3: ("vy", "vz", "bx"), 4: ("vz", "bz"), 5: ("vz", "bz")}
+    bc = [(v, face, BD_SPN if name in odd[face] else BD_SPP, 0.0)
+          for face in range(6) for v, name in enumerate(names)]
+    s = _pack3(x, dx, dxm, y, dy, dym, z, dz, dzm, f, gm, 3.0, bc, safety=0.4, dtmin=1e-10,
+               tend=23.0, dtout=1.0, margin=margin,
+               name=f"magnetic_reconnection_{n}x{n}x{nz}")
     s["et"] = np.asfortranarray(et)
     s["etm"] = np.asfortranarray(etm)
     return s
