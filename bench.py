@@ -53,7 +53,8 @@ def parse():
                    help="skip the secondary 3-D and 1-D workloads")
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
-                            "gravity2d", "resistive2d", "gravity3d", "spicule"],
+                            "gravity2d", "resistive2d", "gravity3d", "resistive3d",
+                            "spicule"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
@@ -84,8 +85,9 @@ def profile_case(case, n):
         st = run.query()
         run.close()
         out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
-    elif case == "gravity3d":
-        s = setups.emerging_flux_3d(n, max(2, n // 4), n)
+    elif case in ("gravity3d", "resistive3d"):
+        s = (setups.emerging_flux_3d(n, max(2, n // 4), n) if case == "gravity3d"
+             else setups.magnetic_reconnection_3d(n, max(4, n // 4)))
         run = drivers.make_run(s)
         run.push(s["state"])
         run.start(nstop=3, safety=s["safety"], dtmin=s["dtmin"])
@@ -198,6 +200,9 @@ def extra_workloads(stream, exact=False):
         "emerging-flux model")
     out["reconnection_512^2_mlw_m_e"] = loop_2d(
         stream, exact, setups.magnetic_reconnection, 512, 100, 256, 500, "reconnection model")
+    out["reconnection_256x256x64_mlw_m_e"] = loop_3d(
+        stream, exact, lambda nx, ny, nz: setups.magnetic_reconnection_3d(nx, nz),
+        (256, 256, 64), 20, (96, 96, 16), 50, "3-D reconnection model")
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
     out["spicule_1024_100000_steps_mlw_m_bg"] = spicule_workload(stream)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
