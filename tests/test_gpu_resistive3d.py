@@ -114,6 +114,24 @@ def test_reconnection_loop_exact_bitwise(gpu, oracle_lib, tile):
     assert_same(s["names"], got, ref, f"reconnection 3-D tile {tile}")
 
 
+def test_reconnection_reference_size_loop_exact_bitwise(gpu, oracle_lib):
+    """md_recon 3-D at the reference's 128 x 128 x 4 (main.f:6): 60
+    iterations of cfl_m_e -> mlw_m_e -> bnd on the device, autotuned tile."""
+    s = setups.magnetic_reconnection_3d(128, 4)
+    ref = setups.copy_state(s)
+    t, ns, merr, _ = oracle.run_3d(s, ref, 60)
+    got = setups.copy_state(s)
+    run = drivers.make_run(s, exact=True)
+    try:
+        run.push(got)
+        run.autotune(1)
+        out = drivers.run_resident(s, got, 60, run=run)
+    finally:
+        run.close()
+    assert out == (t, ns, merr, ns)
+    assert_same(s["names"], got, ref, "reconnection 3-D 128x128x4")
+
+
 def test_reconnection_literal_loop_equals_oracle(gpu, oracle_lib):
     s = setups.magnetic_reconnection_3d(24, 6)
     ref = setups.copy_state(s)
