@@ -708,6 +708,28 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
 }
 
 namespace {
+// The z chunk (at most kmax planes) that fills the GPU best: a launch of b
+// blocks with `slots` resident at a time takes ceil(b / slots) waves, and a
+// block of kc planes costs about kc + 1 plane steps (its prologue loads two
+// planes).  The partition into chunks does not change any result.
+int balance_kchunk(long long bxy, int nz, int kmax, int slots) {
+  if (nz < 1 || kmax < 1 || slots < 1) return kmax;
+  const int c0 = (nz + kmax - 1) / kmax;
+  int best = kmax;
+  long long best_cost = -1;
+  for (int c = c0; c <= nz && c <= 4 * c0 + 8; c++) {
+    const int kc = (nz + c - 1) / c;
+    const long long chunks = (nz + kc - 1) / kc;
+    const long long waves = (bxy * chunks + slots - 1) / slots;
+    const long long cost = waves * (kc + 1);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = kc;
+    }
+  }
+  return best;
+}
+
 template <bool E, int TX, int TY, bool G = false, bool R = false>
 cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
                     const Axis &ax, const Axis &ay, const Axis &az,
@@ -716,15 +738,25 @@ cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
                     const double *res = nullptr) {
   using T = Tile3<TX, TY, G>;
   static bool attr = false;
+  static int slots = 0;  // resident blocks on the whole GPU
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY, G, R>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)T::smem_bytes);
     if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+             &per_sm, k_mlw3d<E, TX, TY, G, R>, T::NT, T::smem_bytes)) != cudaSuccess)
+      return e;
+    slots = sms * (per_sm > 0 ? per_sm : 1);
     attr = true;
   }
-  dim3 grid((ix - 2 + TX - 1) / TX, (jx - 2 + TY - 1) / TY,
-            (kx - 2 + kchunk - 1) / kchunk);
+  const int bx = (ix - 2 + TX - 1) / TX, by = (jx - 2 + TY - 1) / TY;
+  kchunk = balance_kchunk((long long)bx * by, kx - 2, kchunk, slots);
+  dim3 grid(bx, by, (kx - 2 + kchunk - 1) / kchunk);
   dim3 block(T::NT);
   k_mlw3d<E, TX, TY, G, R><<<grid, block, T::smem_bytes, s>>>(
       A, B, ix, jx, kx, ax, ay, az, ph, dt, ctl, box, kchunk, grav, res);
