@@ -243,6 +243,20 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     const double *L = cslot(k), *U = cslot(k + 1);
     const int p00 = cx + cy * T::CX, p10 = p00 + 1, p01 = p00 + T::CX,
               p11 = p01 + 1;
+    // global operands of this corner, loaded before the predictor so that
+    // their latency overlaps its arithmetic
+    const size_t gc = (size_t)a + (size_t)b * ix + (size_t)k * plane;
+    double rq[3] = {0.0, 0.0, 0.0}, gq[3] = {0.0, 0.0, 0.0};
+    if constexpr (R) {
+      rq[0] = res[3 * n + gc];
+      rq[1] = res[4 * n + gc];
+      rq[2] = res[5 * n + gc];
+    }
+    if constexpr (G) {
+      gq[0] = grav[n + gc];
+      gq[1] = grav[3 * n + gc];
+      gq[2] = grav[5 * n + gc];
+    }
     const FT dxim(ax.dim[a]), dyim(ay.dim[b]), dzim(az.dim[k]);
     FT un[8];
     if constexpr (!E) {  // same predictor, fewer rounded operations
@@ -354,10 +368,9 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     FT eyh = -vzh * bxh + vxh * bzh;
     FT ezh = -vxh * byh + vyh * bxh;
     if constexpr (R) {  // mlw_m_e.f:264-269
-      const size_t gc = (size_t)a + (size_t)b * ix + (size_t)k * plane;
-      exh = exh + FT(res[3 * n + gc]);
-      eyh = eyh + FT(res[4 * n + gc]);
-      ezh = ezh + FT(res[5 * n + gc]);
+      exh = exh + FT(rq[0]);
+      eyh = eyh + FT(rq[1]);
+      ezh = ezh + FT(rq[2]);
     }
     FT ep;
     if constexpr (E) ep = prh * gm / gm1 + 0.5 * roh * vv;
@@ -381,8 +394,7 @@ __global__ void __launch_bounds__(((TX + 2) * (TY + 2) + 31) / 32 * 32, 1)
     KS(K3::EY) = eyh.v;
     KS(K3::EZ) = ezh.v;
     if constexpr (G) {  // corner sources (mlw_m_g.f:289-290, 308, 326, 344)
-      const size_t gc = (size_t)a + (size_t)b * ix + (size_t)k * plane;
-      const FT gxm(grav[n + gc]), gym(grav[3 * n + gc]), gzm(grav[5 * n + gc]);
+      const FT gxm(gq[0]), gym(gq[1]), gzm(gq[2]);
       double *gk = gkslot(k);
       gk[tid] = (roh * (vxh * gxm + vyh * gym + vzh * gzm)).v;
       gk[T::NK + tid] = (roh * gxm).v;
