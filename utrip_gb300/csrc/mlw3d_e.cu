@@ -34,13 +34,21 @@ namespace {
 
 // bbtocx (cans3d/common/bbtocx.f:29-35) and its cyclic permutations bbtocy,
 // bbtocz at one point: (b2(+s1) - b2(-s1)) / d1 / 2 - (b1(+s2) - b1(-s2)) / d2 / 2.
-// Every operation rounds once (no contraction), in both policies.
+// Every operation rounds once (no contraction): the exact policy's form.
 __device__ __forceinline__ double bbtoc(const double *__restrict__ b1,
                                         const double *__restrict__ b2, size_t g, size_t s1,
                                         size_t s2, double d1, double d2) {
   const double t1 = __dmul_rn(__ddiv_rn(__dsub_rn(b2[g + s1], b2[g - s1]), d1), 0.5);
   const double t2 = __dmul_rn(__ddiv_rn(__dsub_rn(b1[g + s2], b1[g - s2]), d2), 0.5);
   return __dsub_rn(t1, t2);
+}
+
+// The fast policy's form: the same difference times half the reciprocal
+// spacings h1 = 0.5/d1, h2 = 0.5/d2 (no division).
+__device__ __forceinline__ double bbtoc_fast(const double *__restrict__ b1,
+                                             const double *__restrict__ b2, size_t g,
+                                             size_t s1, size_t s2, double h1, double h2) {
+  return (b2[g + s1] - b2[g - s1]) * h1 - (b1[g + s2] - b1[g - s2]) * h2;
 }
 
 __device__ __forceinline__ void split3(size_t g, int ix, size_t plane, int &i, int &j,
@@ -56,6 +64,7 @@ __device__ __forceinline__ bool inner3(int i, int j, int k, int ix, int jx, int 
 }
 
 // et*J at every cell (zero on the outer layer).
+template <bool E>
 __global__ void k_res3_cells(const double *__restrict__ S, int ix, int jx, int kx,
                              Axis ax, Axis ay, Axis az, const double *__restrict__ et,
                              double *__restrict__ res, const Ctl *__restrict__ ctl) {
@@ -72,9 +81,16 @@ __global__ void k_res3_cells(const double *__restrict__ S, int ix, int jx, int k
     double cx = 0.0, cy = 0.0, cz = 0.0;
     if (inner3(i, j, k, ix, jx, kx)) {
       const double e = et[g];
-      cx = __dmul_rn(e, bbtoc(by, bz, g, ix, plane, ay.d[j], az.d[k]));
-      cy = __dmul_rn(e, bbtoc(bz, bx, g, plane, 1, az.d[k], ax.d[i]));
-      cz = __dmul_rn(e, bbtoc(bx, by, g, 1, ix, ax.d[i], ay.d[j]));
+      if constexpr (E) {
+        cx = __dmul_rn(e, bbtoc(by, bz, g, ix, plane, ay.d[j], az.d[k]));
+        cy = __dmul_rn(e, bbtoc(bz, bx, g, plane, 1, az.d[k], ax.d[i]));
+        cz = __dmul_rn(e, bbtoc(bx, by, g, 1, ix, ax.d[i], ay.d[j]));
+      } else {
+        const double hx = 0.5 * ax.di[i], hy = 0.5 * ay.di[j], hz = 0.5 * az.di[k];
+        cx = e * bbtoc_fast(by, bz, g, ix, plane, hy, hz);
+        cy = e * bbtoc_fast(bz, bx, g, plane, 1, hz, hx);
+        cz = e * bbtoc_fast(bx, by, g, 1, ix, hx, hy);
+      }
     }
     res[g] = cx;
     res[n + g] = cy;
@@ -165,6 +181,7 @@ __global__ void k_bh3(const double *__restrict__ S, const double *__restrict__ r
 
 // etm*Jh at every corner (zero on the outer layer), Jh from the half-step B
 // at the neighbouring corners and the corner spacings dxm, dym, dzm.
+template <bool E>
 __global__ void k_res3_corners(const double *__restrict__ bh, int ix, int jx, int kx,
                                Axis ax, Axis ay, Axis az, const double *__restrict__ etm,
                                double *__restrict__ resc, const Ctl *__restrict__ ctl) {
@@ -178,9 +195,16 @@ __global__ void k_res3_corners(const double *__restrict__ bh, int ix, int jx, in
     double cx = 0.0, cy = 0.0, cz = 0.0;
     if (inner3(i, j, k, ix, jx, kx)) {
       const double e = etm[g];
-      cx = __dmul_rn(e, bbtoc(byh, bzh, g, ix, plane, ay.dm[j], az.dm[k]));
-      cy = __dmul_rn(e, bbtoc(bzh, bxh, g, plane, 1, az.dm[k], ax.dm[i]));
-      cz = __dmul_rn(e, bbtoc(bxh, byh, g, 1, ix, ax.dm[i], ay.dm[j]));
+      if constexpr (E) {
+        cx = __dmul_rn(e, bbtoc(byh, bzh, g, ix, plane, ay.dm[j], az.dm[k]));
+        cy = __dmul_rn(e, bbtoc(bzh, bxh, g, plane, 1, az.dm[k], ax.dm[i]));
+        cz = __dmul_rn(e, bbtoc(bxh, byh, g, 1, ix, ax.dm[i], ay.dm[j]));
+      } else {
+        const double hx = 0.5 * ax.dim[i], hy = 0.5 * ay.dim[j], hz = 0.5 * az.dim[k];
+        cx = e * bbtoc_fast(byh, bzh, g, ix, plane, hy, hz);
+        cy = e * bbtoc_fast(bzh, bxh, g, plane, 1, hz, hx);
+        cz = e * bbtoc_fast(bxh, byh, g, 1, ix, hx, hy);
+      }
     }
     resc[g] = cx;
     resc[n + g] = cy;
@@ -238,15 +262,22 @@ cudaError_t launch_mlw3d_e(bool exact, int tile, const double *A, double *B, int
     return cudaErrorInvalidValue;
   const size_t n = (size_t)ix * jx * kx;
   const int blocks = grid_for(n);
-  k_res3_cells<<<blocks, 256, 0, s>>>(A, ix, jx, kx, ax, ay, az, eta, res, ctl);
+  if (exact)
+    k_res3_cells<true><<<blocks, 256, 0, s>>>(A, ix, jx, kx, ax, ay, az, eta, res, ctl);
+  else
+    k_res3_cells<false><<<blocks, 256, 0, s>>>(A, ix, jx, kx, ax, ay, az, eta, res, ctl);
   count_launch();
   if (exact)
     k_bh3<true><<<blocks, 256, 0, s>>>(A, res, res + 6 * n, ix, jx, kx, ax, ay, az, dt, ctl);
   else
     k_bh3<false><<<blocks, 256, 0, s>>>(A, res, res + 6 * n, ix, jx, kx, ax, ay, az, dt, ctl);
   count_launch();
-  k_res3_corners<<<blocks, 256, 0, s>>>(res + 6 * n, ix, jx, kx, ax, ay, az, eta + n,
-                                        res + 3 * n, ctl);
+  if (exact)
+    k_res3_corners<true><<<blocks, 256, 0, s>>>(res + 6 * n, ix, jx, kx, ax, ay, az,
+                                                eta + n, res + 3 * n, ctl);
+  else
+    k_res3_corners<false><<<blocks, 256, 0, s>>>(res + 6 * n, ix, jx, kx, ax, ay, az,
+                                                 eta + n, res + 3 * n, ctl);
   count_launch();
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
