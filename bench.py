@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary 3-D and 1-D workloads")
+    p.add_argument("--parity-full", action="store_true",
+                   help="only the 3-D parity legs at 256^3 x 200 steps for mLW, Roe-MUSCL "
+                        "and HLLD, both policies, against the oracle; prints one JSON line")
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
                             "gravity2d", "resistive2d", "gravity3d", "resistive3d",
@@ -205,6 +208,7 @@ def extra_workloads(stream, exact=False):
         (256, 256, 64), 20, (96, 96, 16), 50, "3-D reconnection model")
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
     out["spicule_1024_100000_steps_mlw_m_bg"] = spicule_workload(stream)
+    out["literal_drop_in_orszag_tang_512^2"] = literal_drop_in(stream)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
     out["adjoint_shear_256^2_2000_steps"] = adjoint_workload(stream)
     return out
@@ -538,6 +542,43 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
     return out
 
 
+def literal_drop_in(stream, n=512, steps=(10, 100)):
+    """The reference driver's own call pattern (cans2d/md_mhdkh/hdmlw/main.f:
+    169,179,182): per step cfl_m3 -> t += dt -> mlw_m3 -> bnd (one bd* call
+    per variable and axis), each a drop-in C-ABI call on the caller's host
+    arrays.  Unregistered, every call copies its arrays to the device and
+    back; registered (cans_gpu_register), the same calls run on device
+    mirrors and only dt crosses to the host.  Orszag-Tang n^2, wall time of
+    the host loop (it synchronises every call)."""
+    import torch
+    from utrip_gb300 import drivers, setups
+    s = setups.orszag_tang(n)
+    arr = (n + 2) * (n + 2) * 8
+    nvar = len(s["names"])
+    nbd = sum(1 for v, f, k, q in s["bc"] if f % 2 == 0)  # bdper* fills both faces
+    out = {"workload": f"orszag_tang_{n}x{n}_mlw_m3", "host_arrays": "pageable (numpy)"}
+    for mode, nsteps in (("unregistered", steps[0]), ("registered", steps[1])):
+        st = setups.copy_state(s)
+        drivers.run_literal(s, st, 2, resident=mode == "registered")  # warm-up
+        st = setups.copy_state(s)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        drivers.run_literal(s, st, nsteps, resident=mode == "registered")
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        if mode == "unregistered":
+            h2d = (8 + nvar + nbd) * arr  # cfl_m3 (8 arrays), mlw_m3, each bd call
+            d2h = (nvar + nbd) * arr + 8
+        else:  # registration pushes and the final pull happen once per loop
+            h2d = nvar * arr / nsteps
+            d2h = nvar * arr / nsteps + 8
+        out[mode] = {"steps": nsteps, "ms_per_step": el * 1e3 / nsteps,
+                     "zone_updates_per_s": n * n * nsteps / el,
+                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                     "calls_per_step": 2 + nbd}
+    return out
+
+
 def sweep_setups(nruns=64, seed=4):
     """64 magnetised shear layers, sizes drawn from {128,192,256,384}^2 and
     plasma beta log-uniform in [0.1, 10] (seeded)."""
@@ -572,7 +613,7 @@ def beta_sweep(stream, exact=False, nsteps=1000):
     done = all(b.query(g).nexec == nsteps for g in range(len(runs)))
     batch_final = [b.pull(g) for g in (0, len(runs) - 1)]
     b.close()
-    single = {}
+    single, by_size = {}, {}
     for mode in ("plain", "graph"):
         total = 0.0
         finals = []
@@ -586,14 +627,30 @@ def beta_sweep(stream, exact=False, nsteps=1000):
             run.advance(nsteps)
             e1.record(stream)
             torch.cuda.synchronize()
-            total += e0.elapsed_time(e1)
+            ms = e0.elapsed_time(e1)
+            total += ms
+            if mode == "plain":
+                d = by_size.setdefault(str(int(sizes[g])), {"runs": 0, "ms": 0.0})
+                d["runs"] += 1
+                d["ms"] += ms
             if g in (0, len(runs) - 1):
                 finals.append(run.pull())
             run.close()
         single[mode] = total
         diff = max(float(np.max(np.abs(x - y))) / max(float(np.max(np.abs(y))), 1e-300)
                    for f1, f2 in zip(finals, batch_final) for x, y in zip(f1, f2))
+    for k, d in by_size.items():
+        d["zone_updates_per_s"] = int(k) ** 2 * nsteps * d["runs"] / (d["ms"] * 1e-3)
+    # A batch can at best run every zone-update at the rate of a step kernel
+    # that fills the GPU (it is FP64-bound there): the best of the batched
+    # rate and the largest grids' one-at-a-time rate.
+    best_rate = max([zones / (batched_ms * 1e-3)] +
+                    [d["zone_updates_per_s"] for d in by_size.values()])
+    ideal_ms = zones / best_rate * 1e3
     return {"runs": len(runs), "steps_per_run": nsteps, "config": cfg,
+            "one_at_a_time_plain_by_size": by_size,
+            "fp64_bound_ideal_ms": ideal_ms,
+            "max_speedup_vs_plain_if_fp64_bound": single["plain"] / ideal_ms,
             "sizes": {str(k): int(np.sum(sizes == k)) for k in (128, 192, 256, 384)},
             "beta_range": [float(betas.min()), float(betas.max())],
             "batched_ms": batched_ms, "one_at_a_time_plain_ms": single["plain"],
@@ -605,47 +662,157 @@ def beta_sweep(stream, exact=False, nsteps=1000):
             "max_rel_diff_batched_vs_single": diff}
 
 
-def parity_check(n, stream, nsteps=100):
-    """The headline workload checked against the CPU oracle: 100 loop
-    iterations of Orszag-Tang n^2 from the same initial state, relative
-    L-infinity per variable of the fast policy and the number of cells that
-    differ in the exact policy; and the drift of the conserved totals (mass,
-    momentum, total energy, B) over the same run in the periodic box."""
-    import oracle
-    from utrip_gb300 import drivers, setups
-    s = setups.orszag_tang(n)
-    ref = setups.copy_state(s)
-    oracle.run_2d(s, ref, nsteps)
-    out = {"steps": nsteps}
-    for exact in (False, True):
-        got = setups.copy_state(s)
-        run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
-        drivers.run_resident(s, got, nsteps, exact=exact, run=run)
-        run.close()
-        if exact:
-            out["exact_cells_differing"] = int(sum(int(np.sum(a != b)) for a, b in zip(got, ref)))
-        else:
-            # relative to the field's largest value; absolute for a field that
-            # is zero everywhere (vz, bz of this 2-D problem)
-            out["fast_rel_linf"] = {k: float(np.max(np.abs(a - b)) / (np.max(np.abs(b)) or 1.0))
-                                    for k, a, b in zip(s["names"], got, ref)}
-            fast = got
+def _rel_linf(names, got, ref):
+    """Relative L-infinity per variable (to the field's largest value; absolute
+    for a field that is zero everywhere)."""
+    return {k: float(np.max(np.abs(a - b)) / (np.max(np.abs(b)) or 1.0))
+            for k, a, b in zip(names, got, ref)}
 
-    def totals(st):
-        ro, pr, vx, vy, vz, bx, by, bz = st[:8]
-        w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
-        inner = (slice(1, -1), slice(1, -1))
-        ee = pr / (s["gm"] - 1) + 0.5 * ro * (vx ** 2 + vy ** 2 + vz ** 2) + \
-            (bx ** 2 + by ** 2 + bz ** 2) / (8 * np.pi)
-        q = {"mass": ro, "energy": ee, "momentum_x": ro * vx, "momentum_y": ro * vy,
-             "bx": bx, "by": by}
-        return {k: float(np.sum(a[inner] * w)) for k, a in q.items()}
-    t0, t1 = totals(s["state"]), totals(fast)
-    out["conservation_drift"] = {k: (t1[k] - t0[k]) / max(abs(t0[k]), 1e-300) if abs(t0[k]) > 1e-12
-                                 else t1[k] - t0[k] for k in t0}
+
+def _totals(s, st):
+    """Interior totals of mass, momentum, total energy and B of a 2-D or 3-D
+    state (CANS units: magnetic energy B^2/8pi)."""
+    ro, pr, vx, vy, vz, bx, by, bz = st[:8]
+    three = ro.ndim == 3
+    if three:
+        w = (s["dx"][:, None, None] * s["dy"][None, :, None] * s["dz"][None, None, :])
+        m = s["margin"]
+        inner = (slice(m, -m),) * 3
+    else:
+        w = np.outer(s["dx"], s["dy"])
+        m = s["margin"]
+        inner = (slice(m, -m),) * 2
+    w = w[inner]
+    ee = pr / (s["gm"] - 1) + 0.5 * ro * (vx ** 2 + vy ** 2 + vz ** 2) + \
+        (bx ** 2 + by ** 2 + bz ** 2) / (8 * np.pi)
+    q = {"mass": ro, "energy": ee, "momentum_x": ro * vx, "momentum_y": ro * vy,
+         "momentum_z": ro * vz, "bx": bx, "by": by, "bz": bz}
+    return {k: float(np.sum(a[inner] * w)) for k, a in q.items()}
+
+
+def _drift(t0, t1):
+    return {k: (t1[k] - t0[k]) / abs(t0[k]) if abs(t0[k]) > 1e-12 else t1[k] - t0[k]
+            for k in t0}
+
+
+def parity_check(n, stream, nsteps=100, c3_n=256, c3_steps=200, c3_riemann_steps=20):
+    """The benchmark configurations checked against the CPU oracle from the
+    same initial states.
+
+    2-D Orszag-Tang n^2 (the headline): 100 loop iterations, and the whole
+    run to t = pi/2; relative L-infinity per variable of the fast policy, the
+    number of cells that differ in the exact policy, and the drift of the
+    conserved totals (mass, momentum, total energy, B) in the periodic box.
+    3-D beta = 1 turbulence c3_n^3: the mLW loop for c3_steps iterations
+    (both policies), the Roe-MUSCL and HLLD loops for c3_riemann_steps
+    (fast policy), each with the drift of its totals.  The shock tube of
+    md_shktb with B = 0 in 1-D, 2-D and 3-D against the exact solution of
+    its shktb_analytic.pro: L1 distances and their order under refinement."""
+    import oracle
+    from oracle import shktb_analytic as an
+    from utrip_gb300 import drivers, setups
+    out = {}
+    s = setups.orszag_tang(n)
+    for label, nstop in (("orszag_tang_100_steps", nsteps),
+                         ("orszag_tang_to_t_pi_over_2", 10 ** 6)):
+        ref = setups.copy_state(s)
+        t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, nstop)
+        leg = {"steps": int(ns_ref), "t": t_ref}
+        for exact in (False, True):
+            got = setups.copy_state(s)
+            run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+            t, ns, merr, _ = drivers.run_resident(s, got, nstop, exact=exact, run=run)
+            run.close()
+            if exact:
+                leg["exact_cells_differing"] = int(sum(int(np.sum(a != b))
+                                                       for a, b in zip(got, ref)))
+                leg["exact_same_t_and_steps"] = bool(t == t_ref and ns == ns_ref)
+            else:
+                leg["fast_rel_linf"] = _rel_linf(s["names"], got, ref)
+                leg["fast_steps"] = int(ns)
+                leg["conservation_drift_fast"] = _drift(_totals(s, s["state"]),
+                                                        _totals(s, got))
+        leg["conservation_drift_oracle"] = _drift(_totals(s, s["state"]), _totals(s, ref))
+        out[label] = leg
     out["conservation_note"] = ("relative change of the interior totals over the run; "
                                 "absolute change where the total is zero")
+    del s
+    for solver, steps, both in (("mlw_m_3d", c3_steps, True),
+                                ("roe_m_3d", c3_riemann_steps, False),
+                                ("hlld_3d", c3_riemann_steps, False)):
+        out[f"turbulence_{c3_n}^3_{solver}_{steps}_steps"] = parity_3d(
+            stream, solver, c3_n, steps, both)
+    out["sod_shock_tube_exact_solution"] = parity_sod(stream, an)
     return out
+
+
+def parity_3d(stream, solver, n, steps, exact_too):
+    """One 3-D loop of the beta = 1 turbulence box against the oracle: fast
+    policy relative L-infinity and conservation drift (device and oracle),
+    and with exact_too the cells that differ in the exact policy.  HLLD runs
+    at safety 0.2 (see riemann_3d)."""
+    import oracle
+    from utrip_gb300 import drivers, setups
+    s = setups.turbulence_3d(n, solver=solver)
+    if solver == "hlld_3d":
+        s["safety"] = 0.2
+    ref = setups.copy_state(s)
+    t0 = time.perf_counter()
+    t_ref, ns_ref, _, _ = oracle.run_3d(s, ref, steps)
+    leg = {"steps": int(ns_ref), "oracle_s": time.perf_counter() - t0,
+           "oracle_cores": oracle.get_threads()}
+    tot0 = _totals(s, s["state"])
+    for exact in ((False, True) if exact_too else (False,)):
+        got = setups.copy_state(s)
+        t, ns, merr, _ = drivers.run_resident(s, got, steps, exact=exact)
+        if exact:
+            leg["exact_cells_differing"] = int(sum(int(np.sum(a != b)) for a, b in zip(got, ref)))
+        else:
+            leg["fast_rel_linf"] = _rel_linf(s["names"], got, ref)
+            leg["conservation_drift_fast"] = _drift(tot0, _totals(s, got))
+        del got
+    leg["conservation_drift_oracle"] = _drift(tot0, _totals(s, ref))
+    return leg
+
+
+def parity_sod(stream, an, ns=(256, 512, 1024, 2048)):
+    """The md_shktb shock tube with B = 0 on the device (fast policy) in 1-D
+    (mlw_m), 2-D (mlw_m3) and 3-D (mlw_m) to tend = 0.14154: L1 distance of
+    rho, p, vx from the exact solution and the observed order."""
+    from utrip_gb300 import drivers, setups
+    out = {}
+    for ndim in (1, 2, 3):
+        errs = []
+        for n in ns:
+            s = setups.sod_shock_tube(n, ndim)
+            got = setups.copy_state(s)
+            t, nsteps, merr, _ = drivers.run_resident(s, got, 10 ** 6)
+            x, dx, ro, pr, vx = setups.sod_interior_profile(s, got)
+            sd = s["sod"]
+            errs.append(an.l1_errors(x, dx, ro, pr, vx, t, sd["x0"], sd["gm"], sd["ro1"],
+                                     sd["pr1"]))
+        out[f"{ndim}d"] = {"cells": list(ns), "l1": {k: [e[k] for e in errs] for k in errs[0]},
+                           "order": {k: an.observed_order(ns, [e[k] for e in errs])
+                                     for k in errs[0]}}
+    return out
+
+
+def parity_full(n=256, steps=200):
+    """The 3-D configuration at its stated size and length: 256^3 interior
+    cells, 200 loop iterations of mLW, Roe-MUSCL and HLLD, each in both
+    policies against the oracle (all host threads); about a quarter of an
+    hour of CPU time for the oracle."""
+    import torch
+    import oracle
+    oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    out = {"parity_full": f"turbulence_{n}^3_{steps}_steps"}
+    for solver in ("mlw_m_3d", "roe_m_3d", "hlld_3d"):
+        out[solver] = parity_3d(stream, solver, n, steps, True)
+        print(json.dumps({solver: out[solver]}), flush=True)
+    print(json.dumps(out), flush=True)
 
 
 def dist_setup():
@@ -930,6 +1097,9 @@ def main():
     args = parse()
     if args.profile_case:
         profile_case(args.profile_case, args.n)
+        return
+    if args.parity_full:
+        parity_full()
         return
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -92,7 +92,7 @@ def test_resident_loop_mixed_boundaries_exact(gpu, oracle_lib):
     assert_same(s["names"], got, ref, "hlld loop")
 
 
-def test_fast_policy_tolerance_100_steps(gpu):
+def test_fast_policy_tolerance_100_steps(gpu, oracle_lib):
     # Two properties of the reference set the terms of this comparison:
     # (1) its driver pairs the CANS-unit cfl_m (ca^2 = B^2/4 pi rho) with the
     # Heaviside-unit HLLD state, which underestimates the Alfven speed; with
@@ -104,7 +104,7 @@ def test_fast_policy_tolerance_100_steps(gpu):
     s = setups.turbulence_3d(24, solver="hlld_3d", rms=0.05, b0=(0.8, 0.48, 0.36))
     s["safety"] = 0.2
     ex = setups.copy_state(s)
-    drivers.run_resident(s, ex, 100, exact=True)
+    oracle.run_3d(s, ex, 100)
     fa = setups.copy_state(s)
     drivers.run_resident(s, fa, 100, exact=False)
     for k, a, b in zip(s["names"], fa, ex):

@@ -408,6 +408,99 @@ def shock_tube_1d(n: int = 1024, safety: float | None = None, tend: float = 0.1,
                 name=f"shock_tube_{n}" if solver == "mlw_m_1d" else f"shock_tube_{solver}_{n}")
 
 
+def _shktb_axis(n: int, margin: int = 1):
+    """cans1d/md_shktb/hdmlw/model.f:18-31: dx0 = 1/real(ix - 2 margin),
+    cell izero = ix/2 centred at -dx0/2, positions accumulated outward."""
+    ix = n + 2 * margin
+    dx0 = 1.0 / float(np.float32(ix - 2 * margin))
+    dxm0 = np.full(ix, dx0)
+    x = np.empty(ix)
+    iz = ix // 2 - 1  # 0-based index of Fortran izero = ix/2
+    x[iz] = -dxm0[iz] / 2
+    for i in range(iz + 1, ix):
+        x[i] = x[i - 1] + dxm0[i - 1]
+    for i in range(iz - 1, -1, -1):
+        x[i] = x[i + 1] - dxm0[i]
+    dx, _, dxm = grdrdy(x)
+    return x, dx, dxm
+
+
+def sod_shock_tube(n: int = 1024, ndim: int = 1, ncross: int = 4,
+                   safety: float | None = None):
+    """The hydrodynamic shock tube of cans1d/md_shktb/hdmlw (model.f:33-53,
+    main.f:20-23,136-146) run by the ideal-MHD mLW step with B = 0: gamma =
+    1.4; left (x <= 0) rho = 1, p = 1, right rho = 0.125, p = 0.1, at rest;
+    qav = 0.3; tend = 0.14154.  The x axis is model.f's (n cells, the
+    interface at x = 0 on a cell edge); bnd.f: bdsppx for rho and p, bdspnx
+    for vx (the waves do not reach the walls by tend).
+
+    ndim 1 runs the 1-D mlw_m (bx = by = 0) with safety 1.0 as main.f does;
+    ndim 2 and 3 run mlw_m3 and the 3-D mlw_m on an x-aligned tube of
+    ncross cells across (periodic, spacing dx) with the 2-D/3-D drivers'
+    safety 0.4: their cfl_m divides by sqrt(v^2 + c^2), not |v| + c, so
+    safety 1 would put the x Courant number above 1.  The exact answer is
+    oracle/shktb_analytic.py, the restatement of md_shktb's
+    shktb_analytic.pro."""
+    x, dx, dxm = _shktb_axis(n)
+    left = x <= 0.0
+    ro1d = np.where(left, 1.0, 0.125)
+    pr1d = np.where(left, 1.0, 0.1)
+    common = dict(tend=0.14154, dtmin=1e-10, sod=dict(gm=1.4, ro1=0.125, pr1=0.1, ro4=1.0,
+                                                      pr4=1.0, x0=0.0))
+    if ndim == 1:
+        f = {"ro": ro1d, "pr": pr1d, "vx": np.zeros(x.size), "vy": np.zeros(x.size),
+             "by": np.zeros(x.size)}
+        bc = []
+        for v, name in enumerate(VARS["mlw_m_1d"]):
+            kind = BD_SPN if name == "vx" else BD_SPP
+            bc += [(v, 0, kind, 0.0), (v, 1, kind, 0.0)]
+        state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in VARS["mlw_m_1d"]]
+        return dict(solver="mlw_m_1d", solver_id=3, names=VARS["mlw_m_1d"], x=x, dx=dx,
+                    dxm=dxm, bx=np.zeros(x.size), bxm=np.zeros(x.size), state=state, gm=1.4,
+                    qav=0.3, margin=1, bc=bc, safety=1.0 if safety is None else safety,
+                    dtout=0.01, name=f"sod_{n}_1d", **common)
+    yc, dyc, dymc = uniform_axis(ncross, ncross * float(dxm[1]))
+    sf = 0.4 if safety is None else safety
+    if ndim == 2:
+        shape = (x.size, ncross + 2)
+        ro = np.repeat(ro1d[:, None], shape[1], axis=1)
+        pr = np.repeat(pr1d[:, None], shape[1], axis=1)
+        z = np.zeros(shape)
+        f = {"ro": ro, "pr": pr, "vx": z, "vy": z, "vz": z, "bx": z, "by": z, "bz": z,
+             "az": z}
+        bc = []
+        for v, name in enumerate(VARS["mlw_m3"]):
+            kind = BD_SPN if name == "vx" else BD_SPP
+            bc += [(v, 0, kind, 0.0), (v, 1, kind, 0.0), (v, 2, BD_PER, 0.0),
+                   (v, 3, BD_PER, 0.0)]
+        return _pack("mlw_m3", x, dx, dxm, yc, dyc, dymc, f, 1.4, 0.3, bc, safety=sf,
+                     name=f"sod_{n}x{ncross}_mlw_m3", **common)
+    shape = (x.size, ncross + 2, ncross + 2)
+    ro = np.broadcast_to(ro1d[:, None, None], shape).copy()
+    pr = np.broadcast_to(pr1d[:, None, None], shape).copy()
+    z = np.zeros(shape)
+    f = {"ro": ro, "pr": pr, "vx": z, "vy": z, "vz": z, "bx": z, "by": z, "bz": z}
+    bc = []
+    for v, name in enumerate(VARS["mlw_m_3d"]):
+        kind = BD_SPN if name == "vx" else BD_SPP
+        bc += [(v, 0, kind, 0.0), (v, 1, kind, 0.0)]
+        for face in (2, 3, 4, 5):
+            bc.append((v, face, BD_PER, 0.0))
+    return _pack3(x, dx, dxm, yc, dyc, dymc, yc.copy(), dyc.copy(), dymc.copy(), f, 1.4, 0.3,
+                  bc, solver="mlw_m_3d", safety=sf,
+                  name=f"sod_{n}x{ncross}x{ncross}_mlw_m_3d", **common)
+
+
+def sod_interior_profile(setup: dict, state) -> tuple:
+    """(x, dx, ro, pr, vx) along the tube's interior cells; for a 2-D or 3-D
+    tube the first interior row (every row holds the same profile)."""
+    sl = slice(setup["margin"], -setup["margin"])
+    pick = {1: lambda a: a[sl], 2: lambda a: a[sl, 1], 3: lambda a: a[sl, 1, 1]}[state[0].ndim]
+    names = setup["names"]
+    return (setup["x"][sl], setup["dx"][sl], pick(state[names.index("ro")]),
+            pick(state[names.index("pr")]), pick(state[names.index("vx")]))
+
+
 def random_state_1d(ix: int, seed: int = 0):
     """Smooth-plus-noise 1-D state for parity tests (every variable varies)."""
     rng = np.random.default_rng(seed)
