@@ -432,11 +432,22 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
     mlw_m3, 2000 steps, J = final magnetic energy): the reverse sweep with
     binomial checkpointing in 32 stored states timed against the forward run
     of the same frozen dt sequence, and its directional derivatives checked
-    against FP64 central differences (h = 1e-6) of the GPU forward on 16
-    seeded directions of the initial vy field and of the CPU oracle on two;
-    dJ/dbeta the same way.  The artificial viscosity switches on where a
-    velocity jump crosses 1e-4 and the shear layer has jumps there, so the
-    check is also reported with qav = 0, where J is smooth."""
+    against FP64 central differences (h = 1e-6) on 16 seeded directions of
+    the initial vy field, and dJ/dbeta.
+
+    The artificial viscosity q = qav dxm max(0, |dv| - 1e-4) is piecewise
+    affine in dv, and the shear layer has velocity jumps near 1e-4, so J has
+    kinks within h of the base point.  The reverse sweep is the derivative
+    of the branches the base run took; its check therefore holds every
+    face's branch at the recorded one (cans_run_av_record /
+    cans_run_objective_frozen_av), and reports per direction how many face
+    switches the unheld run crosses at +h and -h beside the unheld central
+    difference.  J also bends on the 1e-3 scale of the perturbation the
+    shear layer amplifies, which puts the h^2 term of a second-order
+    difference near 1e-7..1e-6 of J'; the held check uses the fourth-order
+    central difference from h and 2h (both second-order ones are reported).
+    qav = 0 (no viscosity, J smooth) is checked the same way, against the
+    GPU forward and, on two directions, the CPU oracle."""
     import torch
     import oracle
     from utrip_gb300 import drivers, setups
@@ -447,13 +458,8 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
         oracle.apply_bc_program(s["state"], s["bc"], s["margin"], s)
         return s
 
-    def objective(s, state, dts):
-        r = drivers.make_run(s, stream=stream.cuda_stream)
-        r.push([np.asfortranarray(a) for a in state])
-        try:
-            return r.objective(dts)
-        finally:
-            r.close()
+    def shifted(s, z, step):
+        return [np.asfortranarray(a + step * b) for a, b in zip(s["state"], z)]
 
     def smooth_direction(rng, n, kmax=8):
         """A seeded random field of unit RMS made of the Fourier modes
@@ -474,15 +480,34 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
         oracle.apply_bc_program(z, s["bc"], s["margin"], s)
         return z
 
+    def fd24(J):
+        """second-order differences at h and 2h, and the fourth-order one."""
+        d1 = (J[1] - J[-1]) / (2 * h)
+        d2 = (J[2] - J[-2]) / (4 * h)
+        return d1, d2, (4.0 * d1 - d2) / 3.0
+
+    def oracle_J(s, st, dts):
+        st = [np.asfortranarray(a) for a in st]
+        for dt in dts:
+            oracle.step_2d(s, st, dt)
+            oracle.apply_bc_program(st, s["bc"], s["margin"], s)
+        w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
+        e = (st[5] ** 2 + st[6] ** 2 + st[7] ** 2)[1:-1, 1:-1]
+        return float(np.sum(e * w)) / np.pi / 8.0
+
     out = {"nsteps": nsteps, "nsnap": nsnap, "h": h,
-           "directions": "seeded unit-RMS fields of the |k| <= 8 Fourier modes of vy"}
+           "directions": "seeded unit-RMS fields of the |k| <= 8 Fourier modes of vy",
+           "criterion": "|adjoint - fd| <= 1e-6 |fd| + 8 eps |J| / 2h"}
     eps = float(np.finfo(np.float64).eps)
+
+    def within(ad, fd, J):
+        return abs(ad - fd) <= 1e-6 * abs(fd) + 8 * eps * abs(J) / (2 * h)
+
     for qav in (3.0, 0.0):
         s = base(1.0, qav)
         run = drivers.make_run(s, stream=stream.cuda_stream)
         run.push(s["state"])
         dts, J = run.record_dts(nsteps)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         run.objective(dts)  # warm-up
         if qav == 3.0:
             run.adjoint(dts, nsnap=nsnap)  # warm-up (builds the checkpoint schedule)
@@ -501,41 +526,69 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
                 "adjoint_s": time.perf_counter() - t0, "forward_steps_in_adjoint": int(nfwd_all),
                 "grad_equal_to_checkpointed": all(np.array_equal(a, b)
                                                   for a, b in zip(g_all, grad))}
-        run.close()
+        run.av_record(dts)
+        J_held0, flips0 = run.objective_frozen_av(dts)
         rng = np.random.default_rng(5)
-        rel, within = [], 0
+        dirs, n_held, n_unheld = [], 0, 0
         for k in range(ndir):
             d = smooth_direction(rng, 256)
             z = extend(s, d)
             ad = sum(float(np.sum(g * e)) for g, e in zip(grad, z))
-            jp = objective(s, [a + h * b for a, b in zip(s["state"], z)], dts)
-            jm = objective(s, [a - h * b for a, b in zip(s["state"], z)], dts)
-            fd = (jp - jm) / (2 * h)
-            rel.append(abs(ad - fd) / abs(fd))
-            within += abs(ad - fd) <= 1e-6 * abs(fd) + 8 * eps * abs(J) / (2 * h)
-            if k < n_oracle_dirs and qav == 3.0:
-                def oracle_J(st):
-                    st = [np.asfortranarray(a) for a in st]
-                    for dt in dts:
-                        oracle.step_2d(s, st, dt)
-                        oracle.apply_bc_program(st, s["bc"], s["margin"], s)
-                    w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
-                    e = (st[5] ** 2 + st[6] ** 2 + st[7] ** 2)[1:-1, 1:-1]
-                    return float(np.sum(e * w)) / np.pi / 8.0
-                ojp = oracle_J([a + h * b for a, b in zip(s["state"], z)])
-                ojm = oracle_J([a - h * b for a, b in zip(s["state"], z)])
-                out.setdefault("oracle_fd_rel_err", []).append(abs(ad - (ojp - ojm) / (2 * h))
-                                                               / abs((ojp - ojm) / (2 * h)))
+            Jh, fl = {}, {}
+            for m in (1, -1, 2, -2):
+                run.push(shifted(s, z, m * h))
+                Jh[m], fl[m] = run.objective_frozen_av(dts)
+            run.push(shifted(s, z, h))
+            jp = run.objective(dts)
+            run.push(shifted(s, z, -h))
+            jm = run.objective(dts)
+            fd_unheld = (jp - jm) / (2 * h)
+            d1, d2, d4 = fd24(Jh)
+            n_held += within(ad, d4, J)
+            n_unheld += within(ad, fd_unheld, J)
+            row = {"adjoint": ad, "held_fd4_rel_err": abs(ad - d4) / abs(d4),
+                   "held_fd2_h_rel_err": abs(ad - d1) / abs(d4),
+                   "held_fd2_2h_rel_err": abs(ad - d2) / abs(d4),
+                   "unheld_fd2_rel_err": abs(ad - fd_unheld) / abs(fd_unheld),
+                   "switches_crossed_plus_h": int(fl[1]), "switches_crossed_minus_h": int(fl[-1])}
+            if qav == 0.0 and k < n_oracle_dirs:
+                Jo = {m: oracle_J(s, shifted(s, z, m * h), dts) for m in (1, -1, 2, -2)}
+                o1, _, o4 = fd24(Jo)
+                row["oracle_fd4_rel_err"] = abs(ad - o4) / abs(o4)
+                row["oracle_fd2_rel_err"] = abs(ad - o1) / abs(o4)
+            dirs.append(row)
+        run.push(s["state"])
+        # dJ/dbeta: p = 0.625 beta in every cell
         dbeta = 0.625 * float(np.sum(grad[1]))
-        jb = [objective(sb, sb["state"], dts) for sb in (base(1.0 + h, qav), base(1.0 - h, qav))]
-        fdb = (jb[0] - jb[1]) / (2 * h)
+        Jb = {}
+        for m in (1, -1, 2, -2):
+            run.push(base(1.0 + m * h, qav)["state"])
+            Jb[m], _ = run.objective_frozen_av(dts)
+        b1, _, b4 = fd24(Jb)
+        run.push(base(1.0 + h, qav)["state"])
+        jbp = run.objective(dts)
+        run.push(base(1.0 - h, qav)["state"])
+        jbm = run.objective(dts)
+        run.close()
+        held = [r["held_fd4_rel_err"] for r in dirs]
         out[f"qav{qav:g}"] = {
             "J": J, "J_replay_equal": J_fwd == J and J_adj == J,
+            "J_held_equal": J_held0 == J and flips0 == 0,
             "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
             "forward_steps_in_adjoint": int(nfwd),
-            "fd_rel_err_max": max(rel), "fd_rel_err_median": float(np.median(rel)),
-            "fd_within_1e-6": f"{within}/{ndir}",
-            "dJ_dbeta": dbeta, "dJ_dbeta_fd": fdb, "dJ_dbeta_rel_err": abs(dbeta - fdb) / abs(fdb)}
+            "held_fd4_within_1e-6": f"{n_held}/{ndir}",
+            "held_fd4_rel_err_max": max(held), "held_fd4_rel_err_median": float(np.median(held)),
+            "unheld_fd2_within_1e-6": f"{n_unheld}/{ndir}",
+            "unheld_fd2_rel_err_median": float(np.median([r["unheld_fd2_rel_err"]
+                                                          for r in dirs])),
+            "switches_crossed_per_direction": [r["switches_crossed_plus_h"] +
+                                               r["switches_crossed_minus_h"] for r in dirs],
+            "dJ_dbeta": dbeta, "dJ_dbeta_held_fd4": b4,
+            "dJ_dbeta_held_fd4_rel_err": abs(dbeta - b4) / abs(b4),
+            "dJ_dbeta_held_fd2_rel_err": abs(dbeta - b1) / abs(b4),
+            "dJ_dbeta_unheld_fd2_rel_err": abs(dbeta - (jbp - jbm) / (2 * h)) /
+            abs((jbp - jbm) / (2 * h)),
+            "directions": dirs}
     if "store_all_states" in out:
         out["store_all_states"]["adjoint_over_forward"] = (out["store_all_states"]["adjoint_s"]
                                                            / out["qav3"]["forward_s"])
@@ -671,7 +724,8 @@ def _rel_linf(names, got, ref):
 
 def _totals(s, st):
     """Interior totals of mass, momentum, total energy and B of a 2-D or 3-D
-    state (CANS units: magnetic energy B^2/8pi)."""
+    state (magnetic energy B^2/8pi in CANS units; B^2/2mu for the HLLD state,
+    which is in Heaviside units)."""
     ro, pr, vx, vy, vz, bx, by, bz = st[:8]
     three = ro.ndim == 3
     if three:
@@ -683,8 +737,9 @@ def _totals(s, st):
         m = s["margin"]
         inner = (slice(m, -m),) * 2
     w = w[inner]
+    bfac = 1.0 / (2.0 * s["mu"]) if s["solver"] == "hlld_3d" else 1.0 / (8 * np.pi)
     ee = pr / (s["gm"] - 1) + 0.5 * ro * (vx ** 2 + vy ** 2 + vz ** 2) + \
-        (bx ** 2 + by ** 2 + bz ** 2) / (8 * np.pi)
+        (bx ** 2 + by ** 2 + bz ** 2) * bfac
     q = {"mass": ro, "energy": ee, "momentum_x": ro * vx, "momentum_y": ro * vy,
          "momentum_z": ro * vz, "bx": bx, "by": by, "bz": bz}
     return {k: float(np.sum(a[inner] * w)) for k, a in q.items()}
@@ -737,11 +792,17 @@ def parity_check(n, stream, nsteps=100, c3_n=256, c3_steps=200, c3_riemann_steps
     out["conservation_note"] = ("relative change of the interior totals over the run; "
                                 "absolute change where the total is zero")
     del s
-    for solver, steps, both in (("mlw_m_3d", c3_steps, True),
-                                ("roe_m_3d", c3_riemann_steps, False),
-                                ("hlld_3d", c3_riemann_steps, False)):
-        out[f"turbulence_{c3_n}^3_{solver}_{steps}_steps"] = parity_3d(
-            stream, solver, c3_n, steps, both)
+    for solver, steps in (("mlw_m_3d", c3_steps), ("roe_m_3d", c3_riemann_steps),
+                          ("hlld_3d", c3_riemann_steps)):
+        leg = parity_3d(stream, solver, c3_n, steps, True)
+        if solver != "mlw_m_3d":
+            leg["oracle_one_ulp_input_noise_rel_linf"] = one_ulp_conditioning(solver, 64, steps)
+            leg["note"] = ("the mean field lies along x, so the x faces sit at the c_f = c_a "
+                           "degeneracy, where the reference algorithm amplifies rounding: "
+                           "one ulp of input noise in the oracle alone grows to the "
+                           "oracle_one_ulp_input_noise figure (64^3, same steps); the exact "
+                           "policy reproduces the reference's rounding bit for bit")
+        out[f"turbulence_{c3_n}^3_{solver}_{steps}_steps"] = leg
     out["sod_shock_tube_exact_solution"] = parity_sod(stream, an)
     return out
 
@@ -773,6 +834,25 @@ def parity_3d(stream, solver, n, steps, exact_too):
         del got
     leg["conservation_drift_oracle"] = _drift(tot0, _totals(s, ref))
     return leg
+
+
+def one_ulp_conditioning(solver, n, steps):
+    """Relative L-infinity per variable between two oracle runs of the n^3
+    beta = 1 box whose initial velocities differ by at most one ulp."""
+    import oracle
+    from utrip_gb300 import setups
+    s = setups.turbulence_3d(n, solver=solver)
+    if solver == "hlld_3d":
+        s["safety"] = 0.2
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    rng = np.random.default_rng(1)
+    for k in (2, 3, 4):
+        b[k] = np.asfortranarray(b[k] * (1.0 + np.finfo(np.float64).eps *
+                                         rng.choice([-1.0, 0.0, 1.0], size=b[k].shape)))
+    oracle.apply_bc_program_3d(b, s["bc"], s["margin"], s)
+    oracle.run_3d(s, a, steps)
+    oracle.run_3d(s, b, steps)
+    return _rel_linf(s["names"], b, a)
 
 
 def parity_sod(stream, an, ns=(256, 512, 1024, 2048)):
@@ -888,6 +968,20 @@ class Clocks:
         return {"sm_mhz": statistics.median(loaded) if loaded else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
                 "samples": len(rows)}
+
+
+def probe_peaks():
+    """FP64 and FP32 FMA throughput of the device in TFLOP/s, measured now by
+    the benchmark's probe library (utrip_gb300/_lib/libcansprobe.so)."""
+    import ctypes
+    lib = ctypes.CDLL(str(ROOT / "utrip_gb300" / "_lib" / "libcansprobe.so"))
+    out = []
+    for name in ("cans_probe_fp64_tflops", "cans_probe_fp32_tflops"):
+        x = ctypes.c_double(0.0)
+        if getattr(lib, name)(ctypes.byref(x)) != 0:
+            raise RuntimeError(f"{name} failed")
+        out.append(x.value)
+    return out[0], out[1]
 
 
 def measured_peaks():
@@ -1029,7 +1123,7 @@ def run_ours(args, ws, rank, local):
     achieved = B_PER_ZONE * n * n / (step_avg * 1e-3) / 1e9
     ncu = ncu_summary()
     traffic = ncu.get("dram_bytes_per_launch")
-    fp64_peak = capi.measure_fp64_tflops()
+    fp64_peak, fp32_peak = probe_peaks()
     flops_zone = ncu.get("fp64_flops_per_zone")
     fp64 = None
     if flops_zone:
@@ -1078,6 +1172,7 @@ def run_ours(args, ws, rank, local):
                      "step_kernel_ms": step_avg, "iteration_ms": iter_ms / prof_iters},
         "roofline_fp64": fp64,
         "fp64_peak_tflops_measured": fp64_peak,
+        "fp32_peak_tflops_measured": fp32_peak,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": int(launches),

@@ -527,12 +527,6 @@ int cans_batch_set_config(cans_batch *b, int config);
 int cans_batch_autotune(cans_batch *b, int trial_steps, int *config);
 
 /* ------------------------------------------------------------------------ */
-/* Measurement                                                               */
-/* ------------------------------------------------------------------------ */
-/* FP64 fused multiply-add throughput of the current device, TFLOP/s. */
-int cans_measure_fp64_tflops(double *tflops);
-
-/* ------------------------------------------------------------------------ */
 /* Discrete adjoint of the 2-D mlw_m3 run (no counterpart in the reference:  */
 /* the reverse sweep the differentiation pattern adds beside the step)       */
 /* ------------------------------------------------------------------------ */
@@ -555,6 +549,21 @@ int cans_run_objective(cans_run *h, long long nsteps, const double *dts,
 int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts,
                      int nsnap, double *J, double *const *grad,
                      long long *nfwd);
+/* The finite-difference check of the adjoint with the artificial viscosity's
+ * branch held.  q = qav dxm max(0, |dv| - 1e-4) (cans2d/hdmlw/mlw_m3.f:
+ * 325-334) is piecewise affine in dv; the reverse sweep differentiates the
+ * branch each face took in the recorded run.  cans_run_av_record runs the
+ * nsteps steps of dts from P_0 and keeps, for every step and face, whether
+ * the face was active (|dv| > 1e-4) and the sign of dv (2*ix*jx bytes per
+ * step on the device, held until the next record or cans_run_destroy; at
+ * most 64 GiB).  cans_run_objective_frozen_av is cans_run_objective with
+ * every face held at its recorded branch: q = qav dxm (s dv - 1e-4) on the
+ * faces recorded active, s the recorded sign, 0 on the others.  *nflip (if
+ * not NULL) receives the number of face-steps whose own branch differs from
+ * the recorded one: the switches a perturbed run crosses. */
+int cans_run_av_record(cans_run *h, long long nsteps, const double *dts);
+int cans_run_objective_frozen_av(cans_run *h, long long nsteps, const double *dts,
+                                 double *J, long long *nflip);
 /* Transpose of the run's boundary program applied in place to host arrays
  * (one per state variable): folds ghost-cell sensitivities into the cells
  * they are copied from. */

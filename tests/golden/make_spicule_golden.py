@@ -2,7 +2,7 @@
 
 Run from the repository root, where the reference tree is present:
 
-    python tests/golden/make_spicule_golden.py /root/reference
+    python tests/golden/make_spicule_golden.py <root of the reference tree>
 
 The reference ships the output of one run of its spicule model
 (cans_beta_one/cans1d/md_spicule/hdmlw/: params.txt, out.txt and the DAC
@@ -47,4 +47,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_spicule_golden.py <root of the reference tree>")
+    main(sys.argv[1])

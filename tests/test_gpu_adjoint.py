@@ -235,6 +235,91 @@ def test_viscosity_kinks_on_the_shear_layer(gpu):
     assert abs(fd8 - ad) <= 1e-5 * abs(ad)
 
 
+def _frozen_fd(run, s, z, dts, h):
+    """Central differences of the held-branch objective along z: second
+    order at h, and fourth order from h and 2h (Richardson), with the
+    switch crossings counted at +h and -h."""
+    J, fl = {}, {}
+    for m in (1, -1, 2, -2):
+        run.push([np.asfortranarray(a + m * h * b) for a, b in zip(s["state"], z)])
+        J[m], fl[m] = run.objective_frozen_av(dts)
+    run.push(s["state"])
+    d1 = (J[1] - J[-1]) / (2 * h)
+    d2 = (J[2] - J[-2]) / (4 * h)
+    return d1, (4.0 * d1 - d2) / 3.0, fl[1], fl[-1]
+
+
+def test_frozen_branch_record_leaves_the_run_unchanged(gpu):
+    """Recording the viscosity branches runs the same step: holding them at
+    the base point reproduces J bit for bit with no switch crossed."""
+    s = _setup(n=64, ny=64, qav=3.0)
+    run = _run(s)
+    try:
+        dts, J = run.record_dts(60)
+        run.av_record(dts)
+        assert run.objective(dts) == J
+        Jf, nflip = run.objective_frozen_av(dts)
+        assert Jf == J and nflip == 0
+    finally:
+        run.close()
+
+
+def test_frozen_branch_finite_differences_reduced_c5(gpu):
+    """The adjoint configuration reduced to 64^2 and 200 steps at qav = 3:
+    with every viscosity face held at its base-point branch the objective is
+    smooth, and the adjoint matches its central differences (h = 1e-6,
+    fourth order) within 1e-6 on smooth seeded directions of the vy field,
+    and dJ/dbeta the same way.  The unheld objective crosses switches
+    within h on these directions (counted), which is why its own central
+    differences miss the adjoint there."""
+    s = _setup(n=64, ny=64, qav=3.0)
+    run = _run(s)
+    try:
+        dts, J = run.record_dts(200)
+        _, grad, _ = run.adjoint(dts, nsnap=12)
+        run.av_record(dts)
+        rng = np.random.default_rng(5)
+        k = np.fft.fftfreq(64, d=1.0 / 64)
+        KX, KY = np.meshgrid(k, k, indexing="ij")
+        mask = (KX ** 2 + KY ** 2) <= 64.0
+        for _ in range(4):
+            spec = np.where(mask, rng.standard_normal((64, 64)) +
+                            1j * rng.standard_normal((64, 64)), 0.0)
+            d = np.real(np.fft.ifft2(spec))
+            d /= np.sqrt(np.mean(d ** 2))
+            z = _extend(s, d)
+            ad = sum(float(np.sum(g * e)) for g, e in zip(grad, z))
+            fd2, fd4, fp, fm = _frozen_fd(run, s, z, dts, H)
+            assert _close(ad, fd4, J), (ad, fd4, fd2, fp, fm)
+        # dJ/dbeta: p = 0.625 beta in every cell, held branches
+        ad = 0.625 * float(np.sum(grad[1]))
+        Jb = {}
+        for m in (1, -1, 2, -2):
+            run.push(_setup(n=64, ny=64, beta=1.0 + m * H, qav=3.0)["state"])
+            Jb[m], _ = run.objective_frozen_av(dts)
+        d1 = (Jb[1] - Jb[-1]) / (2 * H)
+        fd4 = (4.0 * d1 - (Jb[2] - Jb[-2]) / (4 * H)) / 3.0
+        assert _close(ad, fd4, J), (ad, fd4, d1)
+    finally:
+        run.close()
+
+
+def test_frozen_branch_needs_a_record(gpu):
+    s = _setup(qav=3.0)
+    run = _run(s)
+    try:
+        dts, _ = run.record_dts(10)
+        with pytest.raises(capi.CansError):
+            run.objective_frozen_av(dts)
+        run.av_record(dts[:5])
+        with pytest.raises(capi.CansError):  # longer than the record
+            run.objective_frozen_av(dts)
+        Jf, _ = run.objective_frozen_av(dts[:5])
+        assert np.isfinite(Jf)
+    finally:
+        run.close()
+
+
 def test_adjoint_rejects_other_solvers(gpu):
     s = setups.random_state_3d(12, 12, 12, seed=1)
     run = drivers.make_run(s)

@@ -603,6 +603,43 @@ def test_spicule_corona_amplifies_energy_rounding(oracle_lib):
     assert rel[2] > 1e-6 and rel[0] < 1e-12 and rel[1] < 1e-12, rel
 
 
+def one_ulp_amplification(oracle_lib, solver, b0, n=32, steps=20):
+    """Relative L-infinity per variable between two oracle runs of the 3-D
+    beta = 1 box whose velocities differ by at most one unit in the last
+    place."""
+    s = setups.turbulence_3d(n, solver=solver, b0=b0)
+    if solver == "hlld_3d":
+        s["safety"] = 0.2
+    a, b = setups.copy_state(s), setups.copy_state(s)
+    rng = np.random.default_rng(1)
+    for k in (2, 3, 4):
+        b[k] = np.asfortranarray(b[k] * (1.0 + np.finfo(np.float64).eps *
+                                         rng.choice([-1.0, 0.0, 1.0], size=b[k].shape)))
+    oracle_lib.apply_bc_program_3d(b, s["bc"], s["margin"], s)
+    oracle_lib.run_3d(s, a, steps)
+    oracle_lib.run_3d(s, b, steps)
+    return {k: float(np.max(np.abs(x - y)) / np.max(np.abs(y))) for k, x, y in
+            zip(s["names"], b, a)}
+
+
+@pytest.mark.parametrize("solver", ["roe_m_3d", "hlld_3d"])
+def test_riemann_solvers_amplify_rounding_at_the_aligned_field(oracle_lib, solver):
+    """The conditioning behind the fast-policy results of the Riemann
+    solvers on the 3-D beta = 1 box, whose mean field lies along x: every x
+    face then sits near the c_f = c_a degeneracy, where roeflux_m.f:68-100
+    divides by the small cfast2 - ca2 and bt, and hlld_flux.f90 meets its
+    zfloor guard.  One unit in the last place of the initial velocities
+    grows to more than 1e-12 of a field (Roe) and 1e-10 (HLLD) within 20
+    steps, a hundred times more than with an oblique mean field of the same
+    strength, where it stays below 1e-12."""
+    aligned = one_ulp_amplification(oracle_lib, solver, (1.0, 0.0, 0.0))
+    oblique = one_ulp_amplification(oracle_lib, solver, (0.8, 0.48, 0.36))
+    floor = 1e-12 if solver == "roe_m_3d" else 1e-10
+    assert max(aligned.values()) > floor, aligned
+    assert max(oblique.values()) < 1e-12, oblique
+    assert max(aligned.values()) > 100 * max(oblique.values())
+
+
 # ---- 2-D roe_m3 ---------------------------------------------------------------
 
 def _roe2(ix=16, jx=14, seed=3):

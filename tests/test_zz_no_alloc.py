@@ -51,6 +51,33 @@ def test_noalloc_cfl_matches_cfl_m3_on_two_calls(gpu, exact):
         gpu.set_exact(False)
 
 
+@pytest.mark.parametrize("exact", [True, False])
+def test_noalloc_cfl_at_and_past_one_fold_block(gpu, exact):
+    """Grids whose partials the final fold walks in strides of 1024: one at
+    the scratch limit (1024 x 1024 cells, 4096 partials) and one just over
+    1024 partials (600 x 440 cells, 1032), each against cans_cfl_m3_2d, on
+    two calls in a row."""
+    torch = pytest.importorskip("torch")
+    gpu.set_exact(exact)
+    try:
+        for ix, jx in ((1024, 1024), (600, 440)):
+            s = setups.random_state(ix, jx, seed=ix + jx)
+            st = s["state"]
+            ref_dt, ref_merr = gpu.cfl_m3(0.4, 1e-10, s["gm"], *st[:8], s["dx"], s["dy"])
+            dev = [_device_copy(torch, a) for a in st[:8]]
+            ddx, ddy = _device_copy(torch, s["dx"]), _device_copy(torch, s["dy"])
+            torch.cuda.synchronize()
+            dt, merr = gpu.cfl_m3_noalloc(0.4, 1e-10, s["gm"], [t.data_ptr() for t in dev],
+                                          ddx.data_ptr(), ddy.data_ptr(), ix, jx)
+            assert merr == ref_merr == 0
+            if exact:
+                assert dt == ref_dt
+            else:
+                assert abs(dt - ref_dt) <= 1e-13 * ref_dt
+    finally:
+        gpu.set_exact(False)
+
+
 def test_noalloc_rejects_grids_beyond_its_scratch(gpu):
     # 1025 x 1025 cells exceed the fixed scratch (1,048,576 cells); the call
     # is refused on the host before any device work

@@ -1,4 +1,5 @@
-"""Build the sm_103a CUDA library (libcansgpu.so) in-tree.
+"""Build the sm_103a CUDA library (libcansgpu.so) in-tree, and beside it the
+benchmark's peak probe (libcansprobe.so, not part of the solver's ABI).
 
 Each .cu translation unit is compiled by its own nvcc process (in parallel),
 then linked into utrip_gb300/_lib/libcansgpu.so.  Host code is compiled with
@@ -19,6 +20,8 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 OBJDIR = PKG / "_build"
 LIBNAME = "libcansgpu.so"
+PROBE = PKG / "probe" / "peaks.cu"
+PROBELIB = "libcansprobe.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -69,8 +72,15 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, lib)
+    probe = LIBDIR / PROBELIB
+    if not probe.exists() or probe.stat().st_mtime < PROBE.stat().st_mtime:
+        cmd = [nvcc(), ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+               str(PROBE), "-o", str(probe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"probe build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print(f"built {lib}")
+        print(f"built {lib} and {probe.name}")
     return lib
 
 

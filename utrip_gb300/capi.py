@@ -83,6 +83,9 @@ def load() -> C.CDLL:
         "cans_run_adjoint": (i, [vp, C.c_longlong, _dp, i, _dp, C.POINTER(_dp),
                                  C.POINTER(C.c_longlong)]),
         "cans_run_bc_transpose": (i, [vp, C.POINTER(_dp)]),
+        "cans_run_av_record": (i, [vp, C.c_longlong, _dp]),
+        "cans_run_objective_frozen_av": (i, [vp, C.c_longlong, _dp, _dp,
+                                             C.POINTER(C.c_longlong)]),
         "cans_batch_create": (i, [C.POINTER(vp), i, vp]), "cans_batch_destroy": (i, [vp]),
         "cans_batch_set_bc": (i, [vp, i, i, i, i, d]),
         "cans_batch_push": (i, [vp, i, C.POINTER(_dp)]),
@@ -91,7 +94,6 @@ def load() -> C.CDLL:
         "cans_batch_advance": (i, [vp, i, i]), "cans_batch_query": (i, [vp, i, vp]),
         "cans_batch_configs": (i, []), "cans_batch_set_config": (i, [vp, i]),
         "cans_batch_autotune": (i, [vp, i, _ip]),
-        "cans_measure_fp64_tflops": (i, [_dp]),
     }
     sig["cans_mlw_m_3d"] = (i, [_dp] * 8 + [_dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp, _ip,
                                              _dp, _dp, _ip])
@@ -735,6 +737,25 @@ class Run:
                "cans_run_objective")
         return J.value
 
+    def av_record(self, dts) -> None:
+        """Run the frozen dts from the current state and keep every face's
+        artificial-viscosity branch (active or not, sign of dv) on the
+        device, for objective_frozen_av."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        _check(self.lib.cans_run_av_record(self.h, dts.size, _ptr(dts)), "cans_run_av_record")
+
+    def objective_frozen_av(self, dts):
+        """The objective of the frozen dts with every viscosity face held at
+        its recorded branch; returns (J, nflip), nflip the face-steps whose
+        own branch differs from the recorded one."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        J = C.c_double(0.0)
+        nf = C.c_longlong(0)
+        _check(self.lib.cans_run_objective_frozen_av(self.h, dts.size, _ptr(dts), C.byref(J),
+                                                     C.byref(nf)),
+               "cans_run_objective_frozen_av")
+        return J.value, nf.value
+
     def adjoint(self, dts, nsnap: int = 32):
         """Reverse sweep with binomial checkpointing in nsnap stored states:
         returns (J, grad, nfwd), grad the list of dJ/dP_0 arrays (ghosts
@@ -752,12 +773,6 @@ class Run:
         """Transpose of the boundary program, in place on host arrays."""
         arr = (_dp * self.nvar)(*[_ptr(a) for a in arrays])
         _check(self.lib.cans_run_bc_transpose(self.h, arr), "cans_run_bc_transpose")
-
-
-def measure_fp64_tflops() -> float:
-    x = C.c_double(0.0)
-    _check(load().cans_measure_fp64_tflops(C.byref(x)), "cans_measure_fp64_tflops")
-    return x.value
 
 
 def _desc_for(solver: int, grid: dict, gm: float, qav: float, margin: int, exact: bool,

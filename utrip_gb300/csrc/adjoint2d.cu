@@ -524,42 +524,69 @@ __global__ void k_bc2d_t(int nvar, double *L, int ix, int jx, int axis, BcTable 
   }
 }
 
-// J = sum over the interior of (bx^2+by^2+bz^2)/(8 pi) dx dy (block partial
-// sums, reduced in a fixed order by k_sum_final) and its gradient
+// Error-free sum of two doubles (Knuth's TwoSum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  s = __dadd_rn(a, b);
+  const double bb = __dsub_rn(s, a);
+  e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+// (s, c) += (t, d): a compensated partial sum, the rounding errors of every
+// addition carried in c (the cascaded summation of Ogita, Rump and Oishi,
+// "Accurate sum and dot product", 2005), so that J is the exact sum of its
+// terms to about one rounding -- a finite difference of J then sees the
+// state's rounding, not that of a 65k-term sum.
+__device__ __forceinline__ void comp_add(double &s, double &c, double t, double d) {
+  double e;
+  two_sum(s, t, s, e);
+  c = __dadd_rn(c, __dadd_rn(d, e));
+}
+
+// J = sum over the interior of (bx^2+by^2+bz^2)/(8 pi) dx dy (compensated
+// block partial sums, reduced in a fixed order by k_sum_final) and its
+// gradient
 __global__ void __launch_bounds__(256)
     k_objective(const double *__restrict__ P, double *__restrict__ lam,
                 double *__restrict__ part, G2 g, Axis ax, Axis ay, Phys ph) {
-  __shared__ double red[256];
-  double s = 0.0;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.n;
-       c += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.ix), j = (int)(c / g.ix);
-    const double bx = P[P_BX * g.n + c], by = P[P_BY * g.n + c], bz = P[P_BZ * g.n + c];
+  __shared__ double red[2][256];
+  double s = 0.0, c = 0.0;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < g.n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % g.ix), j = (int)(k / g.ix);
+    const double bx = P[P_BX * g.n + k], by = P[P_BY * g.n + k], bz = P[P_BZ * g.n + k];
     const bool in = interior(g, i, j);
     const double w = in ? ax.d[i] * ay.d[j] : 0.0;
-    s += (bx * bx + by * by + bz * bz) * ph.pi8i * w;
+    comp_add(s, c, (bx * bx + by * by + bz * bz) * ph.pi8i * w, 0.0);
     if (lam) {
 #pragma unroll
-      for (int v = 0; v < 9; v++) lam[v * g.n + c] = 0.0;
-      lam[P_BX * g.n + c] = 2.0 * ph.pi8i * w * bx;
-      lam[P_BY * g.n + c] = 2.0 * ph.pi8i * w * by;
-      lam[P_BZ * g.n + c] = 2.0 * ph.pi8i * w * bz;
+      for (int v = 0; v < 9; v++) lam[v * g.n + k] = 0.0;
+      lam[P_BX * g.n + k] = 2.0 * ph.pi8i * w * bx;
+      lam[P_BY * g.n + k] = 2.0 * ph.pi8i * w * by;
+      lam[P_BZ * g.n + k] = 2.0 * ph.pi8i * w * bz;
     }
   }
-  red[threadIdx.x] = s;
+  red[0][threadIdx.x] = s;
+  red[1][threadIdx.x] = c;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    if ((int)threadIdx.x < o) {
+      double a = red[0][threadIdx.x], b = red[1][threadIdx.x];
+      comp_add(a, b, red[0][threadIdx.x + o], red[1][threadIdx.x + o]);
+      red[0][threadIdx.x] = a;
+      red[1][threadIdx.x] = b;
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = red[0][0];
+    part[2 * blockIdx.x + 1] = red[1][0];
+  }
 }
 
 __global__ void k_sum_final(const double *part, int nb, double *out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nb; b++) s += part[b];
-    *out = s;
+    double s = 0.0, c = 0.0;
+    for (int b = 0; b < nb; b++) comp_add(s, c, part[2 * b], part[2 * b + 1]);
+    *out = __dadd_rn(s, c);
   }
 }
 

@@ -62,6 +62,13 @@ cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
                          Box3 box, cudaStream_t s);
 int mlw2d_tile_count();
+// The mlw_m3 step (no control block) with the artificial viscosity's branch
+// recorded (mode 1) into, or held at (mode 2) the bytes of, avb: 2*ix*jx
+// bytes, x faces then y faces.  Mode 2 adds to *nflip the faces whose own
+// branch differs from the recorded one.
+cudaError_t launch_mlw2d_av(bool exact, int mode, const double *A, double *B, int ix, int jx,
+                            const Axis &ax, const Axis &ay, const Phys &ph, double dt,
+                            unsigned char *avb, unsigned long long *nflip, cudaStream_t s);
 // The same steps with gravity (mlw_m_g / mlw_m3_g): grav holds gx, gxm, gy,
 // gym, ix*jx doubles each, on the device.
 cudaError_t launch_mlw2d_g(int solver, bool exact, int tile, const double *A,

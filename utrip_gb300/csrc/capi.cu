@@ -1461,6 +1461,8 @@ struct cans_run {
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
+  unsigned char *avb = nullptr;  // adjoint check: recorded viscosity branches,
+  long long avb_steps = 0;       //   2*ix*jx bytes per step
 };
 
 namespace {
@@ -1837,6 +1839,7 @@ extern "C" int cans_run_destroy(cans_run *h) {
   if (h->grav) cudaFree(h->grav);
   if (h->eta) cudaFree(h->eta);
   if (h->res) cudaFree(h->res);
+  if (h->avb) cudaFree(h->avb);
   h->ax.release();
   h->ay.release();
   h->az.release();
@@ -2389,6 +2392,66 @@ extern "C" int cans_run_objective(cans_run *h, long long nsteps, const double *d
                             h->ay.a, h->ph, h->s));
   CK(cudaMemcpyAsync(J, W.J, sizeof(double), cudaMemcpyDeviceToHost, h->s));
   CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
+extern "C" int cans_run_av_record(cans_run *h, long long nsteps, const double *dts) {
+  NvtxRange nvtx("cans_run_av_record");
+  if (!h || nsteps < 1 || !dts || !adj_supported(h)) return CANS_ERR_ARG;
+  const size_t per = 2 * h->n;
+  if ((double)per * (double)nsteps > 64.0 * (1ull << 30)) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  if (h->avb_steps != nsteps) {
+    CK(cudaStreamSynchronize(h->s));
+    if (h->avb) cudaFree(h->avb);
+    h->avb = nullptr;
+    h->avb_steps = 0;
+    CK(cudaMalloc(&h->avb, per * (size_t)nsteps));
+  }
+  AdjWork W;
+  if ((rc = adj_setup(h, W, 0))) return rc;
+  const double *src = h->buf[h->host_ctl.cur];
+  int cur = 0;
+  for (long long k = 0; k < nsteps; k++) {
+    CK(launch_mlw2d_av(h->d.exact != 0, 1, src, W.w[cur], h->d.ix, h->d.jx, h->ax.a, h->ay.a,
+                       h->ph, dts[k], h->avb + per * (size_t)k, nullptr, h->s));
+    CK(bc_kernels(h, W.w[cur], nullptr));
+    src = W.w[cur];
+    cur ^= 1;
+  }
+  CK(cudaStreamSynchronize(h->s));
+  h->avb_steps = nsteps;
+  return CANS_OK;
+}
+
+extern "C" int cans_run_objective_frozen_av(cans_run *h, long long nsteps, const double *dts,
+                                            double *J, long long *nflip) {
+  NvtxRange nvtx("cans_run_objective_frozen_av");
+  if (!h || nsteps < 1 || !dts || !J || !adj_supported(h)) return CANS_ERR_ARG;
+  if (!h->avb || nsteps > h->avb_steps) return CANS_ERR_ARG;
+  int rc = read_ctl(h);
+  if (rc) return rc;
+  AdjWork W;
+  if ((rc = adj_setup(h, W, 0))) return rc;
+  const size_t per = 2 * h->n;
+  CK(cudaMemsetAsync(W.bits, 0, sizeof(unsigned long long), h->s));
+  const double *src = h->buf[h->host_ctl.cur];
+  int cur = 0;
+  for (long long k = 0; k < nsteps; k++) {
+    CK(launch_mlw2d_av(h->d.exact != 0, 2, src, W.w[cur], h->d.ix, h->d.jx, h->ax.a, h->ay.a,
+                       h->ph, dts[k], h->avb + per * (size_t)k, W.bits, h->s));
+    CK(bc_kernels(h, W.w[cur], nullptr));
+    src = W.w[cur];
+    cur ^= 1;
+  }
+  CK(launch_adj2d_objective(src, nullptr, W.J, W.scr, h->d.ix, h->d.jx, h->ax.a, h->ay.a,
+                            h->ph, h->s));
+  unsigned long long flips = 0;
+  CK(cudaMemcpyAsync(J, W.J, sizeof(double), cudaMemcpyDeviceToHost, h->s));
+  CK(cudaMemcpyAsync(&flips, W.bits, sizeof flips, cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  if (nflip) *nflip = (long long)flips;
   return CANS_OK;
 }
 

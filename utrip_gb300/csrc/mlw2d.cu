@@ -33,6 +33,38 @@ __global__ void __launch_bounds__(TX *TY / RPT, 1)
                                 nullptr, nullptr, ctl ? &ctl->nonfinite : nullptr);
 }
 
+// The mlw_m3 step with the artificial viscosity's branch recorded (AVF = 1)
+// or held at the recorded one (AVF = 2): the forward of the adjoint's
+// finite-difference check (see tile_step).  32 x 8 tiles, no control block.
+template <bool E, int AVF>
+__global__ void __launch_bounds__(128, 1)
+    k_mlw2d_av(const double *__restrict__ A, double *__restrict__ B, int ix, int jx, Axis ax,
+               Axis ay, Phys ph, double dt, unsigned char *avb, unsigned long long *nflip) {
+  extern __shared__ double smem[];
+  tile_step<E, true, 32, 8, 2, false, false, AVF>(
+      A, B, ix, jx, ax, ay, ph, dt, 0.0, nullptr, Box3{}, blockIdx.x, blockIdx.y, gridDim.x,
+      gridDim.y, smem, nullptr, nullptr, nullptr, avb, nflip);
+}
+
+cudaError_t launch_mlw2d_av(bool exact, int mode, const double *A, double *B, int ix, int jx,
+                            const Axis &ax, const Axis &ay, const Phys &ph, double dt,
+                            unsigned char *avb, unsigned long long *nflip, cudaStream_t s) {
+  if (ix < 3 || jx < 3 || (mode != 1 && mode != 2) || !avb || (mode == 2 && !nflip))
+    return cudaErrorInvalidValue;
+  using T = Tile<32, 8, true, 2>;
+  void (*k)(const double *, double *, int, int, Axis, Axis, Phys, double, unsigned char *,
+            unsigned long long *) =
+      exact ? (mode == 1 ? k_mlw2d_av<true, 1> : k_mlw2d_av<true, 2>)
+            : (mode == 1 ? k_mlw2d_av<false, 1> : k_mlw2d_av<false, 2>);
+  cudaError_t e =
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+  if (e != cudaSuccess) return e;
+  dim3 grid((ix - 2 + 31) / 32, (jx - 2 + 7) / 8);
+  k<<<grid, T::NT, T::smem_bytes, s>>>(A, B, ix, jx, ax, ay, ph, dt, avb, nflip);
+  count_launch();
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Tile configurations offered to the autotuner: (TX, TY).
 namespace {

@@ -31,6 +31,18 @@
 // [x, y, z at the cells, x, y, z at the corners] (ix*jx each) for mlw_m3 and
 // [z at the cells, z at the corners] for mlw_m.
 //
+// With AVF the artificial viscosity's branch is recorded (AVF = 1) or held
+// (AVF = 2), for the finite-difference check of the discrete adjoint: the
+// coefficient q = qav dxm max(0, |dv| - 1e-4) of mlw_m3.f:325-334 is
+// piecewise affine in dv, and the adjoint is the derivative of the branch
+// the base run took.  Per face one byte: bit 0 = |dv| - 1e-4 > 0 (active),
+// bit 1 = dv < 0.  Recording leaves every result unchanged; holding takes
+// q = qav dxm (s dv - 1e-4) on the faces recorded active (s the recorded
+// sign) and 0 on the others, and counts the faces whose own branch differs
+// from the recorded one (each face once).  avb holds the x faces (i, j)
+// between cells i and i+1, then the y faces (i, j) between rows j and j+1,
+// ix*jx bytes each.
+//
 // In the exact policy every operation is the reference's, in its order, so
 // the result equals a -ffp-contract=off CPU build of the Fortran bit for bit.
 // Terms whose flux is identically zero (fx of bx, fy of by) are skipped: the
@@ -107,20 +119,41 @@ template <int TX, int TY, bool M3, int RPT = 2, bool G = false> struct Tile {
 // Zero-flux marker for the corrector / central-difference helpers.
 constexpr int NOFLUX = -1;
 
+// Branch byte of one viscosity face (see tile_step): the face's own branch
+// from dv and a = |dv| - 1e-4 is recorded (AVF = 1) and returned, or
+// compared with the recorded one, which is returned (AVF = 2); a face a
+// tile owns counts a flip of its active bit (or of its sign while active).
+template <int AVF, class FT>
+__device__ __forceinline__ unsigned char av_branch(double dv, FT a, unsigned char *slot,
+                                                   unsigned long long *nflip, bool owned) {
+  const unsigned char mine = (unsigned char)((a.v > 0.0 ? 1 : 0) | (dv < 0.0 ? 2 : 0));
+  if constexpr (AVF == 1) {
+    *slot = mine;
+    return mine;
+  } else {
+    const unsigned char rec = *slot;
+    const unsigned char x = rec ^ mine;
+    if (owned && ((x & 1) || ((rec & mine & 1) && (x & 2)))) atomicAdd(nflip, 1ull);
+    return rec;
+  }
+}
+
 }  // namespace
 
 // One TX x TY tile of one grid: the whole fused step.  Called by the
 // single-grid kernel (one tile per block) and by the batched kernel (tiles
 // of many grids pulled from a work queue by persistent blocks).  If cfl_out
 // is non-null the CFL of the written cells inside `box` is reduced into it.
-template <bool E, bool M3, int TX, int TY, int RPT, bool G = false, bool R = false>
+template <bool E, bool M3, int TX, int TY, int RPT, bool G = false, bool R = false,
+          int AVF = 0>
 __device__ __forceinline__ void tile_step(
     const double *__restrict__ A, double *__restrict__ B, int ix, int jx,
     const Axis &ax, const Axis &ay, const Phys &ph, double dtv, double safety,
     unsigned long long *cfl_out, const Box3 &box, int tile_x, int tile_y,
     int ntiles_x, int ntiles_y, double *smem,
     const double *__restrict__ grav = nullptr,
-    const double *__restrict__ res = nullptr, int *bad_out = nullptr) {
+    const double *__restrict__ res = nullptr, int *bad_out = nullptr,
+    unsigned char *avb = nullptr, unsigned long long *nflip = nullptr) {
   using T = Tile<TX, TY, M3, RPT, G>;
   using C = CellSlots<M3>;
   using K = CornerSlots<M3>;
@@ -379,9 +412,19 @@ __device__ __forceinline__ void tile_step(
     double v = 0.0;
     if (gi + 1 < ix && gj < jx) {
       const int cl = fx + (r + 1) * T::CX;
-      const FT q = qav * FT(ax.dm[gi]) *
-                   max0(fabs_(FT(SC(C::VX, cl + 1)) - FT(SC(C::VX, cl))) - CANS_AV_EPS);
-      v = (q * FT(ax.dim[gi])).v;
+      if constexpr (AVF == 0) {
+        const FT q = qav * FT(ax.dm[gi]) *
+                     max0(fabs_(FT(SC(C::VX, cl + 1)) - FT(SC(C::VX, cl))) - CANS_AV_EPS);
+        v = (q * FT(ax.dim[gi])).v;
+      } else {
+        const FT d = FT(SC(C::VX, cl + 1)) - FT(SC(C::VX, cl));
+        const size_t gf = (size_t)gi + (size_t)gj * ix;
+        const unsigned char br = av_branch<AVF>(d.v, fabs_(d) - CANS_AV_EPS, avb + gf, nflip,
+                                                fx > 0 || tile_x == 0);
+        FT q(0.0);
+        if (br & 1) q = qav * FT(ax.dm[gi]) * (((br & 2) ? -d : d) - CANS_AV_EPS);
+        v = (q * FT(ax.dim[gi])).v;
+      }
     }
     sqx[f] = v;
   }
@@ -391,9 +434,19 @@ __device__ __forceinline__ void tile_step(
     double v = 0.0;
     if (gi < ix && gj + 1 < jx) {
       const int cl = (fx + 1) + r * T::CX;
-      const FT q = qav * FT(ay.dm[gj]) *
-                   max0(fabs_(FT(SC(C::VY, cl + T::CX)) - FT(SC(C::VY, cl))) - CANS_AV_EPS);
-      v = (q * FT(ay.dim[gj])).v;
+      if constexpr (AVF == 0) {
+        const FT q = qav * FT(ay.dm[gj]) *
+                     max0(fabs_(FT(SC(C::VY, cl + T::CX)) - FT(SC(C::VY, cl))) - CANS_AV_EPS);
+        v = (q * FT(ay.dim[gj])).v;
+      } else {
+        const FT d = FT(SC(C::VY, cl + T::CX)) - FT(SC(C::VY, cl));
+        const size_t gf = n + (size_t)gi + (size_t)gj * ix;
+        const unsigned char br = av_branch<AVF>(d.v, fabs_(d) - CANS_AV_EPS, avb + gf, nflip,
+                                                r > 0 || tile_y == 0);
+        FT q(0.0);
+        if (br & 1) q = qav * FT(ay.dm[gj]) * (((br & 2) ? -d : d) - CANS_AV_EPS);
+        v = (q * FT(ay.dim[gj])).v;
+      }
     }
     sqy[f] = v;
   }

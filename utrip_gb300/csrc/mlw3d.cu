@@ -30,6 +30,8 @@
 // to E = -v x B where the reference adds et*c and etm*ch.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "cans_common.cuh"
 #include "cans_internal.h"
 #include "cfl3.cuh"
@@ -742,6 +744,8 @@ int balance_kchunk(long long bxy, int nz, int kmax, int slots) {
   return best;
 }
 
+constexpr int kMaxDevices3 = 64;
+
 template <bool E, int TX, int TY, bool G = false, bool R = false>
 cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
                     const Axis &ax, const Axis &ay, const Axis &az,
@@ -749,22 +753,30 @@ cudaError_t launch3(const double *A, double *B, int ix, int jx, int kx,
                     cudaStream_t s, const double *grav = nullptr,
                     const double *res = nullptr) {
   using T = Tile3<TX, TY, G>;
-  static bool attr = false;
-  static int slots = 0;  // resident blocks on the whole GPU
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY, G, R>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)T::smem_bytes);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0, per_sm = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-      return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-             &per_sm, k_mlw3d<E, TX, TY, G, R>, T::NT, T::smem_bytes)) != cudaSuccess)
-      return e;
-    slots = sms * (per_sm > 0 ? per_sm : 1);
-    attr = true;
+  // per device: the shared-memory attribute is set and the resident blocks
+  // on the whole GPU counted once, under a lock (launches may come from
+  // several host threads and devices)
+  static std::mutex mu;
+  static int slots_of[kMaxDevices3] = {};
+  int dev = 0, slots = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices3) return cudaErrorInvalidDevice;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!slots_of[dev]) {
+      e = cudaFuncSetAttribute(k_mlw3d<E, TX, TY, G, R>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem_bytes);
+      if (e != cudaSuccess) return e;
+      int sms = 0, per_sm = 0;
+      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return e;
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+               &per_sm, k_mlw3d<E, TX, TY, G, R>, T::NT, T::smem_bytes)) != cudaSuccess)
+        return e;
+      slots_of[dev] = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    slots = slots_of[dev];
   }
   const int bx = (ix - 2 + TX - 1) / TX, by = (jx - 2 + TY - 1) / TY;
   kchunk = balance_kchunk((long long)bx * by, kx - 2, kchunk, slots);

@@ -18,7 +18,6 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
-#include <mutex>
 
 #include "cans_gpu.h"
 #include "cans_internal.h"
@@ -71,7 +70,7 @@ __global__ void __launch_bounds__(kNoAllocThreads)
     const int i = (int)(g % ix), j = (int)(g / ix);
     const double d = cfl_m3_cell<E>(ro[g], pr[g], vx[g], vy[g], vz[g], bx[g],
                                         by[g], bz[g], dx[i], dy[j], gm, pi4i, safety);
-    if (d >= 0.0) v = d;  // a NaN never becomes the minimum
+    if (d < v) v = d;  // as cfl_m3.f's `if (dtq .lt. dt)`: a NaN never becomes the minimum
   }
   const double m = block_min(v, red, threadIdx.x, kNoAllocThreads);
   if (threadIdx.x == 0) scratch[blockIdx.x] = m;
@@ -91,23 +90,16 @@ __global__ void __launch_bounds__(1024) k_cfl_m3_final(double *scratch, int nblo
 }
 
 namespace {
-// Device address of the scratch array, looked up once per device.
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-double *g_noalloc_ptr[kMaxDevices] = {};
-
+// Device address of the scratch array on the current device.  It is looked
+// up on every call: the lookup allocates nothing and does no device work once
+// the module is loaded, and a cached address would go stale if the host
+// reset the device between calls.  The first call on a device loads the
+// module, so it should come before any stream capture.
 int noalloc_scratch(double **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  double *p = nullptr;
+  if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p)
     return CANS_ERR_CUDA;
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    double *p = nullptr;
-    if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p)
-      return CANS_ERR_CUDA;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  *out = p;
   return CANS_OK;
 }
 }  // namespace
