@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--mlw-steps", type=int, default=100)
     p.add_argument("--n", type=int, default=N_CELLS)
     p.add_argument("--exact", action="store_true", help="exact arithmetic policy")
+    p.add_argument("--df64", action="store_true",
+                   help="double-float policy of the 2-D mlw_m3 step (FP32 pipes, FP64 "
+                        "accumulation)")
     p.add_argument("--tile", type=int, default=-1,
                    help="2-D tile configuration (default: autotuned)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -427,27 +430,32 @@ def spicule_workload(stream, nstop=100000, cpu_steps=4000):
     return res
 
 
-def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=1e-6):
+def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=1e-6,
+                     h_smooth=2e-5):
     """The differentiation pattern on the 2-D shear layer at beta = 1 (256^2,
     mlw_m3, 2000 steps, J = final magnetic energy): the reverse sweep with
     binomial checkpointing in 32 stored states timed against the forward run
-    of the same frozen dt sequence, and its directional derivatives checked
-    against FP64 central differences (h = 1e-6) on 16 seeded directions of
-    the initial vy field, and dJ/dbeta.
+    of the same frozen dt sequence, and its directional derivatives on 16
+    seeded directions of the initial vy field, and dJ/dbeta, checked against
+    FP64 central differences.
 
-    The artificial viscosity q = qav dxm max(0, |dv| - 1e-4) is piecewise
-    affine in dv, and the shear layer has velocity jumps near 1e-4, so J has
-    kinks within h of the base point.  The reverse sweep is the derivative
-    of the branches the base run took; its check therefore holds every
-    face's branch at the recorded one (cans_run_av_record /
-    cans_run_objective_frozen_av), and reports per direction how many face
-    switches the unheld run crosses at +h and -h beside the unheld central
-    difference.  J also bends on the 1e-3 scale of the perturbation the
-    shear layer amplifies, which puts the h^2 term of a second-order
-    difference near 1e-7..1e-6 of J'; the held check uses the fourth-order
-    central difference from h and 2h (both second-order ones are reported).
-    qav = 0 (no viscosity, J smooth) is checked the same way, against the
-    GPU forward and, on two directions, the CPU oracle."""
+    Two properties of J set the terms of the check.  (1) Its rounding noise:
+    J of the fast and of the exact policy differ by about 1e-14 of J (the
+    unstable shear layer amplifies rounding over 2000 steps), so a central
+    difference at h = 1e-6 carries an error near 1e-14 J / h, a few 1e-6 of
+    the smaller directional derivatives.  The h = 1e-6 difference is
+    reported; the 1e-6 criterion is taken on the fourth-order difference
+    from h_smooth and 2 h_smooth, where J (qav = 0) is smooth and the noise
+    is 20 times smaller.  (2) The artificial viscosity q = qav dxm
+    max(0, |dv| - 1e-4) is piecewise affine in dv and the shear layer has
+    velocity jumps at 1e-4 everywhere: at qav = 3 every direction crosses
+    about a million face switches within +-h (counted).  The adjoint is the
+    derivative of the branches the base run took; the check holding every
+    face at its recorded branch (cans_run_objective_frozen_av) is smooth but
+    leaves negative viscosity on faces pushed past their switch, which makes
+    it strongly non-linear (it diverges beyond about 1e-5).  So qav = 3 is
+    reported, not held to 1e-6; qav = 0 carries the 1e-6 check, with two
+    directions also against the CPU oracle's forward."""
     import torch
     import oracle
     from utrip_gb300 import drivers, setups
@@ -480,10 +488,10 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
         oracle.apply_bc_program(z, s["bc"], s["margin"], s)
         return z
 
-    def fd24(J):
-        """second-order differences at h and 2h, and the fourth-order one."""
-        d1 = (J[1] - J[-1]) / (2 * h)
-        d2 = (J[2] - J[-2]) / (4 * h)
+    def fd24(J, hh):
+        """second-order differences at hh and 2 hh, and the fourth-order one."""
+        d1 = (J[1] - J[-1]) / (2 * hh)
+        d2 = (J[2] - J[-2]) / (4 * hh)
         return d1, d2, (4.0 * d1 - d2) / 3.0
 
     def oracle_J(s, st, dts):
@@ -495,14 +503,9 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
         e = (st[5] ** 2 + st[6] ** 2 + st[7] ** 2)[1:-1, 1:-1]
         return float(np.sum(e * w)) / np.pi / 8.0
 
-    out = {"nsteps": nsteps, "nsnap": nsnap, "h": h,
+    out = {"nsteps": nsteps, "nsnap": nsnap, "h": h, "h_smooth": h_smooth,
            "directions": "seeded unit-RMS fields of the |k| <= 8 Fourier modes of vy",
-           "criterion": "|adjoint - fd| <= 1e-6 |fd| + 8 eps |J| / 2h"}
-    eps = float(np.finfo(np.float64).eps)
-
-    def within(ad, fd, J):
-        return abs(ad - fd) <= 1e-6 * abs(fd) + 8 * eps * abs(J) / (2 * h)
-
+           "criterion": "|adjoint - fd4(h_smooth)| <= 1e-6 |fd4| at qav = 0"}
     for qav in (3.0, 0.0):
         s = base(1.0, qav)
         run = drivers.make_run(s, stream=stream.cuda_stream)
@@ -526,69 +529,89 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
                 "adjoint_s": time.perf_counter() - t0, "forward_steps_in_adjoint": int(nfwd_all),
                 "grad_equal_to_checkpointed": all(np.array_equal(a, b)
                                                   for a, b in zip(g_all, grad))}
-        run.av_record(dts)
-        J_held0, flips0 = run.objective_frozen_av(dts)
+        rx = drivers.make_run(s, exact=True, stream=stream.cuda_stream)
+        rx.push(s["state"])
+        J_exact = rx.objective(dts)
+        rx.close()
+        if qav == 3.0:
+            run.av_record(dts)
+            J_held0, flips0 = run.objective_frozen_av(dts)
         rng = np.random.default_rng(5)
-        dirs, n_held, n_unheld = [], 0, 0
+        dirs, n_pass, n_pass_1e6 = [], 0, 0
         for k in range(ndir):
             d = smooth_direction(rng, 256)
             z = extend(s, d)
             ad = sum(float(np.sum(g * e)) for g, e in zip(grad, z))
-            Jh, fl = {}, {}
-            for m in (1, -1, 2, -2):
+            Jh = {}
+            for m in (1, -1):
                 run.push(shifted(s, z, m * h))
-                Jh[m], fl[m] = run.objective_frozen_av(dts)
-            run.push(shifted(s, z, h))
-            jp = run.objective(dts)
-            run.push(shifted(s, z, -h))
-            jm = run.objective(dts)
-            fd_unheld = (jp - jm) / (2 * h)
-            d1, d2, d4 = fd24(Jh)
-            n_held += within(ad, d4, J)
-            n_unheld += within(ad, fd_unheld, J)
-            row = {"adjoint": ad, "held_fd4_rel_err": abs(ad - d4) / abs(d4),
-                   "held_fd2_h_rel_err": abs(ad - d1) / abs(d4),
-                   "held_fd2_2h_rel_err": abs(ad - d2) / abs(d4),
-                   "unheld_fd2_rel_err": abs(ad - fd_unheld) / abs(fd_unheld),
-                   "switches_crossed_plus_h": int(fl[1]), "switches_crossed_minus_h": int(fl[-1])}
-            if qav == 0.0 and k < n_oracle_dirs:
-                Jo = {m: oracle_J(s, shifted(s, z, m * h), dts) for m in (1, -1, 2, -2)}
-                o1, _, o4 = fd24(Jo)
-                row["oracle_fd4_rel_err"] = abs(ad - o4) / abs(o4)
-                row["oracle_fd2_rel_err"] = abs(ad - o1) / abs(o4)
+                Jh[m] = run.objective(dts)
+            fd_h = (Jh[1] - Jh[-1]) / (2 * h)
+            row = {"adjoint": ad, "fd2_h_rel_err": abs(ad - fd_h) / abs(fd_h),
+                   "fd2_h_noise_floor_rel": abs(J - J_exact) / h / abs(ad)}
+            n_pass_1e6 += abs(ad - fd_h) <= 1e-6 * abs(fd_h)
+            if qav == 3.0:
+                Jf, fl = {}, {}
+                for m in (1, -1, 2, -2):
+                    run.push(shifted(s, z, m * h))
+                    Jf[m], fl[m] = run.objective_frozen_av(dts)
+                f1, _, f4 = fd24(Jf, h)
+                row.update({"held_fd2_h_rel_err": abs(ad - f1) / abs(f4),
+                            "held_fd4_h_rel_err": abs(ad - f4) / abs(f4),
+                            "switches_crossed_plus_h": int(fl[1]),
+                            "switches_crossed_minus_h": int(fl[-1])})
+            else:
+                Js = {}
+                for m in (1, -1, 2, -2):
+                    run.push(shifted(s, z, m * h_smooth))
+                    Js[m] = run.objective(dts)
+                _, _, f4 = fd24(Js, h_smooth)
+                row["fd4_smooth_rel_err"] = abs(ad - f4) / abs(f4)
+                n_pass += abs(ad - f4) <= 1e-6 * abs(f4)
+                if k < n_oracle_dirs:
+                    Jo = {m: oracle_J(s, shifted(s, z, m * h_smooth), dts) for m in (1, -1, 2, -2)}
+                    _, _, o4 = fd24(Jo, h_smooth)
+                    row["oracle_fd4_smooth_rel_err"] = abs(ad - o4) / abs(o4)
             dirs.append(row)
-        run.push(s["state"])
         # dJ/dbeta: p = 0.625 beta in every cell
         dbeta = 0.625 * float(np.sum(grad[1]))
+        hb = h_smooth if qav == 0.0 else h
         Jb = {}
         for m in (1, -1, 2, -2):
-            run.push(base(1.0 + m * h, qav)["state"])
-            Jb[m], _ = run.objective_frozen_av(dts)
-        b1, _, b4 = fd24(Jb)
+            run.push(base(1.0 + m * hb, qav)["state"])
+            Jb[m] = run.objective_frozen_av(dts)[0] if qav == 3.0 else run.objective(dts)
+        b1, _, b4 = fd24(Jb, hb)
         run.push(base(1.0 + h, qav)["state"])
         jbp = run.objective(dts)
         run.push(base(1.0 - h, qav)["state"])
         jbm = run.objective(dts)
         run.close()
-        held = [r["held_fd4_rel_err"] for r in dirs]
-        out[f"qav{qav:g}"] = {
-            "J": J, "J_replay_equal": J_fwd == J and J_adj == J,
-            "J_held_equal": J_held0 == J and flips0 == 0,
-            "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
-            "forward_steps_in_adjoint": int(nfwd),
-            "held_fd4_within_1e-6": f"{n_held}/{ndir}",
-            "held_fd4_rel_err_max": max(held), "held_fd4_rel_err_median": float(np.median(held)),
-            "unheld_fd2_within_1e-6": f"{n_unheld}/{ndir}",
-            "unheld_fd2_rel_err_median": float(np.median([r["unheld_fd2_rel_err"]
-                                                          for r in dirs])),
-            "switches_crossed_per_direction": [r["switches_crossed_plus_h"] +
-                                               r["switches_crossed_minus_h"] for r in dirs],
-            "dJ_dbeta": dbeta, "dJ_dbeta_held_fd4": b4,
-            "dJ_dbeta_held_fd4_rel_err": abs(dbeta - b4) / abs(b4),
-            "dJ_dbeta_held_fd2_rel_err": abs(dbeta - b1) / abs(b4),
-            "dJ_dbeta_unheld_fd2_rel_err": abs(dbeta - (jbp - jbm) / (2 * h)) /
-            abs((jbp - jbm) / (2 * h)),
-            "directions": dirs}
+        leg = {"J": J, "J_replay_equal": J_fwd == J and J_adj == J,
+               "J_rel_diff_fast_vs_exact_policy": abs(J - J_exact) / abs(J),
+               "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
+               "forward_steps_in_adjoint": int(nfwd),
+               "fd2_h_within_1e-6": f"{n_pass_1e6}/{ndir}",
+               "fd2_h_rel_err_median": float(np.median([r["fd2_h_rel_err"] for r in dirs])),
+               "dJ_dbeta": dbeta,
+               "dJ_dbeta_fd2_h_rel_err": abs(dbeta - (jbp - jbm) / (2 * h)) /
+               abs((jbp - jbm) / (2 * h)),
+               "directions": dirs}
+        if qav == 0.0:
+            e4 = [r["fd4_smooth_rel_err"] for r in dirs]
+            leg.update({"fd4_smooth_within_1e-6": f"{n_pass}/{ndir}",
+                        "fd4_smooth_rel_err_max": max(e4),
+                        "fd4_smooth_rel_err_median": float(np.median(e4)),
+                        "dJ_dbeta_fd4_smooth_rel_err": abs(dbeta - b4) / abs(b4)})
+        else:
+            e4 = [r["held_fd4_h_rel_err"] for r in dirs]
+            leg.update({"J_held_equal": J_held0 == J and flips0 == 0,
+                        "held_fd4_h_rel_err_median": float(np.median(e4)),
+                        "held_fd4_h_rel_err_max": max(e4),
+                        "switches_crossed_per_direction": [
+                            r["switches_crossed_plus_h"] + r["switches_crossed_minus_h"]
+                            for r in dirs],
+                        "dJ_dbeta_held_fd4_h_rel_err": abs(dbeta - b4) / abs(b4)})
+        out[f"qav{qav:g}"] = leg
     if "store_all_states" in out:
         out["store_all_states"]["adjoint_over_forward"] = (out["store_all_states"]["adjoint_s"]
                                                            / out["qav3"]["forward_s"])
@@ -773,20 +796,21 @@ def parity_check(n, stream, nsteps=100, c3_n=256, c3_steps=200, c3_riemann_steps
         ref = setups.copy_state(s)
         t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, nstop)
         leg = {"steps": int(ns_ref), "t": t_ref}
-        for exact in (False, True):
+        for policy in ("fast", "exact", "df64"):
             got = setups.copy_state(s)
-            run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
-            t, ns, merr, _ = drivers.run_resident(s, got, nstop, exact=exact, run=run)
+            run = drivers.make_run(s, exact=policy == "exact", stream=stream.cuda_stream,
+                                   df64=policy == "df64")
+            t, ns, merr, _ = drivers.run_resident(s, got, nstop, run=run)
             run.close()
-            if exact:
+            if policy == "exact":
                 leg["exact_cells_differing"] = int(sum(int(np.sum(a != b))
                                                        for a, b in zip(got, ref)))
                 leg["exact_same_t_and_steps"] = bool(t == t_ref and ns == ns_ref)
             else:
-                leg["fast_rel_linf"] = _rel_linf(s["names"], got, ref)
-                leg["fast_steps"] = int(ns)
-                leg["conservation_drift_fast"] = _drift(_totals(s, s["state"]),
-                                                        _totals(s, got))
+                leg[f"{policy}_rel_linf"] = _rel_linf(s["names"], got, ref)
+                leg[f"{policy}_steps"] = int(ns)
+                leg[f"conservation_drift_{policy}"] = _drift(_totals(s, s["state"]),
+                                                             _totals(s, got))
         leg["conservation_drift_oracle"] = _drift(_totals(s, s["state"]), _totals(s, ref))
         out[label] = leg
     out["conservation_note"] = ("relative change of the interior totals over the run; "
@@ -1081,7 +1105,8 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     assert stream.cuda_stream != 0
-    run = drivers.make_run(s, exact=args.exact, stream=stream.cuda_stream, tile=args.tile)
+    run = drivers.make_run(s, exact=args.exact, stream=stream.cuda_stream, tile=args.tile,
+                           df64=args.df64)
     run.push(setups.copy_state(s))
     tile = run.autotune(5) if args.tile < 0 else args.tile
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -1163,7 +1188,8 @@ def run_ours(args, ws, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"orszag_tang_{n}x{n}_mlw_m3", "solver": "mlw_m3",
                    "grid": [n + 2, n + 2], "mlw_steps_per_bench_step": m,
-                   "policy": "exact" if args.exact else "fast", "tile": tile,
+                   "policy": "exact" if args.exact else ("df64" if args.df64 else "fast"),
+                   "tile": tile,
                    "l2": "flushed between benchmark steps (256 MiB write)",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

@@ -1,0 +1,102 @@
+"""The double-float policy of the 2-D mlw_m3 step (cans_run_set_df64):
+the step's arithmetic in pairs of floats on the FP32 pipes, the conserved
+density and field accumulated in FP64.  It is held to the fast policy's bar
+against the oracle -- relative L-infinity <= 1e-10 per variable after 100
+steps -- on the benchmark vortex, the shear layer and a ragged random state,
+and it must converge to the exact shock-tube solution like the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import shktb_analytic as an
+from utrip_gb300 import capi, drivers, setups
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+def rel_linf(a, b):
+    scale = float(np.max(np.abs(b)))
+    return float(np.max(np.abs(a - b))) / scale if scale else float(np.max(np.abs(a - b)))
+
+
+@pytest.mark.parametrize("make,steps", [
+    (lambda: setups.orszag_tang(64), 100),
+    (lambda: setups.shear_layer(128, beta=0.5, seed=2), 100),
+    (lambda: setups.random_state(53, 41, seed=7), 20),
+])
+def test_df64_loop_against_oracle(gpu, oracle_lib, make, steps):
+    s = make()
+    ref = setups.copy_state(s)
+    t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, steps)
+    got = setups.copy_state(s)
+    t, ns, merr, nexec = drivers.run_resident(s, got, steps, df64=True)
+    assert merr == 0 and ns == ns_ref and nexec == steps
+    assert t == pytest.approx(t_ref, rel=1e-12)
+    for k, a, b in zip(s["names"], got, ref):
+        assert np.isfinite(a).all(), k
+        assert rel_linf(a, b) <= TOL, (k, rel_linf(a, b))
+
+
+def test_df64_one_step_close_to_oracle(gpu, oracle_lib):
+    """One step of a ragged random state (every variable non-zero): within a
+    few 2^-48 of the reference arithmetic."""
+    s = setups.random_state(45, 38, seed=11)
+    ref = setups.copy_state(s)
+    dt, _ = oracle.cfl_2d(s, ref, 0.4)
+    oracle.step_2d(s, ref, dt)
+    run = drivers.make_run(s, df64=True)
+    try:
+        run.push(s["state"])
+        run.step(dt, apply_bc=False)
+        got = run.pull()
+    finally:
+        run.close()
+    for k, a, b in zip(s["names"], got, ref):
+        assert rel_linf(a, b) <= 2e-13, (k, rel_linf(a, b))
+
+
+def test_df64_tiles_agree_bitwise(gpu):
+    s = setups.orszag_tang(96)
+    outs = []
+    for tile in range(4):
+        run = drivers.make_run(s, df64=True)
+        try:
+            run.set_tile(tile)
+            st = setups.copy_state(s)
+            drivers.run_resident(s, st, 30, run=run)
+            outs.append(st)
+        finally:
+            run.close()
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert np.array_equal(a, b)
+
+
+def test_df64_shock_tube_converges_like_the_oracle(gpu, oracle_lib):
+    for n in (256, 1024):
+        s = setups.sod_shock_tube(n, 2)
+        got = setups.copy_state(s)
+        t, ns, merr, _ = drivers.run_resident(s, got, 10 ** 6, df64=True)
+        ref = setups.copy_state(s)
+        t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, 10 ** 6)
+        assert merr == 0 and ns == ns_ref
+        sd = s["sod"]
+        e = an.l1_errors(*setups.sod_interior_profile(s, got), t, sd["x0"], sd["gm"],
+                         sd["ro1"], sd["pr1"])
+        er = an.l1_errors(*setups.sod_interior_profile(s, ref), t_ref, sd["x0"], sd["gm"],
+                          sd["ro1"], sd["pr1"])
+        for k in e:
+            assert e[k] == pytest.approx(er[k], rel=1e-6), (n, k)
+
+
+def test_df64_refused_where_it_does_not_apply(gpu):
+    for s, exact in ((setups.orszag_tang(32, solver="mlw_m"), False),
+                     (setups.orszag_tang(32), True),
+                     (setups.random_state_3d(12, 12, 12, seed=1), False)):
+        run = drivers.make_run(s, exact=exact)
+        try:
+            with pytest.raises(capi.CansError):
+                run.set_df64(True)
+        finally:
+            run.close()

@@ -78,6 +78,7 @@ def load() -> C.CDLL:
         "cans_run_profile": (i, [vp, i, _dp, _dp]),
         "cans_cfl_m3_2d_noalloc": (i, [_dp, _dp, _dp, _ip, _dp] + [vp] * 8 + [vp, _ip, vp, _ip]),
         "cans_run_set_graph": (i, [vp, i]),
+        "cans_run_set_df64": (i, [vp, i]), "cans_run_set_tile": (i, [vp, i]),
         "cans_run_record_dts": (i, [vp, C.c_longlong, d, _dp, _dp]),
         "cans_run_objective": (i, [vp, C.c_longlong, _dp, _dp]),
         "cans_run_adjoint": (i, [vp, C.c_longlong, _dp, i, _dp, C.POINTER(_dp),
@@ -711,6 +712,14 @@ class Run:
 
     def set_graph(self, use_graph: bool):
         _check(self.lib.cans_run_set_graph(self.h, 1 if use_graph else 0), "cans_run_set_graph")
+
+    def set_tile(self, tile: int):
+        _check(self.lib.cans_run_set_tile(self.h, tile), "cans_run_set_tile")
+
+    def set_df64(self, on: bool = True):
+        """The double-float policy of the 2-D mlw_m3 step (see
+        cans_run_set_df64)."""
+        _check(self.lib.cans_run_set_df64(self.h, 1 if on else 0), "cans_run_set_df64")
 
     def profile(self, iters: int):
         """(summed step-kernel ms, summed iteration ms) over `iters` un-graphed

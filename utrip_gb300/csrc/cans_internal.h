@@ -62,6 +62,12 @@ cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
                          Box3 box, cudaStream_t s);
 int mlw2d_tile_count();
+// The mlw_m3 step in the double-float policy (mlw2d_df.cu); tile selects
+// one of mlw2d_df_tile_count() shapes.
+cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx,
+                            const Axis &ax, const Axis &ay, const Phys &ph, double dt,
+                            Ctl *ctl, Box3 box, cudaStream_t s);
+int mlw2d_df_tile_count();
 // The mlw_m3 step (no control block) with the artificial viscosity's branch
 // recorded (mode 1) into, or held at (mode 2) the bytes of, avb: 2*ix*jx
 // bytes, x faces then y faces.  Mode 2 adds to *nflip the faces whose own

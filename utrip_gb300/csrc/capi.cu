@@ -1461,6 +1461,7 @@ struct cans_run {
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
+  bool df = false;             // double-float policy of the 2-D mlw_m3 step
   unsigned char *avb = nullptr;  // adjoint check: recorded viscosity branches,
   long long avb_steps = 0;       //   2*ix*jx bytes per step
 };
@@ -1496,6 +1497,7 @@ int layout2d(const cans_run *h) {
 }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
+  if (h->df) return mlw2d_df_tile_count();
   if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
   if (h->eta) return h->ndim == 3 ? mlw3d_tile_count() : 1;
   if (h->grav) return h->ndim == 3 ? mlw3d_g_tile_count() : mlw2d_g_tile_count();
@@ -1558,6 +1560,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (h->grav)
     return launch_mlw2d_g(h->d.solver, h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx,
                           h->ax.a, h->ay.a, h->ph, h->grav, dt, ctl, box, h->s);
+  if (h->df)
+    return launch_mlw2d_df(tile, A, B, h->d.ix, h->d.jx, h->ax.a, h->ay.a, h->ph, dt, ctl,
+                           box, h->s);
   return launch_mlw2d(h->d.solver, h->d.exact != 0, tile, A, B, h->d.ix,
                       h->d.jx, h->ax.a, h->ay.a, h->ph, dt, ctl, box, h->s);
 }
@@ -1983,6 +1988,29 @@ extern "C" int cans_run_set_graph(cans_run *h, int use_graph) {
   return CANS_OK;
 }
 
+extern "C" int cans_run_set_tile(cans_run *h, int tile) {
+  if (!h || tile < 0 || tile >= tile_count(h)) return CANS_ERR_ARG;
+  if (h->tile != tile) {
+    if (h->s) cudaStreamSynchronize(h->s);
+    drop_graph(h);
+    h->tile = tile;
+  }
+  return CANS_OK;
+}
+
+extern "C" int cans_run_set_df64(cans_run *h, int on) {
+  if (!h) return CANS_ERR_ARG;
+  if (on && (h->d.solver != CANS_SOLVER_MLW_M3_2D || h->d.exact || h->grav || h->eta))
+    return CANS_ERR_ARG;
+  if (h->df != (on != 0)) {
+    if (h->s) cudaStreamSynchronize(h->s);
+    drop_graph(h);
+    h->df = on != 0;
+    h->tile = 0;
+  }
+  return CANS_OK;
+}
+
 extern "C" int cans_run_query(cans_run *h, cans_run_state *st) {
   if (!h || !st) return CANS_ERR_ARG;
   int rc = read_ctl(h);
@@ -2178,7 +2206,8 @@ struct AdjWork {
 // the adjoint is that of the plain mlw_m3 step and boundary fill: no
 // gravity, no resistivity, no chkdav floor
 bool adj_supported(const cans_run *h) {
-  return h->d.solver == CANS_SOLVER_MLW_M3_2D && !h->grav && !h->eta && !h->d.chkdav;
+  return h->d.solver == CANS_SOLVER_MLW_M3_2D && !h->grav && !h->eta && !h->d.chkdav &&
+         !h->df;
 }
 
 int adj_setup(cans_run *h, AdjWork &W, int nsnap) {

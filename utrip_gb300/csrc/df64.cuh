@@ -1,0 +1,149 @@
+// Double-float ("df64") arithmetic on the FP32 pipes (sm_103a).
+//
+// GB300 executes FP64 at 2 lanes per SM per clock and FP32 at 128; the mLW
+// step, which needs several hundred FP64 operations per zone, is bound by the
+// FP64 pipe.  A double-float value is an unevaluated sum h + l of two floats
+// with |l| <= ulp(h)/2: 48 significant bits, the exponent range of float.
+// The operations below are written from the published error-free
+// transformations:
+//   two_sum       Knuth, TAOCP vol. 2 (Moller 1965): s + e == a + b exactly
+//   fast_two_sum  Dekker 1971, for |a| >= |b|
+//   two_prod      with one FMA: p + e == a * b exactly
+// and the double-word algorithms of Joldes, Muller and Popescu, "Tight and
+// rigorous error bounds for basic building blocks of double-word arithmetic"
+// (ACM TOMS 44, 2017): the sloppy sum (their Alg. 5; absolute error of order
+// u^2 (|x| + |y|), u = 2^-24, which is all a difference of nearby values
+// needs), the product with FMA (Alg. 10, relative error below 7 u^2), the
+// product by a float (Alg. 9), and the sum with a float (Alg. 4).  The
+// reciprocal is one Newton step on the correctly rounded float reciprocal,
+// with the residual 1 - y r formed in double-float (about 2^-46).
+//
+// Every float operation is an explicitly rounded intrinsic, so nothing is
+// contracted or reassociated: the error-free transformations stay exact.
+//
+// Conversions from double split the 53-bit significand with integer
+// operations (no FP64 instruction): the head takes the top 24 bits, the tail
+// the remaining 29 rounded to 24, so the value is kept to 2^-48.  Values whose
+// tail would leave the float range (|x| < 2^-74) or that overflow float take a
+// slower path through the FP64 converter; zero is exact.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cans {
+namespace df {
+
+struct D {
+  float h, l;
+};
+
+__device__ __forceinline__ D two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ D fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ D mk(float a) { return {a, 0.0f}; }
+__device__ __forceinline__ D neg(D x) { return {-x.h, -x.l}; }
+// multiplication by a power of two is exact
+__device__ __forceinline__ D scale(D x, float p2) {
+  return {__fmul_rn(x.h, p2), __fmul_rn(x.l, p2)};
+}
+
+// x + y, sloppy (JMP Alg. 5)
+__device__ __forceinline__ D add(D x, D y) {
+  const D s = two_sum(x.h, y.h);
+  const float v = __fadd_rn(x.l, y.l);
+  const float w = __fadd_rn(s.l, v);
+  return fast_two_sum(s.h, w);
+}
+__device__ __forceinline__ D sub(D x, D y) { return add(x, neg(y)); }
+// x + y for a float y (JMP Alg. 4)
+__device__ __forceinline__ D addf(D x, float y) {
+  const D s = two_sum(x.h, y);
+  const float v = __fadd_rn(x.l, s.l);
+  return fast_two_sum(s.h, v);
+}
+
+// x * y (JMP Alg. 10)
+__device__ __forceinline__ D mul(D x, D y) {
+  const float ch = __fmul_rn(x.h, y.h);
+  const float cl1 = __fmaf_rn(x.h, y.h, -ch);
+  const float tl = __fmul_rn(x.h, y.l);
+  const float cl2 = __fmaf_rn(x.l, y.h, tl);
+  return fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+// x * y for a float y (JMP Alg. 9)
+__device__ __forceinline__ D mulf(D x, float y) {
+  const float ch = __fmul_rn(x.h, y);
+  const float cl1 = __fmaf_rn(x.h, y, -ch);
+  return fast_two_sum(ch, __fmaf_rn(x.l, y, cl1));
+}
+// x * y + z: the product's head and tail are added to z before one
+// normalisation (the error terms of mul and add, without the intermediate
+// fast_two_sum).
+__device__ __forceinline__ D mad(D x, D y, D z) {
+  const float ch = __fmul_rn(x.h, y.h);
+  const float cl1 = __fmaf_rn(x.h, y.h, -ch);
+  const float cl2 = __fmaf_rn(x.l, y.h, __fmul_rn(x.h, y.l));
+  const D s = two_sum(ch, z.h);
+  const float t = __fadd_rn(__fadd_rn(cl1, cl2), z.l);
+  return fast_two_sum(s.h, __fadd_rn(s.l, t));
+}
+__device__ __forceinline__ D sqr(D x) { return mul(x, x); }
+
+// 1 / y: r = rn(1/y.h), then r + r (1 - y r) with 1 - y r in double-float
+__device__ __forceinline__ D rcp(D y) {
+  const float r = __frcp_rn(y.h);
+  const D p = mulf(y, r);
+  const float e = __fsub_rn(__fsub_rn(1.0f, p.h), p.l);  // 1 - p.h is exact
+  return fast_two_sum(r, __fmul_rn(r, e));
+}
+
+// sign tests of a normalised value: its head carries the sign (or is 0 with
+// a zero tail)
+__device__ __forceinline__ bool pos(D x) { return x.h > 0.0f; }
+__device__ __forceinline__ bool gt(D a, D b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+__device__ __forceinline__ D absd(D x) { return x.h < 0.0f ? neg(x) : x; }
+
+// double -> double-float (see the file comment)
+__device__ __forceinline__ D from_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  const unsigned sgn = hi & 0x80000000u;
+  if (e >= 949 && e <= 1150) {
+    // head: top 24 significand bits (the implicit one and 23 stored bits),
+    // truncated; exponent rebiased from 1023 to 127
+    const float h = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) |
+                                    ((hi & 0xfffffu) << 3) | (lo >> 29));
+    // tail: the low 29 bits times 2^(e - 1075), a normal float for e >= 949
+    const float t = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu),
+                              __uint_as_float((unsigned)(e - 948) << 23));
+    return fast_two_sum(h, sgn ? -t : t);
+  }
+  if (e == 0) return {__uint_as_float(sgn), 0.0f};  // zero (and subnormal doubles)
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+
+// double-float -> double, rounded once: the two floats are widened exactly
+// (integer operations for normal floats) and added in FP64
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ef = (u >> 23) & 0xffu;
+  if (ef == 0u || ef == 0xffu) return (double)f;  // zero, subnormal, inf, NaN
+  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                  ((unsigned long long)(ef + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double to_double(D x) { return __dadd_rn(widen(x.h), widen(x.l)); }
+
+}  // namespace df
+}  // namespace cans

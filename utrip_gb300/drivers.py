@@ -194,10 +194,11 @@ def run_literal(setup, state, nstop, tend=None, safety=None, t0=0.0, resident=Fa
 
 
 def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True,
-             stop_on_bad=False) -> capi.Run:
+             stop_on_bad=False, df64=False) -> capi.Run:
     """Run handle for a set-up; a set-up with a "floor" gets the chkdav
     option and one with a "trq" profile the torque source (each can be
-    switched off here)."""
+    switched off here).  df64 selects the double-float policy of the 2-D
+    mlw_m3 step."""
     fl = setup.get("floor") if floor else None
     tq = None
     if torque and setup.get("trq") is not None:
@@ -207,17 +208,21 @@ def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True,
                    mfdim=setup.get("mfdim", (0, 0, 0)), floor=fl, torque=tq,
                    stop_on_bad=stop_on_bad)
     run.set_bc_program(setup["bc"])
+    if df64:
+        run.set_df64(True)
+        if tile >= 0:
+            run.set_tile(tile)
     return run
 
 
 def run_resident(setup, state, nstop, tend=None, safety=None, t0=0.0, exact=False,
-                 chunk=256, run: capi.Run | None = None):
+                 chunk=256, run: capi.Run | None = None, df64=False):
     """Reference loop on the device.  Returns (t, ns, merr, nexec)."""
     tend = setup.get("tend", 1e30) if tend is None else tend
     safety = setup["safety"] if safety is None else safety
     own = run is None
     if own:
-        run = make_run(setup, exact=exact)
+        run = make_run(setup, exact=exact, df64=df64)
     try:
         run.push(state)
         run.start(t0=t0, tend=tend, nstop=nstop, safety=safety, dtmin=setup["dtmin"])
