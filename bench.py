@@ -529,6 +529,17 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
                 "adjoint_s": time.perf_counter() - t0, "forward_steps_in_adjoint": int(nfwd_all),
                 "grad_equal_to_checkpointed": all(np.array_equal(a, b)
                                                   for a, b in zip(g_all, grad))}
+            # the same sweep with its reverse arithmetic in FP64
+            run.set_adjoint_df64(False)
+            run.adjoint(dts, nsnap=nsnap)
+            t0 = time.perf_counter()
+            _, g64, _ = run.adjoint(dts, nsnap=nsnap)
+            out["reverse_in_fp64"] = {
+                "adjoint_s": time.perf_counter() - t0,
+                "grad_max_rel_diff_vs_double_float": max(
+                    float(np.max(np.abs(a - b))) / max(float(np.max(np.abs(b))), 1e-300)
+                    for a, b in zip(grad, g64))}
+            run.set_adjoint_df64(True)
         rx = drivers.make_run(s, exact=True, stream=stream.cuda_stream)
         rx.push(s["state"])
         J_exact = rx.objective(dts)
@@ -615,6 +626,10 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
     if "store_all_states" in out:
         out["store_all_states"]["adjoint_over_forward"] = (out["store_all_states"]["adjoint_s"]
                                                            / out["qav3"]["forward_s"])
+        out["reverse_in_fp64"]["adjoint_over_forward"] = (out["reverse_in_fp64"]["adjoint_s"]
+                                                          / out["qav3"]["forward_s"])
+    out["reverse_arithmetic"] = ("double-float on the FP32 pipes (cans_run_set_adjoint_df64); "
+                                 "forward recomputation in FP64")
     return out
 
 

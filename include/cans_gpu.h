@@ -580,6 +580,11 @@ int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts,
 int cans_run_av_record(cans_run *h, long long nsteps, const double *dts);
 int cans_run_objective_frozen_av(cans_run *h, long long nsteps, const double *dts,
                                  double *J, long long *nflip);
+/* The arithmetic of the reverse sweep: double-float on the FP32 pipes (on =
+ * 1, the default; about 2^-46 per operation, far below the gradient's use)
+ * or FP64 (on = 0).  The forward steps the sweep recomputes and linearises
+ * about are the run's own FP64 steps either way. */
+int cans_run_set_adjoint_df64(cans_run *h, int on);
 /* Transpose of the run's boundary program applied in place to host arrays
  * (one per state variable): folds ghost-cell sensitivities into the cells
  * they are copied from. */

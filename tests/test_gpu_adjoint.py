@@ -320,6 +320,25 @@ def test_frozen_branch_needs_a_record(gpu):
         run.close()
 
 
+def test_reverse_sweep_in_fp64_and_double_float_agree(gpu):
+    """The reverse arithmetic (double-float by default, FP64 on request)
+    changes the gradient only at the level of its rounding: within 1e-11 of
+    the largest component, with qav = 3 (every viscosity path live)."""
+    s = _setup(n=40, ny=36, qav=3.0)
+    run = _run(s)
+    try:
+        dts, J = run.record_dts(60)
+        Jd, gd, _ = run.adjoint(dts, nsnap=8)
+        run.set_adjoint_df64(False)
+        J6, g6, _ = run.adjoint(dts, nsnap=8)
+    finally:
+        run.close()
+    assert Jd == J6 == J
+    for a, b in zip(gd, g6):
+        scale = max(float(np.max(np.abs(b))), 1e-300)
+        assert float(np.max(np.abs(a - b))) <= 1e-11 * scale
+
+
 def test_adjoint_rejects_other_solvers(gpu):
     s = setups.random_state_3d(12, 12, 12, seed=1)
     run = drivers.make_run(s)

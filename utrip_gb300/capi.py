@@ -79,6 +79,7 @@ def load() -> C.CDLL:
         "cans_cfl_m3_2d_noalloc": (i, [_dp, _dp, _dp, _ip, _dp] + [vp] * 8 + [vp, _ip, vp, _ip]),
         "cans_run_set_graph": (i, [vp, i]),
         "cans_run_set_df64": (i, [vp, i]), "cans_run_set_tile": (i, [vp, i]),
+        "cans_run_set_adjoint_df64": (i, [vp, i]),
         "cans_run_record_dts": (i, [vp, C.c_longlong, d, _dp, _dp]),
         "cans_run_objective": (i, [vp, C.c_longlong, _dp, _dp]),
         "cans_run_adjoint": (i, [vp, C.c_longlong, _dp, i, _dp, C.POINTER(_dp),
@@ -764,6 +765,11 @@ class Run:
                                                      C.byref(nf)),
                "cans_run_objective_frozen_av")
         return J.value, nf.value
+
+    def set_adjoint_df64(self, on: bool = True):
+        """Reverse sweep in double-float (default) or FP64."""
+        _check(self.lib.cans_run_set_adjoint_df64(self.h, 1 if on else 0),
+               "cans_run_set_adjoint_df64")
 
     def adjoint(self, dts, nsnap: int = 32):
         """Reverse sweep with binomial checkpointing in nsnap stored states:

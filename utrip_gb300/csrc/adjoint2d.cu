@@ -31,6 +31,7 @@
 
 #include "cans_common.cuh"
 #include "cans_internal.h"
+#include "df64.cuh"
 
 namespace cans {
 
@@ -50,19 +51,34 @@ __device__ __forceinline__ bool interior(const G2 &g, int i, int j) {
   return i >= 1 && i <= g.ix - 2 && j >= 1 && j <= g.jx - 2;  // 0-based
 }
 
-// (1): conserved values and fluxes of one primitive state (mlw_m3.f:107-202)
-struct CellF {
-  double U[8], FX[8], FY[8];
+// The reverse kernels are written once for a number type R: double (FP64
+// pipe) or df::DF (double-float on the FP32 pipes, about 2^-46 per
+// operation; see df64.cuh).  The gradient is checked to 1e-6 relative, so the
+// reverse sweep may run in double-float; the forward steps it linearises
+// about are the run's own FP64 steps in either case.  Scratch arrays between
+// the kernels hold R values (num_ld / num_st); the states read and the
+// adjoint written are doubles (num_in / num_out).
+template <class R> struct PhysR {
+  R gm1, gm1i, ggm1, pi8i, pi4i, qav;
 };
-__device__ __forceinline__ void cell_forward(const double *p, const Phys &ph,
-                                             CellF &o) {
-  const double ro = p[P_RO], pr = p[P_PR], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
-  const double bx = p[P_BX], by = p[P_BY], bz = p[P_BZ];
-  const double vv = vx * vx + vy * vy + vz * vz, bb = bx * bx + by * by + bz * bz;
-  const double ex = -vy * bz + vz * by, ey = -vz * bx + vx * bz, ez = -vx * by + vy * bx;
-  const double ep = pr * ph.ggm1 + 0.5 * ro * vv;
+template <class R> __device__ __forceinline__ PhysR<R> phys_r(const Phys &ph) {
+  return {num_in<R>(ph.gm1), num_in<R>(ph.gm1i), num_in<R>(ph.ggm1), num_in<R>(ph.pi8i),
+          num_in<R>(ph.pi4i), num_in<R>(ph.qav)};
+}
+
+// (1): conserved values and fluxes of one primitive state (mlw_m3.f:107-202)
+template <class R> struct CellF {
+  R U[8], FX[8], FY[8];
+};
+template <class R>
+__device__ __forceinline__ void cell_forward(const R *p, const PhysR<R> &ph, CellF<R> &o) {
+  const R ro = p[P_RO], pr = p[P_PR], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
+  const R bx = p[P_BX], by = p[P_BY], bz = p[P_BZ];
+  const R vv = vx * vx + vy * vy + vz * vz, bb = bx * bx + by * by + bz * bz;
+  const R ex = -vy * bz + vz * by, ey = -vz * bx + vx * bz, ez = -vx * by + vy * bx;
+  const R ep = pr * ph.ggm1 + 0.5f * ro * vv;
   o.U[C_RO] = ro;
-  o.U[C_EE] = pr * ph.gm1i + 0.5 * ro * vv + ph.pi8i * bb;
+  o.U[C_EE] = pr * ph.gm1i + 0.5f * ro * vv + ph.pi8i * bb;
   o.U[C_RX] = ro * vx;
   o.U[C_RY] = ro * vy;
   o.U[C_RZ] = ro * vz;
@@ -79,22 +95,24 @@ __device__ __forceinline__ void cell_forward(const double *p, const Phys &ph,
   o.FY[C_RY] = ro * vy * vy + pr + ph.pi8i * (bx * bx + bz * bz - by * by);
   o.FX[C_RZ] = ro * vz * vx - ph.pi4i * bz * bx;
   o.FY[C_RZ] = ro * vz * vy - ph.pi4i * bz * by;
-  o.FX[C_BX] = 0.0;
+  o.FX[C_BX] = R(0.0f);
   o.FY[C_BX] = ez;
   o.FX[C_BY] = -ez;
-  o.FY[C_BY] = 0.0;
+  o.FY[C_BY] = R(0.0f);
   o.FX[C_BZ] = ey;
   o.FY[C_BZ] = -ex;
 }
 
 // primitives of a conserved state (mlw_m3.f:214-223, 365-374)
-__device__ __forceinline__ void prim_forward(const double *u, const Phys &ph, double *p) {
-  const double ro = u[C_RO];
-  const double vx = u[C_RX] / ro, vy = u[C_RY] / ro, vz = u[C_RZ] / ro;
-  const double vv = vx * vx + vy * vy + vz * vz;
-  const double bb = u[C_BX] * u[C_BX] + u[C_BY] * u[C_BY] + u[C_BZ] * u[C_BZ];
+template <class R>
+__device__ __forceinline__ void prim_forward(const R *u, const PhysR<R> &ph, R *p) {
+  const R ro = u[C_RO];
+  const R ri = R(1.0f) / ro;
+  const R vx = u[C_RX] * ri, vy = u[C_RY] * ri, vz = u[C_RZ] * ri;
+  const R vv = vx * vx + vy * vy + vz * vz;
+  const R bb = u[C_BX] * u[C_BX] + u[C_BY] * u[C_BY] + u[C_BZ] * u[C_BZ];
   p[P_RO] = ro;
-  p[P_PR] = ph.gm1 * (u[C_EE] - 0.5 * ro * vv - ph.pi8i * bb);
+  p[P_PR] = ph.gm1 * (u[C_EE] - 0.5f * ro * vv - ph.pi8i * bb);
   p[P_VX] = vx;
   p[P_VY] = vy;
   p[P_VZ] = vz;
@@ -105,22 +123,23 @@ __device__ __forceinline__ void prim_forward(const double *u, const Phys &ph, do
 
 // Transpose of (1): given the adjoints aU, aX, aY of U, FX, FY at the point
 // p, add (d(U,FX,FY)/dP)^T (aU, aX, aY) to ap.
-__device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
-                                             const double *aU, const double *aX,
-                                             const double *aY, double *ap) {
-  const double ro = p[P_RO], pr = p[P_PR], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
-  const double bx = p[P_BX], by = p[P_BY], bz = p[P_BZ];
-  const double vv = vx * vx + vy * vy + vz * vz;
-  const double ex = -vy * bz + vz * by, ey = -vz * bx + vx * bz, ez = -vx * by + vy * bx;
-  const double ep = pr * ph.ggm1 + 0.5 * ro * vv;
-  const double p4 = ph.pi4i, p8 = ph.pi8i;
-  double aro = 0, apr = 0, avx = 0, avy = 0, avz = 0, abx = 0, aby = 0, abz = 0;
-  double aep = 0, aex = 0, aey = 0, aez = 0, avv = 0, abb = 0;
+template <class R>
+__device__ __forceinline__ void cell_reverse(const R *p, const PhysR<R> &ph, const R *aU,
+                                             const R *aX, const R *aY, R *ap) {
+  const R ro = p[P_RO], pr = p[P_PR], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
+  const R bx = p[P_BX], by = p[P_BY], bz = p[P_BZ];
+  const R vv = vx * vx + vy * vy + vz * vz;
+  const R ex = -vy * bz + vz * by, ey = -vz * bx + vx * bz, ez = -vx * by + vy * bx;
+  const R ep = pr * ph.ggm1 + 0.5f * ro * vv;
+  const R p4 = ph.pi4i, p8 = ph.pi8i;
+  R aro(0.0f), apr(0.0f), avx(0.0f), avy(0.0f), avz(0.0f), abx(0.0f), aby(0.0f),
+      abz(0.0f);
+  R aep(0.0f), aex(0.0f), aey(0.0f), aez(0.0f), avv(0.0f), abb(0.0f);
   // U
   aro += aU[C_RO];
   apr += aU[C_EE] * ph.gm1i;
-  aro += aU[C_EE] * 0.5 * vv;
-  avv += aU[C_EE] * 0.5 * ro;
+  aro += aU[C_EE] * 0.5f * vv;
+  avv += aU[C_EE] * 0.5f * ro;
   abb += aU[C_EE] * p8;
   aro += aU[C_RX] * vx + aU[C_RY] * vy + aU[C_RZ] * vz;
   avx += aU[C_RX] * ro;
@@ -139,11 +158,11 @@ __device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
   aby -= aX[C_EE] * p4 * ez;
   aez -= aX[C_EE] * p4 * by;
   aro += aX[C_RX] * vx * vx;
-  avx += aX[C_RX] * 2.0 * ro * vx;
+  avx += aX[C_RX] * 2.0f * ro * vx;
   apr += aX[C_RX];
-  aby += aX[C_RX] * p8 * 2.0 * by;
-  abz += aX[C_RX] * p8 * 2.0 * bz;
-  abx -= aX[C_RX] * p8 * 2.0 * bx;
+  aby += aX[C_RX] * p8 * 2.0f * by;
+  abz += aX[C_RX] * p8 * 2.0f * bz;
+  abx -= aX[C_RX] * p8 * 2.0f * bx;
   aro += aX[C_RY] * vy * vx;
   avy += aX[C_RY] * ro * vx;
   avx += aX[C_RY] * ro * vy;
@@ -171,11 +190,11 @@ __device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
   abx -= aY[C_RX] * p4 * by;
   aby -= aY[C_RX] * p4 * bx;
   aro += aY[C_RY] * vy * vy;
-  avy += aY[C_RY] * 2.0 * ro * vy;
+  avy += aY[C_RY] * 2.0f * ro * vy;
   apr += aY[C_RY];
-  abx += aY[C_RY] * p8 * 2.0 * bx;
-  abz += aY[C_RY] * p8 * 2.0 * bz;
-  aby -= aY[C_RY] * p8 * 2.0 * by;
+  abx += aY[C_RY] * p8 * 2.0f * bx;
+  abz += aY[C_RY] * p8 * 2.0f * bz;
+  aby -= aY[C_RY] * p8 * 2.0f * by;
   aro += aY[C_RZ] * vz * vy;
   avz += aY[C_RZ] * ro * vy;
   avy += aY[C_RZ] * ro * vz;
@@ -185,8 +204,8 @@ __device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
   aex -= aY[C_BZ];
   // ep, E, |v|^2, |B|^2
   apr += aep * ph.ggm1;
-  aro += aep * 0.5 * vv;
-  avv += aep * 0.5 * ro;
+  aro += aep * 0.5f * vv;
+  avv += aep * 0.5f * ro;
   avy -= aex * bz;
   abz -= aex * vy;
   avz += aex * by;
@@ -199,12 +218,12 @@ __device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
   aby -= aez * vx;
   avy += aez * bx;
   abx += aez * vy;
-  avx += 2.0 * vx * avv;
-  avy += 2.0 * vy * avv;
-  avz += 2.0 * vz * avv;
-  abx += 2.0 * bx * abb;
-  aby += 2.0 * by * abb;
-  abz += 2.0 * bz * abb;
+  avx += 2.0f * vx * avv;
+  avy += 2.0f * vy * avv;
+  avz += 2.0f * vz * avv;
+  abx += 2.0f * bx * abb;
+  aby += 2.0f * by * abb;
+  abz += 2.0f * bz * abb;
   ap[P_RO] += aro;
   ap[P_PR] += apr;
   ap[P_VX] += avx;
@@ -217,120 +236,142 @@ __device__ __forceinline__ void cell_reverse(const double *p, const Phys &ph,
 
 // Transpose of prim_forward at the point whose primitives are p: given ap,
 // return au = (dP/dU)^T ap.
-__device__ __forceinline__ void prim_reverse(const double *p, const Phys &ph,
-                                             const double *ap, double *au) {
-  const double ro = p[P_RO], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
-  const double vv = vx * vx + vy * vy + vz * vz;
-  const double apr = ap[P_PR];
-  const double avv = -ph.gm1 * 0.5 * ro * apr;
-  const double abb = -ph.gm1 * ph.pi8i * apr;
-  const double ri = 1.0 / ro;
-  const double avx = ap[P_VX] + 2.0 * vx * avv, avy = ap[P_VY] + 2.0 * vy * avv,
-               avz = ap[P_VZ] + 2.0 * vz * avv;
+template <class R>
+__device__ __forceinline__ void prim_reverse(const R *p, const PhysR<R> &ph, const R *ap,
+                                             R *au) {
+  const R ro = p[P_RO], vx = p[P_VX], vy = p[P_VY], vz = p[P_VZ];
+  const R vv = vx * vx + vy * vy + vz * vz;
+  const R apr = ap[P_PR];
+  const R avv = -ph.gm1 * 0.5f * ro * apr;
+  const R abb = -ph.gm1 * ph.pi8i * apr;
+  const R ri = R(1.0f) / ro;
+  const R avx = ap[P_VX] + 2.0f * vx * avv, avy = ap[P_VY] + 2.0f * vy * avv,
+          avz = ap[P_VZ] + 2.0f * vz * avv;
   au[C_EE] = ph.gm1 * apr;
   au[C_RX] = avx * ri;
   au[C_RY] = avy * ri;
   au[C_RZ] = avz * ri;
-  au[C_RO] = ap[P_RO] - ph.gm1 * 0.5 * vv * apr - (avx * vx + avy * vy + avz * vz) * ri;
-  au[C_BX] = ap[P_BX] + 2.0 * p[P_BX] * abb;
-  au[C_BY] = ap[P_BY] + 2.0 * p[P_BY] * abb;
-  au[C_BZ] = ap[P_BZ] + 2.0 * p[P_BZ] * abb;
+  au[C_RO] = ap[P_RO] - ph.gm1 * 0.5f * vv * apr - (avx * vx + avy * vy + avz * vz) * ri;
+  au[C_BX] = ap[P_BX] + 2.0f * p[P_BX] * abb;
+  au[C_BY] = ap[P_BY] + 2.0f * p[P_BY] * abb;
+  au[C_BZ] = ap[P_BZ] + 2.0f * p[P_BZ] * abb;
 }
 
-__device__ __forceinline__ void load_prim(const double *S, size_t n, size_t c, double *p) {
+template <class R>
+__device__ __forceinline__ void load_prim(const double *S, size_t n, size_t c, R *p) {
 #pragma unroll
-  for (int v = 0; v < 8; v++) p[v] = S[v * n + c];
+  for (int v = 0; v < 8; v++) p[v] = num_in<R>(S[v * n + c]);
 }
 
 // a' on the interior, the cell values U, FX, FY of P everywhere
+template <class R>
 __global__ void __launch_bounds__(kT)
-    k_adj_cells(const double *__restrict__ P, const double *__restrict__ R,
+    k_adj_cells(const double *__restrict__ P, const double *__restrict__ Rw,
                 const double *__restrict__ lam, double *__restrict__ A1,
-                double *__restrict__ CU, G2 g, Phys ph) {
+                double *__restrict__ CU, G2 g, Phys ph_) {
   const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (c >= g.n) return;
+  const PhysR<R> ph = phys_r<R>(ph_);
   const int i = (int)(c % g.ix), j = (int)(c / g.ix);
-  double p[8];
+  R p[8];
   load_prim(P, g.n, c, p);
-  CellF f;
+  CellF<R> f;
   cell_forward(p, ph, f);
 #pragma unroll
   for (int v = 0; v < 8; v++) {
-    CU[v * g.n + c] = f.U[v];
-    CU[(8 + v) * g.n + c] = f.FX[v];
-    CU[(16 + v) * g.n + c] = f.FY[v];
+    num_st(CU + v * g.n + c, f.U[v]);
+    num_st(CU + (8 + v) * g.n + c, f.FX[v]);
+    num_st(CU + (16 + v) * g.n + c, f.FY[v]);
   }
-  double au[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  R au[8];
+#pragma unroll
+  for (int v = 0; v < 8; v++) au[v] = R(0.0f);
   if (interior(g, i, j)) {
-    double r[8], ap[8];
-    load_prim(R, g.n, c, r);
+    R r[8], ap[8];
+    load_prim(Rw, g.n, c, r);
     load_prim(lam, g.n, c, ap);
     prim_reverse(r, ph, ap, au);
   }
 #pragma unroll
-  for (int v = 0; v < 8; v++) A1[v * g.n + c] = au[v];
+  for (int v = 0; v < 8; v++) num_st(A1 + v * g.n + c, au[v]);
 }
 
 // corners (p+1/2, q+1/2), p = 0..ix-2, q = 0..jx-2 (0-based), stored at p+q*ix
+template <class R>
 __global__ void __launch_bounds__(kT)
     k_adj_corners(const double *__restrict__ CU, const double *__restrict__ A1,
-                  double *__restrict__ A2, G2 g, Axis ax, Axis ay, Phys ph,
-                  double dt) {
+                  double *__restrict__ A2, G2 g, Axis ax, Axis ay, Phys ph_,
+                  double dt_) {
   const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (c >= g.n) return;
+  const PhysR<R> ph = phys_r<R>(ph_);
+  const R dt = num_in<R>(dt_);
   const int p = (int)(c % g.ix), q = (int)(c / g.ix);
-  double out[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  R out[8];
+#pragma unroll
+  for (int v = 0; v < 8; v++) out[v] = R(0.0f);
   if (p <= g.ix - 2 && q <= g.jx - 2) {
     const size_t c00 = c, c10 = c + 1, c01 = c + g.ix, c11 = c + g.ix + 1;
     // forward corner state (mlwhalf.f part 2)
-    double uh[8];
+    const R hdxim = 0.5f * num_in<R>(ax.dim[p]), hdyim = 0.5f * num_in<R>(ay.dim[q]);
+    R uh[8];
 #pragma unroll
     for (int v = 0; v < 8; v++) {
       const double *U = CU + v * g.n, *FX = CU + (8 + v) * g.n, *FY = CU + (16 + v) * g.n;
-      const double avg = 0.25 * (U[c10] + U[c00] + U[c11] + U[c01]);
-      const double dfdx = ax.dim[p] * (FX[c10] - FX[c00] + FX[c11] - FX[c01]) / 2;
-      const double dfdy = ay.dim[q] * (FY[c01] - FY[c00] + FY[c11] - FY[c10]) / 2;
+      const R avg = 0.25f * (num_ld<R>(U + c10) + num_ld<R>(U + c00) + num_ld<R>(U + c11) +
+                             num_ld<R>(U + c01));
+      const R dfdx = hdxim * (num_ld<R>(FX + c10) - num_ld<R>(FX + c00) +
+                              num_ld<R>(FX + c11) - num_ld<R>(FX + c01));
+      const R dfdy = hdyim * (num_ld<R>(FY + c01) - num_ld<R>(FY + c00) +
+                              num_ld<R>(FY + c11) - num_ld<R>(FY + c10));
       uh[v] = avg - dt * dfdx - dt * dfdy;
     }
-    double ph8[8];
+    R ph8[8];
     prim_forward(uh, ph, ph8);
     // adjoint of GX, GY at this corner: the cells (p,q), (p+1,q), (p,q+1),
     // (p+1,q+1) that read it in mlwfull (0-based cell indices)
     const bool i00 = interior(g, p, q), i10 = interior(g, p + 1, q),
                i01 = interior(g, p, q + 1), i11 = interior(g, p + 1, q + 1);
-    const double hx0 = 0.5 * dt * ax.di[p], hx1 = 0.5 * dt * ax.di[p + 1];
-    const double hy0 = 0.5 * dt * ay.di[q], hy1 = 0.5 * dt * ay.di[q + 1];
-    double aX[8], aY[8];
+    const R hx0 = 0.5f * dt * num_in<R>(ax.di[p]), hx1 = 0.5f * dt * num_in<R>(ax.di[p + 1]);
+    const R hy0 = 0.5f * dt * num_in<R>(ay.di[q]), hy1 = 0.5f * dt * num_in<R>(ay.di[q + 1]);
+    const R uy1q = num_in<R>(ay.u1[q]), uy0q1 = num_in<R>(ay.u0[q + 1]);
+    const R ux1p = num_in<R>(ax.u1[p]), ux0p1 = num_in<R>(ax.u0[p + 1]);
+    R aX[8], aY[8];
 #pragma unroll
     for (int v = 0; v < 8; v++) {
       const double *a = A1 + v * g.n;
-      const double l00 = i00 ? a[c00] : 0.0, l10 = i10 ? a[c10] : 0.0;
-      const double l01 = i01 ? a[c01] : 0.0, l11 = i11 ? a[c11] : 0.0;
-      aX[v] = -hx0 * ay.u1[q] * l00 + hx1 * ay.u1[q] * l10 - hx0 * ay.u0[q + 1] * l01 +
-              hx1 * ay.u0[q + 1] * l11;
-      aY[v] = -hy0 * ax.u1[p] * l00 - hy0 * ax.u0[p + 1] * l10 + hy1 * ax.u1[p] * l01 +
-              hy1 * ax.u0[p + 1] * l11;
+      const R l00 = i00 ? num_ld<R>(a + c00) : R(0.0f), l10 = i10 ? num_ld<R>(a + c10) : R(0.0f);
+      const R l01 = i01 ? num_ld<R>(a + c01) : R(0.0f), l11 = i11 ? num_ld<R>(a + c11) : R(0.0f);
+      aX[v] = -hx0 * uy1q * l00 + hx1 * uy1q * l10 - hx0 * uy0q1 * l01 + hx1 * uy0q1 * l11;
+      aY[v] = -hy0 * ux1p * l00 - hy0 * ux0p1 * l10 + hy1 * ux1p * l01 + hy1 * ux0p1 * l11;
     }
-    double aP[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const double zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    R aP[8], zero8[8];
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      aP[v] = R(0.0f);
+      zero8[v] = R(0.0f);
+    }
     cell_reverse(ph8, ph, zero8, aX, aY, aP);
     prim_reverse(ph8, ph, aP, out);
   }
 #pragma unroll
-  for (int v = 0; v < 8; v++) A2[v * g.n + c] = out[v];
+  for (int v = 0; v < 8; v++) num_st(A2 + v * g.n + c, out[v]);
 }
 
 // adjoint of P for every cell
+template <class R>
 __global__ void __launch_bounds__(kT)
     k_adj_gather(const double *__restrict__ P, const double *__restrict__ CU,
                  const double *__restrict__ A1, const double *__restrict__ A2,
                  const double *__restrict__ lam, double *__restrict__ out, G2 g,
-                 Axis ax, Axis ay, Phys ph, double dt) {
+                 Axis ax, Axis ay, Phys ph_, double dt_) {
   const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (c >= g.n) return;
+  const PhysR<R> ph = phys_r<R>(ph_);
+  const R dt = num_in<R>(dt_);
   const int i = (int)(c % g.ix), j = (int)(c / g.ix);
   const size_t n = g.n, sx = 1, sy = (size_t)g.ix;
-  double p[8];
+  R p[8];
   load_prim(P, n, c, p);
   const bool in_c = interior(g, i, j);
   const bool in_xm = interior(g, i - 1, j), in_xp = interior(g, i + 1, j);
@@ -338,91 +379,109 @@ __global__ void __launch_bounds__(kT)
   // corners around the cell: (i-1+1/2, j-1+1/2) .. (i+1/2, j+1/2)
   const bool k_mm = i >= 1 && j >= 1, k_pm = i <= g.ix - 2 && j >= 1;
   const bool k_mp = i >= 1 && j <= g.jx - 2, k_pp = i <= g.ix - 2 && j <= g.jx - 2;
+  // metrics the coefficients below read
+  const R zero(0.0f);
+  const R dim_xm = i >= 1 ? num_in<R>(ax.dim[i - 1]) : zero, dim_x = num_in<R>(ax.dim[i]);
+  const R dim_ym = j >= 1 ? num_in<R>(ay.dim[j - 1]) : zero, dim_y = num_in<R>(ay.dim[j]);
+  const R di_x = num_in<R>(ax.di[i]), di_y = num_in<R>(ay.di[j]);
+  const R di_xm = i >= 1 ? num_in<R>(ax.di[i - 1]) : zero;
+  const R di_xp = i <= g.ix - 2 ? num_in<R>(ax.di[i + 1]) : zero;
+  const R di_ym = j >= 1 ? num_in<R>(ay.di[j - 1]) : zero;
+  const R di_yp = j <= g.jx - 2 ? num_in<R>(ay.di[j + 1]) : zero;
   // artificial-viscosity coefficients of the four faces (mlw_m3.f:324-334)
+  // and their derivatives in dv: q = qav dxm max(0, |dv| - eps)
   const double *VX = P + P_VX * n, *VY = P + P_VY * n;
-  double qxm = 0, qxp = 0, qym = 0, qyp = 0, gxm = 0, gxp = 0, gym = 0, gyp = 0;
-  const double eps = CANS_AV_EPS;
+  R qxm = zero, qxp = zero, qym = zero, qyp = zero, gxm = zero, gxp = zero, gym = zero,
+    gyp = zero;
+  const float eps = 1.0e-4f;  // the real*4 literal of the reference
   if (i >= 1) {
-    const double d = VX[c] - VX[c - sx];
-    const double e = fabs(d) - eps;
-    qxm = ph.qav * ax.dm[i - 1] * (e > 0.0 ? e : 0.0);
-    gxm = e > 0.0 ? ph.qav * ax.dm[i - 1] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+    const R d = num_in<R>(VX[c]) - num_in<R>(VX[c - sx]);
+    const R e = fabs(d) - eps;
+    const R qd = ph.qav * num_in<R>(ax.dm[i - 1]);
+    qxm = e > 0.0f ? qd * e : zero;
+    gxm = e > 0.0f ? (d > 0.0f ? qd : -qd) : zero;
   }
   if (i <= g.ix - 2) {
-    const double d = VX[c + sx] - VX[c];
-    const double e = fabs(d) - eps;
-    qxp = ph.qav * ax.dm[i] * (e > 0.0 ? e : 0.0);
-    gxp = e > 0.0 ? ph.qav * ax.dm[i] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+    const R d = num_in<R>(VX[c + sx]) - num_in<R>(VX[c]);
+    const R e = fabs(d) - eps;
+    const R qd = ph.qav * num_in<R>(ax.dm[i]);
+    qxp = e > 0.0f ? qd * e : zero;
+    gxp = e > 0.0f ? (d > 0.0f ? qd : -qd) : zero;
   }
   if (j >= 1) {
-    const double d = VY[c] - VY[c - sy];
-    const double e = fabs(d) - eps;
-    qym = ph.qav * ay.dm[j - 1] * (e > 0.0 ? e : 0.0);
-    gym = e > 0.0 ? ph.qav * ay.dm[j - 1] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+    const R d = num_in<R>(VY[c]) - num_in<R>(VY[c - sy]);
+    const R e = fabs(d) - eps;
+    const R qd = ph.qav * num_in<R>(ay.dm[j - 1]);
+    qym = e > 0.0f ? qd * e : zero;
+    gym = e > 0.0f ? (d > 0.0f ? qd : -qd) : zero;
   }
   if (j <= g.jx - 2) {
-    const double d = VY[c + sy] - VY[c];
-    const double e = fabs(d) - eps;
-    qyp = ph.qav * ay.dm[j] * (e > 0.0 ? e : 0.0);
-    gyp = e > 0.0 ? ph.qav * ay.dm[j] * (d > 0.0 ? 1.0 : -1.0) : 0.0;
+    const R d = num_in<R>(VY[c + sy]) - num_in<R>(VY[c]);
+    const R e = fabs(d) - eps;
+    const R qd = ph.qav * num_in<R>(ay.dm[j]);
+    qyp = e > 0.0f ? qd * e : zero;
+    gyp = e > 0.0f ? (d > 0.0f ? qd : -qd) : zero;
   }
+  const bool aqxm_on = qxm != 0.0f, aqxp_on = qxp != 0.0f;
+  const bool aqym_on = qym != 0.0f, aqyp_on = qyp != 0.0f;
   // coefficients shared by the 8 variables: viscosity in U (mlwartv.f),
   // half-step differences (mlwhalf.f part 1), corner predictor (part 2),
   // viscosity in q; zero where the reading cell is not updated
-  const double cxm = in_xm ? dt * ax.di[i - 1] * qxm * ax.dim[i - 1] : 0.0;
-  const double cxp = in_xp ? dt * ax.di[i + 1] * qxp * ax.dim[i] : 0.0;
-  const double cym = in_ym ? dt * ay.di[j - 1] * qym * ay.dim[j - 1] : 0.0;
-  const double cyp = in_yp ? dt * ay.di[j + 1] * qyp * ay.dim[j] : 0.0;
-  const double c0 =
-      in_c ? dt * (ax.di[i] * (qxp * ax.dim[i] + qxm * ax.dim[i - 1]) +
-                   ay.di[j] * (qyp * ay.dim[j] + qym * ay.dim[j - 1]))
-           : 0.0;
-  const bool av = (qxm != 0.0) | (qxp != 0.0) | (qym != 0.0) | (qyp != 0.0);
-  const double hxm = i >= 1 ? 0.25 * dt * ax.di[i - 1] : 0.0;
-  const double hxp = i <= g.ix - 2 ? 0.25 * dt * ax.di[i + 1] : 0.0;
-  const double hym = j >= 1 ? 0.25 * dt * ay.di[j - 1] : 0.0;
-  const double hyp = j <= g.jx - 2 ? 0.25 * dt * ay.di[j + 1] : 0.0;
-  const double pxm = i >= 1 ? 0.5 * dt * ax.dim[i - 1] : 0.0;
-  const double pxp = i <= g.ix - 2 ? 0.5 * dt * ax.dim[i] : 0.0;
-  const double pym = j >= 1 ? 0.5 * dt * ay.dim[j - 1] : 0.0;
-  const double pyp = j <= g.jx - 2 ? 0.5 * dt * ay.dim[j] : 0.0;
+  const R cxm = in_xm ? dt * di_xm * qxm * dim_xm : zero;
+  const R cxp = in_xp ? dt * di_xp * qxp * dim_x : zero;
+  const R cym = in_ym ? dt * di_ym * qym * dim_ym : zero;
+  const R cyp = in_yp ? dt * di_yp * qyp * dim_y : zero;
+  const R c0 = in_c ? dt * (di_x * (qxp * dim_x + qxm * dim_xm) +
+                            di_y * (qyp * dim_y + qym * dim_ym))
+                    : zero;
+  const bool av = aqxm_on | aqxp_on | aqym_on | aqyp_on;
+  const R hxm = i >= 1 ? 0.25f * dt * di_xm : zero;
+  const R hxp = i <= g.ix - 2 ? 0.25f * dt * di_xp : zero;
+  const R hym = j >= 1 ? 0.25f * dt * di_ym : zero;
+  const R hyp = j <= g.jx - 2 ? 0.25f * dt * di_yp : zero;
+  const R pxm = i >= 1 ? 0.5f * dt * dim_xm : zero;
+  const R pxp = i <= g.ix - 2 ? 0.5f * dt * dim_x : zero;
+  const R pym = j >= 1 ? 0.5f * dt * dim_ym : zero;
+  const R pyp = j <= g.jx - 2 ? 0.5f * dt * dim_y : zero;
   // d(du(o))/dq(face) per unit dU: the cell below the face gains, the cell
   // above loses (in_* already folded in)
-  const double wxm_a = in_xm ? dt * ax.dim[i - 1] * ax.di[i - 1] : 0.0;
-  const double wxm_b = (in_c && i >= 1) ? dt * ax.dim[i - 1] * ax.di[i] : 0.0;
-  const double wxp_a = in_c ? dt * ax.dim[i] * ax.di[i] : 0.0;
-  const double wxp_b = in_xp ? dt * ax.dim[i] * ax.di[i + 1] : 0.0;
-  const double wym_a = in_ym ? dt * ay.dim[j - 1] * ay.di[j - 1] : 0.0;
-  const double wym_b = (in_c && j >= 1) ? dt * ay.dim[j - 1] * ay.di[j] : 0.0;
-  const double wyp_a = in_c ? dt * ay.dim[j] * ay.di[j] : 0.0;
-  const double wyp_b = in_yp ? dt * ay.dim[j] * ay.di[j + 1] : 0.0;
-  double aU[8], aX[8], aY[8];
-  double aqxm = 0, aqxp = 0, aqym = 0, aqyp = 0;
+  const R wxm_a = in_xm ? dt * dim_xm * di_xm : zero;
+  const R wxm_b = (in_c && i >= 1) ? dt * dim_xm * di_x : zero;
+  const R wxp_a = in_c ? dt * dim_x * di_x : zero;
+  const R wxp_b = in_xp ? dt * dim_x * di_xp : zero;
+  const R wym_a = in_ym ? dt * dim_ym * di_ym : zero;
+  const R wym_b = (in_c && j >= 1) ? dt * dim_ym * di_y : zero;
+  const R wyp_a = in_c ? dt * dim_y * di_y : zero;
+  const R wyp_b = in_yp ? dt * dim_y * di_yp : zero;
+  R aU[8], aX[8], aY[8];
+  R aqxm = zero, aqxp = zero, aqym = zero, aqyp = zero;
 #pragma unroll
   for (int v = 0; v < 8; v++) {
     const double *a = A1 + v * n, *h = A2 + v * n;
-    const double l0 = in_c ? a[c] : 0.0;
-    const double lxm = in_xm ? a[c - sx] : 0.0, lxp = in_xp ? a[c + sx] : 0.0;
-    const double lym = in_ym ? a[c - sy] : 0.0, lyp = in_yp ? a[c + sy] : 0.0;
-    const double hmm = k_mm ? h[c - sx - sy] : 0.0, hpm = k_pm ? h[c - sy] : 0.0;
-    const double hmp = k_mp ? h[c - sx] : 0.0, hpp = k_pp ? h[c] : 0.0;
-    const double ylo = hmm + hpm, yhi = hmp + hpp;  // corners below / above
+    const R l0 = in_c ? num_ld<R>(a + c) : zero;
+    const R lxm = in_xm ? num_ld<R>(a + c - sx) : zero, lxp = in_xp ? num_ld<R>(a + c + sx) : zero;
+    const R lym = in_ym ? num_ld<R>(a + c - sy) : zero, lyp = in_yp ? num_ld<R>(a + c + sy) : zero;
+    const R hmm = k_mm ? num_ld<R>(h + c - sx - sy) : zero, hpm = k_pm ? num_ld<R>(h + c - sy) : zero;
+    const R hmp = k_mp ? num_ld<R>(h + c - sx) : zero, hpp = k_pp ? num_ld<R>(h + c) : zero;
+    const R ylo = hmm + hpm, yhi = hmp + hpp;  // corners below / above
     // U' = U + du on the interior; 0.25 of each surrounding corner
-    double au = fma(0.25, ylo + yhi, l0);
+    R au = fma(R(0.25f), ylo + yhi, l0);
     if (av) au += cxm * lxm + cxp * lxp + cym * lym + cyp * lyp - c0 * l0;
     aU[v] = au;
     aX[v] = hxp * lxp - hxm * lxm + pxp * (hpm + hpp) - pxm * (hmm + hmp);
     aY[v] = hyp * lyp - hym * lym + pyp * yhi - pym * ylo;
     if (av) {
       const double *U = CU + v * n;
-      const double u0 = U[c];
-      if (qxm != 0.0) aqxm += (u0 - U[c - sx]) * (wxm_a * lxm - wxm_b * l0);
-      if (qxp != 0.0) aqxp += (U[c + sx] - u0) * (wxp_a * l0 - wxp_b * lxp);
-      if (qym != 0.0) aqym += (u0 - U[c - sy]) * (wym_a * lym - wym_b * l0);
-      if (qyp != 0.0) aqyp += (U[c + sy] - u0) * (wyp_a * l0 - wyp_b * lyp);
+      const R u0 = num_ld<R>(U + c);
+      if (aqxm_on) aqxm += (u0 - num_ld<R>(U + c - sx)) * (wxm_a * lxm - wxm_b * l0);
+      if (aqxp_on) aqxp += (num_ld<R>(U + c + sx) - u0) * (wxp_a * l0 - wxp_b * lxp);
+      if (aqym_on) aqym += (u0 - num_ld<R>(U + c - sy)) * (wym_a * lym - wym_b * l0);
+      if (aqyp_on) aqyp += (num_ld<R>(U + c + sy) - u0) * (wyp_a * l0 - wyp_b * lyp);
     }
   }
-  double ap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  R ap[8];
+#pragma unroll
+  for (int v = 0; v < 8; v++) ap[v] = zero;
   cell_reverse(p, ph, aU, aX, aY, ap);
   // q(face) = qav dxm max(0, |v(+) - v(-)| - eps): the cell is (+) of the
   // lower face and (-) of the upper face
@@ -431,10 +490,10 @@ __global__ void __launch_bounds__(kT)
   // cells the step does not update pass the adjoint through
   if (!in_c) {
 #pragma unroll
-    for (int v = 0; v < 8; v++) ap[v] += lam[v * n + c];
+    for (int v = 0; v < 8; v++) ap[v] += num_in<R>(lam[v * n + c]);
   }
 #pragma unroll
-  for (int v = 0; v < 8; v++) out[v * n + c] = ap[v];
+  for (int v = 0; v < 8; v++) out[v * n + c] = num_out(ap[v]);
   out[P_AZ * n + c] = 0.0;
 }
 
@@ -597,13 +656,21 @@ size_t adj2d_scratch_doubles(size_t ncells) { return 40 * ncells + 1024; }
 cudaError_t launch_adj2d_step(const double *P, const double *R, const double *lam_in,
                               double *lam_out, double *scratch, int ix, int jx,
                               const Axis &ax, const Axis &ay, const Phys &ph,
-                              double dt, cudaStream_t s) {
+                              double dt, bool df, cudaStream_t s) {
   G2 g{ix, jx, (size_t)ix * jx};
   double *A1 = scratch, *A2 = scratch + 8 * g.n, *CU = scratch + 16 * g.n;
   const unsigned blocks = (unsigned)((g.n + kT - 1) / kT);
-  k_adj_cells<<<blocks, kT, 0, s>>>(P, R, lam_in, A1, CU, g, ph);
-  k_adj_corners<<<blocks, kT, 0, s>>>(CU, A1, A2, g, ax, ay, ph, dt);
-  k_adj_gather<<<blocks, kT, 0, s>>>(P, CU, A1, A2, lam_in, lam_out, g, ax, ay, ph, dt);
+  if (df) {
+    k_adj_cells<df::DF><<<blocks, kT, 0, s>>>(P, R, lam_in, A1, CU, g, ph);
+    k_adj_corners<df::DF><<<blocks, kT, 0, s>>>(CU, A1, A2, g, ax, ay, ph, dt);
+    k_adj_gather<df::DF><<<blocks, kT, 0, s>>>(P, CU, A1, A2, lam_in, lam_out, g, ax, ay, ph,
+                                               dt);
+  } else {
+    k_adj_cells<double><<<blocks, kT, 0, s>>>(P, R, lam_in, A1, CU, g, ph);
+    k_adj_corners<double><<<blocks, kT, 0, s>>>(CU, A1, A2, g, ax, ay, ph, dt);
+    k_adj_gather<double><<<blocks, kT, 0, s>>>(P, CU, A1, A2, lam_in, lam_out, g, ax, ay, ph,
+                                               dt);
+  }
   count_launch(3);
   return cudaGetLastError();
 }

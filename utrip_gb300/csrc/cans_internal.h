@@ -195,12 +195,13 @@ cudaError_t launch_hlld3d_finish(bool exact, int ix, int jx, int kx,
 // ---- discrete adjoint of the 2-D mlw_m3 step ---------------------------------
 // P: input state (9 arrays), R: the step's raw output, lam_in: adjoint of R
 // (after the transposed boundary fill), lam_out: adjoint of P.  scratch holds
-// adj2d_scratch_doubles(ix*jx) doubles.
+// adj2d_scratch_doubles(ix*jx) doubles.  df: the reverse arithmetic in
+// double-float on the FP32 pipes (else FP64).
 size_t adj2d_scratch_doubles(size_t ncells);
 cudaError_t launch_adj2d_step(const double *P, const double *R,
                               const double *lam_in, double *lam_out,
                               double *scratch, int ix, int jx, const Axis &ax,
-                              const Axis &ay, const Phys &ph, double dt,
+                              const Axis &ay, const Phys &ph, double dt, bool df,
                               cudaStream_t s);
 // raw output of a step (margin 1, no bdsmn* rule) from the filled states
 // before (P_cur: outer layer) and after it (P_next: every other cell)

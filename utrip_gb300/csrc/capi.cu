@@ -1462,6 +1462,7 @@ struct cans_run {
   double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
   bool df = false;             // double-float policy of the 2-D mlw_m3 step
+  bool adj_df = true;          // reverse sweep of the adjoint in double-float
   unsigned char *avb = nullptr;  // adjoint check: recorded viscosity branches,
   long long avb_steps = 0;       //   2*ix*jx bytes per step
 };
@@ -1988,6 +1989,12 @@ extern "C" int cans_run_set_graph(cans_run *h, int use_graph) {
   return CANS_OK;
 }
 
+extern "C" int cans_run_set_adjoint_df64(cans_run *h, int on) {
+  if (!h) return CANS_ERR_ARG;
+  h->adj_df = on != 0;
+  return CANS_OK;
+}
+
 extern "C" int cans_run_set_tile(cans_run *h, int tile) {
   if (!h || tile < 0 || tile >= tile_count(h)) return CANS_ERR_ARG;
   if (h->tile != tile) {
@@ -2333,7 +2340,7 @@ int adj_reverse(AdjRun &r, long long a, long long b, int slot, int free_snaps) {
     CK(launch_bc2d_transpose(h->nvar, W.lam[0], h->d.ix, h->d.jx, h->ax.a, h->ay.a,
                              h->bc, h->s));
     CK(launch_adj2d_step(Sa, W.R, W.lam[0], W.lam[1], W.scr, h->d.ix, h->d.jx, h->ax.a,
-                         h->ay.a, h->ph, r.dts[a], h->s));
+                         h->ay.a, h->ph, r.dts[a], h->adj_df, h->s));
     std::swap(W.lam[0], W.lam[1]);
     if (r.merge) {  // state a is the next one of the step reversed after this
       CK(cudaMemcpyAsync(W.next, Sa, sizeof(double) * n9, cudaMemcpyDeviceToDevice, h->s));

@@ -145,5 +145,62 @@ __device__ __forceinline__ double widen(float f) {
 }
 __device__ __forceinline__ double to_double(D x) { return __dadd_rn(widen(x.h), widen(x.l)); }
 
+// A double-float number with the arithmetic operators, so that code written
+// once for a number type R runs as R = double (FP64 pipe) or R = DF (FP32
+// pipes).  Literal constants in such code are floats (0.5f, 2.0f): exact in
+// both, and a float operand takes the cheaper mixed operations here.
+struct DF {
+  D d;
+  DF() = default;
+  __device__ __forceinline__ DF(float f) : d{f, 0.0f} {}
+  __device__ __forceinline__ explicit DF(D x) : d(x) {}
+};
+__device__ __forceinline__ DF operator+(DF a, DF b) { return DF(add(a.d, b.d)); }
+__device__ __forceinline__ DF operator+(DF a, float b) { return DF(addf(a.d, b)); }
+__device__ __forceinline__ DF operator+(float a, DF b) { return DF(addf(b.d, a)); }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return DF(sub(a.d, b.d)); }
+__device__ __forceinline__ DF operator-(DF a, float b) { return DF(addf(a.d, -b)); }
+__device__ __forceinline__ DF operator-(float a, DF b) { return DF(addf(neg(b.d), a)); }
+__device__ __forceinline__ DF operator-(DF a) { return DF(neg(a.d)); }
+__device__ __forceinline__ DF operator*(DF a, DF b) { return DF(mul(a.d, b.d)); }
+__device__ __forceinline__ DF operator*(DF a, float b) { return DF(mulf(a.d, b)); }
+__device__ __forceinline__ DF operator*(float a, DF b) { return DF(mulf(b.d, a)); }
+__device__ __forceinline__ DF operator/(DF a, DF b) { return DF(mul(a.d, rcp(b.d))); }
+__device__ __forceinline__ DF &operator+=(DF &a, DF b) { return a = a + b; }
+__device__ __forceinline__ DF &operator-=(DF &a, DF b) { return a = a - b; }
+__device__ __forceinline__ bool operator>(DF a, float b) {
+  return a.d.h > b || (a.d.h == b && a.d.l > 0.0f);
+}
+__device__ __forceinline__ bool operator!=(DF a, float b) {
+  return a.d.h != b || a.d.l != 0.0f;
+}
+__device__ __forceinline__ DF fma(DF a, DF b, DF c) { return DF(mad(a.d, b.d, c.d)); }
+__device__ __forceinline__ DF fabs(DF a) { return DF(absd(a.d)); }
+
 }  // namespace df
+
+// Loads and stores for code templated on its number type R.
+//   num_in<R>(x)   a double of the caller's data (state, metrics) as R
+//   num_out(v)     R back to a double for the caller's data
+//   num_ld / num_st  R through scratch of 8 bytes per value that only this
+//                  code reads back: a double-float is stored as its two
+//                  floats, with no conversion
+template <class R> __device__ __forceinline__ R num_in(double x);
+template <> __device__ __forceinline__ double num_in<double>(double x) { return x; }
+template <> __device__ __forceinline__ df::DF num_in<df::DF>(double x) {
+  return df::DF(df::from_double(x));
+}
+__device__ __forceinline__ double num_out(double v) { return v; }
+__device__ __forceinline__ double num_out(df::DF v) { return df::to_double(v.d); }
+template <class R> __device__ __forceinline__ R num_ld(const double *p);
+template <> __device__ __forceinline__ double num_ld<double>(const double *p) { return *p; }
+template <> __device__ __forceinline__ df::DF num_ld<df::DF>(const double *p) {
+  const float2 f = *reinterpret_cast<const float2 *>(p);
+  return df::DF(df::D{f.x, f.y});
+}
+__device__ __forceinline__ void num_st(double *p, double v) { *p = v; }
+__device__ __forceinline__ void num_st(double *p, df::DF v) {
+  *reinterpret_cast<float2 *>(p) = make_float2(v.d.h, v.d.l);
+}
+
 }  // namespace cans
