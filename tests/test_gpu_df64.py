@@ -20,17 +20,22 @@ def rel_linf(a, b):
     return float(np.max(np.abs(a - b))) / scale if scale else float(np.max(np.abs(a - b)))
 
 
+@pytest.mark.parametrize("tile", [0, 4])
 @pytest.mark.parametrize("make,steps", [
     (lambda: setups.orszag_tang(64), 100),
     (lambda: setups.shear_layer(128, beta=0.5, seed=2), 100),
     (lambda: setups.random_state(53, 41, seed=7), 20),
 ])
-def test_df64_loop_against_oracle(gpu, oracle_lib, make, steps):
+def test_df64_loop_against_oracle(gpu, oracle_lib, make, steps, tile):
     s = make()
     ref = setups.copy_state(s)
     t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, steps)
     got = setups.copy_state(s)
-    t, ns, merr, nexec = drivers.run_resident(s, got, steps, df64=True)
+    run = drivers.make_run(s, df64=True, tile=tile)
+    try:
+        t, ns, merr, nexec = drivers.run_resident(s, got, steps, run=run)
+    finally:
+        run.close()
     assert merr == 0 and ns == ns_ref and nexec == ns
     assert t == pytest.approx(t_ref, rel=1e-12)
     for k, a, b in zip(s["names"], got, ref):
@@ -56,10 +61,13 @@ def test_df64_one_step_close_to_oracle(gpu, oracle_lib):
         assert rel_linf(a, b) <= 2e-13, (k, rel_linf(a, b))
 
 
-def test_df64_tiles_agree_bitwise(gpu):
-    s = setups.orszag_tang(96)
+@pytest.mark.parametrize("n", [96, 130])
+def test_df64_tiles_agree_bitwise(gpu, n):
+    """Every tile shape, the y-marching ones included (segments and chunks
+    ragged at 130), gives the same bits."""
+    s = setups.orszag_tang(n)
     outs = []
-    for tile in range(4):
+    for tile in range(6):
         run = drivers.make_run(s, df64=True)
         try:
             run.set_tile(tile)

@@ -22,6 +22,8 @@
 // policy remains the bit-for-bit path.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "cans_common.cuh"
 #include "cans_internal.h"
 #include "df64.cuh"
@@ -382,6 +384,372 @@ __device__ __forceinline__ void tile_step_df(const double *__restrict__ A,
 #undef SK
 }
 
+// ---------------------------------------------------------------------------
+// The same step with the tile marching in y.  A block owns a strip of 32
+// interior columns and a segment of `seg` interior rows, which it takes in
+// chunks of CH rows; between chunks it keeps the last two cell rows and the
+// last corner row instead of recomputing them, so the halo work is that of
+// a 32 x seg tile, while its shared memory is that of a 32 x CH tile.  A
+// block has 34 CH threads (rounded up to whole warps): one per cell of a
+// chunk's new rows (phase 1), one per corner (phase 2) and one per updated
+// cell (phase 3, 32 CH of them).
+template <int CH>
+struct MarchD {
+  static constexpr int TX = 32, CX = TX + 2, KX = TX + 1;
+  static constexpr int CR = CH + 2, KR = CH + 1;       // cell rows, corner rows
+  static constexpr int NC = CX * CR, NK = KX * KR;
+  static constexpr int NQX = KX * CH, NQY = TX * KR;
+  // 34 CH threads rounded up to whole warps: the warp-level reductions at the
+  // end take every lane of a warp
+  static constexpr int NT = (CX * CH + 31) / 32 * 32;
+  static constexpr size_t smem_bytes =
+      sizeof(D) * ((size_t)NCS * NC + (size_t)NKS * NK + NQX + NQY) + sizeof(double) * 32;
+};
+
+// Cell values of one cell (phase 1 of the tile).
+template <int NCc>
+__device__ __forceinline__ void cell_df(const double *__restrict__ A, size_t n, size_t g,
+                                        D *sc, int c, const PhysD &P) {
+#define SC(s, c) sc[(size_t)(s) * NCc + (c)]
+  const D ro = df::from_double(A[PRO * n + g]), pr = df::from_double(A[PPR * n + g]);
+  const D vx = df::from_double(A[PVX * n + g]), vy = df::from_double(A[PVY * n + g]);
+  const D vz = df::from_double(A[PVZ * n + g]);
+  const D bx = df::from_double(A[PBX * n + g]), by = df::from_double(A[PBY * n + g]);
+  const D bz = df::from_double(A[PBZ * n + g]);
+  const D vv = df::mad(vz, vz, df::mad(vy, vy, df::sqr(vx)));
+  const D bb = df::mad(bz, bz, df::mad(by, by, df::sqr(bx)));
+  const D ek = df::mul(df::scale(ro, 0.5f), vv);
+  const D ee = df::mad(pr, P.gm1i, df::mad(P.pi8i, bb, ek));
+  const D ep = df::mad(pr, P.ggm1, ek);
+  const D rx = df::mul(ro, vx), ry = df::mul(ro, vy), rz = df::mul(ro, vz);
+  const D ex = df::mad(vz, by, df::neg(df::mul(vy, bz)));
+  const D ey = df::mad(vx, bz, df::neg(df::mul(vz, bx)));
+  const D ez = df::mad(vy, bx, df::neg(df::mul(vx, by)));
+  const D pt = df::mad(P.pi8i, bb, pr);
+  const D pbx = df::mul(P.pi4i, bx), pby = df::mul(P.pi4i, by);
+  SC(CRO, c) = ro; SC(CEE, c) = ee; SC(CRX, c) = rx; SC(CRY, c) = ry; SC(CRZ, c) = rz;
+  SC(CBX, c) = bx; SC(CBY, c) = by; SC(CBZ, c) = bz;
+  SC(CEX, c) = ex; SC(CEY, c) = ey; SC(CEZ, c) = ez; SC(CVX, c) = vx; SC(CVY, c) = vy;
+  SC(CFXE, c) = df::mad(df::mad(bz, ey, df::neg(df::mul(by, ez))), P.pi4i, df::mul(ep, vx));
+  SC(CFYE, c) = df::mad(df::mad(bx, ez, df::neg(df::mul(bz, ex))), P.pi4i, df::mul(ep, vy));
+  SC(CFXRX, c) = df::mad(rx, vx, df::mad(df::neg(pbx), bx, pt));
+  SC(CFYRY, c) = df::mad(ry, vy, df::mad(df::neg(pby), by, pt));
+  SC(CFXY, c) = df::mad(rx, vy, df::neg(df::mul(pbx, by)));
+  SC(CFXRZ, c) = df::mad(rz, vx, df::neg(df::mul(pbx, bz)));
+  SC(CFYRZ, c) = df::mad(rz, vy, df::neg(df::mul(pby, bz)));
+#undef SC
+}
+
+// Half-step values of one corner from its four cells a, b (x+1), cc (x+1,
+// y+1), d (y+1) (phase 2 of the tile).
+template <int NCc, int NKc>
+__device__ __forceinline__ void corner_df(const D *sc, D *sk, int a, int b, int cc, int d,
+                                          int k, D cxk, D cyk, const PhysD &P) {
+#define SC(s, c) sc[(size_t)(s) * NCc + (c)]
+#define SK(s, c) sk[(size_t)(s) * NKc + (c)]
+  auto pred = [&](int su, int sfx, int sfy, bool negx, bool negy) -> D {
+    D r = df::scale(df::add(df::add(SC(su, b), SC(su, a)), df::add(SC(su, cc), SC(su, d))),
+                    0.25f);
+    if (sfx != NOF) {
+      const D s = df::add(df::sub(SC(sfx, b), SC(sfx, a)), df::sub(SC(sfx, cc), SC(sfx, d)));
+      r = df::mad(negx ? cxk : df::neg(cxk), s, r);
+    }
+    if (sfy != NOF) {
+      const D s = df::add(df::sub(SC(sfy, d), SC(sfy, a)), df::sub(SC(sfy, cc), SC(sfy, b)));
+      r = df::mad(negy ? cyk : df::neg(cyk), s, r);
+    }
+    return r;
+  };
+  const D roh = pred(CRO, CRX, CRY, false, false);
+  const D eeh = pred(CEE, CFXE, CFYE, false, false);
+  const D rxh = pred(CRX, CFXRX, CFXY, false, false);
+  const D ryh = pred(CRY, CFXY, CFYRY, false, false);
+  const D rzh = pred(CRZ, CFXRZ, CFYRZ, false, false);
+  const D bxh = pred(CBX, NOF, CEZ, false, false);
+  const D byh = pred(CBY, CEZ, NOF, true, false);
+  const D bzh = pred(CBZ, CEY, CEX, false, true);
+  const D rinv = df::rcp(roh);
+  const D vxh = df::mul(rxh, rinv), vyh = df::mul(ryh, rinv), vzh = df::mul(rzh, rinv);
+  const D vv = df::mad(vzh, vzh, df::mad(vyh, vyh, df::sqr(vxh)));
+  const D bb = df::mad(bzh, bzh, df::mad(byh, byh, df::sqr(bxh)));
+  const D ek = df::mul(df::scale(roh, 0.5f), vv);
+  const D prh = df::mul(P.gm1, df::sub(df::sub(eeh, ek), df::mul(P.pi8i, bb)));
+  const D ep = df::mad(prh, P.ggm1, ek);
+  const D exh = df::mad(vzh, byh, df::neg(df::mul(vyh, bzh)));
+  const D eyh = df::mad(vxh, bzh, df::neg(df::mul(vzh, bxh)));
+  const D ezh = df::mad(vyh, bxh, df::neg(df::mul(vxh, byh)));
+  const D pt = df::mad(P.pi8i, bb, prh);
+  const D pbx = df::mul(P.pi4i, bxh), pby = df::mul(P.pi4i, byh);
+  SK(KXRO, k) = rxh;
+  SK(KYRO, k) = ryh;
+  SK(KEX, k) = exh; SK(KEY, k) = eyh; SK(KEZ, k) = ezh;
+  SK(KXEE, k) = df::mad(df::mad(bzh, eyh, df::neg(df::mul(byh, ezh))), P.pi4i, df::mul(ep, vxh));
+  SK(KYEE, k) = df::mad(df::mad(bxh, ezh, df::neg(df::mul(bzh, exh))), P.pi4i, df::mul(ep, vyh));
+  SK(KXRX, k) = df::mad(rxh, vxh, df::mad(df::neg(pbx), bxh, pt));
+  SK(KYRY, k) = df::mad(ryh, vyh, df::mad(df::neg(pby), byh, pt));
+  SK(KXY, k) = df::mad(rxh, vyh, df::neg(df::mul(pbx, byh)));
+  SK(KXRZ, k) = df::mad(rzh, vxh, df::neg(df::mul(pbx, bzh)));
+  SK(KYRZ, k) = df::mad(rzh, vyh, df::neg(df::mul(pby, bzh)));
+#undef SC
+#undef SK
+}
+
+template <int CH>
+__global__ void __launch_bounds__(MarchD<CH>::NT, 2)
+    k_mlw2d_df_march(const double *__restrict__ A, double *__restrict__ B, int ix, int jx,
+                     Axis ax, Axis ay, Phys ph, double dt_arg, Ctl *__restrict__ ctl, Box3 box,
+                     int seg) {
+  using T = MarchD<CH>;
+  extern __shared__ D smem_m[];
+  D *sc = smem_m;                          // cells   [NCS][CR][CX]
+  D *sk = sc + (size_t)NCS * T::NC;        // corners [NKS][KR][KX]
+  D *sqx = sk + (size_t)NKS * T::NK;       // q dxim  [CH][KX]
+  D *sqy = sqx + T::NQX;                   // q dyim  [KR][TX]
+  double *sred = reinterpret_cast<double *>(sqy + T::NQY);
+  double dtv = dt_arg, safety = 0.0;
+  unsigned long long *cfl_out = nullptr;
+  if (ctl != nullptr) {
+    if (ctl->done | ctl->pause) return;
+    A = ctl->buf[ctl->cur];
+    B = ctl->buf[ctl->cur ^ 1];
+    dtv = ctl->dt;
+    safety = ctl->safety;
+    cfl_out = &ctl->cfl_bits;
+  }
+#define SC(s, c) sc[(size_t)(s) * T::NC + (c)]
+#define SK(s, c) sk[(size_t)(s) * T::NK + (c)]
+  const size_t n = (size_t)ix * (size_t)jx;
+  const int tid = threadIdx.x;
+  const int i0 = 1 + blockIdx.x * T::TX;
+  const int jb = 1 + blockIdx.y * seg;                 // first interior row of the segment
+  const int je = min(jx - 2, jb + seg - 1);            // last
+  const PhysD P = phys_d(ph);
+  const D dt = df::from_double(dtv);
+  const D hdt = df::scale(dt, 0.5f);
+  const bool edge_x = blockIdx.x == 0 || blockIdx.x == gridDim.x - 1;
+  D kmax = df::mk(0.0f);
+  bool bad = false;
+
+  for (int j0 = jb; j0 <= je; j0 += CH) {
+    const bool first = j0 == jb;
+    if (!first) {
+      // keep the chunk's last two cell rows and last corner row
+      for (int e = tid; e < NCS * 2 * T::CX; e += T::NT) {
+        const int s = e / (2 * T::CX), r = e % (2 * T::CX);
+        SC(s, r) = SC(s, CH * T::CX + r);
+      }
+      for (int e = tid; e < NKS * T::KX; e += T::NT) {
+        const int s = e / T::KX, r = e % T::KX;
+        SK(s, r) = SK(s, CH * T::KX + r);
+      }
+      __syncthreads();
+    }
+    // ---- phase 1: new cell rows (all CH + 2 of the first chunk) ----
+    const int last_row = min(CH + 1, je + 1 - (j0 - 1));  // rows past je+1 are not read
+    for (int c = (first ? 0 : 2 * T::CX) + tid; c < (last_row + 1) * T::CX; c += T::NT) {
+      const int lx = c % T::CX, ly = c / T::CX;
+      const int gi = i0 - 1 + lx, gj = j0 - 1 + ly;
+      if (gi < ix && gj < jx) {
+        cell_df<T::NC>(A, n, (size_t)gi + (size_t)gj * ix, sc, c, P);
+      } else {
+#pragma unroll 1
+        for (int s = 0; s < NCS; s++) SC(s, c) = df::mk(0.0f);
+      }
+    }
+    __syncthreads();
+    // ---- phase 2: new corner rows, and the viscosity faces ----
+    for (int k = (first ? 0 : T::KX) + tid; k < last_row * T::KX; k += T::NT) {
+      const int kx = k % T::KX, ky = k / T::KX;
+      const int gi = i0 - 1 + kx, gj = j0 - 1 + ky;
+      if (gi <= ix - 2 && gj <= jx - 2) {
+        const int a = kx + ky * T::CX;
+        const D cxk = df::scale(df::mul(dt, df::from_double(ax.dim[gi])), 0.5f);
+        const D cyk = df::scale(df::mul(dt, df::from_double(ay.dim[gj])), 0.5f);
+        corner_df<T::NC, T::NK>(sc, sk, a, a + 1, a + 1 + T::CX, a + T::CX, k, cxk, cyk, P);
+      } else {
+#pragma unroll 1
+        for (int s = 0; s < NKS; s++) SK(s, k) = df::mk(0.0f);
+      }
+    }
+    for (int f = tid; f < T::NQX; f += T::NT) {
+      const int fx = f % T::KX, r = f / T::KX;
+      const int gi = i0 - 1 + fx, gj = j0 + r;
+      D v = df::mk(0.0f);
+      if (gi + 1 < ix && gj < jx) {
+        const int cl = fx + (r + 1) * T::CX;
+        const D q = df::addf(df::absd(df::sub(SC(CVX, cl + 1), SC(CVX, cl))), -1.0e-4f);
+        if (df::pos(q))
+          v = df::mul(df::mul(df::mul(P.qav, df::from_double(ax.dm[gi])), q),
+                      df::from_double(ax.dim[gi]));
+      }
+      sqx[f] = v;
+    }
+    for (int f = tid; f < T::NQY; f += T::NT) {
+      const int fx = f % T::TX, r = f / T::TX;
+      const int gi = i0 + fx, gj = j0 - 1 + r;
+      D v = df::mk(0.0f);
+      if (gi < ix && gj + 1 < jx) {
+        const int cl = (fx + 1) + r * T::CX;
+        const D q = df::addf(df::absd(df::sub(SC(CVY, cl + T::CX), SC(CVY, cl))), -1.0e-4f);
+        if (df::pos(q))
+          v = df::mul(df::mul(df::mul(P.qav, df::from_double(ay.dm[gj])), q),
+                      df::from_double(ay.dim[gj]));
+      }
+      sqy[f] = v;
+    }
+    __syncthreads();
+    // ---- phase 3: the chunk's own cells ----
+    if (tid < T::TX * CH) {
+      const int lx = tid % T::TX + 1, ly = tid / T::TX + 1;
+      const int gi = i0 - 1 + lx, gj = j0 - 1 + ly;
+      if (gi <= ix - 2 && gj <= je) {
+        const size_t g = (size_t)gi + (size_t)gj * ix;
+        // the doubles the update adds to, loaded ahead of the arithmetic
+        const double ro0 = A[PRO * n + g], bx0 = A[PBX * n + g], by0 = A[PBY * n + g];
+        const double bz0 = A[PBZ * n + g], az0 = A[PAZ * n + g];
+        const int c = lx + ly * T::CX;
+        const int cE = c + 1, cW = c - 1, cN = c + T::CX, cS = c - T::CX;
+        const int kSW = (lx - 1) + (ly - 1) * T::KX, kSE = kSW + 1;
+        const int kNW = kSW + T::KX, kNE = kNW + 1;
+        const D dxi = df::from_double(ax.di[gi]), dyi = df::from_double(ay.di[gj]);
+        const D ux0 = df::from_double(ax.u0[gi]), ux1 = df::from_double(ax.u1[gi]);
+        const D uy0 = df::from_double(ay.u0[gj]), uy1 = df::from_double(ay.u1[gj]);
+        const D hdx = df::mul(hdt, dxi), hdy = df::mul(hdt, dyi);
+        const D fcx = df::scale(hdx, 0.5f), fcy = df::scale(hdy, 0.5f);
+        const D fx0 = df::mul(hdx, uy0), fx1 = df::mul(hdx, uy1);
+        const D fy0 = df::mul(hdy, ux0), fy1 = df::mul(hdy, ux1);
+        const D dtx = df::mul(dt, dxi), dty = df::mul(dt, dyi);
+        const D ae = df::mul(dtx, sqx[lx + (ly - 1) * T::KX]);
+        const D aw = df::mul(dtx, sqx[lx - 1 + (ly - 1) * T::KX]);
+        const D an = df::mul(dty, sqy[(lx - 1) + ly * T::TX]);
+        const D as = df::mul(dty, sqy[(lx - 1) + (ly - 1) * T::TX]);
+        auto dvar = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx, bool nkx,
+                        int kfy, bool nky) -> D {
+          const D u = SC(su, c);
+          D du = df::mul(ae, df::sub(SC(su, cE), u));
+          du = df::mad(aw, df::sub(SC(su, cW), u), du);
+          du = df::mad(an, df::sub(SC(su, cN), u), du);
+          du = df::mad(as, df::sub(SC(su, cS), u), du);
+          if (sfx != NOF)
+            du = df::mad(negx ? fcx : df::neg(fcx), df::sub(SC(sfx, cE), SC(sfx, cW)), du);
+          if (sfy != NOF)
+            du = df::mad(negy ? fcy : df::neg(fcy), df::sub(SC(sfy, cN), SC(sfy, cS)), du);
+          if (kfx != NOF) {
+            du = df::mad(nkx ? fx0 : df::neg(fx0), df::sub(SK(kfx, kSE), SK(kfx, kSW)), du);
+            du = df::mad(nkx ? fx1 : df::neg(fx1), df::sub(SK(kfx, kNE), SK(kfx, kNW)), du);
+          }
+          if (kfy != NOF) {
+            du = df::mad(nky ? fy0 : df::neg(fy0), df::sub(SK(kfy, kNW), SK(kfy, kSW)), du);
+            du = df::mad(nky ? fy1 : df::neg(fy1), df::sub(SK(kfy, kNE), SK(kfy, kSE)), du);
+          }
+          return du;
+        };
+        const double ro_new =
+            ro0 + df::to_double(dvar(CRO, CRX, false, CRY, false, KXRO, false, KYRO, false));
+        const double bx_new =
+            bx0 + df::to_double(dvar(CBX, NOF, false, CEZ, false, NOF, false, KEZ, false));
+        const double by_new =
+            by0 + df::to_double(dvar(CBY, CEZ, true, NOF, false, KEZ, true, NOF, false));
+        const double bz_new =
+            bz0 + df::to_double(dvar(CBZ, CEY, false, CEX, true, KEY, false, KEX, true));
+        const D ee =
+            df::add(SC(CEE, c), dvar(CEE, CFXE, false, CFYE, false, KXEE, false, KYEE, false));
+        const D rx =
+            df::add(SC(CRX, c), dvar(CRX, CFXRX, false, CFXY, false, KXRX, false, KXY, false));
+        const D ry =
+            df::add(SC(CRY, c), dvar(CRY, CFXY, false, CFYRY, false, KXY, false, KYRY, false));
+        const D rz =
+            df::add(SC(CRZ, c), dvar(CRZ, CFXRZ, false, CFYRZ, false, KXRZ, false, KYRZ, false));
+        {
+          D s = df::mul(ux0, SK(KEZ, kSW));
+          s = df::mad(ux1, SK(KEZ, kSE), s);
+          D t = df::mul(ux0, SK(KEZ, kNW));
+          t = df::mad(ux1, SK(KEZ, kNE), t);
+          s = df::mad(uy1, t, df::mul(uy0, s));
+          s = df::mad(hdt, SC(CEZ, c), df::mul(hdt, s));
+          B[PAZ * n + g] = az0 - df::to_double(s);
+        }
+        const D ro = df::from_double(ro_new);
+        const D bx = df::from_double(bx_new), by = df::from_double(by_new);
+        const D bz = df::from_double(bz_new);
+        const D rinv = df::rcp(ro);
+        const D vx = df::mul(rx, rinv), vy = df::mul(ry, rinv), vz = df::mul(rz, rinv);
+        const D vv = df::mad(vz, vz, df::mad(vy, vy, df::sqr(vx)));
+        const D bb = df::mad(bz, bz, df::mad(by, by, df::sqr(bx)));
+        const D pr = df::mul(P.gm1, df::sub(df::sub(ee, df::mul(df::scale(ro, 0.5f), vv)),
+                                            df::mul(P.pi8i, bb)));
+        const double prd = df::to_double(pr);
+        B[PRO * n + g] = ro_new;
+        B[PPR * n + g] = prd;
+        B[PVX * n + g] = df::to_double(vx);
+        B[PVY * n + g] = df::to_double(vy);
+        B[PVZ * n + g] = df::to_double(vz);
+        B[PBX * n + g] = bx_new;
+        B[PBY * n + g] = by_new;
+        B[PBZ * n + g] = bz_new;
+        if (cfl_out != nullptr && gi >= box.lo[0] && gi <= box.hi[0] && gj >= box.lo[1] &&
+            gj <= box.hi[1]) {
+          const D sk2 = df::mad(df::mad(P.gm, pr, df::mul(P.pi4i, bb)), rinv, vv);
+          const D ix2 = df::sqr(dxi), iy2 = df::sqr(dyi);
+          const D key = df::mul(sk2, df::gt(ix2, iy2) ? ix2 : iy2);
+          if (key.h == key.h && df::gt(key, kmax)) kmax = key;
+          bad |= bad_cell_d(ro_new, prd, key);
+        }
+      }
+    }
+    // ghost cells of the output keep their input values; each is copied by
+    // the chunk owning its nearest interior cell
+    if (edge_x || j0 == 1 || j0 + CH - 1 >= jx - 2) {
+      for (int c = tid; c < T::NC; c += T::NT) {
+        const int hx = c % T::CX, hy = c / T::CX;
+        const int gi = i0 - 1 + hx, gj = j0 - 1 + hy;
+        if (gi >= ix || gj >= jx) continue;
+        if (gi != 0 && gi != ix - 1 && gj != 0 && gj != jx - 1) continue;
+        const int ci = min(max(gi, 1), ix - 2), cj = min(max(gj, 1), jx - 2);
+        if (ci < i0 || ci >= i0 + T::TX || cj < j0 || cj >= j0 + CH || cj > je) continue;
+        const size_t g = (size_t)gi + (size_t)gj * ix;
+#pragma unroll
+        for (int v = 0; v < NPV; v++) B[v * n + g] = A[v * n + g];
+      }
+    }
+    __syncthreads();
+  }
+#undef SC
+#undef SK
+  if (cfl_out != nullptr) {
+    if (ctl != nullptr) count_bad_block(bad, &ctl->nonfinite, tid);
+    kmax = warp_max_d(kmax);
+    const int lane = tid & 31, w = tid >> 5;
+    if (lane == 0) sred[w] = df::to_double(kmax);
+    __syncthreads();
+    if (w == 0) {
+      double x = lane < (T::NT + 31) / 32 ? sred[lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = (y > x || x != x) ? y : x;
+      }
+      if (lane == 0 && x > 0.0) atomic_min_pos(cfl_out, safety / sqrt(x));
+    }
+  }
+}
+
+// Rows per block of the marching kernel: a multiple of CH for which the
+// launch's waves times the block's rows (plus its two-row prologue) is least.
+inline int balance_seg(int strips, int rows, int ch, int slots) {
+  int best = ch, best_cost = -1;
+  for (int seg = ch; seg <= rows + ch - 1; seg += ch) {
+    const int blocks = strips * ((rows + seg - 1) / seg);
+    const int waves = (blocks + slots - 1) / slots;
+    const int cost = waves * (seg + 2);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = seg;
+    }
+  }
+  return best;
+}
+
 template <int TX, int TY, int RPT>
 __global__ void __launch_bounds__(TX *TY / RPT, 1)
     k_mlw2d_df(const double *__restrict__ A, double *__restrict__ B, int ix, int jx, Axis ax,
@@ -420,13 +788,54 @@ cudaError_t launch_df(const double *A, double *B, int ix, int jx, const Axis &ax
 
 }  // namespace
 
-int mlw2d_df_tile_count() { return 4; }
+namespace {
+template <int CH>
+cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis &ax,
+                         const Axis &ay, const Phys &ph, double dt, Ctl *ctl, Box3 box,
+                         cudaStream_t s) {
+  using T = MarchD<CH>;
+  static std::mutex mu;
+  static int slots_of[64] = {};
+  int dev = 0, slots = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!slots_of[dev]) {
+      e = cudaFuncSetAttribute(k_mlw2d_df_march<CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)T::smem_bytes);
+      if (e != cudaSuccess) return e;
+      int sms = 0, per_sm = 0;
+      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return e;
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlw2d_df_march<CH>,
+                                                             T::NT, T::smem_bytes)) !=
+          cudaSuccess)
+        return e;
+      slots_of[dev] = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    slots = slots_of[dev];
+  }
+  const int strips = (ix - 2 + T::TX - 1) / T::TX, rows = jx - 2;
+  const int seg = balance_seg(strips, rows, CH, slots);
+  dim3 grid(strips, (rows + seg - 1) / seg);
+  k_mlw2d_df_march<CH><<<grid, T::NT, T::smem_bytes, s>>>(A, B, ix, jx, ax, ay, ph, dt, ctl,
+                                                         box, seg);
+  count_launch();
+  return cudaGetLastError();
+}
+}  // namespace
+
+int mlw2d_df_tile_count() { return 6; }
 
 cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx,
                             const Axis &ax, const Axis &ay, const Phys &ph, double dt,
                             Ctl *ctl, Box3 box, cudaStream_t s) {
   if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
   switch (tile) {
+    case 4: return launch_march<8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 5: return launch_march<6>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 1: return launch_df<32, 9, 1>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 2: return launch_df<16, 16, 2>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 3: return launch_df<32, 16, 2>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
