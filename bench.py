@@ -166,6 +166,29 @@ def extra_workloads(stream, exact=False):
         "hbm_frac": 128 * zones / (kstep * 1e-3) / 1e9 / hbm_peak, "bytes_per_zone": 128,
         "steps_done": int(st.nexec), "merr": int(st.merr)}
     run.close()
+    # the same box in the double-float policy
+    run = drivers.make_run(s3, stream=stream.cuda_stream, df64=True)
+    run.push(s3["state"])
+    tile = run.autotune(2)
+    run.push(s3["state"])
+    run.start(tend=1e30, nstop=10 ** 12, safety=s3["safety"], dtmin=s3["dtmin"])
+    run.advance(3)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    run.advance(iters)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    step_ms, _ = run.profile(10)
+    st = run.query()
+    kstep = step_ms / 10
+    out["turbulence_256^3_mlw_m_df64"] = {
+        "zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+        "step_kernel_ms": kstep, "tile": tile, "hbm_gbs": 128 * zones / (kstep * 1e-3) / 1e9,
+        "hbm_frac": 128 * zones / (kstep * 1e-3) / 1e9 / hbm_peak, "bytes_per_zone": 128,
+        "steps_done": int(st.nexec), "merr": int(st.merr), "policy": "df64",
+        "parity": "parity_vs_oracle.turbulence_256^3_mlw_m_3d_200_steps.df64_rel_linf"}
+    run.close()
     del s3
     # ---- 1-D: the whole shock-tube run to t = 0.1 in one cluster launch
     s1 = setups.shock_tube_1d(1024)
@@ -862,14 +885,17 @@ def parity_3d(stream, solver, n, steps, exact_too):
     leg = {"steps": int(ns_ref), "oracle_s": time.perf_counter() - t0,
            "oracle_cores": oracle.get_threads()}
     tot0 = _totals(s, s["state"])
-    for exact in ((False, True) if exact_too else (False,)):
+    policies = ["fast"] + (["exact"] if exact_too else []) + \
+        (["df64"] if solver == "mlw_m_3d" else [])
+    for policy in policies:
         got = setups.copy_state(s)
-        t, ns, merr, _ = drivers.run_resident(s, got, steps, exact=exact)
-        if exact:
+        t, ns, merr, _ = drivers.run_resident(s, got, steps, exact=policy == "exact",
+                                              df64=policy == "df64")
+        if policy == "exact":
             leg["exact_cells_differing"] = int(sum(int(np.sum(a != b)) for a, b in zip(got, ref)))
         else:
-            leg["fast_rel_linf"] = _rel_linf(s["names"], got, ref)
-            leg["conservation_drift_fast"] = _drift(tot0, _totals(s, got))
+            leg[f"{policy}_rel_linf"] = _rel_linf(s["names"], got, ref)
+            leg[f"conservation_drift_{policy}"] = _drift(tot0, _totals(s, got))
         del got
     leg["conservation_drift_oracle"] = _drift(tot0, _totals(s, ref))
     return leg
@@ -1106,6 +1132,67 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def policy_line(n, steps, warmup, m, stream, df64, hbm_peak, fp32_peak):
+    """The headline workload in one arithmetic policy, measured as the main
+    line is: autotuned tile, graph-replayed iterations timed with events on
+    the run's stream with the L2 flushed between benchmark steps, the step
+    kernel timed alone, and the same through the public API with host
+    buffers copied in and out every benchmark step."""
+    import torch
+    from utrip_gb300 import capi, drivers, setups
+    s = setups.orszag_tang(n)
+    run = drivers.make_run(s, stream=stream.cuda_stream, df64=df64)
+    run.push(setups.copy_state(s))
+    tile = run.autotune(5)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        run.advance(m)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    c0 = capi.launch_count()
+    for k in range(steps):
+        flush.fill_(1.0)
+        ev[k][0].record(stream)
+        run.advance(m)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    launches = capi.launch_count() - c0
+    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+    st = run.query()
+    step_ms, iter_ms = run.profile(200)
+    step_avg = step_ms / 200
+    host = [torch.empty((n + 2, n + 2), dtype=torch.float64, pin_memory=True).numpy().T
+            for _ in range(run.nvar)]
+    for h, a in zip(host, s["state"]):
+        h[...] = a
+    e2e_steps = max(3, steps // 2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        run.push(host)
+        run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
+        run.advance(m)
+        run.pull(host)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    nbytes = run.nvar * (n + 2) * (n + 2) * 8
+    run.close()
+    achieved = B_PER_ZONE * n * n / (step_avg * 1e-3) / 1e9
+    return {"value": n * n * m * steps / (dev_ms * 1e-3), "unit": UNIT,
+            "ms_per_step": dev_ms / steps, "tile": tile, "gpu_launches": int(launches),
+            "steps_done": int(st.nexec), "merr": int(st.merr),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "bytes_per_zone": B_PER_ZONE,
+                         "step_kernel_ms": step_avg, "iteration_ms": iter_ms / 200},
+            "e2e": {"value": n * n * m * e2e_steps / (e0.elapsed_time(e1) * 1e-3), "unit": UNIT,
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "fp32_peak_tflops_measured": fp32_peak}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     from utrip_gb300 import capi, drivers, setups
@@ -1192,6 +1279,15 @@ def run_ours(args, ws, rank, local):
     e2e_val = n * n * m * e2e_steps * ws / (e2e_ms * 1e-3)
     nbytes = run.nvar * (n + 2) * (n + 2) * 8
     run.close()
+    df64_line = None
+    if not args.exact and not args.df64:
+        hbm_peak0, _ = measured_peaks()
+        df64_line = policy_line(n, args.steps, args.warmup, m, stream, True, hbm_peak0,
+                                fp32_peak)
+        df64_line["policy"] = ("double-float: the step's arithmetic as pairs of floats on the "
+                               "FP32 pipes, density and field accumulated in FP64 "
+                               "(cans_run_set_df64); its parity against the oracle is "
+                               "parity_vs_oracle.orszag_tang_*.df64_rel_linf")
     parity = parity_check(n, stream) if rank == 0 and not args.no_extras else None
     extras = None if args.no_extras else extra_workloads(stream, exact=args.exact)
 
@@ -1220,6 +1316,8 @@ def run_ours(args, ws, rank, local):
         "wall_s": wall,
         "clocks": clk.summary(),
     }
+    if df64_line is not None:
+        line["df64_policy"] = df64_line
     if parity is not None:
         line["parity_vs_oracle"] = parity
     if extras is not None:

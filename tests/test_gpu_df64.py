@@ -1,6 +1,6 @@
-"""The double-float policy of the 2-D mlw_m3 step (cans_run_set_df64):
-the step's arithmetic in pairs of floats on the FP32 pipes, the conserved
-density and field accumulated in FP64.  It is held to the fast policy's bar
+"""The double-float policy of the 2-D mlw_m3 and 3-D mlw_m steps
+(cans_run_set_df64): the step's arithmetic in pairs of floats on the FP32
+pipes, the conserved density and field accumulated in FP64.  It is held to the fast policy's bar
 against the oracle -- relative L-infinity <= 1e-10 per variable after 100
 steps -- on the benchmark vortex, the shear layer and a ragged random state,
 and it must converge to the exact shock-tube solution like the oracle."""
@@ -101,10 +101,67 @@ def test_df64_shock_tube_converges_like_the_oracle(gpu, oracle_lib):
 def test_df64_refused_where_it_does_not_apply(gpu):
     for s, exact in ((setups.orszag_tang(32, solver="mlw_m"), False),
                      (setups.orszag_tang(32), True),
-                     (setups.random_state_3d(12, 12, 12, seed=1), False)):
+                     (setups.random_state_3d(12, 12, 12, seed=1, solver="roe_m_3d"), False),
+                     (setups.random_state_3d(12, 12, 12, seed=1), True)):
         run = drivers.make_run(s, exact=exact)
         try:
             with pytest.raises(capi.CansError):
                 run.set_df64(True)
         finally:
             run.close()
+
+
+# ---- the 3-D mlw_m step ------------------------------------------------------
+
+@pytest.mark.parametrize("tile", [0, 1])
+@pytest.mark.parametrize("make,steps", [
+    (lambda: setups.turbulence_3d(24, rms=0.05), 100),
+    (lambda: setups.random_state_3d(21, 18, 23, seed=4), 20),
+])
+def test_df64_3d_loop_against_oracle(gpu, oracle_lib, make, steps, tile):
+    s = make()
+    ref = setups.copy_state(s)
+    t_ref, ns_ref, _, _ = oracle.run_3d(s, ref, steps)
+    got = setups.copy_state(s)
+    run = drivers.make_run(s, df64=True, tile=tile)
+    try:
+        t, ns, merr, nexec = drivers.run_resident(s, got, steps, run=run)
+    finally:
+        run.close()
+    assert merr == 0 and ns == ns_ref and nexec == ns
+    assert t == pytest.approx(t_ref, rel=1e-12)
+    for k, a, b in zip(s["names"], got, ref):
+        assert np.isfinite(a).all(), k
+        assert rel_linf(a, b) <= TOL, (k, rel_linf(a, b))
+
+
+def test_df64_3d_tiles_agree_bitwise(gpu):
+    s = setups.turbulence_3d(40, rms=0.05)
+    outs = []
+    for tile in range(2):
+        run = drivers.make_run(s, df64=True)
+        try:
+            run.set_tile(tile)
+            st = setups.copy_state(s)
+            drivers.run_resident(s, st, 12, run=run)
+            outs.append(st)
+        finally:
+            run.close()
+    for a, b in zip(outs[1], outs[0]):
+        assert np.array_equal(a, b)
+
+
+def test_df64_3d_shock_tube_converges_like_the_oracle(gpu, oracle_lib):
+    s = setups.sod_shock_tube(512, 3)
+    got = setups.copy_state(s)
+    t, ns, merr, _ = drivers.run_resident(s, got, 10 ** 6, df64=True)
+    ref = setups.copy_state(s)
+    t_ref, ns_ref, _, _ = oracle.run_3d(s, ref, 10 ** 6)
+    assert merr == 0 and ns == ns_ref
+    sd = s["sod"]
+    e = an.l1_errors(*setups.sod_interior_profile(s, got), t, sd["x0"], sd["gm"], sd["ro1"],
+                     sd["pr1"])
+    er = an.l1_errors(*setups.sod_interior_profile(s, ref), t_ref, sd["x0"], sd["gm"],
+                      sd["ro1"], sd["pr1"])
+    for k in e:
+        assert e[k] == pytest.approx(er[k], rel=1e-6), k

@@ -38,6 +38,11 @@ namespace cans {
 namespace {
 
 constexpr int kT = 128;
+// four resident blocks per SM (at most 128 registers a thread): a 258^2
+// grid's 520 blocks then fit in one wave of 152 x 4 slots, where three
+// blocks per SM (the registers the reverse kernels would otherwise take)
+// need two waves, the second nearly empty
+constexpr int kMinBlocks = 4;
 // primitive slots of the state (mlw_m3 order) and conserved slots
 enum { P_RO = 0, P_PR, P_VX, P_VY, P_VZ, P_BX, P_BY, P_BZ, P_AZ };
 enum { C_RO = 0, C_EE, C_RX, C_RY, C_RZ, C_BX, C_BY, C_BZ };
@@ -265,7 +270,7 @@ __device__ __forceinline__ void load_prim(const double *S, size_t n, size_t c, R
 
 // a' on the interior, the cell values U, FX, FY of P everywhere
 template <class R>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(kT, kMinBlocks)
     k_adj_cells(const double *__restrict__ P, const double *__restrict__ Rw,
                 const double *__restrict__ lam, double *__restrict__ A1,
                 double *__restrict__ CU, G2 g, Phys ph_) {
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(kT)
 
 // corners (p+1/2, q+1/2), p = 0..ix-2, q = 0..jx-2 (0-based), stored at p+q*ix
 template <class R>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(kT, kMinBlocks)
     k_adj_corners(const double *__restrict__ CU, const double *__restrict__ A1,
                   double *__restrict__ A2, G2 g, Axis ax, Axis ay, Phys ph_,
                   double dt_) {
@@ -360,7 +365,7 @@ __global__ void __launch_bounds__(kT)
 
 // adjoint of P for every cell
 template <class R>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(kT, kMinBlocks)
     k_adj_gather(const double *__restrict__ P, const double *__restrict__ CU,
                  const double *__restrict__ A1, const double *__restrict__ A2,
                  const double *__restrict__ lam, double *__restrict__ out, G2 g,

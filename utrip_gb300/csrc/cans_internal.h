@@ -68,6 +68,11 @@ cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx
                             const Axis &ax, const Axis &ay, const Phys &ph, double dt,
                             Ctl *ctl, Box3 box, cudaStream_t s);
 int mlw2d_df_tile_count();
+// The 3-D mlw_m step in the double-float policy (mlw3d_df.cu).
+cudaError_t launch_mlw3d_df(int tile, const double *A, double *B, int ix, int jx, int kx,
+                            const Axis &ax, const Axis &ay, const Axis &az, const Phys &ph,
+                            double dt, Ctl *ctl, Box3 box, cudaStream_t s);
+int mlw3d_df_tile_count();
 // The mlw_m3 step (no control block) with the artificial viscosity's branch
 // recorded (mode 1) into, or held at (mode 2) the bytes of, avb: 2*ix*jx
 // bytes, x faces then y faces.  Mode 2 adds to *nflip the faces whose own

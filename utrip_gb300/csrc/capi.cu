@@ -1498,7 +1498,7 @@ int layout2d(const cans_run *h) {
 }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
-  if (h->df) return mlw2d_df_tile_count();
+  if (h->df) return h->ndim == 3 ? mlw3d_df_tile_count() : mlw2d_df_tile_count();
   if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
   if (h->eta) return h->ndim == 3 ? mlw3d_tile_count() : 1;
   if (h->grav) return h->ndim == 3 ? mlw3d_g_tile_count() : mlw2d_g_tile_count();
@@ -1552,6 +1552,9 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (h->ndim == 3 && h->grav)
     return launch_mlw3d_g(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx, h->ax.a,
                           h->ay.a, h->az.a, h->ph, h->grav, dt, ctl, box, h->s);
+  if (h->ndim == 3 && h->df)
+    return launch_mlw3d_df(tile, A, B, h->d.ix, h->d.jx, h->d.kx, h->ax.a, h->ay.a, h->az.a,
+                           h->ph, dt, ctl, box, h->s);
   if (h->ndim == 3)
     return launch_mlw3d(h->d.exact != 0, tile, A, B, h->d.ix, h->d.jx, h->d.kx,
                         h->ax.a, h->ay.a, h->az.a, h->ph, dt, ctl, box, h->s);
@@ -2007,7 +2010,8 @@ extern "C" int cans_run_set_tile(cans_run *h, int tile) {
 
 extern "C" int cans_run_set_df64(cans_run *h, int on) {
   if (!h) return CANS_ERR_ARG;
-  if (on && (h->d.solver != CANS_SOLVER_MLW_M3_2D || h->d.exact || h->grav || h->eta))
+  if (on && ((h->d.solver != CANS_SOLVER_MLW_M3_2D && h->d.solver != CANS_SOLVER_MLW_M_3D) ||
+             h->d.exact || h->grav || h->eta))
     return CANS_ERR_ARG;
   if (h->df != (on != 0)) {
     if (h->s) cudaStreamSynchronize(h->s);
