@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
                             "gravity2d", "resistive2d", "gravity3d", "resistive3d",
-                            "spicule"],
+                            "spicule", "single", "mlw2d_df", "mlw3d_df"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
@@ -98,6 +98,30 @@ def profile_case(case, n):
         run.push(s["state"])
         run.start(nstop=3, safety=s["safety"], dtmin=s["dtmin"])
         run.advance(3)
+        st = run.query()
+        run.close()
+        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+    elif case == "single":
+        # the one-at-a-time baseline of the beta sweep: 5 plain-launch
+        # iterations of a 128^2 and then of a 384^2 shear layer
+        out = {"case": case}
+        for m in (128, 384):
+            s = setups.shear_layer(m, beta=1.0, seed=4)
+            run = drivers.make_run(s)
+            run.set_graph(False)
+            run.push(s["state"])
+            run.start(nstop=5, safety=0.4, dtmin=1e-10)
+            run.advance(5)
+            out[str(m)] = int(run.query().nexec)
+            run.close()
+    elif case in ("mlw2d_df", "mlw3d_df"):
+        # the double-float steps: 4 iterations of the vortex (n^2, y-marching
+        # tile) or of the turbulence box (n^3)
+        s = setups.orszag_tang(n) if case == "mlw2d_df" else setups.turbulence_3d(n)
+        run = drivers.make_run(s, df64=True, tile=4 if case == "mlw2d_df" else 0)
+        run.push(s["state"])
+        run.start(nstop=4, safety=s["safety"], dtmin=1e-10)
+        run.advance(4)
         st = run.query()
         run.close()
         out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
