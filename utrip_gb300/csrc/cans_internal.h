@@ -164,14 +164,14 @@ cudaError_t launch_roe3d(bool exact, const double *A, double *B,
                          double *scratch, int ix, int jx, int kx,
                          const Axis &ax, const Axis &ay, const Axis &az,
                          const Phys &ph, double dt, Ctl *ctl, Box3 box,
-                         cudaStream_t s);
+                         cudaStream_t s, bool df = false);
 
 // 2-D roe_m3 (9 arrays ro,pr,vx,vy,vz,bx,by,bz,az of ix*jx); A -> B, cells
 // outside 3..n-2 copied; scratch of roe3d_scratch_doubles(ix*jx).
 cudaError_t launch_roe2d(bool exact, const double *A, double *B,
                          double *scratch, int ix, int jx, const Axis &ax,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
-                         Box3 box, cudaStream_t s);
+                         Box3 box, cudaStream_t s, bool df = false);
 
 // 1-D roe_m (5 arrays ro,pr,vx,vy,by of ix; bx, bxm, dx device arrays);
 // A -> B, cells outside 3..ix-2 copied; scratch of roe1d_scratch_doubles(ix).

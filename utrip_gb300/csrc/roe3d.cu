@@ -135,10 +135,13 @@ __device__ __forceinline__ size_t stride(const Geo &g, int a) {
 }
 
 // 3-D: roeflux_m.f; 2-D: roeflux_m3.f (alphs without the fix)
-template <bool E, int ND>
+// QF: the fast flux in double-float (the double-float policy; the update
+// kernels stay FP64)
+template <bool E, int ND, bool QF = false>
 __device__ __forceinline__ void roe_flux(const RoeK &K, const double *L,
                                          const double *R, double *f) {
   if constexpr (E) roe_flux_ref<true, ND == 3>(K, L, R, f);
+  else if constexpr (QF) roe_flux_df<ND == 3>(K, L, R, f);
   else roe_flux_fast<ND == 3>(K, L, R, f);
 }
 
@@ -230,7 +233,7 @@ __device__ __forceinline__ void axis_h(const Axis &ax, const Axis &ay,
 
 // ---- predictor --------------------------------------------------------------
 
-template <bool E, int ND>
+template <bool E, int ND, bool QF = false>
 __global__ void __launch_bounds__(kRoeThreads)
     k_roe_flux1(const double *__restrict__ A, double *__restrict__ Fl, Geo g,
                 RoeK K, const Ctl *ctl) {
@@ -256,7 +259,7 @@ __global__ void __launch_bounds__(kRoeThreads)
     for (int v = 0; v < 8; v++) p1[v] = __ldg(A + v * g.n + c + st);
     to_frame<ND>(a, p0, L);
     to_frame<ND>(a, p1, R);
-    roe_flux<E, ND>(K, L, R, f);
+    roe_flux<E, ND, QF>(K, L, R, f);
     store_flux<ND>(Fl + (size_t)a * 8 * g.n, g.n, c, a, f);
   }
 }
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(kRoeThreads)
 
 // ---- corrector --------------------------------------------------------------
 
-template <bool E, int ND>
+template <bool E, int ND, bool QF = false>
 __global__ void __launch_bounds__(kRoeThreads)
     k_roe_flux2(const double *__restrict__ H, double *__restrict__ Fl, Geo g,
                 RoeK K, const Ctl *ctl) {
@@ -331,7 +334,7 @@ __global__ void __launch_bounds__(kRoeThreads)
     }
     to_frame<ND>(a, wl, L);
     to_frame<ND>(a, wr, R);
-    roe_flux<E, ND>(K, L, R, f);
+    roe_flux<E, ND, QF>(K, L, R, f);
     store_flux<ND>(Fl + (size_t)a * 8 * g.n, g.n, c, a, f);
   }
 }
@@ -419,16 +422,16 @@ __global__ void __launch_bounds__(kRoeThreads)
   }
 }
 
-template <bool E, int ND>
+template <bool E, int ND, bool QF = false>
 cudaError_t launch_all(const double *A, double *B, double *scratch, const Geo &g,
                        const Axis &ax, const Axis &ay, const Axis &az,
                        const RoeK &K, const Phys &ph, double dt, Ctl *ctl,
                        Box3 box, cudaStream_t s) {
   const unsigned blocks = (unsigned)((g.n + kRoeThreads - 1) / kRoeThreads);
   double *H = scratch, *Fl = scratch + 8 * g.n;
-  k_roe_flux1<E, ND><<<blocks, kRoeThreads, 0, s>>>(A, Fl, g, K, ctl);
+  k_roe_flux1<E, ND, QF><<<blocks, kRoeThreads, 0, s>>>(A, Fl, g, K, ctl);
   k_roe_half<E, ND><<<blocks, kRoeThreads, 0, s>>>(A, Fl, H, g, ax, ay, az, K, dt, ctl);
-  k_roe_flux2<E, ND><<<blocks, kRoeThreads, 0, s>>>(H, Fl, g, K, ctl);
+  k_roe_flux2<E, ND, QF><<<blocks, kRoeThreads, 0, s>>>(H, Fl, g, K, ctl);
   k_roe_full<E, ND><<<blocks, kRoeThreads, 0, s>>>(A, Fl, H, B, g, ax, ay, az, K, ph,
                                                    dt, ctl, box);
   count_launch(4);
@@ -460,7 +463,7 @@ size_t roe3d_scratch_doubles(size_t ncells) { return 32 * ncells; }
 cudaError_t launch_roe3d(bool exact, const double *A, double *B, double *scratch,
                          int ix, int jx, int kx, const Axis &ax, const Axis &ay,
                          const Axis &az, const Phys &ph, double dt, Ctl *ctl,
-                         Box3 box, cudaStream_t s) {
+                         Box3 box, cudaStream_t s, bool df) {
   Geo g{};
   g.n3[0] = ix;
   g.n3[1] = jx;
@@ -470,6 +473,8 @@ cudaError_t launch_roe3d(bool exact, const double *A, double *B, double *scratch
   g.st[2] = (size_t)ix * jx;
   g.n = g.st[2] * kx;
   const RoeK K = make_roek(ph.gm);
+  if (df && !exact)
+    return launch_all<false, 3, true>(A, B, scratch, g, ax, ay, az, K, ph, dt, ctl, box, s);
   return exact ? launch_all<true, 3>(A, B, scratch, g, ax, ay, az, K, ph, dt, ctl, box, s)
                : launch_all<false, 3>(A, B, scratch, g, ax, ay, az, K, ph, dt, ctl, box, s);
 }
@@ -477,7 +482,7 @@ cudaError_t launch_roe3d(bool exact, const double *A, double *B, double *scratch
 cudaError_t launch_roe2d(bool exact, const double *A, double *B, double *scratch,
                          int ix, int jx, const Axis &ax, const Axis &ay,
                          const Phys &ph, double dt, Ctl *ctl, Box3 box,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool df) {
   Geo g{};
   g.n3[0] = ix;
   g.n3[1] = jx;
@@ -488,6 +493,8 @@ cudaError_t launch_roe2d(bool exact, const double *A, double *B, double *scratch
   g.n = g.st[2];
   const RoeK K = make_roek(ph.gm);
   const Axis none{};
+  if (df && !exact)
+    return launch_all<false, 2, true>(A, B, scratch, g, ax, ay, none, K, ph, dt, ctl, box, s);
   return exact ? launch_all<true, 2>(A, B, scratch, g, ax, ay, none, K, ph, dt, ctl, box, s)
                : launch_all<false, 2>(A, B, scratch, g, ax, ay, none, K, ph, dt, ctl, box, s);
 }

@@ -19,6 +19,7 @@
 // algebra with one reciprocal per repeated divisor and FMA contraction.
 #pragma once
 #include "cans_common.cuh"
+#include "df64.cuh"
 
 namespace cans {
 
@@ -242,129 +243,187 @@ __device__ __forceinline__ double sqrt_(double x) {
   return x == 0.0 ? 0.0 : x * rsq_(x);
 }
 __device__ __forceinline__ double max_(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double sign1_(double x) { return copysign(1.0, x); }
+__device__ __forceinline__ bool ge0_(double x) { return x >= 0.0; }
 
-template <bool FIX = true>
-__device__ __forceinline__ void roe_flux_fast(const RoeK &K, const double *L,
-                                              const double *R, double *f) {
-  const double rl = L[0], pl = L[1], ul = L[2], vl = L[3], wl = L[4];
-  const double bxl = L[5], byl = L[6], bzl = L[7];
-  const double rr = R[0], pr = R[1], ur = R[2], vr = R[3], wr = R[4];
-  const double bxr = R[5], byr = R[6], bzr = R[7];
-  const double pi4i = K.pi4i, pi8i = K.pi8i;
+// The same helpers in double-float (df64.cuh): the reciprocal square root is
+// one Newton step on the correctly rounded float one, with x r^2 formed in
+// double-float (about 2^-46).
+__device__ __forceinline__ df::DF rcp_(df::DF x) { return df::DF(df::rcp(x.d)); }
+__device__ __forceinline__ df::DF rsq_(df::DF x) {
+  const float r = __frsqrt_rn(x.d.h);
+  const df::D q = df::mulf(df::mulf(x.d, r), r);
+  const float e = __fsub_rn(__fsub_rn(1.0f, q.h), q.l);  // 1 - q.h is exact
+  return df::DF(df::fast_two_sum(r, __fmul_rn(__fmul_rn(0.5f, r), e)));
+}
+__device__ __forceinline__ df::DF sqrt_(df::DF x) {
+  return x.d.h == 0.0f ? df::DF(0.0f) : x * rsq_(x);
+}
+__device__ __forceinline__ df::DF max_(df::DF a, df::DF b) { return df::gt(a.d, b.d) ? a : b; }
+__device__ __forceinline__ df::DF sign1_(df::DF x) {
+  return df::DF(copysignf(1.0f, x.d.h));
+}
+__device__ __forceinline__ bool ge0_(df::DF x) { return !(x.d.h < 0.0f); }
+
+// The constants of the fast flux in its number type.
+template <class R> struct RoeKR {
+  R gm1, gm2, gm21, pi4i, pi8i, sqh, gm1i, ggm1, sq4pi, sq4pii, eps12;
+};
+template <class R> __device__ __forceinline__ RoeKR<R> roe_k(const RoeK &K) {
+  return {num_in<R>(K.gm1),  num_in<R>(K.gm2),  num_in<R>(K.gm21),  num_in<R>(K.pi4i),
+          num_in<R>(K.pi8i), num_in<R>(K.sqh),  num_in<R>(K.gm1i),  num_in<R>(K.ggm1),
+          num_in<R>(K.sq4pi), num_in<R>(K.sq4pii), num_in<R>(1.0e-12)};
+}
+
+// The fast flux, written once for a number type R (double: the fast policy;
+// df::DF: the double-float policy).  Literal constants are floats: exact in
+// both types.
+template <class R, bool FIX>
+__device__ __forceinline__ void roe_flux_fast_r(const RoeKR<R> &K, const R *L, const R *Rs,
+                                                R *f) {
+  const R rl = L[0], pl = L[1], ul = L[2], vl = L[3], wl = L[4];
+  const R bxl = L[5], byl = L[6], bzl = L[7];
+  const R rr = Rs[0], pr = Rs[1], ur = Rs[2], vr = Rs[3], wr = Rs[4];
+  const R bxr = Rs[5], byr = Rs[6], bzr = Rs[7];
+  const R pi4i = K.pi4i, pi8i = K.pi8i;
+  const R one(1.0f), half(0.5f), zero(0.0f);
   // Roe averages
-  const double q0 = rsq_(rl), q1 = rsq_(rr);
-  const double sr0 = rl * q0, sr1 = rr * q1;
-  const double irl = q0 * q0, irr = q1 * q1;
-  const double sri = rcp_(sr0 + sr1);
-  const double rhobar = sr0 * sr1, irb = q0 * q1;
-  const double w0 = sr0 * sri, w1 = sr1 * sri;
-  const double ub = fma(w0, ul, w1 * ur), vb = fma(w0, vl, w1 * vr),
-               wb = fma(w0, wl, w1 * wr);
-  const double bxb = fma(w0, bxr, w1 * bxl), byb = fma(w0, byr, w1 * byl),
-               bzb = fma(w0, bzr, w1 * bzl);
-  const double bx2 = bxb * bxb;
-  const double btl = fma(byl, byl, bzl * bzl), btr = fma(byr, byr, bzr * bzr);
-  const double v2l = fma(ul, ul, fma(vl, vl, wl * wl));
-  const double v2r = fma(ur, ur, fma(vr, vr, wr * wr));
-  const double hl = fma(0.5, v2l, irl * fma(K.ggm1, pl, pi4i * (bx2 + btl)));
-  const double hr = fma(0.5, v2r, irr * fma(K.ggm1, pr, pi4i * (bx2 + btr)));
-  const double hbar = fma(w0, hl, w1 * hr);
-  const double dby = byr - byl, dbz = bzr - bzl;
-  const double byave = 0.5 * (byl + byr), bzave = 0.5 * (bzl + bzr);
-  const double delb2 = K.gm21 * fma(dby, dby, dbz * dbz) * (sri * sri) * pi8i;
-  const double vb2 = fma(ub, ub, fma(vb, vb, wb * wb));
-  const double bt2 = fma(byb, byb, bzb * bzb);
-  const double pib = pi4i * irb;
-  const double bbr = (bx2 + bt2) * pib;
-  const double hv = fma(0.5, vb2, delb2);
-  const double qh = hbar - hv;
-  const double cs2 = K.gm1 * (qh - bbr);
-  const double astar2 = fma(K.gm1, qh, -K.gm2 * bbr);
-  const double ca2 = bx2 * pib, cbr2 = bt2 * pib;
-  const double dcs = cs2 - ca2;
-  const double cfast2 = 0.5 * (astar2 + sqrt_(fma(cbr2, astar2 + cs2 + ca2, dcs * dcs)));
-  const double rcf = rsq_(cfast2);
-  const double cfast = cfast2 * rcf;
-  const double rrb = rsq_(rhobar);
-  const double cs = sqrt_(cs2);
-  const double ca = fabs(bxb) * K.sq4pii * rrb;
-  const double cslow2 = cs2 * ca2 * (rcf * rcf);
-  const double cslow = cs * ca * rcf;
+  const R q0 = rsq_(rl), q1 = rsq_(rr);
+  const R sr0 = rl * q0, sr1 = rr * q1;
+  const R irl = q0 * q0, irr = q1 * q1;
+  const R sri = rcp_(sr0 + sr1);
+  const R rhobar = sr0 * sr1, irb = q0 * q1;
+  const R w0 = sr0 * sri, w1 = sr1 * sri;
+  const R ub = fma(w0, ul, w1 * ur), vb = fma(w0, vl, w1 * vr), wb = fma(w0, wl, w1 * wr);
+  const R bxb = fma(w0, bxr, w1 * bxl), byb = fma(w0, byr, w1 * byl),
+          bzb = fma(w0, bzr, w1 * bzl);
+  const R bx2 = bxb * bxb;
+  const R btl = fma(byl, byl, bzl * bzl), btr = fma(byr, byr, bzr * bzr);
+  const R v2l = fma(ul, ul, fma(vl, vl, wl * wl));
+  const R v2r = fma(ur, ur, fma(vr, vr, wr * wr));
+  const R hl = fma(half, v2l, irl * fma(K.ggm1, pl, pi4i * (bx2 + btl)));
+  const R hr = fma(half, v2r, irr * fma(K.ggm1, pr, pi4i * (bx2 + btr)));
+  const R hbar = fma(w0, hl, w1 * hr);
+  const R dby = byr - byl, dbz = bzr - bzl;
+  const R byave = half * (byl + byr), bzave = half * (bzl + bzr);
+  const R delb2 = K.gm21 * fma(dby, dby, dbz * dbz) * (sri * sri) * pi8i;
+  const R vb2 = fma(ub, ub, fma(vb, vb, wb * wb));
+  const R bt2 = fma(byb, byb, bzb * bzb);
+  const R pib = pi4i * irb;
+  const R bbr = (bx2 + bt2) * pib;
+  const R hv = fma(half, vb2, delb2);
+  const R qh = hbar - hv;
+  const R cs2 = K.gm1 * (qh - bbr);
+  const R astar2 = fma(K.gm1, qh, -K.gm2 * bbr);
+  const R ca2 = bx2 * pib, cbr2 = bt2 * pib;
+  const R dcs = cs2 - ca2;
+  const R cfast2 = half * (astar2 + sqrt_(fma(cbr2, astar2 + cs2 + ca2, dcs * dcs)));
+  const R rcf = rsq_(cfast2);
+  const R cfast = cfast2 * rcf;
+  const R rrb = rsq_(rhobar);
+  const R cs = sqrt_(cs2);
+  const R ca = fabs(bxb) * K.sq4pii * rrb;
+  const R cslow2 = cs2 * ca2 * (rcf * rcf);
+  const R cslow = cs * ca * rcf;
   // singular points
-  const double sp = (bt2 - 1.0e-12 >= 0.0) ? 1.0 : 0.0;
-  const double rbt = rsq_(bt2 + 1.0 - sp);
-  const double betay = sp != 0.0 ? byb * rbt : K.sqh;
-  const double betaz = sp != 0.0 ? bzb * rbt : K.sqh;
-  const double sp2 = (fma(bt2, pib, fabs(ca2 - cs2)) - 1.0e-12 >= 0.0) ? 1.0 : 0.0;
-  const double cfca = max_(0.0, cfast2 - ca2);
-  const double cfcs = max_(0.0, cfast2 - cslow2);
-  const double cfa = max_(0.0, cfast2 - cs2);
-  const double rden = rsq_(cfcs + 1.0 - sp2);
-  const double alphf = sp2 * (sqrt_(cfca) * rden) + 1.0 - sp2;
-  const double alphs = FIX ? sp2 * (sqrt_(cfa) * rden) + 1.0 - sp2 : sp2 * (sqrt_(cfa) * rden);
-  const double sg = copysign(1.0, bxb);
+  const bool spb = ge0_(bt2 - K.eps12);
+  const R sp = spb ? one : zero;
+  const R rbt = rsq_(bt2 + one - sp);
+  const R betay = spb ? byb * rbt : K.sqh;
+  const R betaz = spb ? bzb * rbt : K.sqh;
+  const bool sp2b = ge0_(fma(bt2, pib, fabs(ca2 - cs2)) - K.eps12);
+  const R sp2 = sp2b ? one : zero;
+  const R cfca = max_(zero, cfast2 - ca2);
+  const R cfcs = max_(zero, cfast2 - cslow2);
+  const R cfa = max_(zero, cfast2 - cs2);
+  const R rden = rsq_(cfcs + one - sp2);
+  const R alphf = sp2 * (sqrt_(cfca) * rden) + one - sp2;
+  const R alphs = FIX ? sp2 * (sqrt_(cfa) * rden) + one - sp2 : sp2 * (sqrt_(cfa) * rden);
+  const R sg = sign1_(bxb);
   // eigenvalues with the entropy floor
-  const double du = ur - ul;
-  const double eeps = 0.5 * max_(du, 0.0);
-  const double elpf = -max_(fabs(ub + cfast), eeps), elmf = -max_(fabs(ub - cfast), eeps);
-  const double elps = -max_(fabs(ub + cslow), eeps), elms = -max_(fabs(ub - cslow), eeps);
-  const double elpa = -max_(fabs(ub + ca), eeps), elma = -max_(fabs(ub - ca), eeps);
-  const double elze = -max_(fabs(ub), eeps);
+  const R du = ur - ul;
+  const R eeps = half * max_(du, zero);
+  const R elpf = -max_(fabs(ub + cfast), eeps), elmf = -max_(fabs(ub - cfast), eeps);
+  const R elps = -max_(fabs(ub + cslow), eeps), elms = -max_(fabs(ub - cslow), eeps);
+  const R elpa = -max_(fabs(ub + ca), eeps), elma = -max_(fabs(ub - ca), eeps);
+  const R elze = -max_(fabs(ub), eeps);
   // wave amplitudes
-  const double t1 = fma(betay, dby, betaz * dbz);
-  const double t2 = (pr - pl + pi4i * fma(byave, dby, bzave * dbz) +
-                     K.gm2 * pi4i * fma(byb, dby, bzb * dbz)) * K.gm1i;
-  const double t3 = fma(betaz, dby, -betay * dbz);
-  const double s1 = rhobar * du;
-  const double dv = rhobar * (vr - vl), dw = rhobar * (wr - wl);
-  const double s2 = fma(betay, dv, betaz * dw), s3 = fma(betaz, dv, -betay * dw);
-  const double sq4r = K.sq4pi * rrb;
-  const double sqr4 = K.sq4pii * rhobar * rrb;
-  const double cg = cs2 * K.gm21;
-  const double p11 = alphs * cfast * sq4r, p12 = -alphf * cs2 * rcf * sq4r;
-  const double p21 = alphf * (cfast2 - cg), p22 = alphs * (cslow2 - cg);
-  const double q11 = alphf * cfast, q12 = alphs * cslow;
-  const double q21 = -alphs * ca * sg, q22 = alphf * cs * sg;
-  const double rdp = rcp_(fma(p11, p22, -p12 * p21));
-  const double rdq = rcp_(fma(q11, q22, -q12 * q21));
-  const double ap = fma(p22, t1, -p12 * t2) * rdp, aq = fma(q22, s1, -q12 * s2) * rdq;
-  const double bp = fma(p11, t2, -p21 * t1) * rdp, bq = fma(q11, s2, -q21 * s1) * rdq;
-  const double PF = elpf * 0.5 * (ap + aq), MF = elmf * 0.5 * (ap - aq);
-  const double PS = elps * 0.5 * (bp + bq), MS = elms * 0.5 * (bp - bq);
-  const double PA = elpa * 0.5 * fma(sqr4, t3, -sg * s3);
-  const double MA = elma * 0.5 * fma(sqr4, t3, sg * s3);
-  const double ZE = elze * (rr - rl - alphf * ap - alphs * bp);
+  const R t1 = fma(betay, dby, betaz * dbz);
+  const R t2 = (pr - pl + pi4i * fma(byave, dby, bzave * dbz) +
+                K.gm2 * pi4i * fma(byb, dby, bzb * dbz)) * K.gm1i;
+  const R t3 = fma(betaz, dby, -betay * dbz);
+  const R s1 = rhobar * du;
+  const R dv = rhobar * (vr - vl), dw = rhobar * (wr - wl);
+  const R s2 = fma(betay, dv, betaz * dw), s3 = fma(betaz, dv, -betay * dw);
+  const R sq4r = K.sq4pi * rrb;
+  const R sqr4 = K.sq4pii * rhobar * rrb;
+  const R cg = cs2 * K.gm21;
+  const R p11 = alphs * cfast * sq4r, p12 = -alphf * cs2 * rcf * sq4r;
+  const R p21 = alphf * (cfast2 - cg), p22 = alphs * (cslow2 - cg);
+  const R q11 = alphf * cfast, q12 = alphs * cslow;
+  const R q21 = -alphs * ca * sg, q22 = alphf * cs * sg;
+  const R rdp = rcp_(fma(p11, p22, -p12 * p21));
+  const R rdq = rcp_(fma(q11, q22, -q12 * q21));
+  const R ap = fma(p22, t1, -p12 * t2) * rdp, aq = fma(q22, s1, -q12 * s2) * rdq;
+  const R bp = fma(p11, t2, -p21 * t1) * rdp, bq = fma(q11, s2, -q21 * s1) * rdq;
+  const R PF = elpf * half * (ap + aq), MF = elmf * half * (ap - aq);
+  const R PS = elps * half * (bp + bq), MS = elms * half * (bp - bq);
+  const R PA = elpa * half * fma(sqr4, t3, -sg * s3);
+  const R MA = elma * half * fma(sqr4, t3, sg * s3);
+  const R ZE = elze * (rr - rl - alphf * ap - alphs * bp);
   // wave-pair sums
-  const double fS = PF + MF, fD = PF - MF, sS = PS + MS, sD = PS - MS;
-  const double aS = PA + MA, aD = PA - MA;
-  const double dro = fma(alphf, fS, fma(alphs, sS, ZE));
-  const double tcf = fma(-alphs * ca, fD, alphf * cs * sD) * sg;  // shared by ry, rz
-  const double tb = sq4r * fma(alphs * cfast, fS, -cs2 * rcf * alphf * sS);
-  const double bv = fma(betay, vb, betaz * wb);
-  const double cfg = fma(cfast2 - cs2, K.gm2, cfast2) * K.gm1i;
-  const double csg = fma(cslow2 - cs2, K.gm2, cslow2) * K.gm1i;
-  const double dee =
+  const R fS = PF + MF, fD = PF - MF, sS = PS + MS, sD = PS - MS;
+  const R aS = PA + MA, aD = PA - MA;
+  const R dro = fma(alphf, fS, fma(alphs, sS, ZE));
+  const R tcf = fma(-alphs * ca, fD, alphf * cs * sD) * sg;  // shared by ry, rz
+  const R tb = sq4r * fma(alphs * cfast, fS, -cs2 * rcf * alphf * sS);
+  const R bv = fma(betay, vb, betaz * wb);
+  const R cfg = fma(cfast2 - cs2, K.gm2, cfast2) * K.gm1i;
+  const R csg = fma(cslow2 - cs2, K.gm2, cslow2) * K.gm1i;
+  const R dee =
       alphf * fma(hv + cfg, fS, cfast * ub * fD) + alphs * fma(hv + csg, sS, cslow * ub * sD) +
       bv * sg * fma(-alphs * ca, fD, alphf * cs * sD) -
       fma(betaz, vb, -betay * wb) * sg * aD + hv * ZE;
   // physical fluxes of both sides
-  const double ml = rl * ul, mr = rr * ur;
-  const double fro = ml + mr;
-  const double frx = fma(ml, ul, pl) + fma(mr, ur, pr) + (btl + btr - 2.0 * bx2) * pi8i;
-  const double fry = fma(ml, vl, mr * vr) - bxb * (byl + byr) * pi4i;
-  const double frz = fma(ml, wl, mr * wr) - bxb * (bzl + bzr) * pi4i;
-  const double fby = fma(ul, byl, -vl * bxb) + fma(ur, byr, -vr * bxb);
-  const double fbz = fma(ul, bzl, -wl * bxb) + fma(ur, bzr, -wr * bxb);
-  const double fee = fma(ml, hl, mr * hr) -
-                     bxb * pi4i * (fma(bxb, ul, fma(byl, vl, bzl * wl)) +
-                                   fma(bxb, ur, fma(byr, vr, bzr * wr)));
-  f[0] = 0.5 * (fro + dro);
-  f[1] = 0.5 * (fee + dee);
-  f[2] = 0.5 * (frx + fma(ub, dro, fma(alphf * cfast, fD, alphs * cslow * sD)));
-  f[3] = 0.5 * (fry + fma(vb, dro, fma(betay, tcf, -sg * betaz * aD)));
-  f[4] = 0.5 * (frz + fma(wb, dro, fma(betaz, tcf, sg * betay * aD)));
-  f[5] = 0.5 * (fby + fma(betay, tb, sq4r * betaz * aS));
-  f[6] = 0.5 * (fbz + fma(betaz, tb, -sq4r * betay * aS));
+  const R ml = rl * ul, mr = rr * ur;
+  const R fro = ml + mr;
+  const R frx = fma(ml, ul, pl) + fma(mr, ur, pr) + (btl + btr - 2.0f * bx2) * pi8i;
+  const R fry = fma(ml, vl, mr * vr) - bxb * (byl + byr) * pi4i;
+  const R frz = fma(ml, wl, mr * wr) - bxb * (bzl + bzr) * pi4i;
+  const R fby = fma(ul, byl, -vl * bxb) + fma(ur, byr, -vr * bxb);
+  const R fbz = fma(ul, bzl, -wl * bxb) + fma(ur, bzr, -wr * bxb);
+  const R fee = fma(ml, hl, mr * hr) -
+                bxb * pi4i * (fma(bxb, ul, fma(byl, vl, bzl * wl)) +
+                              fma(bxb, ur, fma(byr, vr, bzr * wr)));
+  f[0] = half * (fro + dro);
+  f[1] = half * (fee + dee);
+  f[2] = half * (frx + fma(ub, dro, fma(alphf * cfast, fD, alphs * cslow * sD)));
+  f[3] = half * (fry + fma(vb, dro, fma(betay, tcf, -sg * betaz * aD)));
+  f[4] = half * (frz + fma(wb, dro, fma(betaz, tcf, sg * betay * aD)));
+  f[5] = half * (fby + fma(betay, tb, sq4r * betaz * aS));
+  f[6] = half * (fbz + fma(betaz, tb, -sq4r * betay * aS));
+}
+
+template <bool FIX = true>
+__device__ __forceinline__ void roe_flux_fast(const RoeK &K, const double *L,
+                                              const double *R, double *f) {
+  roe_flux_fast_r<double, FIX>(roe_k<double>(K), L, R, f);
+}
+
+// The double-float policy: the fast flux on the FP32 pipes, states and
+// fluxes converted once.
+template <bool FIX = true>
+__device__ __forceinline__ void roe_flux_df(const RoeK &K, const double *L,
+                                            const double *R, double *f) {
+  df::DF l[8], r[8], o[7];
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    l[v] = num_in<df::DF>(L[v]);
+    r[v] = num_in<df::DF>(R[v]);
+  }
+  roe_flux_fast_r<df::DF, FIX>(roe_k<df::DF>(K), l, r, o);
+#pragma unroll
+  for (int v = 0; v < 7; v++) f[v] = num_out(o[v]);
 }
 
 }  // namespace cans
