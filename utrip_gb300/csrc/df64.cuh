@@ -21,11 +21,12 @@
 // Every float operation is an explicitly rounded intrinsic, so nothing is
 // contracted or reassociated: the error-free transformations stay exact.
 //
-// Conversions from double split the 53-bit significand with integer
-// operations (no FP64 instruction): the head takes the top 24 bits, the tail
-// the remaining 29 rounded to 24, so the value is kept to 2^-48.  Values whose
-// tail would leave the float range (|x| < 2^-74) or that overflow float take a
-// slower path through the FP64 converter; zero is exact.
+// Conversions between double and double-float use integer operations only
+// (on GB300 a double <-> float conversion instruction runs at the FP64 rate):
+// the head takes the top 24 significand bits, the tail the remaining 29
+// rounded to 24, so the value is kept to 2^-48 for 2^-74 <= |x| < 2^128.
+// Outside that range the tail is dropped down to 2^-126, smaller values
+// flush to zero, larger ones are infinite.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -111,37 +112,42 @@ __device__ __forceinline__ bool pos(D x) { return x.h > 0.0f; }
 __device__ __forceinline__ bool gt(D a, D b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
 __device__ __forceinline__ D absd(D x) { return x.h < 0.0f ? neg(x) : x; }
 
-// double -> double-float (see the file comment)
+// double -> double-float (see the file comment), with integer operations
+// only: a head whose exponent fits a float (2^-126 <= |x| < 2^128) keeps the
+// top 24 significand bits; the tail, the low 29 bits rounded to 24, is kept
+// while it is a normal float (|x| >= 2^-74) and dropped below; smaller
+// values flush to zero, larger ones become infinities, and NaN stays NaN.
 __device__ __forceinline__ D from_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
   const int e = (int)((hi >> 20) & 0x7ffu);
   const unsigned sgn = hi & 0x80000000u;
-  if (e >= 949 && e <= 1150) {
-    // head: top 24 significand bits (the implicit one and 23 stored bits),
-    // truncated; exponent rebiased from 1023 to 127
-    const float h = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) |
-                                    ((hi & 0xfffffu) << 3) | (lo >> 29));
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 stored bits
+  if (e >= 897 && e <= 1150) {
+    const float h = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | mant);
+    if (e < 949) return {h, 0.0f};
     // tail: the low 29 bits times 2^(e - 1075), a normal float for e >= 949
     const float t = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu),
                               __uint_as_float((unsigned)(e - 948) << 23));
     return fast_two_sum(h, sgn ? -t : t);
   }
-  if (e == 0) return {__uint_as_float(sgn), 0.0f};  // zero (and subnormal doubles)
-  const float h = __double2float_rn(x);
-  return {h, __double2float_rn(x - (double)h)};
+  if (e < 897) return {__uint_as_float(sgn), 0.0f};
+  // overflow to infinity; NaN keeps a non-zero significand
+  const bool nan = e == 2047 && ((hi & 0xfffffu) | lo) != 0u;
+  return {__uint_as_float(sgn | 0x7f800000u | (nan ? 0x400000u : 0u)), 0.0f};
 }
 
 // double-float -> double, rounded once: the two floats are widened exactly
-// (integer operations for normal floats) and added in FP64
+// with integer operations (a subnormal float, below 2^-126, widens to zero)
+// and added in FP64
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned ef = (u >> 23) & 0xffu;
-  if (ef == 0u || ef == 0xffu) return (double)f;  // zero, subnormal, inf, NaN
-  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                  ((unsigned long long)(ef + 896u) << 52) |
-                                  ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned long long sg = (unsigned long long)(u & 0x80000000u) << 32;
+  if (ef == 0u) return __longlong_as_double((long long)sg);
+  const unsigned long long ed = ef == 0xffu ? 0x7ffull : (unsigned long long)(ef + 896u);
+  return __longlong_as_double(
+      (long long)(sg | (ed << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 __device__ __forceinline__ double to_double(D x) { return __dadd_rn(widen(x.h), widen(x.l)); }
 

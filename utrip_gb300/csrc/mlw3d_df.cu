@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(Tile3D<TX, TY>::NT, Tile3D<TX, TY>::MINB)
     const D cyk = df::scale(df::mul(dt, df::from_double(ay.dim[b])), 0.25f);
     const D czk = df::scale(df::mul(dt, df::from_double(az.dim[k])), 0.25f);
     D un[8];
-#pragma unroll
+#pragma unroll 1
     for (int v = 0; v < 8; v++) {
       const D *Lv = L + (size_t)v * T::NC, *Uv = U + (size_t)v * T::NC;
       D r = df::scale(df::add(df::add(df::add(Lv[p10], Lv[p00]), df::add(Lv[p11], Lv[p01])),
@@ -356,8 +356,10 @@ __global__ void __launch_bounds__(Tile3D<TX, TY>::NT, Tile3D<TX, TY>::MINB)
           ad = df::mul(dtz, df::mul(df::mul(df::mul(P.qav, df::from_double(az.dm[k - 1])), qd),
                                     df::from_double(az.dim[k - 1])));
       }
+      // the eight variables in a rolled loop: unrolled, the kernel's code
+      // outgrows the instruction cache (ncu: "no instruction" stalls)
       D du[8];
-#pragma unroll
+#pragma unroll 1
       for (int v = 0; v < 8; v++) {
         const D *Sv = S0 + (size_t)v * T::NC;
         const D u = Sv[c];
