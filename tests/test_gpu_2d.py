@@ -121,6 +121,9 @@ def test_literal_drop_in_loop_matches_oracle(gpu, oracle_lib):
 
 
 N_TILES_2D = 6  # 32x16, 32x8, 16x16, 64x8, 32x9 (one row per thread), 32x10
+# tile 6 is the y-marching kernel of the fast mlw_m3 step (the exact policy
+# takes the 32x9 tile in its place)
+MARCH_TILE = 6
 
 
 @pytest.mark.parametrize("solver", ["mlw_m3", "mlw_m"])
@@ -213,3 +216,44 @@ def test_oblique_shock_tube_to_tend_exact_bitwise(gpu, oracle_lib):
     assert out == (t, ns, merr, ns) and t >= 0.1
     for k, a, b in zip(s["names"], got, ref):
         assert np.array_equal(a, b), k
+
+
+@pytest.mark.parametrize("make,steps", [
+    (lambda: setups.orszag_tang(64), 100),
+    (lambda: setups.shear_layer(130, beta=0.5, seed=2), 100),
+    (lambda: setups.random_state(53, 41, seed=7), 20),
+])
+def test_fast_marching_tile_against_oracle(gpu, oracle_lib, make, steps):
+    """The y-marching tile of the fast policy (32-column strips taking their
+    rows in chunks, the symmetric momentum flux formed once) holds the fast
+    policy's 1e-10 against the oracle, ragged strips and segments included."""
+    s = make()
+    ref = setups.copy_state(s)
+    t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, steps)
+    got = setups.copy_state(s)
+    run = drivers.make_run(s, tile=MARCH_TILE)
+    try:
+        t, ns, merr, nexec = drivers.run_resident(s, got, steps, run=run)
+    finally:
+        run.close()
+    assert merr == 0 and ns == ns_ref and nexec == ns
+    for k, a, b in zip(s["names"], got, ref):
+        assert rel_linf(a, b) <= TOL_FAST, (k, rel_linf(a, b))
+
+
+def test_marching_tile_falls_back_for_exact_and_mlw_m(gpu, oracle_lib):
+    """Asked of the exact policy or of mlw_m, tile 6 runs the 32x9 tile: still
+    bit for bit."""
+    for solver in ("mlw_m3", "mlw_m"):
+        s = setups.random_state(70, 45, seed=9, solver=solver)
+        ref = setups.copy_state(s)
+        dt, _ = oracle.cfl_2d(s, ref, 0.4)
+        oracle.step_2d(s, ref, dt)
+        run = drivers.make_run(s, exact=True, tile=MARCH_TILE)
+        try:
+            run.push(setups.copy_state(s))
+            run.step(dt, apply_bc=False)
+            got = run.pull()
+        finally:
+            run.close()
+        assert_same(s["names"], got, ref, solver)

@@ -68,6 +68,11 @@ cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx
                             const Axis &ax, const Axis &ay, const Phys &ph, double dt,
                             Ctl *ctl, Box3 box, cudaStream_t s);
 int mlw2d_df_tile_count();
+// The fast policy's mlw_m3 step with the y-marching tile (the FP64 instance
+// of the marching kernel of mlw2d_df.cu).
+cudaError_t launch_mlw2d_march_fast(const double *A, double *B, int ix, int jx,
+                                    const Axis &ax, const Axis &ay, const Phys &ph, double dt,
+                                    Ctl *ctl, Box3 box, cudaStream_t s);
 // The 3-D mlw_m step in the double-float policy (mlw3d_df.cu).
 cudaError_t launch_mlw3d_df(int tile, const double *A, double *B, int ix, int jx, int kx,
                             const Axis &ax, const Axis &ay, const Axis &az, const Phys &ph,

@@ -106,13 +106,20 @@ cudaError_t launch_sel(int tile, const double *A, double *B, int ix, int jx,
 }
 }  // namespace
 
-int mlw2d_tile_count() { return 6; }
+// tile 6: the y-marching kernel of the fast mlw_m3 step (mlw2d_df.cu); the
+// exact policy and mlw_m take the 32 x 9 tile in its place
+int mlw2d_tile_count() { return 7; }
 
 cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
                          double *B, int ix, int jx, const Axis &ax,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
                          Box3 box, cudaStream_t s) {
   if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
+  if (tile == 6) {
+    if (solver == 1 && !exact)
+      return launch_mlw2d_march_fast(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    tile = 4;
+  }
   if (solver == 1) {
     return exact ? launch_sel<true, true>(tile, A, B, ix, jx, ax, ay, ph, dt, ctl, box, s)
                  : launch_sel<false, true>(tile, A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);

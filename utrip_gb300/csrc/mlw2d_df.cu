@@ -393,6 +393,69 @@ __device__ __forceinline__ void tile_step_df(const double *__restrict__ A,
 // block has 34 CH threads (rounded up to whole warps): one per cell of a
 // chunk's new rows (phase 1), one per corner (phase 2) and one per updated
 // cell (phase 3, 32 CH of them).
+// Number operations of the marching kernel, which is written once for
+// both: DFN, double-float on the FP32 pipes (the double-float policy), and
+// F64N, FP64 with FMA contraction (the fast policy).
+struct DFN {
+  using V = df::D;
+  static __device__ __forceinline__ V in(double x) { return df::from_double(x); }
+  static __device__ __forceinline__ double out(V x) { return df::to_double(x); }
+  static __device__ __forceinline__ V zero() { return df::mk(0.0f); }
+  static __device__ __forceinline__ V mad(V a, V b, V c) { return df::mad(a, b, c); }
+  static __device__ __forceinline__ V mul(V a, V b) { return df::mul(a, b); }
+  static __device__ __forceinline__ V add(V a, V b) { return df::add(a, b); }
+  static __device__ __forceinline__ V sub(V a, V b) { return df::sub(a, b); }
+  static __device__ __forceinline__ V neg(V a) { return df::neg(a); }
+  static __device__ __forceinline__ V scale(V a, float p2) { return df::scale(a, p2); }
+  static __device__ __forceinline__ V sqr(V a) { return df::sqr(a); }
+  static __device__ __forceinline__ V rcp(V a) { return df::rcp(a); }
+  static __device__ __forceinline__ V addf(V a, float b) { return df::addf(a, b); }
+  static __device__ __forceinline__ V absd(V a) { return df::absd(a); }
+  static __device__ __forceinline__ bool pos(V a) { return df::pos(a); }
+  static __device__ __forceinline__ bool gt(V a, V b) { return df::gt(a, b); }
+  static __device__ __forceinline__ bool isnan(V a) { return a.h != a.h; }
+  static __device__ __forceinline__ V nan_probe(V a) { return a; }
+  static __device__ __forceinline__ V warp_max(V v) { return warp_max_d(v); }
+};
+struct F64N {
+  using V = double;
+  static __device__ __forceinline__ V in(double x) { return x; }
+  static __device__ __forceinline__ double out(V x) { return x; }
+  static __device__ __forceinline__ V zero() { return 0.0; }
+  static __device__ __forceinline__ V mad(V a, V b, V c) { return fma(a, b, c); }
+  static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
+  static __device__ __forceinline__ V add(V a, V b) { return a + b; }
+  static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
+  static __device__ __forceinline__ V neg(V a) { return -a; }
+  static __device__ __forceinline__ V scale(V a, float p2) { return a * (double)p2; }
+  static __device__ __forceinline__ V sqr(V a) { return a * a; }
+  static __device__ __forceinline__ V rcp(V a) { return 1.0 / a; }
+  static __device__ __forceinline__ V addf(V a, float b) { return a + (double)b; }
+  static __device__ __forceinline__ V absd(V a) { return fabs(a); }
+  static __device__ __forceinline__ bool pos(V a) { return a > 0.0; }
+  static __device__ __forceinline__ bool gt(V a, V b) { return a > b; }
+  static __device__ __forceinline__ bool isnan(V a) { return a != a; }
+  // a float whose NaN-ness is the key's, for bad_cell_d
+  static __device__ __forceinline__ df::D nan_probe(V a) {
+    return {a != a ? __int_as_float(0x7fc00000) : 0.0f, 0.0f};
+  }
+  static __device__ __forceinline__ V warp_max(V v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double w = __shfl_xor_sync(0xffffffffu, v, o);
+      if (w > v || v != v) v = w;
+    }
+    return v;
+  }
+};
+template <class N> struct PhysN {
+  typename N::V gm, gm1, gm1i, ggm1, pi4i, pi8i, qav;
+};
+template <class N> __device__ __forceinline__ PhysN<N> phys_n(const Phys &ph) {
+  return {N::in(ph.gm),   N::in(ph.gm1),  N::in(ph.gm1i), N::in(ph.ggm1),
+          N::in(ph.pi4i), N::in(ph.pi8i), N::in(ph.qav)};
+}
+
 template <int CH>
 struct MarchD {
   static constexpr int TX = 32, CX = TX + 2, KX = TX + 1;
@@ -403,108 +466,112 @@ struct MarchD {
   // end take every lane of a warp
   static constexpr int NT = (CX * CH + 31) / 32 * 32;
   static constexpr size_t smem_bytes =
-      sizeof(D) * ((size_t)NCS * NC + (size_t)NKS * NK + NQX + NQY) + sizeof(double) * 32;
+      sizeof(double) * ((size_t)NCS * NC + (size_t)NKS * NK + NQX + NQY) + sizeof(double) * 32;
 };
 
 // Cell values of one cell (phase 1 of the tile).
-template <int NCc>
-__device__ __forceinline__ void cell_df(const double *__restrict__ A, size_t n, size_t g,
-                                        D *sc, int c, const PhysD &P) {
+template <class N, int NCc>
+__device__ __forceinline__ void cell_m(const double *__restrict__ A, size_t n, size_t g,
+                                        typename N::V *sc, int c, const PhysN<N> &P) {
+  using V = typename N::V;
 #define SC(s, c) sc[(size_t)(s) * NCc + (c)]
-  const D ro = df::from_double(A[PRO * n + g]), pr = df::from_double(A[PPR * n + g]);
-  const D vx = df::from_double(A[PVX * n + g]), vy = df::from_double(A[PVY * n + g]);
-  const D vz = df::from_double(A[PVZ * n + g]);
-  const D bx = df::from_double(A[PBX * n + g]), by = df::from_double(A[PBY * n + g]);
-  const D bz = df::from_double(A[PBZ * n + g]);
-  const D vv = df::mad(vz, vz, df::mad(vy, vy, df::sqr(vx)));
-  const D bb = df::mad(bz, bz, df::mad(by, by, df::sqr(bx)));
-  const D ek = df::mul(df::scale(ro, 0.5f), vv);
-  const D ee = df::mad(pr, P.gm1i, df::mad(P.pi8i, bb, ek));
-  const D ep = df::mad(pr, P.ggm1, ek);
-  const D rx = df::mul(ro, vx), ry = df::mul(ro, vy), rz = df::mul(ro, vz);
-  const D ex = df::mad(vz, by, df::neg(df::mul(vy, bz)));
-  const D ey = df::mad(vx, bz, df::neg(df::mul(vz, bx)));
-  const D ez = df::mad(vy, bx, df::neg(df::mul(vx, by)));
-  const D pt = df::mad(P.pi8i, bb, pr);
-  const D pbx = df::mul(P.pi4i, bx), pby = df::mul(P.pi4i, by);
+  const V ro = N::in(A[PRO * n + g]), pr = N::in(A[PPR * n + g]);
+  const V vx = N::in(A[PVX * n + g]), vy = N::in(A[PVY * n + g]);
+  const V vz = N::in(A[PVZ * n + g]);
+  const V bx = N::in(A[PBX * n + g]), by = N::in(A[PBY * n + g]);
+  const V bz = N::in(A[PBZ * n + g]);
+  const V vv = N::mad(vz, vz, N::mad(vy, vy, N::sqr(vx)));
+  const V bb = N::mad(bz, bz, N::mad(by, by, N::sqr(bx)));
+  const V ek = N::mul(N::scale(ro, 0.5f), vv);
+  const V ee = N::mad(pr, P.gm1i, N::mad(P.pi8i, bb, ek));
+  const V ep = N::mad(pr, P.ggm1, ek);
+  const V rx = N::mul(ro, vx), ry = N::mul(ro, vy), rz = N::mul(ro, vz);
+  const V ex = N::mad(vz, by, N::neg(N::mul(vy, bz)));
+  const V ey = N::mad(vx, bz, N::neg(N::mul(vz, bx)));
+  const V ez = N::mad(vy, bx, N::neg(N::mul(vx, by)));
+  const V pt = N::mad(P.pi8i, bb, pr);
+  const V pbx = N::mul(P.pi4i, bx), pby = N::mul(P.pi4i, by);
   SC(CRO, c) = ro; SC(CEE, c) = ee; SC(CRX, c) = rx; SC(CRY, c) = ry; SC(CRZ, c) = rz;
   SC(CBX, c) = bx; SC(CBY, c) = by; SC(CBZ, c) = bz;
   SC(CEX, c) = ex; SC(CEY, c) = ey; SC(CEZ, c) = ez; SC(CVX, c) = vx; SC(CVY, c) = vy;
-  SC(CFXE, c) = df::mad(df::mad(bz, ey, df::neg(df::mul(by, ez))), P.pi4i, df::mul(ep, vx));
-  SC(CFYE, c) = df::mad(df::mad(bx, ez, df::neg(df::mul(bz, ex))), P.pi4i, df::mul(ep, vy));
-  SC(CFXRX, c) = df::mad(rx, vx, df::mad(df::neg(pbx), bx, pt));
-  SC(CFYRY, c) = df::mad(ry, vy, df::mad(df::neg(pby), by, pt));
-  SC(CFXY, c) = df::mad(rx, vy, df::neg(df::mul(pbx, by)));
-  SC(CFXRZ, c) = df::mad(rz, vx, df::neg(df::mul(pbx, bz)));
-  SC(CFYRZ, c) = df::mad(rz, vy, df::neg(df::mul(pby, bz)));
+  SC(CFXE, c) = N::mad(N::mad(bz, ey, N::neg(N::mul(by, ez))), P.pi4i, N::mul(ep, vx));
+  SC(CFYE, c) = N::mad(N::mad(bx, ez, N::neg(N::mul(bz, ex))), P.pi4i, N::mul(ep, vy));
+  SC(CFXRX, c) = N::mad(rx, vx, N::mad(N::neg(pbx), bx, pt));
+  SC(CFYRY, c) = N::mad(ry, vy, N::mad(N::neg(pby), by, pt));
+  SC(CFXY, c) = N::mad(rx, vy, N::neg(N::mul(pbx, by)));
+  SC(CFXRZ, c) = N::mad(rz, vx, N::neg(N::mul(pbx, bz)));
+  SC(CFYRZ, c) = N::mad(rz, vy, N::neg(N::mul(pby, bz)));
 #undef SC
 }
 
 // Half-step values of one corner from its four cells a, b (x+1), cc (x+1,
 // y+1), d (y+1) (phase 2 of the tile).
-template <int NCc, int NKc>
-__device__ __forceinline__ void corner_df(const D *sc, D *sk, int a, int b, int cc, int d,
-                                          int k, D cxk, D cyk, const PhysD &P) {
+template <class N, int NCc, int NKc>
+__device__ __forceinline__ void corner_m(const typename N::V *sc, typename N::V *sk, int a,
+                                         int b, int cc, int d, int k, typename N::V cxk,
+                                         typename N::V cyk, const PhysN<N> &P) {
+  using V = typename N::V;
 #define SC(s, c) sc[(size_t)(s) * NCc + (c)]
 #define SK(s, c) sk[(size_t)(s) * NKc + (c)]
-  auto pred = [&](int su, int sfx, int sfy, bool negx, bool negy) -> D {
-    D r = df::scale(df::add(df::add(SC(su, b), SC(su, a)), df::add(SC(su, cc), SC(su, d))),
+  auto pred = [&](int su, int sfx, int sfy, bool negx, bool negy) -> V {
+    V r = N::scale(N::add(N::add(SC(su, b), SC(su, a)), N::add(SC(su, cc), SC(su, d))),
                     0.25f);
     if (sfx != NOF) {
-      const D s = df::add(df::sub(SC(sfx, b), SC(sfx, a)), df::sub(SC(sfx, cc), SC(sfx, d)));
-      r = df::mad(negx ? cxk : df::neg(cxk), s, r);
+      const V s = N::add(N::sub(SC(sfx, b), SC(sfx, a)), N::sub(SC(sfx, cc), SC(sfx, d)));
+      r = N::mad(negx ? cxk : N::neg(cxk), s, r);
     }
     if (sfy != NOF) {
-      const D s = df::add(df::sub(SC(sfy, d), SC(sfy, a)), df::sub(SC(sfy, cc), SC(sfy, b)));
-      r = df::mad(negy ? cyk : df::neg(cyk), s, r);
+      const V s = N::add(N::sub(SC(sfy, d), SC(sfy, a)), N::sub(SC(sfy, cc), SC(sfy, b)));
+      r = N::mad(negy ? cyk : N::neg(cyk), s, r);
     }
     return r;
   };
-  const D roh = pred(CRO, CRX, CRY, false, false);
-  const D eeh = pred(CEE, CFXE, CFYE, false, false);
-  const D rxh = pred(CRX, CFXRX, CFXY, false, false);
-  const D ryh = pred(CRY, CFXY, CFYRY, false, false);
-  const D rzh = pred(CRZ, CFXRZ, CFYRZ, false, false);
-  const D bxh = pred(CBX, NOF, CEZ, false, false);
-  const D byh = pred(CBY, CEZ, NOF, true, false);
-  const D bzh = pred(CBZ, CEY, CEX, false, true);
-  const D rinv = df::rcp(roh);
-  const D vxh = df::mul(rxh, rinv), vyh = df::mul(ryh, rinv), vzh = df::mul(rzh, rinv);
-  const D vv = df::mad(vzh, vzh, df::mad(vyh, vyh, df::sqr(vxh)));
-  const D bb = df::mad(bzh, bzh, df::mad(byh, byh, df::sqr(bxh)));
-  const D ek = df::mul(df::scale(roh, 0.5f), vv);
-  const D prh = df::mul(P.gm1, df::sub(df::sub(eeh, ek), df::mul(P.pi8i, bb)));
-  const D ep = df::mad(prh, P.ggm1, ek);
-  const D exh = df::mad(vzh, byh, df::neg(df::mul(vyh, bzh)));
-  const D eyh = df::mad(vxh, bzh, df::neg(df::mul(vzh, bxh)));
-  const D ezh = df::mad(vyh, bxh, df::neg(df::mul(vxh, byh)));
-  const D pt = df::mad(P.pi8i, bb, prh);
-  const D pbx = df::mul(P.pi4i, bxh), pby = df::mul(P.pi4i, byh);
+  const V roh = pred(CRO, CRX, CRY, false, false);
+  const V eeh = pred(CEE, CFXE, CFYE, false, false);
+  const V rxh = pred(CRX, CFXRX, CFXY, false, false);
+  const V ryh = pred(CRY, CFXY, CFYRY, false, false);
+  const V rzh = pred(CRZ, CFXRZ, CFYRZ, false, false);
+  const V bxh = pred(CBX, NOF, CEZ, false, false);
+  const V byh = pred(CBY, CEZ, NOF, true, false);
+  const V bzh = pred(CBZ, CEY, CEX, false, true);
+  const V rinv = N::rcp(roh);
+  const V vxh = N::mul(rxh, rinv), vyh = N::mul(ryh, rinv), vzh = N::mul(rzh, rinv);
+  const V vv = N::mad(vzh, vzh, N::mad(vyh, vyh, N::sqr(vxh)));
+  const V bb = N::mad(bzh, bzh, N::mad(byh, byh, N::sqr(bxh)));
+  const V ek = N::mul(N::scale(roh, 0.5f), vv);
+  const V prh = N::mul(P.gm1, N::sub(N::sub(eeh, ek), N::mul(P.pi8i, bb)));
+  const V ep = N::mad(prh, P.ggm1, ek);
+  const V exh = N::mad(vzh, byh, N::neg(N::mul(vyh, bzh)));
+  const V eyh = N::mad(vxh, bzh, N::neg(N::mul(vzh, bxh)));
+  const V ezh = N::mad(vyh, bxh, N::neg(N::mul(vxh, byh)));
+  const V pt = N::mad(P.pi8i, bb, prh);
+  const V pbx = N::mul(P.pi4i, bxh), pby = N::mul(P.pi4i, byh);
   SK(KXRO, k) = rxh;
   SK(KYRO, k) = ryh;
   SK(KEX, k) = exh; SK(KEY, k) = eyh; SK(KEZ, k) = ezh;
-  SK(KXEE, k) = df::mad(df::mad(bzh, eyh, df::neg(df::mul(byh, ezh))), P.pi4i, df::mul(ep, vxh));
-  SK(KYEE, k) = df::mad(df::mad(bxh, ezh, df::neg(df::mul(bzh, exh))), P.pi4i, df::mul(ep, vyh));
-  SK(KXRX, k) = df::mad(rxh, vxh, df::mad(df::neg(pbx), bxh, pt));
-  SK(KYRY, k) = df::mad(ryh, vyh, df::mad(df::neg(pby), byh, pt));
-  SK(KXY, k) = df::mad(rxh, vyh, df::neg(df::mul(pbx, byh)));
-  SK(KXRZ, k) = df::mad(rzh, vxh, df::neg(df::mul(pbx, bzh)));
-  SK(KYRZ, k) = df::mad(rzh, vyh, df::neg(df::mul(pby, bzh)));
+  SK(KXEE, k) = N::mad(N::mad(bzh, eyh, N::neg(N::mul(byh, ezh))), P.pi4i, N::mul(ep, vxh));
+  SK(KYEE, k) = N::mad(N::mad(bxh, ezh, N::neg(N::mul(bzh, exh))), P.pi4i, N::mul(ep, vyh));
+  SK(KXRX, k) = N::mad(rxh, vxh, N::mad(N::neg(pbx), bxh, pt));
+  SK(KYRY, k) = N::mad(ryh, vyh, N::mad(N::neg(pby), byh, pt));
+  SK(KXY, k) = N::mad(rxh, vyh, N::neg(N::mul(pbx, byh)));
+  SK(KXRZ, k) = N::mad(rzh, vxh, N::neg(N::mul(pbx, bzh)));
+  SK(KYRZ, k) = N::mad(rzh, vyh, N::neg(N::mul(pby, bzh)));
 #undef SC
 #undef SK
 }
 
-template <int CH>
+template <class N, int CH>
 __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
-    k_mlw2d_df_march(const double *__restrict__ A, double *__restrict__ B, int ix, int jx,
+    k_mlw2d_march(const double *__restrict__ A, double *__restrict__ B, int ix, int jx,
                      Axis ax, Axis ay, Phys ph, double dt_arg, Ctl *__restrict__ ctl, Box3 box,
                      int seg) {
   using T = MarchD<CH>;
-  extern __shared__ D smem_m[];
-  D *sc = smem_m;                          // cells   [NCS][CR][CX]
-  D *sk = sc + (size_t)NCS * T::NC;        // corners [NKS][KR][KX]
-  D *sqx = sk + (size_t)NKS * T::NK;       // q dxim  [CH][KX]
-  D *sqy = sqx + T::NQX;                   // q dyim  [KR][TX]
+  using V = typename N::V;
+  extern __shared__ double smem_m_raw[];
+  V *sc = reinterpret_cast<V *>(smem_m_raw);                          // cells   [NCS][CR][CX]
+  V *sk = sc + (size_t)NCS * T::NC;        // corners [NKS][KR][KX]
+  V *sqx = sk + (size_t)NKS * T::NK;       // q dxim  [CH][KX]
+  V *sqy = sqx + T::NQX;                   // q dyim  [KR][TX]
   double *sred = reinterpret_cast<double *>(sqy + T::NQY);
   double dtv = dt_arg, safety = 0.0;
   unsigned long long *cfl_out = nullptr;
@@ -523,11 +590,11 @@ __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
   const int i0 = 1 + blockIdx.x * T::TX;
   const int jb = 1 + blockIdx.y * seg;                 // first interior row of the segment
   const int je = min(jx - 2, jb + seg - 1);            // last
-  const PhysD P = phys_d(ph);
-  const D dt = df::from_double(dtv);
-  const D hdt = df::scale(dt, 0.5f);
+  const PhysN<N> P = phys_n<N>(ph);
+  const V dt = N::in(dtv);
+  const V hdt = N::scale(dt, 0.5f);
   const bool edge_x = blockIdx.x == 0 || blockIdx.x == gridDim.x - 1;
-  D kmax = df::mk(0.0f);
+  V kmax = N::zero();
   bool bad = false;
 
   for (int j0 = jb; j0 <= je; j0 += CH) {
@@ -550,10 +617,10 @@ __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
       const int lx = c % T::CX, ly = c / T::CX;
       const int gi = i0 - 1 + lx, gj = j0 - 1 + ly;
       if (gi < ix && gj < jx) {
-        cell_df<T::NC>(A, n, (size_t)gi + (size_t)gj * ix, sc, c, P);
+        cell_m<N, T::NC>(A, n, (size_t)gi + (size_t)gj * ix, sc, c, P);
       } else {
 #pragma unroll 1
-        for (int s = 0; s < NCS; s++) SC(s, c) = df::mk(0.0f);
+        for (int s = 0; s < NCS; s++) SC(s, c) = N::zero();
       }
     }
     __syncthreads();
@@ -563,37 +630,37 @@ __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
       const int gi = i0 - 1 + kx, gj = j0 - 1 + ky;
       if (gi <= ix - 2 && gj <= jx - 2) {
         const int a = kx + ky * T::CX;
-        const D cxk = df::scale(df::mul(dt, df::from_double(ax.dim[gi])), 0.5f);
-        const D cyk = df::scale(df::mul(dt, df::from_double(ay.dim[gj])), 0.5f);
-        corner_df<T::NC, T::NK>(sc, sk, a, a + 1, a + 1 + T::CX, a + T::CX, k, cxk, cyk, P);
+        const V cxk = N::scale(N::mul(dt, N::in(ax.dim[gi])), 0.5f);
+        const V cyk = N::scale(N::mul(dt, N::in(ay.dim[gj])), 0.5f);
+        corner_m<N, T::NC, T::NK>(sc, sk, a, a + 1, a + 1 + T::CX, a + T::CX, k, cxk, cyk, P);
       } else {
 #pragma unroll 1
-        for (int s = 0; s < NKS; s++) SK(s, k) = df::mk(0.0f);
+        for (int s = 0; s < NKS; s++) SK(s, k) = N::zero();
       }
     }
     for (int f = tid; f < T::NQX; f += T::NT) {
       const int fx = f % T::KX, r = f / T::KX;
       const int gi = i0 - 1 + fx, gj = j0 + r;
-      D v = df::mk(0.0f);
+      V v = N::zero();
       if (gi + 1 < ix && gj < jx) {
         const int cl = fx + (r + 1) * T::CX;
-        const D q = df::addf(df::absd(df::sub(SC(CVX, cl + 1), SC(CVX, cl))), -1.0e-4f);
-        if (df::pos(q))
-          v = df::mul(df::mul(df::mul(P.qav, df::from_double(ax.dm[gi])), q),
-                      df::from_double(ax.dim[gi]));
+        const V q = N::addf(N::absd(N::sub(SC(CVX, cl + 1), SC(CVX, cl))), -1.0e-4f);
+        if (N::pos(q))
+          v = N::mul(N::mul(N::mul(P.qav, N::in(ax.dm[gi])), q),
+                      N::in(ax.dim[gi]));
       }
       sqx[f] = v;
     }
     for (int f = tid; f < T::NQY; f += T::NT) {
       const int fx = f % T::TX, r = f / T::TX;
       const int gi = i0 + fx, gj = j0 - 1 + r;
-      D v = df::mk(0.0f);
+      V v = N::zero();
       if (gi < ix && gj + 1 < jx) {
         const int cl = (fx + 1) + r * T::CX;
-        const D q = df::addf(df::absd(df::sub(SC(CVY, cl + T::CX), SC(CVY, cl))), -1.0e-4f);
-        if (df::pos(q))
-          v = df::mul(df::mul(df::mul(P.qav, df::from_double(ay.dm[gj])), q),
-                      df::from_double(ay.dim[gj]));
+        const V q = N::addf(N::absd(N::sub(SC(CVY, cl + T::CX), SC(CVY, cl))), -1.0e-4f);
+        if (N::pos(q))
+          v = N::mul(N::mul(N::mul(P.qav, N::in(ay.dm[gj])), q),
+                      N::in(ay.dim[gj]));
       }
       sqy[f] = v;
     }
@@ -611,89 +678,89 @@ __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
         const int cE = c + 1, cW = c - 1, cN = c + T::CX, cS = c - T::CX;
         const int kSW = (lx - 1) + (ly - 1) * T::KX, kSE = kSW + 1;
         const int kNW = kSW + T::KX, kNE = kNW + 1;
-        const D dxi = df::from_double(ax.di[gi]), dyi = df::from_double(ay.di[gj]);
-        const D ux0 = df::from_double(ax.u0[gi]), ux1 = df::from_double(ax.u1[gi]);
-        const D uy0 = df::from_double(ay.u0[gj]), uy1 = df::from_double(ay.u1[gj]);
-        const D hdx = df::mul(hdt, dxi), hdy = df::mul(hdt, dyi);
-        const D fcx = df::scale(hdx, 0.5f), fcy = df::scale(hdy, 0.5f);
-        const D fx0 = df::mul(hdx, uy0), fx1 = df::mul(hdx, uy1);
-        const D fy0 = df::mul(hdy, ux0), fy1 = df::mul(hdy, ux1);
-        const D dtx = df::mul(dt, dxi), dty = df::mul(dt, dyi);
-        const D ae = df::mul(dtx, sqx[lx + (ly - 1) * T::KX]);
-        const D aw = df::mul(dtx, sqx[lx - 1 + (ly - 1) * T::KX]);
-        const D an = df::mul(dty, sqy[(lx - 1) + ly * T::TX]);
-        const D as = df::mul(dty, sqy[(lx - 1) + (ly - 1) * T::TX]);
+        const V dxi = N::in(ax.di[gi]), dyi = N::in(ay.di[gj]);
+        const V ux0 = N::in(ax.u0[gi]), ux1 = N::in(ax.u1[gi]);
+        const V uy0 = N::in(ay.u0[gj]), uy1 = N::in(ay.u1[gj]);
+        const V hdx = N::mul(hdt, dxi), hdy = N::mul(hdt, dyi);
+        const V fcx = N::scale(hdx, 0.5f), fcy = N::scale(hdy, 0.5f);
+        const V fx0 = N::mul(hdx, uy0), fx1 = N::mul(hdx, uy1);
+        const V fy0 = N::mul(hdy, ux0), fy1 = N::mul(hdy, ux1);
+        const V dtx = N::mul(dt, dxi), dty = N::mul(dt, dyi);
+        const V ae = N::mul(dtx, sqx[lx + (ly - 1) * T::KX]);
+        const V aw = N::mul(dtx, sqx[lx - 1 + (ly - 1) * T::KX]);
+        const V an = N::mul(dty, sqy[(lx - 1) + ly * T::TX]);
+        const V as = N::mul(dty, sqy[(lx - 1) + (ly - 1) * T::TX]);
         auto dvar = [&](int su, int sfx, bool negx, int sfy, bool negy, int kfx, bool nkx,
-                        int kfy, bool nky) -> D {
-          const D u = SC(su, c);
-          D du = df::mul(ae, df::sub(SC(su, cE), u));
-          du = df::mad(aw, df::sub(SC(su, cW), u), du);
-          du = df::mad(an, df::sub(SC(su, cN), u), du);
-          du = df::mad(as, df::sub(SC(su, cS), u), du);
+                        int kfy, bool nky) -> V {
+          const V u = SC(su, c);
+          V du = N::mul(ae, N::sub(SC(su, cE), u));
+          du = N::mad(aw, N::sub(SC(su, cW), u), du);
+          du = N::mad(an, N::sub(SC(su, cN), u), du);
+          du = N::mad(as, N::sub(SC(su, cS), u), du);
           if (sfx != NOF)
-            du = df::mad(negx ? fcx : df::neg(fcx), df::sub(SC(sfx, cE), SC(sfx, cW)), du);
+            du = N::mad(negx ? fcx : N::neg(fcx), N::sub(SC(sfx, cE), SC(sfx, cW)), du);
           if (sfy != NOF)
-            du = df::mad(negy ? fcy : df::neg(fcy), df::sub(SC(sfy, cN), SC(sfy, cS)), du);
+            du = N::mad(negy ? fcy : N::neg(fcy), N::sub(SC(sfy, cN), SC(sfy, cS)), du);
           if (kfx != NOF) {
-            du = df::mad(nkx ? fx0 : df::neg(fx0), df::sub(SK(kfx, kSE), SK(kfx, kSW)), du);
-            du = df::mad(nkx ? fx1 : df::neg(fx1), df::sub(SK(kfx, kNE), SK(kfx, kNW)), du);
+            du = N::mad(nkx ? fx0 : N::neg(fx0), N::sub(SK(kfx, kSE), SK(kfx, kSW)), du);
+            du = N::mad(nkx ? fx1 : N::neg(fx1), N::sub(SK(kfx, kNE), SK(kfx, kNW)), du);
           }
           if (kfy != NOF) {
-            du = df::mad(nky ? fy0 : df::neg(fy0), df::sub(SK(kfy, kNW), SK(kfy, kSW)), du);
-            du = df::mad(nky ? fy1 : df::neg(fy1), df::sub(SK(kfy, kNE), SK(kfy, kSE)), du);
+            du = N::mad(nky ? fy0 : N::neg(fy0), N::sub(SK(kfy, kNW), SK(kfy, kSW)), du);
+            du = N::mad(nky ? fy1 : N::neg(fy1), N::sub(SK(kfy, kNE), SK(kfy, kSE)), du);
           }
           return du;
         };
         const double ro_new =
-            ro0 + df::to_double(dvar(CRO, CRX, false, CRY, false, KXRO, false, KYRO, false));
+            ro0 + N::out(dvar(CRO, CRX, false, CRY, false, KXRO, false, KYRO, false));
         const double bx_new =
-            bx0 + df::to_double(dvar(CBX, NOF, false, CEZ, false, NOF, false, KEZ, false));
+            bx0 + N::out(dvar(CBX, NOF, false, CEZ, false, NOF, false, KEZ, false));
         const double by_new =
-            by0 + df::to_double(dvar(CBY, CEZ, true, NOF, false, KEZ, true, NOF, false));
+            by0 + N::out(dvar(CBY, CEZ, true, NOF, false, KEZ, true, NOF, false));
         const double bz_new =
-            bz0 + df::to_double(dvar(CBZ, CEY, false, CEX, true, KEY, false, KEX, true));
-        const D ee =
-            df::add(SC(CEE, c), dvar(CEE, CFXE, false, CFYE, false, KXEE, false, KYEE, false));
-        const D rx =
-            df::add(SC(CRX, c), dvar(CRX, CFXRX, false, CFXY, false, KXRX, false, KXY, false));
-        const D ry =
-            df::add(SC(CRY, c), dvar(CRY, CFXY, false, CFYRY, false, KXY, false, KYRY, false));
-        const D rz =
-            df::add(SC(CRZ, c), dvar(CRZ, CFXRZ, false, CFYRZ, false, KXRZ, false, KYRZ, false));
+            bz0 + N::out(dvar(CBZ, CEY, false, CEX, true, KEY, false, KEX, true));
+        const V ee =
+            N::add(SC(CEE, c), dvar(CEE, CFXE, false, CFYE, false, KXEE, false, KYEE, false));
+        const V rx =
+            N::add(SC(CRX, c), dvar(CRX, CFXRX, false, CFXY, false, KXRX, false, KXY, false));
+        const V ry =
+            N::add(SC(CRY, c), dvar(CRY, CFXY, false, CFYRY, false, KXY, false, KYRY, false));
+        const V rz =
+            N::add(SC(CRZ, c), dvar(CRZ, CFXRZ, false, CFYRZ, false, KXRZ, false, KYRZ, false));
         {
-          D s = df::mul(ux0, SK(KEZ, kSW));
-          s = df::mad(ux1, SK(KEZ, kSE), s);
-          D t = df::mul(ux0, SK(KEZ, kNW));
-          t = df::mad(ux1, SK(KEZ, kNE), t);
-          s = df::mad(uy1, t, df::mul(uy0, s));
-          s = df::mad(hdt, SC(CEZ, c), df::mul(hdt, s));
-          B[PAZ * n + g] = az0 - df::to_double(s);
+          V s = N::mul(ux0, SK(KEZ, kSW));
+          s = N::mad(ux1, SK(KEZ, kSE), s);
+          V t = N::mul(ux0, SK(KEZ, kNW));
+          t = N::mad(ux1, SK(KEZ, kNE), t);
+          s = N::mad(uy1, t, N::mul(uy0, s));
+          s = N::mad(hdt, SC(CEZ, c), N::mul(hdt, s));
+          B[PAZ * n + g] = az0 - N::out(s);
         }
-        const D ro = df::from_double(ro_new);
-        const D bx = df::from_double(bx_new), by = df::from_double(by_new);
-        const D bz = df::from_double(bz_new);
-        const D rinv = df::rcp(ro);
-        const D vx = df::mul(rx, rinv), vy = df::mul(ry, rinv), vz = df::mul(rz, rinv);
-        const D vv = df::mad(vz, vz, df::mad(vy, vy, df::sqr(vx)));
-        const D bb = df::mad(bz, bz, df::mad(by, by, df::sqr(bx)));
-        const D pr = df::mul(P.gm1, df::sub(df::sub(ee, df::mul(df::scale(ro, 0.5f), vv)),
-                                            df::mul(P.pi8i, bb)));
-        const double prd = df::to_double(pr);
+        const V ro = N::in(ro_new);
+        const V bx = N::in(bx_new), by = N::in(by_new);
+        const V bz = N::in(bz_new);
+        const V rinv = N::rcp(ro);
+        const V vx = N::mul(rx, rinv), vy = N::mul(ry, rinv), vz = N::mul(rz, rinv);
+        const V vv = N::mad(vz, vz, N::mad(vy, vy, N::sqr(vx)));
+        const V bb = N::mad(bz, bz, N::mad(by, by, N::sqr(bx)));
+        const V pr = N::mul(P.gm1, N::sub(N::sub(ee, N::mul(N::scale(ro, 0.5f), vv)),
+                                            N::mul(P.pi8i, bb)));
+        const double prd = N::out(pr);
         B[PRO * n + g] = ro_new;
         B[PPR * n + g] = prd;
-        B[PVX * n + g] = df::to_double(vx);
-        B[PVY * n + g] = df::to_double(vy);
-        B[PVZ * n + g] = df::to_double(vz);
+        B[PVX * n + g] = N::out(vx);
+        B[PVY * n + g] = N::out(vy);
+        B[PVZ * n + g] = N::out(vz);
         B[PBX * n + g] = bx_new;
         B[PBY * n + g] = by_new;
         B[PBZ * n + g] = bz_new;
         if (cfl_out != nullptr && gi >= box.lo[0] && gi <= box.hi[0] && gj >= box.lo[1] &&
             gj <= box.hi[1]) {
-          const D sk2 = df::mad(df::mad(P.gm, pr, df::mul(P.pi4i, bb)), rinv, vv);
-          const D ix2 = df::sqr(dxi), iy2 = df::sqr(dyi);
-          const D key = df::mul(sk2, df::gt(ix2, iy2) ? ix2 : iy2);
-          if (key.h == key.h && df::gt(key, kmax)) kmax = key;
-          bad |= bad_cell_d(ro_new, prd, key);
+          const V sk2 = N::mad(N::mad(P.gm, pr, N::mul(P.pi4i, bb)), rinv, vv);
+          const V ix2 = N::sqr(dxi), iy2 = N::sqr(dyi);
+          const V key = N::mul(sk2, N::gt(ix2, iy2) ? ix2 : iy2);
+          if (!N::isnan(key) && N::gt(key, kmax)) kmax = key;
+          bad |= bad_cell_d(ro_new, prd, N::nan_probe(key));
         }
       }
     }
@@ -718,9 +785,9 @@ __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
 #undef SK
   if (cfl_out != nullptr) {
     if (ctl != nullptr) count_bad_block(bad, &ctl->nonfinite, tid);
-    kmax = warp_max_d(kmax);
+    kmax = N::warp_max(kmax);
     const int lane = tid & 31, w = tid >> 5;
-    if (lane == 0) sred[w] = df::to_double(kmax);
+    if (lane == 0) sred[w] = N::out(kmax);
     __syncthreads();
     if (w == 0) {
       double x = lane < (T::NT + 31) / 32 ? sred[lane] : 0.0;
@@ -789,7 +856,7 @@ cudaError_t launch_df(const double *A, double *B, int ix, int jx, const Axis &ax
 }  // namespace
 
 namespace {
-template <int CH>
+template <class N, int CH>
 cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis &ax,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl, Box3 box,
                          cudaStream_t s) {
@@ -803,13 +870,13 @@ cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis 
   {
     std::lock_guard<std::mutex> lk(mu);
     if (!slots_of[dev]) {
-      e = cudaFuncSetAttribute(k_mlw2d_df_march<CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(k_mlw2d_march<N, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)T::smem_bytes);
       if (e != cudaSuccess) return e;
       int sms = 0, per_sm = 0;
       if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
         return e;
-      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlw2d_df_march<CH>,
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlw2d_march<N, CH>,
                                                              T::NT, T::smem_bytes)) !=
           cudaSuccess)
         return e;
@@ -820,7 +887,7 @@ cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis 
   const int strips = (ix - 2 + T::TX - 1) / T::TX, rows = jx - 2;
   const int seg = balance_seg(strips, rows, CH, slots);
   dim3 grid(strips, (rows + seg - 1) / seg);
-  k_mlw2d_df_march<CH><<<grid, T::NT, T::smem_bytes, s>>>(A, B, ix, jx, ax, ay, ph, dt, ctl,
+  k_mlw2d_march<N, CH><<<grid, T::NT, T::smem_bytes, s>>>(A, B, ix, jx, ax, ay, ph, dt, ctl,
                                                          box, seg);
   count_launch();
   return cudaGetLastError();
@@ -829,13 +896,21 @@ cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis 
 
 int mlw2d_df_tile_count() { return 6; }
 
+// The fast policy's mlw_m3 step with the y-marching tile (FP64, F64N).
+cudaError_t launch_mlw2d_march_fast(const double *A, double *B, int ix, int jx,
+                                    const Axis &ax, const Axis &ay, const Phys &ph, double dt,
+                                    Ctl *ctl, Box3 box, cudaStream_t s) {
+  if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
+  return launch_march<F64N, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+}
+
 cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx,
                             const Axis &ax, const Axis &ay, const Phys &ph, double dt,
                             Ctl *ctl, Box3 box, cudaStream_t s) {
   if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
   switch (tile) {
-    case 4: return launch_march<8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
-    case 5: return launch_march<6>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 4: return launch_march<DFN, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 5: return launch_march<DFN, 6>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 1: return launch_df<32, 9, 1>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 2: return launch_df<16, 16, 2>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 3: return launch_df<32, 16, 2>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
