@@ -50,7 +50,8 @@ def parse():
                    help="double-float policy of the 2-D mlw_m3 step (FP32 pipes, FP64 "
                         "accumulation)")
     p.add_argument("--tile", type=int, default=-1,
-                   help="2-D tile configuration (default: autotuned)")
+                   help="2-D tile configuration (default: autotuned); also the tile of the "
+                        "mlw2d profile case")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary 3-D and 1-D workloads")
@@ -60,12 +61,12 @@ def parse():
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
                             "gravity2d", "resistive2d", "gravity3d", "resistive3d",
-                            "spicule", "single", "mlw2d_df", "mlw3d_df"],
+                            "spicule", "single", "mlw2d", "mlw2d_df", "mlw3d_df"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
 
-def profile_case(case, n):
+def profile_case(case, n, tile=-1, df64=False):
     """A small fixed case of one secondary path: a few device iterations of
     the 3-D steps on an n^3 box, 20 reverse steps of the 2-D adjoint on n^2,
     or 5 batched iterations of 8 shear layers; prints one JSON line."""
@@ -114,6 +115,20 @@ def profile_case(case, n):
             run.advance(5)
             out[str(m)] = int(run.query().nexec)
             run.close()
+    elif case == "mlw2d":
+        # the FP64 fast-policy step of the vortex on n^2: 4 iterations with the
+        # given tile, or with the autotuner's pick
+        s = setups.orszag_tang(n)
+        run = drivers.make_run(s, tile=tile)
+        run.push(s["state"])
+        if tile < 0:
+            tile = run.autotune(2)
+            run.push(s["state"])
+        run.start(nstop=4, safety=s["safety"], dtmin=1e-10)
+        run.advance(4)
+        st = run.query()
+        run.close()
+        out = {"case": case, "n": n, "tile": tile, "steps": int(st.nexec), "merr": int(st.merr)}
     elif case in ("mlw2d_df", "mlw3d_df"):
         # the double-float steps: 4 iterations of the vortex (n^2, y-marching
         # tile) or of the turbulence box (n^3)
@@ -128,13 +143,14 @@ def profile_case(case, n):
     elif case in ("mlw3d", "roe3d", "hlld3d"):
         solver = {"mlw3d": "mlw_m_3d", "roe3d": "roe_m_3d", "hlld3d": "hlld_3d"}[case]
         s = setups.turbulence_3d(n, solver=solver)
-        run = drivers.make_run(s)
+        run = drivers.make_run(s, df64=df64)
         run.push(s["state"])
         run.start(nstop=3, safety=0.2, dtmin=1e-10)
         run.advance(3)
         st = run.query()
         run.close()
-        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+        out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr),
+               "df64": df64}
     elif case == "adjoint2d":
         s = setups.shear_layer(n, beta=1.0, seed=4)
         run = drivers.make_run(s)
@@ -244,7 +260,12 @@ def extra_workloads(stream, exact=False):
     # ---- 3-D Roe-MUSCL and HLLD steps on the same turbulence box (margin 3)
     for solver, safety in (("roe_m_3d", None), ("hlld_3d", 0.2)):
         out[f"turbulence_256^3_{solver}"] = riemann_3d(stream, solver, safety, exact)
+        if not exact:  # the face flux in double-float
+            out[f"turbulence_256^3_{solver}_df64"] = riemann_3d(stream, solver, safety, False,
+                                                                df64=True)
     out["orszag_tang_512^2_roe_m3"] = roe_2d(stream, exact)
+    if not exact:
+        out["orszag_tang_512^2_roe_m3_df64"] = roe_2d(stream, False, df64=True)
     out["mhd_gravity_wave_512^2_mlw_m3_g"] = loop_2d(
         stream, exact, lambda m: setups.mhd_gravity_wave(m, solver="mlw_m3"), 512, 100, 256, 500,
         "gravity-wave model")
@@ -264,18 +285,20 @@ def extra_workloads(stream, exact=False):
     return out
 
 
-def riemann_3d(stream, solver, safety, exact, iters=10):
+def riemann_3d(stream, solver, safety, exact, iters=10, df64=False):
     """Two-stage Riemann-solver step on the 3-D beta = 1 box, 256^3 interior
     cells + 3 ghost layers: loop iterations timed with events (graph), the
     four step kernels profiled.  HLLD runs in Heaviside units; its reference
     driver pairs that state with the CANS-unit cfl_m, which at safety 0.4 is
-    beyond the three-axis stability limit, so it runs at safety 0.2."""
+    beyond the three-axis stability limit, so it runs at safety 0.2.  df64
+    evaluates the face flux in double-float (the oracle sample is then left
+    to the FP64 leg)."""
     import torch
     from utrip_gb300 import drivers, setups
     s = setups.turbulence_3d(256, solver=solver)
     if safety is not None:
         s["safety"] = safety
-    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream, df64=df64)
     run.push(s["state"])
     run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
     run.advance(2)
@@ -290,32 +313,36 @@ def riemann_3d(stream, solver, safety, exact, iters=10):
     st = run.query()
     run.close()
     zones = 256 ** 3
-    return {"zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
-            "step_kernels_ms": step_ms / 4, "safety": s["safety"], "bound": "fp64",
-            "steps_done": int(st.nexec), "merr": int(st.merr),
-            "policy": "exact" if exact else "fast",
-            "cpu_oracle": cpu_sample_3d(solver, safety)}
+    out = {"zone_updates_per_s": zones * iters / (ms * 1e-3), "ms_per_iteration": ms / iters,
+           "step_kernels_ms": step_ms / 4, "safety": s["safety"],
+           "bound": "fp32 pipes (double-float flux)" if df64 else "fp64",
+           "steps_done": int(st.nexec), "merr": int(st.merr),
+           "policy": "df64" if df64 else ("exact" if exact else "fast")}
+    if not df64:
+        out["cpu_oracle"] = cpu_sample_3d(solver, safety)
+    return out
 
 
-def roe_2d(stream, exact, n=512, iters=50, cpu_n=256, cpu_steps=300):
+def roe_2d(stream, exact, n=512, iters=50, cpu_n=256, cpu_steps=300, df64=False):
     """The 2-D Roe-MUSCL step (roe_m3, margin 2) on the Orszag-Tang vortex of
     the headline, loop iterations timed with events (graph), the four step
     kernels profiled; the oracle on a bounded sample (cpu_n^2, all host
     threads) beside it."""
     from utrip_gb300 import setups
     return loop_2d(stream, exact, lambda m: setups.orszag_tang(m, solver="roe_m3"), n, iters,
-                   cpu_n, cpu_steps, "vortex")
+                   cpu_n, cpu_steps, "vortex", df64=df64)
 
 
-def loop_2d(stream, exact, make, n, iters, cpu_n, cpu_steps, what):
+def loop_2d(stream, exact, make, n, iters, cpu_n, cpu_steps, what, df64=False):
     """A 2-D model loop on the device (graph-replayed iterations timed with
     events, step kernels profiled) and the oracle on a bounded sample of the
-    same model (cpu_n^2, all host threads)."""
+    same model (cpu_n^2, all host threads; left to the FP64 leg when df64
+    selects the double-float policy)."""
     import torch
     import oracle
     from utrip_gb300 import drivers, setups
     s = make(n)
-    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream, df64=df64)
     run.push(s["state"])
     run.start(tend=1e30, nstop=10 ** 12, safety=s["safety"], dtmin=s["dtmin"])
     run.advance(3)
@@ -329,6 +356,11 @@ def loop_2d(stream, exact, make, n, iters, cpu_n, cpu_steps, what):
     step_ms, _ = run.profile(10)
     st = run.query()
     run.close()
+    if df64:
+        return {"zone_updates_per_s": n * n * iters / (ms * 1e-3),
+                "ms_per_iteration": ms / iters, "step_kernels_ms": step_ms / 10,
+                "bound": "fp32 pipes (double-float flux)", "steps_done": int(st.nexec),
+                "merr": int(st.merr), "policy": "df64"}
     c = make(cpu_n)
     cs = setups.copy_state(c)
     t0 = time.perf_counter()
@@ -895,9 +927,9 @@ def parity_check(n, stream, nsteps=100, c3_n=256, c3_steps=200, c3_riemann_steps
 
 def parity_3d(stream, solver, n, steps, exact_too):
     """One 3-D loop of the beta = 1 turbulence box against the oracle: fast
-    policy relative L-infinity and conservation drift (device and oracle),
-    and with exact_too the cells that differ in the exact policy.  HLLD runs
-    at safety 0.2 (see riemann_3d)."""
+    and double-float policy relative L-infinity and conservation drift
+    (device and oracle), and with exact_too the cells that differ in the
+    exact policy.  HLLD runs at safety 0.2 (see riemann_3d)."""
     import oracle
     from utrip_gb300 import drivers, setups
     s = setups.turbulence_3d(n, solver=solver)
@@ -909,8 +941,7 @@ def parity_3d(stream, solver, n, steps, exact_too):
     leg = {"steps": int(ns_ref), "oracle_s": time.perf_counter() - t0,
            "oracle_cores": oracle.get_threads()}
     tot0 = _totals(s, s["state"])
-    policies = ["fast"] + (["exact"] if exact_too else []) + \
-        (["df64"] if solver == "mlw_m_3d" else [])
+    policies = ["fast"] + (["exact"] if exact_too else []) + ["df64"]
     for policy in policies:
         got = setups.copy_state(s)
         t, ns, merr, _ = drivers.run_resident(s, got, steps, exact=policy == "exact",
@@ -1354,7 +1385,7 @@ def run_ours(args, ws, rank, local):
 def main():
     args = parse()
     if args.profile_case:
-        profile_case(args.profile_case, args.n)
+        profile_case(args.profile_case, args.n, args.tile, args.df64)
         return
     if args.parity_full:
         parity_full()

@@ -501,16 +501,17 @@ int cans_run_set_graph(cans_run *h, int use_graph);
 int cans_run_set_tile(cans_run *h, int tile);
 
 /* The double-float policy of the 2-D mlw_m3 and the 3-D mlw_m step, and of
- * the face flux of the Roe-MUSCL steps (no counterpart in the reference: an
- * arithmetic policy beside exact and fast).
+ * the face flux of the Roe-MUSCL and HLLD steps (no counterpart in the
+ * reference: an arithmetic policy beside exact and fast).
  * With on = 1 the step's arithmetic runs as pairs of floats on the FP32
  * pipes (48-bit significands; the exponent range of float, about
  * 1e-38..1e38, bounds the values it holds) and the conserved density and
  * field are accumulated in FP64; the CFL, boundary fill and loop
  * bookkeeping are unchanged.  Held to a relative 1e-10 per variable against
  * the reference arithmetic after 100 steps.  Only fast-policy
- * CANS_SOLVER_MLW_M3_2D, CANS_SOLVER_MLW_M_3D, CANS_SOLVER_ROE_M3_2D and
- * CANS_SOLVER_ROE_M_3D runs without gravity or resistivity take it (else
+ * CANS_SOLVER_MLW_M3_2D, CANS_SOLVER_MLW_M_3D, CANS_SOLVER_ROE_M3_2D,
+ * CANS_SOLVER_ROE_M_3D and CANS_SOLVER_HLLD_3D runs without gravity or
+ * resistivity take it (else
  * CANS_ERR_ARG); the mLW steps select among their own tile shapes
  * (cans_run_autotune). */
 int cans_run_set_df64(cans_run *h, int on);

@@ -121,9 +121,10 @@ def test_literal_drop_in_loop_matches_oracle(gpu, oracle_lib):
 
 
 N_TILES_2D = 6  # 32x16, 32x8, 16x16, 64x8, 32x9 (one row per thread), 32x10
-# tile 6 is the y-marching kernel of the fast mlw_m3 step (the exact policy
-# takes the 32x9 tile in its place)
-MARCH_TILE = 6
+# tiles 6 and 7 are the y-marching kernel of the fast mlw_m3 step, its
+# segments balanced per SM or by waves (the exact policy takes the 32x9 tile
+# in their place)
+MARCH_TILES = (6, 7)
 
 
 @pytest.mark.parametrize("solver", ["mlw_m3", "mlw_m"])
@@ -218,12 +219,13 @@ def test_oblique_shock_tube_to_tend_exact_bitwise(gpu, oracle_lib):
         assert np.array_equal(a, b), k
 
 
+@pytest.mark.parametrize("tile", MARCH_TILES)
 @pytest.mark.parametrize("make,steps", [
     (lambda: setups.orszag_tang(64), 100),
     (lambda: setups.shear_layer(130, beta=0.5, seed=2), 100),
     (lambda: setups.random_state(53, 41, seed=7), 20),
 ])
-def test_fast_marching_tile_against_oracle(gpu, oracle_lib, make, steps):
+def test_fast_marching_tile_against_oracle(gpu, oracle_lib, make, steps, tile):
     """The y-marching tile of the fast policy (32-column strips taking their
     rows in chunks, the symmetric momentum flux formed once) holds the fast
     policy's 1e-10 against the oracle, ragged strips and segments included."""
@@ -231,7 +233,7 @@ def test_fast_marching_tile_against_oracle(gpu, oracle_lib, make, steps):
     ref = setups.copy_state(s)
     t_ref, ns_ref, _, _ = oracle.run_2d(s, ref, steps)
     got = setups.copy_state(s)
-    run = drivers.make_run(s, tile=MARCH_TILE)
+    run = drivers.make_run(s, tile=tile)
     try:
         t, ns, merr, nexec = drivers.run_resident(s, got, steps, run=run)
     finally:
@@ -242,14 +244,14 @@ def test_fast_marching_tile_against_oracle(gpu, oracle_lib, make, steps):
 
 
 def test_marching_tile_falls_back_for_exact_and_mlw_m(gpu, oracle_lib):
-    """Asked of the exact policy or of mlw_m, tile 6 runs the 32x9 tile: still
-    bit for bit."""
+    """Asked of the exact policy or of mlw_m, tiles 6 and 7 run the 32x9
+    tile: still bit for bit."""
     for solver in ("mlw_m3", "mlw_m"):
         s = setups.random_state(70, 45, seed=9, solver=solver)
         ref = setups.copy_state(s)
         dt, _ = oracle.cfl_2d(s, ref, 0.4)
         oracle.step_2d(s, ref, dt)
-        run = drivers.make_run(s, exact=True, tile=MARCH_TILE)
+        run = drivers.make_run(s, exact=True, tile=MARCH_TILES[1])
         try:
             run.push(setups.copy_state(s))
             run.step(dt, apply_bc=False)

@@ -69,10 +69,11 @@ cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx
                             Ctl *ctl, Box3 box, cudaStream_t s);
 int mlw2d_df_tile_count();
 // The fast policy's mlw_m3 step with the y-marching tile (the FP64 instance
-// of the marching kernel of mlw2d_df.cu).
+// of the marching kernel of mlw2d_df.cu); waves selects the segment balance
+// by waves of resident blocks instead of by blocks per SM.
 cudaError_t launch_mlw2d_march_fast(const double *A, double *B, int ix, int jx,
                                     const Axis &ax, const Axis &ay, const Phys &ph, double dt,
-                                    Ctl *ctl, Box3 box, cudaStream_t s);
+                                    Ctl *ctl, Box3 box, cudaStream_t s, bool waves = false);
 // The 3-D mlw_m step in the double-float policy (mlw3d_df.cu).
 cudaError_t launch_mlw3d_df(int tile, const double *A, double *B, int ix, int jx, int kx,
                             const Axis &ax, const Axis &ay, const Axis &az, const Phys &ph,
@@ -190,13 +191,14 @@ cudaError_t launch_roe1d(bool exact, const double *A, double *B, double *scratch
 // A -> B for every cell.  mfdim[a] = 1 marks an active axis.  scratch holds
 // hlld3d_scratch_doubles(ix*jx*kx) doubles.  With ctl the kernels take dt and
 // the buffers from it; launch_hlld3d_finish then reduces the CFL of every
-// cell of the new state and ends the loop iteration.
+// cell of the new state and ends the loop iteration.  df (with exact false)
+// evaluates the face flux in double-float arithmetic.
 size_t hlld3d_scratch_doubles(size_t ncells);
 cudaError_t launch_hlld3d(bool exact, const double *A, double *B,
                           double *scratch, int ix, int jx, int kx,
                           const int *mfdim, const Axis &ax, const Axis &ay,
                           const Axis &az, double gm, double mu, double dt,
-                          const Ctl *ctl, cudaStream_t s);
+                          const Ctl *ctl, cudaStream_t s, bool df = false);
 cudaError_t launch_hlld3d_finish(bool exact, int ix, int jx, int kx,
                                  const Axis &ax, const Axis &ay,
                                  const Axis &az, const Phys &ph, Ctl *ctl,

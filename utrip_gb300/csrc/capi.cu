@@ -1498,7 +1498,8 @@ int layout2d(const cans_run *h) {
 }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
-  if (h->df && !is_roe(h)) return h->ndim == 3 ? mlw3d_df_tile_count() : mlw2d_df_tile_count();
+  if (h->df && !is_roe(h) && !is_hlld(h))
+    return h->ndim == 3 ? mlw3d_df_tile_count() : mlw2d_df_tile_count();
   if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
   if (h->eta) return h->ndim == 3 ? mlw3d_tile_count() : 1;
   if (h->grav) return h->ndim == 3 ? mlw3d_g_tile_count() : mlw2d_g_tile_count();
@@ -1539,7 +1540,7 @@ cudaError_t step_kernel(cans_run *h, int tile, const double *A, double *B,
   if (is_hlld(h))
     return launch_hlld3d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->d.kx,
                          h->mfdim, h->ax.a, h->ay.a, h->az.a, h->ph.gm, h->mu, dt,
-                         ctl, h->s);
+                         ctl, h->s, h->df);
   if (is_roe(h) && h->ndim == 2)
     return launch_roe2d(h->d.exact != 0, A, B, h->roe, h->d.ix, h->d.jx, h->ax.a,
                         h->ay.a, h->ph, dt, ctl, box, h->s, h->df);
@@ -2011,7 +2012,7 @@ extern "C" int cans_run_set_tile(cans_run *h, int tile) {
 extern "C" int cans_run_set_df64(cans_run *h, int on) {
   if (!h) return CANS_ERR_ARG;
   if (on && ((h->d.solver != CANS_SOLVER_MLW_M3_2D && h->d.solver != CANS_SOLVER_MLW_M_3D &&
-              !is_roe(h)) ||
+              !is_roe(h) && !is_hlld(h)) ||
              h->d.exact || h->grav || h->eta))
     return CANS_ERR_ARG;
   if (h->df != (on != 0)) {

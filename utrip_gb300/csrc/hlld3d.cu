@@ -17,6 +17,9 @@
 //
 // The normal-field flux of an axis is zero (hlld_mh.f:74,91,108), so that
 // component is not updated in its own pass.
+//
+// The double-float policy (QF) evaluates the face flux in double-float
+// arithmetic on the FP32 pipes; face states, updates and primitives stay FP64.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -117,7 +120,7 @@ __device__ __forceinline__ double minmod(double a, double b) {
   return x >= 0 ? copysign(fmin(fabs(a), fabs(b)), a) : 0.0;
 }
 
-template <bool E, int STAGE>
+template <bool E, int STAGE, bool QF>
 __global__ void __launch_bounds__(kThreads)
     k_hlld_flux(const double *__restrict__ P, double *__restrict__ Fl, Geo g,
                 HlldK K, const Ctl *ctl) {
@@ -174,7 +177,8 @@ __global__ void __launch_bounds__(kThreads)
     // bb: the cell-centred normal field of the stage input averaged onto the face
     const double *bn = P + (P3::BX + a) * g.n + c;
     const double bb = ((T(__ldg(bn)) + T(__ldg(bn + s))) / T(2.0)).v;
-    hlld_flux<E>(K, L, R, bb, f);
+    if constexpr (QF) hlld_flux_t<df::DF>(K, L, R, bb, f);
+    else hlld_flux<E>(K, L, R, bb, f);
     double *Fa = Fl + (size_t)a * 8 * g.n;
     Fa[U_RO * g.n + c] = f[0];
     Fa[U_EE * g.n + c] = f[1];
@@ -274,16 +278,16 @@ Geo make_geo(int ix, int jx, int kx, const int *mfdim) {
   return g;
 }
 
-template <bool E>
+template <bool E, bool QF>
 cudaError_t launch_all(const double *A, double *B, double *scratch, const Geo &g,
                        const Axis &ax, const Axis &ay, const Axis &az,
                        const HlldK &K, double mu2, double dt, const Ctl *ctl,
                        cudaStream_t s) {
   const unsigned blocks = (unsigned)((g.n + kThreads - 1) / kThreads);
   double *H = scratch, *Fl = scratch + 8 * g.n;
-  k_hlld_flux<E, 1><<<blocks, kThreads, 0, s>>>(A, Fl, g, K, ctl);
+  k_hlld_flux<E, 1, QF><<<blocks, kThreads, 0, s>>>(A, Fl, g, K, ctl);
   k_hlld_update<E, 1><<<blocks, kThreads, 0, s>>>(A, Fl, H, g, ax, ay, az, K, mu2, dt, ctl);
-  k_hlld_flux<E, 2><<<blocks, kThreads, 0, s>>>(H, Fl, g, K, ctl);
+  k_hlld_flux<E, 2, QF><<<blocks, kThreads, 0, s>>>(H, Fl, g, K, ctl);
   k_hlld_update<E, 2><<<blocks, kThreads, 0, s>>>(A, Fl, B, g, ax, ay, az, K, mu2, dt, ctl);
   count_launch(4);
   return cudaGetLastError();
@@ -296,7 +300,7 @@ size_t hlld3d_scratch_doubles(size_t ncells) { return 32 * ncells; }
 cudaError_t launch_hlld3d(bool exact, const double *A, double *B, double *scratch,
                           int ix, int jx, int kx, const int *mfdim, const Axis &ax,
                           const Axis &ay, const Axis &az, double gm, double mu,
-                          double dt, const Ctl *ctl, cudaStream_t s) {
+                          double dt, const Ctl *ctl, cudaStream_t s, bool df) {
   const Geo g = make_geo(ix, jx, kx, mfdim);
   HlldK K{};
   K.gm = gm;
@@ -304,8 +308,9 @@ cudaError_t launch_hlld3d(bool exact, const double *A, double *B, double *scratc
   K.zfloor = 1.0e-10;
   K.gm1i = 1.0 / (gm - 1.0);
   const double mu2 = 2.0 * mu;
-  return exact ? launch_all<true>(A, B, scratch, g, ax, ay, az, K, mu2, dt, ctl, s)
-               : launch_all<false>(A, B, scratch, g, ax, ay, az, K, mu2, dt, ctl, s);
+  if (exact) return launch_all<true, false>(A, B, scratch, g, ax, ay, az, K, mu2, dt, ctl, s);
+  if (df) return launch_all<false, true>(A, B, scratch, g, ax, ay, az, K, mu2, dt, ctl, s);
+  return launch_all<false, false>(A, B, scratch, g, ax, ay, az, K, mu2, dt, ctl, s);
 }
 
 cudaError_t launch_hlld3d_finish(bool exact, int ix, int jx, int kx,

@@ -6,12 +6,17 @@
 // bt1, bt2) with bn unused -- the normal field is the face value bxs; the
 // flux comes back as (ro, ee, rn, rt1, rt2, bt1, bt2).
 //
-// E=true evaluates the expressions in the Fortran order with separately
-// rounded operations.  E=false uses the same expressions with FMA
-// contraction and reciprocals in place of the repeated divisions.
+// The flux is written once for its number type T:
+//   F<true>   the exact policy: the expressions in the Fortran order with
+//             separately rounded operations;
+//   F<false>  the fast policy: the same expressions with FMA contraction and
+//             reciprocals in place of the repeated divisions;
+//   df::DF    the double-float policy: the fast policy's algebra on the FP32
+//             pipes (df64.cuh), face states and fluxes converted once.
 #pragma once
 #include "cans_common.cuh"
-#include "roe_flux.cuh"  // fmax_, fsign_
+#include "df64.cuh"
+#include "roe_flux.cuh"  // fmax_, fsign_, the double-float rcp_ and sqrt_
 
 namespace cans {
 
@@ -21,24 +26,66 @@ struct HlldK {
   double gm1i;      // fast policy: 1/(gm-1)
 };
 
-template <bool E>
-__device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
-                                          const double *R, double bxv,
-                                          double *f) {
-  using T = F<E>;
-  const T gm(K.gm), gm1(K.gm1), zf(K.zfloor);
-  const T bxs(bxv);
+// What the flux needs of its number type beyond the arithmetic operators:
+// conversion from and to the caller's doubles, the sign tests of its
+// branches and the reciprocal of the fast algebra.
+template <class T> struct HNum;
+template <bool E> struct HNum<F<E>> {
+  static constexpr bool exact = E;
+  static __device__ __forceinline__ F<E> in(double x) { return F<E>(x); }
+  static __device__ __forceinline__ double out(F<E> x) { return x.v; }
+  static __device__ __forceinline__ bool ge0(F<E> x) { return x.v >= 0.0; }
+  static __device__ __forceinline__ bool gt0(F<E> x) { return x.v > 0.0; }
+  static __device__ __forceinline__ bool le0(F<E> x) { return x.v <= 0.0; }
+  static __device__ __forceinline__ F<E> rcp(F<E> x) { return F<E>(1.0) / x; }
+};
+// a normalised double-float carries its sign in the head (a zero head has a
+// zero tail)
+template <> struct HNum<df::DF> {
+  static constexpr bool exact = false;
+  static __device__ __forceinline__ df::DF in(double x) { return num_in<df::DF>(x); }
+  static __device__ __forceinline__ double out(df::DF x) { return num_out(x); }
+  static __device__ __forceinline__ bool ge0(df::DF x) { return !(x.d.h < 0.0f); }
+  static __device__ __forceinline__ bool gt0(df::DF x) { return x.d.h > 0.0f; }
+  static __device__ __forceinline__ bool le0(df::DF x) { return !(x.d.h > 0.0f); }
+  static __device__ __forceinline__ df::DF rcp(df::DF x) { return rcp_(x); }
+};
+// Fortran max, min, sign, abs and sqrt of double-floats, in the forms the
+// F<E> versions take
+__device__ __forceinline__ df::DF fmax_(df::DF a, df::DF b) {
+  return df::gt(a.d, b.d) ? a : b;
+}
+__device__ __forceinline__ df::DF fmin_(df::DF a, df::DF b) {
+  return df::gt(b.d, a.d) ? a : b;
+}
+__device__ __forceinline__ df::DF fsign_(df::DF a, df::DF b) {
+  const df::D m = df::absd(a.d);
+  return df::DF(signbit(b.d.h) ? df::neg(m) : m);
+}
+__device__ __forceinline__ df::DF fabs_(df::DF a) { return df::DF(df::absd(a.d)); }
+__device__ __forceinline__ df::DF fsqrt(df::DF a) { return sqrt_(a); }
+
+template <class T>
+__device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
+                                            const double *R, double bxv,
+                                            double *f) {
+  using N = HNum<T>;
+  constexpr bool E = N::exact;
+  const T gm = N::in(K.gm), gm1 = N::in(K.gm1), zf = N::in(K.zfloor);
+  const T bxs = N::in(bxv);
   const T bxsq = bxs * bxs;
   // left and right states (:152-191)
-  const T rol(L[0]), prl(L[1]), vxl(L[2]), vyl(L[3]), vzl(L[4]), byl(L[6]), bzl(L[7]);
-  const T ror(R[0]), prr(R[1]), vxr(R[2]), vyr(R[3]), vzr(R[4]), byr(R[6]), bzr(R[7]);
+  const T rol = N::in(L[0]), prl = N::in(L[1]), vxl = N::in(L[2]), vyl = N::in(L[3]),
+          vzl = N::in(L[4]), byl = N::in(L[6]), bzl = N::in(L[7]);
+  const T ror = N::in(R[0]), prr = N::in(R[1]), vxr = N::in(R[2]), vyr = N::in(R[3]),
+          vzr = N::in(R[4]), byr = N::in(R[6]), bzr = N::in(R[7]);
   const T pbl = T(0.5) * (bxs * bxs + byl * byl + bzl * bzl);
   const T ptl = prl + pbl;
   T eel, eer;
   if constexpr (E) {
     eel = prl / gm1 + T(0.5) * rol * (vxl * vxl + vyl * vyl + vzl * vzl) + pbl;
   } else {
-    eel = prl * T(K.gm1i) + T(0.5) * rol * (vxl * vxl + vyl * vyl + vzl * vzl) + pbl;
+    eel = prl * N::in(K.gm1i) + T(0.5) * rol * (vxl * vxl + vyl * vyl + vzl * vzl) + pbl;
   }
   const T rxl = rol * vxl, ryl = rol * vyl, rzl = rol * vzl;
   const T pbr = T(0.5) * (bxs * bxs + byr * byr + bzr * bzr);
@@ -46,7 +93,7 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
   if constexpr (E) {
     eer = prr / gm1 + T(0.5) * (ror * (vxr * vxr + vyr * vyr + vzr * vzr)) + pbr;
   } else {
-    eer = prr * T(K.gm1i) + T(0.5) * (ror * (vxr * vxr + vyr * vyr + vzr * vzr)) + pbr;
+    eer = prr * N::in(K.gm1i) + T(0.5) * (ror * (vxr * vxr + vyr * vyr + vzr * vzr)) + pbr;
   }
   const T rxr = ror * vxr, ryr = ror * vyr, rzr = ror * vzr;
   // wave speeds (:197-207)
@@ -73,14 +120,14 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
   const T fbyr = byr * vxr - bxs * vyr;
   const T fbzr = bzr * vxr - bxs * vzr;
   // supersonic cases (:235-255)
-  if (sl.v >= 0.0) {
-    f[0] = frol.v; f[1] = feel.v; f[2] = frxl.v; f[3] = fryl.v; f[4] = frzl.v;
-    f[5] = fbyl.v; f[6] = fbzl.v;
+  if (N::ge0(sl)) {
+    f[0] = N::out(frol); f[1] = N::out(feel); f[2] = N::out(frxl); f[3] = N::out(fryl);
+    f[4] = N::out(frzl); f[5] = N::out(fbyl); f[6] = N::out(fbzl);
     return;
   }
-  if (sr.v <= 0.0) {
-    f[0] = fror.v; f[1] = feer.v; f[2] = frxr.v; f[3] = fryr.v; f[4] = frzr.v;
-    f[5] = fbyr.v; f[6] = fbzr.v;
+  if (N::le0(sr)) {
+    f[0] = N::out(fror); f[1] = N::out(feer); f[2] = N::out(frxr); f[3] = N::out(fryr);
+    f[4] = N::out(frzr); f[5] = N::out(fbyr); f[6] = N::out(fbzr);
     return;
   }
   // contact speed and star total pressure (:260-275)
@@ -91,7 +138,7 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
     sm = (sdr * ror * vxr - sdl * rol * vxl - ptr + ptl) / den;
     ptst = (sdr * ror * ptl - sdl * rol * ptr + rol * ror * sdr * sdl * (vxr - vxl)) / den;
   } else {
-    const T di = T(1.0) / den;
+    const T di = N::rcp(den);
     sm = (sdr * ror * vxr - sdl * rol * vxl - ptr + ptl) * di;
     ptst = (sdr * ror * ptl - sdl * rol * ptr + rol * ror * sdr * sdl * (vxr - vxl)) * di;
   }
@@ -114,10 +161,10 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
       tmp2 = (ro * (sd * sd) - bxsq) / dd;
       rsd = ro * sd / sdm;
     } else {
-      const T ddi = T(1.0) / dd;
+      const T ddi = N::rcp(dd);
       tmp = bxs * (sd - sdm) * ddi;
       tmp2 = (ro * (sd * sd) - bxsq) * ddi;
-      rsd = ro * sd * (T(1.0) / sdm);
+      rsd = ro * sd * N::rcp(sdm);
     }
     rost[s] = mx * rsd - mn * ro;
     const T vxst = mx * sm - mn * vx;
@@ -131,7 +178,7 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
     vdbst[s] = vxst * bxs + vyst[s] * byst[s] + vzst[s] * bzst[s];
     const T num = sd * ee - pt * vx + ptst * sm + bxs * (vx * bxs + vy * by + vz * bz - vdbst[s]);
     if constexpr (E) esd = num / sdm;
-    else esd = num * (T(1.0) / sdm);
+    else esd = num * N::rcp(sdm);
     eest[s] = mx * esd - mn * ee;
   }
   // double-star states (:347-414)
@@ -141,8 +188,8 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
     slst = sm - fabs_(bxs) / sqrtrol;
     srst = sm + fabs_(bxs) / sqrtror;
   } else {
-    slst = sm - fabs_(bxs) * (T(1.0) / sqrtrol);
-    srst = sm + fabs_(bxs) * (T(1.0) / sqrtror);
+    slst = sm - fabs_(bxs) * N::rcp(sqrtrol);
+    srst = sm + fabs_(bxs) * N::rcp(sqrtror);
   }
   T ryd[2], rzd[2], byd, bzd, eed[2];
   if (bxv == 0.0) {
@@ -152,7 +199,7 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
     byd = byst[0];  // unused: the flux takes byst of each side below
     bzd = bzst[0];
   } else {
-    const T invsumro = T(1.0) / (sqrtrol + sqrtror);
+    const T invsumro = N::rcp(sqrtrol + sqrtror);
     const T signbx = fsign_(T(1.0), bxs);
     const T vyd = invsumro * (sqrtrol * vyst[0] + sqrtror * vyst[1] + signbx * (byst[1] - byst[0]));
     ryd[0] = rost[0] * vyd;
@@ -170,43 +217,50 @@ __device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
   }
   const bool zb = bxv == 0.0;
   // flux (:446-480)
-  if (slst.v >= 0.0) {
-    f[0] = (frol + sl * (rost[0] - rol)).v;
-    f[2] = (frxl + sl * (rxst[0] - rxl)).v;
-    f[3] = (fryl + sl * (ryst[0] - ryl)).v;
-    f[4] = (frzl + sl * (rzst[0] - rzl)).v;
-    f[1] = (feel + sl * (eest[0] - eel)).v;
-    f[5] = (fbyl + sl * (byst[0] - byl)).v;
-    f[6] = (fbzl + sl * (bzst[0] - bzl)).v;
-  } else if (sm.v >= 0.0) {
+  if (N::ge0(slst)) {
+    f[0] = N::out(frol + sl * (rost[0] - rol));
+    f[2] = N::out(frxl + sl * (rxst[0] - rxl));
+    f[3] = N::out(fryl + sl * (ryst[0] - ryl));
+    f[4] = N::out(frzl + sl * (rzst[0] - rzl));
+    f[1] = N::out(feel + sl * (eest[0] - eel));
+    f[5] = N::out(fbyl + sl * (byst[0] - byl));
+    f[6] = N::out(fbzl + sl * (bzst[0] - bzl));
+  } else if (N::ge0(sm)) {
     const T temp = slst - sl;
     const T byd0 = zb ? byst[0] : byd, bzd0 = zb ? bzst[0] : bzd;
-    f[0] = (frol - sl * rol - temp * rost[0] + slst * rost[0]).v;
-    f[2] = (frxl - sl * rxl - temp * rxst[0] + slst * rxst[0]).v;
-    f[3] = (fryl - sl * ryl - temp * ryst[0] + slst * ryd[0]).v;
-    f[4] = (frzl - sl * rzl - temp * rzst[0] + slst * rzd[0]).v;
-    f[1] = (feel - sl * eel - temp * eest[0] + slst * eed[0]).v;
-    f[5] = (fbyl - sl * byl - temp * byst[0] + slst * byd0).v;
-    f[6] = (fbzl - sl * bzl - temp * bzst[0] + slst * bzd0).v;
-  } else if (srst.v > 0.0) {
+    f[0] = N::out(frol - sl * rol - temp * rost[0] + slst * rost[0]);
+    f[2] = N::out(frxl - sl * rxl - temp * rxst[0] + slst * rxst[0]);
+    f[3] = N::out(fryl - sl * ryl - temp * ryst[0] + slst * ryd[0]);
+    f[4] = N::out(frzl - sl * rzl - temp * rzst[0] + slst * rzd[0]);
+    f[1] = N::out(feel - sl * eel - temp * eest[0] + slst * eed[0]);
+    f[5] = N::out(fbyl - sl * byl - temp * byst[0] + slst * byd0);
+    f[6] = N::out(fbzl - sl * bzl - temp * bzst[0] + slst * bzd0);
+  } else if (N::gt0(srst)) {
     const T temp = srst - sr;
     const T byd1 = zb ? byst[1] : byd, bzd1 = zb ? bzst[1] : bzd;
-    f[0] = (fror - sr * ror - temp * rost[1] + srst * rost[1]).v;
-    f[2] = (frxr - sr * rxr - temp * rxst[1] + srst * rxst[1]).v;
-    f[3] = (fryr - sr * ryr - temp * ryst[1] + srst * ryd[1]).v;
-    f[4] = (frzr - sr * rzr - temp * rzst[1] + srst * rzd[1]).v;
-    f[1] = (feer - sr * eer - temp * eest[1] + srst * eed[1]).v;
-    f[5] = (fbyr - sr * byr - temp * byst[1] + srst * byd1).v;
-    f[6] = (fbzr - sr * bzr - temp * bzst[1] + srst * bzd1).v;
+    f[0] = N::out(fror - sr * ror - temp * rost[1] + srst * rost[1]);
+    f[2] = N::out(frxr - sr * rxr - temp * rxst[1] + srst * rxst[1]);
+    f[3] = N::out(fryr - sr * ryr - temp * ryst[1] + srst * ryd[1]);
+    f[4] = N::out(frzr - sr * rzr - temp * rzst[1] + srst * rzd[1]);
+    f[1] = N::out(feer - sr * eer - temp * eest[1] + srst * eed[1]);
+    f[5] = N::out(fbyr - sr * byr - temp * byst[1] + srst * byd1);
+    f[6] = N::out(fbzr - sr * bzr - temp * bzst[1] + srst * bzd1);
   } else {
-    f[0] = (fror + sr * (rost[1] - ror)).v;
-    f[2] = (frxr + sr * (rxst[1] - rxr)).v;
-    f[3] = (fryr + sr * (ryst[1] - ryr)).v;
-    f[4] = (frzr + sr * (rzst[1] - rzr)).v;
-    f[1] = (feer + sr * (eest[1] - eer)).v;
-    f[5] = (fbyr + sr * (byst[1] - byr)).v;
-    f[6] = (fbzr + sr * (bzst[1] - bzr)).v;
+    f[0] = N::out(fror + sr * (rost[1] - ror));
+    f[2] = N::out(frxr + sr * (rxst[1] - rxr));
+    f[3] = N::out(fryr + sr * (ryst[1] - ryr));
+    f[4] = N::out(frzr + sr * (rzst[1] - rzr));
+    f[1] = N::out(feer + sr * (eest[1] - eer));
+    f[5] = N::out(fbyr + sr * (byst[1] - byr));
+    f[6] = N::out(fbzr + sr * (bzst[1] - bzr));
   }
+}
+
+template <bool E>
+__device__ __forceinline__ void hlld_flux(const HlldK &K, const double *L,
+                                          const double *R, double bxv,
+                                          double *f) {
+  hlld_flux_t<F<E>>(K, L, R, bxv, f);
 }
 
 }  // namespace cans

@@ -108,16 +108,16 @@ cudaError_t launch_sel(int tile, const double *A, double *B, int ix, int jx,
 
 // tile 6: the y-marching kernel of the fast mlw_m3 step (mlw2d_df.cu); the
 // exact policy and mlw_m take the 32 x 9 tile in its place
-int mlw2d_tile_count() { return 7; }
+int mlw2d_tile_count() { return 8; }
 
 cudaError_t launch_mlw2d(int solver, bool exact, int tile, const double *A,
                          double *B, int ix, int jx, const Axis &ax,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl,
                          Box3 box, cudaStream_t s) {
   if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
-  if (tile == 6) {
+  if (tile >= 6) {  // the y-marching tile (segments balanced per SM, or by waves)
     if (solver == 1 && !exact)
-      return launch_mlw2d_march_fast(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+      return launch_mlw2d_march_fast(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s, tile == 7);
     tile = 4;
   }
   if (solver == 1) {
@@ -188,60 +188,79 @@ cudaError_t launch_cfl2d_full(int solver, bool exact, const double *S, int ix,
 // iteration by the last block to finish.
 // With all = 1 the CFL covers every cell: a loop whose chkdav changes cells
 // after the step reduces its CFL here alone.
+
+// Cell (i, j) of frame index f: rows j < w or j >= jx-w (all i), then
+// columns i < w or i >= ix-w of the remaining rows (every cell with all).
+__device__ __forceinline__ void frame_cell(long long f, int ix, int jx, int w, int all,
+                                           int &i, int &j) {
+  const long long nrow = 2LL * w * ix;
+  if (all) {
+    i = (int)(f % ix);
+    j = (int)(f / ix);
+  } else if (f < nrow) {
+    const long long r = f / ix;
+    i = (int)(f % ix);
+    j = (r < w) ? (int)r : (int)(jx - 2 * w + r);
+  } else {
+    const long long q = f - nrow;
+    const long long r = q / (2 * w);
+    const int cidx = (int)(q % (2 * w));
+    j = (int)(w + r);
+    i = (cidx < w) ? cidx : (ix - 2 * w + cidx);
+  }
+}
+__host__ __device__ __forceinline__ long long frame_cells(int ix, int jx, int w, int all) {
+  const long long inner_rows = jx - 2LL * w;
+  return all ? (long long)ix * jx
+             : 2LL * w * ix + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
+}
+
+// cfl_m3 (cfl_m for the 8-array layout) of one cell: safety * the cell's
+// time-step limit; bad is set for a cell the CFL cannot use.
+template <bool E, bool M3>
+__device__ __forceinline__ double frame_dtq(const double *__restrict__ S, size_t n, int i,
+                                            int j, int ix, const Axis &ax, const Axis &ay,
+                                            const Phys &ph, double safety, bool &bad) {
+  using FT = F<E>;
+  using P = Prim<M3>;
+  const FT gm(ph.gm), pi4i(ph.pi4i);
+  const size_t g = (size_t)i + (size_t)j * ix;
+  const FT ro(S[P::RO * n + g]), pr(S[P::PR * n + g]);
+  const FT vx(S[P::VX * n + g]), vy(S[P::VY * n + g]);
+  const FT bx(S[P::BX * n + g]), by(S[P::BY * n + g]);
+  FT b2, v2;
+  if constexpr (M3) {
+    const FT vz(S[P::VZ * n + g]), bz(S[P::BZ * n + g]);
+    b2 = bx * bx + by * by + bz * bz;
+    v2 = vx * vx + vy * vy + vz * vz;
+  } else {
+    b2 = bx * bx + by * by;
+    v2 = vx * vx + vy * vy;
+  }
+  const FT ca2 = b2 * pi4i / ro;
+  const FT cs2 = gm * pr / ro;
+  const FT dtcfl = fmin_(FT(ax.d[i]), FT(ay.d[j])) / fsqrt(v2 + cs2 + ca2);
+  const double dtq = (FT(safety) * dtcfl).v;
+  bad |= bad_cell(ro.v, pr.v, dtq);
+  return dtq;
+}
+
 template <bool E, bool M3>
 __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
                           Axis ax, Axis ay, Phys ph, int w, int all, Ctl *ctl) {
-  using FT = F<E>;
-  using P = Prim<M3>;
   __shared__ double red[32];
   if (ctl->done | ctl->pause) return;
   S = ctl->buf[ctl->cur ^ 1];  // the state the step just wrote
   const size_t n = (size_t)ix * jx;
-  // frame = rows j < w or j >= jx-w (all i), plus columns i < w or
-  // i >= ix-w of the remaining rows
-  const long long nrow = 2LL * w * ix;
-  const long long inner_rows = jx - 2LL * w;
-  const long long total =
-      all ? (long long)ix * jx : nrow + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
+  const long long total = frame_cells(ix, jx, w, all);
   double dmin = __longlong_as_double(0x7ff0000000000000LL);
   bool bad = false;
-  const FT gm(ph.gm), pi4i(ph.pi4i);
   for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
        f < total; f += (long long)gridDim.x * blockDim.x) {
     int i, j;
-    if (all) {
-      i = (int)(f % ix);
-      j = (int)(f / ix);
-    } else if (f < nrow) {
-      const long long r = f / ix;
-      i = (int)(f % ix);
-      j = (r < w) ? (int)r : (int)(jx - 2 * w + r);
-    } else {
-      const long long q = f - nrow;
-      const long long r = q / (2 * w);
-      const int cidx = (int)(q % (2 * w));
-      j = (int)(w + r);
-      i = (cidx < w) ? cidx : (ix - 2 * w + cidx);
-    }
-    const size_t g = (size_t)i + (size_t)j * ix;
-    const FT ro(S[P::RO * n + g]), pr(S[P::PR * n + g]);
-    const FT vx(S[P::VX * n + g]), vy(S[P::VY * n + g]);
-    const FT bx(S[P::BX * n + g]), by(S[P::BY * n + g]);
-    FT b2, v2;
-    if constexpr (M3) {
-      const FT vz(S[P::VZ * n + g]), bz(S[P::BZ * n + g]);
-      b2 = bx * bx + by * by + bz * bz;
-      v2 = vx * vx + vy * vy + vz * vz;
-    } else {
-      b2 = bx * bx + by * by;
-      v2 = vx * vx + vy * vy;
-    }
-    const FT ca2 = b2 * pi4i / ro;
-    const FT cs2 = gm * pr / ro;
-    const FT dtcfl = fmin_(FT(ax.d[i]), FT(ay.d[j])) / fsqrt(v2 + cs2 + ca2);
-    const double dtq = (FT(ctl->safety) * dtcfl).v;
+    frame_cell(f, ix, jx, w, all, i, j);
+    const double dtq = frame_dtq<E, M3>(S, n, i, j, ix, ax, ay, ph, ctl->safety, bad);
     if (dtq < dmin) dmin = dtq;
-    bad |= bad_cell(ro.v, pr.v, dtq);
   }
   count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
   block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
@@ -261,7 +280,7 @@ cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
                            const Phys &ph, int margin, Ctl *ctl,
                            cudaStream_t s, int all) {
   const int w = margin + 1;
-  const long long total = all ? (long long)ix * jx : 2LL * w * ix + 2LL * w * (jx - 2LL * w);
+  const long long total = frame_cells(ix, jx, w, all);
   int blocks = (int)((total + 255) / 256);
   if (blocks < 1) blocks = 1;
   if (blocks > (all ? 152 * 4 : 152)) blocks = all ? 152 * 4 : 152;

@@ -801,9 +801,30 @@ __global__ void __launch_bounds__(MarchD<CH>::NT, 2)
   }
 }
 
-// Rows per block of the marching kernel: a multiple of CH for which the
-// launch's waves times the block's rows (plus its two-row prologue) is least.
-inline int balance_seg(int strips, int rows, int ch, int slots) {
+// Rows per block of the marching kernel.  The step is bound by the
+// arithmetic pipes, so a launch takes as long as its busiest SM: the blocks
+// an SM gets (all blocks spread evenly over the SMs) times the rows a block
+// computes -- its segment, the two-row prologue and one row's worth of
+// barriers per chunk.  A segment need not be a whole number of chunks (its
+// last chunk may be short, as at the end of the grid).
+inline int balance_seg(int strips, int rows, int ch, int sms) {
+  int best = rows;
+  long long best_cost = -1;
+  for (int seg = ch > 1 ? ch / 2 : 1; seg <= rows; seg++) {
+    const long long blocks = (long long)strips * ((rows + seg - 1) / seg);
+    const long long per_sm = (blocks + sms - 1) / sms;
+    const long long cost = per_sm * (seg + 2 + (seg + ch - 1) / ch);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = seg;
+    }
+  }
+  return best;
+}
+// The same with whole chunks per block, balanced by waves of resident
+// blocks (slots = SMs x resident blocks per SM): for a step that is bound by
+// latency more than by one pipe, fewer and longer blocks can win.
+inline int balance_seg_waves(int strips, int rows, int ch, int slots) {
   int best = ch, best_cost = -1;
   for (int seg = ch; seg <= rows + ch - 1; seg += ch) {
     const int blocks = strips * ((rows + seg - 1) / seg);
@@ -859,33 +880,36 @@ namespace {
 template <class N, int CH>
 cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis &ax,
                          const Axis &ay, const Phys &ph, double dt, Ctl *ctl, Box3 box,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool waves = false) {
   using T = MarchD<CH>;
   static std::mutex mu;
-  static int slots_of[64] = {};
-  int dev = 0, slots = 0;
+  static int sms_of[64] = {}, slots_of[64] = {};
+  int dev = 0, sms = 0, slots = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   {
     std::lock_guard<std::mutex> lk(mu);
-    if (!slots_of[dev]) {
+    if (!sms_of[dev]) {
       e = cudaFuncSetAttribute(k_mlw2d_march<N, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)T::smem_bytes);
       if (e != cudaSuccess) return e;
-      int sms = 0, per_sm = 0;
-      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      int m = 0, per_sm = 0;
+      if ((e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
         return e;
       if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlw2d_march<N, CH>,
                                                              T::NT, T::smem_bytes)) !=
           cudaSuccess)
         return e;
-      slots_of[dev] = sms * (per_sm > 0 ? per_sm : 1);
+      sms_of[dev] = m > 0 ? m : 1;
+      slots_of[dev] = sms_of[dev] * (per_sm > 0 ? per_sm : 1);
     }
+    sms = sms_of[dev];
     slots = slots_of[dev];
   }
   const int strips = (ix - 2 + T::TX - 1) / T::TX, rows = jx - 2;
-  const int seg = balance_seg(strips, rows, CH, slots);
+  const int seg = waves ? balance_seg_waves(strips, rows, CH, slots)
+                        : balance_seg(strips, rows, CH, sms);
   dim3 grid(strips, (rows + seg - 1) / seg);
   k_mlw2d_march<N, CH><<<grid, T::NT, T::smem_bytes, s>>>(A, B, ix, jx, ax, ay, ph, dt, ctl,
                                                          box, seg);
@@ -894,14 +918,14 @@ cudaError_t launch_march(const double *A, double *B, int ix, int jx, const Axis 
 }
 }  // namespace
 
-int mlw2d_df_tile_count() { return 6; }
+int mlw2d_df_tile_count() { return 7; }
 
 // The fast policy's mlw_m3 step with the y-marching tile (FP64, F64N).
 cudaError_t launch_mlw2d_march_fast(const double *A, double *B, int ix, int jx,
                                     const Axis &ax, const Axis &ay, const Phys &ph, double dt,
-                                    Ctl *ctl, Box3 box, cudaStream_t s) {
+                                    Ctl *ctl, Box3 box, cudaStream_t s, bool waves) {
   if (ix < 3 || jx < 3) return cudaErrorInvalidValue;
-  return launch_march<F64N, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+  return launch_march<F64N, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s, waves);
 }
 
 cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx,
@@ -911,6 +935,7 @@ cudaError_t launch_mlw2d_df(int tile, const double *A, double *B, int ix, int jx
   switch (tile) {
     case 4: return launch_march<DFN, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 5: return launch_march<DFN, 6>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
+    case 6: return launch_march<DFN, 8>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s, true);
     case 1: return launch_df<32, 9, 1>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 2: return launch_df<16, 16, 2>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
     case 3: return launch_df<32, 16, 2>(A, B, ix, jx, ax, ay, ph, dt, ctl, box, s);
