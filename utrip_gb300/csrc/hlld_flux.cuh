@@ -14,6 +14,8 @@
 //   df::DF    the double-float policy: the fast policy's algebra on the FP32
 //             pipes (df64.cuh), face states and fluxes converted once.
 #pragma once
+#include <type_traits>
+
 #include "cans_common.cuh"
 #include "df64.cuh"
 #include "roe_flux.cuh"  // fmax_, fsign_, the double-float rcp_ and sqrt_
@@ -119,13 +121,18 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
   const T feer = vxr * (eer + ptr - bxsq) - bxs * (vyr * byr + vzr * bzr);
   const T fbyr = byr * vxr - bxs * vyr;
   const T fbzr = bzr * vxr - bxs * vzr;
+  // The double-float instance runs one straight-line path: its instruction
+  // footprint, not its arithmetic, bounds it, so the branches below become
+  // selects (SL: the face takes a one-sided state; the supersonic cases keep
+  // the physical flux of their side).
+  constexpr bool SL = std::is_same<T, df::DF>::value;
   // supersonic cases (:235-255)
-  if (N::ge0(sl)) {
+  if (!SL && N::ge0(sl)) {
     f[0] = N::out(frol); f[1] = N::out(feel); f[2] = N::out(frxl); f[3] = N::out(fryl);
     f[4] = N::out(frzl); f[5] = N::out(fbyl); f[6] = N::out(fbzl);
     return;
   }
-  if (N::le0(sr)) {
+  if (!SL && N::le0(sr)) {
     f[0] = N::out(fror); f[1] = N::out(feer); f[2] = N::out(frxr); f[3] = N::out(fryr);
     f[4] = N::out(frzr); f[5] = N::out(fbyr); f[6] = N::out(fbzr);
     return;
@@ -192,7 +199,7 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
     srst = sm + fabs_(bxs) * N::rcp(sqrtror);
   }
   T ryd[2], rzd[2], byd, bzd, eed[2];
-  if (bxv == 0.0) {
+  if (!SL && bxv == 0.0) {
     ryd[0] = ryst[0]; ryd[1] = ryst[1];
     rzd[0] = rzst[0]; rzd[1] = rzst[1];
     eed[0] = eest[0]; eed[1] = eest[1];
@@ -217,7 +224,33 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
   }
   const bool zb = bxv == 0.0;
   // flux (:446-480)
-  if (N::ge0(slst)) {
+  if constexpr (SL) {
+    // one side s and f = F_s + c1 (U*_s - U_s) + c2 (U**_s - U*_s): c1 = sl or
+    // sr, c2 = slst or srst in the inner fans, 0 in the outer ones (the
+    // branches of the reference, rearranged); the supersonic cases select the
+    // physical flux.  With bx = 0 the double-star state is the star state.
+    const bool right = !N::ge0(sm), sup = N::ge0(sl) || N::le0(sr);
+    const bool supr = N::le0(sr) && !N::ge0(sl);
+    const bool inner = right ? N::gt0(srst) : !N::ge0(slst);
+    const T c1 = right ? sr : sl;
+    const T c2 = inner ? (right ? srst : slst) : T(0.0f);
+    auto put = [&](int v, T fl, T fr, T ul, T ur, T usv, T udv) {
+      const T fv = (right ? fr : fl) + c1 * (usv - (right ? ur : ul)) + c2 * (udv - usv);
+      f[v] = N::out(sup ? (supr ? fr : fl) : fv);
+    };
+    // the star and double-star values of side s, picked by selects (an index
+    // into the two-element arrays would place them in local memory)
+    auto pick = [&](const T *x) { return right ? x[1] : x[0]; };
+    const T ro_s = pick(rost), ee_s = pick(eest), ry_s = pick(ryst), rz_s = pick(rzst);
+    const T by_s = pick(byst), bz_s = pick(bzst);
+    put(0, frol, fror, rol, ror, ro_s, ro_s);
+    put(1, feel, feer, eel, eer, ee_s, zb ? ee_s : pick(eed));
+    put(2, frxl, frxr, rxl, rxr, pick(rxst), pick(rxst));
+    put(3, fryl, fryr, ryl, ryr, ry_s, zb ? ry_s : pick(ryd));
+    put(4, frzl, frzr, rzl, rzr, rz_s, zb ? rz_s : pick(rzd));
+    put(5, fbyl, fbyr, byl, byr, by_s, zb ? by_s : byd);
+    put(6, fbzl, fbzr, bzl, bzr, bz_s, zb ? bz_s : bzd);
+  } else if (N::ge0(slst)) {
     f[0] = N::out(frol + sl * (rost[0] - rol));
     f[2] = N::out(frxl + sl * (rxst[0] - rxl));
     f[3] = N::out(fryl + sl * (ryst[0] - ryl));
