@@ -68,6 +68,69 @@ __device__ __forceinline__ void bd_line(int kind, int mbnd, int m0, int m1,
 #undef QL
 }
 
+// The value at position l (1-based) of a line of n values after bd_line's
+// lower-face rule and then its upper-face rule, with margin m on both faces,
+// computed without writing: get(l') supplies the line's values at positions
+// that neither rule changes.  The operations (the only arithmetic is bdfrd's)
+// are those of bd_line in the same order, so the value is the same bits.
+__device__ __forceinline__ bool bd_changes(int klo, int khi, int m, int n, int l) {
+  return (klo >= 0 && (l <= m || (klo == BD_SMN && l == 1 + m))) ||
+         (khi >= 0 && (l > n - m || (khi == BD_SMN && l == n - m)));
+}
+template <class G>
+__device__ __forceinline__ double bd_value(int klo, int khi, int m, int n, double q0lo,
+                                           double q0hi, const double *dxm, int l, G get) {
+  // after the lower-face rule
+  auto vlo = [&](int p) -> double {
+    const int b = 1 + m;
+    if (klo >= 0 && p <= m) {
+      const int i = b - p;
+      switch (klo) {
+        case BD_PER: return get(p + n - 2 * m);
+        case BD_SPP: return get(b - 1 + i);
+        case BD_SPN: return -get(b - 1 + i);
+        case BD_SMP: return get(b + i);
+        case BD_SMN: return -get(b + i);
+        case BD_FRE: return get(b);
+        case BD_CNS: return q0lo;
+        case BD_FRD: {
+          const double qb = get(b);
+          const double dqq = __ddiv_rn(__dsub_rn(get(b + 1), qb), dxm[b - 1]);
+          double v = qb;
+          for (int k = 1; k <= i; k++) v = __dsub_rn(v, __dmul_rn(dqq, dxm[b - k - 1]));
+          return v;
+        }
+        default: break;
+      }
+    }
+    if (klo == BD_SMN && p == b) return 0.0;
+    return get(p);
+  };
+  const int b = n - m;
+  if (khi >= 0 && l > b) {
+    const int i = l - b;
+    switch (khi) {
+      case BD_PER: return vlo(l - (n - 2 * m));
+      case BD_SPP: return vlo(b + 1 - i);
+      case BD_SPN: return -vlo(b + 1 - i);
+      case BD_SMP: return vlo(b - i);
+      case BD_SMN: return -vlo(b - i);
+      case BD_FRE: return vlo(b);
+      case BD_CNS: return q0hi;
+      case BD_FRD: {
+        const double qb = vlo(b);
+        const double dqq = __ddiv_rn(__dsub_rn(qb, vlo(b - 1)), dxm[b - 2]);
+        double v = qb;
+        for (int k = 1; k <= i; k++) v = __dadd_rn(v, __dmul_rn(dqq, dxm[b + k - 2]));
+        return v;
+      }
+      default: break;
+    }
+  }
+  if (khi == BD_SMN && l == b) return 0.0;
+  return vlo(l);
+}
+
 // Lines along `axis` of an (n0, n1, n2) array: line index -> base offset.
 __device__ __forceinline__ size_t line_base(int axis, long long line, int n0,
                                             int n1) {

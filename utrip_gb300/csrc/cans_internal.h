@@ -117,6 +117,13 @@ cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,
                            int jx, const Axis &ax, const Axis &ay,
                            const Phys &ph, int margin, Ctl *ctl,
                            cudaStream_t s, int all = 0);
+// launch_bc2d (with ctl) followed by launch_frame2d (all = 0) as one launch:
+// the boundary program of the state the step just wrote, the frame CFL and
+// the end of the loop iteration.  nvar must be that of the solver's layout
+// (9 or 7) and each extent at least 2 margin + 3.
+cudaError_t launch_bcframe2d(int solver, bool exact, int nvar, int ix, int jx, const Axis &ax,
+                             const Axis &ay, const Phys &ph, const BcTable &bc, Ctl *ctl,
+                             cudaStream_t s);
 
 // ---- 3-D ------------------------------------------------------------------
 // mlw_m 3-D on 8 arrays (ro,pr,vx,vy,vz,bx,by,bz) of ix*jx*kx doubles.

@@ -1609,6 +1609,13 @@ cudaError_t cfl_full_kernel(cans_run *h, const double *S, double safety,
 // frame CFL (+ start of the next iteration).
 int enqueue_iteration(cans_run *h) {
   CK(step_kernel(h, h->tile, nullptr, nullptr, 0.0, h->ctl, inner_box(h)));
+  if (h->ndim == 2 && !h->d.chkdav && h->nvar == (layout2d(h) == 1 ? 9 : 7) &&
+      h->d.ix >= 2 * h->bc.margin + 3 && h->d.jx >= 2 * h->bc.margin + 3) {
+    // boundary program, frame CFL and loop end in one launch
+    CK(launch_bcframe2d(layout2d(h), h->d.exact != 0, h->nvar, h->d.ix, h->d.jx, h->ax.a,
+                        h->ay.a, h->ph, h->bc, h->ctl, h->s));
+    return CANS_OK;
+  }
   CK(bc_kernels(h, nullptr, h->ctl));
   // chkdav of ro, then pr, after the boundary fill (cans2d/md_efr/hdmlw/
   // main.f:183-185): velocities zeroed where a floor applies (vx, vy in 2-D,

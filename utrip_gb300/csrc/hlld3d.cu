@@ -19,7 +19,9 @@
 // component is not updated in its own pass.
 //
 // The double-float policy (QF) evaluates the face flux in double-float
-// arithmetic on the FP32 pipes; face states, updates and primitives stay FP64.
+// arithmetic on the FP32 pipes, and a face whose star state is
+// ill-conditioned for it (hlld_flux_t) in FP64; face states, updates and
+// primitives stay FP64.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -177,8 +179,13 @@ __global__ void __launch_bounds__(kThreads)
     // bb: the cell-centred normal field of the stage input averaged onto the face
     const double *bn = P + (P3::BX + a) * g.n + c;
     const double bb = ((T(__ldg(bn)) + T(__ldg(bn + s))) / T(2.0)).v;
-    if constexpr (QF) hlld_flux_t<df::DF>(K, L, R, bb, f);
-    else hlld_flux<E>(K, L, R, bb, f);
+    if constexpr (QF) {
+      bool ill = false;
+      hlld_flux_t<df::DF>(K, L, R, bb, f, &ill);
+      if (ill) hlld_flux<false>(K, L, R, bb, f);  // ill-conditioned: FP64
+    } else {
+      hlld_flux<E>(K, L, R, bb, f);
+    }
     double *Fa = Fl + (size_t)a * 8 * g.n;
     Fa[U_RO * g.n + c] = f[0];
     Fa[U_EE * g.n + c] = f[1];

@@ -67,10 +67,15 @@ __device__ __forceinline__ df::DF fsign_(df::DF a, df::DF b) {
 __device__ __forceinline__ df::DF fabs_(df::DF a) { return df::DF(df::absd(a.d)); }
 __device__ __forceinline__ df::DF fsqrt(df::DF a) { return sqrt_(a); }
 
+// ill (double-float instance): set when a subsonic face's star state is
+// ill-conditioned for double-float -- its denominator
+// ro (S - vn)(S - S_M) - bn^2 a difference of nearly equal terms, below
+// kIllCond of them, where the star state's error grows as the rounding unit
+// over that ratio -- so that the caller evaluates the face in FP64.
 template <class T>
 __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
                                             const double *R, double bxv,
-                                            double *f) {
+                                            double *f, bool *ill = nullptr) {
   using N = HNum<T>;
   constexpr bool E = N::exact;
   const T gm = N::in(K.gm), gm1 = N::in(K.gm1), zf = N::in(K.zfloor);
@@ -153,12 +158,19 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
   // one-sided star state (:281-342); side 0 left, 1 right
   T rost[2], rxst[2], ryst[2], rzst[2], vyst[2], vzst[2], byst[2], bzst[2], eest[2];
   T vdbst[2];
+  bool illv = false;
 #pragma unroll
   for (int s = 0; s < 2; s++) {
     const T ro = s ? ror : rol, vx = s ? vxr : vxl, vy = s ? vyr : vyl, vz = s ? vzr : vzl;
     const T by = s ? byr : byl, bz = s ? bzr : bzl, pt = s ? ptr : ptl, ee = s ? eer : eel;
     const T sd = s ? sdr : sdl, sdm = s ? sdmr : sdml;
     const T temp_fst = ro * sd * sdm - bxsq;
+    if constexpr (std::is_same<T, df::DF>::value) {
+      if (ill != nullptr) {
+        const float big = fabsf(ro.d.h * sd.d.h * sdm.d.h) + bxsq.d.h;
+        if (!(fabsf(temp_fst.d.h) >= kIllCond * big)) illv = true;
+      }
+    }
     const T s3 = fsign_(T(1.0), temp_fst + zf) * fsign_(T(1.0), temp_fst - zf);
     const T mx = fmax_(T(0.0), s3), mn = fmin_(T(0.0), s3);
     const T dd = temp_fst + mn;
@@ -189,6 +201,12 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
     eest[s] = mx * esd - mn * ee;
   }
   // double-star states (:347-414)
+  if constexpr (SL) {
+    if (ill != nullptr && illv && !(N::ge0(sl) || N::le0(sr))) {
+      *ill = true;  // the caller evaluates the face in FP64
+      return;
+    }
+  }
   const T sqrtrol = fsqrt(rost[0]), sqrtror = fsqrt(rost[1]);
   T slst, srst;
   if constexpr (E) {
@@ -230,6 +248,7 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
     // branches of the reference, rearranged); the supersonic cases select the
     // physical flux.  With bx = 0 the double-star state is the star state.
     const bool right = !N::ge0(sm), sup = N::ge0(sl) || N::le0(sr);
+    if (ill != nullptr) *ill = illv && !sup;
     const bool supr = N::le0(sr) && !N::ge0(sl);
     const bool inner = right ? N::gt0(srst) : !N::ge0(slst);
     const T c1 = right ? sr : sl;

@@ -3,6 +3,7 @@
 // (phases 1-3, one TX x TY tile) is in mlw2d_tile.cuh.
 #include <cuda_runtime.h>
 
+#include "bc_line.cuh"
 #include "cans_common.cuh"
 #include "cans_internal.h"
 #include "mlw2d_tile.cuh"
@@ -215,22 +216,22 @@ __host__ __device__ __forceinline__ long long frame_cells(int ix, int jx, int w,
              : 2LL * w * ix + (inner_rows > 0 ? inner_rows * 2LL * w : 0);
 }
 
-// cfl_m3 (cfl_m for the 8-array layout) of one cell: safety * the cell's
-// time-step limit; bad is set for a cell the CFL cannot use.
+// cfl_m3 (cfl_m for the 7-array layout) of one cell from its values q[v]:
+// safety * the cell's time-step limit; bad is set for a cell the CFL cannot
+// use.
 template <bool E, bool M3>
-__device__ __forceinline__ double frame_dtq(const double *__restrict__ S, size_t n, int i,
-                                            int j, int ix, const Axis &ax, const Axis &ay,
-                                            const Phys &ph, double safety, bool &bad) {
+__device__ __forceinline__ double cell_dtq(const double *q, int i, int j, const Axis &ax,
+                                           const Axis &ay, const Phys &ph, double safety,
+                                           bool &bad) {
   using FT = F<E>;
   using P = Prim<M3>;
   const FT gm(ph.gm), pi4i(ph.pi4i);
-  const size_t g = (size_t)i + (size_t)j * ix;
-  const FT ro(S[P::RO * n + g]), pr(S[P::PR * n + g]);
-  const FT vx(S[P::VX * n + g]), vy(S[P::VY * n + g]);
-  const FT bx(S[P::BX * n + g]), by(S[P::BY * n + g]);
+  const FT ro(q[P::RO]), pr(q[P::PR]);
+  const FT vx(q[P::VX]), vy(q[P::VY]);
+  const FT bx(q[P::BX]), by(q[P::BY]);
   FT b2, v2;
   if constexpr (M3) {
-    const FT vz(S[P::VZ * n + g]), bz(S[P::BZ * n + g]);
+    const FT vz(q[P::VZ]), bz(q[P::BZ]);
     b2 = bx * bx + by * by + bz * bz;
     v2 = vx * vx + vy * vy + vz * vz;
   } else {
@@ -243,6 +244,17 @@ __device__ __forceinline__ double frame_dtq(const double *__restrict__ S, size_t
   const double dtq = (FT(safety) * dtcfl).v;
   bad |= bad_cell(ro.v, pr.v, dtq);
   return dtq;
+}
+template <bool E, bool M3>
+__device__ __forceinline__ double frame_dtq(const double *__restrict__ S, size_t n, int i,
+                                            int j, int ix, const Axis &ax, const Axis &ay,
+                                            const Phys &ph, double safety, bool &bad) {
+  using P = Prim<M3>;
+  const size_t g = (size_t)i + (size_t)j * ix;
+  double q[P::N];
+#pragma unroll
+  for (int v = 0; v < P::N; v++) q[v] = (v == P::AZ) ? 0.0 : S[(size_t)v * n + g];
+  return cell_dtq<E, M3>(q, i, j, ax, ay, ph, safety, bad);
 }
 
 template <bool E, bool M3>
@@ -273,6 +285,112 @@ __global__ void k_frame2d(const double *__restrict__ S, int ix, int jx,
       finish_iteration(ctl);
     }
   }
+}
+
+// The value at 1-based position l of row `row` after the x rules.  Not
+// inlined: bc_xy_value calls it from each of its rule cases.
+__device__ __noinline__ double bc_x_value(const double *row, int ix, int m, int kxl, int kxh,
+                                          double q0l, double q0h, const double *dxm, int l) {
+  return bd_value(kxl, kxh, m, ix, q0l, q0h, dxm, l, [&](int p) { return row[p - 1]; });
+}
+// The value at 1-based (i, j) of one variable's array after the x rules of
+// every row and then (cy: where they change the cell) the y rules of column i.
+__device__ __noinline__ double bc_xy_value(const double *sv, int ix, int jx, int m, int kxl,
+                                           int kxh, int kyl, int kyh, double qxl, double qxh,
+                                           double qyl, double qyh, const double *dxmx,
+                                           const double *dxmy, int i, int j, bool cy) {
+  auto xval = [&](int j1) {
+    return bc_x_value(sv + (size_t)(j1 - 1) * ix, ix, m, kxl, kxh, qxl, qxh, dxmx, i);
+  };
+  if (!cy) return xval(j);
+  return bd_value(kyl, kyh, m, jx, qyl, qyh, dxmy, j, xval);
+}
+
+// The boundary program and the frame CFL of one loop iteration in one
+// launch, for a 2-D loop without chkdav.  A thread owns one frame cell and
+// computes each variable's value there as the x rules and then the y rules
+// of the program leave it (bd_value of the y rules over a column whose values
+// are bd_value of the x rules over their rows): the same operations as
+// k_bc_axis (x), k_bc_axis (y), so the same bits, with no barrier between the
+// axes.  A thread reads only cells that no rule changes (the step's output)
+// and writes only its own cell, so the threads are independent.  It then
+// reduces the CFL over the frame as k_frame2d does, from the values in
+// registers, and the last block ends the iteration.
+template <bool E, bool M3>
+__global__ void __launch_bounds__(32 * Prim<M3>::N)
+    k_bcframe2d(int ix, int jx, Axis ax, Axis ay, Phys ph, BcTable bc, Ctl *ctl) {
+  using P = Prim<M3>;
+  // a block takes 32 frame cells; thread (c, v) = (lane, warp) evaluates
+  // variable v of cell c, and the first warp reduces the CFL of the 32 cells
+  __shared__ double q[P::N][32];
+  __shared__ double red[32];
+  if (ctl->done | ctl->pause) return;
+  double *S = ctl->buf[ctl->cur ^ 1];  // the state the step just wrote
+  const size_t n = (size_t)ix * jx;
+  const int m = bc.margin, w = m + 1;
+  const long long total = frame_cells(ix, jx, w, 0);
+  const int c = threadIdx.x & 31, v = threadIdx.x >> 5;
+  double dmin = __longlong_as_double(0x7ff0000000000000LL);
+  bool bad = false;
+  for (long long f0 = blockIdx.x * 32LL; f0 < total; f0 += gridDim.x * 32LL) {
+    const long long f = f0 + c;
+    int i = 0, j = 0;
+    if (f < total) {
+      frame_cell(f, ix, jx, w, 0, i, j);
+      const double *sv = S + (size_t)v * n;
+      const int kxl = bc.kind[v][0], kxh = bc.kind[v][1];
+      const int kyl = bc.kind[v][2], kyh = bc.kind[v][3];
+      const bool cx = bd_changes(kxl, kxh, m, ix, i + 1);
+      const bool cy = bd_changes(kyl, kyh, m, jx, j + 1);
+      const double val = bc_xy_value(sv, ix, jx, m, kxl, kxh, kyl, kyh, bc.q0[v][0],
+                                     bc.q0[v][1], bc.q0[v][2], bc.q0[v][3], ax.dm, ay.dm,
+                                     i + 1, j + 1, cy);
+      if (cx || cy) S[(size_t)v * n + (size_t)i + (size_t)j * ix] = val;
+      q[v][c] = val;
+    }
+    __syncthreads();
+    if (v == 0 && f < total) {
+      double qc[P::N];
+#pragma unroll
+      for (int u = 0; u < P::N; u++) qc[u] = q[u][c];
+      const double dtq = cell_dtq<E, M3>(qc, i, j, ax, ay, ph, ctl->safety, bad);
+      if (dtq < dmin) dmin = dtq;
+    }
+    __syncthreads();
+  }
+  count_bad_block(bad, &ctl->nonfinite, threadIdx.x);
+  block_min_to(&ctl->cfl_bits, dmin, red, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&ctl->frame_blocks_done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      finish_iteration(ctl);
+    }
+  }
+}
+
+cudaError_t launch_bcframe2d(int solver, bool exact, int nvar, int ix, int jx, const Axis &ax,
+                             const Axis &ay, const Phys &ph, const BcTable &bc, Ctl *ctl,
+                             cudaStream_t s) {
+  const int need = solver == 1 ? 9 : 7;
+  if (nvar != need || ix < 2 * bc.margin + 3 || jx < 2 * bc.margin + 3)
+    return cudaErrorInvalidValue;
+  const int w = bc.margin + 1;
+  int blocks = (int)((frame_cells(ix, jx, w, 0) + 31) / 32);
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  const int nt = 32 * nvar;
+  if (solver == 1) {
+    if (exact) k_bcframe2d<true, true><<<blocks, nt, 0, s>>>(ix, jx, ax, ay, ph, bc, ctl);
+    else k_bcframe2d<false, true><<<blocks, nt, 0, s>>>(ix, jx, ax, ay, ph, bc, ctl);
+  } else {
+    if (exact) k_bcframe2d<true, false><<<blocks, nt, 0, s>>>(ix, jx, ax, ay, ph, bc, ctl);
+    else k_bcframe2d<false, false><<<blocks, nt, 0, s>>>(ix, jx, ax, ay, ph, bc, ctl);
+  }
+  count_launch();
+  return cudaGetLastError();
 }
 
 cudaError_t launch_frame2d(int solver, bool exact, const double *S, int ix,

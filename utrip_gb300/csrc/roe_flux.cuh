@@ -18,6 +18,7 @@
 // build of the same expressions).  E=false is the fast policy: the same
 // algebra with one reciprocal per repeated divisor and FMA contraction.
 #pragma once
+#include <type_traits>
 #include "cans_common.cuh"
 #include "df64.cuh"
 
@@ -278,9 +279,18 @@ template <class R> __device__ __forceinline__ RoeKR<R> roe_k(const RoeK &K) {
 // The fast flux, written once for a number type R (double: the fast policy;
 // df::DF: the double-float policy).  Literal constants are floats: exact in
 // both types.
+// Where the double-float flux hands a face to the FP64 one: the normalised
+// eigenvector weights alphf = sqrt(cf^2 - ca^2) / sqrt(cf^2 - cs_slow^2) and
+// alphs = sqrt(cf^2 - cs^2) / ... are square roots of differences of nearly
+// equal squares near the c_f = c_a and c_f = c_s degeneracies, where their
+// absolute error grows as the rounding unit / sqrt(difference / cf^2).  Below
+// kIllCond the 48-bit significand of double-float would leave it 32 times the
+// FP64 flux's; there the face is evaluated in FP64.
+constexpr float kIllCond = 1.0e-3f;
+
 template <class R, bool FIX>
 __device__ __forceinline__ void roe_flux_fast_r(const RoeKR<R> &K, const R *L, const R *Rs,
-                                                R *f) {
+                                                R *f, bool *ill = nullptr) {
   const R rl = L[0], pl = L[1], ul = L[2], vl = L[3], wl = L[4];
   const R bxl = L[5], byl = L[6], bzl = L[7];
   const R rr = Rs[0], pr = Rs[1], ur = Rs[2], vr = Rs[3], wr = Rs[4];
@@ -336,6 +346,13 @@ __device__ __forceinline__ void roe_flux_fast_r(const RoeKR<R> &K, const R *L, c
   const R cfca = max_(zero, cfast2 - ca2);
   const R cfcs = max_(zero, cfast2 - cslow2);
   const R cfa = max_(zero, cfast2 - cs2);
+  if constexpr (std::is_same<R, df::DF>::value) {
+    if (ill != nullptr) {
+      const float lim = kIllCond * cfast2.d.h;
+      *ill = !(cfca.d.h >= lim && cfa.d.h >= lim);
+      if (*ill) return;  // the caller evaluates the face in FP64
+    }
+  }
   const R rden = rsq_(cfcs + one - sp2);
   const R alphf = sp2 * (sqrt_(cfca) * rden) + one - sp2;
   const R alphs = FIX ? sp2 * (sqrt_(cfa) * rden) + one - sp2 : sp2 * (sqrt_(cfa) * rden);
@@ -412,6 +429,8 @@ __device__ __forceinline__ void roe_flux_fast(const RoeK &K, const double *L,
 
 // The double-float policy: the fast flux on the FP32 pipes, states and
 // fluxes converted once.
+// A face whose flux is ill-conditioned for double-float (kIllCond) is
+// evaluated again by the FP64 fast flux.
 template <bool FIX = true>
 __device__ __forceinline__ void roe_flux_df(const RoeK &K, const double *L,
                                             const double *R, double *f) {
@@ -421,7 +440,12 @@ __device__ __forceinline__ void roe_flux_df(const RoeK &K, const double *L,
     l[v] = num_in<df::DF>(L[v]);
     r[v] = num_in<df::DF>(R[v]);
   }
-  roe_flux_fast_r<df::DF, FIX>(roe_k<df::DF>(K), l, r, o);
+  bool ill = false;
+  roe_flux_fast_r<df::DF, FIX>(roe_k<df::DF>(K), l, r, o, &ill);
+  if (ill) {
+    roe_flux_fast_r<double, FIX>(roe_k<double>(K), L, R, f);
+    return;
+  }
 #pragma unroll
   for (int v = 0; v < 7; v++) f[v] = num_out(o[v]);
 }
