@@ -217,3 +217,24 @@ def test_df64_hlld_brio_wu_like_the_oracle(gpu, oracle_lib):
     assert merr == 0 and ns == ns_ref
     for k, a, b in zip(s["names"], got, ref):
         assert rel_linf(a, b) <= TOL, (k, rel_linf(a, b))
+
+
+@pytest.mark.parametrize("solver", ["roe_m_3d", "hlld_3d"])
+def test_df64_riemann_degenerate_faces_take_fp64(gpu, oracle_lib, solver):
+    """On the x-aligned box every x face sits at the c_f = c_a degeneracy,
+    where the reference algorithm amplifies rounding and the double-float flux
+    alone ended 3e-5 from the oracle (HLLD, 256^3, 20 steps).  With the
+    ill-conditioned faces evaluated in FP64 the double-float step stays within
+    a small factor of the FP64 fast policy there."""
+    s = setups.turbulence_3d(40, solver=solver)
+    if solver == "hlld_3d":
+        s["safety"] = 0.2
+    ref = setups.copy_state(s)
+    oracle.run_3d(s, ref, 20)
+    err = {}
+    for pol in ("fast", "df64"):
+        got = setups.copy_state(s)
+        t, ns, merr, _ = drivers.run_resident(s, got, 20, df64=pol == "df64")
+        assert merr == 0 and ns == 20
+        err[pol] = max(rel_linf(a, b) for a, b in zip(got, ref))
+    assert err["df64"] <= max(10 * err["fast"], 1e-11), err
