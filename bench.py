@@ -976,24 +976,32 @@ def one_ulp_conditioning(solver, n, steps):
 
 
 def parity_sod(stream, an, ns=(256, 512, 1024, 2048)):
-    """The md_shktb shock tube with B = 0 on the device (fast policy) in 1-D
-    (mlw_m), 2-D (mlw_m3) and 3-D (mlw_m) to tend = 0.14154: L1 distance of
-    rho, p, vx from the exact solution and the observed order."""
+    """The md_shktb shock tube with B = 0 on the device (fast policy) to
+    tend = 0.14154: L1 distance of rho, p, vx from the exact solution and the
+    observed order, for the mLW step in 1-D (mlw_m), 2-D (mlw_m3) and 3-D
+    (mlw_m), and for the Riemann-solver steps (1-D roe_m through its
+    drop-in calls, 2-D roe_m3, 3-D roe_m, the HLLD engine along x)."""
     from utrip_gb300 import drivers, setups
     out = {}
-    for ndim in (1, 2, 3):
+    cases = [(f"{d}d", lambda n, d=d: setups.sod_shock_tube(n, d)) for d in (1, 2, 3)]
+    cases += [(sv, lambda n, sv=sv: setups.sod_shock_tube_riemann(n, sv))
+              for sv in ("roe_m_1d", "roe_m3", "roe_m_3d", "hlld_3d")]
+    for name, make in cases:
         errs = []
         for n in ns:
-            s = setups.sod_shock_tube(n, ndim)
+            s = make(n)
             got = setups.copy_state(s)
-            t, nsteps, merr, _ = drivers.run_resident(s, got, 10 ** 6)
+            if s["solver"] == "roe_m_1d":
+                t, nsteps, merr, _ = drivers.run_literal(s, got, 10 ** 6, resident=True)
+            else:
+                t, nsteps, merr, _ = drivers.run_resident(s, got, 10 ** 6)
             x, dx, ro, pr, vx = setups.sod_interior_profile(s, got)
             sd = s["sod"]
             errs.append(an.l1_errors(x, dx, ro, pr, vx, t, sd["x0"], sd["gm"], sd["ro1"],
                                      sd["pr1"]))
-        out[f"{ndim}d"] = {"cells": list(ns), "l1": {k: [e[k] for e in errs] for k in errs[0]},
-                           "order": {k: an.observed_order(ns, [e[k] for e in errs])
-                                     for k in errs[0]}}
+        out[name] = {"cells": list(ns), "l1": {k: [e[k] for e in errs] for k in errs[0]},
+                     "order": {k: an.observed_order(ns, [e[k] for e in errs])
+                               for k in errs[0]}}
     return out
 
 

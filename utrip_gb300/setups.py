@@ -491,11 +491,86 @@ def sod_shock_tube(n: int = 1024, ndim: int = 1, ncross: int = 4,
                   name=f"sod_{n}x{ncross}x{ncross}_mlw_m_3d", **common)
 
 
+def sod_shock_tube_riemann(n: int = 1024, solver: str = "roe_m_3d", ncross: int = 4,
+                           safety: float | None = None):
+    """The md_shktb hydrodynamic shock tube (model.f:18-53: gamma = 1.4, left
+    rho = 1, p = 1, right rho = 0.125, p = 0.1, at rest, the interface at
+    x = 0 on a cell edge; tend = 0.14154) run by the ideal-MHD Riemann-solver
+    steps with B = 0, with their packages' three ghost layers:
+    - "roe_m_1d": the 1-D roe_m, safety 1.0 (md_shktb/hdroe/main.f:92, whose
+      1-D CFL divides by |v| + c as this one does);
+    - "roe_m3": the 2-D roe_m3 on an x-aligned tube ncross cells across;
+    - "roe_m_3d": the 3-D roe_m on an x-aligned tube ncross x ncross across;
+    - "hlld_3d": the HLLD engine along x alone (jx = kx = 1, mfdim = 1,0,0,
+      as the hdhlld-x package runs its shock tube).
+    The 2-D/3-D CFL divides by sqrt(v^2 + c^2), so those take the 0.4 of
+    their drivers.  x faces: bdsppx for every variable but vx, bdspnx for vx
+    (md_shktb bnd.f); cross axes periodic.  The exact answer is
+    oracle/shktb_analytic.py."""
+    m = 3
+    x, dx, dxm = _shktb_axis(n, margin=m)
+    left = x <= 0.0
+    ro1d = np.where(left, 1.0, 0.125)
+    pr1d = np.where(left, 1.0, 0.1)
+    common = dict(tend=0.14154, dtmin=1e-10, dtout=0.01, margin=m,
+                  sod=dict(gm=1.4, ro1=0.125, pr1=0.1, ro4=1.0, pr4=1.0, x0=0.0))
+
+    def xfaces(names, cross_faces=()):
+        bc = []
+        for v, name in enumerate(names):
+            kind = BD_SPN if name == "vx" else BD_SPP
+            bc += [(v, 0, kind, 0.0), (v, 1, kind, 0.0)]
+            bc += [(v, f, BD_PER, 0.0) for f in cross_faces]
+        return bc
+
+    if solver == "roe_m_1d":
+        names = VARS["mlw_m_1d"]
+        f = {"ro": ro1d, "pr": pr1d, "vx": np.zeros(x.size), "vy": np.zeros(x.size),
+             "by": np.zeros(x.size)}
+        state = [np.ascontiguousarray(f[k], dtype=np.float64) for k in names]
+        return dict(solver=solver, solver_id=3, names=names, x=x, dx=dx, dxm=dxm,
+                    bx=np.zeros(x.size), bxm=np.zeros(x.size), state=state, gm=1.4, qav=0.0,
+                    bc=xfaces(names), safety=1.0 if safety is None else safety,
+                    name=f"sod_{n}_roe_m_1d", **common)
+    sf = 0.4 if safety is None else safety
+    if solver == "roe_m3":
+        yc, dyc, dymc = uniform_axis(ncross, ncross * float(dxm[m]), margin=m)
+        shape = (x.size, yc.size)
+        f = {k: np.zeros(shape) for k in VARS["roe_m3"]}
+        f["ro"] = np.repeat(ro1d[:, None], shape[1], axis=1)
+        f["pr"] = np.repeat(pr1d[:, None], shape[1], axis=1)
+        return _pack("roe_m3", x, dx, dxm, yc, dyc, dymc, f, 1.4, 0.0,
+                     xfaces(VARS["roe_m3"], (2, 3)), safety=sf,
+                     name=f"sod_{n}x{ncross}_roe_m3", **common)
+    if solver == "roe_m_3d":
+        yc, dyc, dymc = uniform_axis(ncross, ncross * float(dxm[m]), margin=m)
+        shape = (x.size, yc.size, yc.size)
+        f = {k: np.zeros(shape) for k in VARS["roe_m_3d"]}
+        f["ro"] = np.broadcast_to(ro1d[:, None, None], shape).copy()
+        f["pr"] = np.broadcast_to(pr1d[:, None, None], shape).copy()
+        return _pack3(x, dx, dxm, yc, dyc, dymc, yc.copy(), dyc.copy(), dymc.copy(), f, 1.4,
+                      0.0, xfaces(VARS["roe_m_3d"], (2, 3, 4, 5)), solver="roe_m_3d",
+                      safety=sf, name=f"sod_{n}x{ncross}x{ncross}_roe_m_3d", **common)
+    if solver == "hlld_3d":
+        one = (np.array([0.5]), np.array([1.0]), np.array([1.0]))  # an inactive axis
+        shape = (x.size, 1, 1)
+        f = {k: np.zeros(shape) for k in VARS["hlld_3d"]}
+        f["ro"] = ro1d[:, None, None].copy()
+        f["pr"] = pr1d[:, None, None].copy()
+        return _pack3(x, dx, dxm, *one, *one, f, 1.4, 0.0, xfaces(VARS["hlld_3d"]),
+                      solver="hlld_3d", mu=1.0, mfdim=(1, 0, 0), safety=sf,
+                      name=f"sod_{n}_hlld", **common)
+    raise ValueError(f"no Riemann-solver shock tube for {solver!r}")
+
+
 def sod_interior_profile(setup: dict, state) -> tuple:
     """(x, dx, ro, pr, vx) along the tube's interior cells; for a 2-D or 3-D
     tube the first interior row (every row holds the same profile)."""
-    sl = slice(setup["margin"], -setup["margin"])
-    pick = {1: lambda a: a[sl], 2: lambda a: a[sl, 1], 3: lambda a: a[sl, 1, 1]}[state[0].ndim]
+    m = setup["margin"]
+    sl = slice(m, -m)
+    # the first interior cell across the tube (an inactive axis has one cell)
+    j = m if state[0].ndim > 1 and state[0].shape[1] > 2 * m else 0
+    pick = {1: lambda a: a[sl], 2: lambda a: a[sl, j], 3: lambda a: a[sl, j, j]}[state[0].ndim]
     names = setup["names"]
     return (setup["x"][sl], setup["dx"][sl], pick(state[names.index("ro")]),
             pick(state[names.index("pr")]), pick(state[names.index("vx")]))
