@@ -279,6 +279,7 @@ def extra_workloads(stream, exact=False):
         (256, 256, 64), 20, (96, 96, 16), 50, "3-D reconnection model")
     out["hlld_brio_wu_1024_to_t0.1"] = hlld_brio_wu(stream, exact)
     out["spicule_1024_100000_steps_mlw_m_bg"] = spicule_workload(stream)
+    out["spicule_beta_sweep_64x1024_2000_steps"] = spicule_beta_sweep(stream)
     out["literal_drop_in_orszag_tang_512^2"] = literal_drop_in(stream)
     out["beta_sweep_64x2d_1000_steps"] = beta_sweep(stream, exact)
     out["adjoint_shear_256^2_2000_steps"] = adjoint_workload(stream)
@@ -507,6 +508,78 @@ def spicule_workload(stream, nstop=100000, cpu_steps=4000):
                          "sample": f"first {cpu_steps} iterations of the same run"}
     res["speedup_vs_cpu_oracle"] = res["cpu_oracle"]["us_per_step"] / res["fast"]["us_per_step"]
     return res
+
+
+def spicule_beta_sweep(stream, nruns=64, steps=2000, cpu_steps=1000, seed=11):
+    """The reference's parameter studies on their own model: nruns spicule
+    runs (cans1d/md_spicule/hdmlw, 1024 cells, torque and floor on) with the
+    plasma beta at the base (model.f's onebeta) log-uniform in [0.1, 10] and
+    their own torque seeds, `steps` loop iterations each, advanced in one
+    launch (cans_run_advance_group: one cluster per run) against the same
+    runs one at a time (each run's loop as its own cluster launch, as
+    cans_run_advance gives it), and against the oracle's loop timed on one
+    host core (the reference runs each model as one serial process)."""
+    import torch
+    from utrip_gb300 import capi, drivers, setups
+    import oracle
+    rng = np.random.default_rng(seed)
+    betas = 10.0 ** rng.uniform(-1.0, 1.0, size=nruns)
+    sets = [setups.spicule_1d(1024, beta=float(b), seed=k) for k, b in enumerate(betas)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def started(s):
+        run = drivers.make_run(s, stream=stream.cuda_stream)
+        run.push(s["state"])
+        run.start(tend=s["tend"], nstop=s["nstop"], safety=s["safety"], dtmin=s["dtmin"])
+        return run
+
+    runs = [started(s) for s in sets]
+    torch.cuda.synchronize()
+    e0.record(stream)
+    capi.Run.advance_group(runs, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    group_ms = e0.elapsed_time(e1)
+    states = [r.query() for r in runs]
+    group_final = [runs[k].pull() for k in (0, nruns - 1)]
+    for r in runs:
+        r.close()
+    alone_ms, alone_final = 0.0, []
+    for k, s in enumerate(sets):
+        run = started(s)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run.advance(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        alone_ms += e0.elapsed_time(e1)
+        if k in (0, nruns - 1):
+            alone_final.append(run.pull())
+        run.close()
+    # the fast policy: the group kernel may fuse multiply-adds differently
+    # (vx of this model amplifies one rounding of the energy up to ~1e-5)
+    diff = {name: max(float(np.max(np.abs(f1[v] - f2[v]))) /
+                      max(float(np.max(np.abs(f2[v]))), 1e-300)
+                      for f1, f2 in zip(group_final, alone_final))
+            for v, name in enumerate(sets[0]["names"])}
+    ref = setups.copy_state(sets[0])
+    t0 = time.perf_counter()
+    oracle.run_spicule_c(sets[0], ref, cpu_steps)
+    cpu_us = (time.perf_counter() - t0) * 1e6 / cpu_steps
+    run_steps = nruns * steps
+    return {
+        "runs": nruns, "cells": 1024, "steps_per_run": steps,
+        "beta_range": [float(betas.min()), float(betas.max())],
+        "all_runs_completed": all(st.nexec == steps and st.merr == 0 for st in states),
+        "group_ms": group_ms, "one_at_a_time_ms": alone_ms,
+        "speedup_group_vs_one_at_a_time": alone_ms / group_ms,
+        "group_run_steps_per_s": run_steps / (group_ms * 1e-3),
+        "group_zone_updates_per_s": 1024 * run_steps / (group_ms * 1e-3),
+        "first_and_last_run_rel_linf_vs_alone": diff,
+        "cpu_oracle": {"us_per_step": cpu_us, "cores": 1,
+                       "sample": f"first {cpu_steps} iterations of the first run"},
+        "speedup_group_vs_one_cpu_core": cpu_us * run_steps / (group_ms * 1e3),
+    }
 
 
 def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=1e-6,

@@ -473,6 +473,19 @@ int cans_run_start(cans_run *h, double t0, double tend, long long nstop,
                    int pause_on_output);
 /* Enqueue up to `iters` further loop iterations (asynchronous). */
 int cans_run_advance(cans_run *h, int iters);
+/* No counterpart in the reference: its parameter studies (cans_beta_one,
+ * cans_beta_vary: cans1d/md_spicule/hdmlw at several plasma betas, the
+ * onebeta of model.f) run every 1-D model as its own process.  This advances
+ * `nruns` started 1-D runs (MLW_M_1D or MLW_M_BG_1D, all of one solver
+ * family and one arithmetic policy, each run once) by up to `iters` loop
+ * iterations each, in one kernel launch: one cluster per run, so runs too
+ * small to use the GPU alone share it.  Each run ends where its own loop
+ * would (tend, nstop, dtmin, output pause).  In the exact policy its state
+ * and loop state are those cans_run_advance gives, bit for bit; in the fast
+ * policy the group kernel may fuse multiply-adds differently, within that
+ * policy's tolerance.  Asynchronous, on the first run's stream; the other
+ * runs' streams are ordered before and after it. */
+int cans_run_advance_group(cans_run *const *runs, int nruns, int iters);
 /* Wait for the stream and read the loop state. */
 int cans_run_query(cans_run *h, cans_run_state *st);
 /* Clear a pause after the host has read the output state. */

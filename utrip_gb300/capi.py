@@ -72,6 +72,7 @@ def load() -> C.CDLL:
         "cans_run_push": (i, [vp, C.POINTER(_dp)]), "cans_run_pull": (i, [vp, C.POINTER(_dp)]),
         "cans_run_start": (i, [vp, d, d, C.c_longlong, d, d, d, i]),
         "cans_run_advance": (i, [vp, i]), "cans_run_query": (i, [vp, vp]),
+        "cans_run_advance_group": (i, [C.POINTER(vp), i, i]),
         "cans_run_resume": (i, [vp]), "cans_run_step": (i, [vp, _dp, i]),
         "cans_run_cfl": (i, [vp, d, _dp]), "cans_run_autotune": (i, [vp, i, _ip]),
         "cans_run_device_state": (i, [vp, C.POINTER(_dp)]),
@@ -687,6 +688,18 @@ class Run:
 
     def advance(self, iters: int):
         _check(self.lib.cans_run_advance(self.h, iters), "cans_run_advance")
+
+    @staticmethod
+    def advance_group(runs, iters: int):
+        """Up to `iters` loop iterations of every run in `runs` (started 1-D
+        runs of one solver family and policy), in one launch
+        (cans_run_advance_group)."""
+        runs = list(runs)
+        if not runs:
+            raise ValueError("advance_group needs at least one run")
+        arr = (C.c_void_p * len(runs))(*[r.h.value for r in runs])
+        _check(runs[0].lib.cans_run_advance_group(arr, len(runs), iters),
+               "cans_run_advance_group")
 
     def query(self) -> RunState:
         st = RunState()

@@ -259,6 +259,22 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          const Axis &ax, const Phys &ph, const BcTable &bc,
                          Ctl *ctl, int max_steps, int fixed, double dt_fixed,
                          int start, cudaStream_t s);
+// One run of a group advanced by launch_mlw1d_group (a started resident
+// loop: ctl is its control block).
+struct Run1DArgs {
+  double *S;
+  const double *bx, *bxm;
+  Loop1D opt;
+  int ix;
+  Axis ax;
+  Phys ph;
+  BcTable bc;
+  Ctl *ctl;
+};
+// Up to max_steps iterations of each run's loop, all runs in one launch (one
+// cluster per run); every run has the BG variant or none has.
+cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int nruns,
+                               int max_steps, cudaStream_t s);
 // chkdav (cans1d/common/chkdav.f:68-76) on device arrays: da below floor is
 // raised to it and vx zeroed there; the count is added to *count (device).
 // chkdav of 2-D / 3-D states (mlw1d.cu): na density-like slots a0, a1 of S

@@ -1994,6 +1994,75 @@ extern "C" int cans_run_advance(cans_run *h, int iters) {
   return CANS_OK;
 }
 
+// No counterpart in the reference, whose studies (cans_beta_one,
+// cans_beta_vary: the md_spicule model at several plasma betas) run each 1-D
+// model as its own process: many started 1-D runs advanced together, one
+// cluster per run in one launch, on the first run's stream (the others'
+// streams are ordered before and after it with events).
+extern "C" int cans_run_advance_group(cans_run *const *runs, int nruns, int iters) {
+  NvtxRange nvtx("cans_run_advance_group");
+  if (!runs || nruns < 1 || iters < 0) return CANS_ERR_ARG;
+  for (int k = 0; k < nruns; k++) {
+    const cans_run *h = runs[k];
+    if (!h || h->ndim != 1 || !h->ctl) return CANS_ERR_ARG;
+    if ((h->d.exact != 0) != (runs[0]->d.exact != 0)) return CANS_ERR_ARG;
+    if ((h->loop1d.bg != nullptr) != (runs[0]->loop1d.bg != nullptr)) return CANS_ERR_ARG;
+    for (int j = 0; j < k; j++)
+      if (runs[j] == h) return CANS_ERR_ARG;  // a run once
+  }
+  if (iters == 0) return CANS_OK;
+  std::vector<Run1DArgs> args((size_t)nruns);
+  for (int k = 0; k < nruns; k++) {
+    cans_run *h = runs[k];
+    args[k] = Run1DArgs{h->buf[0], h->bx1, h->bx1 + h->d.ix, h->loop1d, h->d.ix,
+                        h->ax.a,    h->ph,  h->bc,           h->ctl};
+  }
+  const cudaStream_t s0 = runs[0]->s;
+  std::vector<cudaEvent_t> evs;
+  auto cleanup = [&]() {
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
+  };
+  // the work already queued on every run's stream comes first
+  for (int k = 1; k < nruns; k++) {
+    if (runs[k]->s == s0) continue;
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cleanup();
+      return CANS_ERR_CUDA;
+    }
+    evs.push_back(e);
+    if (cudaEventRecord(e, runs[k]->s) != cudaSuccess ||
+        cudaStreamWaitEvent(s0, e, 0) != cudaSuccess) {
+      cleanup();
+      return CANS_ERR_CUDA;
+    }
+  }
+  cudaError_t err = launch_mlw1d_group(runs[0]->d.exact != 0, runs[0]->loop1d.bg != nullptr,
+                                       args.data(), nruns, iters, s0);
+  if (err != cudaSuccess) {
+    cleanup();
+    return err == cudaErrorInvalidValue ? CANS_ERR_ARG : CANS_ERR_CUDA;
+  }
+  // and every run's later work waits for the group
+  cudaEvent_t done;
+  if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+    cleanup();
+    return CANS_ERR_CUDA;
+  }
+  evs.push_back(done);
+  if (cudaEventRecord(done, s0) != cudaSuccess) {
+    cleanup();
+    return CANS_ERR_CUDA;
+  }
+  for (int k = 1; k < nruns; k++)
+    if (runs[k]->s != s0 && cudaStreamWaitEvent(runs[k]->s, done, 0) != cudaSuccess) {
+      cleanup();
+      return CANS_ERR_CUDA;
+    }
+  cleanup();
+  return CANS_OK;
+}
+
 extern "C" int cans_run_set_graph(cans_run *h, int use_graph) {
   if (!h) return CANS_ERR_ARG;
   h->use_graph = use_graph != 0;

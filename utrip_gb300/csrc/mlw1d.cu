@@ -28,6 +28,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "cans_common.cuh"
 #include "cans_internal.h"
 
@@ -148,8 +150,10 @@ __device__ __forceinline__ F<E> torque_add(const Run1D &p, F<E> vy, F<E> dt, lon
   return vy + dt * FT(p.trq0) * q * FT(p.trq[g]);
 }
 
+// The loop of one run on one cluster (the kernels below): p lives in the
+// kernel parameters (one run) or in shared memory (a group of runs).
 template <bool E, bool BG>
-__global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
+__device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   using FT = F<E>;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
@@ -642,6 +646,23 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
   }
 }
 
+template <bool E, bool BG>
+__global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
+  mlw1d_body<E, BG>(p);
+}
+
+// A group of independent runs, one cluster each: cluster c runs runs[c].  The
+// run's parameters are copied to shared memory once; the runs share nothing
+// else, so a cluster that finishes early leaves its SMs to the next ones.
+template <bool E, bool BG>
+__global__ void __launch_bounds__(256, 2) k_mlw1d_group(const Run1D *__restrict__ runs) {
+  __shared__ Run1D sp;
+  const unsigned c = blockIdx.x / cg::this_cluster().num_blocks();
+  if (threadIdx.x == 0) sp = runs[c];
+  __syncthreads();
+  mlw1d_body<E, BG>(sp);
+}
+
 // Smallest grid the 1-D loop kernel accepts (one block of 4 interior cells).
 int mlw1d_min_cells() { return 6; }
 
@@ -682,24 +703,17 @@ static int cluster_max(void (*kern)(Run1D), size_t smem) {
   return best;
 }
 
-// Host launcher: the cluster kernel over a state of 5 arrays of ix doubles,
-// updated in place.
-cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
-                         const double *bxm, const Loop1D &opt, int ix,
-                         const Axis &ax, const Phys &ph, const BcTable &bc,
-                         Ctl *ctl, int max_steps, int fixed, double dt_fixed,
-                         int start, cudaStream_t s) {
-  if (ix < mlw1d_min_cells()) return cudaErrorInvalidValue;
-  const bool bgv = opt.bg != nullptr;
-  // the torque reads the rr profile; the floor counts into the control block
-  if ((opt.trq && !bgv) || (opt.chk && !ctl && !fixed)) return cudaErrorInvalidValue;
-  void (*kern)(Run1D) = bgv ? (exact ? k_mlw1d<true, true> : k_mlw1d<false, true>)
-                            : (exact ? k_mlw1d<true, false> : k_mlw1d<false, false>);
-  const size_t per_cell = (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 4 : 0);
-  // shared memory of the largest block the grid can have (16 blocks)
-  const size_t smem_probe = sizeof(double) * (per_cell * ((ix - 2) / 16 + 4) + 64 + 32);
-  const int CS = cluster_for(ix, cluster_max(kern, smem_probe));
-  Run1D p{};
+namespace {
+constexpr size_t per_cell_doubles(bool bgv) {
+  return (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 4 : 0);
+}
+
+// The parameters of one run on a cluster of CS blocks; false when a block
+// would own too few cells for the boundary rules.
+bool fill_run1d(Run1D &p, double *S, const double *bx, const double *bxm, const Loop1D &opt,
+                int ix, const Axis &ax, const Phys &ph, const BcTable &bc, Ctl *ctl,
+                int max_steps, int fixed, double dt_fixed, int start, int CS) {
+  p = Run1D{};
   p.S = S; p.bx = bx; p.bxm = bxm; p.ax = ax; p.ph = ph; p.bc = bc; p.ctl = ctl;
   p.bg = opt.bg;
   p.trq = fixed ? nullptr : opt.trq;
@@ -716,13 +730,38 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
   p.dt_fixed = dt_fixed;
   p.start = start;
   // each block must own at least margin+1 cells for the boundary rules
-  if (p.q < bc.margin + 1) return cudaErrorInvalidValue;
+  if (p.q < bc.margin + 1) return false;
   // a face rule reads at most 2*margin cells in from its end of the line
   // (bdsmp*: cell b+margin); block 0 and the last block own at least q cells
   p.bnd_local = 2 * bc.margin <= p.q ? 1 : 0;
   for (int v = 0; v < NV1; v++)
     for (int f = 0; f < 2; f++)
       if (bc.kind[v][f] == BD_PER) p.bnd_local = 0;
+  return true;
+}
+}  // namespace
+
+// Host launcher: the cluster kernel over a state of 5 arrays of ix doubles,
+// updated in place.
+cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
+                         const double *bxm, const Loop1D &opt, int ix,
+                         const Axis &ax, const Phys &ph, const BcTable &bc,
+                         Ctl *ctl, int max_steps, int fixed, double dt_fixed,
+                         int start, cudaStream_t s) {
+  if (ix < mlw1d_min_cells()) return cudaErrorInvalidValue;
+  const bool bgv = opt.bg != nullptr;
+  // the torque reads the rr profile; the floor counts into the control block
+  if ((opt.trq && !bgv) || (opt.chk && !ctl && !fixed)) return cudaErrorInvalidValue;
+  void (*kern)(Run1D) = bgv ? (exact ? k_mlw1d<true, true> : k_mlw1d<false, true>)
+                            : (exact ? k_mlw1d<true, false> : k_mlw1d<false, false>);
+  const size_t per_cell = per_cell_doubles(bgv);
+  // shared memory of the largest block the grid can have (16 blocks)
+  const size_t smem_probe = sizeof(double) * (per_cell * ((ix - 2) / 16 + 4) + 64 + 32);
+  const int CS = cluster_for(ix, cluster_max(kern, smem_probe));
+  Run1D p;
+  if (!fill_run1d(p, S, bx, bxm, opt, ix, ax, ph, bc, ctl, max_steps, fixed, dt_fixed, start,
+                  CS))
+    return cudaErrorInvalidValue;
   const size_t smem = sizeof(double) * (per_cell * p.lmax + 4 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -751,6 +790,74 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
   e = cudaLaunchKernelEx(&cfg, kern, p);
   count_launch();
   if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// Host launcher of a group of runs (k_mlw1d_group): every run gets a cluster
+// of the same size CS, the smallest power of two (at most 8) that leaves
+// each block of every run at most 256 interior cells (a thread per cell, the
+// two halo cells of a full block taken in a second pass), two blocks per SM;
+// the runs' parameters go to the device in one stream-ordered allocation.
+// All runs share exact and the BG variant.
+cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int nruns,
+                               int max_steps, cudaStream_t s) {
+  if (nruns < 1) return cudaErrorInvalidValue;
+  int ixmax = 0;
+  for (int k = 0; k < nruns; k++) {
+    const Run1DArgs &a = runs[k];
+    if (a.ix < mlw1d_min_cells() || !a.ctl) return cudaErrorInvalidValue;
+    if ((a.opt.bg != nullptr) != bgv || (a.opt.trq && !bgv)) return cudaErrorInvalidValue;
+    ixmax = a.ix > ixmax ? a.ix : ixmax;
+  }
+  int CS = 1;
+  while (CS < 8 && (ixmax - 2 + CS - 1) / CS > 256) CS <<= 1;
+  std::vector<Run1D> host((size_t)nruns);
+  int lmax = 0;
+  for (int k = 0; k < nruns; k++) {
+    const Run1DArgs &a = runs[k];
+    if (!fill_run1d(host[k], a.S, a.bx, a.bxm, a.opt, a.ix, a.ax, a.ph, a.bc, a.ctl,
+                    max_steps, 0, 0.0, 0, CS) ||
+        host[k].q < 4)
+      return cudaErrorInvalidValue;
+    lmax = host[k].lmax > lmax ? host[k].lmax : lmax;
+  }
+  void (*kern)(const Run1D *) =
+      bgv ? (exact ? k_mlw1d_group<true, true> : k_mlw1d_group<false, true>)
+          : (exact ? k_mlw1d_group<true, false> : k_mlw1d_group<false, false>);
+  const size_t smem = sizeof(double) * (per_cell_doubles(bgv) * lmax + 4 * CS + 32);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  Run1D *dev = nullptr;
+  const size_t bytes = sizeof(Run1D) * (size_t)nruns;
+  if ((e = cudaMallocAsync((void **)&dev, bytes, s)) != cudaSuccess) return e;
+  // from pageable memory: the call returns once the bytes are staged, so the
+  // host vector may go
+  if ((e = cudaMemcpyAsync(dev, host.data(), bytes, cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess) {
+    cudaFreeAsync(dev, s);
+    return e;
+  }
+  int nt = ((lmax + 31) / 32) * 32;
+  nt = nt < 32 ? 32 : (nt > 256 ? 256 : nt);
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)(CS * nruns), 1, 1);
+  cfg.blockDim = dim3(nt, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, (const Run1D *)dev);
+  count_launch();
+  const cudaError_t e2 = cudaFreeAsync(dev, s);
+  if (e != cudaSuccess) return e;
+  if (e2 != cudaSuccess) return e2;
   return cudaGetLastError();
 }
 

@@ -721,7 +721,7 @@ def chkdav_host(da: np.ndarray, vx: np.ndarray, floor: float) -> int:
 
 
 def spicule_1d(nx: int = 1024, torque: float = 30.0, seed: int = 0, tend: float = 100.0,
-               nstop: int = 100000, dtout: float = 0.5):
+               nstop: int = 100000, dtout: float = 0.5, beta: float = 1.0):
     """The spicule model: cans1d/md_spicule/hdmlw/model.f with the set-up
     part of main.f (grdrdy, bnd, scrdy twice, bndsc, chkdav of ro and pr),
     margin 1, ix = nx + 2.
@@ -732,7 +732,8 @@ def spicule_1d(nx: int = 1024, torque: float = 30.0, seed: int = 0, tend: float 
     cell position, model.f:104-110), then bdspnx / bdsmnx.  A temperature
     step of width 0.5 at ztr = 15 from 1 to 300, hydrostatic density built
     outward from the base cell with ro0 = 1, p = ro T / gm.  Flux tube:
-    rr = 1, bx uniform with beta = 1 at the bottom, cross section 1/bx.
+    rr = 1, bx uniform with plasma beta `beta` at the bottom (model.f's
+    onebeta, 1.0 in the package; the studies' parameter), cross section 1/bx.
     Boundaries (bnd.f): bdsppx (vx: bdspnx) at the bottom, bdfrex at the top.
     The loop (main.f:160-219): cfl_m with safety 0.8 and dtmin 1e-10,
     mlw_m_bg with qav = 1, the torque source of trqalfven.f, bnd, chkdav of
@@ -789,7 +790,7 @@ def spicule_1d(nx: int = 1024, torque: float = 30.0, seed: int = 0, tend: float 
     pr1 = pr0 * (ro1 / ro0) * (te / te0)
     # ---- field and flux tube (model.f:150-185) -------------------------------
     pi = math.acos(-1.0)
-    onebeta = 1.0
+    onebeta = float(beta)
     bx = np.empty(ix)
     bx[0] = math.sqrt(onebeta * 8 * pi * pr1[0])
     bx[1:] = bx[0] * (rr[0] / rr[1:]) ** 2
@@ -833,7 +834,7 @@ def spicule_1d(nx: int = 1024, torque: float = 30.0, seed: int = 0, tend: float 
                 dxm=dxm, bx=bx, bxm=bxm, state=state, gm=gm, qav=1.0, margin=margin, bc=bc,
                 safety=0.8, dtmin=1e-10, tend=tend, nstop=nstop, dtout=dtout, floor=floor,
                 trq=trq, trq0=float(torque), seed=int(seed), ztr=ztr, tcor=200.0,
-                name=f"spicule_{nx}", **prof)
+                beta=float(beta), name=f"spicule_{nx}", **prof)
 
 
 # ---- 2-D steps with gravity (mlw_m_g / mlw_m3_g) -------------------------------
