@@ -55,13 +55,18 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary 3-D and 1-D workloads")
+    p.add_argument("--adjoint-export", default=None, metavar="PATH",
+                   help="run the adjoint configuration once and write its initial state, "
+                        "dt sequence, J and gradient to PATH (.npz) for the long-double "
+                        "finite-difference check (oracle/adjoint_fd_longdouble.py), and exit")
     p.add_argument("--parity-full", action="store_true",
                    help="only the 3-D parity legs at 256^3 x 200 steps for mLW, Roe-MUSCL "
                         "and HLLD, both policies, against the oracle; prints one JSON line")
     p.add_argument("--profile-case", default=None,
                    choices=["mlw3d", "roe3d", "hlld3d", "adjoint2d", "batch", "roe2d",
                             "gravity2d", "resistive2d", "gravity3d", "resistive3d",
-                            "spicule", "single", "mlw2d", "mlw2d_df", "mlw3d_df"],
+                            "spicule", "spicule_group", "single", "mlw2d", "mlw2d_df",
+                            "mlw3d_df"],
                    help="run one small fixed case of a secondary path (for ncu) and exit")
     return p.parse_args()
 
@@ -92,6 +97,22 @@ def profile_case(case, n, tile=-1, df64=False):
         st = run.query()
         run.close()
         out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
+    elif case == "spicule_group":
+        # the spicule beta sweep's group launch: n runs of 1024 cells (beta
+        # log-uniform in [0.1, 10]), 100 loop iterations each
+        rng = np.random.default_rng(11)
+        runs = []
+        for k, b in enumerate(10.0 ** rng.uniform(-1.0, 1.0, size=n)):
+            s = setups.spicule_1d(1024, beta=float(b), seed=k)
+            run = drivers.make_run(s)
+            run.push(s["state"])
+            run.start(tend=s["tend"], nstop=s["nstop"], safety=s["safety"], dtmin=s["dtmin"])
+            runs.append(run)
+        capi.Run.advance_group(runs, 100)
+        done = [int(r.query().nexec) for r in runs]
+        for r in runs:
+            r.close()
+        out = {"case": case, "runs": n, "steps": min(done)}
     elif case in ("gravity3d", "resistive3d"):
         s = (setups.emerging_flux_3d(n, max(2, n // 4), n) if case == "gravity3d"
              else setups.magnetic_reconnection_3d(n, max(4, n // 4)))
@@ -785,6 +806,54 @@ def adjoint_workload(stream, nsteps=2000, nsnap=32, ndir=16, n_oracle_dirs=2, h=
     return out
 
 
+def adjoint_export(path, n=256, nsteps=2000, nsnap=32, qav=3.0, beta=1.0, seed=4,
+                   exact=False):
+    """The adjoint configuration (shear layer, beta = 1, qav = 3, 2000
+    steps, 32 stored states) run once on the GPU; writes what the
+    long-double finite-difference check needs: the initial state (its
+    transcendental set-up values as this host computed them), the frozen dt
+    sequence, J and the gradient dJ/dP_0 of every variable."""
+    import oracle
+    from utrip_gb300 import drivers, setups
+    s = setups.shear_layer(n, beta=beta, seed=seed)
+    s["qav"] = qav
+    oracle.apply_bc_program(s["state"], s["bc"], s["margin"], s)
+    run = drivers.make_run(s, exact=exact)
+    try:
+        run.push(s["state"])
+        dts, J = run.record_dts(nsteps)
+        J_adj, grad, nfwd = run.adjoint(dts, nsnap=nsnap)
+        run.set_adjoint_df64(False)  # the same sweep with its reverse arithmetic in FP64
+        _, grad64, _ = run.adjoint(dts, nsnap=nsnap)
+        run.set_adjoint_df64(True)
+        # the same sweep about the exact policy's forward run of the same dts
+        rx = drivers.make_run(s, exact=True)
+        try:
+            rx.push(s["state"])
+            J_ex, grad_ex, _ = rx.adjoint(dts, nsnap=nsnap)
+        finally:
+            rx.close()
+        # the viscosity branches of the run the adjoint linearises, as bit
+        # planes (bit 0: active, bit 1: dv < 0) of every step
+        run.av_record(dts)
+        br = [run.av_branches(k) for k in range(nsteps)]
+        active = np.packbits(np.stack([b & 1 for b in br]).astype(bool), axis=1)
+        negative = np.packbits(np.stack([(b >> 1) & 1 for b in br]).astype(bool), axis=1)
+        J_held, flips = run.objective_frozen_av(dts)
+    finally:
+        run.close()
+    np.savez_compressed(path, n=n, beta=beta, seed=seed, qav=qav, nsnap=nsnap, exact=exact,
+                        state=np.stack([np.asarray(a) for a in s["state"]]),
+                        dts=np.asarray(dts), J=J, J_adjoint_replay=J_adj, J_held=J_held,
+                        forward_steps=int(nfwd), grad=np.stack([np.asarray(g) for g in grad]),
+                        grad_fp64_reverse=np.stack([np.asarray(g) for g in grad64]),
+                        J_exact_policy=J_ex,
+                        grad_exact_policy=np.stack([np.asarray(g) for g in grad_ex]),
+                        av_active=active, av_negative=negative)
+    print(json.dumps({"adjoint_export": str(path), "J": J, "steps": nsteps,
+                      "forward_steps_in_adjoint": int(nfwd)}))
+
+
 def literal_drop_in(stream, n=512, steps=(10, 100)):
     """The reference driver's own call pattern (cans2d/md_mhdkh/hdmlw/main.f:
     169,179,182): per step cfl_m3 -> t += dt -> mlw_m3 -> bnd (one bd* call
@@ -1470,6 +1539,9 @@ def main():
         return
     if args.parity_full:
         parity_full()
+        return
+    if args.adjoint_export:
+        adjoint_export(args.adjoint_export, exact=args.exact)
         return
     ws, rank, local = dist_setup()
     if args.impl == "reference":

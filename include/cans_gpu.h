@@ -595,6 +595,11 @@ int cans_run_adjoint(cans_run *h, long long nsteps, const double *dts,
  * not NULL) receives the number of face-steps whose own branch differs from
  * the recorded one: the switches a perturbed run crosses. */
 int cans_run_av_record(cans_run *h, long long nsteps, const double *dts);
+/* Copy the branches cans_run_av_record kept for step `step` (2*ix*jx bytes:
+ * x faces at i + j*ix, then y faces; bit 0 active, bit 1 dv < 0) to host
+ * memory, so that a check run elsewhere can hold the same branches.
+ * Synchronous. */
+int cans_run_av_branches(cans_run *h, long long step, unsigned char *out);
 int cans_run_objective_frozen_av(cans_run *h, long long nsteps, const double *dts,
                                  double *J, long long *nflip);
 /* The arithmetic of the reverse sweep: double-float on the FP32 pipes (on =

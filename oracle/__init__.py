@@ -28,6 +28,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libcansoracle.so"
 _lib = None
 _dp = C.POINTER(C.c_double)
+_ldp = C.POINTER(C.c_longdouble)
 _ip = C.POINTER(C.c_int)
 BD_PER, BD_SPP, BD_SPN, BD_SMP, BD_SMN, BD_FRE, BD_CNS, BD_FRD = range(8)
 
@@ -87,6 +88,10 @@ def load():
         lib.oracle_spicule_run.restype = i
         lib.oracle_set_threads.argtypes = [i]
         lib.oracle_get_threads.restype = i
+        lib.oracle_set_av_branch.argtypes = [i, C.c_void_p]
+        ld = C.c_longdouble
+        lib.oracle_ld_set_av_branch.argtypes = [i, C.c_void_p]
+        lib.oracle_ld_mlw_m3_2d.argtypes = [_ldp] * 9 + [ld, ld, ld, _ldp, _ldp, i, _ldp, _ldp, i]
         _lib = lib
     return _lib
 
@@ -94,6 +99,34 @@ def load():
 def P(a):
     assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim == 1)
     return a.ctypes.data_as(_dp)
+
+
+def PL(a):
+    assert a.dtype == np.longdouble and (a.flags.f_contiguous or a.ndim == 1)
+    return a.ctypes.data_as(_ldp)
+
+
+def set_av_branch(mode: int, rec=None, long_double: bool = False) -> None:
+    """The artificial viscosity's branch in the mlw_m3 step (not a
+    reference routine; for the finite-difference check of the adjoint):
+    mode 0 as mlw_m3.f, 1 records each face's branch into rec (uint8,
+    2 ix jx bytes: x faces then y faces), 2 holds every face at the branch
+    rec holds.  long_double: the setting of the long-double build."""
+    if mode:
+        assert rec is not None and rec.dtype == np.uint8 and rec.flags.c_contiguous
+    ptr = rec.ctypes.data if mode else None
+    f = load().oracle_ld_set_av_branch if long_double else load().oracle_set_av_branch
+    f(int(mode), ptr)
+
+
+def mlw_m3_ld(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, dx, dxm, dy, dym):
+    """cans2d/hdmlw/mlw_m3.f:1, the restatement evaluated in long double
+    (mlw2d_ld.c): every array np.longdouble, Fortran order."""
+    ix, jx = ro.shape
+    ld = np.longdouble
+    load().oracle_ld_mlw_m3_2d(*[PL(a) for a in (ro, pr, vx, vy, vz, bx, by, bz, az)],
+                               ld(dt), ld(qav), ld(gm), PL(dx), PL(dxm), ix, PL(dy), PL(dym),
+                               jx)
 
 
 def set_threads(n: int) -> None:

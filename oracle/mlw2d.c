@@ -26,6 +26,31 @@
 
 static oracle_arena arena2d;
 
+/* The artificial viscosity's branch, for the finite-difference check of the
+ * adjoint (not a reference routine): mode 0 evaluates q = qav dxm
+ * max(0, |dv| - 1e-4) as mlw_m3.f:325-334 does; mode 1 does the same and
+ * records each face's branch (bit 0: the max takes |dv| - 1e-4, bit 1:
+ * dv < 0) in av_rec, 2 ix jx bytes per step (x faces, then y faces); mode 2
+ * holds every face at the recorded branch, q = qav dxm (s dv - 1e-4) on
+ * active faces with s the recorded sign, 0 on the others. */
+static int av_mode = 0;
+static unsigned char *av_rec = NULL;
+
+void oracle_set_av_branch(int mode, unsigned char *rec) {
+  av_mode = mode;
+  av_rec = rec;
+}
+
+static inline double av_coef(double d, size_t f) {
+  const double a = fabs(d) - R4_1EM4;
+  if (av_mode == 2) {
+    const unsigned char b = av_rec[f];
+    return (b & 1) ? ((b & 2) ? -d : d) - R4_1EM4 : 0.0;
+  }
+  if (av_mode == 1) av_rec[f] = (unsigned char)((a > 0.0) | ((d < 0.0) << 1));
+  return fmax2(0.0, a);
+}
+
 /* cans2d/hdmlw/mlwhalf.f:36-52 */
 static void mlwhalf2(const double *u, double *un, double *du, double dt,
                      const double *fx, const double *dxi, const double *dxim,
@@ -539,19 +564,16 @@ static void mlw_m3_core(double *ro, double *pr, double *vx, double *vy,
   mlwsrcf2(daz, dt, ss, ux0, ux1, ix, uy0, uy1, jx);
 
   /* artificial-viscosity coefficients (:324-334) */
-  const double zero = 0.0;
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
     for (int i = 1; i <= ix - 1; i++)
       qx[I2(i, j)] =
-          qav * dxm[I1(i)] *
-          fmax2(zero, fabs(vx[I2(i + 1, j)] - vx[I2(i, j)]) - R4_1EM4);
+          qav * dxm[I1(i)] * av_coef(vx[I2(i + 1, j)] - vx[I2(i, j)], I2(i, j));
   OMP_FOR
   for (int j = 1; j <= jx - 1; j++)
     for (int i = 1; i <= ix; i++)
       qy[I2(i, j)] =
-          qav * dym[I1(j)] *
-          fmax2(zero, fabs(vy[I2(i, j + 1)] - vy[I2(i, j)]) - R4_1EM4);
+          qav * dym[I1(j)] * av_coef(vy[I2(i, j + 1)] - vy[I2(i, j)], n + I2(i, j));
   /* apply artificial viscosity (:338-345) */
   mlwartv2(ro, dro, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);
   mlwartv2(ee, dee, dt, qx, dxi, dxim, ix, qy, dyi, dyim, jx);

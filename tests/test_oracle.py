@@ -1108,3 +1108,43 @@ def test_mhd_wind_setup_follows_the_model(oracle_lib):
     st = setups.copy_state(s)
     t, ns, merr, _ = oracle_lib.run_1d(s, st, 50)
     assert ns == 50 and merr == 0 and st[3][0] == 0.15
+
+
+def test_viscosity_branch_record_and_hold_reproduce_the_step(oracle_lib):
+    """The oracle's held-branch hook (for the adjoint's finite-difference
+    check): recording the branches changes nothing, and holding the
+    recorded branches reproduces the same step bit for bit."""
+    s = setups.random_state(40, 33, seed=6)
+    st = setups.copy_state(s)
+    dt, _ = oracle_lib.cfl_2d(s, st, 0.4)
+    ref = setups.copy_state(s)
+    oracle_lib.step_2d(s, ref, dt)
+    rec = np.zeros(2 * st[0].size, dtype=np.uint8)
+    for mode in (1, 2):
+        got = setups.copy_state(s)
+        oracle_lib.set_av_branch(mode, rec)
+        try:
+            oracle_lib.step_2d(s, got, dt)
+        finally:
+            oracle_lib.set_av_branch(0)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+    assert 0 < int(np.count_nonzero(rec & 1)) < rec.size  # faces on both branches
+
+
+def test_long_double_step_agrees_with_the_double_step(oracle_lib):
+    """mlw2d_ld.c is the same restatement with every double widened: one
+    step of a random state agrees with the double oracle to rounding."""
+    s = setups.random_state(40, 33, seed=5)
+    st = setups.copy_state(s)
+    dt, _ = oracle_lib.cfl_2d(s, st, 0.4)
+    ld = [np.asfortranarray(a, dtype=np.longdouble) for a in st]
+    g = {k: np.asarray(s[k], dtype=np.longdouble) for k in ("dx", "dxm", "dy", "dym")}
+    oracle_lib.step_2d(s, st, dt)
+    oracle_lib.mlw_m3_ld(*ld, dt, s["qav"], s["gm"], g["dx"], g["dxm"], g["dy"], g["dym"])
+    for a, b in zip(ld, st):
+        scale = float(np.max(np.abs(b))) or 1.0
+        assert float(np.max(np.abs(np.asarray(a, dtype=np.float64) - b))) <= 1e-14 * scale
+    # and it carries more digits than a double: the widened result is not
+    # the double one
+    assert any(np.any(a != np.asarray(a, dtype=np.float64)) for a in ld)

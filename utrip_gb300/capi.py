@@ -87,6 +87,7 @@ def load() -> C.CDLL:
                                  C.POINTER(C.c_longlong)]),
         "cans_run_bc_transpose": (i, [vp, C.POINTER(_dp)]),
         "cans_run_av_record": (i, [vp, C.c_longlong, _dp]),
+        "cans_run_av_branches": (i, [vp, C.c_longlong, vp]),
         "cans_run_objective_frozen_av": (i, [vp, C.c_longlong, _dp, _dp,
                                              C.POINTER(C.c_longlong)]),
         "cans_batch_create": (i, [C.POINTER(vp), i, vp]), "cans_batch_destroy": (i, [vp]),
@@ -766,6 +767,14 @@ class Run:
         device, for objective_frozen_av."""
         dts = np.ascontiguousarray(dts, dtype=np.float64)
         _check(self.lib.cans_run_av_record(self.h, dts.size, _ptr(dts)), "cans_run_av_record")
+
+    def av_branches(self, step: int):
+        """The branches av_record kept for one step: uint8, 2 ix jx (x faces,
+        then y faces; bit 0 active, bit 1 dv < 0)."""
+        out = np.zeros(2 * int(np.prod(self.shape)), dtype=np.uint8)
+        _check(self.lib.cans_run_av_branches(self.h, int(step), out.ctypes.data),
+               "cans_run_av_branches")
+        return out
 
     def objective_frozen_av(self, dts):
         """The objective of the frozen dts with every viscosity face held at

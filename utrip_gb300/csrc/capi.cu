@@ -2543,6 +2543,14 @@ extern "C" int cans_run_av_record(cans_run *h, long long nsteps, const double *d
   return CANS_OK;
 }
 
+extern "C" int cans_run_av_branches(cans_run *h, long long step, unsigned char *out) {
+  if (!h || !out || !h->avb || step < 0 || step >= h->avb_steps) return CANS_ERR_ARG;
+  const size_t per = 2 * h->n;
+  CK(cudaMemcpyAsync(out, h->avb + per * (size_t)step, per, cudaMemcpyDeviceToHost, h->s));
+  CK(cudaStreamSynchronize(h->s));
+  return CANS_OK;
+}
+
 extern "C" int cans_run_objective_frozen_av(cans_run *h, long long nsteps, const double *dts,
                                             double *J, long long *nflip) {
   NvtxRange nvtx("cans_run_objective_frozen_av");
