@@ -8,13 +8,14 @@ tests, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use it.
 Parity status: the 1-D spicule loop (mlw_m_bg, chkdav, torque, bnd) is
 pinned against the output the reference ships for its spicule run
 (tests/golden/spicule_reference.npz, checked in tests/test_oracle.py and
-tests/test_dac.py).  The mLW step in 1-D, 2-D and 3-D (mlw_m, mlw_m3) is
-pinned against the reference's own known answer for its shock-tube model,
-the exact solution of cans1d/md_shktb/hdmlw/shktb_analytic.pro
-(shktb_analytic.py here; tests/test_sod.py).  The other routines are parity
-unpinned against the Fortran itself (no Fortran compiler is available and
-the reference ships no golden vectors for them); they are pinned by
-invariants and frozen fixtures in tests/golden/.
+tests/test_dac.py).  The mLW step in 1-D, 2-D and 3-D (mlw_m, mlw_m3), the
+Roe-MUSCL step in 1-D, 2-D and 3-D and the HLLD engine are pinned against
+the reference's own known answer for its shock-tube model, the exact
+solution of cans1d/md_shktb/hdmlw/shktb_analytic.pro (shktb_analytic.py
+here; tests/test_sod.py).  No output of the Fortran itself exists for these
+(no Fortran compiler is available and the reference ships no golden vectors
+for them); beyond the known answer they are pinned by invariants and frozen
+fixtures in tests/golden/.
 """
 from __future__ import annotations
 

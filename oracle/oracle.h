@@ -10,12 +10,16 @@
  * boundary program) is pinned against the output the reference ships for its
  * spicule run (tests/golden/spicule_reference.npz): the set-up to the last
  * bits of an 80-bit evaluation, the 100000-step run to 2.6e-8 in time and
- * 2e-4 in the density and pressure profiles.  The other routines are parity
- * unpinned against the Fortran itself: no Fortran compiler exists in the
- * build or GPU environment and the reference ships no golden vectors for
- * mlw_m / mlw_m3 / roe_m / HLLD, so they are pinned by hand-checkable
- * invariants instead (uniform-state invariance, mirror symmetry, exact
- * periodic conservation, axis rotation) and by the committed fixtures in
+ * 2e-4 in the density and pressure profiles.  The mLW step in 1-D, 2-D and
+ * 3-D, the Roe-MUSCL step in 1-D, 2-D and 3-D and the HLLD engine, each with
+ * its CFL loop, are pinned against the reference's own known answer for its
+ * shock-tube model, the exact solution of cans1d/md_shktb/hdmlw/
+ * shktb_analytic.pro (shktb_analytic.py; tests/test_sod.py): they converge
+ * to it under refinement.  No output of the Fortran itself exists for these
+ * (no Fortran compiler in the build or GPU environment, no golden vectors in
+ * the reference), so beyond that they are pinned by hand-checkable
+ * invariants (uniform-state invariance, mirror symmetry, exact periodic
+ * conservation, axis rotation) and by the committed fixtures in
  * tests/golden/ that freeze their outputs.
  *
  * Fidelity rules followed throughout:
