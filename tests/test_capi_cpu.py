@@ -116,3 +116,20 @@ def test_hlld_and_roe_run_arguments_rejected_without_a_device(lib):
     with pytest.raises(capi.CansError) as e:  # y is one cell long: cannot be active
         capi.Run(capi.SOLVER_HLLD_3D, s, s["gm"], 0.0, margin=3, mfdim=(1, 1, 0))
     assert e.value.code == capi.CANS_ERR_ARG
+
+
+def test_advance_group_arguments_rejected_without_a_device(lib):
+    """cans_run_advance_group refuses an empty group, a null list and null
+    handles before any device work."""
+    assert lib.cans_run_advance_group(None, 1, 5) == capi.CANS_ERR_ARG
+    arr = (C.c_void_p * 2)(None, None)
+    assert lib.cans_run_advance_group(arr, 0, 5) == capi.CANS_ERR_ARG
+    assert lib.cans_run_advance_group(arr, 2, 5) == capi.CANS_ERR_ARG
+    assert lib.cans_run_advance_group(arr, 2, -1) == capi.CANS_ERR_ARG
+    with pytest.raises(ValueError):
+        capi.Run.advance_group([], 5)
+
+
+def test_av_branches_rejects_a_null_handle(lib):
+    out = np.zeros(8, dtype=np.uint8)
+    assert lib.cans_run_av_branches(None, 0, out.ctypes.data) == capi.CANS_ERR_ARG

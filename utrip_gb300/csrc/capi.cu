@@ -16,6 +16,7 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <algorithm>
 #include <vector>
 
 #include "cans_gpu.h"
@@ -2007,8 +2008,11 @@ extern "C" int cans_run_advance_group(cans_run *const *runs, int nruns, int iter
     if (!h || h->ndim != 1 || !h->ctl) return CANS_ERR_ARG;
     if ((h->d.exact != 0) != (runs[0]->d.exact != 0)) return CANS_ERR_ARG;
     if ((h->loop1d.bg != nullptr) != (runs[0]->loop1d.bg != nullptr)) return CANS_ERR_ARG;
-    for (int j = 0; j < k; j++)
-      if (runs[j] == h) return CANS_ERR_ARG;  // a run once
+  }
+  {  // a run once: two clusters on one state would race
+    std::vector<const cans_run *> sorted(runs, runs + nruns);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return CANS_ERR_ARG;
   }
   if (iters == 0) return CANS_OK;
   std::vector<Run1DArgs> args((size_t)nruns);
