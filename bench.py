@@ -35,6 +35,11 @@ METRIC = "mLW MHD zone-updates/s"
 UNIT = "zone-updates/s"
 N_CELLS = 512
 B_PER_ZONE = 144  # mlw_m3: 9 arrays read once and written once, 8 B each
+# floating-point operations of one reference mlw_m3 step and cfl_m3 per
+# interior zone of the 512^2 vortex (adds, multiplies, divides, square
+# roots: 791.8 + 19.2), from the oracle's counting build (oracle/opcount.cpp,
+# held exact in tests/test_oracle.py); the counts do not depend on the data
+REF_FLOPS_PER_ZONE = 811.0
 
 
 def parse():
@@ -1463,6 +1468,13 @@ def run_ours(args, ws, rank, local):
         ach = flops_zone * n * n / (step_avg * 1e-3) / 1e12
         fp64 = {"achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
                 "flops_per_zone": flops_zone, "peak_kind": "measured live (FP64 FMA chains)"}
+        # the reference algorithm's own arithmetic per zone-update (mlw_m3 and
+        # cfl_m3 at 512^2), counted by oracle/opcount.cpp: the rate at which
+        # the loop delivers it, step and bookkeeping included
+        ref_ach = REF_FLOPS_PER_ZONE * value / 1e12
+        fp64.update({"reference_algorithm_flops_per_zone": REF_FLOPS_PER_ZONE,
+                     "reference_algorithm_tflops_delivered": ref_ach,
+                     "reference_algorithm_frac_of_peak": ref_ach / fp64_peak})
 
     # end to end through the public API with pinned host buffers
     host = [torch.empty((n + 2, n + 2), dtype=torch.float64, pin_memory=True).numpy().T

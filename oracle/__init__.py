@@ -130,6 +130,35 @@ def mlw_m3_ld(ro, pr, vx, vy, vz, bx, by, bz, az, dt, qav, gm, dx, dxm, dy, dym)
                                jx)
 
 
+_oplib = None
+
+
+def opcount_mlw_m3(setup, state, dt):
+    """Floating-point operations of one reference mlw_m3 step and one cfl_m3
+    of `state` (updated in place by the step), counted by the oracle's
+    restatement compiled with a counting number type (opcount.cpp):
+    {"step": {...}, "cfl": {...}}, each with add (and subtract), mul, div,
+    sqrt and cmp."""
+    global _oplib
+    if _oplib is None:
+        if not (HERE / "_build" / "libcansopcount.so").exists():
+            build()
+        lib = C.CDLL(str(HERE / "_build" / "libcansopcount.so"))
+        d, i = C.c_double, C.c_int
+        lib.oracle_opcount_mlw_m3_2d.argtypes = [C.POINTER(_dp), d, d, d, _dp, _dp, i, _dp,
+                                                 _dp, i, _dp]
+        _oplib = lib
+    ix, jx = state[0].shape
+    arr = (_dp * 9)(*[P(a) for a in state])
+    out = np.zeros(10)
+    _oplib.oracle_opcount_mlw_m3_2d(arr, dt, setup["qav"], setup["gm"], P(setup["dx"]),
+                                    P(setup["dxm"]), ix, P(setup["dy"]), P(setup["dym"]), jx,
+                                    P(out))
+    keys = ("add", "mul", "div", "sqrt", "cmp")
+    return {"step": dict(zip(keys, out[:5].astype(int).tolist())),
+            "cfl": dict(zip(keys, out[5:].astype(int).tolist()))}
+
+
 def set_threads(n: int) -> None:
     load().oracle_set_threads(int(n))
 

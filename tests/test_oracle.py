@@ -1148,3 +1148,24 @@ def test_long_double_step_agrees_with_the_double_step(oracle_lib):
     # and it carries more digits than a double: the widened result is not
     # the double one
     assert any(np.any(a != np.asarray(a, dtype=np.float64)) for a in ld)
+
+
+def test_operation_count_of_the_reference_step(oracle_lib):
+    """The reference algorithm's own arithmetic (oracle/opcount.cpp: the
+    restatement with a counting number type): one mlw_m3 step and one cfl_m3
+    of the 128^2 vortex.  The counts depend on the grid only, not on the
+    data; the counted step equals the oracle's bit for bit.  Per interior
+    zone this is about 792 operations for the step (338 add/subtract, 428
+    multiply, 26 divide) and 19 for the CFL (one square root)."""
+    s = setups.orszag_tang(128)
+    st = setups.copy_state(s)
+    dt, _ = oracle_lib.cfl_2d(s, st, 0.4)
+    ref = setups.copy_state(s)
+    oracle_lib.step_2d(s, ref, dt)
+    c = oracle_lib.opcount_mlw_m3(s, st, dt)
+    for a, b in zip(st, ref):
+        assert np.array_equal(a, b)
+    assert c["step"] == {"add": 5570823, "mul": 7059341, "div": 433449, "sqrt": 0,
+                         "cmp": 33411}
+    assert c["cfl"] == {"add": 101400, "mul": 152100, "div": 50702, "sqrt": 16900,
+                        "cmp": 33801}
