@@ -115,6 +115,25 @@ __device__ __forceinline__ void to_primitive(const F<E> *u, double gm1, double m
   p[P3::BZ] = u[U_BX + 2].v;
 }
 
+// The double-float policy's forecast of a face the double-float flux would
+// hand to FP64 (hlld_flux_t's test of the star-state denominators): the
+// field of both face states within about 1/32 of the face normal and the
+// normal field's pressure above about a sixteenth of the gas pressure, the
+// c_f = c_a degeneracy.  Judged on the exponent fields with integer
+// operations.  When every active lane of a warp forecasts it, the warp takes
+// the FP64 flux directly; a warp with any other face takes the double-float
+// flux with its own test, so that no warp pays for both paths on a forecast
+// alone.
+__device__ __forceinline__ int exp_field(double x) {
+  return (__double2hiint(x) >> 20) & 0x7ff;
+}
+__device__ __forceinline__ bool near_degenerate(const double *L, const double *R, double bn) {
+  const int en = exp_field(bn);
+  const int et = max(max(exp_field(L[6]), exp_field(L[7])), max(exp_field(R[6]), exp_field(R[7])));
+  const int ep = max(exp_field(L[1]), exp_field(R[1]));
+  return en > 0 && et + 6 <= en && 2 * en - 1019 >= ep;
+}
+
 // minmod of the fast policy (flmt of inp_tvdminmod.f:118 up to the sign of a
 // zero result)
 __device__ __forceinline__ double minmod(double a, double b) {
@@ -180,8 +199,8 @@ __global__ void __launch_bounds__(kThreads)
     const double *bn = P + (P3::BX + a) * g.n + c;
     const double bb = ((T(__ldg(bn)) + T(__ldg(bn + s))) / T(2.0)).v;
     if constexpr (QF) {
-      bool ill = false;
-      hlld_flux_t<df::DF>(K, L, R, bb, f, &ill);
+      bool ill = __all_sync(__activemask(), near_degenerate(L, R, bb));
+      if (!ill) hlld_flux_t<df::DF>(K, L, R, bb, f, &ill);
       if (ill) hlld_flux<false>(K, L, R, bb, f);  // ill-conditioned: FP64
     } else {
       hlld_flux<E>(K, L, R, bb, f);

@@ -158,22 +158,36 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
   // one-sided star state (:281-342); side 0 left, 1 right
   T rost[2], rxst[2], ryst[2], rzst[2], vyst[2], vzst[2], byst[2], bzst[2], eest[2];
   T vdbst[2];
+  // the star states' denominators first: where one is ill-conditioned for
+  // double-float the caller evaluates the face in FP64, and the double-float
+  // instance stops before the rest of the star states
+  T temp_fst[2];
   bool illv = false;
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    const T ro = s ? ror : rol, sd = s ? sdr : sdl, sdm = s ? sdmr : sdml;
+    temp_fst[s] = ro * sd * sdm - bxsq;
+    if constexpr (std::is_same<T, df::DF>::value) {
+      if (ill != nullptr) {
+        const float big = fabsf(ro.d.h * sd.d.h * sdm.d.h) + bxsq.d.h;
+        if (!(fabsf(temp_fst[s].d.h) >= kIllCond * big)) illv = true;
+      }
+    }
+  }
+  if constexpr (SL) {
+    if (ill != nullptr && illv && !(N::ge0(sl) || N::le0(sr))) {
+      *ill = true;  // the caller evaluates the face in FP64
+      return;
+    }
+  }
 #pragma unroll
   for (int s = 0; s < 2; s++) {
     const T ro = s ? ror : rol, vx = s ? vxr : vxl, vy = s ? vyr : vyl, vz = s ? vzr : vzl;
     const T by = s ? byr : byl, bz = s ? bzr : bzl, pt = s ? ptr : ptl, ee = s ? eer : eel;
     const T sd = s ? sdr : sdl, sdm = s ? sdmr : sdml;
-    const T temp_fst = ro * sd * sdm - bxsq;
-    if constexpr (std::is_same<T, df::DF>::value) {
-      if (ill != nullptr) {
-        const float big = fabsf(ro.d.h * sd.d.h * sdm.d.h) + bxsq.d.h;
-        if (!(fabsf(temp_fst.d.h) >= kIllCond * big)) illv = true;
-      }
-    }
-    const T s3 = fsign_(T(1.0), temp_fst + zf) * fsign_(T(1.0), temp_fst - zf);
+    const T s3 = fsign_(T(1.0), temp_fst[s] + zf) * fsign_(T(1.0), temp_fst[s] - zf);
     const T mx = fmax_(T(0.0), s3), mn = fmin_(T(0.0), s3);
-    const T dd = temp_fst + mn;
+    const T dd = temp_fst[s] + mn;
     T tmp, tmp2, rsd, esd;
     if constexpr (E) {
       tmp = bxs * (sd - sdm) / dd;
@@ -201,12 +215,6 @@ __device__ __forceinline__ void hlld_flux_t(const HlldK &K, const double *L,
     eest[s] = mx * esd - mn * ee;
   }
   // double-star states (:347-414)
-  if constexpr (SL) {
-    if (ill != nullptr && illv && !(N::ge0(sl) || N::le0(sr))) {
-      *ill = true;  // the caller evaluates the face in FP64
-      return;
-    }
-  }
   const T sqrtrol = fsqrt(rost[0]), sqrtror = fsqrt(rost[1]);
   T slst, srst;
   if constexpr (E) {

@@ -431,9 +431,30 @@ __device__ __forceinline__ void roe_flux_fast(const RoeK &K, const double *L,
 // fluxes converted once.
 // A face whose flux is ill-conditioned for double-float (kIllCond) is
 // evaluated again by the FP64 fast flux.
+// The forecast of such a face, before any double-float work: the field of
+// both face states within about 1/32 of the face normal (judged on the
+// exponent fields with integer operations), where c_f meets c_a or c_s.
+// When every active lane of a warp forecasts it (a field along the axis, as
+// on the faces of that axis), the warp takes the FP64 flux directly; a warp
+// with any other face takes the double-float flux with its own test, so
+// that no warp pays for both paths on a forecast alone.
+__device__ __forceinline__ int roe_exp_field(double x) {
+  return (__double2hiint(x) >> 20) & 0x7ff;
+}
+__device__ __forceinline__ bool roe_near_degenerate(const double *L, const double *R) {
+  const int en = min(roe_exp_field(L[5]), roe_exp_field(R[5]));
+  const int et = max(max(roe_exp_field(L[6]), roe_exp_field(L[7])),
+                     max(roe_exp_field(R[6]), roe_exp_field(R[7])));
+  return en > 0 && et + 6 <= en;
+}
+
 template <bool FIX = true>
 __device__ __forceinline__ void roe_flux_df(const RoeK &K, const double *L,
                                             const double *R, double *f) {
+  if (__all_sync(__activemask(), roe_near_degenerate(L, R))) {
+    roe_flux_fast_r<double, FIX>(roe_k<double>(K), L, R, f);
+    return;
+  }
   df::DF l[8], r[8], o[7];
 #pragma unroll
   for (int v = 0; v < 8; v++) {
