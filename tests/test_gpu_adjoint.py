@@ -304,6 +304,42 @@ def test_frozen_branch_finite_differences_reduced_c5(gpu):
         run.close()
 
 
+def test_recorded_branches_hold_the_oracle_to_the_same_run(gpu, oracle_lib):
+    """The branches the GPU records (cans_run_av_branches) in the format the
+    oracle holds: a 64^2 shear layer at qav = 3, 40 steps in the exact
+    policy; the oracle's run holding the GPU's branches equals the GPU's
+    held run bit for bit, and so does the oracle's plain run (on the base
+    trajectory the held branches are its own)."""
+    s = _setup(n=64, ny=64, qav=3.0)
+    run = _run(s, exact=True)
+    try:
+        dts, J = run.record_dts(40)
+        run.av_record(dts)
+        Jh, nflip = run.objective_frozen_av(dts)
+        rec = [run.av_branches(k) for k in range(40)]
+    finally:
+        run.close()
+    assert Jh == J and nflip == 0
+    assert any(int(np.count_nonzero(r & 1)) for r in rec)  # viscosity faces active
+    final = {}
+    for mode in (0, 2):
+        st = setups.copy_state(s)
+        try:
+            for k, dt in enumerate(dts):
+                oracle_lib.set_av_branch(mode, rec[k])
+                oracle_lib.step_2d(s, st, dt)
+                oracle_lib.apply_bc_program(st, s["bc"], s["margin"], s)
+        finally:
+            oracle_lib.set_av_branch(0)
+        final[mode] = st
+        w = np.outer(s["dx"], s["dy"])[1:-1, 1:-1]
+        e = (st[5] ** 2 + st[6] ** 2 + st[7] ** 2)[1:-1, 1:-1]
+        Jo = float(np.sum(e * w)) / np.pi / 8.0
+        assert abs(Jo - J) <= 1e-13 * abs(J), (mode, Jo, J)  # summation order only
+    for a, b in zip(final[2], final[0]):
+        assert np.array_equal(a, b)
+
+
 def test_frozen_branch_needs_a_record(gpu):
     s = _setup(qav=3.0)
     run = _run(s)
