@@ -479,8 +479,8 @@ int cans_run_advance(cans_run *h, int iters);
  * `nruns` started 1-D runs (MLW_M_1D or MLW_M_BG_1D, all of one solver
  * family and one arithmetic policy, each run once) by up to `iters` loop
  * iterations each, in one kernel launch: one cluster per run, so runs too
- * small to use the GPU alone share it (a run of up to about 6800 cells; a
- * larger one is refused with CANS_ERR_ARG).  Each run ends where its own
+ * small to use the GPU alone share it (a run of up to about 7800 cells, 6000
+ * with mlw_m_bg; a larger one is refused with CANS_ERR_ARG).  Each run ends where its own
  * loop would (tend, nstop, dtmin, output pause).  In the exact policy its state
  * and loop state are those cans_run_advance gives, bit for bit; in the fast
  * policy the group kernel may fuse multiply-adds differently, within that

@@ -162,7 +162,8 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   const int ix = p.ix, L = p.lmax;
   extern __shared__ double sm[];
   // layout: prim[2][5][L], U[5][L], FX[5][L], K[5][L], Q[L],
-  // (BG: SS[2][L] cell sources, SH[2][L] corner sources), slots[2][CS],
+  // (BG: SS[2][L] cell sources, SH[2][L] corner sources, RI[4][L] the
+  // reciprocals 1/sc, 1/scm, 1/rr, 1/rrm of the own cells), slots[2][CS],
   // bad[2][CS], red[32]
   double *prim = sm;
   double *U = prim + 2 * NV1 * L;
@@ -171,7 +172,8 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   double *Q = K + NV1 * L;
   double *SS = Q + L;
   double *SH = SS + (BG ? 2 * L : 0);
-  double *slots = SH + (BG ? 2 * L : 0);
+  double *RI = SH + (BG ? 2 * L : 0);
+  double *slots = RI + (BG ? 4 * L : 0);
   double *bslots = slots + 2 * CS;  // per block: 1 if its CFL saw a bad cell
   double *red = bslots + 2 * CS;
   const double *bg = p.bg;
@@ -200,6 +202,15 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
     const int g = lo - 1 + l;
 #pragma unroll
     for (int v = 0; v < NV1; v++) P(0, v, l) = p.S[(size_t)v * ix + g];
+    if constexpr (BG) {
+      // the cross-section and radius profiles are constant through the run:
+      // the fast policy multiplies by their reciprocals instead of dividing
+      // by them every step (1.0 / x, the value the step's own 1.0 / sc gave)
+      RI[0 * L + l] = 1.0 / bg[2 * nx + g];
+      RI[1 * L + l] = 1.0 / bg[3 * nx + g];
+      RI[2 * L + l] = 1.0 / bg[6 * nx + g];
+      RI[3 * L + l] = 1.0 / bg[7 * nx + g];
+    }
   }
   if (tid == 0) {
     if (p.ctl) {
@@ -305,15 +316,24 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
         const FT ez = -vx * by + vy * bx;
         const FT bbm = by * by - bx * bx;
         U[0 * L + l] = (ro * sc).v; U[1 * L + l] = (ee * sc).v; U[2 * L + l] = (rx * sc).v;
-        U[3 * L + l] = (ro * vy * sc * rr).v; U[4 * L + l] = (by * sc / rr).v;
+        U[3 * L + l] = (ro * vy * sc * rr).v;
         FX[0 * L + l] = (rx * sc).v;                                          // :121-122
         FX[1 * L + l] = ((ep * vx - by * ez * pi4i) * sc).v;                  // :130-131
         SS[0 * L + l] = (rx * gx * sc).v;                                     // :132-133
         FX[2 * L + l] = ((ro * (vx * vx) + pr + bbm * pi8i) * sc).v;          // :144,147
-        SS[1 * L + l] = ((ro * gx + (ro * (vy * vy) - (by * by) * pi4i) / rr * drr) * sc +
-                         (pr + bb * pi8i) * dsc).v;                           // :145-148
         FX[3 * L + l] = ((ro * vx * vy - bx * by * pi4i) * sc * rr).v;        // :155-156
-        FX[4 * L + l] = ((-ez) * sc / rr).v;                                  // :162-164
+        if constexpr (E) {
+          U[4 * L + l] = (by * sc / rr).v;
+          SS[1 * L + l] = ((ro * gx + (ro * (vy * vy) - (by * by) * pi4i) / rr * drr) * sc +
+                           (pr + bb * pi8i) * dsc).v;                         // :145-148
+          FX[4 * L + l] = ((-ez) * sc / rr).v;                                // :162-164
+        } else {
+          const FT rri(RI[2 * L + l]);
+          U[4 * L + l] = (by * sc * rri).v;
+          SS[1 * L + l] = ((ro * gx + (ro * (vy * vy) - (by * by) * pi4i) * rri * drr) * sc +
+                           (pr + bb * pi8i) * dsc).v;
+          FX[4 * L + l] = ((-ez) * sc * rri).v;
+        }
       }
     } else
     for (int l = tid; l < nl; l += NT) {
@@ -368,11 +388,11 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
           vyh = un[3] / un[0] / rrm;
           byh = un[4] / scm * rrm;
         } else {
-          const FT si(1.0 / scm.v), ri(1.0 / un[0].v);
+          const FT si(RI[1 * L + l]), ri(1.0 / un[0].v);
           roh = un[0] * si;
           eeh = un[1] * si;
           vxh = un[2] * ri;
-          vyh = un[3] * ri / rrm;
+          vyh = un[3] * ri * FT(RI[3 * L + l]);
           byh = un[4] * si * rrm;
         }
         const FT vv = vxh * vxh + vyh * vyh;
@@ -387,10 +407,19 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
         K[1 * L + l] = ((eph * vxh - byh * ezh * pi4i) * scm).v;
         SH[0 * L + l] = (roh * vxh * gxm * scm).v;
         K[2 * L + l] = ((roh * (vxh * vxh) + prh + bbm * pi8i) * scm).v;
-        SH[1 * L + l] = ((roh * gxm + (roh * (vyh * vyh) - (byh * byh) * pi4i) / rrm * drrm) * scm +
-                         (prh + bb * pi8i) * dscm).v;
         K[3 * L + l] = ((roh * vxh * vyh - bxm * byh * pi4i) * scm * rrm).v;
-        K[4 * L + l] = ((-ezh) * scm / rrm).v;
+        if constexpr (E) {
+          SH[1 * L + l] = ((roh * gxm + (roh * (vyh * vyh) - (byh * byh) * pi4i) / rrm * drrm) *
+                               scm +
+                           (prh + bb * pi8i) * dscm).v;
+          K[4 * L + l] = ((-ezh) * scm / rrm).v;
+        } else {
+          const FT rrmi(RI[3 * L + l]);
+          SH[1 * L + l] = ((roh * gxm + (roh * (vyh * vyh) - (byh * byh) * pi4i) * rrmi * drrm) *
+                               scm +
+                           (prh + bb * pi8i) * dscm).v;
+          K[4 * L + l] = ((-ezh) * scm * rrmi).v;
+        }
         const FT q = qav * FT(ax.dm[g]) *
                      max0(fabs_(FT(P(cur, 2, l + 1)) - FT(P(cur, 2, l))) - CANS_AV_EPS);
         Q[l] = (q * dxim).v;
@@ -468,12 +497,12 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
           vx = rx / ro;
           vy = ry / ro;
         } else {
-          const FT si(1.0 / sc.v);
+          const FT si(RI[0 * L + l]);
           ro = u[0] * si;
           ee = u[1] * si;
           const FT rinv(1.0 / u[0].v);  // 1/(ro sc)
           vx = u[2] * rinv;
-          vy = u[3] * rinv / rr;
+          vy = u[3] * rinv * FT(RI[2 * L + l]);
           by = u[4] * si * rr;
         }
         const FT pr = gm1 * (ee - 0.5 * ro * (vx * vx + vy * vy) - pi8i * (bx * bx + by * by));
@@ -705,7 +734,7 @@ static int cluster_max(void (*kern)(Run1D), size_t smem) {
 
 namespace {
 constexpr size_t per_cell_doubles(bool bgv) {
-  return (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 4 : 0);
+  return (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 8 : 0);
 }
 
 // The parameters of one run on a cluster of CS blocks; false when a block
