@@ -823,23 +823,33 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
 }
 
 // Host launcher of a group of runs (k_mlw1d_group): every run gets a cluster
-// of the same size CS, the smallest power of two (at most 8) that leaves
-// each block of every run at most 256 interior cells (a thread per cell, the
-// two halo cells of a full block taken in a second pass), two blocks per SM;
-// the runs' parameters go to the device in one stream-ordered allocation.
-// All runs share exact and the BG variant.
+// of the same size CS, at first the smallest power of two (at most 8) that
+// leaves each block of every run at most 256 interior cells (a thread per
+// cell, the two halo cells of a full block taken in a second pass), two
+// blocks per SM.  A group too small to cover the SMs with one block each then
+// takes larger clusters: 1024-cell runs step in 17 us on 8 SMs against 30 us
+// on 4 (CS doubles while the grid stays within one block per SM and every
+// block keeps 32 cells).  The runs' parameters go to the device in one
+// stream-ordered allocation.  All runs share exact and the BG variant.
 cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int nruns,
                                int max_steps, cudaStream_t s) {
   if (nruns < 1) return cudaErrorInvalidValue;
-  int ixmax = 0;
+  int ixmax = 0, ixmin = 1 << 30;
   for (int k = 0; k < nruns; k++) {
     const Run1DArgs &a = runs[k];
     if (a.ix < mlw1d_min_cells() || !a.ctl) return cudaErrorInvalidValue;
     if ((a.opt.bg != nullptr) != bgv || (a.opt.trq && !bgv)) return cudaErrorInvalidValue;
     ixmax = a.ix > ixmax ? a.ix : ixmax;
+    ixmin = a.ix < ixmin ? a.ix : ixmin;
   }
   int CS = 1;
   while (CS < 8 && (ixmax - 2 + CS - 1) / CS > 256) CS <<= 1;
+  int devno = 0, nsm = 0;
+  cudaError_t e = cudaGetDevice(&devno);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, devno);
+  if (e != cudaSuccess) return e;
+  while (CS < 8 && 2LL * CS * nruns <= nsm && (ixmin - 2) / (2 * CS) >= 32) CS <<= 1;
   std::vector<Run1D> host((size_t)nruns);
   int lmax = 0;
   for (int k = 0; k < nruns; k++) {
@@ -855,8 +865,7 @@ cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int 
           : (exact ? k_mlw1d_group<true, false> : k_mlw1d_group<false, false>);
   const size_t smem = sizeof(double) * (per_cell_doubles(bgv) * lmax + 4 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   Run1D *dev = nullptr;
   const size_t bytes = sizeof(Run1D) * (size_t)nruns;
