@@ -495,11 +495,12 @@ def hlld_brio_wu(stream, exact):
 def spicule_workload(stream, nstop=100000, cpu_steps=4000):
     """The reference's spicule run (cans1d/md_spicule/hdmlw: 1024 cells,
     100000 iterations of cfl_m, mlw_m_bg, the random torque, bnd and chkdav)
-    as one cluster launch, in both arithmetic policies, against the output
-    the reference ships for this run (tests/golden/spicule_reference.npz:
-    the time reached and the ro, pr, vx profiles; vy and by follow the
-    random torque, whose stream differs) and against the oracle's loop
-    timed on a bounded sample of the same run on one host core."""
+    as one cluster launch, in the fast, exact and double-float policies,
+    against the output the reference ships for this run
+    (tests/golden/spicule_reference.npz: the time reached and the ro, pr, vx
+    profiles; vy and by follow the random torque, whose stream differs) and
+    against the oracle's loop timed on a bounded sample of the same run on
+    one host core."""
     import torch
     from utrip_gb300 import drivers, setups
     import oracle
@@ -507,8 +508,9 @@ def spicule_workload(stream, nstop=100000, cpu_steps=4000):
     gold = dict(np.load(ROOT / "tests" / "golden" / "spicule_reference.npz"))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     res = {}
-    for policy, exact in (("fast", False), ("exact", True)):
-        run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream)
+    for policy, exact, df64 in (("fast", False, False), ("exact", True, False),
+                                ("df64", False, True)):
+        run = drivers.make_run(s, exact=exact, stream=stream.cuda_stream, df64=df64)
         run.push(s["state"])
         torch.cuda.synchronize()
         e0.record(stream)
@@ -546,9 +548,9 @@ def spicule_beta_sweep(stream, nruns=64, steps=2000, cpu_steps=1000, seed=11):
     their own torque seeds, `steps` loop iterations each, advanced in one
     launch (cans_run_advance_group: one cluster per run) against the same
     runs one at a time (each run's loop as its own cluster launch, as
-    cans_run_advance gives it), and against the oracle's loop timed on one
-    host core (the reference runs each model as one serial process;
-    cpu_steps = 0 leaves that leg out)."""
+    cans_run_advance gives it), the same group in the double-float policy,
+    and the oracle's loop timed on one host core (the reference runs each
+    model as one serial process; cpu_steps = 0 leaves that leg out)."""
     import torch
     from utrip_gb300 import capi, drivers, setups
     import oracle
@@ -557,23 +559,29 @@ def spicule_beta_sweep(stream, nruns=64, steps=2000, cpu_steps=1000, seed=11):
     sets = [setups.spicule_1d(1024, beta=float(b), seed=k) for k, b in enumerate(betas)]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    def started(s):
-        run = drivers.make_run(s, stream=stream.cuda_stream)
+    def started(s, df64=False):
+        run = drivers.make_run(s, stream=stream.cuda_stream, df64=df64)
         run.push(s["state"])
         run.start(tend=s["tend"], nstop=s["nstop"], safety=s["safety"], dtmin=s["dtmin"])
         return run
 
-    runs = [started(s) for s in sets]
-    torch.cuda.synchronize()
-    e0.record(stream)
-    capi.Run.advance_group(runs, steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    group_ms = e0.elapsed_time(e1)
-    states = [r.query() for r in runs]
-    group_final = [runs[k].pull() for k in (0, nruns - 1)]
-    for r in runs:
-        r.close()
+    def group(df64):
+        runs = [started(s, df64) for s in sets]
+        torch.cuda.synchronize()
+        e0.record(stream)
+        capi.Run.advance_group(runs, steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        states = [r.query() for r in runs]
+        final = [runs[k].pull() for k in (0, nruns - 1)]
+        for r in runs:
+            r.close()
+        return ms, states, final
+
+    group_ms, states, group_final = group(False)
+    # the same runs in the double-float policy (the step on the FP32 pipes)
+    df_ms, df_states, df_final = group(True)
     alone_ms, alone_final = 0.0, []
     for k, s in enumerate(sets):
         run = started(s)
@@ -586,12 +594,15 @@ def spicule_beta_sweep(stream, nruns=64, steps=2000, cpu_steps=1000, seed=11):
         if k in (0, nruns - 1):
             alone_final.append(run.pull())
         run.close()
+    def rel(f1, f2):  # per variable, the larger over the first and last run
+        return {name: max(float(np.max(np.abs(a[v] - b[v]))) /
+                          max(float(np.max(np.abs(b[v]))), 1e-300)
+                          for a, b in zip(f1, f2))
+                for v, name in enumerate(sets[0]["names"])}
+
     # the fast policy: the group kernel may fuse multiply-adds differently
     # (vx of this model amplifies one rounding of the energy up to ~1e-5)
-    diff = {name: max(float(np.max(np.abs(f1[v] - f2[v]))) /
-                      max(float(np.max(np.abs(f2[v]))), 1e-300)
-                      for f1, f2 in zip(group_final, alone_final))
-            for v, name in enumerate(sets[0]["names"])}
+    diff = rel(group_final, alone_final)
     run_steps = nruns * steps
     res = {
         "runs": nruns, "cells": 1024, "steps_per_run": steps,
@@ -603,6 +614,14 @@ def spicule_beta_sweep(stream, nruns=64, steps=2000, cpu_steps=1000, seed=11):
         "group_us_per_run_step_each_run": group_ms * 1e3 / steps,
         "group_zone_updates_per_s": 1024 * run_steps / (group_ms * 1e-3),
         "first_and_last_run_rel_linf_vs_alone": diff,
+        "df64_policy": {
+            "group_ms": df_ms,
+            "all_runs_completed": all(st.nexec == steps and st.merr == 0 for st in df_states),
+            "speedup_vs_fp64_group": group_ms / df_ms,
+            "speedup_vs_fp64_one_at_a_time": alone_ms / df_ms,
+            "group_zone_updates_per_s": 1024 * run_steps / (df_ms * 1e-3),
+            "first_and_last_run_rel_linf_vs_fp64_group": rel(df_final, group_final),
+        },
     }
     if cpu_steps > 0:
         ref = setups.copy_state(sets[0])

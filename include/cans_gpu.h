@@ -514,20 +514,23 @@ int cans_run_set_graph(cans_run *h, int use_graph);
  * kernel; cans_run_autotune picks one by timing them all). */
 int cans_run_set_tile(cans_run *h, int tile);
 
-/* The double-float policy of the 2-D mlw_m3 and the 3-D mlw_m step, and of
- * the face flux of the Roe-MUSCL and HLLD steps (no counterpart in the
- * reference: an arithmetic policy beside exact and fast).
+/* The double-float policy of the 2-D mlw_m3 and the 3-D mlw_m step, of the
+ * face flux of the Roe-MUSCL and HLLD steps, and of the 1-D mlw_m and
+ * mlw_m_bg loops (no counterpart in the reference: an arithmetic policy
+ * beside exact and fast).
  * With on = 1 the step's arithmetic runs as pairs of floats on the FP32
  * pipes (48-bit significands; the exponent range of float, about
  * 1e-38..1e38, bounds the values it holds) and the conserved density and
  * field are accumulated in FP64; the CFL, boundary fill and loop
  * bookkeeping are unchanged.  Held to a relative 1e-10 per variable against
- * the reference arithmetic after 100 steps.  Only fast-policy
- * CANS_SOLVER_MLW_M3_2D, CANS_SOLVER_MLW_M_3D, CANS_SOLVER_ROE_M3_2D,
+ * the reference arithmetic after 100 steps (mlw_m_bg: the fast policy's
+ * bounds, 1e-10 and vx 1e-4, whose static B_x terms stay in FP64).  Only
+ * fast-policy CANS_SOLVER_MLW_M3_2D, CANS_SOLVER_MLW_M_3D,
+ * CANS_SOLVER_MLW_M_1D, CANS_SOLVER_MLW_M_BG_1D, CANS_SOLVER_ROE_M3_2D,
  * CANS_SOLVER_ROE_M_3D and CANS_SOLVER_HLLD_3D runs without gravity or
- * resistivity take it (else
- * CANS_ERR_ARG); the mLW steps select among their own tile shapes
- * (cans_run_autotune). */
+ * resistivity take it (else CANS_ERR_ARG); the 2-D and 3-D mLW steps
+ * select among their own tile shapes (cans_run_autotune).  A group of 1-D
+ * runs (cans_run_advance_group) must share the policy. */
 int cans_run_set_df64(cans_run *h, int on);
 
 /* ------------------------------------------------------------------------ */

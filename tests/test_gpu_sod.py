@@ -142,3 +142,20 @@ def test_double_float_riemann_steps_on_the_exact_shock_tube(gpu, solver):
     assert res[True][0] == res[False][0]
     for k in ("ro", "pr", "vx"):
         assert res[True][1][k] == pytest.approx(res[False][1][k], rel=1e-6), k
+
+
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+def test_double_float_mlw_steps_on_the_exact_shock_tube(gpu, ndim):
+    """The double-float mLW loops (1-D mlw_m, 2-D mlw_m3, 3-D mlw_m) take the
+    FP64 fast policy's steps and reach its distance from the exact answer
+    (within 1e-6 of it) at 1024 cells."""
+    s = setups.sod_shock_tube(1024, ndim)
+    res = {}
+    for df in (False, True):
+        st = setups.copy_state(s)
+        t, ns, merr, nexec = drivers.run_resident(s, st, 10 ** 6, df64=df)
+        assert merr == 0 and t >= s["tend"] and nexec == ns
+        res[df] = (ns, l1(s, st, t))
+    assert res[True][0] == res[False][0]
+    for k in ("ro", "pr", "vx"):
+        assert res[True][1][k] == pytest.approx(res[False][1][k], rel=1e-6), k

@@ -732,8 +732,9 @@ class Run:
         _check(self.lib.cans_run_set_tile(self.h, tile), "cans_run_set_tile")
 
     def set_df64(self, on: bool = True):
-        """The double-float policy of the 2-D mlw_m3 step (see
-        cans_run_set_df64)."""
+        """The double-float policy of the step: 2-D mlw_m3, 3-D mlw_m, the
+        1-D mlw_m and mlw_m_bg loops, the Roe-MUSCL and HLLD face fluxes
+        (see cans_run_set_df64)."""
         _check(self.lib.cans_run_set_df64(self.h, 1 if on else 0), "cans_run_set_df64")
 
     def profile(self, iters: int):

@@ -254,11 +254,13 @@ struct Loop1D {
   double floor = 0.0;
   int chk = 0;
 };
+// The 1-D loop (or one fixed step) on one cluster; dfp: the double-float
+// policy (exact false).
 cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          const double *bxm, const Loop1D &opt, int ix,
                          const Axis &ax, const Phys &ph, const BcTable &bc,
                          Ctl *ctl, int max_steps, int fixed, double dt_fixed,
-                         int start, cudaStream_t s);
+                         int start, cudaStream_t s, bool dfp = false);
 // One run of a group advanced by launch_mlw1d_group (a started resident
 // loop: ctl is its control block).
 struct Run1DArgs {
@@ -273,8 +275,9 @@ struct Run1DArgs {
 };
 // Up to max_steps iterations of each run's loop, all runs in one launch (one
 // cluster per run); every run has the BG variant or none has.
+// dfp: the double-float policy (exact false).
 cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int nruns,
-                               int max_steps, cudaStream_t s);
+                               int max_steps, cudaStream_t s, bool dfp = false);
 // chkdav (cans1d/common/chkdav.f:68-76) on device arrays: da below floor is
 // raised to it and vx zeroed there; the count is added to *count (device).
 // chkdav of 2-D / 3-D states (mlw1d.cu): na density-like slots a0, a1 of S

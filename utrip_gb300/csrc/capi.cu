@@ -1462,7 +1462,7 @@ struct cans_run {
   int mfdim[3] = {1, 1, 1};    // HLLD: active axes
   double mu = 1.0;             // HLLD: permeability
   bool use_graph = true;       // replay iterations as a CUDA graph
-  bool df = false;             // double-float policy of the 2-D mlw_m3 step
+  bool df = false;             // double-float policy of the step
   bool adj_df = true;          // reverse sweep of the adjoint in double-float
   unsigned char *avb = nullptr;  // adjoint check: recorded viscosity branches,
   long long avb_steps = 0;       //   2*ix*jx bytes per step
@@ -1499,6 +1499,7 @@ int layout2d(const cans_run *h) {
 }
 bool is_hlld(const cans_run *h) { return h->d.solver == CANS_SOLVER_HLLD_3D; }
 int tile_count(const cans_run *h) {
+  if (h->ndim == 1) return 1;
   if (h->df && !is_roe(h) && !is_hlld(h))
     return h->ndim == 3 ? mlw3d_df_tile_count() : mlw2d_df_tile_count();
   if (is_roe(h) || is_hlld(h) || h->ndim == 1) return 1;
@@ -1511,7 +1512,7 @@ cudaError_t launch_1d(cans_run *h, int max_steps, int fixed, double dt,
                       int start) {
   return launch_mlw1d(h->d.exact != 0, h->buf[0], h->bx1, h->bx1 + h->d.ix, h->loop1d,
                       h->d.ix, h->ax.a, h->ph, h->bc, fixed ? nullptr : h->ctl,
-                      max_steps, fixed, dt, start, h->s);
+                      max_steps, fixed, dt, start, h->s, h->df);
 }
 
 // cells whose CFL the step kernel reduces: all but the frame of width
@@ -2008,6 +2009,7 @@ extern "C" int cans_run_advance_group(cans_run *const *runs, int nruns, int iter
     if (!h || h->ndim != 1 || !h->ctl) return CANS_ERR_ARG;
     if ((h->d.exact != 0) != (runs[0]->d.exact != 0)) return CANS_ERR_ARG;
     if ((h->loop1d.bg != nullptr) != (runs[0]->loop1d.bg != nullptr)) return CANS_ERR_ARG;
+    if (h->df != runs[0]->df) return CANS_ERR_ARG;
   }
   {  // a run once: two clusters on one state would race
     std::vector<const cans_run *> sorted(runs, runs + nruns);
@@ -2042,7 +2044,7 @@ extern "C" int cans_run_advance_group(cans_run *const *runs, int nruns, int iter
     }
   }
   cudaError_t err = launch_mlw1d_group(runs[0]->d.exact != 0, runs[0]->loop1d.bg != nullptr,
-                                       args.data(), nruns, iters, s0);
+                                       args.data(), nruns, iters, s0, runs[0]->df);
   if (err != cudaSuccess) {
     cleanup();
     return err == cudaErrorInvalidValue ? CANS_ERR_ARG : CANS_ERR_CUDA;
@@ -2092,6 +2094,7 @@ extern "C" int cans_run_set_tile(cans_run *h, int tile) {
 extern "C" int cans_run_set_df64(cans_run *h, int on) {
   if (!h) return CANS_ERR_ARG;
   if (on && ((h->d.solver != CANS_SOLVER_MLW_M3_2D && h->d.solver != CANS_SOLVER_MLW_M_3D &&
+              h->d.solver != CANS_SOLVER_MLW_M_1D && h->d.solver != CANS_SOLVER_MLW_M_BG_1D &&
               !is_roe(h) && !is_hlld(h)) ||
              h->d.exact || h->grav || h->eta))
     return CANS_ERR_ARG;

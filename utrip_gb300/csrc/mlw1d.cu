@@ -32,6 +32,7 @@
 
 #include "cans_common.cuh"
 #include "cans_internal.h"
+#include "df64.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -150,10 +151,237 @@ __device__ __forceinline__ F<E> torque_add(const Run1D &p, F<E> vy, F<E> dt, lon
   return vy + dt * FT(p.trq0) * q * FT(p.trq[g]);
 }
 
+// ---- the double-float policy of the 1-D step -------------------------------
+// The stages below are the fast policy's algebra evaluated in double-float
+// (df64.cuh) on the FP32 pipes: the state stays in FP64 (converted on load
+// and store), the scratch arrays hold double-float values in their 8-byte
+// slots, and the torque, boundary program, chkdav and the cluster's CFL
+// minimum stay in FP64.
+//
+// mlw_m_bg carries bx^2/8pi in the energy, and -bx^2/8pi sc and bx^2/8pi dsc
+// in the x-momentum flux and source.  In a low-beta corona those static terms
+// are many orders above the gas pressure, and p = (gm-1)(e - ek - b^2/8pi)
+// and the force balance of the tube would lose their digits to the 48-bit
+// significand.  So the double-float values leave them out (they are constant
+// in time), and the scheme gets them back through static arrays formed once
+// in FP64, where it sees them:
+//   XS[0][l] = es(l+1) - es(l), es = pi8i bx^2 sc: the viscosity term of the
+//            energy update;
+//   XS[1][l] = the corner average of es over scm, minus pi8i bxm^2: the
+//            corner pressure;
+//   XS[2][l] = the static x-momentum flux difference and source of the
+//            corner predictor (times dt);
+//   XS[3][l] = those of the cell update, cell and corner terms (times dt/2).
+namespace d1 {
+using R = df::DF;
+__device__ __forceinline__ R in(double x) { return num_in<R>(x); }
+__device__ __forceinline__ R ld(const double *p) { return num_ld<R>(p); }
+__device__ __forceinline__ void st(double *p, R v) { num_st(p, v); }
+__device__ __forceinline__ R half(R x) { return R(df::scale(x.d, 0.5f)); }
+__device__ __forceinline__ R sq(R x) { return R(df::sqr(x.d)); }
+__device__ __forceinline__ R rcp(R x) { return R(df::rcp(x.d)); }
+// square root: the correctly rounded float root s, then one Newton step
+// s + (x - s^2) / (2 s), with s^2 exact as a float pair and x - s^2 formed
+// to float precision (the head difference is exact: s^2 and x.h are within
+// an ulp of each other)
+__device__ __forceinline__ R sqrt_(R x) {
+  const float s = __fsqrt_rn(x.d.h);
+  if (!(s > 0.0f) || s == __int_as_float(0x7f800000)) return R(s);  // 0, NaN, inf
+  const float ph = __fmul_rn(s, s), pl = __fmaf_rn(s, s, -ph);
+  const float e = __fadd_rn(__fsub_rn(__fsub_rn(x.d.h, ph), pl), x.d.l);
+  return R(df::fast_two_sum(s, __fmul_rn(e, __fmul_rn(0.5f, __frcp_rn(s)))));
+}
+struct Phys1 {
+  R gm, gm1, gm1i, ggm1, pi4i, pi8i, qav;
+};
+__device__ __forceinline__ Phys1 phys1(const Phys &ph) {
+  return {in(ph.gm), in(ph.gm1), in(ph.gm1i), in(ph.ggm1), in(ph.pi4i), in(ph.pi8i),
+          in(ph.qav)};
+}
+
+// cell stage of local cell l (global g): conserved values U, fluxes FX and
+// (BG) cell sources SS from the primitives pc (5 arrays of stride L)
+template <bool BG>
+__device__ __forceinline__ void cell(const Run1D &p, const double *pc, int L, int l, int g,
+                                     const double *RI, double *U, double *FX, double *SS,
+                                     const Phys1 &c) {
+  const size_t nx = (size_t)p.ix;
+  const R ro = in(pc[l]), pr = in(pc[L + l]), vx = in(pc[2 * L + l]), vy = in(pc[3 * L + l]),
+          by = in(pc[4 * L + l]);
+  const R bx = in(p.bx[g]);
+  const R ek = half(ro) * fma(vy, vy, sq(vx));
+  const R rx = ro * vx;
+  const R ez = fma(vy, bx, -(vx * by));
+  if constexpr (BG) {
+    const double *bg = p.bg;
+    const R sc = in(bg[2 * nx + g]), rr = in(bg[6 * nx + g]), gx = in(bg[g]),
+            dsc = in(bg[4 * nx + g]), drr = in(bg[8 * nx + g]), rri = in(RI[2 * L + l]);
+    const R pty = fma(sq(by), c.pi8i, pr);  // pressure without pi8i bx^2
+    const R eey = fma(pr, c.gm1i, fma(c.pi8i, sq(by), ek));
+    const R ep = fma(pr, c.ggm1, ek);
+    const R rxs = rx * sc, scri = sc * rri;
+    st(&U[l], ro * sc);
+    st(&U[L + l], eey * sc);
+    st(&U[2 * L + l], rxs);
+    st(&U[3 * L + l], (ro * vy) * (sc * rr));
+    st(&U[4 * L + l], by * scri);
+    st(&FX[l], rxs);
+    st(&FX[L + l], fma(-(by * ez), c.pi4i, ep * vx) * sc);
+    st(&FX[2 * L + l], fma(rx, vx, pty) * sc);
+    st(&FX[3 * L + l], fma(rx, vy, -(bx * by * c.pi4i)) * (sc * rr));
+    st(&FX[4 * L + l], -(ez * scri));
+    st(&SS[l], rxs * gx);
+    st(&SS[L + l], fma(fma(fma(ro * vy, vy, -(sq(by) * c.pi4i)), rri * drr, ro * gx), sc,
+                       pty * dsc));
+  } else {
+    const R bb = sq(by);
+    const R ee = fma(pr, c.gm1i, fma(c.pi8i, bb, ek));
+    const R ep = fma(pr, c.ggm1, ek);
+    st(&U[l], ro);
+    st(&U[L + l], ee);
+    st(&U[2 * L + l], rx);
+    st(&U[3 * L + l], ro * vy);
+    st(&U[4 * L + l], by);
+    st(&FX[l], rx);
+    st(&FX[L + l], fma(-(by * ez), c.pi4i, ep * vx));
+    st(&FX[2 * L + l], fma(rx, vx, fma(bb, c.pi8i, pr)));
+    st(&FX[3 * L + l], fma(rx, vy, -(bx * by * c.pi4i)));
+    st(&FX[4 * L + l], -ez);
+  }
+}
+
+// corner between local cells l and l+1 (global g, g+1): half-step fluxes K,
+// (BG) corner sources SH and the viscosity coefficient Q
+template <bool BG>
+__device__ __forceinline__ void corner(const Run1D &p, const double *pc, int L, int l, int g,
+                                       const double *RI, const double *XS, const double *U,
+                                       const double *FX,
+                                       const double *SS, double *K, double *SH, double *Q,
+                                       R dt, const Phys1 &c) {
+  const size_t nx = (size_t)p.ix;
+  const R dxim = in(p.ax.dim[g]);
+  R un[NV1];
+#pragma unroll
+  for (int v = 0; v < NV1; v++) {
+    const R uh = half(ld(&U[v * L + l + 1]) + ld(&U[v * L + l]));
+    un[v] = fma(-dt, dxim * (ld(&FX[v * L + l + 1]) - ld(&FX[v * L + l])), uh);
+  }
+  const R bxm = in(p.bxm[g]);
+  if constexpr (BG) {
+    const double *bg = p.bg;
+    un[1] = fma(dt, half(ld(&SS[l + 1]) + ld(&SS[l])), un[1]);
+    un[2] = fma(dt, half(ld(&SS[L + l + 1]) + ld(&SS[L + l])) + ld(&XS[2 * L + l]), un[2]);
+    const R scm = in(bg[3 * nx + g]), rrm = in(bg[7 * nx + g]), gxm = in(bg[nx + g]),
+            dscm = in(bg[5 * nx + g]), drrm = in(bg[9 * nx + g]);
+    const R si = in(RI[L + l]), rrmi = in(RI[3 * L + l]), ri = rcp(un[0]);
+    const R roh = un[0] * si, eeh = un[1] * si, vxh = un[2] * ri, vyh = un[3] * ri * rrmi,
+            byh = un[4] * si * rrm;
+    const R ek = half(roh) * fma(vyh, vyh, sq(vxh));
+    const R prh = c.gm1 * (eeh - ek - c.pi8i * sq(byh) + ld(&XS[L + l]));
+    const R pty = fma(sq(byh), c.pi8i, prh);  // without pi8i bxm^2
+    const R ezh = fma(vyh, bxm, -(vxh * byh));
+    const R eph = fma(prh, c.ggm1, ek);
+    const R rvx = roh * vxh;
+    st(&K[l], rvx * scm);
+    st(&K[L + l], fma(-(byh * ezh), c.pi4i, eph * vxh) * scm);
+    st(&K[2 * L + l], fma(rvx, vxh, pty) * scm);
+    st(&K[3 * L + l], fma(rvx, vyh, -(bxm * byh * c.pi4i)) * (scm * rrm));
+    st(&K[4 * L + l], -(ezh * (scm * rrmi)));
+    st(&SH[l], rvx * gxm * scm);
+    st(&SH[L + l], fma(fma(fma(roh * vyh, vyh, -(sq(byh) * c.pi4i)), rrmi * drrm, roh * gxm),
+                       scm, pty * dscm));
+  } else {
+    const R roh = un[0], ri = rcp(roh);
+    const R vxh = un[2] * ri, vyh = un[3] * ri, byh = un[4];
+    const R bb = sq(byh);
+    const R ek = half(roh) * fma(vyh, vyh, sq(vxh));
+    const R prh = c.gm1 * (un[1] - ek - c.pi8i * bb);
+    const R ezh = fma(vyh, bxm, -(vxh * byh));
+    const R eph = fma(prh, c.ggm1, ek);
+    const R rvx = roh * vxh;
+    st(&K[l], rvx);
+    st(&K[L + l], fma(-(byh * ezh), c.pi4i, eph * vxh));
+    st(&K[2 * L + l], fma(rvx, vxh, fma(bb, c.pi8i, prh)));
+    st(&K[3 * L + l], fma(rvx, vyh, -(bxm * byh * c.pi4i)));
+    st(&K[4 * L + l], -ezh);
+  }
+  // q = qav dxm max(0, |vx(i+1) - vx(i)| - 1.0e-4), the threshold a
+  // single-precision literal in the reference, so exactly the float 1.0e-4f
+  const R a = fabs(in(pc[2 * L + l + 1]) - in(pc[2 * L + l])) - 1.0e-4f;
+  const R q = a > 0.0f ? c.qav * in(p.ax.dm[g]) * a : R(0.0f);
+  st(&Q[l], q * dxim);
+}
+
+// full step of own local cell l (global g): the new primitives into pn
+template <bool BG>
+__device__ __forceinline__ void update(const Run1D &p, double *pn, int L, int l, int g,
+                                       const double *RI, const double *XS, const double *U,
+                                       const double *FX,
+                                       const double *SS, const double *K, const double *SH,
+                                       const double *Q, R dt, const Phys1 &c) {
+  const R hdt = half(dt), dxi = in(p.ax.di[g]), hdx = half(dxi);
+  const R ql = ld(&Q[l]), qm = ld(&Q[l - 1]);
+  R u[NV1];
+#pragma unroll
+  for (int v = 0; v < NV1; v++) {
+    R du = -(hdt * (hdx * (ld(&FX[v * L + l + 1]) - ld(&FX[v * L + l - 1]))));
+    if (BG && (v == 1 || v == 2)) du = fma(hdt, ld(&SS[(v - 1) * L + l]), du);
+    du = fma(-hdt, dxi * (ld(&K[v * L + l]) - ld(&K[v * L + l - 1])), du);
+    if (BG && (v == 1 || v == 2))
+      du = fma(hdt,
+               fma(in(p.ax.u0[g]), ld(&SH[(v - 1) * L + l - 1]),
+                   in(p.ax.u1[g]) * ld(&SH[(v - 1) * L + l])),
+               du);
+    const R uc = ld(&U[v * L + l]);
+    du = fma(dt, dxi * (ql * (ld(&U[v * L + l + 1]) - uc) - qm * (uc - ld(&U[v * L + l - 1]))),
+             du);
+    if (BG && v == 1) du = fma(dt, dxi * (ql * ld(&XS[l]) - qm * ld(&XS[l - 1])), du);
+    if (BG && v == 2) du = fma(hdt, ld(&XS[3 * L + l]), du);
+    u[v] = uc + du;
+  }
+  const R rinv = rcp(u[0]);
+  R ro, ee, vx, vy, by;
+  if constexpr (BG) {
+    const R si = in(RI[l]);
+    ro = u[0] * si;
+    ee = u[1] * si;
+    vx = u[2] * rinv;
+    vy = u[3] * rinv * in(RI[2 * L + l]);
+    by = u[4] * si * in(p.bg[6 * (size_t)p.ix + g]);
+  } else {
+    ro = u[0];
+    ee = u[1];
+    vx = u[2] * rinv;
+    vy = u[3] * rinv;
+    by = u[4];
+  }
+  // (BG: ee without pi8i bx^2, as the cell stage stores it)
+  const R pr = c.gm1 * (ee - half(ro) * fma(vy, vy, sq(vx)) - c.pi8i * sq(by));
+  pn[l] = num_out(ro);
+  pn[L + l] = num_out(pr);
+  pn[2 * L + l] = num_out(vx);
+  pn[3 * L + l] = num_out(vy);
+  pn[4 * L + l] = num_out(by);
+}
+
+// safety * dx / (|vx| + c_f) of one cell (cfl_m.f:53-60), c_f from the
+// fast magnetosonic speed squared (b^2 pi4i + gm pr) / ro
+__device__ __forceinline__ double cfl(const Run1D &p, const double *pc, int L, int l, int g,
+                                      double safety, const Phys1 &c) {
+  const R ro = in(pc[l]), pr = in(pc[L + l]), vx = in(pc[2 * L + l]), by = in(pc[4 * L + l]);
+  const R bx = in(p.bx[g]);
+  const R s = fma(c.gm, pr, fma(bx, bx, sq(by)) * c.pi4i) * rcp(ro);
+  const R den = fabs(vx) + sqrt_(s);
+  return num_out(in(safety) * in(p.ax.d[g]) * rcp(den));
+}
+}  // namespace d1
+
 // The loop of one run on one cluster (the kernels below): p lives in the
-// kernel parameters (one run) or in shared memory (a group of runs).
-template <bool E, bool BG>
+// kernel parameters (one run) or in shared memory (a group of runs).  DFP:
+// the double-float policy (E false).
+template <bool E, bool BG, bool DFP = false>
 __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
+  static_assert(!(E && DFP), "the double-float policy is a fast policy");
   using FT = F<E>;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
@@ -163,7 +391,8 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   extern __shared__ double sm[];
   // layout: prim[2][5][L], U[5][L], FX[5][L], K[5][L], Q[L],
   // (BG: SS[2][L] cell sources, SH[2][L] corner sources, RI[4][L] the
-  // reciprocals 1/sc, 1/scm, 1/rr, 1/rrm of the own cells), slots[2][CS],
+  // reciprocals 1/sc, 1/scm, 1/rr, 1/rrm of the own cells; BG and DFP: XS[4][L]
+  // the static-field terms of the double-float stages), slots[2][CS],
   // bad[2][CS], red[32]
   double *prim = sm;
   double *U = prim + 2 * NV1 * L;
@@ -173,7 +402,8 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   double *SS = Q + L;
   double *SH = SS + (BG ? 2 * L : 0);
   double *RI = SH + (BG ? 2 * L : 0);
-  double *slots = RI + (BG ? 4 * L : 0);
+  double *XS = RI + (BG ? 4 * L : 0);
+  double *slots = XS + ((BG && DFP) ? 4 * L : 0);
   double *bslots = slots + 2 * CS;  // per block: 1 if its CFL saw a bad cell
   double *red = bslots + 2 * CS;
   const double *bg = p.bg;
@@ -189,6 +419,8 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   const int lo = first_cell(r);
   const int hi = lo + own_count(r) - 1;
   const int nl = hi - lo + 3;  // local cells incl. one halo each side
+  d1::Phys1 cdf;  // the double-float policy's constants
+  if constexpr (DFP) cdf = d1::phys1(p.ph);
   const FT gm(p.ph.gm), gm1(p.ph.gm1), pi8i(p.ph.pi8i), pi4i(p.ph.pi4i),
       qav(p.ph.qav);
   const Axis &ax = p.ax;
@@ -210,6 +442,28 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
       RI[1 * L + l] = 1.0 / bg[3 * nx + g];
       RI[2 * L + l] = 1.0 / bg[6 * nx + g];
       RI[3 * L + l] = 1.0 / bg[7 * nx + g];
+    }
+    if constexpr (BG && DFP) {
+      // formed in FP64: differences of nearly equal terms
+      const double c8 = p.ph.pi8i;
+      auto b2 = [&](int gg) { return p.bx[gg] * p.bx[gg]; };
+      auto bm2 = [&](int gg) { return p.bxm[gg] * p.bxm[gg]; };
+      auto es = [&](int gg) { return c8 * b2(gg) * bg[2 * nx + gg]; };       // energy
+      auto fxs = [&](int gg) { return -(c8 * b2(gg)) * bg[2 * nx + gg]; };   // x-momentum flux
+      auto sss = [&](int gg) { return c8 * b2(gg) * bg[4 * nx + gg]; };      // and source
+      auto kxs = [&](int gg) { return -(c8 * bm2(gg)) * bg[3 * nx + gg]; };  // at corners
+      auto shs = [&](int gg) { return c8 * bm2(gg) * bg[5 * nx + gg]; };
+      if (l <= nl - 2) {
+        num_st(&XS[l], d1::in(es(g + 1) - es(g)));
+        num_st(&XS[L + l], d1::in(0.5 * (es(g + 1) + es(g)) / bg[3 * nx + g] - c8 * bm2(g)));
+        num_st(&XS[2 * L + l], d1::in(-ax.dim[g] * (fxs(g + 1) - fxs(g)) +
+                                      0.5 * (sss(g + 1) + sss(g))));
+      }
+      if (l >= 1 && l <= nl - 2)
+        num_st(&XS[3 * L + l],
+               d1::in(-(0.5 * ax.di[g]) * (fxs(g + 1) - fxs(g - 1)) + sss(g) -
+                      ax.di[g] * (kxs(g) - kxs(g - 1)) + ax.u0[g] * shs(g - 1) +
+                      ax.u1[g] * shs(g)));
     }
   }
   if (tid == 0) {
@@ -235,6 +489,12 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
     const FT safety(p.ctl ? p.ctl->safety : 1.0), pi4c(p.ph.pi4i);
     for (int l = 1 + tid; l <= nl - 2; l += NT) {
       const int g = lo - 1 + l;
+      if constexpr (DFP) {
+        const double dtq = d1::cfl(p, &P(buf, 0, 0), L, l, g, safety.v, cdf);
+        if (dtq < dmin || dmin != dmin) dmin = dtq;
+        bad |= bad_cell(P(buf, 0, l), P(buf, 1, l), dtq);
+        continue;
+      }
       const FT ro(P(buf, 0, l)), pr(P(buf, 1, l)), vx(P(buf, 2, l)), by(P(buf, 4, l));
       const FT bx(p.bx[g]);
       const FT onero = 1.0 / ro;
@@ -295,7 +555,10 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
     const long long ns_now = s_ns;
     const int nb = cur ^ 1;
     // ---- cell stage (mlw_m.f:37-73; mlw_m_bg.f:97-166) ---------------------
-    if constexpr (BG) {
+    if constexpr (DFP) {
+      for (int l = tid; l < nl; l += NT)
+        d1::cell<BG>(p, &P(cur, 0, 0), L, l, lo - 1 + l, RI, U, FX, SS, cdf);
+    } else if constexpr (BG) {
       for (int l = tid; l < nl; l += NT) {
         const int g = lo - 1 + l;
         const FT ro(P(cur, 0, l)), pr(P(cur, 1, l)), vx(P(cur, 2, l)), vy(P(cur, 3, l)),
@@ -363,7 +626,12 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
     }
     __syncthreads();
     // ---- corners (mlwhalf.f:42-46, mlw_m.f:74-110) and AV faces -----------
-    if constexpr (BG) {
+    if constexpr (DFP) {
+      const d1::R dtr = d1::in(s_dt);
+      for (int l = tid; l < nl - 1; l += NT)
+        d1::corner<BG>(p, &P(cur, 0, 0), L, l, lo - 1 + l, RI, XS, U, FX, SS, K, SH, Q, dtr,
+                       cdf);
+    } else if constexpr (BG) {
       // mlwhalf + mlwsrch, conversion (mlw_m_bg.f:170-183), corner fluxes
       // and sources (:188-234)
       for (int l = tid; l < nl - 1; l += NT) {
@@ -464,7 +732,14 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
     }
     __syncthreads();
     // ---- full step of the own cells ---------------------------------------
-    if constexpr (BG) {
+    if constexpr (DFP) {
+      const d1::R dtr = d1::in(s_dt);
+      for (int l = 1 + tid; l <= nl - 2; l += NT) {
+        const int g = lo - 1 + l;
+        d1::update<BG>(p, &P(nb, 0, 0), L, l, g, RI, XS, U, FX, SS, K, SH, Q, dtr, cdf);
+        if (BG && p.trq) P(nb, 3, l) = torque_add<false>(p, FT(P(nb, 3, l)), dt, ns_now, g).v;
+      }
+    } else if constexpr (BG) {
       // mlwhalf/mlwsrch increments, mlwfull + mlwsrcf, mlwartv, then the
       // update and conversion (mlw_m_bg.f:251-268) and the torque
       for (int l = 1 + tid; l <= nl - 2; l += NT) {
@@ -675,21 +950,29 @@ __device__ __forceinline__ void mlw1d_body(const Run1D &p) {
   }
 }
 
-template <bool E, bool BG>
+template <bool E, bool BG, bool DFP>
 __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
-  mlw1d_body<E, BG>(p);
+  mlw1d_body<E, BG, DFP>(p);
 }
 
 // A group of independent runs, one cluster each: cluster c runs runs[c].  The
 // run's parameters are copied to shared memory once; the runs share nothing
 // else, so a cluster that finishes early leaves its SMs to the next ones.
-template <bool E, bool BG>
+template <bool E, bool BG, bool DFP>
 __global__ void __launch_bounds__(256, 2) k_mlw1d_group(const Run1D *__restrict__ runs) {
   __shared__ Run1D sp;
   const unsigned c = blockIdx.x / cg::this_cluster().num_blocks();
   if (threadIdx.x == 0) sp = runs[c];
   __syncthreads();
-  mlw1d_body<E, BG>(sp);
+  mlw1d_body<E, BG, DFP>(sp);
+}
+
+// the kernel instance of a policy (exact, fast or double-float) and variant
+template <class K>
+K pick1d(bool exact, bool bgv, bool dfp, K ef, K eb, K ff, K fb, K df, K db) {
+  if (dfp) return bgv ? db : df;
+  if (exact) return bgv ? eb : ef;
+  return bgv ? fb : ff;
 }
 
 // Smallest grid the 1-D loop kernel accepts (one block of 4 interior cells).
@@ -733,8 +1016,8 @@ static int cluster_max(void (*kern)(Run1D), size_t smem) {
 }
 
 namespace {
-constexpr size_t per_cell_doubles(bool bgv) {
-  return (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 8 : 0);
+constexpr size_t per_cell_doubles(bool bgv, bool dfp) {
+  return (size_t)(2 * NV1 + 3 * NV1 + 1) + (bgv ? 8 : 0) + (bgv && dfp ? 4 : 0);
 }
 
 // The parameters of one run on a cluster of CS blocks; false when a block
@@ -776,14 +1059,16 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
                          const double *bxm, const Loop1D &opt, int ix,
                          const Axis &ax, const Phys &ph, const BcTable &bc,
                          Ctl *ctl, int max_steps, int fixed, double dt_fixed,
-                         int start, cudaStream_t s) {
-  if (ix < mlw1d_min_cells()) return cudaErrorInvalidValue;
+                         int start, cudaStream_t s, bool dfp) {
+  if (ix < mlw1d_min_cells() || (dfp && exact)) return cudaErrorInvalidValue;
   const bool bgv = opt.bg != nullptr;
   // the torque reads the rr profile; the floor counts into the control block
   if ((opt.trq && !bgv) || (opt.chk && !ctl && !fixed)) return cudaErrorInvalidValue;
-  void (*kern)(Run1D) = bgv ? (exact ? k_mlw1d<true, true> : k_mlw1d<false, true>)
-                            : (exact ? k_mlw1d<true, false> : k_mlw1d<false, false>);
-  const size_t per_cell = per_cell_doubles(bgv);
+  void (*kern)(Run1D) =
+      pick1d(exact, bgv, dfp, k_mlw1d<true, false, false>, k_mlw1d<true, true, false>,
+             k_mlw1d<false, false, false>, k_mlw1d<false, true, false>,
+             k_mlw1d<false, false, true>, k_mlw1d<false, true, true>);
+  const size_t per_cell = per_cell_doubles(bgv, dfp);
   // shared memory of the largest block the grid can have (16 blocks)
   const size_t smem_probe = sizeof(double) * (per_cell * ((ix - 2) / 16 + 4) + 64 + 32);
   const int CS = cluster_for(ix, cluster_max(kern, smem_probe));
@@ -832,8 +1117,8 @@ cudaError_t launch_mlw1d(bool exact, double *S, const double *bx,
 // block keeps 32 cells).  The runs' parameters go to the device in one
 // stream-ordered allocation.  All runs share exact and the BG variant.
 cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int nruns,
-                               int max_steps, cudaStream_t s) {
-  if (nruns < 1) return cudaErrorInvalidValue;
+                               int max_steps, cudaStream_t s, bool dfp) {
+  if (nruns < 1 || (dfp && exact)) return cudaErrorInvalidValue;
   int ixmax = 0, ixmin = 1 << 30;
   for (int k = 0; k < nruns; k++) {
     const Run1DArgs &a = runs[k];
@@ -861,9 +1146,11 @@ cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int 
     lmax = host[k].lmax > lmax ? host[k].lmax : lmax;
   }
   void (*kern)(const Run1D *) =
-      bgv ? (exact ? k_mlw1d_group<true, true> : k_mlw1d_group<false, true>)
-          : (exact ? k_mlw1d_group<true, false> : k_mlw1d_group<false, false>);
-  const size_t smem = sizeof(double) * (per_cell_doubles(bgv) * lmax + 4 * CS + 32);
+      pick1d(exact, bgv, dfp, k_mlw1d_group<true, false, false>,
+             k_mlw1d_group<true, true, false>, k_mlw1d_group<false, false, false>,
+             k_mlw1d_group<false, true, false>, k_mlw1d_group<false, false, true>,
+             k_mlw1d_group<false, true, true>);
+  const size_t smem = sizeof(double) * (per_cell_doubles(bgv, dfp) * lmax + 4 * CS + 32);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

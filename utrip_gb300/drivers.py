@@ -197,8 +197,8 @@ def make_run(setup, exact=False, tile=-1, stream=None, floor=True, torque=True,
              stop_on_bad=False, df64=False) -> capi.Run:
     """Run handle for a set-up; a set-up with a "floor" gets the chkdav
     option and one with a "trq" profile the torque source (each can be
-    switched off here).  df64 selects the double-float policy of the 2-D
-    mlw_m3 step."""
+    switched off here).  df64 selects the double-float policy of the step
+    (cans_run_set_df64)."""
     fl = setup.get("floor") if floor else None
     tq = None
     if torque and setup.get("trq") is not None:
