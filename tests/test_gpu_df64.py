@@ -101,7 +101,7 @@ def test_df64_shock_tube_converges_like_the_oracle(gpu, oracle_lib):
 def test_df64_refused_where_it_does_not_apply(gpu):
     for s, exact in ((setups.orszag_tang(32, solver="mlw_m"), False),
                      (setups.orszag_tang(32), True),
-                     (setups.random_state_1d(40, seed=1), False),
+                     (setups.random_state_1d(40, seed=1), True),
                      (setups.random_state_3d(12, 12, 12, seed=1), True)):
         run = drivers.make_run(s, exact=exact)
         try:
