@@ -95,7 +95,7 @@ def profile_case(case, n, tile=-1, df64=False):
         out = {"case": case, "n": n, "steps": int(st.nexec), "merr": int(st.merr)}
     elif case == "spicule":
         s = setups.spicule_1d(n)
-        run = drivers.make_run(s)
+        run = drivers.make_run(s, df64=df64)
         run.push(s["state"])
         run.start(nstop=200, tend=s["tend"], safety=s["safety"], dtmin=s["dtmin"])
         run.advance(200)
@@ -109,7 +109,7 @@ def profile_case(case, n, tile=-1, df64=False):
         runs = []
         for k, b in enumerate(10.0 ** rng.uniform(-1.0, 1.0, size=n)):
             s = setups.spicule_1d(1024, beta=float(b), seed=k)
-            run = drivers.make_run(s)
+            run = drivers.make_run(s, df64=df64)
             run.push(s["state"])
             run.start(tend=s["tend"], nstop=s["nstop"], safety=s["safety"], dtmin=s["dtmin"])
             runs.append(run)
@@ -117,7 +117,7 @@ def profile_case(case, n, tile=-1, df64=False):
         done = [int(r.query().nexec) for r in runs]
         for r in runs:
             r.close()
-        out = {"case": case, "runs": n, "steps": min(done)}
+        out = {"case": case, "runs": n, "steps": min(done), "df64": df64}
     elif case in ("gravity3d", "resistive3d"):
         s = (setups.emerging_flux_3d(n, max(2, n // 4), n) if case == "gravity3d"
              else setups.magnetic_reconnection_3d(n, max(4, n // 4)))
