@@ -958,8 +958,12 @@ __global__ void __launch_bounds__(256, 1) k_mlw1d(Run1D p) {
 // A group of independent runs, one cluster each: cluster c runs runs[c].  The
 // run's parameters are copied to shared memory once; the runs share nothing
 // else, so a cluster that finishes early leaves its SMs to the next ones.
+// Two blocks a SM; the double-float instance takes up to 288 threads (96
+// registers), so that the two halo cells of a 256-cell block get a warp of
+// their own instead of a second pass of warp 0 that the others wait for.
 template <bool E, bool BG, bool DFP>
-__global__ void __launch_bounds__(256, 2) k_mlw1d_group(const Run1D *__restrict__ runs) {
+__global__ void __launch_bounds__(DFP ? 288 : 256, 2)
+    k_mlw1d_group(const Run1D *__restrict__ runs) {
   __shared__ Run1D sp;
   const unsigned c = blockIdx.x / cg::this_cluster().num_blocks();
   if (threadIdx.x == 0) sp = runs[c];
@@ -1164,8 +1168,9 @@ cudaError_t launch_mlw1d_group(bool exact, bool bgv, const Run1DArgs *runs, int 
     cudaFreeAsync(dev, s);
     return e;
   }
+  const int ntmax = dfp ? 288 : 256;  // the kernel's launch bound
   int nt = ((lmax + 31) / 32) * 32;
-  nt = nt < 32 ? 32 : (nt > 256 ? 256 : nt);
+  nt = nt < 32 ? 32 : (nt > ntmax ? ntmax : nt);
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3((unsigned)(CS * nruns), 1, 1);
   cfg.blockDim = dim3(nt, 1, 1);
