@@ -28,6 +28,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <vector>
 
 #include "cans_common.cuh"
@@ -993,10 +994,20 @@ static int cluster_for(int ix, int cmax) {
 }
 
 // Largest cluster the device co-schedules for this kernel: 16 blocks where
-// non-portable cluster sizes are available, else the portable 8.
+// non-portable cluster sizes are available, else the portable 8.  Asked once
+// per device (the same answer for every instance of the kernel), under a lock:
+// launches may come from several host threads and devices.
 static int cluster_max(void (*kern)(Run1D), size_t smem) {
-  static int cached = 0;  // the same answer for every instance of the kernel
-  if (cached) return cached;
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static int cached_of[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return 8;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (cached_of[dev]) return cached_of[dev];
   int best = 8;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
       cudaSuccess) {
@@ -1015,7 +1026,7 @@ static int cluster_max(void (*kern)(Run1D), size_t smem) {
     if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) == cudaSuccess && n > 0) best = 16;
   }
   cudaGetLastError();  // a refused query leaves no error behind
-  cached = best;
+  cached_of[dev] = best;
   return best;
 }
 
