@@ -96,6 +96,22 @@ def test_spicule_loop_every_source_term(gpu, oracle_lib):
         assert rel_linf(a, b) < (1e-4 if k == "vx" else 1e-9), (k, rel_linf(a, b))
 
 
+def test_mhd_wind_loop(gpu, oracle_lib):
+    """cans1d/md_mhdwind on its stretched grid: the cross-section (0.7 to
+    1.1e4), B_x and the radius vary, and the gas pressure falls to 6e-6 of
+    B_x^2/8pi, so every static field term of the double-float mlw_m_bg is in
+    play.  200 iterations: 1e-10, vx 1e-6 (the fast policy ends 1.9e-8 from
+    the oracle in vx there; over longer runs this wind amplifies any
+    rounding, and only the exact policy stays on the oracle's trajectory)."""
+    s = setups.mhd_wind_1d(1024)
+    ref = setups.copy_state(s)
+    t_ref, ns_ref, _, _ = oracle.run_1d(s, ref, 200)
+    got, (t, ns, merr, nexec) = loop_df64(s, 200)
+    assert merr == 0 and ns == ns_ref and t == pytest.approx(t_ref, rel=1e-10)
+    for k, a, b in zip(s["names"], got, ref):
+        assert rel_linf(a, b) < (1e-6 if k == "vx" else TOL), (k, rel_linf(a, b))
+
+
 def test_group_equals_runs_alone(gpu):
     """Spicule runs at beta 0.3, 1 and 3 advanced as one double-float group
     end where each ends alone, to the fast policy's group bounds: the
