@@ -603,6 +603,27 @@ def test_spicule_corona_amplifies_energy_rounding(oracle_lib):
     assert rel[2] > 1e-6 and rel[0] < 1e-12 and rel[1] < 1e-12, rel
 
 
+def test_mhd_wind_amplifies_one_ulp(oracle_lib):
+    """The conditioning behind the short parity runs of the MHD wind
+    (cans1d/md_mhdwind): one unit in the last place of every density stays
+    below 1e-9 of vx after 200 iterations of the oracle's loop, but moves vx
+    by more than 1e-6 and the time reached by more than 1e-8 after 2000."""
+    s = setups.mhd_wind_1d(1024)
+
+    def drift(n):
+        a, b = setups.copy_state(s), setups.copy_state(s)
+        b[0][:] = np.nextafter(b[0], np.inf)
+        ta = oracle_lib.run_1d(s, a, n)[0]
+        tb = oracle_lib.run_1d(s, b, n)[0]
+        vx = float(np.max(np.abs(a[2] - b[2])) / np.max(np.abs(a[2])))
+        return abs(ta - tb) / ta, vx
+
+    t200, vx200 = drift(200)
+    t2000, vx2000 = drift(2000)
+    assert vx200 < 1e-9, vx200
+    assert vx2000 > 1e-6 and t2000 > 1e-8, (vx2000, t2000)
+
+
 def one_ulp_amplification(oracle_lib, solver, b0, n=32, steps=20):
     """Relative L-infinity per variable between two oracle runs of the 3-D
     beta = 1 box whose velocities differ by at most one unit in the last
